@@ -1,0 +1,242 @@
+"""Oracle for the CommonNN fit path (TEST INFRASTRUCTURE ONLY).
+
+This module is the checker the CUDA library is compared against.  Only the
+tests, ``__graft_entry__.smoke()`` and the CPU-baseline legs of ``bench.py``
+import it; the library itself never imports, links or falls back to it.
+
+It wraps the C restatement in ``cnn_oracle.c`` (compiled by ``build.py``)
+and restates the pure-Python parts of the reference with numpy:
+
+* ``make_parameters``    -- ``Fitter.make_parameters``
+                            (src/cnnclustering/_fit.pyx:51-85, 130-161)
+* ``sort_by_size``       -- ``Labels.sort_by_size``
+                            (src/cnnclustering/_types.pyx:212-286)
+* ``clustering_fit``     -- ``Clustering.fit`` orchestration: cnn_offset,
+                            label initialisation / frozen labels,
+                            parameters, fit, sort_by_size
+                            (src/cnnclustering/cluster.pyx:256-392)
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import build as _build
+
+METRIC_EUCLIDEAN_REDUCED = 0
+METRIC_EUCLIDEAN = 1
+FP_SEPARATE = 0
+FP_FUSED = 1
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = ctypes.CDLL(path)
+        i64, i32, dbl, i = ctypes.c_int64, ctypes.c_int32, ctypes.c_double, ctypes.c_int
+        p = ctypes.c_void_p
+        L.oracle_sqdist.restype = dbl
+        L.oracle_sqdist.argtypes = [p, p, i32, i]
+        for name in ("oracle_neighbour_counts", "oracle_neighbour_counts_grid"):
+            f = getattr(L, name)
+            f.restype = i
+            f.argtypes = [p, i64, i32, dbl, i, i, i, p]
+        for name in ("oracle_neighbour_fill", "oracle_neighbour_fill_grid"):
+            f = getattr(L, name)
+            f.restype = i
+            f.argtypes = [p, i64, i32, dbl, i, i, i, p, p]
+        L.oracle_check_sorted.restype = i
+        L.oracle_check_sorted.argtypes = [p, i64, p, i64, i64]
+        L.oracle_count_common_sorted.restype = i64
+        L.oracle_count_common_sorted.argtypes = [p, i64, p, i64]
+        L.oracle_fit_bfs_csr.restype = i64
+        L.oracle_fit_bfs_csr.argtypes = [p, p, i64, i64, i64, i64, p, p]
+        L.oracle_fit_bfs_points.restype = i64
+        L.oracle_fit_bfs_points.argtypes = [p, i64, i32, dbl, i, i, i64, i64, i64, p, p]
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _nthreads(nthreads: Optional[int]) -> int:
+    if nthreads is None:
+        return max(1, len(os.sched_getaffinity(0)))
+    return max(1, int(nthreads))
+
+
+def sqdist(xa, xb, fpmode=FP_SEPARATE) -> float:
+    xa = np.ascontiguousarray(xa, dtype=np.float64)
+    xb = np.ascontiguousarray(xb, dtype=np.float64)
+    return lib().oracle_sqdist(_ptr(xa), _ptr(xb), xa.shape[0], fpmode)
+
+
+def neighbourhoods(x, radius_cutoff: float, metric=METRIC_EUCLIDEAN_REDUCED,
+                   fpmode=FP_SEPARATE, nthreads=None, grid: bool = True):
+    """Sorted CSR neighbourhoods (self included) of every point.
+
+    ``radius_cutoff`` is the adjusted value the getter compares with
+    (r**2 for the reduced metric).  Returns (offsets int64[n+1],
+    indices int32[nnz]).
+    """
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    if x.ndim == 1:
+        x = x.reshape(-1, 1)
+    n, d = x.shape
+    counts = np.zeros(n, dtype=np.int64)
+    L = lib()
+    nt = _nthreads(nthreads)
+    fc = L.oracle_neighbour_counts_grid if grid else L.oracle_neighbour_counts
+    ff = L.oracle_neighbour_fill_grid if grid else L.oracle_neighbour_fill
+    if fc(_ptr(x), n, d, float(radius_cutoff), metric, fpmode, nt, _ptr(counts)) != 0:
+        raise MemoryError("oracle neighbour count failed")
+    offsets = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(counts, out=offsets[1:])
+    indices = np.empty(int(offsets[-1]), dtype=np.int32)
+    if ff(_ptr(x), n, d, float(radius_cutoff), metric, fpmode, nt, _ptr(offsets), _ptr(indices)) != 0:
+        raise MemoryError("oracle neighbour fill failed")
+    return offsets, indices
+
+
+def check_sorted(a, b, c: int) -> bool:
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    b = np.ascontiguousarray(b, dtype=np.int32)
+    return bool(lib().oracle_check_sorted(_ptr(a), a.shape[0], _ptr(b), b.shape[0], int(c)))
+
+
+def count_common_sorted(a, b) -> int:
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    b = np.ascontiguousarray(b, dtype=np.int32)
+    return int(lib().oracle_count_common_sorted(_ptr(a), a.shape[0], _ptr(b), b.shape[0]))
+
+
+def make_parameters(radius_cutoff: float, cnn_cutoff: int, current_start: int = 1,
+                    metric=METRIC_EUCLIDEAN_REDUCED, is_selfcounting: bool = True):
+    """Fitter.make_parameters (src/cnnclustering/_fit.pyx:130-161)."""
+    if metric == METRIC_EUCLIDEAN_REDUCED:
+        radius_cutoff = radius_cutoff ** 2
+    n_member_cutoff = cnn_cutoff
+    similarity_cutoff = cnn_cutoff
+    if is_selfcounting:
+        n_member_cutoff += 1
+        similarity_cutoff += 2
+    return {"radius_cutoff": float(radius_cutoff), "similarity_cutoff": int(similarity_cutoff),
+            "n_member_cutoff": int(n_member_cutoff), "current_start": int(current_start)}
+
+
+def fit_bfs_csr(offsets, indices, similarity_cutoff, n_member_cutoff, current_start,
+                consider, labels) -> int:
+    """FitterExtBFS._fit over sorted CSR lists; updates labels/consider in place."""
+    assert consider.dtype == np.uint8 and consider.flags.c_contiguous
+    assert labels.dtype == np.int64 and labels.flags.c_contiguous
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    indices = np.ascontiguousarray(indices, dtype=np.int32)
+    n = offsets.shape[0] - 1
+    r = lib().oracle_fit_bfs_csr(_ptr(offsets), _ptr(indices), n, int(similarity_cutoff),
+                                 int(n_member_cutoff), int(current_start), _ptr(consider),
+                                 _ptr(labels))
+    if r < 0:
+        raise MemoryError("oracle fit failed")
+    return int(r)
+
+
+def fit_bfs_points(x, radius_cutoff, similarity_cutoff, n_member_cutoff, current_start,
+                   consider, labels, metric=METRIC_EUCLIDEAN_REDUCED, fpmode=FP_SEPARATE) -> int:
+    """FitterExtBFS._fit with the brute-force getter (default recipe)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    n, d = x.shape
+    r = lib().oracle_fit_bfs_points(_ptr(x), n, d, float(radius_cutoff), metric, fpmode,
+                                    int(similarity_cutoff), int(n_member_cutoff),
+                                    int(current_start), _ptr(consider), _ptr(labels))
+    if r < 0:
+        raise MemoryError("oracle fit failed")
+    return int(r)
+
+
+def sort_by_size(labels: np.ndarray, member_cutoff: Optional[int] = None,
+                 max_clusters: Optional[int] = None) -> dict:
+    """Labels.sort_by_size in place (src/cnnclustering/_types.pyx:212-286).
+
+    ``Counter.most_common`` orders by count, descending, and keeps the
+    insertion (first occurrence) order for ties.  Returns the reassign map.
+    """
+    if member_cutoff is None:
+        member_cutoff = 2
+    uniq, first, counts = np.unique(labels, return_index=True, return_counts=True)
+    keep = uniq != 0
+    uniq, first, counts = uniq[keep], first[keep], counts[keep]
+    if uniq.shape[0] == 0:
+        return {}
+    if max_clusters is None:
+        max_clusters = uniq.shape[0]
+    order = np.lexsort((first, -counts))
+    reassign = {0: 0}
+    new_label = 1
+    for cluster_count, k in enumerate(order, 1):
+        old = int(uniq[k])
+        if cluster_count > max_clusters:
+            reassign[old] = 0
+            continue
+        if counts[k] >= member_cutoff:
+            reassign[old] = new_label
+            new_label += 1
+            continue
+        reassign[old] = 0
+    keys = np.array(list(reassign.keys()), dtype=np.int64)
+    vals = np.array(list(reassign.values()), dtype=np.int64)
+    srt = np.argsort(keys)
+    pos = np.searchsorted(keys[srt], labels)
+    labels[:] = vals[srt][pos]
+    return reassign
+
+
+def clustering_fit(x, radius_cutoff: float, cnn_cutoff: int, member_cutoff=None,
+                   max_clusters=None, cnn_offset=None, sort: bool = True,
+                   metric=METRIC_EUCLIDEAN_REDUCED, fpmode=FP_SEPARATE,
+                   labels=None, consider=None, frozen: bool = False,
+                   neighbours=None, brute_force: bool = False, nthreads=None):
+    """Clustering.fit (src/cnnclustering/cluster.pyx:256-392) on the oracle.
+
+    Returns (labels, info) where info holds the CSR and counters.
+    """
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    if x.ndim == 1:
+        x = x.reshape(-1, 1)
+    n = x.shape[0]
+    if cnn_offset is None:
+        cnn_offset = 0
+    cnn_cutoff -= cnn_offset
+    assert cnn_cutoff >= 0
+    if labels is None or not frozen:
+        labels = np.zeros(n, dtype=np.int64)
+        consider = np.ones(n, dtype=np.uint8)
+        current_start = 1
+    else:
+        labels = np.array(labels, dtype=np.int64)
+        consider = (np.ones(n, dtype=np.uint8) if consider is None
+                    else np.array(consider, dtype=np.uint8))
+        current_start = int(labels.max()) + 1 if n else 1
+    params = make_parameters(radius_cutoff, cnn_cutoff, current_start, metric)
+    info = {"params": params}
+    if brute_force:
+        info["n_checks"] = fit_bfs_points(x, params["radius_cutoff"], params["similarity_cutoff"],
+                                          params["n_member_cutoff"], current_start, consider,
+                                          labels, metric, fpmode)
+    else:
+        if neighbours is None:
+            neighbours = neighbourhoods(x, params["radius_cutoff"], metric, fpmode, nthreads)
+        offsets, indices = neighbours
+        info["offsets"], info["indices"] = offsets, indices
+        info["n_checks"] = fit_bfs_csr(offsets, indices, params["similarity_cutoff"],
+                                       params["n_member_cutoff"], current_start, consider, labels)
+    if sort:
+        sort_by_size(labels, member_cutoff, max_clusters)
+    return labels, info

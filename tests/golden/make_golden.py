@@ -1,0 +1,235 @@
+"""Generate the golden fixtures in this folder by running the REFERENCE.
+
+The reference (cnnclustering 0.5.0) is a Cython package.  It is installed
+from its source tree into ``baseline/_ref`` once, without network:
+
+    cp -r <reference checkout> /tmp/refsrc
+    python -m pip install --no-index --no-build-isolation --no-deps \
+        --find-links /opt/wheelhouse --target baseline/_ref /tmp/refsrc
+
+and then this script imports it from there (x86-64 build, GCC, baseline
+ISA: the distance sum is computed with a separate multiply and add).
+Run from the repository root:
+
+    python tests/golden/make_golden.py
+
+Every fixture stores the inputs next to the reference's outputs, so the
+tests need neither the reference nor scikit-learn at run time.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "baseline", "_ref"))
+sys.path.insert(0, ROOT)
+
+from cnnclustering import cluster, _types, _fit  # noqa: E402
+from cnnclustering._types import Labels, ClusterParameters  # noqa: E402
+
+from commonnnclustering_gb300 import workloads  # noqa: E402
+
+
+def csr_digest(offsets: np.ndarray, indices: np.ndarray) -> str:
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(offsets, dtype=np.int64).tobytes())
+    h.update(np.ascontiguousarray(indices, dtype=np.int32).tobytes())
+    return h.hexdigest()
+
+
+def reference_neighbourhoods(x: np.ndarray, r: float, metric: str = "euclidean_r"):
+    """Rows of the reference's own brute-force getter, index order."""
+    metric_type = {"euclidean_r": _types.MetricExtEuclideanReduced,
+                   "euclidean": _types.MetricExtEuclidean}[metric]
+    m = metric_type()
+    getter = _types.NeighboursGetterExtBruteForce(_types.DistanceGetterExtMetric(m))
+    data = _types.InputDataExtComponentsMemoryview(np.ascontiguousarray(x, dtype=np.float64))
+    radius = r * r if metric == "euclidean_r" else r
+    params = ClusterParameters(radius)
+    nb = _types.NeighboursExtVector(64)
+    rows = []
+    for i in range(x.shape[0]):
+        getter.get(i, data, nb, params)
+        rows.append(np.array([nb.get_member(k) for k in range(nb.n_points)], dtype=np.int32))
+    offsets = np.zeros(x.shape[0] + 1, dtype=np.int64)
+    offsets[1:] = np.cumsum([len(a) for a in rows])
+    indices = np.concatenate(rows) if rows else np.zeros(0, dtype=np.int32)
+    return offsets, indices
+
+
+def ref_fit(x, r, c, recipe="coordinates", **fit_kwargs):
+    cl = cluster.Clustering(np.ascontiguousarray(x, dtype=np.float64), recipe=recipe)
+    t = time.time()
+    cl.fit(r, c, v=False, **fit_kwargs)
+    return np.array(cl.labels, dtype=np.int64), time.time() - t
+
+
+def ref_fit_metric(x, r, c, metric_type, **fit_kwargs):
+    recipe = {
+        "input_data": _types.InputDataExtComponentsMemoryview,
+        "fitter": _fit.FitterExtBFS,
+        "fitter.ngetter": _types.NeighboursGetterExtBruteForce,
+        "fitter.na": _types.NeighboursExtVectorCPPUnorderedSet,
+        "fitter.checker": _types.SimilarityCheckerExtSwitchContains,
+        "fitter.queue": _types.QueueExtFIFOQueue,
+        "fitter.ngetter.dgetter": _types.DistanceGetterExtMetric,
+        "fitter.ngetter.dgetter.metric": metric_type,
+    }
+    cl = cluster.Clustering(np.ascontiguousarray(x, dtype=np.float64), recipe=recipe)
+    cl.fit(r, c, v=False, **fit_kwargs)
+    return np.array(cl.labels, dtype=np.int64)
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name)
+    np.savez_compressed(path, **arrays)
+    print("wrote", path, {k: getattr(v, "shape", v) for k, v in arrays.items()})
+
+
+def fit_case(name, x, r, c, store_csr=True, fit_kwargs=None):
+    fit_kwargs = dict(fit_kwargs or {})
+    labels, t = ref_fit(x, r, c, **fit_kwargs)
+    offsets, indices = reference_neighbourhoods(x, r)
+    arrays = dict(points=np.asarray(x, dtype=np.float64), labels=labels,
+                  radius_cutoff=np.float64(r), cnn_cutoff=np.int64(c),
+                  member_cutoff=np.int64(fit_kwargs.get("member_cutoff", -1)),
+                  max_clusters=np.int64(fit_kwargs.get("max_clusters", -1) or -1),
+                  cnn_offset=np.int64(fit_kwargs.get("cnn_offset", 0) or 0),
+                  sort_by_size=np.bool_(fit_kwargs.get("sort_by_size", True)),
+                  degrees=np.diff(offsets).astype(np.int32),
+                  csr_sha256=np.array(csr_digest(offsets, indices)),
+                  ref_fit_seconds=np.float64(t))
+    if store_csr:
+        arrays["offsets"] = offsets
+        arrays["indices"] = indices
+    # the sorted-neighbourhoods recipe on the same lists must agree
+    cl = cluster.Clustering([indices[offsets[i]:offsets[i + 1]] for i in range(x.shape[0])],
+                            recipe="sorted_neighbourhoods")
+    cl.fit(r, c, v=False, **fit_kwargs)
+    assert np.array_equal(np.asarray(cl.labels), labels), name
+    save(name, **arrays)
+
+
+def main():
+    # 1. README quickstart (README.md:71-93)
+    q = np.array([[0, 0], [1, 1], [1, 0], [0, -1], [0.5, -0.5], [2, 1.5], [2.5, -0.5],
+                  [4, 2], [4.5, 2.5], [5, -1], [5.5, -0.5], [5.5, -1.5]], dtype=np.float64)
+    fit_case("quickstart.npz", q, 1.5, 1)
+
+    # 2. the 5,000-point 2D blobs workload, default recipe (brute force)
+    x = workloads.blobs2d()
+    fit_case("blobs2d_5k.npz", x, 0.3, 5, store_csr=False, fit_kwargs={"member_cutoff": 10})
+
+    # 3./4. the integration-test toy sets (test/integration/test_procedures.py:126-139)
+    from sklearn import datasets
+    from sklearn.preprocessing import StandardScaler
+    pts, _ = datasets.make_moons(n_samples=1500, random_state=0)
+    pts = StandardScaler().fit_transform(pts)
+    fit_case("moons_1500.npz", pts, 0.2, 5)
+    pts, _ = datasets.make_blobs(n_samples=1500, cluster_std=[1.0, 2.5, 0.5], random_state=170)
+    pts = StandardScaler().fit_transform(pts)
+    fit_case("varied_1500.npz", pts, 0.25, 20, fit_kwargs={"member_cutoff": 20})
+
+    # 5. fit options: no sorting, max_clusters, cnn_offset
+    fit_case("varied_nosort.npz", pts, 0.25, 20, fit_kwargs={"sort_by_size": False})
+    fit_case("varied_maxclusters.npz", pts, 0.25, 10,
+             fit_kwargs={"member_cutoff": 5, "max_clusters": 2, "cnn_offset": 2})
+
+    # 6. non-reduced Euclidean metric (sqrt then compare with r)
+    rng = np.random.default_rng(11)
+    xe = np.vstack([rng.normal(0, 0.4, size=(300, 3)), rng.normal(2, 0.3, size=(200, 3)),
+                    rng.uniform(-2, 4, size=(100, 3))])
+    lab_e = ref_fit_metric(xe, 0.35, 4, _types.MetricExtEuclidean, member_cutoff=5)
+    off_e, idx_e = reference_neighbourhoods(xe, 0.35, metric="euclidean")
+    save("euclidean_sqrt.npz", points=xe, labels=lab_e, radius_cutoff=np.float64(0.35),
+         cnn_cutoff=np.int64(4), member_cutoff=np.int64(5), offsets=off_e, indices=idx_e)
+
+    # 7. frozen labels: fit, freeze, refit the unassigned points
+    pts, _ = datasets.make_moons(n_samples=800, noise=0.08, random_state=3)
+    pts = StandardScaler().fit_transform(pts)
+    cl = cluster.Clustering(pts)
+    cl.fit(0.25, 8, v=False, member_cutoff=5)
+    first = np.array(cl.labels, dtype=np.int64)
+    cl._bundle._labels.meta["frozen"] = True
+    consider = (first == 0).astype(np.uint8)
+    cl._bundle._labels.consider[:] = consider
+    cl.fit(0.35, 3, v=False, member_cutoff=2)
+    second = np.array(cl.labels, dtype=np.int64)
+    save("frozen_refit.npz", points=pts, first_labels=first, consider=consider,
+         second_labels=second, r1=np.float64(0.25), c1=np.int64(8), m1=np.int64(5),
+         r2=np.float64(0.35), c2=np.int64(3), m2=np.int64(2))
+
+    # 8. sort_by_size vectors (test/unit/test_types.py:98-117) plus random ones
+    base = np.array([1, 1, 2, 2, 0, 1, 3, 3, 3, 1, 5], dtype=np.int64)
+    cases = [({"member_cutoff": 1}, base), ({}, base),
+             ({"member_cutoff": 2, "max_clusters": 2}, base)]
+    rng = np.random.default_rng(5)
+    for k in range(6):
+        lab = rng.integers(0, 9, size=200).astype(np.int64)
+        cases.append(({"member_cutoff": int(k % 4), "max_clusters": (None if k < 3 else 3 + k)}, lab))
+    lab = rng.integers(0, 3000, size=5000).astype(np.int64) * 7 - 50
+    lab[rng.random(5000) < 0.2] = 0
+    cases.append(({"member_cutoff": 2}, lab))
+    ins, outs, mcs, mxs = [], [], [], []
+    for kw, lab in cases:
+        L = Labels(lab.copy())
+        L.sort_by_size(**kw)
+        ins.append(lab)
+        outs.append(np.asarray(L.labels).copy())
+        mcs.append(-1 if kw.get("member_cutoff") is None else kw["member_cutoff"])
+        mxs.append(-1 if kw.get("max_clusters") is None else kw["max_clusters"])
+    save("sort_by_size.npz", n_cases=np.int64(len(cases)),
+         member_cutoff=np.array(mcs, dtype=np.int64), max_clusters=np.array(mxs, dtype=np.int64),
+         **{f"in_{i}": a for i, a in enumerate(ins)}, **{f"out_{i}": a for i, a in enumerate(outs)})
+
+    # 9. similarity check truth table (test/unit/test_check_similarity.py:38-48)
+    #    on sorted members with the screensorted checker, plus random lists
+    table = [([], [], 0), ([], [], 1), ([1, 2, 3], [2, 5], 1), ([1, 2, 3], [2, 5, 8, 9], 2),
+             ([1, 2, 3, 9, 10], [2, 5, 8, 9, 10], 3), ([1, 2, 3, 9, 10, 18], [2, 5, 8, 9, 10, 11, 18], 3)]
+    for k in range(40):
+        a = np.unique(rng.integers(0, 200, size=rng.integers(1, 120)))
+        b = np.unique(rng.integers(0, 200, size=rng.integers(1, 120)))
+        table.append((a.tolist(), b.tolist(), int(rng.integers(0, 40))))
+    checker = _types.SimilarityCheckerExtScreensorted()
+    res, flat_a, flat_b, la, lb, cs = [], [], [], [], [], []
+    for a, b, c in table:
+        na_, nb_ = _types.NeighboursExtVector(8), _types.NeighboursExtVector(8)
+        for m in a:
+            na_.assign(m)
+        for m in b:
+            nb_.assign(m)
+        res.append(bool(checker.check(na_, nb_, ClusterParameters(0.0, similarity_cutoff=c))))
+        flat_a += list(a); flat_b += list(b); la.append(len(a)); lb.append(len(b)); cs.append(c)
+    save("check_table.npz", a=np.array(flat_a, dtype=np.int32), b=np.array(flat_b, dtype=np.int32),
+         len_a=np.array(la, dtype=np.int64), len_b=np.array(lb, dtype=np.int64),
+         c=np.array(cs, dtype=np.int64), expected=np.array(res, dtype=np.bool_))
+
+    # 10. edge cases: exact-boundary distances, duplicates, 1-D and 3-D, tiny sets
+    g = np.array([[i, j] for i in range(8) for j in range(8)], dtype=np.float64)
+    fit_case("edge_grid_boundary.npz", g, 1.0, 2)            # s == r**2 exactly for lattice neighbours
+    dup = np.repeat(rng.normal(size=(40, 2)), 3, axis=0)
+    fit_case("edge_duplicates.npz", dup, 0.3, 2)
+    line = np.sort(rng.uniform(0, 10, size=300))[:, None]
+    fit_case("edge_1d.npz", line, 0.15, 3)
+    cube = np.vstack([rng.normal(0, 0.2, size=(250, 3)), rng.normal(1.5, 0.25, size=(250, 3))])
+    fit_case("edge_3d.npz", cube, 0.2, 6, fit_kwargs={"member_cutoff": 3})
+    fit_case("edge_single.npz", np.zeros((1, 2)), 0.5, 0)
+    fit_case("edge_allnoise.npz", rng.uniform(0, 100, size=(60, 2)), 0.5, 1)
+    fit_case("edge_c0.npz", cube[:200], 0.15, 0, fit_kwargs={"member_cutoff": 1})
+
+    # 11. higher dimensions (the generic / Gram neighbour search paths)
+    for d in (16, 64):
+        xh = workloads.features(n=600, d=d, seed=7, n_clusters=6)
+        dist = np.sqrt(((xh[:50, None, :] - xh[None, :, :]) ** 2).sum(-1))
+        r = float(np.quantile(np.sort(dist, axis=1)[:, 25], 0.5))
+        fit_case(f"highdim_{d}.npz", xh, r, 5, fit_kwargs={"member_cutoff": 5})
+
+
+if __name__ == "__main__":
+    main()
