@@ -1,0 +1,315 @@
+"""ctypes binding of libcnngpu.so (the C ABI declared in include/cnngpu.h).
+
+The library is the only compute path: if it cannot be loaded, every entry
+point raises.  There is no CPU fallback.
+
+Arrays handed to the library are numpy arrays (host memory, copied by the
+library) or CUDA device arrays: torch tensors on a CUDA device or any
+object exposing ``__cuda_array_interface__`` (used in place, on the
+context's stream).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+from typing import Optional
+
+import numpy as np
+
+from . import _build
+
+CNN_OK = 0
+_STATUS = {1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "timeout",
+           5: "unsupported", 6: "bad state"}
+
+METRIC_EUCLIDEAN_REDUCED = 0
+METRIC_EUCLIDEAN = 1
+FP_SEPARATE = 0
+FP_FUSED = 1
+DTYPE_F64 = 0
+DTYPE_F32 = 1
+MEM_HOST = 0
+MEM_DEVICE = 1
+
+
+class CNNError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{_STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class cnn_stats(ctypes.Structure):
+    _fields_ = [
+        ("n_points", ctypes.c_int64), ("n_nonzero", ctypes.c_int64), ("n_nodes", ctypes.c_int64),
+        ("n_checks", ctypes.c_int64), ("n_accepted", ctypes.c_int64), ("n_exact", ctypes.c_int64),
+        ("n_candidates", ctypes.c_int64), ("n_clusters", ctypes.c_int64),
+        ("search_kind", ctypes.c_int32), ("filter_enabled", ctypes.c_int32), ("filter_band", ctypes.c_double),
+        ("ms_bbox", ctypes.c_float), ("ms_cells", ctypes.c_float), ("ms_count", ctypes.c_float),
+        ("ms_scan", ctypes.c_float), ("ms_fill", ctypes.c_float), ("ms_nodes", ctypes.c_float),
+        ("ms_check", ctypes.c_float), ("ms_label", ctypes.c_float), ("ms_sort", ctypes.c_float),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+# every symbol include/cnngpu.h declares, with its ctypes signature
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int32
+_INT = ctypes.c_int
+SIGNATURES = {
+    "cnn_abi_version": (_INT, []),
+    "cnn_create": (_INT, [ctypes.POINTER(_P), _INT, _P]),
+    "cnn_destroy": (_INT, [_P]),
+    "cnn_set_stream": (_INT, [_P, _P]),
+    "cnn_last_error": (ctypes.c_char_p, [_P]),
+    "cnn_set_timing": (_INT, [_P, _INT]),
+    "cnn_get_stats": (_INT, [_P, ctypes.POINTER(cnn_stats)]),
+    "cnn_set_points": (_INT, [_P, _P, _INT, _I64, _I32, _INT]),
+    "cnn_build_neighbours": (_INT, [_P, ctypes.c_double, _INT, _INT]),
+    "cnn_set_neighbours": (_INT, [_P, _P, _P, _I64, _INT]),
+    "cnn_neighbour_count": (_INT, [_P, ctypes.POINTER(_I64)]),
+    "cnn_get_neighbours": (_INT, [_P, _P, _P, _INT]),
+    "cnn_fit": (_INT, [_P, _I64, _I64, _I64, _P, _P, _INT]),
+    "cnn_sort_by_size": (_INT, [_P, _P, _I64, _I64, _I64, _INT]),
+    "cnn_check_lists": (_INT, [_P, _P, _I64, _P, _I64, _I64, _P, _INT]),
+}
+
+_lib = None
+_lib_lock = threading.Lock()
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load libcnngpu.so (building it first when it is missing or stale)."""
+    global _lib
+    with _lib_lock:
+        if _lib is None:
+            path = _build.LIB
+            if build_if_missing:
+                _build.build()
+            if not os.path.exists(path):
+                raise ImportError(f"libcnngpu.so not found at {path}; build it with "
+                                  "python -c 'import __graft_entry__ as g; g.build()'")
+            L = ctypes.CDLL(path)
+            for name, (res, args) in SIGNATURES.items():
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
+            _lib = L
+    return _lib
+
+
+# ---------------------------------------------------------------------------
+# array helpers
+# ---------------------------------------------------------------------------
+def _torch():
+    try:
+        import torch
+        return torch
+    except ImportError:  # pragma: no cover
+        return None
+
+
+def is_device_array(a) -> bool:
+    t = _torch()
+    if t is not None and isinstance(a, t.Tensor):
+        return a.is_cuda
+    return hasattr(a, "__cuda_array_interface__")
+
+
+def device_pointer(a, dtype, writable=False) -> int:
+    """Pointer of a contiguous CUDA array of the given numpy dtype."""
+    t = _torch()
+    if t is not None and isinstance(a, t.Tensor):
+        want = {np.float64: t.float64, np.float32: t.float32, np.int64: t.int64,
+                np.int32: t.int32, np.uint8: t.uint8}[np.dtype(dtype).type]
+        if a.dtype != want:
+            raise TypeError(f"expected a {want} tensor, got {a.dtype}")
+        if not a.is_contiguous():
+            raise ValueError("device tensors must be contiguous")
+        return int(a.data_ptr())
+    cai = a.__cuda_array_interface__
+    if np.dtype(cai["typestr"]) != np.dtype(dtype):
+        raise TypeError(f"expected {np.dtype(dtype)}, got {cai['typestr']}")
+    if cai.get("strides") not in (None,):
+        exp = np.empty(cai["shape"], dtype=dtype).strides
+        if tuple(cai["strides"]) != tuple(exp):
+            raise ValueError("device arrays must be C-contiguous")
+    if writable and cai["data"][1]:
+        raise ValueError("device array is read-only")
+    return int(cai["data"][0])
+
+
+def host_array(a, dtype, writable=False) -> np.ndarray:
+    arr = np.asarray(a)
+    if arr.dtype != np.dtype(dtype) or not arr.flags.c_contiguous:
+        if writable:
+            raise TypeError(f"in-place arrays must be C-contiguous {np.dtype(dtype)}")
+        arr = np.ascontiguousarray(arr, dtype=dtype)
+    if writable and not arr.flags.writeable:
+        raise ValueError("array is read-only")
+    return arr
+
+
+def current_torch_stream(device: int) -> Optional[int]:
+    t = _torch()
+    if t is None or not t.cuda.is_available():
+        return None
+    return int(t.cuda.current_stream(device).cuda_stream)
+
+
+class Context:
+    """One library context: device workspace, neighbour graph, stream."""
+
+    def __init__(self, device: int = 0, stream: Optional[int] = None):
+        self._lib = load()
+        h = ctypes.c_void_p()
+        st = self._lib.cnn_create(ctypes.byref(h), int(device), ctypes.c_void_p(stream) if stream else None)
+        if st != CNN_OK:
+            raise CNNError(st, f"cnn_create(device={device}) failed (is a CUDA device visible?)")
+        self._h = h
+        self.device = int(device)
+        self.stream = stream
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.cnn_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int, what: str):
+        if st != CNN_OK:
+            msg = self._lib.cnn_last_error(self._h)
+            raise CNNError(st, f"{what}: {msg.decode() if msg else ''}")
+
+    # -- configuration -------------------------------------------------------
+    def set_stream(self, stream: Optional[int]):
+        self._check(self._lib.cnn_set_stream(self._h, ctypes.c_void_p(stream) if stream else None),
+                    "cnn_set_stream")
+        self.stream = stream
+
+    def set_timing(self, enabled: bool):
+        self._check(self._lib.cnn_set_timing(self._h, 1 if enabled else 0), "cnn_set_timing")
+
+    def stats(self) -> dict:
+        s = cnn_stats()
+        self._check(self._lib.cnn_get_stats(self._h, ctypes.byref(s)), "cnn_get_stats")
+        return s.as_dict()
+
+    # -- neighbour graph -------------------------------------------------------
+    def set_points(self, points):
+        """points: [n, d] float64/float32 numpy array or CUDA array."""
+        if is_device_array(points):
+            shape = tuple(points.shape)
+            dt = np.float32 if "float32" in str(points.dtype) else np.float64
+            ptr = device_pointer(points, dt)
+            mem, keep = MEM_DEVICE, points
+        else:
+            arr = np.asarray(points)
+            dt = np.float32 if arr.dtype == np.float32 else np.float64
+            arr = host_array(arr, dt)
+            shape = arr.shape
+            ptr, mem, keep = arr.ctypes.data, MEM_HOST, arr
+        if len(shape) == 1:
+            shape = (shape[0], 1)
+        if len(shape) != 2:
+            raise ValueError("points must be a 2D array [n_points, n_dim]")
+        self._check(self._lib.cnn_set_points(self._h, ctypes.c_void_p(ptr), DTYPE_F32 if dt == np.float32 else DTYPE_F64,
+                                             int(shape[0]), int(shape[1]), mem), "cnn_set_points")
+        self._points_ref = keep
+        return shape
+
+    def build_neighbours(self, radius_cutoff: float, metric: int = METRIC_EUCLIDEAN_REDUCED,
+                         fpmode: int = FP_SEPARATE):
+        self._check(self._lib.cnn_build_neighbours(self._h, float(radius_cutoff), int(metric), int(fpmode)),
+                    "cnn_build_neighbours")
+
+    def set_neighbours(self, offsets, indices):
+        if is_device_array(offsets):
+            n = int(offsets.shape[0]) - 1
+            self._check(self._lib.cnn_set_neighbours(
+                self._h, ctypes.c_void_p(device_pointer(offsets, np.int64)),
+                ctypes.c_void_p(device_pointer(indices, np.int32)), n, MEM_DEVICE), "cnn_set_neighbours")
+            self._points_ref = (offsets, indices)
+        else:
+            off = host_array(offsets, np.int64)
+            idx = host_array(indices, np.int32)
+            n = off.shape[0] - 1
+            self._check(self._lib.cnn_set_neighbours(self._h, ctypes.c_void_p(off.ctypes.data),
+                                                     ctypes.c_void_p(idx.ctypes.data), n, MEM_HOST),
+                        "cnn_set_neighbours")
+
+    def neighbour_count(self) -> int:
+        v = ctypes.c_int64()
+        self._check(self._lib.cnn_neighbour_count(self._h, ctypes.byref(v)), "cnn_neighbour_count")
+        return int(v.value)
+
+    def get_neighbours(self, n_points: int):
+        """Sorted CSR (offsets int64[n+1], indices int32[nnz]) as numpy arrays."""
+        nnz = self.neighbour_count()
+        off = np.empty(n_points + 1, dtype=np.int64)
+        idx = np.empty(max(nnz, 1), dtype=np.int32)
+        self._check(self._lib.cnn_get_neighbours(self._h, ctypes.c_void_p(off.ctypes.data),
+                                                 ctypes.c_void_p(idx.ctypes.data), MEM_HOST),
+                    "cnn_get_neighbours")
+        return off, idx[:nnz]
+
+    # -- fit -------------------------------------------------------------------
+    def fit(self, similarity_cutoff: int, n_member_cutoff: int, current_start: int, consider, labels):
+        """Cluster the current graph; labels/consider updated in place."""
+        if is_device_array(labels):
+            lp = device_pointer(labels, np.int64, writable=True)
+            cp = device_pointer(consider, np.uint8, writable=True)
+            mem = MEM_DEVICE
+        else:
+            lab = host_array(labels, np.int64, writable=True)
+            con = host_array(consider, np.uint8, writable=True)
+            lp, cp, mem = lab.ctypes.data, con.ctypes.data, MEM_HOST
+        self._check(self._lib.cnn_fit(self._h, int(similarity_cutoff), int(n_member_cutoff), int(current_start),
+                                      ctypes.c_void_p(cp), ctypes.c_void_p(lp), mem), "cnn_fit")
+
+    def sort_by_size(self, labels, member_cutoff: int, max_clusters: Optional[int]):
+        mx = -1 if max_clusters is None else int(max_clusters)
+        if mx < -1:
+            mx = 0  # a negative limit keeps no cluster (every rank exceeds it)
+        if is_device_array(labels):
+            lp, mem, n = device_pointer(labels, np.int64, writable=True), MEM_DEVICE, int(labels.shape[0])
+        else:
+            lab = host_array(labels, np.int64, writable=True)
+            lp, mem, n = lab.ctypes.data, MEM_HOST, lab.shape[0]
+        self._check(self._lib.cnn_sort_by_size(self._h, ctypes.c_void_p(lp), n, int(member_cutoff), mx, mem),
+                    "cnn_sort_by_size")
+
+    def check_lists(self, a, b, c: int) -> bool:
+        a = host_array(a, np.int32)
+        b = host_array(b, np.int32)
+        r = np.zeros(1, dtype=np.int32)
+        self._check(self._lib.cnn_check_lists(self._h, ctypes.c_void_p(a.ctypes.data), a.shape[0],
+                                              ctypes.c_void_p(b.ctypes.data), b.shape[0], int(c),
+                                              ctypes.c_void_p(r.ctypes.data), MEM_HOST), "cnn_check_lists")
+        return bool(r[0])
+
+
+_tls = threading.local()
+
+
+def default_context(device: int = 0) -> Context:
+    """A per-thread, per-device context (contexts are not thread-safe)."""
+    ctxs = getattr(_tls, "ctxs", None)
+    if ctxs is None:
+        ctxs = _tls.ctxs = {}
+    ctx = ctxs.get(device)
+    if ctx is None:
+        ctx = ctxs[device] = Context(device)
+    return ctx

@@ -1,0 +1,330 @@
+// cnngpu.cu -- the C ABI: context lifetime, argument checks, host<->device
+// staging, and dispatch to the kernels in search.cu / fit.cu / prims.cu.
+#include <stdio.h>
+#include <string.h>
+
+#include <new>
+
+#include "common.cuh"
+
+namespace cnn {
+
+void stage_begin(cnn_context *ctx, int slot) {
+    if (!ctx->timing || slot < 0 || slot >= cnn_context::kSlots) return;
+    cudaEventRecord(ctx->ev_begin[slot], ctx->stream);
+}
+
+void stage_end(cnn_context *ctx, int slot) {
+    if (!ctx->timing || slot < 0 || slot >= cnn_context::kSlots) return;
+    cudaEventRecord(ctx->ev_end[slot], ctx->stream);
+    ctx->slot_pending[slot] = true;
+}
+
+namespace {
+
+__global__ void widen_f32_kernel(const float *__restrict__ in, int64_t total, double *__restrict__ out) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+        out[e] = (double)in[e];
+}
+
+cnn_status check_ctx(cnn_context *ctx) {
+    if (!ctx) return CNN_ERR_INVALID_ARG;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return ctx->fail(CNN_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    return CNN_OK;
+}
+
+// Copy a host array into a staging buffer or pass a device pointer through.
+template <typename T>
+cnn_status stage_in(cnn_context *ctx, cnn::DevBuf &buf, const T *src, int64_t count, cnn_memspace mem,
+                    const T **dev_out) {
+    if (mem == CNN_MEM_DEVICE) {
+        *dev_out = src;
+        return CNN_OK;
+    }
+    CNN_TRY(ctx->ensure(buf, sizeof(T) * (size_t)(count > 0 ? count : 1)));
+    if (count > 0)
+        CNN_CUDA(ctx, cudaMemcpyAsync(buf.ptr, src, sizeof(T) * (size_t)count, cudaMemcpyHostToDevice, ctx->stream));
+    *dev_out = buf.as<T>();
+    return CNN_OK;
+}
+
+}  // namespace
+}  // namespace cnn
+
+using namespace cnn;
+
+extern "C" {
+
+CNN_API int cnn_abi_version(void) { return CNN_ABI_VERSION; }
+
+CNN_API cnn_status cnn_create(cnn_context **out, int device, void *stream) {
+    if (!out) return CNN_ERR_INVALID_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+        (void)cudaGetLastError();
+        return CNN_ERR_CUDA;
+    }
+    cnn_context *ctx = new (std::nothrow) cnn_context();
+    if (!ctx) return CNN_ERR_OOM;
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) {
+        delete ctx;
+        return CNN_ERR_CUDA;
+    }
+    if (stream) {
+        ctx->stream = static_cast<cudaStream_t>(stream);
+    } else {
+        if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete ctx;
+            return CNN_ERR_CUDA;
+        }
+        ctx->own_stream = true;
+    }
+    for (int i = 0; i < cnn_context::kSlots; ++i) {
+        if (cudaEventCreate(&ctx->ev_begin[i]) != cudaSuccess || cudaEventCreate(&ctx->ev_end[i]) != cudaSuccess) {
+            (void)cudaGetLastError();
+            cnn_destroy(ctx);
+            return CNN_ERR_CUDA;
+        }
+    }
+    *out = ctx;
+    return CNN_OK;
+}
+
+CNN_API cnn_status cnn_destroy(cnn_context *ctx) {
+    if (!ctx) return CNN_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    cnn::DevBuf *bufs[] = {&ctx->x_own, &ctx->x_f32_stage, &ctx->perm, &ctx->inv, &ctx->deg, &ctx->row_off,
+                           &ctx->cols, &ctx->xf4, &ctx->cell_of, &ctx->cell_start, &ctx->node, &ctx->parent,
+                           &ctx->comp_min, &ctx->flag, &ctx->counters, &ctx->stage_labels,
+                           &ctx->stage_consider, &ctx->stage_offsets, &ctx->stage_indices, &ctx->stage_misc,
+                           &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->scratch_a, &ctx->scratch_b,
+                           &ctx->scratch_c, &ctx->scratch_d, &ctx->scan_tmp};
+    for (cnn::DevBuf *b : bufs)
+        if (b->ptr) cudaFree(b->ptr);
+    for (int i = 0; i < cnn_context::kSlots; ++i) {
+        if (ctx->ev_begin[i]) cudaEventDestroy(ctx->ev_begin[i]);
+        if (ctx->ev_end[i]) cudaEventDestroy(ctx->ev_end[i]);
+    }
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    (void)cudaGetLastError();
+    delete ctx;
+    return CNN_OK;
+}
+
+CNN_API cnn_status cnn_set_stream(cnn_context *ctx, void *stream) {
+    CNN_TRY(check_ctx(ctx));
+    CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->own_stream) {
+        cudaStreamDestroy(ctx->stream);
+        ctx->own_stream = false;
+    }
+    if (stream) {
+        ctx->stream = static_cast<cudaStream_t>(stream);
+    } else {
+        CNN_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        ctx->own_stream = true;
+    }
+    return CNN_OK;
+}
+
+CNN_API const char *cnn_last_error(const cnn_context *ctx) {
+    if (!ctx) return "null context";
+    return ctx->last_error.c_str();
+}
+
+CNN_API cnn_status cnn_set_timing(cnn_context *ctx, int enabled) {
+    if (!ctx) return CNN_ERR_INVALID_ARG;
+    ctx->timing = enabled != 0;
+    for (int i = 0; i < cnn_context::kSlots; ++i) ctx->slot_pending[i] = false;
+    return CNN_OK;
+}
+
+CNN_API cnn_status cnn_get_stats(const cnn_context *cctx, cnn_stats *out) {
+    cnn_context *ctx = const_cast<cnn_context *>(cctx);
+    if (!ctx || !out) return CNN_ERR_INVALID_ARG;
+    CNN_TRY(check_ctx(ctx));
+    CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    float *slot_field[cnn_context::kSlots] = {
+        &ctx->stats.ms_bbox, &ctx->stats.ms_cells, &ctx->stats.ms_count, &ctx->stats.ms_scan,
+        &ctx->stats.ms_fill, &ctx->stats.ms_nodes, &ctx->stats.ms_check, &ctx->stats.ms_label,
+        &ctx->stats.ms_sort, nullptr, nullptr, nullptr};
+    for (int i = 0; i < cnn_context::kSlots; ++i) {
+        if (!ctx->slot_pending[i] || !slot_field[i]) continue;
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, ctx->ev_begin[i], ctx->ev_end[i]) == cudaSuccess) *slot_field[i] = ms;
+        (void)cudaGetLastError();
+    }
+    *out = ctx->stats;
+    return CNN_OK;
+}
+
+CNN_API cnn_status cnn_set_points(cnn_context *ctx, const void *points, cnn_dtype dtype, int64_t n_points,
+                                  int32_t n_dim, cnn_memspace mem) {
+    CNN_TRY(check_ctx(ctx));
+    if (n_points < 0 || n_points > INT32_MAX - 1 || n_dim < 1 || (n_points > 0 && !points))
+        return ctx->fail(CNN_ERR_INVALID_ARG, "n_points must be in [0, 2^31-2], n_dim >= 1");
+    if (dtype != CNN_DTYPE_F64 && dtype != CNN_DTYPE_F32) return ctx->fail(CNN_ERR_INVALID_ARG, "bad dtype");
+    if (mem != CNN_MEM_HOST && mem != CNN_MEM_DEVICE) return ctx->fail(CNN_ERR_INVALID_ARG, "bad memspace");
+    ctx->have_graph = false;
+    ctx->n = n_points;
+    ctx->d = n_dim;
+    const int64_t total = n_points * n_dim;
+    if (dtype == CNN_DTYPE_F64) {
+        if (mem == CNN_MEM_DEVICE) {
+            ctx->x = static_cast<const double *>(points);
+        } else {
+            CNN_TRY(ctx->ensure(ctx->x_own, sizeof(double) * (size_t)(total > 0 ? total : 1)));
+            if (total > 0)
+                CNN_CUDA(ctx, cudaMemcpyAsync(ctx->x_own.ptr, points, sizeof(double) * (size_t)total,
+                                              cudaMemcpyHostToDevice, ctx->stream));
+            ctx->x = ctx->x_own.as<double>();
+        }
+    } else {
+        const float *src = static_cast<const float *>(points);
+        if (mem == CNN_MEM_HOST) {
+            CNN_TRY(ctx->ensure(ctx->x_f32_stage, sizeof(float) * (size_t)(total > 0 ? total : 1)));
+            if (total > 0)
+                CNN_CUDA(ctx, cudaMemcpyAsync(ctx->x_f32_stage.ptr, points, sizeof(float) * (size_t)total,
+                                              cudaMemcpyHostToDevice, ctx->stream));
+            src = ctx->x_f32_stage.as<float>();
+        }
+        CNN_TRY(ctx->ensure(ctx->x_own, sizeof(double) * (size_t)(total > 0 ? total : 1)));
+        if (total > 0) {
+            widen_f32_kernel<<<grid_for(total, 256) > 4096 ? 4096 : grid_for(total, 256), 256, 0, ctx->stream>>>(
+                src, total, ctx->x_own.as<double>());
+            CNN_LAUNCH_CHECK(ctx);
+        }
+        ctx->x = ctx->x_own.as<double>();
+    }
+    return CNN_OK;
+}
+
+CNN_API cnn_status cnn_build_neighbours(cnn_context *ctx, double radius_cutoff, cnn_metric metric,
+                                        cnn_fpmode fpmode) {
+    CNN_TRY(check_ctx(ctx));
+    if (metric != CNN_METRIC_EUCLIDEAN_REDUCED && metric != CNN_METRIC_EUCLIDEAN)
+        return ctx->fail(CNN_ERR_INVALID_ARG, "unknown metric");
+    if (fpmode != CNN_FP_SEPARATE && fpmode != CNN_FP_FUSED) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown fpmode");
+    if (ctx->d < 1) return ctx->fail(CNN_ERR_STATE, "no points: call cnn_set_points first");
+    return build_neighbours_impl(ctx, radius_cutoff, metric, fpmode);
+}
+
+CNN_API cnn_status cnn_set_neighbours(cnn_context *ctx, const int64_t *offsets, const int32_t *indices,
+                                      int64_t n_points, cnn_memspace mem) {
+    CNN_TRY(check_ctx(ctx));
+    if (n_points < 0 || n_points > INT32_MAX - 1 || !offsets)
+        return ctx->fail(CNN_ERR_INVALID_ARG, "n_points must be in [0, 2^31-2] and offsets given");
+    int64_t nnz = 0;
+    if (mem == CNN_MEM_HOST) {
+        nnz = offsets[n_points];
+        if (offsets[0] != 0 || nnz < 0) return ctx->fail(CNN_ERR_INVALID_ARG, "offsets must start at 0");
+        if (nnz > 0 && !indices) return ctx->fail(CNN_ERR_INVALID_ARG, "indices missing");
+    }
+    const int64_t *off_dev = nullptr;
+    const int32_t *idx_dev = nullptr;
+    CNN_TRY(stage_in<int64_t>(ctx, ctx->stage_offsets, offsets, n_points + 1, mem, &off_dev));
+    CNN_TRY(stage_in<int32_t>(ctx, ctx->stage_indices, indices, nnz, mem, &idx_dev));
+    return set_neighbours_impl(ctx, off_dev, idx_dev, n_points);
+}
+
+CNN_API cnn_status cnn_neighbour_count(cnn_context *ctx, int64_t *nnz) {
+    CNN_TRY(check_ctx(ctx));
+    if (!nnz) return ctx->fail(CNN_ERR_INVALID_ARG, "null output");
+    if (!ctx->have_graph) return ctx->fail(CNN_ERR_STATE, "no neighbour graph");
+    *nnz = ctx->nnz;
+    return CNN_OK;
+}
+
+CNN_API cnn_status cnn_get_neighbours(cnn_context *ctx, int64_t *offsets, int32_t *indices, cnn_memspace mem) {
+    CNN_TRY(check_ctx(ctx));
+    if (!ctx->have_graph) return ctx->fail(CNN_ERR_STATE, "no neighbour graph");
+    if (!offsets || (ctx->nnz > 0 && !indices)) return ctx->fail(CNN_ERR_INVALID_ARG, "null output");
+    const int64_t n = ctx->n, nnz = ctx->nnz;
+    int64_t *off_dev = offsets;
+    int32_t *idx_dev = indices;
+    if (mem == CNN_MEM_HOST) {
+        CNN_TRY(ctx->ensure(ctx->stage_offsets, sizeof(int64_t) * (size_t)(n + 1)));
+        CNN_TRY(ctx->ensure(ctx->stage_indices, sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1)));
+        off_dev = ctx->stage_offsets.as<int64_t>();
+        idx_dev = ctx->stage_indices.as<int32_t>();
+    }
+    CNN_TRY(export_neighbours_impl(ctx, off_dev, idx_dev));
+    if (mem == CNN_MEM_HOST) {
+        CNN_CUDA(ctx, cudaMemcpyAsync(offsets, off_dev, sizeof(int64_t) * (size_t)(n + 1), cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+        if (nnz > 0)
+            CNN_CUDA(ctx, cudaMemcpyAsync(indices, idx_dev, sizeof(int32_t) * (size_t)nnz, cudaMemcpyDeviceToHost,
+                                          ctx->stream));
+    }
+    CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return CNN_OK;
+}
+
+CNN_API cnn_status cnn_fit(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
+                           int64_t current_start, uint8_t *consider, int64_t *labels, cnn_memspace mem) {
+    CNN_TRY(check_ctx(ctx));
+    if (!ctx->have_graph) return ctx->fail(CNN_ERR_STATE, "no neighbour graph: build or set neighbours first");
+    const int64_t n = ctx->n;
+    if (n > 0 && (!consider || !labels)) return ctx->fail(CNN_ERR_INVALID_ARG, "consider and labels are required");
+    uint8_t *cons_dev = consider;
+    int64_t *lab_dev = labels;
+    if (mem == CNN_MEM_HOST) {
+        const uint8_t *c_in = nullptr;
+        const int64_t *l_in = nullptr;
+        CNN_TRY(stage_in<uint8_t>(ctx, ctx->stage_consider, consider, n, mem, &c_in));
+        CNN_TRY(stage_in<int64_t>(ctx, ctx->stage_labels, labels, n, mem, &l_in));
+        cons_dev = const_cast<uint8_t *>(c_in);
+        lab_dev = const_cast<int64_t *>(l_in);
+    }
+    CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
+    if (mem == CNN_MEM_HOST && n > 0) {
+        CNN_CUDA(ctx, cudaMemcpyAsync(labels, lab_dev, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+        CNN_CUDA(ctx, cudaMemcpyAsync(consider, cons_dev, (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+        CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return CNN_OK;
+}
+
+CNN_API cnn_status cnn_sort_by_size(cnn_context *ctx, int64_t *labels, int64_t n, int64_t member_cutoff,
+                                    int64_t max_clusters, cnn_memspace mem) {
+    CNN_TRY(check_ctx(ctx));
+    if (n < 0 || (n > 0 && !labels)) return ctx->fail(CNN_ERR_INVALID_ARG, "bad labels");
+    int64_t *lab_dev = labels;
+    if (mem == CNN_MEM_HOST) {
+        const int64_t *l_in = nullptr;
+        CNN_TRY(stage_in<int64_t>(ctx, ctx->stage_labels, labels, n, mem, &l_in));
+        lab_dev = const_cast<int64_t *>(l_in);
+    }
+    CNN_TRY(sort_by_size_impl(ctx, lab_dev, n, member_cutoff, max_clusters));
+    if (mem == CNN_MEM_HOST && n > 0) {
+        CNN_CUDA(ctx, cudaMemcpyAsync(labels, lab_dev, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+        CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return CNN_OK;
+}
+
+CNN_API cnn_status cnn_check_lists(cnn_context *ctx, const int32_t *a, int64_t na, const int32_t *b, int64_t nb,
+                                   int64_t c, int32_t *result, cnn_memspace mem) {
+    CNN_TRY(check_ctx(ctx));
+    if (na < 0 || nb < 0 || !result || (na > 0 && !a) || (nb > 0 && !b))
+        return ctx->fail(CNN_ERR_INVALID_ARG, "bad lists");
+    const int32_t *a_dev = a, *b_dev = b;
+    int32_t *r_dev = result;
+    if (mem == CNN_MEM_HOST) {
+        CNN_TRY(stage_in<int32_t>(ctx, ctx->stage_offsets, a, na, mem, &a_dev));
+        CNN_TRY(stage_in<int32_t>(ctx, ctx->stage_indices, b, nb, mem, &b_dev));
+        CNN_TRY(ctx->ensure(ctx->stage_misc, 64));
+        r_dev = ctx->stage_misc.as<int32_t>();
+    }
+    CNN_TRY(check_lists_impl(ctx, a_dev, na, b_dev, nb, c, r_dev));
+    if (mem == CNN_MEM_HOST)
+        CNN_CUDA(ctx, cudaMemcpyAsync(result, r_dev, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return CNN_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,167 @@
+// common.cuh -- shared device helpers and the context definition.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "cnngpu.h"
+
+namespace cnn {
+
+constexpr int kWarp = 32;
+
+// ---------------------------------------------------------------------------
+// Status plumbing: every CUDA call goes through CNN_CUDA, which records the
+// message on the context and returns CNN_ERR_CUDA (or CNN_ERR_OOM).
+// ---------------------------------------------------------------------------
+struct Error {
+    cnn_status status;
+    std::string msg;
+};
+
+#define CNN_CUDA(ctx, expr)                                                             \
+    do {                                                                                \
+        cudaError_t e_ = (expr);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            (void)cudaGetLastError();                                                   \
+            return (ctx)->fail(e_ == cudaErrorMemoryAllocation ? CNN_ERR_OOM : CNN_ERR_CUDA, \
+                               std::string(#expr) + ": " + cudaGetErrorString(e_));     \
+        }                                                                               \
+    } while (0)
+
+#define CNN_TRY(expr)                       \
+    do {                                    \
+        cnn_status s_ = (expr);             \
+        if (s_ != CNN_OK) return s_;        \
+    } while (0)
+
+#define CNN_LAUNCH_CHECK(ctx) CNN_CUDA(ctx, cudaGetLastError())
+
+// A grow-only device buffer.  Memory is returned only when the context is
+// destroyed, so repeated fits of the same size allocate nothing.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t cap = 0;
+    template <typename T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+// Stage timer: CUDA events on the context stream.
+struct StageTimer {
+    cudaEvent_t a = nullptr, b = nullptr;
+};
+
+}  // namespace cnn
+
+// The context behind the opaque cnn_context handle.
+struct cnn_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    bool timing = false;
+    std::string last_error;
+    cnn_stats stats{};
+
+    // points (original order, row-major float64)
+    int64_t n = 0;
+    int32_t d = 0;
+    const double *x = nullptr;  // device pointer (borrowed or owned copy)
+    cnn::DevBuf x_own;
+    cnn::DevBuf x_f32_stage;    // float32 input staged before widening
+
+    // neighbour graph in internal (permuted) index space
+    bool have_graph = false;
+    bool identity_perm = true;
+    int64_t nnz = 0;
+    cnn::DevBuf perm;     // int32[n]: internal -> point index
+    cnn::DevBuf inv;      // int32[n]: point index -> internal
+    cnn::DevBuf deg;      // int32[n]
+    cnn::DevBuf row_off;  // int64[n+1]
+    cnn::DevBuf cols;     // int32[nnz], ascending internal indices per row
+    cnn::DevBuf xf4;      // float4[n] permuted float32 coordinates (grid search)
+    cnn::DevBuf cell_of;  // int32[n] cell id per point (original order)
+    cnn::DevBuf cell_start;  // int32[ncells+2]
+
+    // fit work arrays
+    cnn::DevBuf node;     // uint8[n]
+    cnn::DevBuf parent;   // int32[n]
+    cnn::DevBuf comp_min; // int32[n]
+    cnn::DevBuf flag;     // int32[n+1]
+    cnn::DevBuf counters; // unsigned long long[16]
+
+    // staging for host<->device transfers and general scratch
+    cnn::DevBuf stage_labels, stage_consider, stage_offsets, stage_indices, stage_misc;
+    cnn::DevBuf io_a, io_b, io_c;
+    cnn::DevBuf scratch_a, scratch_b, scratch_c, scratch_d, scan_tmp;
+
+    // stage timing: events recorded on the stream, read in cnn_get_stats
+    static constexpr int kSlots = 12;
+    cudaEvent_t ev_begin[kSlots] = {};
+    cudaEvent_t ev_end[kSlots] = {};
+    bool slot_pending[kSlots] = {};
+
+    cnn_status fail(cnn_status s, const std::string &msg) {
+        last_error = msg;
+        return s;
+    }
+    cnn_status ensure(cnn::DevBuf &b, size_t bytes) {
+        if (bytes <= b.cap) return CNN_OK;
+        if (b.ptr) {
+            cudaError_t e = cudaStreamSynchronize(stream);
+            if (e != cudaSuccess) return fail(CNN_ERR_CUDA, cudaGetErrorString(e));
+            cudaFree(b.ptr);
+            b.ptr = nullptr;
+            b.cap = 0;
+        }
+        size_t want = bytes < 256 ? 256 : bytes;
+        want = (want + 255) & ~size_t(255);
+        cudaError_t e = cudaMalloc(&b.ptr, want);
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            b.ptr = nullptr;
+            return fail(e == cudaErrorMemoryAllocation ? CNN_ERR_OOM : CNN_ERR_CUDA,
+                        std::string("cudaMalloc(") + std::to_string(want) + "): " + cudaGetErrorString(e));
+        }
+        b.cap = want;
+        return CNN_OK;
+    }
+};
+
+namespace cnn {
+
+// ---- launchers implemented in the .cu files --------------------------------
+
+// prims.cu
+cnn_status scan_exclusive_i64(cnn_context *ctx, const int64_t *in, int64_t *out, int64_t n);
+cnn_status scan_exclusive_i32_to_i64(cnn_context *ctx, const int32_t *in, int64_t *out, int64_t n);
+cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits);
+cnn_status fill_i32(cnn_context *ctx, int32_t *p, int64_t n, int32_t v);
+cnn_status iota_i32(cnn_context *ctx, int32_t *p, int64_t n);
+
+// search.cu
+cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode);
+cnn_status export_neighbours_impl(cnn_context *ctx, int64_t *offsets_dev, int32_t *indices_dev);
+cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev,
+                               const int32_t *indices_dev, int64_t n);
+
+// fit.cu
+cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
+                    int64_t current_start, uint8_t *consider_dev, int64_t *labels_dev);
+cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels_dev, int64_t n,
+                             int64_t member_cutoff, int64_t max_clusters);
+cnn_status check_lists_impl(cnn_context *ctx, const int32_t *a, int64_t na, const int32_t *b,
+                            int64_t nb, int64_t c, int32_t *result_dev);
+
+// timing helpers (cnngpu.cu): events only, no synchronisation
+void stage_begin(cnn_context *ctx, int slot);
+void stage_end(cnn_context *ctx, int slot);
+
+inline unsigned grid_for(int64_t n, int block) {
+    int64_t g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > 0x7fffffff) g = 0x7fffffff;
+    return (unsigned)g;
+}
+
+}  // namespace cnn

@@ -1,0 +1,499 @@
+// fit.cu -- cluster assignment on the neighbour graph.
+//
+// Reference: FitterExtBFS._fit (src/cnnclustering/_fit.pyx:408-491) grows
+// clusters breadth-first.  A point is a node when it has more than
+// n_member_cutoff neighbours (NeighboursExtVector._enough,
+// _types.pyx:1408-1411, strict '>') and consider == 1.  From a node a, a
+// neighbour b that is also a node joins a's cluster when the two lists
+// share at least similarity_cutoff members
+// (SimilarityCheckerExtScreensorted._check, _types.pyx:2654-2706: c == 0
+// passes, otherwise count common members until c).  Because the neighbour
+// relation of a metric is symmetric and the check is symmetric in (a, b),
+// the set labelled by one BFS is exactly one connected component of the
+// graph {nodes, accepted edges}, and labels are handed out in the order of
+// each component's lowest point index (the BFS seeds are visited in index
+// order and a seed is always the lowest unvisited node of its component).
+//
+// GB300 form:
+//   1. node flags;
+//   2. one warp per node a walks its neighbours b > a.  An edge is checked
+//      only if find(a) != find(b) at that moment: edges inside an already
+//      joined set cannot change the components, so skipping them is exact.
+//      The check streams N(b) through the warp, each lane binary-searching
+//      one member in N(a) (held in shared memory), and stops as soon as the
+//      count reaches the cutoff or can no longer reach it.  Accepted edges
+//      are joined with a lock-free union-find (CAS on roots, path halving);
+//   3. per component, the minimum point index; ranks of those minima give
+//      the labels (current_start + rank), written in point order.
+#include <climits>
+
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace cnn {
+
+namespace {
+
+constexpr int kCheckWarps = 8;
+constexpr int kListCap = 1024;  // members of N(a) kept in shared memory per warp
+
+__device__ __forceinline__ int32_t uf_find(int32_t *parent, int32_t x) {
+    int32_t cur = x;
+    int32_t next = *(volatile int32_t *)&parent[cur];
+    while (next != cur) {
+        int32_t nn = *(volatile int32_t *)&parent[next];
+        if (nn != next) *(volatile int32_t *)&parent[cur] = nn;  // path halving
+        cur = next;
+        next = nn;
+    }
+    return cur;
+}
+
+// Join the sets of a and b; the smaller root index becomes the root.
+// Lock-free: a failed CAS means another thread changed that root first.
+__device__ __forceinline__ void uf_unite(int32_t *parent, int32_t a, int32_t b) {
+    for (;;) {
+        a = uf_find(parent, a);
+        b = uf_find(parent, b);
+        if (a == b) return;
+        if (a > b) { int32_t t = a; a = b; b = t; }
+        if (atomicCAS(&parent[b], b, a) == b) return;
+    }
+}
+
+__device__ __forceinline__ bool bsearch_contains(const int32_t *A, int32_t la, int32_t v) {
+    int32_t lo = 0, hi = la;
+    while (lo < hi) {
+        int32_t mid = (lo + hi) >> 1;
+        if (A[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    return lo < la && A[lo] == v;
+}
+
+// Warp-cooperative: does |A & B| reach `needed` (> 0)?  A and B ascending.
+__device__ __forceinline__ bool warp_shares_at_least(const int32_t *A, int32_t la, const int32_t *__restrict__ B,
+                                                     int32_t lb, int32_t needed, int lane) {
+    if (la < needed || lb < needed) return false;
+    // members of B outside [A[0], A[la-1]] cannot match
+    const int32_t amin = A[0], amax = A[la - 1];
+    int32_t count = 0;
+    for (int32_t k0 = 0; k0 < lb; k0 += 32) {
+        const int32_t k = k0 + lane;
+        bool found = false;
+        if (k < lb) {
+            const int32_t v = B[k];
+            if (v >= amin && v <= amax) found = bsearch_contains(A, la, v);
+        }
+        count += __popc(__ballot_sync(0xffffffffu, found));
+        if (count >= needed) return true;
+        const int32_t remaining = lb - (k0 + 32);
+        if (count + (remaining > 0 ? remaining : 0) < needed) return false;
+    }
+    return false;
+}
+
+__global__ void node_kernel(const int32_t *__restrict__ deg, const int32_t *__restrict__ perm,
+                            const uint8_t *__restrict__ consider, int64_t n, int64_t n_member_cutoff,
+                            uint8_t *__restrict__ node, int32_t *__restrict__ parent,
+                            int32_t *__restrict__ comp_min, unsigned long long *__restrict__ counters) {
+    unsigned long long local = 0;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        const bool is_node = (int64_t)deg[p] > n_member_cutoff && consider[perm[p]] != 0;
+        node[p] = is_node ? 1 : 0;
+        parent[p] = (int32_t)p;
+        comp_min[p] = INT_MAX;
+        local += is_node;
+    }
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(&counters[4], local);
+}
+
+__global__ void __launch_bounds__(kCheckWarps * 32) check_union_kernel(
+    int64_t n, const int64_t *__restrict__ row_off, const int32_t *__restrict__ cols,
+    const uint8_t *__restrict__ node, int32_t *__restrict__ parent, int32_t needed,
+    unsigned long long *__restrict__ counters) {
+    __shared__ int32_t s_list[kCheckWarps][kListCap];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t a64 = (int64_t)blockIdx.x * kCheckWarps + wid;
+    if (a64 >= n) return;
+    const int32_t a = (int32_t)a64;
+    if (!node[a]) return;
+    const int64_t s = row_off[a], e = row_off[a + 1];
+    const int32_t la = (int32_t)(e - s);
+    const int32_t *A = cols + s;
+    if (la <= kListCap) {
+        for (int32_t k = lane; k < la; k += 32) s_list[wid][k] = A[k];
+        __syncwarp();
+        A = s_list[wid];
+    }
+    unsigned long long n_checks = 0, n_acc = 0;
+    for (int64_t k0 = s; k0 < e; k0 += 32) {
+        const int64_t k = k0 + lane;
+        int32_t b = -1;
+        bool cand = false;
+        if (k < e) {
+            b = cols[k];
+            cand = b > a && node[b];
+        }
+        unsigned mask = __ballot_sync(0xffffffffu, cand);
+        while (mask) {
+            const int src = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const int32_t bb = __shfl_sync(0xffffffffu, b, src);
+            int same = 0;
+            if (lane == 0) same = uf_find(parent, a) == uf_find(parent, bb);
+            same = __shfl_sync(0xffffffffu, same, 0);
+            if (same) continue;
+            bool ok;
+            if (needed <= 0) {
+                ok = needed == 0;
+            } else {
+                const int64_t bs = row_off[bb];
+                const int32_t lb = (int32_t)(row_off[bb + 1] - bs);
+                ok = warp_shares_at_least(A, la, cols + bs, lb, needed, lane);
+                ++n_checks;
+            }
+            if (ok) {
+                if (lane == 0) uf_unite(parent, a, bb);
+                ++n_acc;
+            }
+        }
+    }
+    if (lane == 0 && n_checks) atomicAdd(&counters[5], n_checks);
+    if (lane == 0 && n_acc) atomicAdd(&counters[6], n_acc);
+}
+
+// Full path compression and per-component minimum point index.
+__global__ void root_min_kernel(int64_t n, const uint8_t *__restrict__ node, int32_t *__restrict__ parent,
+                                const int32_t *__restrict__ perm, int32_t *__restrict__ comp_min) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        if (!node[p]) continue;
+        const int32_t r = uf_find(parent, (int32_t)p);
+        atomicMin(&comp_min[r], perm[p]);
+    }
+}
+
+__global__ void root_store_kernel(int64_t n, const uint8_t *__restrict__ node, int32_t *__restrict__ parent) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        if (!node[p]) continue;
+        parent[p] = uf_find(parent, (int32_t)p);
+    }
+}
+
+__global__ void min_flag_kernel(int64_t n, const uint8_t *__restrict__ node, const int32_t *__restrict__ parent,
+                                const int32_t *__restrict__ comp_min, int32_t *__restrict__ flag) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        if (!node[p]) continue;
+        if (parent[p] == (int32_t)p) flag[comp_min[p]] = 1;
+    }
+}
+
+__global__ void label_kernel(int64_t n, const uint8_t *__restrict__ node, const int32_t *__restrict__ parent,
+                             const int32_t *__restrict__ comp_min, const int32_t *__restrict__ perm,
+                             const int64_t *__restrict__ rank, int64_t current_start, int64_t *__restrict__ labels) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        if (!node[p]) continue;
+        const int32_t m = comp_min[parent[p]];
+        labels[perm[p]] = current_start + rank[m];
+    }
+}
+
+// ---- sort_by_size ---------------------------------------------------------
+__global__ void label_range_kernel(const int64_t *__restrict__ labels, int64_t n, long long *__restrict__ out) {
+    long long lo = LLONG_MAX, hi = LLONG_MIN;
+    unsigned long long nz = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const long long v = labels[i];
+        if (v == 0) continue;
+        lo = v < lo ? v : lo;
+        hi = v > hi ? v : hi;
+        ++nz;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        long long l2 = __shfl_down_sync(0xffffffffu, lo, o);
+        long long h2 = __shfl_down_sync(0xffffffffu, hi, o);
+        nz += __shfl_down_sync(0xffffffffu, nz, o);
+        lo = l2 < lo ? l2 : lo;
+        hi = h2 > hi ? h2 : hi;
+    }
+    if ((threadIdx.x & 31) == 0 && nz) {
+        atomicMin(&out[0], lo);
+        atomicMax(&out[1], hi);
+        atomicAdd((unsigned long long *)&out[2], nz);
+    }
+}
+
+__global__ void init_range_kernel(long long *out) {
+    out[0] = LLONG_MAX;
+    out[1] = LLONG_MIN;
+    out[2] = 0;
+}
+
+__global__ void dense_id_kernel(const int64_t *__restrict__ labels, int64_t n, long long lo, int32_t *__restrict__ ids) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = labels[i];
+        ids[i] = v == 0 ? -1 : (int32_t)(v - lo);
+    }
+}
+
+// Sparse label values: order-preserving 64-bit keys (sign bit flipped).
+__global__ void label_keys_kernel(const int64_t *__restrict__ labels, int64_t n, uint64_t *__restrict__ keys) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        keys[i] = (uint64_t)labels[i] ^ 0x8000000000000000ull;
+}
+
+__global__ void unique_flag_kernel(const uint64_t *__restrict__ keys, int64_t n, int32_t *__restrict__ flag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        flag[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
+}
+
+__global__ void unique_compact_kernel(const uint64_t *__restrict__ keys, const int32_t *__restrict__ flag,
+                                      const int64_t *__restrict__ pos, int64_t n, uint64_t *__restrict__ uniq) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (flag[i]) uniq[pos[i]] = keys[i];
+}
+
+__global__ void sparse_id_kernel(const int64_t *__restrict__ labels, int64_t n, const uint64_t *__restrict__ uniq,
+                                 int64_t nu, int32_t *__restrict__ ids) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = labels[i];
+        if (v == 0) { ids[i] = -1; continue; }
+        const uint64_t key = (uint64_t)v ^ 0x8000000000000000ull;
+        int64_t lo = 0, hi = nu;
+        while (lo < hi) {
+            int64_t mid = (lo + hi) >> 1;
+            if (uniq[mid] < key) lo = mid + 1; else hi = mid;
+        }
+        ids[i] = (int32_t)lo;
+    }
+}
+
+__global__ void count_first_kernel(const int32_t *__restrict__ ids, int64_t n, int32_t *__restrict__ cnt,
+                                   int32_t *__restrict__ first) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t id = ids[i];
+        if (id < 0) continue;
+        atomicAdd(&cnt[id], 1);
+        atomicMin(&first[id], (int32_t)i);
+    }
+}
+
+__global__ void cluster_flag_kernel(const int32_t *__restrict__ cnt, int64_t r, int32_t *__restrict__ flag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < r; i += (int64_t)gridDim.x * blockDim.x)
+        flag[i] = cnt[i] > 0 ? 1 : 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) flag[r] = 0;
+}
+
+// key = (n - size) << bits_n | first: ascending key = size descending, then
+// first occurrence ascending (Counter.most_common's order).
+__global__ void cluster_key_kernel(const int32_t *__restrict__ cnt, const int32_t *__restrict__ first,
+                                   const int64_t *__restrict__ pos, int64_t r, int64_t n, int bits_n,
+                                   uint64_t *__restrict__ keys) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < r; i += (int64_t)gridDim.x * blockDim.x) {
+        if (cnt[i] <= 0) continue;
+        keys[pos[i]] = ((uint64_t)(n - cnt[i]) << bits_n) | (uint64_t)first[i];
+    }
+}
+
+__global__ void new_label_kernel(const uint64_t *__restrict__ keys, int64_t k, int64_t n, int bits_n,
+                                 const int32_t *__restrict__ ids, int64_t member_cutoff, int64_t max_clusters,
+                                 int64_t *__restrict__ newlab) {
+    const uint64_t mask = (1ull << bits_n) - 1;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < k; q += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t key = keys[q];
+        const int64_t first = (int64_t)(key & mask);
+        const int64_t size = n - (int64_t)(key >> bits_n);
+        const int64_t rank = q + 1;  // cluster_count in the reference loop
+        newlab[ids[first]] = (rank > max_clusters) ? 0 : (size >= member_cutoff ? rank : 0);
+    }
+}
+
+__global__ void apply_label_kernel(int64_t *__restrict__ labels, const int32_t *__restrict__ ids, int64_t n,
+                                   const int64_t *__restrict__ newlab) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t id = ids[i];
+        labels[i] = id < 0 ? 0 : newlab[id];
+    }
+}
+
+__global__ void check_lists_kernel(const int32_t *__restrict__ a, int64_t na, const int32_t *__restrict__ b,
+                                   int64_t nb, int64_t c, int32_t *__restrict__ result) {
+    const int lane = threadIdx.x & 31;
+    int32_t r;
+    if (c == 0) r = 1;
+    else if (na == 0 || nb == 0 || c < 0) r = 0;
+    else if (c > na || c > nb) r = 0;
+    else r = warp_shares_at_least(a, (int32_t)na, b, (int32_t)nb, (int32_t)c, lane) ? 1 : 0;
+    if (lane == 0) *result = r;
+}
+
+unsigned blocks_for(int64_t n) { return std::min<unsigned>(grid_for(n, 256), 152u * 16u); }
+
+}  // namespace
+
+int bits_for_fit(int64_t n) {
+    int b = 1;
+    while (b < 62 && (int64_t(1) << b) < n) ++b;
+    return b;
+}
+
+cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff, int64_t current_start,
+                    uint8_t *consider_dev, int64_t *labels_dev) {
+    if (!ctx->have_graph) return ctx->fail(CNN_ERR_STATE, "no neighbour graph: call cnn_build_neighbours first");
+    const int64_t n = ctx->n;
+    cudaStream_t st = ctx->stream;
+    if (n == 0) return CNN_OK;
+    // no list is longer than 2^31-1; any negative cutoff rejects every pair
+    if (similarity_cutoff > INT32_MAX) similarity_cutoff = INT32_MAX;
+    if (similarity_cutoff < -1) similarity_cutoff = -1;
+    CNN_TRY(ctx->ensure(ctx->node, (size_t)n));
+    CNN_TRY(ctx->ensure(ctx->parent, sizeof(int32_t) * (size_t)n));
+    CNN_TRY(ctx->ensure(ctx->comp_min, sizeof(int32_t) * (size_t)n));
+    CNN_TRY(ctx->ensure(ctx->flag, sizeof(int32_t) * (size_t)(n + 1)));
+    CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(int64_t) * (size_t)(n + 1)));
+    unsigned long long *counters = ctx->counters.as<unsigned long long>();
+    CNN_CUDA(ctx, cudaMemsetAsync(counters + 4, 0, 4 * sizeof(unsigned long long), st));
+    uint8_t *node = ctx->node.as<uint8_t>();
+    int32_t *parent = ctx->parent.as<int32_t>();
+    int32_t *comp_min = ctx->comp_min.as<int32_t>();
+    const int32_t *perm = ctx->perm.as<int32_t>();
+
+    stage_begin(ctx, 5);
+    node_kernel<<<blocks_for(n), 256, 0, st>>>(ctx->deg.as<int32_t>(), perm, consider_dev, n, n_member_cutoff,
+                                               node, parent, comp_min, counters);
+    CNN_LAUNCH_CHECK(ctx);
+    stage_end(ctx, 5);
+
+    stage_begin(ctx, 6);
+    check_union_kernel<<<grid_for(n, kCheckWarps), kCheckWarps * 32, 0, st>>>(
+        n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), node, parent, (int32_t)similarity_cutoff,
+        counters);
+    CNN_LAUNCH_CHECK(ctx);
+    stage_end(ctx, 6);
+
+    stage_begin(ctx, 7);
+    int32_t *flag = ctx->flag.as<int32_t>();
+    int64_t *rank = ctx->scratch_a.as<int64_t>();
+    CNN_CUDA(ctx, cudaMemsetAsync(flag, 0, sizeof(int32_t) * (size_t)(n + 1), st));
+    root_min_kernel<<<blocks_for(n), 256, 0, st>>>(n, node, parent, perm, comp_min);
+    CNN_LAUNCH_CHECK(ctx);
+    root_store_kernel<<<blocks_for(n), 256, 0, st>>>(n, node, parent);
+    CNN_LAUNCH_CHECK(ctx);
+    min_flag_kernel<<<blocks_for(n), 256, 0, st>>>(n, node, parent, comp_min, flag);
+    CNN_LAUNCH_CHECK(ctx);
+    CNN_TRY(scan_exclusive_i32_to_i64(ctx, flag, rank, n + 1));
+    label_kernel<<<blocks_for(n), 256, 0, st>>>(n, node, parent, comp_min, perm, rank, current_start, labels_dev);
+    CNN_LAUNCH_CHECK(ctx);
+    // every point with consider == 1 is visited by the reference loop and
+    // left at consider == 0; points already at 0 stay 0
+    CNN_CUDA(ctx, cudaMemsetAsync(consider_dev, 0, (size_t)n, st));
+    stage_end(ctx, 7);
+
+    unsigned long long hc[4] = {0, 0, 0, 0};
+    int64_t k = 0;
+    CNN_CUDA(ctx, cudaMemcpyAsync(hc, counters + 4, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    CNN_CUDA(ctx, cudaMemcpyAsync(&k, rank + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    CNN_CUDA(ctx, cudaStreamSynchronize(st));
+    ctx->stats.n_nodes = (int64_t)hc[0];
+    ctx->stats.n_checks = (int64_t)hc[1];
+    ctx->stats.n_accepted = (int64_t)hc[2];
+    ctx->stats.n_clusters = k;
+    return CNN_OK;
+}
+
+cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64_t member_cutoff,
+                             int64_t max_clusters) {
+    cudaStream_t st = ctx->stream;
+    if (n <= 0) return CNN_OK;
+    if (n > INT32_MAX) return ctx->fail(CNN_ERR_UNSUPPORTED, "more than 2^31-1 labels");
+    stage_begin(ctx, 8);
+    CNN_TRY(ctx->ensure(ctx->io_c, 4 * sizeof(long long)));
+    long long *range = ctx->io_c.as<long long>();
+    init_range_kernel<<<1, 1, 0, st>>>(range);
+    CNN_LAUNCH_CHECK(ctx);
+    label_range_kernel<<<blocks_for(n), 256, 0, st>>>(labels, n, range);
+    CNN_LAUNCH_CHECK(ctx);
+    long long hr[3];
+    CNN_CUDA(ctx, cudaMemcpyAsync(hr, range, sizeof(hr), cudaMemcpyDeviceToHost, st));
+    CNN_CUDA(ctx, cudaStreamSynchronize(st));
+    if (hr[2] == 0) {  // only noise
+        stage_end(ctx, 8);
+        return CNN_OK;
+    }
+    const long long lo = hr[0], hi = hr[1];
+    CNN_TRY(ctx->ensure(ctx->io_a, sizeof(int32_t) * (size_t)n));
+    int32_t *ids = ctx->io_a.as<int32_t>();
+    // dense id space when the label values are compact enough
+    const double span = (double)hi - (double)lo + 1.0;
+    int64_t r;
+    if (span <= 4.0 * (double)n + 1024.0) {
+        r = (int64_t)(hi - lo + 1);
+        dense_id_kernel<<<blocks_for(n), 256, 0, st>>>(labels, n, lo, ids);
+        CNN_LAUNCH_CHECK(ctx);
+    } else {
+        CNN_TRY(ctx->ensure(ctx->io_b, sizeof(uint64_t) * (size_t)n * 2 + 64));
+        uint64_t *keys = ctx->io_b.as<uint64_t>();
+        uint64_t *uniq = keys + n;
+        CNN_TRY(ctx->ensure(ctx->flag, sizeof(int32_t) * (size_t)(n + 1)));
+        CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(int64_t) * (size_t)(n + 1)));
+        label_keys_kernel<<<blocks_for(n), 256, 0, st>>>(labels, n, keys);
+        CNN_LAUNCH_CHECK(ctx);
+        CNN_TRY(radix_sort_u64(ctx, keys, n, 64));
+        int32_t *flag = ctx->flag.as<int32_t>();
+        int64_t *pos = ctx->scratch_a.as<int64_t>();
+        unique_flag_kernel<<<blocks_for(n), 256, 0, st>>>(keys, n, flag);
+        CNN_LAUNCH_CHECK(ctx);
+        CNN_CUDA(ctx, cudaMemsetAsync(flag + n, 0, sizeof(int32_t), st));
+        CNN_TRY(scan_exclusive_i32_to_i64(ctx, flag, pos, n + 1));
+        unique_compact_kernel<<<blocks_for(n), 256, 0, st>>>(keys, flag, pos, n, uniq);
+        CNN_LAUNCH_CHECK(ctx);
+        int64_t nu = 0;
+        CNN_CUDA(ctx, cudaMemcpyAsync(&nu, pos + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CNN_CUDA(ctx, cudaStreamSynchronize(st));
+        sparse_id_kernel<<<blocks_for(n), 256, 0, st>>>(labels, n, uniq, nu, ids);
+        CNN_LAUNCH_CHECK(ctx);
+        r = nu;
+    }
+    // per id: size and first occurrence
+    CNN_TRY(ctx->ensure(ctx->scratch_b, sizeof(int32_t) * (size_t)(2 * r + 2)));
+    int32_t *cnt = ctx->scratch_b.as<int32_t>();
+    int32_t *first = cnt + r;
+    CNN_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (size_t)r, st));
+    CNN_TRY(fill_i32(ctx, first, r, INT32_MAX));
+    count_first_kernel<<<blocks_for(n), 256, 0, st>>>(ids, n, cnt, first);
+    CNN_LAUNCH_CHECK(ctx);
+    CNN_TRY(ctx->ensure(ctx->scratch_d, sizeof(int32_t) * (size_t)(r + 1) + sizeof(int64_t) * (size_t)(r + 1) + 64));
+    int32_t *cflag = ctx->scratch_d.as<int32_t>();
+    int64_t *cpos = reinterpret_cast<int64_t *>((reinterpret_cast<uintptr_t>(cflag + r + 1) + 15) & ~uintptr_t(15));
+    cluster_flag_kernel<<<blocks_for(r + 1), 256, 0, st>>>(cnt, r, cflag);
+    CNN_LAUNCH_CHECK(ctx);
+    CNN_TRY(scan_exclusive_i32_to_i64(ctx, cflag, cpos, r + 1));
+    int64_t k = 0;
+    CNN_CUDA(ctx, cudaMemcpyAsync(&k, cpos + r, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    CNN_CUDA(ctx, cudaStreamSynchronize(st));
+    const int bits_n = bits_for_fit(n);
+    CNN_TRY(ctx->ensure(ctx->io_b, sizeof(uint64_t) * (size_t)(k + 1) + sizeof(int64_t) * (size_t)(r + 1) + 64));
+    uint64_t *ckeys = ctx->io_b.as<uint64_t>();
+    int64_t *newlab = reinterpret_cast<int64_t *>(ckeys + k + 1);
+    cluster_key_kernel<<<blocks_for(r), 256, 0, st>>>(cnt, first, cpos, r, n, bits_n, ckeys);
+    CNN_LAUNCH_CHECK(ctx);
+    CNN_TRY(radix_sort_u64(ctx, ckeys, k, bits_n + bits_for_fit(n + 1)));
+    const int64_t maxc = max_clusters < 0 ? k : max_clusters;
+    new_label_kernel<<<blocks_for(k), 256, 0, st>>>(ckeys, k, n, bits_n, ids, member_cutoff, maxc, newlab);
+    CNN_LAUNCH_CHECK(ctx);
+    apply_label_kernel<<<blocks_for(n), 256, 0, st>>>(labels, ids, n, newlab);
+    CNN_LAUNCH_CHECK(ctx);
+    stage_end(ctx, 8);
+    return CNN_OK;
+}
+
+cnn_status check_lists_impl(cnn_context *ctx, const int32_t *a, int64_t na, const int32_t *b, int64_t nb,
+                            int64_t c, int32_t *result_dev) {
+    if (na > INT32_MAX || nb > INT32_MAX) return ctx->fail(CNN_ERR_UNSUPPORTED, "list longer than 2^31-1");
+    check_lists_kernel<<<1, 32, 0, ctx->stream>>>(a, na, b, nb, c, result_dev);
+    CNN_LAUNCH_CHECK(ctx);
+    return CNN_OK;
+}
+
+}  // namespace cnn

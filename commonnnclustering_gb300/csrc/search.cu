@@ -1,0 +1,688 @@
+// search.cu -- radius neighbour search producing sorted CSR neighbourhoods.
+//
+// Reference: NeighboursGetterExtBruteForce._get (src/cnnclustering/
+// _types.pyx:1692-1710) keeps every i with distance(p, i) <= radius_cutoff,
+// distance from MetricExtEuclideanReduced._calc_distance (:2253-2267):
+// a float64 sum of (a-b)^2 over dimensions 0..d-1 starting from 0.0.  The
+// neighbour SET is fixed by that predicate; the kernels here only change
+// which pairs are looked at and how cheaply obvious ones are decided:
+//
+//  * Cell grid (d <= 3).  Points are bucketed into cubic cells of edge
+//    h >= R (R = search radius) and ordered by cell id (x fastest).  A
+//    point's candidates are the 3x3x3 cells around its own; for a fixed
+//    (dy, dz) the three x-cells are contiguous, so candidates form 9 runs of
+//    consecutive internal indices, visited in increasing order.  Rows come
+//    out ascending in internal index without any sort.
+//  * Tiled all-pairs (any d).  Candidate tiles of 32 points are staged in
+//    shared memory; each warp tests its query against the tile.
+//
+// Every candidate is first tested in float32 on coordinates shifted to the
+// bounding-box minimum.  A host-computed error bound gives a band around
+// the cutoff; only pairs inside it are recomputed in float64 with exactly
+// the reference's operation order (explicit __dsub_rn/__dmul_rn/__dadd_rn
+// or __fma_rn, so the compiler cannot re-contract them).  Outside the band
+// the float32 decision is provably the float64 one.
+//
+// Internal index space: the grid path stores the graph in cell order
+// (perm: internal -> point index).  Intersections and connected
+// components are invariant under that relabelling; export to point order
+// happens only on request (cnn_get_neighbours).
+#include <math.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+
+namespace cnn {
+
+namespace {
+
+struct SearchParams {
+    double rc;        // radius_cutoff as the getter compares it
+    int metric;       // cnn_metric
+    int fpmode;       // cnn_fpmode
+    float thr_in;     // sf <= thr_in  -> neighbour
+    float thr_out;    // sf >  thr_out -> not a neighbour; else float64
+};
+
+// Exact float64 predicate in the reference's operation order.
+__device__ __forceinline__ bool exact_in_radius(const double *__restrict__ xa, const double *__restrict__ xb,
+                                                int d, const SearchParams &sp) {
+    double s = 0.0;
+    if (sp.fpmode == CNN_FP_FUSED) {
+        for (int k = 0; k < d; ++k) {
+            double t = __dsub_rn(xa[k], xb[k]);
+            s = __fma_rn(t, t, s);
+        }
+    } else {
+        for (int k = 0; k < d; ++k) {
+            double t = __dsub_rn(xa[k], xb[k]);
+            s = __dadd_rn(s, __dmul_rn(t, t));
+        }
+    }
+    if (sp.metric == CNN_METRIC_EUCLIDEAN) s = __dsqrt_rn(s);
+    return s <= sp.rc;
+}
+
+constexpr int kMaxGridDim = 3;
+
+// General-d extents: per dimension min/max of finite rows (for the float32
+// error bound of the all-pairs path).  part: [blocks][2*d + 1].
+__global__ void extent_partial_kernel(const double *__restrict__ x, int64_t n, int d,
+                                      double *__restrict__ part) {
+    // one block per (dimension chunk): thread-strided over rows, dimension k
+    const int k = blockIdx.y;
+    double lo = INFINITY, hi = -INFINITY, bad = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double v = x[i * d + k];
+        if (!isfinite(v)) { bad += 1; continue; }
+        lo = fmin(lo, v);
+        hi = fmax(hi, v);
+    }
+    __shared__ double s[3][256];
+    s[0][threadIdx.x] = lo; s[1][threadIdx.x] = hi; s[2][threadIdx.x] = bad;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            s[0][threadIdx.x] = fmin(s[0][threadIdx.x], s[0][threadIdx.x + w]);
+            s[1][threadIdx.x] = fmax(s[1][threadIdx.x], s[1][threadIdx.x + w]);
+            s[2][threadIdx.x] += s[2][threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double *o = part + ((int64_t)blockIdx.x * d + k) * 3;
+        o[0] = s[0][0]; o[1] = s[1][0]; o[2] = s[2][0];
+    }
+}
+
+// ---- grid construction ---------------------------------------------------
+struct GridGeom {
+    double lo[3];
+    double h;
+    int32_t g[3];      // cells per dimension (1 for unused dimensions)
+    int64_t ncells;    // g0*g1*g2; bucket ncells holds non-finite points
+};
+
+__device__ __forceinline__ int32_t cell_coord(double v, double lo, double h, int32_t g) {
+    double c = floor(__ddiv_rn(__dsub_rn(v, lo), h));
+    if (!(c >= 0.0)) c = 0.0;
+    if (c > (double)(g - 1)) c = (double)(g - 1);
+    return (int32_t)c;
+}
+
+__global__ void cell_assign_kernel(const double *__restrict__ x, int64_t n, int d, GridGeom geo,
+                                   int32_t *__restrict__ cell_of, int32_t *__restrict__ cell_count) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        bool fin = true;
+        for (int k = 0; k < d; ++k) fin = fin && isfinite(x[i * d + k]);
+        int64_t id;
+        if (!fin) {
+            id = geo.ncells;
+        } else {
+            int32_t c[3] = {0, 0, 0};
+            for (int k = 0; k < d; ++k) c[k] = cell_coord(x[i * d + k], geo.lo[k], geo.h, geo.g[k]);
+            id = (int64_t)c[0] + (int64_t)geo.g[0] * ((int64_t)c[1] + (int64_t)geo.g[1] * c[2]);
+        }
+        cell_of[i] = (int32_t)id;
+        atomicAdd(&cell_count[id], 1);
+    }
+}
+
+// Sort key: cell id in the high bits, point index in the low bits, so the
+// permutation (cell order, ties by point index) is deterministic.
+__global__ void cell_key_kernel(const int32_t *__restrict__ cell_of, int64_t n, int bits_n,
+                                uint64_t *__restrict__ keys) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        keys[i] = ((uint64_t)(uint32_t)cell_of[i] << bits_n) | (uint64_t)i;
+}
+
+__global__ void perm_gather_kernel(const uint64_t *__restrict__ keys, int64_t n, int bits_n,
+                                   const double *__restrict__ x, int d, GridGeom geo,
+                                   int32_t *__restrict__ perm, int32_t *__restrict__ inv,
+                                   float4 *__restrict__ xf4) {
+    const uint64_t mask = (bits_n >= 64) ? ~0ull : ((1ull << bits_n) - 1);
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        int32_t i = (int32_t)(keys[p] & mask);
+        perm[p] = i;
+        inv[i] = (int32_t)p;
+        float v[3] = {0.f, 0.f, 0.f};
+        for (int k = 0; k < d; ++k) v[k] = (float)__dsub_rn(x[(int64_t)i * d + k], geo.lo[k]);
+        xf4[p] = make_float4(v[0], v[1], v[2], 0.f);
+    }
+}
+
+// ---- grid search: one warp per query, lanes over 32 consecutive candidates
+template <bool kFill>
+__global__ void __launch_bounds__(256) grid_search_kernel(
+    const double *__restrict__ x, int d, int64_t n, GridGeom geo, SearchParams sp,
+    const int32_t *__restrict__ perm, const int32_t *__restrict__ cell_of,
+    const int64_t *__restrict__ cell_start, const float4 *__restrict__ xf4,
+    int32_t *__restrict__ deg, const int64_t *__restrict__ row_off, int32_t *__restrict__ cols,
+    unsigned long long *__restrict__ counters) {
+    const int lane = threadIdx.x & 31;
+    const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (p >= n) return;
+    const int32_t i = perm[p];
+    const int32_t cid = cell_of[i];
+    if (cid >= geo.ncells) {  // non-finite coordinates: no neighbours at all
+        if (!kFill && lane == 0) deg[p] = 0;
+        return;
+    }
+    const int32_t cx = cid % geo.g[0];
+    const int32_t cy = (cid / geo.g[0]) % geo.g[1];
+    const int32_t cz = cid / (geo.g[0] * geo.g[1]);
+    const float4 q = xf4[p];
+    double xq[3] = {0.0, 0.0, 0.0};
+    for (int k = 0; k < d; ++k) xq[k] = x[(int64_t)i * d + k];
+    const unsigned lt = (1u << lane) - 1u;
+    int64_t w = kFill ? row_off[p] : 0;
+    int64_t cnt = 0;
+    unsigned long long n_exact = 0, n_cand = 0;
+    const int32_t xlo = cx > 0 ? cx - 1 : 0;
+    const int32_t xhi = cx + 1 < geo.g[0] ? cx + 1 : geo.g[0] - 1;
+    for (int dz = -1; dz <= 1; ++dz) {
+        const int32_t z = cz + dz;
+        if (z < 0 || z >= geo.g[2]) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int32_t y = cy + dy;
+            if (y < 0 || y >= geo.g[1]) continue;
+            const int64_t row = (int64_t)geo.g[0] * ((int64_t)y + (int64_t)geo.g[1] * z);
+            const int64_t rs = cell_start[row + xlo];
+            const int64_t re = cell_start[row + xhi + 1];
+            n_cand += (unsigned long long)(re - rs);
+            for (int64_t j0 = rs; j0 < re; j0 += 32) {
+                const int64_t j = j0 + lane;
+                bool in = false;
+                if (j < re) {
+                    const float4 c = __ldg(&xf4[j]);
+                    const float ex = q.x - c.x, ey = q.y - c.y, ez = q.z - c.z;
+                    const float sf = ex * ex + ey * ey + ez * ez;
+                    if (sf <= sp.thr_in) {
+                        in = true;
+                    } else if (sf <= sp.thr_out) {
+                        double xb[3] = {0.0, 0.0, 0.0};
+                        const int32_t jj = perm[j];
+                        for (int k = 0; k < d; ++k) xb[k] = x[(int64_t)jj * d + k];
+                        in = exact_in_radius(xq, xb, d, sp);
+                        ++n_exact;
+                    }
+                }
+                const unsigned hit = __ballot_sync(0xffffffffu, in);
+                if (kFill && in) cols[w + cnt + __popc(hit & lt)] = (int32_t)j;
+                cnt += __popc(hit);
+            }
+        }
+    }
+    if (!kFill) {
+        if (lane == 0) {
+            deg[p] = (int32_t)cnt;
+            atomicAdd(&counters[1], n_cand);
+        }
+        // float64 rechecks: summed over lanes
+        for (int o = 16; o > 0; o >>= 1) n_exact += __shfl_down_sync(0xffffffffu, n_exact, o);
+        if (lane == 0 && n_exact) atomicAdd(&counters[0], n_exact);
+    }
+}
+
+// ---- tiled all-pairs search (any d) -----------------------------------------
+constexpr int kTileWarps = 8;
+constexpr int kTileCand = 32;
+
+template <bool kFill>
+__global__ void __launch_bounds__(kTileWarps * 32) tile_search_kernel(
+    const double *__restrict__ x, const float *__restrict__ xf, int d, int64_t n, SearchParams sp,
+    int32_t *__restrict__ deg, const int64_t *__restrict__ row_off, int32_t *__restrict__ cols,
+    unsigned long long *__restrict__ counters) {
+    extern __shared__ float smem[];
+    const int ds = d + 1;                      // odd stride: conflict-free rows
+    float *cand = smem;                        // [kTileCand][ds]
+    float *qry = smem + kTileCand * ds;        // [kTileWarps][ds]
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t p = (int64_t)blockIdx.x * kTileWarps + wid;
+    const bool active = p < n;
+    for (int k = lane; k < d; k += 32) qry[wid * ds + k] = active ? xf[p * d + k] : 0.f;
+    const unsigned lt = (1u << lane) - 1u;
+    int64_t w = (kFill && active) ? row_off[p] : 0;
+    int64_t cnt = 0;
+    unsigned long long n_exact = 0;
+    for (int64_t j0 = 0; j0 < n; j0 += kTileCand) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < kTileCand * d; e += blockDim.x) {
+            int r = e / d, k = e - r * d;
+            int64_t j = j0 + r;
+            cand[r * ds + k] = j < n ? xf[j * d + k] : 0.f;
+        }
+        __syncthreads();
+        const int64_t j = j0 + lane;
+        bool in = false;
+        if (active && j < n) {
+            float sf = 0.f;
+            const float *cr = cand + lane * ds;
+            const float *qr = qry + wid * ds;
+            for (int k = 0; k < d; ++k) {
+                float t = qr[k] - cr[k];
+                sf = fmaf(t, t, sf);
+            }
+            if (sf <= sp.thr_in) {
+                in = true;
+            } else if (!(sf > sp.thr_out)) {   // also catches NaN (non-finite candidate)
+                in = exact_in_radius(x + p * d, x + j * d, d, sp);
+                ++n_exact;
+            }
+        }
+        const unsigned hit = __ballot_sync(0xffffffffu, in);
+        if (kFill && in) cols[w + cnt + __popc(hit & lt)] = (int32_t)j;
+        cnt += __popc(hit);
+    }
+    if (!kFill) {
+        if (active && lane == 0) deg[p] = (int32_t)cnt;
+        for (int o = 16; o > 0; o >>= 1) n_exact += __shfl_down_sync(0xffffffffu, n_exact, o);
+        if (lane == 0 && n_exact) atomicAdd(&counters[0], n_exact);
+        if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&counters[1], (unsigned long long)n * (unsigned long long)n);
+    }
+}
+
+__global__ void to_f32_kernel(const double *__restrict__ x, int64_t n, int d, const double *__restrict__ lo,
+                              float *__restrict__ xf) {
+    const int64_t total = n * d;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        int k = (int)(e % d);
+        double v = x[e];
+        xf[e] = isfinite(v) ? (float)__dsub_rn(v, lo[k]) : __int_as_float(0x7fc00000);
+    }
+}
+
+__global__ void set_last_zero_kernel(int32_t *deg, int64_t n) { deg[n] = 0; }
+
+// ---- export / import ----------------------------------------------------------
+__global__ void export_keys_kernel(const int64_t *__restrict__ row_off, const int32_t *__restrict__ cols,
+                                   const int32_t *__restrict__ perm, int64_t n, int bits_n,
+                                   uint64_t *__restrict__ keys) {
+    const int lane = threadIdx.x & 31;
+    const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (p >= n) return;
+    const uint64_t r = (uint64_t)(uint32_t)perm[p] << bits_n;
+    for (int64_t e = row_off[p] + lane; e < row_off[p + 1]; e += 32)
+        keys[e] = r | (uint64_t)(uint32_t)perm[cols[e]];
+}
+
+__global__ void keys_to_cols_kernel(const uint64_t *__restrict__ keys, int64_t nnz, int bits_n,
+                                    int32_t *__restrict__ cols) {
+    const uint64_t mask = (1ull << bits_n) - 1;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x)
+        cols[e] = (int32_t)(keys[e] & mask);
+}
+
+__global__ void deg_by_point_kernel(const int32_t *__restrict__ deg, const int32_t *__restrict__ inv, int64_t n,
+                                    int64_t *__restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = deg[inv[i]];
+    if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = 0;
+}
+
+__global__ void import_keys_kernel(const int64_t *__restrict__ off, const int32_t *__restrict__ idx, int64_t n,
+                                   int bits_n, uint64_t *__restrict__ keys, int32_t *__restrict__ deg,
+                                   unsigned long long *__restrict__ bad) {
+    const int lane = threadIdx.x & 31;
+    const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (p >= n) return;
+    const int64_t s = off[p], e = off[p + 1];
+    if (lane == 0) deg[p] = (int32_t)(e - s);
+    for (int64_t k = s + lane; k < e; k += 32) {
+        int32_t c = idx[k];
+        if (c < 0 || (int64_t)c >= n) { atomicAdd(bad, 1ull); c = 0; }
+        keys[k] = ((uint64_t)p << bits_n) | (uint64_t)(uint32_t)c;
+    }
+}
+
+__global__ void check_offsets_kernel(const int64_t *__restrict__ off, int64_t n, unsigned long long *bad) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        int64_t len = off[p + 1] - off[p];
+        if (len < 0 || len > 0x7fffffff) atomicAdd(bad, 1ull);
+    }
+}
+
+int bits_for(int64_t n) {
+    int b = 1;
+    while (b < 62 && (int64_t(1) << b) < n) ++b;
+    return b;
+}
+
+// Float32 prefilter thresholds.  ext[k] = max |x_k - lo_k| over finite
+// points.  For a pair with true squared distance D <= 4 R^2 the float32
+// value sf differs from D by at most err (derivation in the comments);
+// sf <= rc2 - err - margin then implies the float64 s <= rc2 and
+// sf > rc2 + err + margin implies s > rc2.  Pairs with D > 4 R^2 have
+// sf > rc2 + err + margin whenever the per-coordinate error is below
+// R/1000, which is required for the filter to be used at all.
+bool filter_thresholds(const std::vector<double> &ext, double R, double rc2, float *thr_in,
+                       float *thr_out, double *band) {
+    const double u32 = ldexp(1.0, -24), u64 = ldexp(1.0, -53);
+    const int d = (int)ext.size();
+    double emax = 0;
+    for (double e : ext) emax = std::max(emax, e);
+    if (!(R > 1e-30) || !(R < 1e30) || !isfinite(emax)) return false;
+    // conversion error of one coordinate: rounding of (x - lo) in float64,
+    // then to float32
+    double err = 0;
+    for (int k = 0; k < d; ++k) {
+        double delta = ext[k] * (u32 + 2 * u64);
+        if (delta > 1e-3 * R) return false;
+        // |dx - D_k| <= 2 delta + u32 (|D_k| + 2 delta) with |D_k| <= 2R
+        double eta = 2 * delta + u32 * (2 * R + 2 * delta);
+        err += eta * (4 * R + eta);
+    }
+    // rounding of the float32 squares and sum (fma chain): gamma_{d+1}
+    double gam = (d + 2) * u32 / (1 - (d + 2) * u32);
+    err += gam * (4 * R * R) * 1.0 + gam * err;
+    // float64 result vs exact sum, and the sqrt-metric boundary: a few ulps
+    double margin = 8 * (d + 2) * u64 * rc2 + 1e-300;
+    double b = 2 * (err + margin);          // safety factor 2
+    if (!(b < 0.25 * rc2)) return false;
+    double tin = rc2 - b, tout = rc2 + b;
+    float fin = (float)tin, fout = (float)tout;
+    if ((double)fin > tin) fin = nextafterf(fin, -INFINITY);
+    if ((double)fout < tout) fout = nextafterf(fout, INFINITY);
+    if (!(fin > 0.f)) fin = -1.f;  // never "certainly in" by float32
+    *thr_in = fin;
+    *thr_out = fout;
+    *band = b;
+    return true;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode) {
+    const int64_t n = ctx->n;
+    const int d = ctx->d;
+    cudaStream_t st = ctx->stream;
+    ctx->have_graph = false;
+    ctx->stats = cnn_stats{};
+    ctx->stats.n_points = n;
+    CNN_TRY(ctx->ensure(ctx->counters, 16 * sizeof(unsigned long long)));
+    CNN_CUDA(ctx, cudaMemsetAsync(ctx->counters.ptr, 0, 16 * sizeof(unsigned long long), st));
+    CNN_TRY(ctx->ensure(ctx->deg, sizeof(int32_t) * (size_t)(n + 1)));
+    CNN_TRY(ctx->ensure(ctx->row_off, sizeof(int64_t) * (size_t)(n + 1)));
+    CNN_TRY(ctx->ensure(ctx->perm, sizeof(int32_t) * (size_t)(n > 0 ? n : 1)));
+    CNN_TRY(ctx->ensure(ctx->inv, sizeof(int32_t) * (size_t)(n > 0 ? n : 1)));
+
+    SearchParams sp;
+    sp.rc = radius_cutoff;
+    sp.metric = metric;
+    sp.fpmode = fpmode;
+    sp.thr_in = -1.f;
+    sp.thr_out = INFINITY;
+
+    if (n == 0) {
+        CNN_CUDA(ctx, cudaMemsetAsync(ctx->row_off.ptr, 0, sizeof(int64_t), st));
+        ctx->nnz = 0;
+        ctx->identity_perm = true;
+        ctx->have_graph = true;
+        return CNN_OK;
+    }
+
+    // search radius R in coordinate units.  A NaN or negative cutoff admits
+    // no pair; +inf admits every pair whose distance is not NaN, which only
+    // the all-pairs search with every pair decided in float64 can express.
+    double R = metric == CNN_METRIC_EUCLIDEAN ? radius_cutoff : sqrt(radius_cutoff);
+    const bool radius_ok = radius_cutoff >= 0.0 && isfinite(radius_cutoff);
+    const bool radius_inf = radius_cutoff == INFINITY;
+
+    stage_begin(ctx, 0);
+    // ---- extents of finite points
+    std::vector<double> lo(d), hi(d);
+    int64_t n_bad = 0;
+    {
+        const int blocks = (int)std::min<int64_t>(256, (n + 255) / 256);
+        CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(double) * (size_t)blocks * (size_t)d * 3 + 64));
+        extent_partial_kernel<<<dim3(blocks, d), 256, 0, st>>>(ctx->x, n, d, ctx->scratch_a.as<double>());
+        CNN_LAUNCH_CHECK(ctx);
+        std::vector<double> part((size_t)blocks * d * 3);
+        CNN_CUDA(ctx, cudaMemcpyAsync(part.data(), ctx->scratch_a.ptr, sizeof(double) * part.size(),
+                                      cudaMemcpyDeviceToHost, st));
+        CNN_CUDA(ctx, cudaStreamSynchronize(st));
+        for (int k = 0; k < d; ++k) { lo[k] = INFINITY; hi[k] = -INFINITY; }
+        double bad0 = 0;
+        for (int b = 0; b < blocks; ++b)
+            for (int k = 0; k < d; ++k) {
+                const double *o = &part[((size_t)b * d + k) * 3];
+                lo[k] = std::min(lo[k], o[0]);
+                hi[k] = std::max(hi[k], o[1]);
+                if (k == 0) bad0 += o[2];
+            }
+        n_bad = (int64_t)bad0;  // rows with a non-finite first coordinate (diagnostic)
+        for (int k = 0; k < d; ++k)
+            if (!(lo[k] <= hi[k])) { lo[k] = 0; hi[k] = 0; }  // no finite point
+    }
+    (void)n_bad;
+    stage_end(ctx, 0);
+
+    std::vector<double> ext(d);
+    for (int k = 0; k < d; ++k) ext[k] = std::max(std::fabs(hi[k] - lo[k]), 0.0);
+    double band = 0;
+    bool filt = false;
+    if (radius_ok && (metric == CNN_METRIC_EUCLIDEAN_REDUCED || metric == CNN_METRIC_EUCLIDEAN)) {
+        const double rc2 = metric == CNN_METRIC_EUCLIDEAN ? radius_cutoff * radius_cutoff : radius_cutoff;
+        filt = filter_thresholds(ext, R, rc2, &sp.thr_in, &sp.thr_out, &band);
+    }
+    if (!radius_ok && !radius_inf) {
+        // nothing satisfies `s <= NaN`; a negative cutoff admits nothing
+        sp.thr_in = -1.f;
+        sp.thr_out = -1.f;  // everything is "certainly out"
+        filt = true;
+    }
+    ctx->stats.filter_enabled = filt ? 1 : 0;
+    ctx->stats.filter_band = band;
+
+    // ---- choose the search
+    GridGeom geo{};
+    bool use_grid = d <= 3 && radius_ok && R > 0 && isfinite(R);
+    if (use_grid) {
+        double h = R * (1.0 + 1e-6);
+        const double max_cells = std::max<double>(4.0 * (double)n, 4096.0);
+        for (int attempt = 0; attempt < 200; ++attempt) {
+            double cells = 1;
+            for (int k = 0; k < 3; ++k) {
+                double g = k < d ? floor(ext[k] / h) + 1.0 : 1.0;
+                geo.g[k] = (int32_t)std::min(g, 2.0e9);
+                cells *= g;
+            }
+            if (cells <= max_cells && cells < 2.0e9) break;
+            h *= 1.25;
+        }
+        geo.h = h;
+        for (int k = 0; k < 3; ++k) geo.lo[k] = k < d ? lo[k] : 0.0;
+        geo.ncells = (int64_t)geo.g[0] * geo.g[1] * geo.g[2];
+        if (geo.ncells >= 0x7ffffff0LL) use_grid = false;
+    }
+    ctx->stats.search_kind = use_grid ? 1 : 2;
+
+    int32_t *deg = ctx->deg.as<int32_t>();
+    int64_t *row_off = ctx->row_off.as<int64_t>();
+    unsigned long long *counters = ctx->counters.as<unsigned long long>();
+
+    if (use_grid) {
+        stage_begin(ctx, 1);
+        const int bits_n = bits_for(n);
+        CNN_TRY(ctx->ensure(ctx->cell_of, sizeof(int32_t) * (size_t)n));
+        CNN_TRY(ctx->ensure(ctx->cell_start, sizeof(int64_t) * (size_t)(geo.ncells + 2)));
+        CNN_TRY(ctx->ensure(ctx->scratch_b, sizeof(int32_t) * (size_t)(geo.ncells + 2)));
+        CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(uint64_t) * (size_t)n));
+        CNN_TRY(ctx->ensure(ctx->xf4, sizeof(float4) * (size_t)n));
+        int32_t *cell_count = ctx->scratch_b.as<int32_t>();
+        CNN_CUDA(ctx, cudaMemsetAsync(cell_count, 0, sizeof(int32_t) * (size_t)(geo.ncells + 2), st));
+        const unsigned gb = std::min<unsigned>(grid_for(n, 256), 152u * 16u);
+        cell_assign_kernel<<<gb, 256, 0, st>>>(ctx->x, n, d, geo, ctx->cell_of.as<int32_t>(), cell_count);
+        CNN_LAUNCH_CHECK(ctx);
+        CNN_TRY(scan_exclusive_i32_to_i64(ctx, cell_count, ctx->cell_start.as<int64_t>(), geo.ncells + 2));
+        uint64_t *keys = ctx->scratch_a.as<uint64_t>();
+        cell_key_kernel<<<gb, 256, 0, st>>>(ctx->cell_of.as<int32_t>(), n, bits_n, keys);
+        CNN_LAUNCH_CHECK(ctx);
+        CNN_TRY(radix_sort_u64(ctx, keys, n, bits_n + bits_for(geo.ncells + 2)));
+        perm_gather_kernel<<<gb, 256, 0, st>>>(keys, n, bits_n, ctx->x, d, geo, ctx->perm.as<int32_t>(),
+                                                ctx->inv.as<int32_t>(), ctx->xf4.as<float4>());
+        CNN_LAUNCH_CHECK(ctx);
+        stage_end(ctx, 1);
+
+        stage_begin(ctx, 2);
+        const unsigned gq = grid_for(n * 32, 256);
+        grid_search_kernel<false><<<gq, 256, 0, st>>>(ctx->x, d, n, geo, sp, ctx->perm.as<int32_t>(),
+                                                       ctx->cell_of.as<int32_t>(), ctx->cell_start.as<int64_t>(),
+                                                       ctx->xf4.as<float4>(), deg, nullptr, nullptr, counters);
+        CNN_LAUNCH_CHECK(ctx);
+        stage_end(ctx, 2);
+        ctx->identity_perm = false;
+    } else {
+        stage_begin(ctx, 1);
+        CNN_TRY(iota_i32(ctx, ctx->perm.as<int32_t>(), n));
+        CNN_TRY(iota_i32(ctx, ctx->inv.as<int32_t>(), n));
+        CNN_TRY(ctx->ensure(ctx->scratch_b, sizeof(float) * (size_t)n * d));
+        CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(double) * (size_t)d + 64));
+        CNN_CUDA(ctx, cudaMemcpyAsync(ctx->scratch_a.ptr, lo.data(), sizeof(double) * d, cudaMemcpyHostToDevice, st));
+        const unsigned gb = std::min<unsigned>(grid_for(n * d, 256), 152u * 16u);
+        to_f32_kernel<<<gb, 256, 0, st>>>(ctx->x, n, d, ctx->scratch_a.as<double>(), ctx->scratch_b.as<float>());
+        CNN_LAUNCH_CHECK(ctx);
+        stage_end(ctx, 1);
+        if (d > 1024) return ctx->fail(CNN_ERR_UNSUPPORTED, "n_dim > 1024 is not supported");
+        const size_t smem = sizeof(float) * (size_t)(kTileCand + kTileWarps) * (d + 1);
+        CNN_CUDA(ctx, cudaFuncSetAttribute(tile_search_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CNN_CUDA(ctx, cudaFuncSetAttribute(tile_search_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        stage_begin(ctx, 2);
+        const unsigned gq = grid_for(n, kTileWarps);
+        tile_search_kernel<false><<<gq, kTileWarps * 32, smem, st>>>(ctx->x, ctx->scratch_b.as<float>(), d, n, sp, deg,
+                                                                      nullptr, nullptr, counters);
+        CNN_LAUNCH_CHECK(ctx);
+        stage_end(ctx, 2);
+        ctx->identity_perm = true;
+    }
+
+    // ---- offsets
+    stage_begin(ctx, 3);
+    set_last_zero_kernel<<<1, 1, 0, st>>>(deg, n);
+    CNN_LAUNCH_CHECK(ctx);
+    CNN_TRY(scan_exclusive_i32_to_i64(ctx, deg, row_off, n + 1));
+    int64_t nnz = 0;
+    CNN_CUDA(ctx, cudaMemcpyAsync(&nnz, row_off + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    CNN_CUDA(ctx, cudaStreamSynchronize(st));
+    stage_end(ctx, 3);
+    CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1)));
+
+    stage_begin(ctx, 4);
+    if (use_grid) {
+        const unsigned gq = grid_for(n * 32, 256);
+        grid_search_kernel<true><<<gq, 256, 0, st>>>(ctx->x, d, n, geo, sp, ctx->perm.as<int32_t>(),
+                                                      ctx->cell_of.as<int32_t>(), ctx->cell_start.as<int64_t>(),
+                                                      ctx->xf4.as<float4>(), deg, row_off, ctx->cols.as<int32_t>(),
+                                                      counters);
+    } else {
+        const size_t smem = sizeof(float) * (size_t)(kTileCand + kTileWarps) * (d + 1);
+        tile_search_kernel<true><<<grid_for(n, kTileWarps), kTileWarps * 32, smem, st>>>(
+            ctx->x, ctx->scratch_b.as<float>(), d, n, sp, deg, row_off, ctx->cols.as<int32_t>(), counters);
+    }
+    CNN_LAUNCH_CHECK(ctx);
+    stage_end(ctx, 4);
+
+    unsigned long long hc[2] = {0, 0};
+    CNN_CUDA(ctx, cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    CNN_CUDA(ctx, cudaStreamSynchronize(st));
+    ctx->stats.n_exact = (int64_t)hc[0];
+    ctx->stats.n_candidates = (int64_t)hc[1];
+    ctx->stats.n_nonzero = nnz;
+    ctx->nnz = nnz;
+    ctx->have_graph = true;
+    return CNN_OK;
+}
+
+// Graph as CSR in point-index order (device output buffers).
+cnn_status export_neighbours_impl(cnn_context *ctx, int64_t *offsets_dev, int32_t *indices_dev) {
+    const int64_t n = ctx->n, nnz = ctx->nnz;
+    cudaStream_t st = ctx->stream;
+    if (ctx->identity_perm) {
+        CNN_CUDA(ctx, cudaMemcpyAsync(offsets_dev, ctx->row_off.ptr, sizeof(int64_t) * (size_t)(n + 1),
+                                      cudaMemcpyDeviceToDevice, st));
+        if (nnz > 0)
+            CNN_CUDA(ctx, cudaMemcpyAsync(indices_dev, ctx->cols.ptr, sizeof(int32_t) * (size_t)nnz,
+                                          cudaMemcpyDeviceToDevice, st));
+        return CNN_OK;
+    }
+    CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(int64_t) * (size_t)(n + 1)));
+    deg_by_point_kernel<<<std::min<unsigned>(grid_for(n + 1, 256), 4096u), 256, 0, st>>>(
+        ctx->deg.as<int32_t>(), ctx->inv.as<int32_t>(), n, ctx->scratch_a.as<int64_t>());
+    CNN_LAUNCH_CHECK(ctx);
+    CNN_TRY(scan_exclusive_i64(ctx, ctx->scratch_a.as<int64_t>(), offsets_dev, n + 1));
+    if (nnz == 0) return CNN_OK;
+    const int bits_n = bits_for(n);
+    CNN_TRY(ctx->ensure(ctx->scratch_b, sizeof(uint64_t) * (size_t)nnz));
+    uint64_t *keys = ctx->scratch_b.as<uint64_t>();
+    export_keys_kernel<<<grid_for(n * 32, 256), 256, 0, st>>>(ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(),
+                                                              ctx->perm.as<int32_t>(), n, bits_n, keys);
+    CNN_LAUNCH_CHECK(ctx);
+    CNN_TRY(radix_sort_u64(ctx, keys, nnz, 2 * bits_n));
+    keys_to_cols_kernel<<<std::min<unsigned>(grid_for(nnz, 256), 152u * 32u), 256, 0, st>>>(keys, nnz, bits_n,
+                                                                                             indices_dev);
+    CNN_LAUNCH_CHECK(ctx);
+    return CNN_OK;
+}
+
+// Precomputed neighbourhoods: rows sorted on the device, identity order.
+cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev, const int32_t *indices_dev,
+                               int64_t n) {
+    cudaStream_t st = ctx->stream;
+    ctx->have_graph = false;
+    ctx->stats = cnn_stats{};
+    ctx->stats.n_points = n;
+    ctx->n = n;
+    ctx->d = 0;
+    ctx->x = nullptr;
+    CNN_TRY(ctx->ensure(ctx->counters, 16 * sizeof(unsigned long long)));
+    CNN_CUDA(ctx, cudaMemsetAsync(ctx->counters.ptr, 0, 16 * sizeof(unsigned long long), st));
+    CNN_TRY(ctx->ensure(ctx->deg, sizeof(int32_t) * (size_t)(n + 1)));
+    CNN_TRY(ctx->ensure(ctx->row_off, sizeof(int64_t) * (size_t)(n + 1)));
+    CNN_TRY(ctx->ensure(ctx->perm, sizeof(int32_t) * (size_t)(n > 0 ? n : 1)));
+    CNN_TRY(ctx->ensure(ctx->inv, sizeof(int32_t) * (size_t)(n > 0 ? n : 1)));
+    int64_t first = 0, nnz = 0;
+    CNN_CUDA(ctx, cudaMemcpyAsync(&first, offsets_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    CNN_CUDA(ctx, cudaMemcpyAsync(&nnz, offsets_dev + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    CNN_CUDA(ctx, cudaStreamSynchronize(st));
+    if (first != 0 || nnz < 0) return ctx->fail(CNN_ERR_INVALID_ARG, "offsets must start at 0 and not decrease");
+    unsigned long long *counters = ctx->counters.as<unsigned long long>();
+    check_offsets_kernel<<<std::min<unsigned>(grid_for(n, 256), 4096u), 256, 0, st>>>(offsets_dev, n, counters + 2);
+    CNN_LAUNCH_CHECK(ctx);
+    unsigned long long bad = 0;
+    CNN_CUDA(ctx, cudaMemcpyAsync(&bad, counters + 2, sizeof(bad), cudaMemcpyDeviceToHost, st));
+    CNN_CUDA(ctx, cudaStreamSynchronize(st));
+    if (bad) return ctx->fail(CNN_ERR_INVALID_ARG, "offsets must not decrease");
+    CNN_TRY(iota_i32(ctx, ctx->perm.as<int32_t>(), n));
+    CNN_TRY(iota_i32(ctx, ctx->inv.as<int32_t>(), n));
+    CNN_CUDA(ctx, cudaMemcpyAsync(ctx->row_off.ptr, offsets_dev, sizeof(int64_t) * (size_t)(n + 1),
+                                  cudaMemcpyDeviceToDevice, st));
+    CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1)));
+    if (n > 0) {
+        const int bits_n = bits_for(n);
+        CNN_TRY(ctx->ensure(ctx->scratch_b, sizeof(uint64_t) * (size_t)(nnz > 0 ? nnz : 1)));
+        uint64_t *keys = ctx->scratch_b.as<uint64_t>();
+        import_keys_kernel<<<grid_for(n * 32, 256), 256, 0, st>>>(offsets_dev, indices_dev, n, bits_n, keys,
+                                                                  ctx->deg.as<int32_t>(), counters + 3);
+        CNN_LAUNCH_CHECK(ctx);
+        CNN_CUDA(ctx, cudaMemcpyAsync(&bad, counters + 3, sizeof(bad), cudaMemcpyDeviceToHost, st));
+        CNN_CUDA(ctx, cudaStreamSynchronize(st));
+        if (bad) return ctx->fail(CNN_ERR_INVALID_ARG, "neighbour index out of range");
+        if (nnz > 0) {
+            CNN_TRY(radix_sort_u64(ctx, keys, nnz, 2 * bits_n));
+            keys_to_cols_kernel<<<std::min<unsigned>(grid_for(nnz, 256), 152u * 32u), 256, 0, st>>>(
+                keys, nnz, bits_n, ctx->cols.as<int32_t>());
+            CNN_LAUNCH_CHECK(ctx);
+        }
+    }
+    ctx->nnz = nnz;
+    ctx->identity_perm = true;
+    ctx->have_graph = true;
+    ctx->stats.n_nonzero = nnz;
+    ctx->stats.search_kind = 0;
+    return CNN_OK;
+}
+
+}  // namespace cnn

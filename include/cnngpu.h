@@ -1,0 +1,181 @@
+/*
+ * cnngpu.h -- C ABI of the GB300 CommonNN fit library (libcnngpu.so).
+ *
+ * The library replaces the hot path of cnnclustering 0.5.0's
+ * Clustering.fit: radius neighbour search, the common-neighbour similarity
+ * check and the BFS cluster growth, plus Labels.sort_by_size.  All entry
+ * points take plain pointers and sizes; arrays may live on the host or on
+ * the device (cnn_memspace).  Nothing here depends on torch.
+ *
+ * Reference interfaces each entry point stands in for (paths relative to
+ * the reference project root):
+ *
+ *   cnn_set_points        InputDataExtComponentsMemoryview.__cinit__
+ *                           src/cnnclustering/_types.pyx:1040-1048
+ *   cnn_build_neighbours  NeighboursGetterExtBruteForce._get for every point
+ *                           src/cnnclustering/_types.pyx:1692-1710 with
+ *                           MetricExtEuclideanReduced._calc_distance
+ *                           :2253-2267 / MetricExtEuclidean :2173-2187
+ *   cnn_set_neighbours    InputDataExtNeighbourhoodsMemoryview +
+ *                           NeighboursGetterExtLookup._get
+ *                           src/cnnclustering/_types.pyx:1159-1171, 1806-1817
+ *   cnn_get_neighbours    the per-point lists those getters return, as CSR
+ *   cnn_fit               FitterExtBFS._fit (with _enough and _check)
+ *                           src/cnnclustering/_fit.pyx:408-491,
+ *                           _types.pyx:1408-1411, 2580-2610, 2654-2706
+ *   cnn_sort_by_size      Labels.sort_by_size
+ *                           src/cnnclustering/_types.pyx:212-286
+ *   cnn_check_lists       SimilarityCheckerExtScreensorted._check
+ *                           src/cnnclustering/_types.pyx:2654-2706
+ *
+ * Threading: a context is not thread-safe; use one per host thread.  All
+ * device work of a context runs on its stream, in order.  Calls that
+ * return host-visible results synchronise that stream.
+ *
+ * Errors: every call returns a cnn_status; cnn_last_error() gives the
+ * message of the last failure on that context.  No C++ exception crosses
+ * this boundary.
+ */
+#ifndef CNNGPU_H
+#define CNNGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define CNN_API __attribute__((visibility("default")))
+#else
+#define CNN_API
+#endif
+
+#define CNN_ABI_VERSION 1
+
+typedef struct cnn_context cnn_context;
+
+typedef enum cnn_status {
+    CNN_OK = 0,
+    CNN_ERR_INVALID_ARG = 1,
+    CNN_ERR_OOM = 2,
+    CNN_ERR_CUDA = 3,
+    CNN_ERR_TIMEOUT = 4,
+    CNN_ERR_UNSUPPORTED = 5,
+    CNN_ERR_STATE = 6
+} cnn_status;
+
+/* Which distance the getter compares with radius_cutoff. */
+typedef enum cnn_metric {
+    CNN_METRIC_EUCLIDEAN_REDUCED = 0, /* sum of squares <= radius_cutoff (= r*r) */
+    CNN_METRIC_EUCLIDEAN = 1          /* sqrt(sum of squares) <= radius_cutoff (= r) */
+} cnn_metric;
+
+/* How each term of the float64 distance sum is accumulated:
+ * SEPARATE: total = total + (t*t), two roundings (reference built for
+ *           x86-64 without FMA);
+ * FUSED:    total = fma(t, t, total), one rounding (reference built with
+ *           FMA contraction, e.g. GCC's default on aarch64). */
+typedef enum cnn_fpmode {
+    CNN_FP_SEPARATE = 0,
+    CNN_FP_FUSED = 1
+} cnn_fpmode;
+
+typedef enum cnn_dtype {
+    CNN_DTYPE_F64 = 0,
+    CNN_DTYPE_F32 = 1 /* widened to float64 exactly before any compare */
+} cnn_dtype;
+
+typedef enum cnn_memspace {
+    CNN_MEM_HOST = 0,
+    CNN_MEM_DEVICE = 1
+} cnn_memspace;
+
+/* Per-context counters and stage times of the most recent calls.  Times
+ * are milliseconds between CUDA events recorded on the context stream
+ * (0 when timing is off). */
+typedef struct cnn_stats {
+    int64_t n_points;
+    int64_t n_nonzero;        /* neighbour pairs stored (self included) */
+    int64_t n_nodes;          /* core points with consider == 1 */
+    int64_t n_checks;         /* similarity checks executed */
+    int64_t n_accepted;       /* checks that passed */
+    int64_t n_exact;          /* candidate pairs decided in float64 */
+    int64_t n_candidates;     /* candidate pairs tested by the search */
+    int64_t n_clusters;       /* clusters found by the last fit */
+    int32_t search_kind;      /* 1 = cell grid (d <= 3), 2 = tiled all-pairs */
+    int32_t filter_enabled;   /* 1 when the float32 prefilter was usable */
+    double filter_band;       /* half-width of the float64 recheck band on d^2 */
+    float ms_bbox, ms_cells, ms_count, ms_scan, ms_fill;   /* neighbour build */
+    float ms_nodes, ms_check, ms_label;                    /* fit */
+    float ms_sort;                                         /* sort_by_size */
+} cnn_stats;
+
+CNN_API int cnn_abi_version(void);
+
+/* Create a context on `device`.  `stream` is a cudaStream_t (may be NULL:
+ * the context creates its own non-blocking stream). */
+CNN_API cnn_status cnn_create(cnn_context **out, int device, void *stream);
+CNN_API cnn_status cnn_destroy(cnn_context *ctx);
+CNN_API cnn_status cnn_set_stream(cnn_context *ctx, void *stream);
+CNN_API const char *cnn_last_error(const cnn_context *ctx);
+CNN_API cnn_status cnn_set_timing(cnn_context *ctx, int enabled);
+CNN_API cnn_status cnn_get_stats(const cnn_context *ctx, cnn_stats *out);
+
+/* Points, row-major [n_points x n_dim].  Device arrays are used in place
+ * (they must stay alive and unchanged until the next cnn_set_points);
+ * host arrays are copied. */
+CNN_API cnn_status cnn_set_points(cnn_context *ctx, const void *points, cnn_dtype dtype,
+                                  int64_t n_points, int32_t n_dim, cnn_memspace mem);
+
+/* Radius neighbourhoods of every point (self included) for the adjusted
+ * radius_cutoff the reference's getter compares with (r*r for the reduced
+ * metric, r for the Euclidean metric).  The graph stays on the device. */
+CNN_API cnn_status cnn_build_neighbours(cnn_context *ctx, double radius_cutoff,
+                                        cnn_metric metric, cnn_fpmode fpmode);
+
+/* Precomputed neighbourhoods in CSR form (offsets int64[n+1], indices
+ * int32[nnz]); rows are sorted on the device, so any order is accepted.
+ * Replaces the points of the context. */
+CNN_API cnn_status cnn_set_neighbours(cnn_context *ctx, const int64_t *offsets,
+                                      const int32_t *indices, int64_t n_points,
+                                      cnn_memspace mem);
+
+/* Number of stored neighbour pairs of the current graph. */
+CNN_API cnn_status cnn_neighbour_count(cnn_context *ctx, int64_t *nnz);
+
+/* The current graph as CSR in point-index order with ascending rows:
+ * offsets int64[n+1], indices int32[nnz]. */
+CNN_API cnn_status cnn_get_neighbours(cnn_context *ctx, int64_t *offsets, int32_t *indices,
+                                      cnn_memspace mem);
+
+/* Cluster the current graph.  Semantics of FitterExtBFS._fit: points with
+ * more than n_member_cutoff neighbours and consider == 1 are nodes; two
+ * nodes that are neighbours and share at least similarity_cutoff
+ * neighbours are joined; each connected set of nodes gets one label,
+ * numbered from current_start in the order of its lowest point index.
+ * labels[] of nodes and consider[] of every visited point are written in
+ * place as the reference does; other entries are left as they are. */
+CNN_API cnn_status cnn_fit(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
+                           int64_t current_start, uint8_t *consider, int64_t *labels,
+                           cnn_memspace mem);
+
+/* Labels.sort_by_size on labels[n] in place: renumber clusters by size
+ * (descending, ties by first occurrence), zero clusters with fewer than
+ * member_cutoff members and all clusters after the first max_clusters
+ * (max_clusters < 0: no limit).  Label 0 stays 0. */
+CNN_API cnn_status cnn_sort_by_size(cnn_context *ctx, int64_t *labels, int64_t n,
+                                    int64_t member_cutoff, int64_t max_clusters,
+                                    cnn_memspace mem);
+
+/* Similarity check of two ascending member lists: *result = 1 when they
+ * share at least c members (c == 0: always 1; an empty list: 0). */
+CNN_API cnn_status cnn_check_lists(cnn_context *ctx, const int32_t *a, int64_t na,
+                                   const int32_t *b, int64_t nb, int64_t c, int32_t *result,
+                                   cnn_memspace mem);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CNNGPU_H */

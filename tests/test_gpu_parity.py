@@ -1,0 +1,258 @@
+"""GPU parity: the CUDA path against the reference's golden fixtures and
+against the oracle, through the C ABI (libcnngpu.so).
+
+Integer/index results are compared bit-exactly: neighbour lists (CSR),
+labels, consider flags.
+"""
+import numpy as np
+import pytest
+
+from conftest import FIT_CASES, fit_kwargs, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def cnn():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import commonnnclustering_gb300 as cnn
+    return cnn
+
+
+@pytest.fixture(scope="module")
+def oracle():
+    from oracle import cnn_oracle
+    return cnn_oracle
+
+
+def gpu_csr(cnn, x, radius_cutoff, metric=0, fpmode=0):
+    ctx = cnn.Context(0)
+    ctx.set_points(np.ascontiguousarray(x))
+    ctx.build_neighbours(radius_cutoff, metric, fpmode)
+    off, idx = ctx.get_neighbours(x.shape[0])
+    st = ctx.stats()
+    ctx.close()
+    return off, idx, st
+
+
+@pytest.mark.parametrize("name", FIT_CASES)
+def test_golden_neighbourhoods(cnn, name):
+    import hashlib
+    g = load_golden(name)
+    r = float(g["radius_cutoff"])
+    off, idx, _ = gpu_csr(cnn, g["points"], r * r)
+    assert np.array_equal(np.diff(off), g["degrees"])
+    h = hashlib.sha256()
+    h.update(off.astype(np.int64).tobytes())
+    h.update(idx.astype(np.int32).tobytes())
+    assert h.hexdigest() == str(g["csr_sha256"])
+
+
+@pytest.mark.parametrize("name", FIT_CASES)
+def test_golden_fit_labels(cnn, name):
+    g = load_golden(name)
+    kw = fit_kwargs(g)
+    cl = cnn.Clustering(g["points"])
+    cl.fit(float(g["radius_cutoff"]), int(g["cnn_cutoff"]), v=False, **kw)
+    assert np.array_equal(np.asarray(cl.labels), g["labels"])
+
+
+def test_readme_quickstart(cnn):
+    data = [[0, 0], [1, 1], [1, 0], [0, -1], [0.5, -0.5], [2, 1.5], [2.5, -0.5], [4, 2], [4.5, 2.5],
+            [5, -1], [5.5, -0.5], [5.5, -1.5]]
+    cl = cnn.Clustering(data)
+    cl.fit(radius_cutoff=1.5, cnn_cutoff=1, v=False)
+    assert cl.labels.tolist() == [1, 1, 1, 1, 1, 0, 0, 0, 0, 2, 2, 2]
+
+
+def test_golden_euclidean_sqrt_metric(cnn):
+    g = load_golden("euclidean_sqrt.npz")
+    r = float(g["radius_cutoff"])
+    off, idx, _ = gpu_csr(cnn, g["points"], r, metric=1)
+    assert np.array_equal(off, g["offsets"]) and np.array_equal(idx, g["indices"])
+    b = cnn.recipes.Builder("coordinates", **{"fitter.ngetter.dgetter.metric": "euclidean"})
+    cl = cnn.Clustering(g["points"], fitter=b.make_component("fitter"))
+    cl.fit(r, int(g["cnn_cutoff"]), member_cutoff=int(g["member_cutoff"]), v=False)
+    assert np.array_equal(np.asarray(cl.labels), g["labels"])
+
+
+def test_golden_frozen_refit(cnn):
+    g = load_golden("frozen_refit.npz")
+    cl = cnn.Clustering(g["points"])
+    cl.fit(float(g["r1"]), int(g["c1"]), member_cutoff=int(g["m1"]), v=False)
+    assert np.array_equal(np.asarray(cl.labels), g["first_labels"])
+    cl._bundle._labels.meta["frozen"] = True
+    cl._bundle._labels.consider[:] = g["consider"]
+    cl.fit(float(g["r2"]), int(g["c2"]), member_cutoff=int(g["m2"]), v=False)
+    assert np.array_equal(np.asarray(cl.labels), g["second_labels"])
+
+
+def test_golden_sort_by_size(cnn):
+    g = load_golden("sort_by_size.npz")
+    for i in range(int(g["n_cases"])):
+        lab = cnn.Labels(g[f"in_{i}"].copy())
+        mc, mx = int(g["member_cutoff"][i]), int(g["max_clusters"][i])
+        lab.sort_by_size(None if mc < 0 else mc, None if mx < 0 else mx)
+        assert np.array_equal(lab.labels, g[f"out_{i}"]), i
+
+
+def test_golden_check_truth_table(cnn):
+    g = load_golden("check_table.npz")
+    ctx = cnn.default_context(0)
+    pa = pb = 0
+    for k in range(g["c"].shape[0]):
+        a = g["a"][pa:pa + g["len_a"][k]]
+        b = g["b"][pb:pb + g["len_b"][k]]
+        pa += g["len_a"][k]
+        pb += g["len_b"][k]
+        assert ctx.check_lists(a, b, int(g["c"][k])) == bool(g["expected"][k]), k
+
+
+@pytest.mark.parametrize("d", [1, 2, 3, 5, 16, 64])
+@pytest.mark.parametrize("fpmode", [0, 1])
+def test_random_csr_against_oracle(cnn, oracle, d, fpmode):
+    rng = np.random.default_rng(100 + d)
+    n = 3000 if d <= 3 else 1500
+    x = np.vstack([rng.normal(0, 1, size=(n // 2, d)), rng.normal(3, 0.5, size=(n - n // 2, d))])
+    # radius giving ~30 neighbours
+    sub = x[rng.choice(n, 64, replace=False)]
+    dd = np.sort(((sub[:, None, :] - x[None]) ** 2).sum(-1), axis=1)[:, 30]
+    r2 = float(np.median(dd))
+    want = oracle.neighbourhoods(x, r2, fpmode=fpmode, grid=True)
+    off, idx, st = gpu_csr(cnn, x, r2, fpmode=fpmode)
+    assert np.array_equal(off, want[0]) and np.array_equal(idx, want[1])
+
+
+def test_boundary_ties_on_lattice(cnn, oracle):
+    # integer lattice: many squared distances equal r**2 exactly
+    g = np.array([[i, j, k] for i in range(12) for j in range(12) for k in range(12)], dtype=np.float64)
+    for r2 in (1.0, 2.0, 3.0, 4.0):
+        want = oracle.neighbourhoods(g, r2)
+        off, idx, _ = gpu_csr(cnn, g, r2)
+        assert np.array_equal(off, want[0]) and np.array_equal(idx, want[1]), r2
+
+
+def test_nonfinite_points_have_no_neighbours(cnn, oracle):
+    rng = np.random.default_rng(3)
+    x = rng.normal(size=(500, 3))
+    x[7, 1] = np.nan
+    x[11, 0] = np.inf
+    x[12, 0] = np.inf
+    want = oracle.neighbourhoods(x, 0.25, grid=False)
+    off, idx, _ = gpu_csr(cnn, x, 0.25)
+    assert np.array_equal(off, want[0]) and np.array_equal(idx, want[1])
+    assert off[8] - off[7] == 0
+
+
+def test_degenerate_radius(cnn, oracle):
+    rng = np.random.default_rng(4)
+    x = np.round(rng.normal(size=(300, 2)), 1)  # many duplicates
+    for r2 in (0.0, -1.0, float("nan"), float("inf")):
+        want = oracle.neighbourhoods(x, r2, grid=False)
+        off, idx, _ = gpu_csr(cnn, x, r2)
+        assert np.array_equal(off, want[0]) and np.array_equal(idx, want[1]), r2
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_random_fit_against_oracle(cnn, oracle, seed):
+    from commonnnclustering_gb300 import workloads
+    rng = np.random.default_rng(seed)
+    x = workloads.md3d(n=20000, seed=seed, centre_spread=2.0)
+    r = 0.12
+    for c, mc in ((0, 2), (3, 5), (10, 10), (40, 2)):
+        want, _ = oracle.clustering_fit(x, r, c, member_cutoff=mc)
+        cl = cnn.Clustering(x)
+        cl.fit(r, c, member_cutoff=mc, v=False)
+        assert np.array_equal(np.asarray(cl.labels), want), (seed, c)
+
+
+def test_fit_unsorted_and_raw_numbering(cnn, oracle):
+    from commonnnclustering_gb300 import workloads
+    x = workloads.blobs2d()
+    want, _ = oracle.clustering_fit(x, 0.3, 5, sort=False)
+    cl = cnn.Clustering(x)
+    cl.fit(0.3, 5, sort_by_size=False, v=False)
+    assert np.array_equal(np.asarray(cl.labels), want)
+
+
+def test_abi_fit_consider_and_current_start(cnn, oracle):
+    from commonnnclustering_gb300 import workloads
+    x = workloads.blobs2d(n=3000, seed=5)
+    p = oracle.make_parameters(0.3, 4, 7)
+    off, idx = oracle.neighbourhoods(x, p["radius_cutoff"])
+    rng = np.random.default_rng(9)
+    consider = (rng.random(x.shape[0]) < 0.8).astype(np.uint8)
+    labels0 = np.where(consider == 0, 3, 0).astype(np.int64)
+    want_l, want_c = labels0.copy(), consider.copy()
+    oracle.fit_bfs_csr(off, idx, p["similarity_cutoff"], p["n_member_cutoff"], 7, want_c, want_l)
+    ctx = cnn.Context(0)
+    ctx.set_points(x)
+    ctx.build_neighbours(p["radius_cutoff"])
+    got_l, got_c = labels0.copy(), consider.copy()
+    ctx.fit(p["similarity_cutoff"], p["n_member_cutoff"], 7, got_c, got_l)
+    assert np.array_equal(got_l, want_l) and np.array_equal(got_c, want_c)
+
+
+def test_precomputed_neighbourhoods_recipe(cnn):
+    g = load_golden("moons_1500.npz")
+    off, idx = g["offsets"], g["indices"]
+    rng = np.random.default_rng(0)
+    rows = [rng.permutation(idx[off[i]:off[i + 1]]) for i in range(off.shape[0] - 1)]  # unsorted rows
+    cl = cnn.Clustering(rows, recipe="neighbourhoods")
+    cl.fit(float(g["radius_cutoff"]), int(g["cnn_cutoff"]), v=False)
+    assert np.array_equal(np.asarray(cl.labels), g["labels"])
+
+
+def test_device_tensor_input_and_graph_reuse(cnn, oracle):
+    import torch
+    from commonnnclustering_gb300 import workloads
+    x = workloads.blobs2d()
+    xt = torch.from_numpy(x).cuda()
+    cl = cnn.Clustering(xt)
+    for r, c in ((0.3, 5), (0.3, 8), (0.25, 5)):
+        cl.fit(r, c, member_cutoff=10, v=False)
+        want, _ = oracle.clustering_fit(x, r, c, member_cutoff=10)
+        assert cl.labels.is_cuda
+        assert np.array_equal(cl.labels.cpu().numpy(), want)
+
+
+def test_float32_input_widened_exactly(cnn, oracle):
+    from commonnnclustering_gb300 import workloads
+    x32 = workloads.nested3d(n=20000, seed=1, n_parents=4)
+    x64 = x32.astype(np.float64)
+    want, _ = oracle.clustering_fit(x64, 0.06, 5, member_cutoff=10)
+    cl = cnn.Clustering(cnn.InputDataGPUComponents(x32))
+    cl.fit(0.06, 5, member_cutoff=10, v=False)
+    assert np.array_equal(np.asarray(cl.labels), want)
+
+
+def test_repeated_fits_are_identical(cnn):
+    from commonnnclustering_gb300 import workloads
+    x = workloads.md3d(n=50000, seed=3)
+    outs = []
+    for _ in range(3):
+        cl = cnn.Clustering(x)
+        cl.fit(0.1, 10, member_cutoff=50, v=False)
+        outs.append(np.asarray(cl.labels).copy())
+    assert all(np.array_equal(outs[0], o) for o in outs[1:])
+
+
+def test_empty_and_single_point(cnn):
+    cl = cnn.Clustering(np.zeros((1, 3)))
+    cl.fit(0.5, 0, v=False)
+    assert cl.labels.tolist() == [0]
+    ctx = cnn.Context(0)
+    ctx.set_points(np.zeros((0, 2)))
+    ctx.build_neighbours(0.25)
+    assert ctx.neighbour_count() == 0
+    ctx.fit(2, 1, 1, np.zeros(0, dtype=np.uint8), np.zeros(0, dtype=np.int64))
+
+
+def test_errors_are_reported(cnn):
+    ctx = cnn.Context(0)
+    with pytest.raises(cnn.CNNError):
+        ctx.fit(2, 1, 1, np.ones(3, dtype=np.uint8), np.zeros(3, dtype=np.int64))  # no graph yet
+    with pytest.raises(cnn.CNNError):
+        ctx.set_neighbours(np.array([0, 2, 3], dtype=np.int64), np.array([0, 5, 1], dtype=np.int32))

@@ -1,0 +1,98 @@
+"""Host-side logic that needs no GPU: recipes, parameters, input
+preparation, records; and registration with the reference package when
+it is importable here."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from commonnnclustering_gb300 import (ClusterParameters, FitterGPU, Labels, MetricGPUEuclidean, recipes)
+from commonnnclustering_gb300.report import Record, Summary
+
+
+def test_default_recipe_builds_gpu_fitter():
+    f = recipes.Builder().make_component("fitter")
+    assert isinstance(f, FitterGPU)
+    assert f._neighbours_getter.is_selfcounting
+
+
+@pytest.mark.parametrize("r,c,cs", [(0.3, 5, 1), (1.5, 0, 4), (2.0, 10, 1)])
+def test_make_parameters_matches_reference_rule(r, c, cs):
+    # _fit.pyx:130-161: r -> r**2 (reduced metric); self-counting: +1 / +2
+    p = recipes.Builder().make_component("fitter").make_parameters(r, c, cs)
+    assert p.radius_cutoff == r ** 2
+    assert p.n_member_cutoff == c + 1 and p.similarity_cutoff == c + 2 and p.current_start == cs
+
+
+def test_make_parameters_euclidean_metric_keeps_radius():
+    b = recipes.Builder(recipes.get_registered_recipe("coordinates"),
+                        **{"fitter.ngetter.dgetter.metric": MetricGPUEuclidean})
+    p = b.make_component("fitter").make_parameters(0.7, 3, 1)
+    assert p.radius_cutoff == 0.7
+
+
+def test_recipe_aliases_and_dunder_keys():
+    b = recipes.Builder("coordinates", fitter__ngetter__dgetter__metric="euclidean")
+    assert "fitter.neighbours_getter.distance_getter.metric" in b.recipe
+    f = b.make_component("fitter")
+    assert isinstance(f._neighbours_getter._distance_getter._metric, MetricGPUEuclidean)
+
+
+def test_prepare_points_from_parts():
+    (data,), kw = recipes.prepare_points_from_parts([[[0, 0], [1, 1]], [[2, 2], [3, 3]]])
+    assert data.shape == (4, 2) and kw["meta"]["edges"] == [2, 2]
+    (data,), kw = recipes.prepare_points_from_parts([[0, 0], [1, 1], [2, 2]])
+    assert data.shape == (3, 2) and data.dtype == np.float64
+    (data,), kw = recipes.prepare_points_from_parts([1.0, 2.0, 3.0])
+    assert data.shape == (1, 3)
+
+
+def test_prepare_neighbourhoods_to_csr():
+    (off, idx), _ = recipes.prepare_neighbourhoods([[0, 1], [1, 0, 2], [2]])
+    assert off.tolist() == [0, 2, 5, 6] and idx.tolist() == [0, 1, 1, 0, 2, 2]
+
+
+def test_cluster_parameters_defaults():
+    p = ClusterParameters(0.5, 3)
+    assert p.n_member_cutoff == 3 and p.current_start == 1
+    assert set(p.to_dict()) == {"radius_cutoff", "similarity_cutoff", "similarity_cutoff_continuous",
+                                "n_member_cutoff", "current_start"}
+
+
+def test_labels_host_bookkeeping():
+    L = Labels(np.array([1, 1, 2, 2, 0, 1], dtype=np.int64))
+    assert L.to_set() == {0, 1, 2}
+    assert dict(L.to_mapping()) == {0: [4], 1: [0, 1, 5], 2: [2, 3]}
+    assert L.consider.dtype == np.uint8 and L.consider.tolist() == [1] * 6
+    with pytest.raises(ValueError):
+        Labels(np.zeros(3, dtype=np.int64), consider=np.ones(2, dtype=np.uint8))
+
+
+def test_record_and_summary():
+    s = Summary()
+    s.append(Record(100, 0.3, 5, 10, None, 3, 0.5, 0.1, 0.25))
+    assert len(s) == 1 and "#points" in str(s[0])
+    with pytest.raises(TypeError):
+        s.append(1)
+
+
+def test_register_with_reference_package():
+    ref = os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isdir(os.path.join(ref, "cnnclustering")):
+        pytest.skip("reference package not installed here")
+    sys.path.insert(0, ref)
+    try:
+        pytest.importorskip("cnnclustering")
+        from cnnclustering import cluster as ref_cluster
+        from cnnclustering import _fit as ref_fit
+        from commonnnclustering_gb300 import interop
+        interop.register_with_reference()
+        cl = ref_cluster.Clustering(np.zeros((4, 2)), recipe="gpu")
+        assert isinstance(cl._fitter, FitterGPU)
+        assert isinstance(cl._fitter, ref_fit.Fitter)
+        p = cl._fitter.make_parameters(0.5, 2, 1)
+        assert p.radius_cutoff == 0.25 and p.similarity_cutoff == 4
+    finally:
+        sys.path.remove(ref)
