@@ -1,0 +1,356 @@
+"""Benchmark: CommonNN fit points/s on the 200,000 x 3 MD-like workload.
+
+One step = one complete fit of 200,000 points in 3D float64 (20
+anisotropic Gaussians + 5 % background, mean degree ~215): cell-grid
+radius search (r = 0.1) -> CSR, common-neighbour check (c = 10) +
+union-find, canonical labels, sort_by_size (member_cutoff = 50).
+
+* ``value``  -- points/s with the points already resident in HBM (device
+  pointers through the C ABI), CUDA events around each step on the
+  library's stream; L2 is flushed (a 256 MiB write) between steps,
+  outside the timed events.
+* ``e2e``    -- the same fit through the C ABI with HOST buffers: the
+  H2D copy of the points, labels and consider and the D2H copy of labels
+  and consider are inside the timed region (pinned host memory).
+* ``roofline`` -- the dominant kernel's algorithmic bytes per launch over
+  its CUDA-event time (library stage events, same stream).
+* ``cpu_baseline`` -- the oracle port of the reference path on this
+  host's cores (1 thread, like the reference).
+
+``--impl reference`` times the reference's CPU path instead (the oracle
+port: grid-restated neighbour lists on all host threads, then the
+reference's BFS with the sorted-merge check on one thread, then
+sort_by_size), one full fit per step.
+
+With torchrun (N > 1) every rank fits its own replica of the workload on
+its own GPU (the fit does not shard); value = points of all ranks / the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="md3d-200k", n=200_000, d=3, radius_cutoff=0.1, cnn_cutoff=10, member_cutoff=50)
+METRIC = "CommonNN fit points/s (bit-exact labels)"
+UNIT = "points/s"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def reduce_max(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.samples = []
+        self._stop = threading.Event()
+        self._th = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([c.strip() for c in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._th = threading.Thread(target=self._run, daemon=True)
+        self._th.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._th:
+            self._th.join(timeout=6)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 5 + i and s[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def make_points():
+    from commonnnclustering_gb300 import workloads
+    return workloads.md3d(n=WORKLOAD["n"])
+
+
+def roofline_entry(stats_list, nnz, n, peaks):
+    """Dominant kernel by mean stage time; algorithmic bytes per launch."""
+    d = WORKLOAD["d"]
+    stages = {
+        # stage -> (kernel name, algorithmic bytes per launch)
+        "ms_fill": ("grid_search_kernel<fill>", n * d * 8 + 4 * nnz + 8 * (n + 1)),
+        "ms_count": ("grid_search_kernel<count>", n * d * 8 + 4 * n),
+        "ms_check": ("check_union_kernel", 4 * nnz + 8 * (n + 1) + n + 8 * n),
+        "ms_cells": ("cell binning + radix sort", 4 * 8 * n),
+        "ms_label": ("labelling", 24 * n),
+        "ms_sort": ("sort_by_size", 32 * n),
+    }
+    means = {k: statistics.mean(s[k] for s in stats_list) for k in stages}
+    top = max(means, key=means.get)
+    kname, bytes_ = stages[top]
+    ms = means[top]
+    achieved = bytes_ / (ms * 1e-3) / 1e9 if ms > 0 else None
+    peak = peaks.get("hbm_gbs")
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            with open(tpath) as f:
+                traffic = json.load(f).get(kname)
+        except Exception:
+            traffic = None
+    return {
+        "kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": (achieved / peak) if (achieved and peak) else None, "traffic": traffic,
+        "algorithmic_bytes": bytes_, "ms_per_launch": ms,
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback 6800",
+        "stage_ms": {k: round(v, 4) for k, v in means.items()},
+    }
+
+
+def cpu_baseline(x, budget_s=25.0):
+    from oracle import cnn_oracle
+    W = WORKLOAD
+    t0 = time.perf_counter()
+    times = []
+    while True:
+        t = time.perf_counter()
+        cnn_oracle.clustering_fit(x, W["radius_cutoff"], W["cnn_cutoff"], member_cutoff=W["member_cutoff"],
+                                  nthreads=1)
+        times.append(time.perf_counter() - t)
+        if time.perf_counter() - t0 + times[-1] > budget_s or len(times) >= 3:
+            break
+    best = min(times)
+    return {"value": W["n"] / best, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{len(times)} full fits of {W['name']} (oracle restatement: grid neighbour lists + "
+                      f"BFS with sorted-merge check + sort_by_size, 1 thread), best {best:.2f} s"}
+
+
+def run_gpu(args):
+    import torch
+    from commonnnclustering_gb300 import _abi
+
+    rank, world, local = dist_env()
+    dist = init_dist(world)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    W = WORKLOAD
+    x = make_points()
+    n = x.shape[0]
+    stream = torch.cuda.Stream(device=dev)
+    ctx = _abi.Context(local, stream=int(stream.cuda_stream))
+    ctx.set_timing(True)
+    xt = torch.from_numpy(x).to(dev)
+    labels = torch.zeros(n, dtype=torch.int64, device=dev)
+    consider = torch.ones(n, dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    r2 = W["radius_cutoff"] ** 2
+    sc, nm = W["cnn_cutoff"] + 2, W["cnn_cutoff"] + 1
+    torch.cuda.synchronize()
+
+    def step():
+        with torch.cuda.stream(stream):
+            labels.zero_()
+            consider.fill_(1)
+        ctx.set_points(xt)
+        ctx.build_neighbours(r2)
+        ctx.fit(sc, nm, 1, consider, labels)
+        ctx.sort_by_size(labels, W["member_cutoff"], None)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    launches0 = ctx.stats()["n_launches"]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stats_list = []
+    barrier(dist)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter()
+    with ClockSampler(local) as clocks:
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()  # 256 MiB write: evicts L2 between steps
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+            stats_list.append(ctx.stats())
+        torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall
+    barrier(dist)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    mean_ms = statistics.mean(step_ms)
+    max_ms = reduce_max(dist, mean_ms)
+    launches = (stats_list[-1]["n_launches"] - launches0) // max(args.steps, 1)
+    nnz = stats_list[-1]["n_nonzero"]
+    check_labels = labels.cpu().numpy()
+
+    # e2e: host buffers through the C ABI (pinned), copies inside the timed region
+    x_host = torch.from_numpy(x).pin_memory().numpy()
+    lab_host = torch.zeros(n, dtype=torch.int64).pin_memory().numpy()
+    con_host = torch.ones(n, dtype=torch.uint8).pin_memory().numpy()
+    e2e_ctx = _abi.Context(local)
+
+    def e2e_step():
+        lab_host[:] = 0
+        con_host[:] = 1
+        e2e_ctx.set_points(x_host)
+        e2e_ctx.build_neighbours(r2)
+        e2e_ctx.fit(sc, nm, 1, con_host, lab_host)
+        e2e_ctx.sort_by_size(lab_host, W["member_cutoff"], None)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        e2e_step()
+        e2e_times.append(time.perf_counter() - t)
+    e2e_max = reduce_max(dist, statistics.mean(e2e_times))
+    if not np.array_equal(lab_host, check_labels):
+        raise SystemExit("bench: host-buffer and device-buffer fits disagree")
+    h2d = n * W["d"] * 8 + n * 8 * 2 + n      # points, labels (fit + sort), consider
+    d2h = n * 8 * 2 + n                       # labels (fit + sort), consider
+
+    if rank != 0:
+        return
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        peaks = {"hbm_gbs": 6800.0}
+    line = {
+        "metric": METRIC, "value": world * n / (max_ms * 1e-3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": max_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded md3d generator)",
+        "config": {"workload": W["name"], "n_points": n, "n_dim": W["d"], "radius_cutoff": W["radius_cutoff"],
+                   "cnn_cutoff": W["cnn_cutoff"], "member_cutoff": W["member_cutoff"],
+                   "neighbour_pairs": nnz, "l2": "flushed between steps (256 MiB write)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": world * n / e2e_max, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches) * args.steps,
+        "gpu_launches_per_step": int(launches),
+        "clocks": clocks.summary(),
+        "roofline": roofline_entry(stats_list, nnz, n, peaks),
+        "wall_s_timed_region": t_wall,
+        "fit_stats": {k: stats_list[-1][k] for k in ("n_nodes", "n_checks", "n_accepted", "n_exact",
+                                                     "n_candidates", "n_clusters", "filter_band")},
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(x)
+    print(json.dumps(line), flush=True)
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    from oracle import cnn_oracle
+    W = WORKLOAD
+    x = make_points()
+    n = x.shape[0]
+    cores = max(1, len(os.sched_getaffinity(0)))
+
+    def step():
+        cnn_oracle.clustering_fit(x, W["radius_cutoff"], W["cnn_cutoff"], member_cutoff=W["member_cutoff"],
+                                  nthreads=cores)
+
+    for _ in range(args.warmup):
+        step()
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        step()
+        times.append(time.perf_counter() - t)
+    mean_s = statistics.mean(times)
+    value = n / mean_s
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean_s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded md3d generator)",
+        "config": {"workload": W["name"], "n_points": n, "n_dim": W["d"], "radius_cutoff": W["radius_cutoff"],
+                   "cnn_cutoff": W["cnn_cutoff"], "member_cutoff": W["member_cutoff"]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"full {W['name']} fit per step: neighbour lists restated on {cores} threads, "
+                                   "the reference's BFS + sorted-merge check on 1 thread, sort_by_size"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl != "reference":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -158,6 +158,7 @@ CNN_API cnn_status cnn_get_stats(const cnn_context *cctx, cnn_stats *out) {
         if (cudaEventElapsedTime(&ms, ctx->ev_begin[i], ctx->ev_end[i]) == cudaSuccess) *slot_field[i] = ms;
         (void)cudaGetLastError();
     }
+    ctx->stats.n_launches = ctx->n_launches;
     *out = ctx->stats;
     return CNN_OK;
 }

@@ -37,7 +37,12 @@ struct Error {
         if (s_ != CNN_OK) return s_;        \
     } while (0)
 
-#define CNN_LAUNCH_CHECK(ctx) CNN_CUDA(ctx, cudaGetLastError())
+// Called after every kernel launch: checks the launch and counts it.
+#define CNN_LAUNCH_CHECK(ctx)             \
+    do {                                  \
+        ++(ctx)->n_launches;              \
+        CNN_CUDA(ctx, cudaGetLastError()); \
+    } while (0)
 
 // A grow-only device buffer.  Memory is returned only when the context is
 // destroyed, so repeated fits of the same size allocate nothing.
@@ -60,6 +65,7 @@ struct cnn_context {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     bool timing = false;
+    int64_t n_launches = 0;
     std::string last_error;
     cnn_stats stats{};
 

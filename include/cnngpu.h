@@ -109,6 +109,7 @@ typedef struct cnn_stats {
     float ms_bbox, ms_cells, ms_count, ms_scan, ms_fill;   /* neighbour build */
     float ms_nodes, ms_check, ms_label;                    /* fit */
     float ms_sort;                                         /* sort_by_size */
+    int64_t n_launches;       /* kernels launched by this context since creation */
 } cnn_stats;
 
 CNN_API int cnn_abi_version(void);
