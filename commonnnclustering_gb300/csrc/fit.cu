@@ -36,7 +36,6 @@ namespace cnn {
 namespace {
 
 constexpr int kCheckWarps = 8;
-constexpr int kListCap = 1024;  // members of N(a) kept in shared memory per warp
 
 __device__ __forceinline__ int32_t uf_find(int32_t *parent, int32_t x) {
     int32_t cur = x;
@@ -62,33 +61,35 @@ __device__ __forceinline__ void uf_unite(int32_t *parent, int32_t a, int32_t b) 
     }
 }
 
-__device__ __forceinline__ bool bsearch_contains(const int32_t *A, int32_t la, int32_t v) {
-    int32_t lo = 0, hi = la;
-    while (lo < hi) {
-        int32_t mid = (lo + hi) >> 1;
-        if (A[mid] < v) lo = mid + 1; else hi = mid;
-    }
-    return lo < la && A[lo] == v;
-}
-
-// Warp-cooperative: does |A & B| reach `needed` (> 0)?  A and B ascending.
-__device__ __forceinline__ bool warp_shares_at_least(const int32_t *A, int32_t la, const int32_t *__restrict__ B,
-                                                     int32_t lb, int32_t needed, int lane) {
+// Warp-cooperative merge-path count: does |A & B| reach `needed` (> 0)?
+// A and B ascending, duplicate-free, values < 2^31 - 2.  Each step loads
+// one 32-wide chunk of each list (coalesced), every lane finds its B value
+// among the 32 A values with a 5-step shuffle binary search, and the chunk
+// with the smaller maximum is consumed (no pair can match across it).
+// Stops at `needed` matches, or when the rest cannot reach it.
+__device__ __forceinline__ bool warp_shares_at_least(const int32_t *__restrict__ A, int32_t la,
+                                                     const int32_t *__restrict__ B, int32_t lb, int32_t needed,
+                                                     int lane) {
     if (la < needed || lb < needed) return false;
-    // members of B outside [A[0], A[la-1]] cannot match
-    const int32_t amin = A[0], amax = A[la - 1];
-    int32_t count = 0;
-    for (int32_t k0 = 0; k0 < lb; k0 += 32) {
-        const int32_t k = k0 + lane;
-        bool found = false;
-        if (k < lb) {
-            const int32_t v = B[k];
-            if (v >= amin && v <= amax) found = bsearch_contains(A, la, v);
+    int32_t ia = 0, ib = 0, count = 0;
+    while (ia < la && ib < lb) {
+        const int32_t va = ia + lane < la ? __ldg(A + ia + lane) : INT_MAX;      // padding never matches:
+        const int32_t vb = ib + lane < lb ? __ldg(B + ib + lane) : INT_MAX - 1;  // A pads differ from B pads
+        int pos = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+            const int32_t probe = __shfl_sync(0xffffffffu, va, pos + step - 1);
+            if (probe < vb) pos += step;
         }
+        const bool found = __shfl_sync(0xffffffffu, va, pos) == vb;
         count += __popc(__ballot_sync(0xffffffffu, found));
         if (count >= needed) return true;
-        const int32_t remaining = lb - (k0 + 32);
-        if (count + (remaining > 0 ? remaining : 0) < needed) return false;
+        const int32_t amax = __shfl_sync(0xffffffffu, va, 31);
+        const int32_t bmax = __shfl_sync(0xffffffffu, vb, 31);
+        if (amax <= bmax) ia += 32;
+        if (bmax <= amax) ib += 32;
+        const int32_t rest = min(la - ia, lb - ib);
+        if (count + (rest > 0 ? rest : 0) < needed) return false;
     }
     return false;
 }
@@ -101,7 +102,7 @@ __global__ void node_kernel(const int32_t *__restrict__ deg, const int32_t *__re
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
         const bool is_node = (int64_t)deg[p] > n_member_cutoff && consider[perm[p]] != 0;
         node[p] = is_node ? 1 : 0;
-        parent[p] = (int32_t)p;
+        parent[p] = is_node ? (int32_t)p : -1;  // -1: not a node (never joined)
         comp_min[p] = INT_MAX;
         local += is_node;
     }
@@ -109,54 +110,80 @@ __global__ void node_kernel(const int32_t *__restrict__ deg, const int32_t *__re
     if ((threadIdx.x & 31) == 0 && local) atomicAdd(&counters[4], local);
 }
 
+// Persistent warps stride over nodes.  For node a, candidate edges (a, b)
+// with b > a and b a node (parent[b] >= 0) are taken 32 at a time; their
+// roots are resolved in parallel (one lane each) and re-resolved only after
+// this warp joined something: a stale "different" only costs an extra
+// check, never a wrong skip.  max_edges bounds the candidate edges one node
+// examines (the hook pass uses 2).
 __global__ void __launch_bounds__(kCheckWarps * 32) check_union_kernel(
     int64_t n, const int64_t *__restrict__ row_off, const int32_t *__restrict__ cols,
-    const uint8_t *__restrict__ node, int32_t *__restrict__ parent, int32_t needed,
+    int32_t *__restrict__ parent, int32_t needed, int32_t max_edges,
     unsigned long long *__restrict__ counters) {
-    __shared__ int32_t s_list[kCheckWarps][kListCap];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int64_t a64 = (int64_t)blockIdx.x * kCheckWarps + wid;
-    if (a64 >= n) return;
-    const int32_t a = (int32_t)a64;
-    if (!node[a]) return;
-    const int64_t s = row_off[a], e = row_off[a + 1];
-    const int32_t la = (int32_t)(e - s);
-    const int32_t *A = cols + s;
-    if (la <= kListCap) {
-        for (int32_t k = lane; k < la; k += 32) s_list[wid][k] = A[k];
-        __syncwarp();
-        A = s_list[wid];
-    }
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     unsigned long long n_checks = 0, n_acc = 0;
-    for (int64_t k0 = s; k0 < e; k0 += 32) {
-        const int64_t k = k0 + lane;
-        int32_t b = -1;
-        bool cand = false;
-        if (k < e) {
-            b = cols[k];
-            cand = b > a && node[b];
-        }
-        unsigned mask = __ballot_sync(0xffffffffu, cand);
-        while (mask) {
-            const int src = __ffs(mask) - 1;
-            mask &= mask - 1;
-            const int32_t bb = __shfl_sync(0xffffffffu, b, src);
-            int same = 0;
-            if (lane == 0) same = uf_find(parent, a) == uf_find(parent, bb);
-            same = __shfl_sync(0xffffffffu, same, 0);
-            if (same) continue;
-            bool ok;
-            if (needed <= 0) {
-                ok = needed == 0;
-            } else {
-                const int64_t bs = row_off[bb];
-                const int32_t lb = (int32_t)(row_off[bb + 1] - bs);
-                ok = warp_shares_at_least(A, la, cols + bs, lb, needed, lane);
-                ++n_checks;
+    for (int64_t a64 = warp0; a64 < n; a64 += nwarps) {
+        const int32_t a = (int32_t)a64;
+        if (*(volatile int32_t *)&parent[a] < 0) continue;  // not a node
+        const int64_t s = row_off[a], e = row_off[a + 1];
+        const int32_t la = (int32_t)(e - s);
+        const int32_t *A = cols + s;
+        int32_t ra = -1;
+        bool dirty = true;
+        int32_t seen = 0;
+        for (int64_t k0 = s; k0 < e && seen < max_edges; k0 += 32) {
+            const int64_t k = k0 + lane;
+            int32_t b = -1, pb = -1;
+            if (k < e) {
+                b = cols[k];
+                if (b > a) pb = *(volatile int32_t *)&parent[b];
             }
-            if (ok) {
-                if (lane == 0) uf_unite(parent, a, bb);
-                ++n_acc;
+            bool cand = pb >= 0;
+            unsigned cmask = __ballot_sync(0xffffffffu, cand);
+            if (!cmask) continue;
+            if (seen + __popc(cmask) > max_edges) {  // keep only the first edges
+                const int keep = max_edges - seen;
+                unsigned m = cmask, kept = 0;
+                for (int i = 0; i < keep; ++i) { kept |= m & (0u - m); m &= m - 1; }
+                cmask = kept;
+                cand = (cmask >> lane) & 1u;
+            }
+            seen += __popc(cmask);
+            if (dirty) {
+                ra = uf_find(parent, a);
+                dirty = false;
+            }
+            int32_t rb = cand ? uf_find(parent, pb) : -1;
+            unsigned mask = __ballot_sync(0xffffffffu, cand && rb != ra);
+            while (mask) {
+                if (dirty) {
+                    ra = uf_find(parent, a);
+                    const bool live = (mask >> lane) & 1u;
+                    if (live) rb = uf_find(parent, rb);
+                    mask = __ballot_sync(0xffffffffu, live && rb != ra);
+                    dirty = false;
+                    if (!mask) break;
+                }
+                const int src = __ffs(mask) - 1;
+                mask &= mask - 1;
+                const int32_t bb = __shfl_sync(0xffffffffu, b, src);
+                bool ok;
+                if (needed <= 0) {
+                    ok = needed == 0;
+                } else {
+                    const int64_t bs = row_off[bb];
+                    const int32_t lb = (int32_t)(row_off[bb + 1] - bs);
+                    ok = warp_shares_at_least(A, la, cols + bs, lb, needed, lane);
+                    ++n_checks;
+                }
+                if (ok) {
+                    if (lane == 0) uf_unite(parent, a, bb);
+                    __syncwarp();
+                    ++n_acc;
+                    dirty = true;
+                }
             }
         }
     }
@@ -366,8 +393,16 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     stage_end(ctx, 5);
 
     stage_begin(ctx, 6);
-    check_union_kernel<<<grid_for(n, kCheckWarps), kCheckWarps * 32, 0, st>>>(
-        n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), node, parent, (int32_t)similarity_cutoff,
+    // hook: every node checks its first two candidate edges; compress; then
+    // the full pass, where edges inside already joined sets cost one load
+    const unsigned check_blocks = std::min<unsigned>(grid_for(n, kCheckWarps), 152u * 8u);
+    check_union_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(
+        n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff, 2, counters);
+    CNN_LAUNCH_CHECK(ctx);
+    root_store_kernel<<<blocks_for(n), 256, 0, st>>>(n, node, parent);
+    CNN_LAUNCH_CHECK(ctx);
+    check_union_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(
+        n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff, INT32_MAX,
         counters);
     CNN_LAUNCH_CHECK(ctx);
     stage_end(ctx, 6);

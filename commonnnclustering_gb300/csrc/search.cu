@@ -153,76 +153,163 @@ __global__ void perm_gather_kernel(const uint64_t *__restrict__ keys, int64_t n,
     }
 }
 
-// ---- grid search: one warp per query, lanes over 32 consecutive candidates
+// ---- grid search -----------------------------------------------------------
+// Work item = (cell, up to kItemQueries consecutive queries of that cell).
+// The block packs the cell's 9 candidate runs (3x3 (y,z) neighbours, each
+// three x-cells long and contiguous in internal order) into shared-memory
+// tiles of kGridTile candidates; each warp owns kQueriesPerWarp queries
+// held in registers and tests every packed candidate of the tile against
+// all of them (lanes over candidates, one shared load per candidate).
+// Packed order = run order = ascending internal index, so each query's
+// hits come out sorted.
+constexpr int kGridWarps = 8;
+constexpr int kQueriesPerWarp = 4;
+constexpr int kItemQueries = kGridWarps * kQueriesPerWarp;  // 32
+constexpr int kGridTile = 1024;
+
+// Float64 predicate on rows of the original-order coordinate array.
+__device__ __forceinline__ bool exact_rows(const double *__restrict__ x, int d, int32_t ia, int32_t ib,
+                                           const SearchParams &sp) {
+    const double *xa = x + (int64_t)ia * d;
+    const double *xb = x + (int64_t)ib * d;
+    return exact_in_radius(xa, xb, d, sp);
+}
+
+__global__ void item_count_kernel(const int64_t *__restrict__ cell_start, int64_t ncells,
+                                  int32_t *__restrict__ items_per_cell) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncells; c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = cell_start[c + 1] - cell_start[c];
+        items_per_cell[c] = (int32_t)((q + kItemQueries - 1) / kItemQueries);
+    }
+}
+
+__global__ void item_fill_kernel(const int64_t *__restrict__ cell_start, int64_t ncells,
+                                 const int64_t *__restrict__ item_off, int2 *__restrict__ items) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncells; c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = item_off[c], e = item_off[c + 1];
+        for (int64_t k = b; k < e; ++k)
+            items[k] = make_int2((int32_t)c, (int32_t)(cell_start[c] + (k - b) * kItemQueries));
+    }
+}
+
 template <bool kFill>
-__global__ void __launch_bounds__(256) grid_search_kernel(
-    const double *__restrict__ x, int d, int64_t n, GridGeom geo, SearchParams sp,
-    const int32_t *__restrict__ perm, const int32_t *__restrict__ cell_of,
-    const int64_t *__restrict__ cell_start, const float4 *__restrict__ xf4,
+__global__ void __launch_bounds__(kGridWarps * 32) grid_search_kernel(
+    const int2 *__restrict__ items, const double *__restrict__ x, int d, GridGeom geo, SearchParams sp,
+    const int32_t *__restrict__ perm, const int64_t *__restrict__ cell_start, const float4 *__restrict__ xf4,
     int32_t *__restrict__ deg, const int64_t *__restrict__ row_off, int32_t *__restrict__ cols,
     unsigned long long *__restrict__ counters) {
-    const int lane = threadIdx.x & 31;
-    const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (p >= n) return;
-    const int32_t i = perm[p];
-    const int32_t cid = cell_of[i];
-    if (cid >= geo.ncells) {  // non-finite coordinates: no neighbours at all
-        if (!kFill && lane == 0) deg[p] = 0;
-        return;
+    __shared__ float4 s_xf[kGridTile];
+    __shared__ int32_t s_j[kGridTile];
+    __shared__ int64_t s_rs[9];
+    __shared__ int32_t s_cum[10];
+    __shared__ int32_t s_nruns;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int2 item = items[blockIdx.x];
+    const int32_t cid = item.x;
+    const int64_t q0 = item.y;
+    const int64_t qend = cell_start[cid + 1];
+    if (threadIdx.x == 0) {
+        const int32_t cx = cid % geo.g[0];
+        const int32_t cy = (cid / geo.g[0]) % geo.g[1];
+        const int32_t cz = cid / (geo.g[0] * geo.g[1]);
+        const int32_t xlo = cx > 0 ? cx - 1 : 0;
+        const int32_t xhi = cx + 1 < geo.g[0] ? cx + 1 : geo.g[0] - 1;
+        int nr = 0;
+        int32_t cum = 0;
+        for (int dz = -1; dz <= 1; ++dz) {
+            const int32_t z = cz + dz;
+            if (z < 0 || z >= geo.g[2]) continue;
+            for (int dy = -1; dy <= 1; ++dy) {
+                const int32_t y = cy + dy;
+                if (y < 0 || y >= geo.g[1]) continue;
+                const int64_t row = (int64_t)geo.g[0] * ((int64_t)y + (int64_t)geo.g[1] * z);
+                const int64_t rs = cell_start[row + xlo];
+                const int64_t re = cell_start[row + xhi + 1];
+                if (re <= rs) continue;
+                s_rs[nr] = rs;
+                s_cum[nr] = cum;
+                cum += (int32_t)(re - rs);
+                ++nr;
+            }
+        }
+        s_cum[nr] = cum;
+        s_nruns = nr;
     }
-    const int32_t cx = cid % geo.g[0];
-    const int32_t cy = (cid / geo.g[0]) % geo.g[1];
-    const int32_t cz = cid / (geo.g[0] * geo.g[1]);
-    const float4 q = xf4[p];
-    double xq[3] = {0.0, 0.0, 0.0};
-    for (int k = 0; k < d; ++k) xq[k] = x[(int64_t)i * d + k];
+    __syncthreads();
+    const int nruns = s_nruns;
+    const int32_t total = s_cum[nruns];
+
+    // this warp's queries: kQueriesPerWarp consecutive ones, so that short
+    // items leave whole warps idle instead of spreading one query per warp
+    int64_t q[kQueriesPerWarp];
+    float4 qf[kQueriesPerWarp];
+    int64_t wpos[kQueriesPerWarp];
+    int32_t cnt[kQueriesPerWarp];
+#pragma unroll
+    for (int k = 0; k < kQueriesPerWarp; ++k) {
+        q[k] = q0 + (int64_t)wid * kQueriesPerWarp + k;
+        const bool ok = q[k] < qend;
+        qf[k] = ok ? xf4[q[k]] : make_float4(0.f, 0.f, 0.f, 0.f);
+        wpos[k] = (kFill && ok) ? row_off[q[k]] : 0;
+        cnt[k] = 0;
+        if (!ok) q[k] = -1;
+    }
+    const bool warp_has_work = q[0] >= 0;
     const unsigned lt = (1u << lane) - 1u;
-    int64_t w = kFill ? row_off[p] : 0;
-    int64_t cnt = 0;
-    unsigned long long n_exact = 0, n_cand = 0;
-    const int32_t xlo = cx > 0 ? cx - 1 : 0;
-    const int32_t xhi = cx + 1 < geo.g[0] ? cx + 1 : geo.g[0] - 1;
-    for (int dz = -1; dz <= 1; ++dz) {
-        const int32_t z = cz + dz;
-        if (z < 0 || z >= geo.g[2]) continue;
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int32_t y = cy + dy;
-            if (y < 0 || y >= geo.g[1]) continue;
-            const int64_t row = (int64_t)geo.g[0] * ((int64_t)y + (int64_t)geo.g[1] * z);
-            const int64_t rs = cell_start[row + xlo];
-            const int64_t re = cell_start[row + xhi + 1];
-            n_cand += (unsigned long long)(re - rs);
-            for (int64_t j0 = rs; j0 < re; j0 += 32) {
-                const int64_t j = j0 + lane;
-                bool in = false;
-                if (j < re) {
-                    const float4 c = __ldg(&xf4[j]);
-                    const float ex = q.x - c.x, ey = q.y - c.y, ez = q.z - c.z;
-                    const float sf = ex * ex + ey * ey + ez * ez;
-                    if (sf <= sp.thr_in) {
-                        in = true;
-                    } else if (sf <= sp.thr_out) {
-                        double xb[3] = {0.0, 0.0, 0.0};
-                        const int32_t jj = perm[j];
-                        for (int k = 0; k < d; ++k) xb[k] = x[(int64_t)jj * d + k];
-                        in = exact_in_radius(xq, xb, d, sp);
+    unsigned long long n_exact = 0;
+    for (int32_t t0 = 0; t0 < total; t0 += kGridTile) {
+        const int32_t tlen = min(kGridTile, total - t0);
+        const int32_t tpad = (tlen + 31) & ~31;
+        __syncthreads();
+        for (int32_t t = threadIdx.x; t < tpad; t += blockDim.x) {
+            if (t < tlen) {
+                const int32_t pos = t0 + t;
+                int r = 0;
+                while (r + 1 < nruns && s_cum[r + 1] <= pos) ++r;
+                const int32_t j = (int32_t)(s_rs[r] + (pos - s_cum[r]));
+                s_j[t] = j;
+                s_xf[t] = xf4[j];
+            } else {  // padding: +inf is never within the radius
+                s_j[t] = -1;
+                s_xf[t] = make_float4(INFINITY, INFINITY, INFINITY, 0.f);
+            }
+        }
+        __syncthreads();
+        if (!warp_has_work) continue;
+        for (int32_t c0 = 0; c0 < tpad; c0 += 32) {
+            const int32_t t = c0 + lane;
+            const float4 cf = s_xf[t];
+#pragma unroll
+            for (int k = 0; k < kQueriesPerWarp; ++k) {
+                if (q[k] < 0) break;  // warp-uniform; invalid queries come last
+                const float ex = qf[k].x - cf.x, ey = qf[k].y - cf.y, ez = qf[k].z - cf.z;
+                const float sf = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                bool in = sf <= sp.thr_in;
+                const bool amb = !in && sf <= sp.thr_out;
+                if (__any_sync(0xffffffffu, amb)) {  // rare: decide in float64
+                    if (amb) {
+                        in = exact_rows(x, d, perm[q[k]], perm[s_j[t]], sp);
                         ++n_exact;
                     }
                 }
                 const unsigned hit = __ballot_sync(0xffffffffu, in);
-                if (kFill && in) cols[w + cnt + __popc(hit & lt)] = (int32_t)j;
-                cnt += __popc(hit);
+                if (kFill && in) cols[wpos[k] + cnt[k] + __popc(hit & lt)] = s_j[t];
+                cnt[k] += __popc(hit);
             }
         }
     }
     if (!kFill) {
         if (lane == 0) {
-            deg[p] = (int32_t)cnt;
-            atomicAdd(&counters[1], n_cand);
+#pragma unroll
+            for (int k = 0; k < kQueriesPerWarp; ++k)
+                if (q[k] >= 0) deg[q[k]] = cnt[k];
         }
-        // float64 rechecks: summed over lanes
         for (int o = 16; o > 0; o >>= 1) n_exact += __shfl_down_sync(0xffffffffu, n_exact, o);
         if (lane == 0 && n_exact) atomicAdd(&counters[0], n_exact);
+        if (threadIdx.x == 0) {
+            const int64_t nq = (qend < q0 + kItemQueries ? qend : q0 + kItemQueries) - q0;
+            atomicAdd(&counters[1], (unsigned long long)total * (unsigned long long)nq);
+        }
     }
 }
 
@@ -502,6 +589,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
 
     int32_t *deg = ctx->deg.as<int32_t>();
     int64_t *row_off = ctx->row_off.as<int64_t>();
+    int64_t grid_items = 0;
     unsigned long long *counters = ctx->counters.as<unsigned long long>();
 
     if (use_grid) {
@@ -525,14 +613,34 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         perm_gather_kernel<<<gb, 256, 0, st>>>(keys, n, bits_n, ctx->x, d, geo, ctx->perm.as<int32_t>(),
                                                 ctx->inv.as<int32_t>(), ctx->xf4.as<float4>());
         CNN_LAUNCH_CHECK(ctx);
+
+        // work items: (cell, first query) for every 32 queries of a cell
+        CNN_TRY(ctx->ensure(ctx->io_a, sizeof(int32_t) * (size_t)(geo.ncells + 1)));
+        CNN_TRY(ctx->ensure(ctx->io_b, sizeof(int64_t) * (size_t)(geo.ncells + 1)));
+        item_count_kernel<<<std::min<unsigned>(grid_for(geo.ncells, 256), 152u * 16u), 256, 0, st>>>(
+            ctx->cell_start.as<int64_t>(), geo.ncells, ctx->io_a.as<int32_t>());
+        CNN_LAUNCH_CHECK(ctx);
+        CNN_CUDA(ctx, cudaMemsetAsync(ctx->io_a.as<int32_t>() + geo.ncells, 0, sizeof(int32_t), st));
+        CNN_TRY(scan_exclusive_i32_to_i64(ctx, ctx->io_a.as<int32_t>(), ctx->io_b.as<int64_t>(), geo.ncells + 1));
+        int64_t nitems = 0;
+        CNN_CUDA(ctx, cudaMemcpyAsync(&nitems, ctx->io_b.as<int64_t>() + geo.ncells, sizeof(int64_t),
+                                      cudaMemcpyDeviceToHost, st));
+        CNN_CUDA(ctx, cudaStreamSynchronize(st));
+        CNN_TRY(ctx->ensure(ctx->io_c, sizeof(int2) * (size_t)(nitems > 0 ? nitems : 1)));
+        item_fill_kernel<<<std::min<unsigned>(grid_for(geo.ncells, 256), 152u * 16u), 256, 0, st>>>(
+            ctx->cell_start.as<int64_t>(), geo.ncells, ctx->io_b.as<int64_t>(), ctx->io_c.as<int2>());
+        CNN_LAUNCH_CHECK(ctx);
+        grid_items = nitems;
         stage_end(ctx, 1);
 
         stage_begin(ctx, 2);
-        const unsigned gq = grid_for(n * 32, 256);
-        grid_search_kernel<false><<<gq, 256, 0, st>>>(ctx->x, d, n, geo, sp, ctx->perm.as<int32_t>(),
-                                                       ctx->cell_of.as<int32_t>(), ctx->cell_start.as<int64_t>(),
-                                                       ctx->xf4.as<float4>(), deg, nullptr, nullptr, counters);
-        CNN_LAUNCH_CHECK(ctx);
+        CNN_CUDA(ctx, cudaMemsetAsync(deg, 0, sizeof(int32_t) * (size_t)n, st));
+        if (nitems > 0) {
+            grid_search_kernel<false><<<(unsigned)nitems, kGridWarps * 32, 0, st>>>(
+                ctx->io_c.as<int2>(), ctx->x, d, geo, sp, ctx->perm.as<int32_t>(), ctx->cell_start.as<int64_t>(),
+                ctx->xf4.as<float4>(), deg, nullptr, nullptr, counters);
+            CNN_LAUNCH_CHECK(ctx);
+        }
         stage_end(ctx, 2);
         ctx->identity_perm = false;
     } else {
@@ -572,17 +680,18 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
 
     stage_begin(ctx, 4);
     if (use_grid) {
-        const unsigned gq = grid_for(n * 32, 256);
-        grid_search_kernel<true><<<gq, 256, 0, st>>>(ctx->x, d, n, geo, sp, ctx->perm.as<int32_t>(),
-                                                      ctx->cell_of.as<int32_t>(), ctx->cell_start.as<int64_t>(),
-                                                      ctx->xf4.as<float4>(), deg, row_off, ctx->cols.as<int32_t>(),
-                                                      counters);
+        if (grid_items > 0) {
+            grid_search_kernel<true><<<(unsigned)grid_items, kGridWarps * 32, 0, st>>>(
+                ctx->io_c.as<int2>(), ctx->x, d, geo, sp, ctx->perm.as<int32_t>(), ctx->cell_start.as<int64_t>(),
+                ctx->xf4.as<float4>(), deg, row_off, ctx->cols.as<int32_t>(), counters);
+            CNN_LAUNCH_CHECK(ctx);
+        }
     } else {
         const size_t smem = sizeof(float) * (size_t)(kTileCand + kTileWarps) * (d + 1);
         tile_search_kernel<true><<<grid_for(n, kTileWarps), kTileWarps * 32, smem, st>>>(
             ctx->x, ctx->scratch_b.as<float>(), d, n, sp, deg, row_off, ctx->cols.as<int32_t>(), counters);
+        CNN_LAUNCH_CHECK(ctx);
     }
-    CNN_LAUNCH_CHECK(ctx);
     stage_end(ctx, 4);
 
     unsigned long long hc[2] = {0, 0};
