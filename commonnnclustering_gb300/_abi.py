@@ -76,6 +76,7 @@ SIGNATURES = {
     "cnn_fit": (_INT, [_P, _I64, _I64, _I64, _P, _P, _INT]),
     "cnn_sort_by_size": (_INT, [_P, _P, _I64, _I64, _I64, _INT]),
     "cnn_check_lists": (_INT, [_P, _P, _I64, _P, _I64, _I64, _P, _INT]),
+    "cnn_fit_csr_noalloc": (_INT, [_P, _P, _I64, _I64, _I64, _I64, _P, _P, _P]),
 }
 
 _lib = None

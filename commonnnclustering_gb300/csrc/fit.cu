@@ -30,201 +30,11 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "fit_kernels.cuh"
 
 namespace cnn {
 
 namespace {
-
-constexpr int kCheckWarps = 8;
-
-__device__ __forceinline__ int32_t uf_find(int32_t *parent, int32_t x) {
-    int32_t cur = x;
-    int32_t next = *(volatile int32_t *)&parent[cur];
-    while (next != cur) {
-        int32_t nn = *(volatile int32_t *)&parent[next];
-        if (nn != next) *(volatile int32_t *)&parent[cur] = nn;  // path halving
-        cur = next;
-        next = nn;
-    }
-    return cur;
-}
-
-// Join the sets of a and b; the smaller root index becomes the root.
-// Lock-free: a failed CAS means another thread changed that root first.
-__device__ __forceinline__ void uf_unite(int32_t *parent, int32_t a, int32_t b) {
-    for (;;) {
-        a = uf_find(parent, a);
-        b = uf_find(parent, b);
-        if (a == b) return;
-        if (a > b) { int32_t t = a; a = b; b = t; }
-        if (atomicCAS(&parent[b], b, a) == b) return;
-    }
-}
-
-// Warp-cooperative merge-path count: does |A & B| reach `needed` (> 0)?
-// A and B ascending, duplicate-free, values < 2^31 - 2.  Each step loads
-// one 32-wide chunk of each list (coalesced), every lane finds its B value
-// among the 32 A values with a 5-step shuffle binary search, and the chunk
-// with the smaller maximum is consumed (no pair can match across it).
-// Stops at `needed` matches, or when the rest cannot reach it.
-__device__ __forceinline__ bool warp_shares_at_least(const int32_t *__restrict__ A, int32_t la,
-                                                     const int32_t *__restrict__ B, int32_t lb, int32_t needed,
-                                                     int lane) {
-    if (la < needed || lb < needed) return false;
-    int32_t ia = 0, ib = 0, count = 0;
-    while (ia < la && ib < lb) {
-        const int32_t va = ia + lane < la ? __ldg(A + ia + lane) : INT_MAX;      // padding never matches:
-        const int32_t vb = ib + lane < lb ? __ldg(B + ib + lane) : INT_MAX - 1;  // A pads differ from B pads
-        int pos = 0;
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1) {
-            const int32_t probe = __shfl_sync(0xffffffffu, va, pos + step - 1);
-            if (probe < vb) pos += step;
-        }
-        const bool found = __shfl_sync(0xffffffffu, va, pos) == vb;
-        count += __popc(__ballot_sync(0xffffffffu, found));
-        if (count >= needed) return true;
-        const int32_t amax = __shfl_sync(0xffffffffu, va, 31);
-        const int32_t bmax = __shfl_sync(0xffffffffu, vb, 31);
-        if (amax <= bmax) ia += 32;
-        if (bmax <= amax) ib += 32;
-        const int32_t rest = min(la - ia, lb - ib);
-        if (count + (rest > 0 ? rest : 0) < needed) return false;
-    }
-    return false;
-}
-
-__global__ void node_kernel(const int32_t *__restrict__ deg, const int32_t *__restrict__ perm,
-                            const uint8_t *__restrict__ consider, int64_t n, int64_t n_member_cutoff,
-                            uint8_t *__restrict__ node, int32_t *__restrict__ parent,
-                            int32_t *__restrict__ comp_min, unsigned long long *__restrict__ counters) {
-    unsigned long long local = 0;
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        const bool is_node = (int64_t)deg[p] > n_member_cutoff && consider[perm[p]] != 0;
-        node[p] = is_node ? 1 : 0;
-        parent[p] = is_node ? (int32_t)p : -1;  // -1: not a node (never joined)
-        comp_min[p] = INT_MAX;
-        local += is_node;
-    }
-    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
-    if ((threadIdx.x & 31) == 0 && local) atomicAdd(&counters[4], local);
-}
-
-// Persistent warps stride over nodes.  For node a, candidate edges (a, b)
-// with b > a and b a node (parent[b] >= 0) are taken 32 at a time; their
-// roots are resolved in parallel (one lane each) and re-resolved only after
-// this warp joined something: a stale "different" only costs an extra
-// check, never a wrong skip.  max_edges bounds the candidate edges one node
-// examines (the hook pass uses 2).
-__global__ void __launch_bounds__(kCheckWarps * 32) check_union_kernel(
-    int64_t n, const int64_t *__restrict__ row_off, const int32_t *__restrict__ cols,
-    int32_t *__restrict__ parent, int32_t needed, int32_t max_edges,
-    unsigned long long *__restrict__ counters) {
-    const int lane = threadIdx.x & 31;
-    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    unsigned long long n_checks = 0, n_acc = 0;
-    for (int64_t a64 = warp0; a64 < n; a64 += nwarps) {
-        const int32_t a = (int32_t)a64;
-        if (*(volatile int32_t *)&parent[a] < 0) continue;  // not a node
-        const int64_t s = row_off[a], e = row_off[a + 1];
-        const int32_t la = (int32_t)(e - s);
-        const int32_t *A = cols + s;
-        int32_t ra = -1;
-        bool dirty = true;
-        int32_t seen = 0;
-        for (int64_t k0 = s; k0 < e && seen < max_edges; k0 += 32) {
-            const int64_t k = k0 + lane;
-            int32_t b = -1, pb = -1;
-            if (k < e) {
-                b = cols[k];
-                if (b > a) pb = *(volatile int32_t *)&parent[b];
-            }
-            bool cand = pb >= 0;
-            unsigned cmask = __ballot_sync(0xffffffffu, cand);
-            if (!cmask) continue;
-            if (seen + __popc(cmask) > max_edges) {  // keep only the first edges
-                const int keep = max_edges - seen;
-                unsigned m = cmask, kept = 0;
-                for (int i = 0; i < keep; ++i) { kept |= m & (0u - m); m &= m - 1; }
-                cmask = kept;
-                cand = (cmask >> lane) & 1u;
-            }
-            seen += __popc(cmask);
-            if (dirty) {
-                ra = uf_find(parent, a);
-                dirty = false;
-            }
-            int32_t rb = cand ? uf_find(parent, pb) : -1;
-            unsigned mask = __ballot_sync(0xffffffffu, cand && rb != ra);
-            while (mask) {
-                if (dirty) {
-                    ra = uf_find(parent, a);
-                    const bool live = (mask >> lane) & 1u;
-                    if (live) rb = uf_find(parent, rb);
-                    mask = __ballot_sync(0xffffffffu, live && rb != ra);
-                    dirty = false;
-                    if (!mask) break;
-                }
-                const int src = __ffs(mask) - 1;
-                mask &= mask - 1;
-                const int32_t bb = __shfl_sync(0xffffffffu, b, src);
-                bool ok;
-                if (needed <= 0) {
-                    ok = needed == 0;
-                } else {
-                    const int64_t bs = row_off[bb];
-                    const int32_t lb = (int32_t)(row_off[bb + 1] - bs);
-                    ok = warp_shares_at_least(A, la, cols + bs, lb, needed, lane);
-                    ++n_checks;
-                }
-                if (ok) {
-                    if (lane == 0) uf_unite(parent, a, bb);
-                    __syncwarp();
-                    ++n_acc;
-                    dirty = true;
-                }
-            }
-        }
-    }
-    if (lane == 0 && n_checks) atomicAdd(&counters[5], n_checks);
-    if (lane == 0 && n_acc) atomicAdd(&counters[6], n_acc);
-}
-
-// Full path compression and per-component minimum point index.
-__global__ void root_min_kernel(int64_t n, const uint8_t *__restrict__ node, int32_t *__restrict__ parent,
-                                const int32_t *__restrict__ perm, int32_t *__restrict__ comp_min) {
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        if (!node[p]) continue;
-        const int32_t r = uf_find(parent, (int32_t)p);
-        atomicMin(&comp_min[r], perm[p]);
-    }
-}
-
-__global__ void root_store_kernel(int64_t n, const uint8_t *__restrict__ node, int32_t *__restrict__ parent) {
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        if (!node[p]) continue;
-        parent[p] = uf_find(parent, (int32_t)p);
-    }
-}
-
-__global__ void min_flag_kernel(int64_t n, const uint8_t *__restrict__ node, const int32_t *__restrict__ parent,
-                                const int32_t *__restrict__ comp_min, int32_t *__restrict__ flag) {
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        if (!node[p]) continue;
-        if (parent[p] == (int32_t)p) flag[comp_min[p]] = 1;
-    }
-}
-
-__global__ void label_kernel(int64_t n, const uint8_t *__restrict__ node, const int32_t *__restrict__ parent,
-                             const int32_t *__restrict__ comp_min, const int32_t *__restrict__ perm,
-                             const int64_t *__restrict__ rank, int64_t current_start, int64_t *__restrict__ labels) {
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        if (!node[p]) continue;
-        const int32_t m = comp_min[parent[p]];
-        labels[perm[p]] = current_start + rank[m];
-    }
-}
 
 // ---- sort_by_size ---------------------------------------------------------
 __global__ void label_range_kernel(const int64_t *__restrict__ labels, int64_t n, long long *__restrict__ out) {

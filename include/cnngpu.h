@@ -175,6 +175,38 @@ CNN_API cnn_status cnn_check_lists(cnn_context *ctx, const int32_t *a, int64_t n
                                    const int32_t *b, int64_t nb, int64_t c, int32_t *result,
                                    cnn_memspace mem);
 
+/* ---------------------------------------------------------------------
+ * Fit without device memory allocation.  This entry point has no
+ * counterpart in the reference.
+ *
+ * For callers that must not allocate device memory while they run: a
+ * serving loop whose memory budget is fixed at start-up, a plug-in inside
+ * a framework whose caching allocator already holds the free memory, or a
+ * latency-critical loop that cannot afford cudaMalloc/cudaFree (either may
+ * synchronise the whole device).  The caller passes inputs and outputs;
+ * the only other memory used is a fixed scratch block compiled into the
+ * library (about 1.9 MB per GPU, held by every GPU that loads the library
+ * until the process exits).
+ *
+ * Same result as cnn_set_neighbours + cnn_fit on the same graph.  All
+ * pointers are device pointers; rows of `indices` must be ascending and the
+ * neighbour relation symmetric (as produced by cnn_get_neighbours).  Work
+ * is queued on `stream` (a cudaStream_t, NULL = legacy default stream) on
+ * the current device; the call returns before it finishes.
+ *
+ * Limits and sharing: n_points above CNN_NOALLOC_MAX_POINTS returns
+ * CNN_ERR_INVALID_ARG without touching the GPU.  All calls share the one
+ * scratch block, so calls whose GPU work overlaps (other streams, other
+ * host threads) race and must be serialised by the caller.  The first call
+ * on a device looks up the scratch block's device address once (with that
+ * device current); make that first call before any stream capture. */
+#define CNN_NOALLOC_MAX_POINTS 65536
+
+CNN_API cnn_status cnn_fit_csr_noalloc(const int64_t *offsets, const int32_t *indices,
+                                       int64_t n_points, int64_t similarity_cutoff,
+                                       int64_t n_member_cutoff, int64_t current_start,
+                                       uint8_t *consider, int64_t *labels, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
