@@ -36,6 +36,124 @@ namespace cnn {
 
 namespace {
 
+// candidate edges each node checks in the hook pass
+#ifndef CNN_HOOK_EDGES
+#define CNN_HOOK_EDGES 2
+#endif
+constexpr int32_t kHookEdges = CNN_HOOK_EDGES;
+
+// ---- cross-edge worklist ------------------------------------------------------
+// After the hook pass and a full compression, parent[] holds every node's
+// root.  A read-only pass streams the graph and keeps only candidate edges
+// (a, b > a, both nodes) whose roots differ; everything else is already
+// joined.  The worklist is then checked edge by edge with the same lazy
+// rule.  If it overflows its capacity, the full lazy pass runs instead.
+__global__ void __launch_bounds__(256) cross_filter_kernel(int64_t n, const int64_t *__restrict__ row_off,
+                                                           const int32_t *__restrict__ cols,
+                                                           const int32_t *__restrict__ parent,
+                                                           int2 *__restrict__ wl,
+                                                           unsigned long long *__restrict__ wl_count,
+                                                           int64_t cap) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t a64 = warp0; a64 < n; a64 += nwarps) {
+        const int32_t a = (int32_t)a64;
+        const int32_t pa = parent[a];
+        if (pa < 0) continue;
+        const int64_t s = row_off[a], e = row_off[a + 1];
+        for (int64_t k0 = s; k0 < e; k0 += 32) {
+            const int64_t k = k0 + lane;
+            int32_t b = -1, pb = -1;
+            if (k < e) {
+                b = cols[k];
+                if (b > a) pb = parent[b];
+            }
+            const bool cross = pb >= 0 && pb != pa;
+            const unsigned mask = __ballot_sync(0xffffffffu, cross);
+            if (!mask) continue;
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(wl_count, (unsigned long long)__popc(mask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            const unsigned long long idx = base + __popc(mask & lt);
+            if (cross && idx < (unsigned long long)cap) wl[idx] = make_int2(a, b);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) edge_check_kernel(const int2 *__restrict__ wl,
+                                                         const unsigned long long *__restrict__ wl_count,
+                                                         int64_t cap, const int64_t *__restrict__ row_off,
+                                                         const int32_t *__restrict__ cols,
+                                                         int32_t *__restrict__ parent, int32_t needed,
+                                                         unsigned long long *__restrict__ counters) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const unsigned long long total = *wl_count;
+    if (total > (unsigned long long)cap) return;  // overflow: the full lazy pass runs instead
+    const int64_t count = (int64_t)total;
+    unsigned long long n_checks = 0, n_acc = 0;
+    for (int64_t base = warp0 * 32; base < count; base += nwarps * 32) {
+        const int64_t e = base + lane;
+        const bool valid = e < count;
+        int32_t a = -1, b = -1, ra = -1, rb = -1;
+        if (valid) {
+            const int2 ed = wl[e];
+            a = ed.x;
+            b = ed.y;
+            ra = uf_find(parent, a);
+            rb = uf_find(parent, b);
+        }
+        unsigned mask = __ballot_sync(0xffffffffu, valid && ra != rb);
+        bool dirty = false;
+        while (mask) {
+            if (dirty) {
+                const bool live = (mask >> lane) & 1u;
+                if (live) {
+                    ra = uf_find(parent, ra);
+                    rb = uf_find(parent, rb);
+                }
+                mask = __ballot_sync(0xffffffffu, live && ra != rb);
+                dirty = false;
+                if (!mask) break;
+            }
+            const int src = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const int32_t aa = __shfl_sync(0xffffffffu, a, src);
+            const int32_t bb = __shfl_sync(0xffffffffu, b, src);
+            bool ok;
+            if (needed <= 0) {
+                ok = needed == 0;
+            } else {
+                const int64_t as = row_off[aa], bs = row_off[bb];
+                ok = warp_shares_at_least(cols + as, (int32_t)(row_off[aa + 1] - as), cols + bs,
+                                          (int32_t)(row_off[bb + 1] - bs), needed, lane);
+                ++n_checks;
+            }
+            if (ok) {
+                if (lane == 0) uf_unite(parent, aa, bb);
+                __syncwarp();
+                ++n_acc;
+                dirty = true;
+            }
+        }
+    }
+    if (lane == 0 && n_checks) atomicAdd(&counters[5], n_checks);
+    if (lane == 0 && n_acc) atomicAdd(&counters[6], n_acc);
+}
+
+// The full lazy pass, run only when the worklist overflowed.
+__global__ void __launch_bounds__(kCheckWarps * 32) check_union_if_overflow_kernel(
+    int64_t n, const int64_t *__restrict__ row_off, const int32_t *__restrict__ cols, int32_t *__restrict__ parent,
+    int32_t needed, const unsigned long long *__restrict__ wl_count, int64_t cap,
+    unsigned long long *__restrict__ counters) {
+    if (*wl_count <= (unsigned long long)cap) return;
+    // same body as the full pass of check_union_kernel
+    check_union_body(n, row_off, cols, parent, needed, INT32_MAX, counters);
+}
+
 // ---- sort_by_size ---------------------------------------------------------
 __global__ void label_range_kernel(const int64_t *__restrict__ labels, int64_t n, long long *__restrict__ out) {
     long long lo = LLONG_MAX, hi = LLONG_MIN;
@@ -190,7 +308,7 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     CNN_TRY(ctx->ensure(ctx->flag, sizeof(int32_t) * (size_t)(n + 1)));
     CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(int64_t) * (size_t)(n + 1)));
     unsigned long long *counters = ctx->counters.as<unsigned long long>();
-    CNN_CUDA(ctx, cudaMemsetAsync(counters + 4, 0, 4 * sizeof(unsigned long long), st));
+    CNN_CUDA(ctx, cudaMemsetAsync(counters + 4, 0, 5 * sizeof(unsigned long long), st));
     uint8_t *node = ctx->node.as<uint8_t>();
     int32_t *parent = ctx->parent.as<int32_t>();
     int32_t *comp_min = ctx->comp_min.as<int32_t>();
@@ -207,12 +325,25 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     // the full pass, where edges inside already joined sets cost one load
     const unsigned check_blocks = std::min<unsigned>(grid_for(n, kCheckWarps), 152u * 8u);
     check_union_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(
-        n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff, 2, counters);
+        n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff, kHookEdges,
+        counters);
     CNN_LAUNCH_CHECK(ctx);
     root_store_kernel<<<blocks_for(n), 256, 0, st>>>(n, node, parent);
     CNN_LAUNCH_CHECK(ctx);
-    check_union_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(
-        n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff, INT32_MAX,
+    // cross edges between the hooked sets -> worklist -> checks
+    const int64_t wl_cap = std::max<int64_t>(int64_t(1) << 20, ctx->nnz / 16);
+    CNN_TRY(ctx->ensure(ctx->io_c, sizeof(int2) * (size_t)wl_cap));
+    unsigned long long *wl_count = counters + 8;
+    CNN_CUDA(ctx, cudaMemsetAsync(wl_count, 0, sizeof(unsigned long long), st));
+    cross_filter_kernel<<<check_blocks, 256, 0, st>>>(n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent,
+                                                      ctx->io_c.as<int2>(), wl_count, wl_cap);
+    CNN_LAUNCH_CHECK(ctx);
+    edge_check_kernel<<<check_blocks, 256, 0, st>>>(ctx->io_c.as<int2>(), wl_count, wl_cap, ctx->row_off.as<int64_t>(),
+                                                    ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff,
+                                                    counters);
+    CNN_LAUNCH_CHECK(ctx);
+    check_union_if_overflow_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(
+        n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff, wl_count, wl_cap,
         counters);
     CNN_LAUNCH_CHECK(ctx);
     stage_end(ctx, 6);

@@ -91,7 +91,7 @@ __global__ void node_kernel(const int32_t *__restrict__ deg, const int32_t *__re
 // this warp joined something: a stale "different" only costs an extra
 // check, never a wrong skip.  max_edges bounds the candidate edges one node
 // examines (the hook pass uses 2).
-__global__ void __launch_bounds__(kCheckWarps * 32) check_union_kernel(
+__device__ __forceinline__ void check_union_body(
     int64_t n, const int64_t *__restrict__ row_off, const int32_t *__restrict__ cols,
     int32_t *__restrict__ parent, int32_t needed, int32_t max_edges,
     unsigned long long *__restrict__ counters) {
@@ -164,6 +164,13 @@ __global__ void __launch_bounds__(kCheckWarps * 32) check_union_kernel(
     }
     if (lane == 0 && n_checks) atomicAdd(&counters[5], n_checks);
     if (lane == 0 && n_acc) atomicAdd(&counters[6], n_acc);
+}
+
+__global__ void __launch_bounds__(kCheckWarps * 32) check_union_kernel(
+    int64_t n, const int64_t *__restrict__ row_off, const int32_t *__restrict__ cols,
+    int32_t *__restrict__ parent, int32_t needed, int32_t max_edges,
+    unsigned long long *__restrict__ counters) {
+    check_union_body(n, row_off, cols, parent, needed, max_edges, counters);
 }
 
 // Full path compression and per-component minimum point index.

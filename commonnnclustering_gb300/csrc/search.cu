@@ -240,7 +240,9 @@ __global__ void __launch_bounds__(kGridWarps * 32) grid_search_kernel(
     const int32_t total = s_cum[nruns];
 
     // this warp's queries: kQueriesPerWarp consecutive ones, so that short
-    // items leave whole warps idle instead of spreading one query per warp
+    // items leave whole warps idle instead of spreading one query per warp.
+    // Missing queries get +inf coordinates: they never match and are never
+    // ambiguous, so the inner loop needs no per-query branch.
     int64_t q[kQueriesPerWarp];
     float4 qf[kQueriesPerWarp];
     int64_t wpos[kQueriesPerWarp];
@@ -249,7 +251,7 @@ __global__ void __launch_bounds__(kGridWarps * 32) grid_search_kernel(
     for (int k = 0; k < kQueriesPerWarp; ++k) {
         q[k] = q0 + (int64_t)wid * kQueriesPerWarp + k;
         const bool ok = q[k] < qend;
-        qf[k] = ok ? xf4[q[k]] : make_float4(0.f, 0.f, 0.f, 0.f);
+        qf[k] = ok ? xf4[q[k]] : make_float4(INFINITY, INFINITY, INFINITY, 0.f);
         wpos[k] = (kFill && ok) ? row_off[q[k]] : 0;
         cnt[k] = 0;
         if (!ok) q[k] = -1;
@@ -261,44 +263,59 @@ __global__ void __launch_bounds__(kGridWarps * 32) grid_search_kernel(
         const int32_t tlen = min(kGridTile, total - t0);
         const int32_t tpad = (tlen + 31) & ~31;
         __syncthreads();
-        for (int32_t t = threadIdx.x; t < tpad; t += blockDim.x) {
-            if (t < tlen) {
-                const int32_t pos = t0 + t;
-                int r = 0;
-                while (r + 1 < nruns && s_cum[r + 1] <= pos) ++r;
+        // pack: warp w copies runs w, w+8, ... (their part inside this tile)
+        for (int r = wid; r < nruns; r += kGridWarps) {
+            const int32_t lo = max(s_cum[r], t0), hi = min(s_cum[r + 1], t0 + tlen);
+            for (int32_t pos = lo + lane; pos < hi; pos += 32) {
                 const int32_t j = (int32_t)(s_rs[r] + (pos - s_cum[r]));
-                s_j[t] = j;
-                s_xf[t] = xf4[j];
-            } else {  // padding: +inf is never within the radius
-                s_j[t] = -1;
-                s_xf[t] = make_float4(INFINITY, INFINITY, INFINITY, 0.f);
+                s_j[pos - t0] = j;
+                s_xf[pos - t0] = xf4[j];
             }
+        }
+        for (int32_t t = tlen + threadIdx.x; t < tpad; t += blockDim.x) {  // +inf never matches
+            s_j[t] = -1;
+            s_xf[t] = make_float4(INFINITY, INFINITY, INFINITY, 0.f);
         }
         __syncthreads();
         if (!warp_has_work) continue;
         for (int32_t c0 = 0; c0 < tpad; c0 += 32) {
             const int32_t t = c0 + lane;
             const float4 cf = s_xf[t];
+            bool in[kQueriesPerWarp], amb[kQueriesPerWarp];
+            bool any_amb = false;
 #pragma unroll
             for (int k = 0; k < kQueriesPerWarp; ++k) {
-                if (q[k] < 0) break;  // warp-uniform; invalid queries come last
                 const float ex = qf[k].x - cf.x, ey = qf[k].y - cf.y, ez = qf[k].z - cf.z;
                 const float sf = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
-                bool in = sf <= sp.thr_in;
-                const bool amb = !in && sf <= sp.thr_out;
-                if (__any_sync(0xffffffffu, amb)) {  // rare: decide in float64
-                    if (amb) {
-                        in = exact_rows(x, d, perm[q[k]], perm[s_j[t]], sp);
+                in[k] = sf <= sp.thr_in;
+                amb[k] = !in[k] && sf <= sp.thr_out;
+                any_amb |= amb[k];
+            }
+            if (__any_sync(0xffffffffu, any_amb)) {  // rare: decide those pairs in float64
+#pragma unroll
+                for (int k = 0; k < kQueriesPerWarp; ++k) {
+                    if (amb[k]) {
+                        in[k] = exact_rows(x, d, perm[q[k]], perm[s_j[t]], sp);
                         ++n_exact;
                     }
                 }
-                const unsigned hit = __ballot_sync(0xffffffffu, in);
-                if (kFill && in) cols[wpos[k] + cnt[k] + __popc(hit & lt)] = s_j[t];
-                cnt[k] += __popc(hit);
+            }
+#pragma unroll
+            for (int k = 0; k < kQueriesPerWarp; ++k) {
+                if (kFill) {
+                    const unsigned hit = __ballot_sync(0xffffffffu, in[k]);
+                    if (in[k]) cols[wpos[k] + cnt[k] + __popc(hit & lt)] = s_j[t];
+                    cnt[k] += __popc(hit);
+                } else {
+                    cnt[k] += in[k];  // per-lane count, summed over the warp at the end
+                }
             }
         }
     }
     if (!kFill) {
+#pragma unroll
+        for (int k = 0; k < kQueriesPerWarp; ++k)
+            for (int o = 16; o > 0; o >>= 1) cnt[k] += __shfl_down_sync(0xffffffffu, cnt[k], o);
         if (lane == 0) {
 #pragma unroll
             for (int k = 0; k < kQueriesPerWarp; ++k)
