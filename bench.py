@@ -42,7 +42,18 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = dict(name="md3d-200k", n=200_000, d=3, radius_cutoff=0.1, cnn_cutoff=10, member_cutoff=50)
+WORKLOADS = {
+    # the headline workload: 200,000 x 3, cell-grid search
+    "md3d-200k": dict(name="md3d-200k", n=200_000, d=3, radius_cutoff=0.1, cnn_cutoff=10, member_cutoff=50,
+                      gen=("md3d", {})),
+    # 5,000 x 2 blobs (the reference's own brute-force recipe is timed beside it)
+    "blobs2d-5k": dict(name="blobs2d-5k", n=5000, d=2, radius_cutoff=0.3, cnn_cutoff=5, member_cutoff=10,
+                       gen=("blobs2d", {})),
+    # 500,000 x 64 feature vectors, tensor-core Gram search (mean degree ~100)
+    "features-500k-d64": dict(name="features-500k-d64", n=500_000, d=64, radius_cutoff=2.9, cnn_cutoff=8,
+                              member_cutoff=None, gen=("features", {})),
+}
+WORKLOAD = WORKLOADS["md3d-200k"]
 METRIC = "CommonNN fit points/s (bit-exact labels)"
 UNIT = "points/s"
 
@@ -126,12 +137,31 @@ class ClockSampler:
 
 def make_points():
     from commonnnclustering_gb300 import workloads
-    return workloads.md3d(n=WORKLOAD["n"])
+    name, kw = WORKLOAD["gen"]
+    return getattr(workloads, name)(n=WORKLOAD["n"], **kw)
 
 
 def roofline_entry(stats_list, nnz, n, peaks):
     """Dominant kernel by mean stage time; algorithmic bytes per launch."""
     d = WORKLOAD["d"]
+    if d >= 16:  # tensor-core Gram kernel: useful FLOPs (upper triangle, 128-row tiles) per launch
+        ms = statistics.mean(s["ms_gram"] for s in stats_list)
+        nblk = (n + 127) // 128
+        pairs = nblk * (nblk + 1) // 2 * 128 * 128
+        dp = (d + 63) // 64 * 64
+        useful = 2.0 * pairs * dp
+        issued = 3.0 * useful  # BF16x3: hi.hi + hi.lo + lo.hi
+        peak = peaks.get("bf16_tflops")
+        achieved = issued / (ms * 1e-3) / 1e12 if ms > 0 else None
+        return {
+            "kernel": "gram_search_kernel (tcgen05 BF16x3)", "bound": "tensor", "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": (achieved / peak) if (achieved and peak) else None, "traffic": None,
+            "algorithmic_flops_issued": issued, "algorithmic_flops_useful": useful,
+            "useful_tflops": useful / (ms * 1e-3) / 1e12 if ms > 0 else None, "ms_per_launch": ms,
+            "peak_source": "MEASURED_PEAKS.json bf16_tflops (measured burst)" if peak else "fallback",
+            "stage_ms": {k: round(statistics.mean(s[k] for s in stats_list), 4)
+                         for k in ("ms_count", "ms_gram", "ms_check", "ms_label", "ms_sort")},
+        }
     stages = {
         # stage -> (kernel name, algorithmic bytes per launch)
         "ms_fill": ("grid_search_kernel<fill>", n * d * 8 + 4 * nnz + 8 * (n + 1)),
@@ -167,6 +197,30 @@ def roofline_entry(stats_list, nnz, n, peaks):
 def cpu_baseline(x, budget_s=25.0):
     from oracle import cnn_oracle
     W = WORKLOAD
+    if W["d"] >= 16:
+        # all-pairs float64 rows on 1 thread for a sample of query points; the
+        # full fit would take hours, so the rate is per query row, stated as such
+        rng = np.random.default_rng(0)
+        k = 64
+        idx = rng.choice(x.shape[0], k, replace=False)
+        t = time.perf_counter()
+        r2 = W["radius_cutoff"] ** 2
+        for i in idx:
+            cnn_oracle.neighbour_row(x, int(i), r2)
+        dt = time.perf_counter() - t
+        per_row = dt / k
+        return {"value": 1.0 / per_row, "unit": "query rows/s (neighbour search only)", "cores": 1, "kind": "port",
+                "sample": f"{k} brute-force float64 neighbour rows of {W['name']} against all {x.shape[0]} points "
+                          f"(oracle restatement of the reference getter), {dt:.1f} s; a full fit needs "
+                          f"{x.shape[0]} rows (~{per_row * x.shape[0] / 3600:.1f} h on 1 thread)"}
+    if W["name"] == "blobs2d-5k":
+        t = time.perf_counter()
+        cnn_oracle.clustering_fit(x, W["radius_cutoff"], W["cnn_cutoff"], member_cutoff=W["member_cutoff"],
+                                  brute_force=True)
+        dt = time.perf_counter() - t
+        return {"value": W["n"] / dt, "unit": UNIT, "cores": 1, "kind": "port",
+                "sample": f"1 full fit of {W['name']} with the reference's default recipe restated "
+                          f"(brute-force getter per query + BFS), {dt:.2f} s"}
     t0 = time.perf_counter()
     times = []
     while True:
@@ -202,6 +256,7 @@ def run_gpu(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     r2 = W["radius_cutoff"] ** 2
     sc, nm = W["cnn_cutoff"] + 2, W["cnn_cutoff"] + 1
+    sort_cutoff = W["member_cutoff"] if W["member_cutoff"] is not None else 2  # Labels.sort_by_size default
     torch.cuda.synchronize()
 
     def step():
@@ -211,7 +266,7 @@ def run_gpu(args):
         ctx.set_points(xt)
         ctx.build_neighbours(r2)
         ctx.fit(sc, nm, 1, consider, labels)
-        ctx.sort_by_size(labels, W["member_cutoff"], None)
+        ctx.sort_by_size(labels, sort_cutoff, None)
 
     for _ in range(args.warmup):
         step()
@@ -252,7 +307,7 @@ def run_gpu(args):
         e2e_ctx.set_points(x_host)
         e2e_ctx.build_neighbours(r2)
         e2e_ctx.fit(sc, nm, 1, con_host, lab_host)
-        e2e_ctx.sort_by_size(lab_host, W["member_cutoff"], None)
+        e2e_ctx.sort_by_size(lab_host, sort_cutoff, None)
 
     for _ in range(max(1, args.warmup)):
         e2e_step()
@@ -292,7 +347,8 @@ def run_gpu(args):
         "roofline": roofline_entry(stats_list, nnz, n, peaks),
         "wall_s_timed_region": t_wall,
         "fit_stats": {k: stats_list[-1][k] for k in ("n_nodes", "n_checks", "n_accepted", "n_exact",
-                                                     "n_candidates", "n_clusters", "filter_band")},
+                                                     "n_candidates", "n_clusters", "filter_band", "max_abs_err",
+                                                     "search_kind")},
     }
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(x)
@@ -308,6 +364,25 @@ def run_reference(args):
     x = make_points()
     n = x.shape[0]
     cores = max(1, len(os.sched_getaffinity(0)))
+    if W["d"] >= 16:
+        # the reference's brute-force getter over all pairs is hours per fit
+        # here; each step times a bounded sample of query rows on all cores
+        base = cpu_baseline(x)
+        rows_per_s = base["value"] * cores
+        line = {
+            "impl": "reference", "metric": METRIC, "value": rows_per_s, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / rows_per_s,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded features generator)",
+            "config": {"workload": W["name"], "n_points": n, "n_dim": W["d"], "radius_cutoff": W["radius_cutoff"],
+                       "cnn_cutoff": W["cnn_cutoff"]},
+            "cpu_baseline": {"value": rows_per_s, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": base["sample"] + f"; scaled to {cores} threads; neighbour search only "
+                                       "(an upper bound on the fit rate)"},
+            "e2e": {"value": rows_per_s, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line), flush=True)
+        return
 
     def step():
         cnn_oracle.clustering_fit(x, W["radius_cutoff"], W["cnn_cutoff"], member_cutoff=W["member_cutoff"],
@@ -343,7 +418,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="md3d-200k", choices=sorted(WORKLOADS))
     args = ap.parse_args()
+    global WORKLOAD
+    WORKLOAD = WORKLOADS[args.workload]
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.impl == "reference":

@@ -48,7 +48,7 @@ class cnn_stats(ctypes.Structure):
         ("ms_bbox", ctypes.c_float), ("ms_cells", ctypes.c_float), ("ms_count", ctypes.c_float),
         ("ms_scan", ctypes.c_float), ("ms_fill", ctypes.c_float), ("ms_nodes", ctypes.c_float),
         ("ms_check", ctypes.c_float), ("ms_label", ctypes.c_float), ("ms_sort", ctypes.c_float),
-        ("n_launches", ctypes.c_int64),
+        ("n_launches", ctypes.c_int64), ("ms_gram", ctypes.c_float), ("max_abs_err", ctypes.c_float),
     ]
 
     def as_dict(self):

@@ -99,7 +99,8 @@ CNN_API cnn_status cnn_destroy(cnn_context *ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     cnn::DevBuf *bufs[] = {&ctx->x_own, &ctx->x_f32_stage, &ctx->perm, &ctx->inv, &ctx->deg, &ctx->row_off,
                            &ctx->cols, &ctx->xf4, &ctx->cell_of, &ctx->cell_start, &ctx->node, &ctx->parent,
-                           &ctx->comp_min, &ctx->flag, &ctx->counters, &ctx->stage_labels,
+                           &ctx->comp_min, &ctx->flag, &ctx->counters, &ctx->stage_labels, &ctx->gram_hi,
+                           &ctx->gram_lo, &ctx->gram_aux, &ctx->gram_keys, &ctx->gram_amb,
                            &ctx->stage_consider, &ctx->stage_offsets, &ctx->stage_indices, &ctx->stage_misc,
                            &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->scratch_a, &ctx->scratch_b,
                            &ctx->scratch_c, &ctx->scratch_d, &ctx->scan_tmp};
@@ -151,7 +152,7 @@ CNN_API cnn_status cnn_get_stats(const cnn_context *cctx, cnn_stats *out) {
     float *slot_field[cnn_context::kSlots] = {
         &ctx->stats.ms_bbox, &ctx->stats.ms_cells, &ctx->stats.ms_count, &ctx->stats.ms_scan,
         &ctx->stats.ms_fill, &ctx->stats.ms_nodes, &ctx->stats.ms_check, &ctx->stats.ms_label,
-        &ctx->stats.ms_sort, nullptr, nullptr, nullptr};
+        &ctx->stats.ms_sort, &ctx->stats.ms_gram, nullptr, nullptr};
     for (int i = 0; i < cnn_context::kSlots; ++i) {
         if (!ctx->slot_pending[i] || !slot_field[i]) continue;
         float ms = 0.f;

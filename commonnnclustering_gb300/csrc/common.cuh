@@ -89,6 +89,10 @@ struct cnn_context {
     cnn::DevBuf cell_of;  // int32[n] cell id per point (original order)
     cnn::DevBuf cell_start;  // int32[ncells+2]
 
+    // tensor-core (Gram) search for n_dim >= 16
+    cnn::DevBuf gram_hi, gram_lo, gram_aux, gram_keys, gram_amb;
+    int64_t gram_key_hint = 0;
+
     // fit work arrays
     cnn::DevBuf node;     // uint8[n]
     cnn::DevBuf parent;   // int32[n]
@@ -150,6 +154,9 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
 cnn_status export_neighbours_impl(cnn_context *ctx, int64_t *offsets_dev, int32_t *indices_dev);
 cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev,
                                const int32_t *indices_dev, int64_t n);
+
+// gram.cu: tensor-core search (n_dim >= 16); *used = false when it declined
+cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode, bool *used);
 
 // fit.cu
 cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,

@@ -103,13 +103,16 @@ typedef struct cnn_stats {
     int64_t n_exact;          /* candidate pairs decided in float64 */
     int64_t n_candidates;     /* candidate pairs tested by the search */
     int64_t n_clusters;       /* clusters found by the last fit */
-    int32_t search_kind;      /* 1 = cell grid (d <= 3), 2 = tiled all-pairs */
+    int32_t search_kind;      /* 1 = cell grid (d <= 3), 2 = tiled all-pairs float32,
+                                 3 = tensor-core Gram (d >= 16), 0 = precomputed */
     int32_t filter_enabled;   /* 1 when the float32 prefilter was usable */
     double filter_band;       /* half-width of the float64 recheck band on d^2 */
     float ms_bbox, ms_cells, ms_count, ms_scan, ms_fill;   /* neighbour build */
     float ms_nodes, ms_check, ms_label;                    /* fit */
     float ms_sort;                                         /* sort_by_size */
     int64_t n_launches;       /* kernels launched by this context since creation */
+    float ms_gram;            /* tensor-core distance kernel alone (n_dim >= 16) */
+    float max_abs_err;        /* max |d^2 tensor-core - d^2 float64| over rechecked pairs */
 } cnn_stats;
 
 CNN_API int cnn_abi_version(void);

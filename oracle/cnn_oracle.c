@@ -157,6 +157,18 @@ int oracle_neighbour_fill(const double *x, int64_t n, int32_t d, double radius_c
     return run_rows(nb_fill_worker, &t, nthreads);
 }
 
+/* One query row by brute force (_types.pyx:1692-1710 for a single index):
+ * writes the ascending indices i with predicate(query, x_i) into out and
+ * returns their number. */
+int64_t oracle_neighbour_row(const double *x, int64_t n, int32_t d, const double *query,
+                             double radius_cutoff, int metric, int fpmode, int32_t *out)
+{
+    int64_t c = 0;
+    for (int64_t i = 0; i < n; ++i)
+        if (oracle_in_radius(query, x + i * d, d, radius_cutoff, metric, fpmode)) out[c++] = (int32_t)i;
+    return c;
+}
+
 /* ------------------------------------------------------------------ */
 /* Similarity check: two-pointer merge with early exit.                */
 /* ------------------------------------------------------------------ */

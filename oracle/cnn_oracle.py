@@ -51,6 +51,8 @@ def lib():
             f = getattr(L, name)
             f.restype = i
             f.argtypes = [p, i64, i32, dbl, i, i, i, p, p]
+        L.oracle_neighbour_row.restype = i64
+        L.oracle_neighbour_row.argtypes = [p, i64, i32, p, dbl, i, i, p]
         L.oracle_check_sorted.restype = i
         L.oracle_check_sorted.argtypes = [p, i64, p, i64, i64]
         L.oracle_count_common_sorted.restype = i64
@@ -104,6 +106,17 @@ def neighbourhoods(x, radius_cutoff: float, metric=METRIC_EUCLIDEAN_REDUCED,
     if ff(_ptr(x), n, d, float(radius_cutoff), metric, fpmode, nt, _ptr(offsets), _ptr(indices)) != 0:
         raise MemoryError("oracle neighbour fill failed")
     return offsets, indices
+
+
+def neighbour_row(x, i: int, radius_cutoff: float, metric=METRIC_EUCLIDEAN_REDUCED,
+                  fpmode=FP_SEPARATE) -> np.ndarray:
+    """Ascending neighbour indices of point i (self included), brute force."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    n, d = x.shape
+    q = np.ascontiguousarray(x[i], dtype=np.float64)
+    out = np.empty(n, dtype=np.int32)
+    c = lib().oracle_neighbour_row(_ptr(x), n, d, _ptr(q), float(radius_cutoff), metric, fpmode, _ptr(out))
+    return out[:c].copy()
 
 
 def check_sorted(a, b, c: int) -> bool:

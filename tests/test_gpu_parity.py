@@ -256,3 +256,28 @@ def test_errors_are_reported(cnn):
         ctx.fit(2, 1, 1, np.ones(3, dtype=np.uint8), np.zeros(3, dtype=np.int64))  # no graph yet
     with pytest.raises(cnn.CNNError):
         ctx.set_neighbours(np.array([0, 2, 3], dtype=np.int64), np.array([0, 5, 1], dtype=np.int32))
+
+
+@pytest.mark.parametrize("d", [16, 64])
+def test_tensor_core_search_against_oracle(cnn, oracle, d):
+    """n_dim >= 16 takes the tcgen05 Gram path; the CSR must equal the oracle's."""
+    from commonnnclustering_gb300 import workloads
+    x = workloads.features(n=12000, d=d, seed=31, n_clusters=12)
+    rng = np.random.default_rng(5)
+    sub = x[rng.choice(x.shape[0], 64, replace=False)]
+    dd = np.sort(((sub[:, None, :] - x[None]) ** 2).sum(-1), axis=1)[:, 60]
+    r2 = float(np.median(dd))
+    for fpmode in (0, 1):
+        want = oracle.neighbourhoods(x, r2, fpmode=fpmode, grid=False)
+        off, idx, st = gpu_csr(cnn, x, r2, fpmode=fpmode)
+        assert st["search_kind"] == 3, st
+        assert np.array_equal(off, want[0]) and np.array_equal(idx, want[1])
+
+
+def test_tensor_core_fit_labels(cnn, oracle):
+    from commonnnclustering_gb300 import workloads
+    x = workloads.features(n=8000, d=64, seed=32, n_clusters=8)
+    want, info = oracle.clustering_fit(x, 3.1, 5)
+    cl = cnn.Clustering(x)
+    cl.fit(3.1, 5, v=False)
+    assert np.array_equal(np.asarray(cl.labels), want)
