@@ -52,6 +52,17 @@ WORKLOADS = {
     # 500,000 x 64 feature vectors, tensor-core Gram search (mean degree ~100)
     "features-500k-d64": dict(name="features-500k-d64", n=500_000, d=64, radius_cutoff=2.9, cnn_cutoff=8,
                               member_cutoff=None, gen=("features", {})),
+    # 1,000,000 x 3 float32 nested blobs: 8 radii x 8 cnn_cutoffs in one batched sweep
+    "nested3d-1m-sweep": dict(name="nested3d-1m-sweep", n=1_000_000, d=3, radius_cutoff=0.15, cnn_cutoff=None,
+                              member_cutoff=None, gen=("nested3d", {}), kind="sweep",
+                              radii=[float(r) for r in np.linspace(0.03, 0.15, 8)],
+                              cuts=[2, 5, 10, 20, 40, 80, 120, 160]),
+    # served request stream: Poisson arrivals of jobs of uneven size and dimension
+    "serve-stream": dict(name="serve-stream", n=None, d=None, radius_cutoff=None, cnn_cutoff=None,
+                         member_cutoff=10, gen=None, kind="serve", n_jobs=2000, rates=[10.0, 100.0, 500.0]),
+    # the same generator at 100,000 points (small enough for a full ncu capture)
+    "features-100k-d64": dict(name="features-100k-d64", n=100_000, d=64, radius_cutoff=2.9, cnn_cutoff=8,
+                              member_cutoff=None, gen=("features", {})),
 }
 WORKLOAD = WORKLOADS["md3d-200k"]
 METRIC = "CommonNN fit points/s (bit-exact labels)"
@@ -355,6 +366,134 @@ def run_gpu(args):
     print(json.dumps(line), flush=True)
 
 
+def run_sweep(args):
+    """Batched sweep vs the same 64 fits run one by one (both on the GPU)."""
+    import torch
+    from commonnnclustering_gb300 import _abi
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    W = WORKLOAD
+    x = make_points()  # float32, widened exactly inside the library
+    n = x.shape[0]
+    radii, cuts = W["radii"], W["cuts"]
+    r2 = [r * r for r in radii]
+    cut_pairs = [(c + 2, c + 1) for c in cuts]
+    stream = torch.cuda.Stream(device=dev)
+    ctx = _abi.Context(local, stream=int(stream.cuda_stream))
+    xt = torch.from_numpy(x).to(dev)
+    out = torch.empty((len(radii), len(cuts), n), dtype=torch.int64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def batched():
+        ctx.set_points(xt)
+        ctx.sweep(r2, cut_pairs, member_cutoff=2, labels_out=out)
+
+    lab = torch.zeros(n, dtype=torch.int64, device=dev)
+    con = torch.ones(n, dtype=torch.uint8, device=dev)
+
+    def one_by_one(check=None):
+        for k, rr in enumerate(r2):
+            for j, (sc, nm) in enumerate(cut_pairs):
+                with torch.cuda.stream(stream):
+                    lab.zero_()
+                    con.fill_(1)
+                ctx.set_points(xt)
+                ctx.build_neighbours(rr)
+                ctx.fit(sc, nm, 1, con, lab)
+                ctx.sort_by_size(lab, 2, None)
+                if check is not None and not torch.equal(lab, check[k, j]):
+                    raise SystemExit(f"bench: sweep differs from the separate fit at r={radii[k]}, c={cuts[j]}")
+
+    def timed(fn, steps):
+        ts = []
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return statistics.mean(ts)
+
+    for _ in range(args.warmup):
+        batched()
+    one_by_one(check=out)  # also the parity check: every pair equals its separate fit
+    with ClockSampler(local) as clocks:
+        ms_batched = timed(batched, args.steps)
+        ms_plain = timed(one_by_one, max(1, min(args.steps, 2)))
+    fits = len(radii) * len(cuts)
+    st = ctx.stats()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": n * fits / (ms_batched * 1e-3), "unit": "points/s (summed over the fits)",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_batched,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded nested3d generator, float32-stored)",
+        "config": {"workload": W["name"], "n_points": n, "n_dim": 3, "radii": radii, "cnn_cutoffs": cuts,
+                   "member_cutoff": 2, "fits_per_step": fits, "l2": "flushed between steps (256 MiB write)",
+                   "largest_radius_pairs": st["n_nonzero"]},
+        "plain_one_by_one_ms": ms_plain, "speedup_vs_one_by_one": ms_plain / ms_batched,
+        "fits_per_s": fits / (ms_batched * 1e-3), "clocks": clocks.summary(),
+        "gpu_launches_per_step": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args):
+    """Served stream: continuous batching vs one job at a time, per arrival rate."""
+    import torch
+    from commonnnclustering_gb300 import serve, workloads
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    W = WORKLOAD
+    results = []
+    t_gen = time.perf_counter()
+    raw = workloads.job_stream(n_jobs=W["n_jobs"], rate=1.0, seed=11)
+    t_gen = time.perf_counter() - t_gen
+    # arrival gaps of the trace at rate 1; each rate rescales them
+    base = np.array([j["arrival"] for j in raw])
+    srv = serve.Server(n_slots=args.slots, device=local)
+    try:
+        # warm-up: every slot sees the largest jobs once (device workspaces grown)
+        big = sorted(raw, key=lambda j: -j["points"].shape[0] * j["points"].shape[1])[: 2 * args.slots]
+        srv.serve([serve.Job(job_id=-1 - i, **dict(j, arrival=0.0)) for i, j in enumerate(big)], realtime=False)
+        srv.done.clear()
+        for rate in W["rates"]:
+            n_jobs = W["n_jobs"] if rate >= 100 else min(W["n_jobs"], int(rate * 60))  # <= 60 s of arrivals
+            jobs = [serve.Job(job_id=i, **dict(raw[i], arrival=float(base[i] / rate))) for i in range(n_jobs)]
+            srv.done.clear()
+            srv.serve(jobs, realtime=True)
+            batched = serve.latency_summary(jobs)
+            plain_jobs = [serve.Job(job_id=i, **dict(raw[i], arrival=float(base[i] / rate))) for i in range(n_jobs)]
+            serve.serve_one_at_a_time(plain_jobs, device=local, realtime=True)
+            plain = serve.latency_summary(plain_jobs)
+            same = all(np.array_equal(a.labels, b.labels) for a, b in zip(jobs, plain_jobs))
+            results.append({"rate_jobs_per_s": rate, "jobs": n_jobs, "continuous_batching": batched,
+                            "one_at_a_time": plain, "identical_labels": same,
+                            "max_jobs_in_flight": srv.max_in_flight})
+    finally:
+        srv.close()
+    if rank != 0:
+        return
+    top = results[-1]
+    line = {
+        "metric": "served CommonNN fits: jobs/s and p50/p99 latency", "value": top["continuous_batching"]["jobs_per_s"],
+        "unit": "jobs/s", "n_gpus": world, "steps": len(results), "warmup": 1, "ms_per_step": None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded job stream: lognormal sizes, d in {2,3,16,64}, Poisson arrivals)",
+        "config": {"workload": W["name"], "n_jobs": W["n_jobs"], "rates": W["rates"], "slots": args.slots,
+                   "trace_generation_s": t_gen},
+        "per_rate": results,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -419,6 +558,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="md3d-200k", choices=sorted(WORKLOADS))
+    ap.add_argument("--slots", type=int, default=4, help="concurrent jobs of the served stream")
     args = ap.parse_args()
     global WORKLOAD
     WORKLOAD = WORKLOADS[args.workload]
@@ -426,6 +566,10 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif WORKLOAD.get("kind") == "sweep":
+        run_sweep(args)
+    elif WORKLOAD.get("kind") == "serve":
+        run_serve(args)
     else:
         run_gpu(args)
 

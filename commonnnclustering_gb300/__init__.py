@@ -18,6 +18,7 @@ from ._types import (ClusterParameters, DistanceGetterGPUMetric, InputData, Inpu
                      SimilarityCheckerGPU)
 from .cluster import Bundle, Clustering
 from .report import Record, Summary
+from .sweep import sweep
 
 __version__ = "0.1.0"
 
@@ -26,5 +27,5 @@ __all__ = [
     "ClusterParameters", "DistanceGetterGPUMetric", "InputData", "InputDataGPUComponents",
     "InputDataGPUNeighbourhoods", "Labels", "MetricGPUEuclidean", "MetricGPUEuclideanReduced",
     "NeighboursGetterGPUGrid", "NeighboursGetterGPULookup", "NeighboursGPU", "QueueGPUUnionFind",
-    "SimilarityCheckerGPU", "Bundle", "Clustering", "Record", "Summary",
+    "SimilarityCheckerGPU", "Bundle", "Clustering", "Record", "Summary", "sweep",
 ]

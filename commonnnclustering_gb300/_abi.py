@@ -77,6 +77,7 @@ SIGNATURES = {
     "cnn_sort_by_size": (_INT, [_P, _P, _I64, _I64, _I64, _INT]),
     "cnn_check_lists": (_INT, [_P, _P, _I64, _P, _I64, _I64, _P, _INT]),
     "cnn_fit_csr_noalloc": (_INT, [_P, _P, _I64, _I64, _I64, _I64, _P, _P, _P]),
+    "cnn_sweep": (_INT, [_P, _P, _I32, _P, _P, _I32, _INT, _INT, _I64, _I64, _P, _INT]),
 }
 
 _lib = None
@@ -230,6 +231,7 @@ class Context:
         self._check(self._lib.cnn_set_points(self._h, ctypes.c_void_p(ptr), DTYPE_F32 if dt == np.float32 else DTYPE_F64,
                                              int(shape[0]), int(shape[1]), mem), "cnn_set_points")
         self._points_ref = keep
+        self._n_points = int(shape[0])
         return shape
 
     def build_neighbours(self, radius_cutoff: float, metric: int = METRIC_EUCLIDEAN_REDUCED,
@@ -292,6 +294,31 @@ class Context:
             lp, mem, n = lab.ctypes.data, MEM_HOST, lab.shape[0]
         self._check(self._lib.cnn_sort_by_size(self._h, ctypes.c_void_p(lp), n, int(member_cutoff), mx, mem),
                     "cnn_sort_by_size")
+
+    def sweep(self, radius_cutoffs, cuts, member_cutoff: int = 2, max_clusters: Optional[int] = None,
+              metric: int = METRIC_EUCLIDEAN_REDUCED, fpmode: int = FP_SEPARATE, labels_out=None):
+        """Fits for every (radius, cut) pair on the current points.
+
+        radius_cutoffs: adjusted cutoffs, ascending.  cuts: sequence of
+        (similarity_cutoff, n_member_cutoff).  Returns labels of shape
+        [n_radii, n_cuts, n_points] (host numpy array unless a CUDA tensor
+        is given as labels_out).
+        """
+        rc = np.ascontiguousarray(radius_cutoffs, dtype=np.float64)
+        sc = np.ascontiguousarray([c[0] for c in cuts], dtype=np.int64)
+        nm = np.ascontiguousarray([c[1] for c in cuts], dtype=np.int64)
+        mx = -1 if max_clusters is None else int(max_clusters)
+        n = int(self._n_points)
+        if labels_out is not None and is_device_array(labels_out):
+            ptr, mem, out = device_pointer(labels_out, np.int64, writable=True), MEM_DEVICE, labels_out
+        else:
+            out = np.empty((rc.shape[0], sc.shape[0], n), dtype=np.int64)
+            ptr, mem = out.ctypes.data, MEM_HOST
+        self._check(self._lib.cnn_sweep(self._h, ctypes.c_void_p(rc.ctypes.data), rc.shape[0],
+                                        ctypes.c_void_p(sc.ctypes.data), ctypes.c_void_p(nm.ctypes.data),
+                                        sc.shape[0], int(metric), int(fpmode), int(member_cutoff), mx,
+                                        ctypes.c_void_p(ptr), mem), "cnn_sweep")
+        return out
 
     def check_lists(self, a, b, c: int) -> bool:
         a = host_array(a, np.int32)

@@ -101,6 +101,8 @@ CNN_API cnn_status cnn_destroy(cnn_context *ctx) {
                            &ctx->cols, &ctx->xf4, &ctx->cell_of, &ctx->cell_start, &ctx->node, &ctx->parent,
                            &ctx->comp_min, &ctx->flag, &ctx->counters, &ctx->stage_labels, &ctx->gram_hi,
                            &ctx->gram_lo, &ctx->gram_aux, &ctx->gram_keys, &ctx->gram_amb,
+                           &ctx->sweep_bucket, &ctx->sweep_row_off_max, &ctx->sweep_cols_max,
+                           &ctx->sweep_deg_max, &ctx->sweep_consider,
                            &ctx->stage_consider, &ctx->stage_offsets, &ctx->stage_indices, &ctx->stage_misc,
                            &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->scratch_a, &ctx->scratch_b,
                            &ctx->scratch_c, &ctx->scratch_d, &ctx->scan_tmp};
@@ -306,6 +308,33 @@ CNN_API cnn_status cnn_sort_by_size(cnn_context *ctx, int64_t *labels, int64_t n
         CNN_CUDA(ctx, cudaMemcpyAsync(labels, lab_dev, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
         CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     }
+    return CNN_OK;
+}
+
+CNN_API cnn_status cnn_sweep(cnn_context *ctx, const double *radius_cutoffs, int32_t n_radii,
+                             const int64_t *similarity_cutoffs, const int64_t *n_member_cutoffs, int32_t n_cuts,
+                             cnn_metric metric, cnn_fpmode fpmode, int64_t member_cutoff, int64_t max_clusters,
+                             int64_t *labels_out, cnn_memspace mem) {
+    CNN_TRY(check_ctx(ctx));
+    if (ctx->d < 1) return ctx->fail(CNN_ERR_STATE, "no points: call cnn_set_points first");
+    if (n_radii < 1 || n_radii > 16 || n_cuts < 1 || !radius_cutoffs || !similarity_cutoffs || !n_member_cutoffs ||
+        !labels_out)
+        return ctx->fail(CNN_ERR_INVALID_ARG, "need 1..16 radii, >= 1 cut and all arrays");
+    if (metric != CNN_METRIC_EUCLIDEAN_REDUCED && metric != CNN_METRIC_EUCLIDEAN)
+        return ctx->fail(CNN_ERR_INVALID_ARG, "unknown metric");
+    if (fpmode != CNN_FP_SEPARATE && fpmode != CNN_FP_FUSED) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown fpmode");
+    const int64_t total = (int64_t)n_radii * n_cuts * ctx->n;
+    int64_t *lab_dev = labels_out;
+    if (mem == CNN_MEM_HOST) {
+        CNN_TRY(ctx->ensure(ctx->stage_labels, sizeof(int64_t) * (size_t)(total > 0 ? total : 1)));
+        lab_dev = ctx->stage_labels.as<int64_t>();
+    }
+    CNN_TRY(sweep_impl(ctx, radius_cutoffs, n_radii, similarity_cutoffs, n_member_cutoffs, n_cuts, metric, fpmode,
+                       member_cutoff, max_clusters, lab_dev));
+    if (mem == CNN_MEM_HOST && total > 0)
+        CNN_CUDA(ctx, cudaMemcpyAsync(labels_out, lab_dev, sizeof(int64_t) * (size_t)total, cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+    CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return CNN_OK;
 }
 

@@ -89,6 +89,13 @@ struct cnn_context {
     cnn::DevBuf cell_of;  // int32[n] cell id per point (original order)
     cnn::DevBuf cell_start;  // int32[ncells+2]
 
+    // extents (max - min of finite points) per dimension of the last grid search
+    double grid_extent[3] = {0.0, 0.0, 0.0};
+
+    // batched (radius, cut) sweep: the largest-radius graph kept aside,
+    // per-pair radius buckets, consider flags of the per-fit runs
+    cnn::DevBuf sweep_bucket, sweep_row_off_max, sweep_cols_max, sweep_deg_max, sweep_consider;
+
     // tensor-core (Gram) search for n_dim >= 16
     cnn::DevBuf gram_hi, gram_lo, gram_aux, gram_keys, gram_amb;
     int64_t gram_key_hint = 0;
@@ -165,6 +172,15 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels_dev, int64_t n,
                              int64_t member_cutoff, int64_t max_clusters);
 cnn_status check_lists_impl(cnn_context *ctx, const int32_t *a, int64_t na, const int32_t *b,
                             int64_t nb, int64_t c, int32_t *result_dev);
+// a fresh fit (labels 0, consider 1, current_start 1) and sort_by_size into labels_dev
+cnn_status fit_and_sort_into(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
+                             int64_t sort_member_cutoff, int64_t max_clusters, int64_t *labels_dev);
+
+// sweep.cu
+cnn_status sweep_impl(cnn_context *ctx, const double *radius_cutoffs, int32_t n_radii,
+                      const int64_t *similarity_cutoffs, const int64_t *n_member_cutoffs, int32_t n_cuts,
+                      int metric, int fpmode, int64_t sort_member_cutoff, int64_t max_clusters,
+                      int64_t *labels_dev);
 
 // timing helpers (cnngpu.cu): events only, no synchronisation
 void stage_begin(cnn_context *ctx, int slot);

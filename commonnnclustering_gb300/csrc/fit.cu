@@ -464,6 +464,21 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64
     return CNN_OK;
 }
 
+// What Clustering.fit does around the fitter for fresh labels
+// (src/cnnclustering/cluster.pyx:316-364): labels 0, consider 1,
+// current_start 1, the fit, then sort_by_size.
+cnn_status fit_and_sort_into(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
+                             int64_t sort_member_cutoff, int64_t max_clusters, int64_t *labels_dev) {
+    const int64_t n = ctx->n;
+    cudaStream_t st = ctx->stream;
+    if (n == 0) return CNN_OK;
+    CNN_TRY(ctx->ensure(ctx->sweep_consider, (size_t)n));
+    CNN_CUDA(ctx, cudaMemsetAsync(labels_dev, 0, sizeof(int64_t) * (size_t)n, st));
+    CNN_CUDA(ctx, cudaMemsetAsync(ctx->sweep_consider.ptr, 1, (size_t)n, st));
+    CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, 1, ctx->sweep_consider.as<uint8_t>(), labels_dev));
+    return sort_by_size_impl(ctx, labels_dev, n, sort_member_cutoff, max_clusters);
+}
+
 cnn_status check_lists_impl(cnn_context *ctx, const int32_t *a, int64_t na, const int32_t *b, int64_t nb,
                             int64_t c, int32_t *result_dev) {
     if (na > INT32_MAX || nb > INT32_MAX) return ctx->fail(CNN_ERR_UNSUPPORTED, "list longer than 2^31-1");

@@ -10,16 +10,17 @@
 // neighbours, pairs above are not, pairs inside are recomputed in float64
 // with the reference's exact operation order (the only float64 step).
 //
-// Kernel structure (one persistent CTA per SM, 6 warps):
+// Kernel structure (one persistent CTA per SM, 10 warps):
 //   warp 0  TMA producer: hi/lo tiles of the row block I and the column
 //           block J (cp.async.bulk.tensor, 128-byte swizzle) into a 2-stage
 //           shared-memory ring, completion counted on an mbarrier;
 //   warp 1  allocates 256 TMEM columns (two 128-column accumulators) and
 //           issues the MMAs from one thread; tcgen05.commit frees the
 //           shared stage and publishes the accumulator;
-//   warps 2-5  epilogue: each thread owns one tile row (its TMEM lane),
-//           loads 32 columns at a time with tcgen05.ld, compares, and
-//           appends hits / band pairs to global lists.
+//   warps 2-9  epilogue, two per TMEM lane quadrant: each thread owns one
+//           tile row (its TMEM lane) and 64 of the columns, loads 32
+//           columns at a time with tcgen05.ld, compares, and appends hits /
+//           band pairs to global lists.
 // Only tiles with J >= I are computed; off-diagonal hits are emitted in
 // both directions.  Every wait is bounded (globaltimer): on timeout the
 // kernel records an error, stops issuing work and frees its TMEM.
@@ -42,7 +43,7 @@ constexpr int kKB = 64;               // K block: 64 bf16 = 128 bytes per row
 constexpr int kStages = 2;
 constexpr int kTileBytes = kTM * kKB * 2;          // 16 KB: one operand tile
 constexpr int kStageBytes = 4 * kTileBytes;         // A_hi, A_lo, B_hi, B_lo
-constexpr int kGramThreads = 192;
+constexpr int kGramThreads = 320;  // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
 constexpr uint32_t kTmemCols = 256;
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 
@@ -112,6 +113,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
         if (mbar_try_wait(bar, parity)) return true;
         if (*abort_flag) return false;
         if (globaltimer() - t0 > kWaitNs) return false;
+        __nanosleep(32);  // back off: waiting warps leave issue slots and shared-memory bandwidth
     }
 }
 
@@ -170,6 +172,88 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+struct EpilogueTile {
+    int64_t gi;
+    bool row_ok, diag;
+    float ni, thr_in, thr_out;
+    int32_t J;
+};
+
+__device__ __forceinline__ void tmem_ld32_async(uint32_t taddr, uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
+          "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+          "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+}
+
+// Waits for the outstanding tcgen05.ld; the registers are listed as
+// operands so no use of them can be scheduled before the wait.
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&v)[32]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]), "+r"(v[6]), "+r"(v[7]),
+                   "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]), "+r"(v[12]), "+r"(v[13]), "+r"(v[14]),
+                   "+r"(v[15]), "+r"(v[16]), "+r"(v[17]), "+r"(v[18]), "+r"(v[19]), "+r"(v[20]), "+r"(v[21]),
+                   "+r"(v[22]), "+r"(v[23]), "+r"(v[24]), "+r"(v[25]), "+r"(v[26]), "+r"(v[27]), "+r"(v[28]),
+                   "+r"(v[29]), "+r"(v[30]), "+r"(v[31])
+                 :
+                 : "memory");
+}
+
+// Emission for a 32-column chunk with at least one neighbour or band pair
+// somewhere in the warp: one warp-wide atomic per output list reserves the
+// slots, then each thread writes its pairs.  Fully unrolled so the
+// accumulator registers are never indexed dynamically.
+__device__ __forceinline__ void epilogue_emit_masks(const GramArgs &args, const EpilogueTile &et,
+                                                    const uint32_t (&v)[32], const float *norms, int col0, int lane,
+                                                    uint32_t in_mask, uint32_t amb_mask) {
+    const int per_hit = et.diag ? 1 : 2;
+    const int my_keys = __popc(in_mask) * per_hit, my_amb = __popc(amb_mask);
+    int inc_k = my_keys, inc_a = my_amb;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int uk = __shfl_up_sync(0xffffffffu, inc_k, o);
+        const int ua = __shfl_up_sync(0xffffffffu, inc_a, o);
+        if (lane >= o) {
+            inc_k += uk;
+            inc_a += ua;
+        }
+    }
+    const int tot_k = __shfl_sync(0xffffffffu, inc_k, 31), tot_a = __shfl_sync(0xffffffffu, inc_a, 31);
+    unsigned long long base_k = 0, base_a = 0;
+    if (lane == 31) {
+        if (tot_k) base_k = atomicAdd(args.nkeys, (unsigned long long)tot_k);
+        if (tot_a) base_a = atomicAdd(args.namb, (unsigned long long)tot_a);
+    }
+    unsigned long long wk = __shfl_sync(0xffffffffu, base_k, 31) + (unsigned long long)(inc_k - my_keys);
+    unsigned long long wa = __shfl_sync(0xffffffffu, base_a, 31) + (unsigned long long)(inc_a - my_amb);
+    if (!(in_mask | amb_mask)) return;
+    const uint64_t gi = (uint64_t)et.gi;
+#pragma unroll
+    for (int jj = 0; jj < 32; ++jj) {
+        const uint64_t gj = (uint64_t)et.J * kTM + (uint64_t)(col0 + jj);
+        if ((in_mask >> jj) & 1u) {
+            if (wk < (unsigned long long)args.key_cap) args.keys[wk] = (gi << 32) | gj;
+            ++wk;
+            if (!et.diag) {
+                if (wk < (unsigned long long)args.key_cap) args.keys[wk] = (gj << 32) | gi;
+                ++wk;
+            }
+        }
+        if ((amb_mask >> jj) & 1u) {
+            if (wa < (unsigned long long)args.amb_cap) {
+                args.amb[wa] = (gi << 32) | gj | (et.diag ? 0ull : (1ull << 63));
+                args.amb_d2[wa] = fmaf(-2.f, __uint_as_float(v[jj]), et.ni + norms[jj]);
+            }
+            ++wa;
+        }
+    }
+}
+
 // tile t of the upper triangle (J >= I), row-major over I
 __device__ __forceinline__ void tile_coords(int64_t t, int32_t nblk, int32_t &I, int32_t &J) {
     int32_t i = 0;
@@ -195,6 +279,7 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
     __shared__ __align__(8) uint64_t done_bar;
     __shared__ uint32_t tmem_base_sh;
     __shared__ int abort_sh;
+    __shared__ float s_colnorm[8][64];  // per epilogue warp: its 64 column norms
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // contiguous range of tiles for this CTA
@@ -211,7 +296,7 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&accf_bar[b], 1);
-            mbar_init(&acce_bar[b], 4);  // one arrival per epilogue warp
+            mbar_init(&acce_bar[b], 8);  // one arrival per epilogue warp
         }
         mbar_init(&done_bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -304,12 +389,15 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
             }
         }
     } else {
-        // ---------------- epilogue (warps 2..5) ----------------
-        const int quad = warp & 3;  // TMEM lanes 32*quad .. 32*quad+31
+        // ---------------- epilogue (warps 2..9) ----------------
+        // two warps per TMEM lane quadrant (so each scheduler has two to
+        // alternate between), each owning 64 of the tile's 128 columns
+        const int quad = warp & 3;            // TMEM lanes 32*quad .. 32*quad+31
+        const int half = (warp - 2) >> 2;     // columns 64*half .. 64*half+63
         const int row_in_tile = quad * 32 + lane;
+        float *my_norms = s_colnorm[warp - 2];
         int32_t I = 0, J = 0;
         if (my_tiles > 0) tile_coords(t_begin, args.nblk, I, J);
-        const unsigned lt = (1u << lane) - 1u;
         for (int64_t tl = 0; tl < my_tiles; ++tl) {
             const int b = (int)(tl & 1);
             const uint32_t acc_ph = (uint32_t)((tl >> 1) & 1);
@@ -319,85 +407,47 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
                 break;
             }
             fence_after_sync();
-            const int64_t gi = (int64_t)I * kTM + row_in_tile;  // global row
-            const bool row_ok = gi < args.n;
-            const float ni = row_ok ? args.norm2[gi] : 0.f;
-            const float band =
-                fmaxf(args.coef * args.blk_norm[I] * args.blk_norm[J] +
-                          args.slack_coef * (args.blk_norm2[I] + args.blk_norm2[J]),
-                      args.min_band);
-            const float thr_in = args.rc2 - band, thr_out = args.rc2 + band;
-            const bool diag = I == J;
-            for (int c = 0; c < kTM / 32; ++c) {
+            EpilogueTile et;
+            et.gi = (int64_t)I * kTM + row_in_tile;
+            et.row_ok = et.gi < args.n;
+            et.ni = et.row_ok ? args.norm2[et.gi] : 0.f;
+            const float band = fmaxf(args.coef * args.blk_norm[I] * args.blk_norm[J] +
+                                         args.slack_coef * (args.blk_norm2[I] + args.blk_norm2[J]),
+                                     args.min_band);
+            et.thr_in = args.rc2 - band;
+            et.thr_out = args.rc2 + band;
+            et.diag = I == J;
+            et.J = J;
+            // this warp's 64 column norms, read back as shared broadcasts
+            for (int h = 0; h < 2; ++h) {
+                const int64_t gj = (int64_t)J * kTM + half * 64 + h * 32 + lane;
+                my_norms[h * 32 + lane] = gj < args.n ? args.norm2[gj] : INFINITY;
+            }
+            __syncwarp();
+            const uint32_t taddr =
+                tmem_base + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * kTM + half * 64);
+#pragma unroll 1
+            for (int c = 0; c < 2; ++c) {
                 uint32_t v[32];
-                tmem_ld32(tmem_base + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * kTM + c * 32), v);
+                tmem_ld32_async(taddr + (uint32_t)(c * 32), v);
+                tmem_wait_ld(v);
                 uint32_t in_mask = 0, amb_mask = 0;
 #pragma unroll
                 for (int jj = 0; jj < 32; ++jj) {
-                    const int64_t gj = (int64_t)J * kTM + c * 32 + jj;
-                    const float nj = gj < args.n ? __ldg(&args.norm2[gj]) : INFINITY;
-                    const float d2 = fmaf(-2.f, __uint_as_float(v[jj]), ni + nj);
-                    const bool in = d2 <= thr_in;
-                    const bool amb = !in && d2 <= thr_out;
+                    const float d2 = fmaf(-2.f, __uint_as_float(v[jj]), et.ni + my_norms[c * 32 + jj]);
+                    const bool in = d2 <= et.thr_in;
                     in_mask |= (uint32_t)in << jj;
-                    amb_mask |= (uint32_t)amb << jj;
+                    amb_mask |= (uint32_t)(!in && d2 <= et.thr_out) << jj;
                 }
-                if (!row_ok) { in_mask = 0; amb_mask = 0; }
-                // neighbours: one key per direction
-                const int per_hit = diag ? 1 : 2;
-                const int my_keys = __popc(in_mask) * per_hit;
-                int incl = my_keys;
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int u = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += u;
+                if (!et.row_ok) {
+                    in_mask = 0;
+                    amb_mask = 0;
                 }
-                const int tot = __shfl_sync(0xffffffffu, incl, 31);
-                if (tot) {
-                    unsigned long long base = 0;
-                    if (lane == 31) base = atomicAdd(args.nkeys, (unsigned long long)tot);
-                    base = __shfl_sync(0xffffffffu, base, 31);
-                    unsigned long long w = base + (unsigned long long)(incl - my_keys);
-                    uint32_t m = in_mask;
-                    while (m) {
-                        const int jj = __ffs(m) - 1;
-                        m &= m - 1;
-                        const uint64_t gj = (uint64_t)J * kTM + (uint64_t)(c * 32 + jj);
-                        if (w < (unsigned long long)args.key_cap) args.keys[w] = ((uint64_t)gi << 32) | gj;
-                        ++w;
-                        if (!diag) {
-                            if (w < (unsigned long long)args.key_cap) args.keys[w] = (gj << 32) | (uint64_t)gi;
-                            ++w;
-                        }
-                    }
-                }
-                // band pairs: recomputed in float64 later
-                const int my_amb = __popc(amb_mask);
-                int incl_a = my_amb;
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int u = __shfl_up_sync(0xffffffffu, incl_a, o);
-                    if (lane >= o) incl_a += u;
-                }
-                const int tot_a = __shfl_sync(0xffffffffu, incl_a, 31);
-                if (tot_a) {
-                    unsigned long long base = 0;
-                    if (lane == 31) base = atomicAdd(args.namb, (unsigned long long)tot_a);
-                    base = __shfl_sync(0xffffffffu, base, 31);
-                    unsigned long long w = base + (unsigned long long)(incl_a - my_amb);
-                    uint32_t m = amb_mask;
-                    while (m) {
-                        const int jj = __ffs(m) - 1;
-                        m &= m - 1;
-                        const uint64_t gj = (uint64_t)J * kTM + (uint64_t)(c * 32 + jj);
-                        if (w < (unsigned long long)args.amb_cap) {
-                            args.amb[w] = ((uint64_t)gi << 32) | gj | (diag ? 0ull : (1ull << 63));
-                            const float nj = __ldg(&args.norm2[gj]);
-                            args.amb_d2[w] = fmaf(-2.f, __uint_as_float(v[jj]), ni + nj);
-                        }
-                        ++w;
-                    }
-                }
-                (void)lt;
+                if (__any_sync(0xffffffffu, (in_mask | amb_mask) != 0))
+                    epilogue_emit_masks(args, et, v, my_norms + c * 32, half * 64 + c * 32, lane, in_mask,
+                                        amb_mask);
             }
+            __syncwarp();
             fence_before_sync();
             __syncwarp();
             if (lane == 0) mbar_arrive(&acce_bar[b]);

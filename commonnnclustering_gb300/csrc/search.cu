@@ -566,6 +566,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
 
     std::vector<double> ext(d);
     for (int k = 0; k < d; ++k) ext[k] = std::max(std::fabs(hi[k] - lo[k]), 0.0);
+    for (int k = 0; k < 3; ++k) ctx->grid_extent[k] = k < d ? ext[k] : 0.0;
     double band = 0;
     bool filt = false;
     if (radius_ok && (metric == CNN_METRIC_EUCLIDEAN_REDUCED || metric == CNN_METRIC_EUCLIDEAN)) {
@@ -586,7 +587,9 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     bool use_grid = d <= 3 && radius_ok && R > 0 && isfinite(R);
     if (use_grid) {
         double h = R * (1.0 + 1e-6);
-        const double max_cells = std::max<double>(4.0 * (double)n, 4096.0);
+        // cells cost 12 bytes each (count + start); allow up to 64 per point
+        // (at most 64M) so sparse sets in large boxes keep cells of edge ~R
+        const double max_cells = std::max<double>(std::min<double>(64.0 * (double)n, 67108864.0), 4096.0);
         for (int attempt = 0; attempt < 200; ++attempt) {
             double cells = 1;
             for (int k = 0; k < 3; ++k) {

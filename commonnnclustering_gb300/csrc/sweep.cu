@@ -1,0 +1,226 @@
+// sweep.cu -- batched fits over many (radius, cnn_cutoff) pairs.
+//
+// Reference caller: HierarchicalFitterRepeat (src/cnnclustering/
+// _fit.pyx:1014-1187) refits all points from scratch for every
+// (radius_cutoff, cnn_cutoff) step (:1131-1141), each fit recomputing every
+// neighbourhood.  Here the neighbour search runs once, at the largest
+// radius: every stored pair (p, j) gets the index of the smallest radius
+// whose cutoff admits it ("bucket").  Because the float64 distance does not
+// depend on the radius, the neighbourhood at radius k is exactly the pairs
+// with bucket <= k -- a stable filter of the index-sorted r_max rows, so the
+// filtered rows stay sorted.  Each radius's graph is materialised once and
+// fitted for every cut; every fit and sort is the same code cnn_fit and
+// cnn_sort_by_size run, so each result equals a separate fit.
+#include <math.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+
+namespace cnn {
+
+namespace {
+
+constexpr int kMaxRadii = 16;
+
+struct Ladder {
+    int32_t k;                  // number of radii
+    double rc[kMaxRadii];       // cutoffs as compared (ascending)
+    float thr_in[kMaxRadii];    // float32 sure-in thresholds on squared distance
+    float thr_out[kMaxRadii];   // float32 sure-out thresholds
+    int32_t metric, fpmode;
+};
+
+__device__ __forceinline__ double exact_s(const double *__restrict__ x, int d, int32_t a, int32_t b, int fpmode) {
+    const double *xa = x + (int64_t)a * d, *xb = x + (int64_t)b * d;
+    double s = 0.0;
+    if (fpmode == CNN_FP_FUSED) {
+        for (int k = 0; k < d; ++k) {
+            const double t = __dsub_rn(xa[k], xb[k]);
+            s = __fma_rn(t, t, s);
+        }
+    } else {
+        for (int k = 0; k < d; ++k) {
+            const double t = __dsub_rn(xa[k], xb[k]);
+            s = __dadd_rn(s, __dmul_rn(t, t));
+        }
+    }
+    return s;
+}
+
+// One warp per row of the r_max graph (internal order): bucket of each pair.
+__global__ void bucket_kernel(const double *__restrict__ x, int d, int64_t n, const int32_t *__restrict__ perm,
+                              const float4 *__restrict__ xf4, const int64_t *__restrict__ row_off,
+                              const int32_t *__restrict__ cols, Ladder lad, uint8_t *__restrict__ bucket,
+                              unsigned long long *__restrict__ n_exact) {
+    const int lane = threadIdx.x & 31;
+    const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (p >= n) return;
+    const float4 q = xf4[p];
+    const int32_t ip = perm[p];
+    unsigned long long ex = 0;
+    for (int64_t e = row_off[p] + lane; e < row_off[p + 1]; e += 32) {
+        const int32_t j = cols[e];
+        const float4 c = xf4[j];
+        const float dx = q.x - c.x, dy = q.y - c.y, dz = q.z - c.z;
+        const float sf = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        int k = 0;
+        while (k < lad.k - 1 && sf > lad.thr_out[k]) ++k;  // radii that are certainly too small
+        int b = k;
+        if (!(sf <= lad.thr_in[k])) {  // inside the band of radius k: decide in float64
+            double s = exact_s(x, d, ip, perm[j], lad.fpmode);
+            if (lad.metric == CNN_METRIC_EUCLIDEAN) s = __dsqrt_rn(s);
+            b = lad.k - 1;
+            for (int kk = k; kk < lad.k; ++kk)
+                if (s <= lad.rc[kk]) {
+                    b = kk;
+                    break;
+                }
+            ++ex;
+        }
+        bucket[e] = (uint8_t)b;
+    }
+    for (int o = 16; o > 0; o >>= 1) ex += __shfl_down_sync(0xffffffffu, ex, o);
+    if (lane == 0 && ex) atomicAdd(n_exact, ex);
+}
+
+__global__ void filter_count_kernel(int64_t n, const int64_t *__restrict__ row_off, const uint8_t *__restrict__ bucket,
+                                    int k, int32_t *__restrict__ deg) {
+    const int lane = threadIdx.x & 31;
+    const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (p >= n) return;
+    int32_t c = 0;
+    for (int64_t e = row_off[p] + lane; e < row_off[p + 1]; e += 32) c += bucket[e] <= k;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if (lane == 0) deg[p] = c;
+}
+
+__global__ void filter_fill_kernel(int64_t n, const int64_t *__restrict__ row_off, const int32_t *__restrict__ cols,
+                                   const uint8_t *__restrict__ bucket, int k, const int64_t *__restrict__ out_off,
+                                   int32_t *__restrict__ out_cols) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (p >= n) return;
+    int64_t w = out_off[p];
+    for (int64_t e0 = row_off[p]; e0 < row_off[p + 1]; e0 += 32) {
+        const int64_t e = e0 + lane;
+        const bool keep = e < row_off[p + 1] && bucket[e] <= k;
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep) out_cols[w + __popc(m & lt)] = cols[e];
+        w += __popc(m);
+    }
+}
+
+__global__ void set_zero_tail_kernel(int32_t *deg, int64_t n) { deg[n] = 0; }
+
+bool ladder_thresholds(const std::vector<double> &ext, const std::vector<double> &rcs, int metric, Ladder *lad) {
+    // float32 bands per radius: the same bound as the single-radius search,
+    // evaluated at the largest radius (it only grows with R)
+    const double u32 = ldexp(1.0, -24), u64 = ldexp(1.0, -53);
+    const int d = (int)ext.size();
+    const double rmax = metric == CNN_METRIC_EUCLIDEAN ? rcs.back() : sqrt(rcs.back());
+    double err = 0;
+    for (int k = 0; k < d; ++k) {
+        const double delta = ext[k] * (u32 + 2 * u64);
+        if (delta > 1e-3 * rmax) return false;
+        const double eta = 2 * delta + u32 * (2 * rmax + 2 * delta);
+        err += eta * (4 * rmax + eta);
+    }
+    const double gam = (d + 2) * u32 / (1 - (d + 2) * u32);
+    err += gam * 4 * rmax * rmax + gam * err;
+    for (size_t i = 0; i < rcs.size(); ++i) {
+        const double rc2 = metric == CNN_METRIC_EUCLIDEAN ? rcs[i] * rcs[i] : rcs[i];
+        const double b = 2 * (err + 8 * (d + 2) * u64 * rc2 + 1e-300);
+        float fin = (float)(rc2 - b), fout = (float)(rc2 + b);
+        if ((double)fin > rc2 - b) fin = nextafterf(fin, -INFINITY);
+        if ((double)fout < rc2 + b) fout = nextafterf(fout, INFINITY);
+        lad->thr_in[i] = fin > 0.f ? fin : -1.f;
+        lad->thr_out[i] = fout;
+        lad->rc[i] = rcs[i];
+    }
+    return true;
+}
+
+}  // namespace
+
+cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, const int64_t *sim_cut,
+                      const int64_t *member_cut, int32_t n_cuts, int metric, int fpmode, int64_t sort_member_cutoff,
+                      int64_t max_clusters, int64_t *labels_dev) {
+    const int64_t n = ctx->n;
+    const int d = ctx->d;
+    cudaStream_t st = ctx->stream;
+    std::vector<double> rcs(rcs_in, rcs_in + n_radii);
+    for (int i = 1; i < n_radii; ++i)
+        if (!(rcs[i] >= rcs[i - 1])) return ctx->fail(CNN_ERR_INVALID_ARG, "radius cutoffs must be ascending");
+
+    // one search, at the largest radius (the same search cnn_build_neighbours runs)
+    CNN_TRY(build_neighbours_impl(ctx, rcs.back(), metric, fpmode));
+    const int64_t nnz = ctx->nnz;
+    Ladder lad{};
+    lad.k = n_radii;
+    lad.metric = metric;
+    lad.fpmode = fpmode;
+    const bool ladder = ctx->stats.search_kind == 1 && n_radii > 1 && n > 0 &&
+                        ladder_thresholds(std::vector<double>(ctx->grid_extent, ctx->grid_extent + d), rcs, metric,
+                                          &lad);
+    if (!ladder) {
+        // no cell-grid graph to filter (all-pairs or tensor-core search):
+        // search every radius on its own, smallest first
+        for (int32_t k = 0; k < n_radii; ++k) {
+            if (k < n_radii - 1) CNN_TRY(build_neighbours_impl(ctx, rcs[k], metric, fpmode));
+            else if (n_radii > 1) CNN_TRY(build_neighbours_impl(ctx, rcs.back(), metric, fpmode));
+            for (int32_t j = 0; j < n_cuts; ++j)
+                CNN_TRY(fit_and_sort_into(ctx, sim_cut[j], member_cut[j], sort_member_cutoff, max_clusters,
+                                          labels_dev + ((int64_t)k * n_cuts + j) * n));
+        }
+        return CNN_OK;
+    }
+
+    // buckets of the largest-radius graph, then keep it aside
+    CNN_TRY(ctx->ensure(ctx->sweep_bucket, (size_t)(nnz > 0 ? nnz : 1)));
+    uint8_t *bucket = ctx->sweep_bucket.as<uint8_t>();
+    unsigned long long *counters = ctx->counters.as<unsigned long long>();
+    bucket_kernel<<<grid_for(n * 32, 256), 256, 0, st>>>(ctx->x, d, n, ctx->perm.as<int32_t>(), ctx->xf4.as<float4>(),
+                                                          ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), lad,
+                                                          bucket, counters + 15);
+    CNN_LAUNCH_CHECK(ctx);
+    std::swap(ctx->row_off, ctx->sweep_row_off_max);
+    std::swap(ctx->cols, ctx->sweep_cols_max);
+    std::swap(ctx->deg, ctx->sweep_deg_max);
+    const int64_t *off_max = ctx->sweep_row_off_max.as<int64_t>();
+    const int32_t *cols_max = ctx->sweep_cols_max.as<int32_t>();
+    CNN_TRY(ctx->ensure(ctx->row_off, sizeof(int64_t) * (size_t)(n + 1)));
+    CNN_TRY(ctx->ensure(ctx->deg, sizeof(int32_t) * (size_t)(n + 1)));
+    for (int32_t k = 0; k < n_radii; ++k) {
+        int64_t nnz_k = nnz;
+        if (k < n_radii - 1) {
+            filter_count_kernel<<<grid_for(n * 32, 256), 256, 0, st>>>(n, off_max, bucket, k, ctx->deg.as<int32_t>());
+            CNN_LAUNCH_CHECK(ctx);
+            set_zero_tail_kernel<<<1, 1, 0, st>>>(ctx->deg.as<int32_t>(), n);
+            CNN_LAUNCH_CHECK(ctx);
+            CNN_TRY(scan_exclusive_i32_to_i64(ctx, ctx->deg.as<int32_t>(), ctx->row_off.as<int64_t>(), n + 1));
+            CNN_CUDA(ctx, cudaMemcpyAsync(&nnz_k, ctx->row_off.as<int64_t>() + n, sizeof(int64_t),
+                                          cudaMemcpyDeviceToHost, st));
+            CNN_CUDA(ctx, cudaStreamSynchronize(st));
+            CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nnz_k > 0 ? nnz_k : 1)));
+            filter_fill_kernel<<<grid_for(n * 32, 256), 256, 0, st>>>(n, off_max, cols_max, bucket, k,
+                                                                       ctx->row_off.as<int64_t>(),
+                                                                       ctx->cols.as<int32_t>());
+            CNN_LAUNCH_CHECK(ctx);
+        } else {
+            // the largest radius is the kept graph itself
+            std::swap(ctx->row_off, ctx->sweep_row_off_max);
+            std::swap(ctx->cols, ctx->sweep_cols_max);
+            std::swap(ctx->deg, ctx->sweep_deg_max);
+        }
+        ctx->nnz = nnz_k;
+        for (int32_t j = 0; j < n_cuts; ++j)
+            CNN_TRY(fit_and_sort_into(ctx, sim_cut[j], member_cut[j], sort_member_cutoff, max_clusters,
+                                      labels_dev + ((int64_t)k * n_cuts + j) * n));
+    }
+    return CNN_OK;
+}
+
+}  // namespace cnn

@@ -1,0 +1,187 @@
+"""A served stream of clustering jobs with continuous batching.
+
+Jobs (points + radius_cutoff, cnn_cutoff, member_cutoff) arrive over time.
+The server owns ``n_slots`` library contexts, each with its own CUDA stream
+and device-resident workspace that persists across jobs.  A dispatcher
+admits a waiting job as soon as a slot is free AND its estimated HBM
+footprint fits the remaining budget -- the oldest job first, and when the
+oldest does not fit yet, any later job that does (backfill), so small jobs
+keep flowing past a large one.  Admitted jobs run concurrently on their
+slots' streams; the host threads release the GIL inside every library call,
+so their copies and kernels overlap on the device.
+
+Each job is one ``Clustering.fit`` (fresh labels, current_start 1, then
+sort_by_size) through the C ABI with host buffers, so its result does not
+depend on what else is running: ``tests/test_gpu_serve.py`` checks every
+job alone against the same job in the mix.
+"""
+from __future__ import annotations
+
+import collections
+import threading
+import time
+from dataclasses import dataclass, field
+from typing import Callable, List, Optional
+
+import numpy as np
+
+from . import _abi
+
+
+@dataclass
+class Job:
+    job_id: int
+    points: np.ndarray
+    radius_cutoff: float
+    cnn_cutoff: int
+    member_cutoff: Optional[int] = 10
+    arrival: float = 0.0             # seconds from the start of the stream
+    expected_degree: float = 300.0   # for the footprint estimate
+    labels: Optional[np.ndarray] = None
+    t_admit: Optional[float] = None
+    t_done: Optional[float] = None
+    slot: Optional[int] = None
+    error: Optional[str] = None
+
+    @property
+    def latency(self) -> Optional[float]:
+        if self.t_done is None:
+            return None
+        return self.t_done - self.arrival
+
+
+def footprint_bytes(n: int, d: int, expected_degree: float) -> int:
+    """Device bytes a fit of n x d points needs (upper estimate)."""
+    pts = n * d * 8
+    graph = int(n * expected_degree * 4 * 1.25) + n * 48
+    work = n * 64
+    if d >= 16:  # bf16 split, float norms, key and band lists of the tensor-core search
+        dp = (d + 63) // 64 * 64
+        graph += n * dp * 4 + n * 256 * 8 + n * 64 * 12
+    elif d > 3:
+        graph += n * d * 4
+    else:
+        graph += n * 32 + min(64 * n, 1 << 26) * 12
+    return pts + graph + work
+
+
+def run_job_alone(ctx: _abi.Context, job: Job) -> np.ndarray:
+    """One job exactly as Clustering.fit runs it (host buffers)."""
+    x = np.ascontiguousarray(job.points)
+    n = x.shape[0]
+    labels = np.zeros(n, dtype=np.int64)
+    consider = np.ones(n, dtype=np.uint8)
+    ctx.set_points(x)
+    ctx.build_neighbours(job.radius_cutoff ** 2)
+    ctx.fit(job.cnn_cutoff + 2, job.cnn_cutoff + 1, 1, consider, labels)
+    ctx.sort_by_size(labels, 2 if job.member_cutoff is None else job.member_cutoff, None)
+    return labels
+
+
+class Server:
+    def __init__(self, n_slots: int = 4, hbm_budget_bytes: Optional[int] = None, device: int = 0,
+                 backfill: bool = True):
+        if hbm_budget_bytes is None:
+            try:
+                import torch
+                free, _ = torch.cuda.mem_get_info(device)
+                hbm_budget_bytes = int(free * 0.6)
+            except Exception:
+                hbm_budget_bytes = 32 << 30
+        self.budget = int(hbm_budget_bytes)
+        self.in_use = 0
+        self.backfill = backfill
+        self.contexts = [_abi.Context(device) for _ in range(n_slots)]
+        self.free_slots = collections.deque(range(n_slots))
+        self.waiting: collections.deque = collections.deque()
+        self.cv = threading.Condition()
+        self.done: List[Job] = []
+        self.t0 = 0.0
+        self.max_in_flight = 0
+        self._in_flight = 0
+
+    def _admit_locked(self):
+        """Start every waiting job that fits (oldest first, then backfill)."""
+        started = True
+        while started and self.free_slots and self.waiting:
+            started = False
+            for idx, job in enumerate(self.waiting):
+                need = footprint_bytes(job.points.shape[0], job.points.shape[1], job.expected_degree)
+                if need <= self.budget - self.in_use or (self.in_use == 0 and need > self.budget):
+                    del self.waiting[idx]
+                    self.in_use += need
+                    slot = self.free_slots.popleft()
+                    job.slot = slot
+                    job.t_admit = time.perf_counter() - self.t0
+                    self._in_flight += 1
+                    self.max_in_flight = max(self.max_in_flight, self._in_flight)
+                    threading.Thread(target=self._run, args=(job, need), daemon=True).start()
+                    started = True
+                    break
+                if not self.backfill:
+                    break
+
+    def _run(self, job: Job, need: int):
+        try:
+            job.labels = run_job_alone(self.contexts[job.slot], job)
+        except Exception as e:  # the job fails alone; the server keeps going
+            job.error = f"{type(e).__name__}: {e}"
+        job.t_done = time.perf_counter() - self.t0
+        with self.cv:
+            self.in_use -= need
+            self.free_slots.append(job.slot)
+            self._in_flight -= 1
+            self.done.append(job)
+            self._admit_locked()
+            self.cv.notify_all()
+
+    def serve(self, jobs: List[Job], realtime: bool = True, on_done: Optional[Callable] = None) -> List[Job]:
+        """Feed jobs at their arrival times; return them when all are done."""
+        jobs = sorted(jobs, key=lambda j: j.arrival)
+        self.t0 = time.perf_counter()
+        for job in jobs:
+            if realtime:
+                delay = job.arrival - (time.perf_counter() - self.t0)
+                if delay > 0:
+                    time.sleep(delay)
+            else:
+                job.arrival = time.perf_counter() - self.t0
+            with self.cv:
+                self.waiting.append(job)
+                self._admit_locked()
+        with self.cv:
+            while len(self.done) < len(jobs):
+                self.cv.wait(timeout=1.0)
+        return jobs
+
+    def close(self):
+        for c in self.contexts:
+            c.close()
+
+
+def serve_one_at_a_time(jobs: List[Job], device: int = 0, realtime: bool = True) -> List[Job]:
+    """The plain path: one context, jobs strictly in arrival order."""
+    ctx = _abi.Context(device)
+    t0 = time.perf_counter()
+    for job in sorted(jobs, key=lambda j: j.arrival):
+        if realtime:
+            delay = job.arrival - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+        job.t_admit = time.perf_counter() - t0
+        job.labels = run_job_alone(ctx, job)
+        job.t_done = time.perf_counter() - t0
+    ctx.close()
+    return jobs
+
+
+def latency_summary(jobs: List[Job]) -> dict:
+    lat = np.array([j.latency for j in jobs if j.latency is not None])
+    span = max(j.t_done for j in jobs) - min(j.arrival for j in jobs)
+    return {"jobs": len(jobs), "p50_ms": float(np.percentile(lat, 50) * 1e3),
+            "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3),
+            "jobs_per_s": len(jobs) / span if span > 0 else None,
+            "points_per_s": sum(j.points.shape[0] for j in jobs) / span if span > 0 else None}
+
+
+__all__ = ["Job", "Server", "footprint_bytes", "run_job_alone", "serve_one_at_a_time", "latency_summary"]

@@ -79,6 +79,74 @@ def nested3d(n: int = 1_000_000, seed: int = 3, n_parents: int = 100,
     return np.ascontiguousarray(x, dtype=np.float32)
 
 
+def mixture(n: int, d: int, n_components: int, seed: int, noise: float = 0.05) -> np.ndarray:
+    """Gaussian mixture (unit within-component std) plus uniform noise in its box."""
+    rng = np.random.default_rng(seed)
+    spread = 6.0 * max(1.0, n_components ** (1.0 / d)) if d <= 3 else 4.0
+    centres = rng.uniform(-spread, spread, size=(n_components, d)) if d <= 3 else \
+        rng.normal(0.0, spread, size=(n_components, d))
+    n_noise = int(round(noise * n))
+    counts = rng.multinomial(n - n_noise, rng.dirichlet(np.ones(n_components)))
+    x = np.vstack([c + rng.normal(size=(k, d)) for c, k in zip(centres, counts)])
+    lo, hi = x.min(axis=0), x.max(axis=0)
+    x = np.vstack([x, rng.uniform(lo, hi, size=(n_noise, d))])
+    return np.ascontiguousarray(x[rng.permutation(n)], dtype=np.float64)
+
+
+def degree_radius(x: np.ndarray, degree: float, seed: int = 0, queries: int = 128) -> float:
+    """Radius giving about `degree` neighbours per point (sampled estimate)."""
+    rng = np.random.default_rng(seed)
+    n = x.shape[0]
+    m = min(n, 20000)
+    sample = x[rng.choice(n, m, replace=False)] if m < n else x
+    q = x[rng.choice(n, min(queries, n), replace=False)]
+    k = max(2, int(round(degree * m / n)))
+    d2 = (q * q).sum(1)[:, None] + (sample * sample).sum(1)[None] - 2.0 * q @ sample.T
+    kth = np.sort(d2, axis=1)[:, min(k, m - 1)]
+    r = float(np.sqrt(max(np.median(kth), 1e-12)))
+    if k > degree * m / n:  # the sample was too small for the target: shrink by volume
+        r *= (degree * m / n / k) ** (1.0 / x.shape[1])
+    return r
+
+
+def job_stream(n_jobs: int = 2000, rate: float = 100.0, seed: int = 11, pool: int = 48,
+               max_points_tensor: int = 300_000):
+    """Served workload: Poisson arrivals of clustering jobs.
+
+    Point counts lognormal (median 20k, sigma 1.2) clipped to [1k, 2M]
+    (to `max_points_tensor` for d >= 16, which bounds the all-pairs tensor
+    work per job); d from {2, 3, 16, 64}; 5-200 Gaussian components + 5 %
+    uniform noise; a radius tuned for a mean degree in [50, 300];
+    cnn_cutoff in [3, 50]; member_cutoff 10.  Jobs draw their points from
+    a pool of `pool` generated datasets (generation is the host's cost,
+    not the server's) and their own degree target and cnn_cutoff.
+    Returns a list of dicts: arrival, points, radius_cutoff, cnn_cutoff,
+    member_cutoff, expected_degree.
+    """
+    rng = np.random.default_rng(seed)
+    datasets = []
+    for p in range(pool):
+        d = int(rng.choice([2, 3, 16, 64]))
+        n = int(np.clip(np.exp(rng.normal(np.log(20000.0), 1.2)), 1000, 2_000_000))
+        if d >= 16:
+            n = min(n, max_points_tensor)
+        k = int(rng.integers(5, 201))
+        x = mixture(n, d, k, seed=seed * 1000 + p)
+        radii = {deg: degree_radius(x, deg, seed=p) for deg in (50, 100, 200, 300)}
+        datasets.append((x, radii))
+    t = 0.0
+    jobs = []
+    for i in range(n_jobs):
+        t += rng.exponential(1.0 / rate)
+        x, radii = datasets[int(rng.integers(0, pool))]
+        deg = float(rng.uniform(50, 300))
+        keys = sorted(radii)
+        r = float(np.interp(deg, keys, [radii[k] for k in keys]))
+        jobs.append(dict(arrival=t, points=x, radius_cutoff=r, cnn_cutoff=int(rng.integers(3, 51)),
+                         member_cutoff=10, expected_degree=deg * 1.5))
+    return jobs
+
+
 WORKLOADS = {
     "blobs2d-5k": dict(gen=blobs2d, n=5000, radius_cutoff=0.3, cnn_cutoff=5, member_cutoff=10),
     "md3d-200k": dict(gen=md3d, n=200_000, radius_cutoff=0.1, cnn_cutoff=10, member_cutoff=50),

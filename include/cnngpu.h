@@ -178,6 +178,22 @@ CNN_API cnn_status cnn_check_lists(cnn_context *ctx, const int32_t *a, int64_t n
                                    const int32_t *b, int64_t nb, int64_t c, int32_t *result,
                                    cnn_memspace mem);
 
+/* Batched fits over n_radii x n_cuts (radius, cut) pairs on the current
+ * points -- the scan HierarchicalFitterRepeat performs
+ * (src/cnnclustering/_fit.pyx:1014-1187, one full fit per step at
+ * :1131-1141) -- with the neighbour search run once at the largest radius.
+ * radius_cutoffs: adjusted cutoffs, ascending (<= 16).  Cut j is
+ * (similarity_cutoffs[j], n_member_cutoffs[j]) as make_parameters gives them.
+ * Every pair is fitted from fresh labels (current_start 1) and sorted with
+ * (member_cutoff, max_clusters < 0: no limit); labels_out[(k * n_cuts + j) *
+ * n_points + i] then equals what cnn_fit + cnn_sort_by_size give at radius
+ * k and cut j.  The context keeps the largest-radius graph afterwards. */
+CNN_API cnn_status cnn_sweep(cnn_context *ctx, const double *radius_cutoffs, int32_t n_radii,
+                             const int64_t *similarity_cutoffs, const int64_t *n_member_cutoffs,
+                             int32_t n_cuts, cnn_metric metric, cnn_fpmode fpmode,
+                             int64_t member_cutoff, int64_t max_clusters, int64_t *labels_out,
+                             cnn_memspace mem);
+
 /* ---------------------------------------------------------------------
  * Fit without device memory allocation.  This entry point has no
  * counterpart in the reference.

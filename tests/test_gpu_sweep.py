@@ -1,0 +1,63 @@
+"""Batched (radius, cnn_cutoff) sweep: every result must equal a separate fit."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def cnn():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import commonnnclustering_gb300 as cnn
+    return cnn
+
+
+def separate_fit(cnn, x, r, c, member_cutoff):
+    cl = cnn.Clustering(cnn.InputDataGPUComponents(x))
+    cl.fit(r, c, member_cutoff=member_cutoff, v=False)
+    return np.asarray(cl.labels)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_sweep_equals_separate_fits(cnn, dtype):
+    from commonnnclustering_gb300 import workloads
+    x = workloads.nested3d(n=30000, seed=2, n_parents=6, box=3.0).astype(dtype)
+    radii = [0.03, 0.06, 0.09, 0.12]
+    cuts = [2, 5, 20, 60]
+    got = cnn.sweep(x, radii, cuts, member_cutoff=5)
+    assert got.shape == (4, 4, x.shape[0])
+    for k, r in enumerate(radii):
+        for j, c in enumerate(cuts):
+            assert np.array_equal(got[k, j], separate_fit(cnn, x, r, c, 5)), (r, c)
+
+
+def test_sweep_against_oracle(cnn):
+    from commonnnclustering_gb300 import workloads
+    from oracle import cnn_oracle
+    x = workloads.nested3d(n=8000, seed=5, n_parents=3, box=2.0).astype(np.float64)
+    radii, cuts = [0.05, 0.1], [3, 10]
+    got = cnn.sweep(x, radii, cuts, member_cutoff=2)
+    for k, r in enumerate(radii):
+        for j, c in enumerate(cuts):
+            want, _ = cnn_oracle.clustering_fit(x, r, c, member_cutoff=2)
+            assert np.array_equal(got[k, j], want), (r, c)
+
+
+def test_sweep_without_grid_searches_each_radius(cnn):
+    rng = np.random.default_rng(3)
+    x = np.vstack([rng.normal(0, 1, size=(1500, 5)), rng.normal(4, 0.5, size=(1500, 5))])
+    radii, cuts = [0.6, 0.9], [2, 8]
+    got = cnn.sweep(x, radii, cuts, member_cutoff=2)
+    for k, r in enumerate(radii):
+        for j, c in enumerate(cuts):
+            assert np.array_equal(got[k, j], separate_fit(cnn, x, r, c, 2)), (r, c)
+
+
+def test_sweep_rejects_descending_radii(cnn):
+    ctx = cnn.Context(0)
+    ctx.set_points(np.random.default_rng(0).normal(size=(50, 2)))
+    with pytest.raises(cnn.CNNError):
+        ctx.sweep([0.04, 0.01], [(3, 2)])
+    ctx.close()
