@@ -155,10 +155,11 @@ def make_points():
 def roofline_entry(stats_list, nnz, n, peaks):
     """Dominant kernel by mean stage time; algorithmic bytes per launch."""
     d = WORKLOAD["d"]
-    if d >= 16:  # tensor-core Gram kernel: useful FLOPs (upper triangle, 128-row tiles) per launch
+    if d >= 16:  # tensor-core Gram kernel: FLOPs of the 128 x 128 tiles it actually computed
         ms = statistics.mean(s["ms_gram"] for s in stats_list)
         nblk = (n + 127) // 128
-        pairs = nblk * (nblk + 1) // 2 * 128 * 128
+        all_pairs = nblk * (nblk + 1) // 2 * 128 * 128
+        pairs = statistics.mean(s["n_candidates"] for s in stats_list)  # tiles left after pruning x 128^2
         dp = (d + 63) // 64 * 64
         useful = 2.0 * pairs * dp
         issued = 3.0 * useful  # BF16x3: hi.hi + hi.lo + lo.hi
@@ -168,6 +169,7 @@ def roofline_entry(stats_list, nnz, n, peaks):
             "kernel": "gram_search_kernel (tcgen05 BF16x3)", "bound": "tensor", "achieved": achieved, "peak": peak,
             "unit": "TFLOP/s", "frac": (achieved / peak) if (achieved and peak) else None, "traffic": None,
             "algorithmic_flops_issued": issued, "algorithmic_flops_useful": useful,
+            "tile_pairs_computed": pairs, "tile_pairs_unpruned": all_pairs,
             "useful_tflops": useful / (ms * 1e-3) / 1e12 if ms > 0 else None, "ms_per_launch": ms,
             "peak_source": "MEASURED_PEAKS.json bf16_tflops (measured burst)" if peak else "fallback",
             "stage_ms": {k: round(statistics.mean(s[k] for s in stats_list), 4)

@@ -101,6 +101,7 @@ CNN_API cnn_status cnn_destroy(cnn_context *ctx) {
                            &ctx->cols, &ctx->xf4, &ctx->cell_of, &ctx->cell_start, &ctx->node, &ctx->parent,
                            &ctx->comp_min, &ctx->flag, &ctx->counters, &ctx->stage_labels, &ctx->gram_hi,
                            &ctx->gram_lo, &ctx->gram_aux, &ctx->gram_keys, &ctx->gram_amb,
+                           &ctx->gram_blocks, &ctx->gram_tiles,
                            &ctx->sweep_bucket, &ctx->sweep_row_off_max, &ctx->sweep_cols_max,
                            &ctx->sweep_deg_max, &ctx->sweep_consider,
                            &ctx->stage_consider, &ctx->stage_offsets, &ctx->stage_indices, &ctx->stage_misc,

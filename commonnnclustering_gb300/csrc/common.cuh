@@ -97,7 +97,7 @@ struct cnn_context {
     cnn::DevBuf sweep_bucket, sweep_row_off_max, sweep_cols_max, sweep_deg_max, sweep_consider;
 
     // tensor-core (Gram) search for n_dim >= 16
-    cnn::DevBuf gram_hi, gram_lo, gram_aux, gram_keys, gram_amb;
+    cnn::DevBuf gram_hi, gram_lo, gram_aux, gram_keys, gram_amb, gram_blocks, gram_tiles;
     int64_t gram_key_hint = 0;
 
     // fit work arrays

@@ -51,7 +51,8 @@ struct GramArgs {
     int64_t n;
     int32_t nkb;        // K blocks of 64
     int32_t nblk;       // row blocks of 128
-    int64_t ntiles;     // upper-triangle tiles
+    int64_t ntiles;     // tiles in the list
+    const int2 *tiles;  // (I, J >= I) block pairs that can hold a neighbour pair
     float rc2;          // squared radius the float32 value is compared with
     float coef;         // band = coef * maxnorm_I * maxnorm_J + slack
     float slack_coef;   // float32 epilogue rounding: slack_coef * (maxn2_I + maxn2_J)
@@ -254,18 +255,6 @@ __device__ __forceinline__ void epilogue_emit_masks(const GramArgs &args, const 
     }
 }
 
-// tile t of the upper triangle (J >= I), row-major over I
-__device__ __forceinline__ void tile_coords(int64_t t, int32_t nblk, int32_t &I, int32_t &J) {
-    int32_t i = 0;
-    int64_t rem = t;
-    while (rem >= nblk - i) {
-        rem -= nblk - i;
-        ++i;
-    }
-    I = i;
-    J = i + (int32_t)rem;
-}
-
 __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __grid_constant__ CUtensorMap map_hi,
                                                                       const __grid_constant__ CUtensorMap map_lo,
                                                                       GramArgs args) {
@@ -316,11 +305,11 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
     if (warp == 0) {
         // ---------------- TMA producer ----------------
         if (lane == 0 && my_tiles > 0) {
-            int32_t I, J;
-            tile_coords(t_begin, args.nblk, I, J);
             int64_t it = 0;  // (tile, k block) iterations
             bool ok = true;
             for (int64_t t = t_begin; t < t_end && ok; ++t) {
+                const int2 tile = args.tiles[t];
+                const int32_t I = tile.x, J = tile.y;
                 for (int32_t kb = 0; kb < args.nkb; ++kb, ++it) {
                     const int s = (int)(it % kStages);
                     const uint32_t ph = (uint32_t)((it / kStages) & 1);
@@ -331,10 +320,6 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
                     tma_load_2d(st + 1 * kTileBytes, &map_lo, kb * kKB, I * kTM, &full_bar[s]);
                     tma_load_2d(st + 2 * kTileBytes, &map_hi, kb * kKB, J * kTM, &full_bar[s]);
                     tma_load_2d(st + 3 * kTileBytes, &map_lo, kb * kKB, J * kTM, &full_bar[s]);
-                }
-                if (++J == args.nblk) {
-                    ++I;
-                    J = I;
                 }
             }
             if (!ok) {
@@ -396,9 +381,9 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
         const int half = (warp - 2) >> 2;     // columns 64*half .. 64*half+63
         const int row_in_tile = quad * 32 + lane;
         float *my_norms = s_colnorm[warp - 2];
-        int32_t I = 0, J = 0;
-        if (my_tiles > 0) tile_coords(t_begin, args.nblk, I, J);
         for (int64_t tl = 0; tl < my_tiles; ++tl) {
+            const int2 tile = args.tiles[t_begin + tl];
+            const int32_t I = tile.x, J = tile.y;
             const int b = (int)(tl & 1);
             const uint32_t acc_ph = (uint32_t)((tl >> 1) & 1);
             if (!mbar_wait(&accf_bar[b], acc_ph, abort_flag)) {
@@ -451,10 +436,6 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
             fence_before_sync();
             __syncwarp();
             if (lane == 0) mbar_arrive(&acce_bar[b]);
-            if (++J == args.nblk) {
-                ++I;
-                J = I;
-            }
         }
     }
 
@@ -479,22 +460,24 @@ __global__ void column_sum_kernel(const double *__restrict__ x, int64_t n, int d
     if ((threadIdx.x & 31) == 0) atomicAdd(&sum[k], s);
 }
 
-// One warp per point: split x - mean into hi/lo bf16 (K padded with zeros to
-// dp), float32 squared norm, per-block max norm (as ordered int bits).
+// One warp per point (internal order i = perm position): split x - mean into
+// hi/lo bf16 (K padded with zeros to dp), float32 squared norm, per-block max
+// norm (as ordered int bits).
 __global__ void gram_prep_kernel(const double *__restrict__ x, int64_t n, int d, int dp,
-                                 const double *__restrict__ sum, __nv_bfloat16 *__restrict__ hi,
-                                 __nv_bfloat16 *__restrict__ lo, float *__restrict__ norm2,
-                                 unsigned *__restrict__ blk_norm_bits, unsigned *__restrict__ blk_norm2_bits,
-                                 int *__restrict__ nonfinite) {
+                                 const double *__restrict__ sum, const int32_t *__restrict__ perm,
+                                 __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ lo,
+                                 float *__restrict__ norm2, unsigned *__restrict__ blk_norm_bits,
+                                 unsigned *__restrict__ blk_norm2_bits, int *__restrict__ nonfinite) {
     const int lane = threadIdx.x & 31;
     const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (i >= n) return;
+    const int64_t src = perm[i];
     double s2 = 0;
     bool fin = true;
     for (int k = lane; k < dp; k += 32) {
         float h = 0.f, l = 0.f;
         if (k < d) {
-            const double v = x[i * d + k];
+            const double v = x[src * d + k];
             fin = fin && isfinite(v);
             const double c = v - sum[k] / (double)n;
             const float cf = (float)c;
@@ -515,6 +498,146 @@ __global__ void gram_prep_kernel(const double *__restrict__ x, int64_t n, int d,
         const float nrm = sqrtf(fin ? (float)s2 : 0.f) * (1.f + 1e-6f);
         atomicMax(&blk_norm_bits[i / kTM], __float_as_uint(nrm));
         atomicMax(&blk_norm2_bits[i / kTM], __float_as_uint(fin ? (float)s2 * (1.f + 1e-6f) : 0.f));
+    }
+}
+
+// ---- tile pruning ---------------------------------------------------------------
+// Points are grouped by their nearest pivot (float32, centred coordinates;
+// any grouping gives the same result, compact groups let more tiles go).
+// One warp per point, lane k holding coordinates k, k+32, k+64, k+96
+// (n_dim <= 128); pivots staged in shared memory.
+__global__ void pivot_assign_kernel(const double *__restrict__ x, int64_t n, int d, const double *__restrict__ sum,
+                                    int32_t n_pivots, int bits_n, uint64_t *__restrict__ keys) {
+    extern __shared__ float s_piv[];  // [n_pivots][d]
+    const int64_t stride = n / n_pivots;
+    for (int e = threadIdx.x; e < n_pivots * d; e += blockDim.x) {
+        const int kp = e / d, k = e - kp * d;
+        s_piv[e] = (float)(x[(int64_t)kp * stride * d + k] - sum[k] / (double)n);
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = w0; i < n; i += nw) {
+        float xc[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int k = lane + 32 * c;
+            xc[c] = k < d ? (float)(x[i * d + k] - sum[k] / (double)n) : 0.f;
+        }
+        float best = INFINITY;
+        int32_t bi = 0;
+        for (int kp = 0; kp < n_pivots; ++kp) {
+            const float *pv = s_piv + kp * d;
+            float acc = 0.f;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int k = lane + 32 * c;
+                if (k < d) {
+                    const float t = xc[c] - pv[k];
+                    acc = fmaf(t, t, acc);
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (acc < best) {
+                best = acc;
+                bi = kp;
+            }
+        }
+        if (lane == 0) keys[i] = ((uint64_t)(uint32_t)bi << bits_n) | (uint64_t)i;
+    }
+}
+
+__global__ void perm_from_keys_kernel(const uint64_t *__restrict__ keys, int64_t n, int bits_n,
+                                      int32_t *__restrict__ perm) {
+    const uint64_t mask = (1ull << bits_n) - 1;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
+        perm[p] = (int32_t)(keys[p] & mask);
+}
+
+// Per row block (internal order): centroid and radius of its points.
+// Float32 values rounded outward enough for the pruning test below.
+__global__ void block_bounds_kernel(const double *__restrict__ x, int64_t n, int d, const double *__restrict__ sum,
+                                    const int32_t *__restrict__ perm, float *__restrict__ centroid,
+                                    float *__restrict__ radius) {
+    __shared__ double s_c[128];
+    __shared__ double s_r[256];
+    const int64_t I = blockIdx.x;
+    const int64_t r0 = I * kTM, r1 = min(n, r0 + kTM);
+    const int rows = (int)(r1 - r0);
+    for (int k = threadIdx.x; k < d; k += blockDim.x) {
+        double c = 0;
+        for (int r = 0; r < rows; ++r) c += x[(int64_t)perm[r0 + r] * d + k] - sum[k] / (double)n;
+        s_c[k] = c / rows;
+        centroid[I * d + k] = (float)s_c[k];
+    }
+    __syncthreads();
+    double m = 0;
+    for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+        double s = 0;
+        const int64_t src = perm[r0 + r];
+        for (int k = 0; k < d; ++k) {
+            // distance to the float32 centroid actually used in the test
+            const double t = (x[src * d + k] - sum[k] / (double)n) - (double)(float)s_c[k];
+            s += t * t;
+        }
+        m = fmax(m, s);
+    }
+    s_r[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) s_r[threadIdx.x] = fmax(s_r[threadIdx.x], s_r[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) radius[I] = (float)(sqrt(s_r[0]) * (1.0 + 1e-6) + 1e-30);
+}
+
+// Can blocks I and J (J >= I) hold a pair within R?  |c_I - c_J| - rho_I -
+// rho_J > R means every pair is farther than R (triangle inequality); the
+// margin covers the float32 evaluation of the centroid distance.
+__device__ __forceinline__ bool blocks_may_touch(const float *__restrict__ centroid, const float *__restrict__ radius,
+                                                 int d, int64_t I, int64_t J, float R) {
+    if (I == J) return true;
+    const float *a = centroid + I * d, *b = centroid + J * d;
+    float s = 0.f, na = 0.f, nb = 0.f;
+    for (int k = 0; k < d; ++k) {
+        const float t = a[k] - b[k];
+        s = fmaf(t, t, s);
+        na = fmaf(a[k], a[k], na);
+        nb = fmaf(b[k], b[k], nb);
+    }
+    const float margin = 1e-5f * (sqrtf(na) + sqrtf(nb) + radius[I] + radius[J] + R);
+    return sqrtf(s) - radius[I] - radius[J] <= R + margin;
+}
+
+// Row I of the tile triangle: count (pass 1) or write (pass 2) its kept J.
+template <bool kWrite>
+__global__ void tile_list_kernel(const float *__restrict__ centroid, const float *__restrict__ radius, int d,
+                                 int64_t nblk, float R, int32_t *__restrict__ row_count,
+                                 const int64_t *__restrict__ row_off, int2 *__restrict__ tiles) {
+    __shared__ int32_t s_cnt;
+    const int64_t I = blockIdx.x;
+    if (threadIdx.x == 0) s_cnt = 0;
+    __syncthreads();
+    for (int64_t J = I + threadIdx.x; J < nblk; J += blockDim.x) {
+        if (blocks_may_touch(centroid, radius, d, I, J, R)) {
+            const int32_t k = atomicAdd(&s_cnt, 1);
+            if (kWrite) tiles[row_off[I] + k] = make_int2((int32_t)I, (int32_t)J);
+        }
+    }
+    __syncthreads();
+    if (!kWrite && threadIdx.x == 0) row_count[I] = s_cnt;
+}
+
+// internal indices -> point indices in the key lists (bit 63 kept)
+__global__ void map_keys_kernel(uint64_t *__restrict__ keys, const unsigned long long *__restrict__ count,
+                                int64_t cap, const int32_t *__restrict__ perm) {
+    const int64_t nk = min((int64_t)*count, cap);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nk; e += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = keys[e];
+        const uint64_t flag = k & (1ull << 63);
+        const uint64_t a = (k >> 32) & 0x7fffffffull, b = k & 0xffffffffull;
+        keys[e] = flag | ((uint64_t)(uint32_t)perm[a] << 32) | (uint64_t)(uint32_t)perm[b];
     }
 }
 
@@ -618,7 +741,6 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     const int dp = (d + kKB - 1) / kKB * kKB;
     const int nkb = dp / kKB;
     const int64_t nblk = (n + kTM - 1) / kTM;
-    const int64_t ntiles = nblk * (nblk + 1) / 2;
     const double rc2 = metric == CNN_METRIC_EUCLIDEAN ? radius_cutoff * radius_cutoff : radius_cutoff;
 
     // buffers: hi, lo (bf16 n x dp), norm2 (n), block norms, counters
@@ -643,7 +765,29 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
         column_sum_kernel<<<dim3(blocks, d), 256, 0, st>>>(ctx->x, n, d, colsum);
         CNN_LAUNCH_CHECK(ctx);
     }
-    gram_prep_kernel<<<grid_for(n * 32, 256), 256, 0, st>>>(ctx->x, n, d, dp, colsum, ctx->gram_hi.as<__nv_bfloat16>(),
+    // internal order: points grouped by nearest pivot, so that 128-point
+    // blocks are compact and far-apart block pairs can be skipped
+    const int bits_n = [&] { int b = 1; while (b < 62 && (int64_t(1) << b) < n) ++b; return b; }();
+    const bool prune = d <= 128 && n >= 8 * kTM;
+    int32_t *perm = ctx->perm.as<int32_t>();
+    if (prune) {
+        const int n_pivots = (int)std::max<int64_t>(1, std::min<int64_t>({512, n / 1024, 98304 / (4 * d)}));
+        CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(uint64_t) * (size_t)n));
+        uint64_t *pkeys = ctx->scratch_a.as<uint64_t>();
+        const size_t psmem = sizeof(float) * (size_t)n_pivots * d;
+        CNN_CUDA(ctx, cudaFuncSetAttribute(pivot_assign_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+        pivot_assign_kernel<<<152 * 4, 256, psmem, st>>>(ctx->x, n, d, colsum, n_pivots, bits_n, pkeys);
+        CNN_LAUNCH_CHECK(ctx);
+        int pb = 1;
+        while ((1 << pb) < n_pivots) ++pb;
+        CNN_TRY(radix_sort_u64(ctx, pkeys, n, bits_n + pb));
+        perm_from_keys_kernel<<<std::min<unsigned>(grid_for(n, 256), 4096u), 256, 0, st>>>(pkeys, n, bits_n, perm);
+        CNN_LAUNCH_CHECK(ctx);
+    } else {
+        CNN_TRY(iota_i32(ctx, perm, n));
+    }
+    gram_prep_kernel<<<grid_for(n * 32, 256), 256, 0, st>>>(ctx->x, n, d, dp, colsum, perm,
+                                                            ctx->gram_hi.as<__nv_bfloat16>(),
                                                             ctx->gram_lo.as<__nv_bfloat16>(), norm2, blk_norm_bits,
                                                             blk_norm2_bits, nonfinite);
     CNN_LAUNCH_CHECK(ctx);
@@ -651,6 +795,35 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     CNN_CUDA(ctx, cudaMemcpyAsync(&h_nonfinite, nonfinite, sizeof(int), cudaMemcpyDeviceToHost, st));
     CNN_CUDA(ctx, cudaStreamSynchronize(st));
     if (h_nonfinite) return CNN_OK;  // non-finite coordinates: the all-pairs path handles them
+
+    // the list of block pairs (I, J >= I) that can hold a pair within R
+    const double Rsearch = (metric == CNN_METRIC_EUCLIDEAN ? radius_cutoff : sqrt(radius_cutoff)) * (1.0 + 1e-6);
+    CNN_TRY(ctx->ensure(ctx->gram_blocks, sizeof(float) * (size_t)nblk * (d + 1) +
+                                              (sizeof(int32_t) + sizeof(int64_t)) * (size_t)(nblk + 1) + 256));
+    float *centroid = ctx->gram_blocks.as<float>();
+    float *bradius = centroid + nblk * d;
+    int32_t *row_count = reinterpret_cast<int32_t *>(bradius + nblk);
+    int64_t *row_off = reinterpret_cast<int64_t *>(
+        (reinterpret_cast<uintptr_t>(row_count + nblk + 1) + 15) & ~uintptr_t(15));
+    const float Rf = prune ? (float)Rsearch : INFINITY;
+    if (prune) {
+        block_bounds_kernel<<<(unsigned)nblk, 256, 0, st>>>(ctx->x, n, d, colsum, perm, centroid, bradius);
+        CNN_LAUNCH_CHECK(ctx);
+    } else {
+        CNN_CUDA(ctx, cudaMemsetAsync(centroid, 0, sizeof(float) * (size_t)nblk * (d + 1), st));
+    }
+    tile_list_kernel<false><<<(unsigned)nblk, 256, 0, st>>>(centroid, bradius, d, nblk, Rf, row_count, nullptr,
+                                                             nullptr);
+    CNN_LAUNCH_CHECK(ctx);
+    CNN_CUDA(ctx, cudaMemsetAsync(row_count + nblk, 0, sizeof(int32_t), st));
+    CNN_TRY(scan_exclusive_i32_to_i64(ctx, row_count, row_off, nblk + 1));
+    int64_t ntiles = 0;
+    CNN_CUDA(ctx, cudaMemcpyAsync(&ntiles, row_off + nblk, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    CNN_CUDA(ctx, cudaStreamSynchronize(st));
+    CNN_TRY(ctx->ensure(ctx->gram_tiles, sizeof(int2) * (size_t)(ntiles > 0 ? ntiles : 1)));
+    tile_list_kernel<true><<<(unsigned)nblk, 256, 0, st>>>(centroid, bradius, d, nblk, Rf, nullptr, row_off,
+                                                            ctx->gram_tiles.as<int2>());
+    CNN_LAUNCH_CHECK(ctx);
 
     CUtensorMap map_hi, map_lo;
     if (!make_map(&map_hi, ctx->gram_hi.ptr, n, dp) || !make_map(&map_lo, ctx->gram_lo.ptr, n, dp))
@@ -662,6 +835,7 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     a.nkb = nkb;
     a.nblk = (int32_t)nblk;
     a.ntiles = ntiles;
+    a.tiles = ctx->gram_tiles.as<int2>();
     a.rc2 = (float)rc2;
     a.coef = (float)coef;
     a.slack_coef = (float)(8.0 * ldexp(1.0, -24));  // float32 rounding of |x|^2, |y|^2 and the fma
@@ -695,6 +869,11 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
         gram_search_kernel<<<grid, kGramThreads, smem, st>>>(map_hi, map_lo, a);
         CNN_LAUNCH_CHECK(ctx);
         stage_end(ctx, 9);
+        // internal indices -> point indices (before the recheck appends more keys)
+        map_keys_kernel<<<152u * 8u, 256, 0, st>>>(a.keys, nkeys, key_cap, perm);
+        CNN_LAUNCH_CHECK(ctx);
+        map_keys_kernel<<<152u * 8u, 256, 0, st>>>(a.amb, namb, amb_cap, perm);
+        CNN_LAUNCH_CHECK(ctx);
         gram_recheck_kernel<<<std::min<unsigned>(grid_for(amb_cap, 256), 152u * 8u), 256, 0, st>>>(
             ctx->x, d, a.amb, namb, amb_cap, radius_cutoff, metric, fpmode, a.keys, nkeys, key_cap, a.amb_d2,
             max_err_bits);
@@ -718,7 +897,6 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
             ctx->stats.filter_band = std::max(coef, 0.0);
             ctx->stats.filter_enabled = 1;
             // CSR: sort keys by (row, col), rows from the high half
-            const int bits_n = [&] { int b = 1; while (b < 62 && (int64_t(1) << b) < n) ++b; return b; }();
             CNN_TRY(radix_sort_u64(ctx, a.keys, nk, 32 + bits_n));
             CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nk > 0 ? nk : 1)));
             int32_t *deg = ctx->deg.as<int32_t>();
