@@ -348,7 +348,7 @@ def run_gpu(args):
     line = {
         "metric": METRIC, "value": world * n / (max_ms * 1e-3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": max_ms, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded md3d generator)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": f"synthetic (seeded {WORKLOAD['gen'][0]} generator)",
         "config": {"workload": W["name"], "n_points": n, "n_dim": W["d"], "radius_cutoff": W["radius_cutoff"],
                    "cnn_cutoff": W["cnn_cutoff"], "member_cutoff": W["member_cutoff"],
                    "neighbour_pairs": nnz, "l2": "flushed between steps (256 MiB write)",
@@ -405,6 +405,8 @@ def run_sweep(args):
                 ctx.build_neighbours(rr)
                 ctx.fit(sc, nm, 1, con, lab)
                 ctx.sort_by_size(lab, 2, None)
+                if check is not None:
+                    stream.synchronize()  # the library writes lab on its own stream
                 if check is not None and not torch.equal(lab, check[k, j]):
                     raise SystemExit(f"bench: sweep differs from the separate fit at r={radii[k]}, c={cuts[j]}")
 
@@ -475,9 +477,22 @@ def run_serve(args):
             plain_jobs = [serve.Job(job_id=i, **dict(raw[i], arrival=float(base[i] / rate))) for i in range(n_jobs)]
             serve.serve_one_at_a_time(plain_jobs, device=local, realtime=True)
             plain = serve.latency_summary(plain_jobs)
-            same = all(np.array_equal(a.labels, b.labels) for a, b in zip(jobs, plain_jobs))
+            differ = [(a, b) for a, b in zip(jobs, plain_jobs)
+                      if a.labels is None or b.labels is None or not np.array_equal(a.labels, b.labels)]
+            detail = []
+            for a, b in differ[:5]:
+                from commonnnclustering_gb300 import _abi
+                c = _abi.Context(local)
+                alone = serve.run_job_alone(c, a)  # a fresh context decides which side is off
+                c.close()
+                detail.append({"job": a.job_id, "n": int(a.points.shape[0]), "d": int(a.points.shape[1]),
+                               "radius_cutoff": a.radius_cutoff, "cnn_cutoff": a.cnn_cutoff,
+                               "error_mix": a.error, "error_alone": b.error,
+                               "mix_equals_fresh": a.labels is not None and bool(np.array_equal(a.labels, alone)),
+                               "alone_equals_fresh": b.labels is not None and bool(np.array_equal(b.labels, alone))})
             results.append({"rate_jobs_per_s": rate, "jobs": n_jobs, "continuous_batching": batched,
-                            "one_at_a_time": plain, "identical_labels": same,
+                            "one_at_a_time": plain, "identical_labels": not differ,
+                            "jobs_differing": len(differ), "differing": detail,
                             "max_jobs_in_flight": srv.max_in_flight})
     finally:
         srv.close()
@@ -541,7 +556,7 @@ def run_reference(args):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean_s * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded md3d generator)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": f"synthetic (seeded {WORKLOAD['gen'][0]} generator)",
         "config": {"workload": W["name"], "n_points": n, "n_dim": W["d"], "radius_cutoff": W["radius_cutoff"],
                    "cnn_cutoff": W["cnn_cutoff"], "member_cutoff": W["member_cutoff"]},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",

@@ -1,6 +1,7 @@
 // cnngpu.cu -- the C ABI: context lifetime, argument checks, host<->device
 // staging, and dispatch to the kernels in search.cu / fit.cu / prims.cu.
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <new>
@@ -69,6 +70,7 @@ CNN_API cnn_status cnn_create(cnn_context **out, int device, void *stream) {
     cnn_context *ctx = new (std::nothrow) cnn_context();
     if (!ctx) return CNN_ERR_OOM;
     ctx->device = device;
+    if (const char *pz = getenv("CNN_DEBUG_POISON")) ctx->poison = atoi(pz) & 0xff;
     if (cudaSetDevice(device) != cudaSuccess) {
         delete ctx;
         return CNN_ERR_CUDA;
@@ -101,9 +103,9 @@ CNN_API cnn_status cnn_destroy(cnn_context *ctx) {
                            &ctx->cols, &ctx->xf4, &ctx->cell_of, &ctx->cell_start, &ctx->node, &ctx->parent,
                            &ctx->comp_min, &ctx->flag, &ctx->counters, &ctx->stage_labels, &ctx->gram_hi,
                            &ctx->gram_lo, &ctx->gram_aux, &ctx->gram_keys, &ctx->gram_amb,
-                           &ctx->gram_blocks, &ctx->gram_tiles,
+                           &ctx->gram_blocks, &ctx->gram_tiles, &ctx->gram_perm,
                            &ctx->sweep_bucket, &ctx->sweep_row_off_max, &ctx->sweep_cols_max,
-                           &ctx->sweep_deg_max, &ctx->sweep_consider,
+                           &ctx->sweep_deg_max, &ctx->sweep_consider, &ctx->sweep_forest,
                            &ctx->stage_consider, &ctx->stage_offsets, &ctx->stage_indices, &ctx->stage_misc,
                            &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->scratch_a, &ctx->scratch_b,
                            &ctx->scratch_c, &ctx->scratch_d, &ctx->scan_tmp};

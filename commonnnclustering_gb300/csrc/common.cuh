@@ -65,6 +65,7 @@ struct cnn_context {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     bool timing = false;
+    int poison = -1;  // >= 0: fill every new workspace allocation with this byte (CNN_DEBUG_POISON)
     int64_t n_launches = 0;
     std::string last_error;
     cnn_stats stats{};
@@ -94,10 +95,10 @@ struct cnn_context {
 
     // batched (radius, cut) sweep: the largest-radius graph kept aside,
     // per-pair radius buckets, consider flags of the per-fit runs
-    cnn::DevBuf sweep_bucket, sweep_row_off_max, sweep_cols_max, sweep_deg_max, sweep_consider;
+    cnn::DevBuf sweep_bucket, sweep_row_off_max, sweep_cols_max, sweep_deg_max, sweep_consider, sweep_forest;
 
     // tensor-core (Gram) search for n_dim >= 16
-    cnn::DevBuf gram_hi, gram_lo, gram_aux, gram_keys, gram_amb, gram_blocks, gram_tiles;
+    cnn::DevBuf gram_hi, gram_lo, gram_aux, gram_keys, gram_amb, gram_blocks, gram_tiles, gram_perm;
     int64_t gram_key_hint = 0;
 
     // fit work arrays
@@ -141,6 +142,11 @@ struct cnn_context {
                         std::string("cudaMalloc(") + std::to_string(want) + "): " + cudaGetErrorString(e));
         }
         b.cap = want;
+        if (poison >= 0) {
+            // debugging aid: stale workspace contents must never change a result
+            e = cudaMemsetAsync(b.ptr, poison, want, stream);
+            if (e != cudaSuccess) return fail(CNN_ERR_CUDA, cudaGetErrorString(e));
+        }
         return CNN_OK;
     }
 };
@@ -166,15 +172,19 @@ cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev,
 cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode, bool *used);
 
 // fit.cu
+// seed_a / seed_b (optional, internal order): per point a node of a finished
+// fit on the same graph order whose components refine this fit's (-1: none)
 cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
-                    int64_t current_start, uint8_t *consider_dev, int64_t *labels_dev);
+                    int64_t current_start, uint8_t *consider_dev, int64_t *labels_dev,
+                    const int32_t *seed_a = nullptr, const int32_t *seed_b = nullptr);
 cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels_dev, int64_t n,
                              int64_t member_cutoff, int64_t max_clusters);
 cnn_status check_lists_impl(cnn_context *ctx, const int32_t *a, int64_t na, const int32_t *b,
                             int64_t nb, int64_t c, int32_t *result_dev);
 // a fresh fit (labels 0, consider 1, current_start 1) and sort_by_size into labels_dev
 cnn_status fit_and_sort_into(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
-                             int64_t sort_member_cutoff, int64_t max_clusters, int64_t *labels_dev);
+                             int64_t sort_member_cutoff, int64_t max_clusters, int64_t *labels_dev,
+                             const int32_t *seed_a = nullptr, const int32_t *seed_b = nullptr);
 
 // sweep.cu
 cnn_status sweep_impl(cnn_context *ctx, const double *radius_cutoffs, int32_t n_radii,

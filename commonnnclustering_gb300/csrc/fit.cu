@@ -293,8 +293,20 @@ int bits_for_fit(int64_t n) {
     return b;
 }
 
+// Seeds (batched sweep): join every node p with seed[p] (a node, or -1) of
+// a finished fit whose components refine this fit's components.
+__global__ void seed_union_kernel(int64_t n, const uint8_t *__restrict__ node, int32_t *__restrict__ parent,
+                                  const int32_t *__restrict__ seed_a, const int32_t *__restrict__ seed_b) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        if (!node[p]) continue;
+        const int32_t a = seed_a ? seed_a[p] : -1, b = seed_b ? seed_b[p] : -1;
+        if (a >= 0 && a != p && node[a]) uf_unite(parent, (int32_t)p, a);
+        if (b >= 0 && b != p && node[b]) uf_unite(parent, (int32_t)p, b);
+    }
+}
+
 cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff, int64_t current_start,
-                    uint8_t *consider_dev, int64_t *labels_dev) {
+                    uint8_t *consider_dev, int64_t *labels_dev, const int32_t *seed_a, const int32_t *seed_b) {
     if (!ctx->have_graph) return ctx->fail(CNN_ERR_STATE, "no neighbour graph: call cnn_build_neighbours first");
     const int64_t n = ctx->n;
     cudaStream_t st = ctx->stream;
@@ -318,6 +330,10 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     node_kernel<<<blocks_for(n), 256, 0, st>>>(ctx->deg.as<int32_t>(), perm, consider_dev, n, n_member_cutoff,
                                                node, parent, comp_min, counters);
     CNN_LAUNCH_CHECK(ctx);
+    if (seed_a || seed_b) {
+        seed_union_kernel<<<blocks_for(n), 256, 0, st>>>(n, node, parent, seed_a, seed_b);
+        CNN_LAUNCH_CHECK(ctx);
+    }
     stage_end(ctx, 5);
 
     stage_begin(ctx, 6);
@@ -468,14 +484,16 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64
 // (src/cnnclustering/cluster.pyx:316-364): labels 0, consider 1,
 // current_start 1, the fit, then sort_by_size.
 cnn_status fit_and_sort_into(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
-                             int64_t sort_member_cutoff, int64_t max_clusters, int64_t *labels_dev) {
+                             int64_t sort_member_cutoff, int64_t max_clusters, int64_t *labels_dev,
+                             const int32_t *seed_a, const int32_t *seed_b) {
     const int64_t n = ctx->n;
     cudaStream_t st = ctx->stream;
     if (n == 0) return CNN_OK;
     CNN_TRY(ctx->ensure(ctx->sweep_consider, (size_t)n));
     CNN_CUDA(ctx, cudaMemsetAsync(labels_dev, 0, sizeof(int64_t) * (size_t)n, st));
     CNN_CUDA(ctx, cudaMemsetAsync(ctx->sweep_consider.ptr, 1, (size_t)n, st));
-    CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, 1, ctx->sweep_consider.as<uint8_t>(), labels_dev));
+    CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, 1, ctx->sweep_consider.as<uint8_t>(), labels_dev,
+                     seed_a, seed_b));
     return sort_by_size_impl(ctx, labels_dev, n, sort_member_cutoff, max_clusters);
 }
 

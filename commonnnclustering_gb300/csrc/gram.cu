@@ -449,37 +449,47 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
 }
 
 // ---- preparation: centring, BF16 split, norms ------------------------------------
-__global__ void column_sum_kernel(const double *__restrict__ x, int64_t n, int d, double *__restrict__ sum) {
+// Column sums of the finite coordinates; *nonfinite set if any coordinate is not.
+__global__ void column_sum_kernel(const double *__restrict__ x, int64_t n, int d, double *__restrict__ sum,
+                                  int *__restrict__ nonfinite) {
     const int k = blockIdx.y;
     double s = 0;
+    bool fin = true;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double v = x[i * d + k];
         if (isfinite(v)) s += v;
+        else fin = false;
     }
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&sum[k], s);
+    fin = __all_sync(0xffffffffu, fin);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&sum[k], s);
+        if (!fin) atomicExch(nonfinite, 1);
+    }
 }
 
-// One warp per point (internal order i = perm position): split x - mean into
-// hi/lo bf16 (K padded with zeros to dp), float32 squared norm, per-block max
-// norm (as ordered int bits).
-__global__ void gram_prep_kernel(const double *__restrict__ x, int64_t n, int d, int dp,
-                                 const double *__restrict__ sum, const int32_t *__restrict__ perm,
+__global__ void column_mean_kernel(double *__restrict__ sum, int d, int64_t n) {
+    for (int k = threadIdx.x; k < d; k += blockDim.x) sum[k] = sum[k] / (double)n;
+}
+
+// One warp per row of the padded internal order (perm[i] = point index, -1
+// for an empty row): split x - mean into hi/lo bf16 (K padded with zeros to
+// dp), float32 squared norm (+inf for an empty row), per-block max norm (as
+// ordered int bits).  All coordinates are finite here.
+__global__ void gram_prep_kernel(const double *__restrict__ x, int64_t n_rows, int64_t n, int d, int dp,
+                                 const double *__restrict__ mean, const int32_t *__restrict__ perm,
                                  __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ lo,
                                  float *__restrict__ norm2, unsigned *__restrict__ blk_norm_bits,
-                                 unsigned *__restrict__ blk_norm2_bits, int *__restrict__ nonfinite) {
+                                 unsigned *__restrict__ blk_norm2_bits) {
     const int lane = threadIdx.x & 31;
     const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (i >= n) return;
+    if (i >= n_rows) return;
     const int64_t src = perm[i];
     double s2 = 0;
-    bool fin = true;
     for (int k = lane; k < dp; k += 32) {
         float h = 0.f, l = 0.f;
-        if (k < d) {
-            const double v = x[src * d + k];
-            fin = fin && isfinite(v);
-            const double c = v - sum[k] / (double)n;
+        if (k < d && src >= 0) {
+            const double c = x[src * d + k] - mean[k];
             const float cf = (float)c;
             const __nv_bfloat16 hb = __float2bfloat16_rn(cf);
             h = __bfloat162float(hb);
@@ -490,95 +500,159 @@ __global__ void gram_prep_kernel(const double *__restrict__ x, int64_t n, int d,
         lo[i * dp + k] = __float2bfloat16_rn(l);
     }
     for (int o = 16; o > 0; o >>= 1) s2 += __shfl_down_sync(0xffffffffu, s2, o);
-    fin = __all_sync(0xffffffffu, fin);
     if (lane == 0) {
-        const float n2 = fin ? (float)s2 : INFINITY;
-        norm2[i] = n2;
-        if (!fin) atomicExch(nonfinite, 1);
-        const float nrm = sqrtf(fin ? (float)s2 : 0.f) * (1.f + 1e-6f);
-        atomicMax(&blk_norm_bits[i / kTM], __float_as_uint(nrm));
-        atomicMax(&blk_norm2_bits[i / kTM], __float_as_uint(fin ? (float)s2 * (1.f + 1e-6f) : 0.f));
+        if (src < 0) {
+            norm2[i] = INFINITY;
+        } else {
+            norm2[i] = (float)s2;
+            const float nrm = sqrtf((float)s2) * (1.f + 1e-6f);
+            atomicMax(&blk_norm_bits[i / kTM], __float_as_uint(nrm));
+            atomicMax(&blk_norm2_bits[i / kTM], __float_as_uint((float)s2 * (1.f + 1e-6f)));
+        }
     }
 }
 
 // ---- tile pruning ---------------------------------------------------------------
 // Points are grouped by their nearest pivot (float32, centred coordinates;
-// any grouping gives the same result, compact groups let more tiles go).
-// One warp per point, lane k holding coordinates k, k+32, k+64, k+96
-// (n_dim <= 128); pivots staged in shared memory.
-__global__ void pivot_assign_kernel(const double *__restrict__ x, int64_t n, int d, const double *__restrict__ sum,
-                                    int32_t n_pivots, int bits_n, uint64_t *__restrict__ keys) {
-    extern __shared__ float s_piv[];  // [n_pivots][d]
+// any grouping gives the same result, compact groups let more tiles go) and
+// every group starts on a 128-row block boundary, so that no block mixes two
+// groups.  Rows left over at a group's end are empty (no point, infinite
+// norm): they never produce a pair.
+//
+// One thread per point, its coordinates in registers (n_dim <= 4 * kV4,
+// padded with zeros to a multiple of 4); pivots in shared memory as float4 rows
+// read by broadcast.  The score |p|^2 - 2 x.p ranks pivots like |x - p|^2.
+template <int kV4>
+__global__ void __launch_bounds__(256) pivot_assign_kernel(const double *__restrict__ x, int64_t n, int d,
+                                                           const double *__restrict__ mean, int32_t n_pivots,
+                                                           int bits_n, uint64_t *__restrict__ keys) {
+    extern __shared__ float4 s_piv4[];  // [n_pivots][nv4], then |p|^2 per pivot
+    const int nv4 = (d + 3) / 4;
+    float *s_pn = reinterpret_cast<float *>(s_piv4 + (size_t)n_pivots * nv4);
+    float *s_piv = reinterpret_cast<float *>(s_piv4);
     const int64_t stride = n / n_pivots;
-    for (int e = threadIdx.x; e < n_pivots * d; e += blockDim.x) {
-        const int kp = e / d, k = e - kp * d;
-        s_piv[e] = (float)(x[(int64_t)kp * stride * d + k] - sum[k] / (double)n);
+    for (int e = threadIdx.x; e < n_pivots * nv4 * 4; e += blockDim.x) {
+        const int kp = e / (nv4 * 4), k = e - kp * nv4 * 4;
+        s_piv[e] = k < d ? (float)(x[(int64_t)kp * stride * d + k] - mean[k]) : 0.f;
     }
     __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t i = w0; i < n; i += nw) {
-        float xc[4];
+    for (int kp = threadIdx.x; kp < n_pivots; kp += blockDim.x) {
+        float s2 = 0.f;
+        for (int k = 0; k < nv4 * 4; ++k) s2 = fmaf(s_piv[kp * nv4 * 4 + k], s_piv[kp * nv4 * 4 + k], s2);
+        s_pn[kp] = s2;
+    }
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float4 xv[kV4];
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const int k = lane + 32 * c;
-            xc[c] = k < d ? (float)(x[i * d + k] - sum[k] / (double)n) : 0.f;
+        for (int v = 0; v < kV4; ++v) {
+            float c[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int k = 4 * v + q;
+                c[q] = k < d ? (float)(x[i * d + k] - mean[k]) : 0.f;
+            }
+            xv[v] = make_float4(-2.f * c[0], -2.f * c[1], -2.f * c[2], -2.f * c[3]);
         }
         float best = INFINITY;
         int32_t bi = 0;
         for (int kp = 0; kp < n_pivots; ++kp) {
-            const float *pv = s_piv + kp * d;
-            float acc = 0.f;
+            const float4 *pv = s_piv4 + (size_t)kp * nv4;
+            float acc = s_pn[kp];
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const int k = lane + 32 * c;
-                if (k < d) {
-                    const float t = xc[c] - pv[k];
-                    acc = fmaf(t, t, acc);
+            for (int v = 0; v < kV4; ++v) {
+                if (v < nv4) {
+                    const float4 p = pv[v];
+                    acc = fmaf(xv[v].x, p.x, acc);
+                    acc = fmaf(xv[v].y, p.y, acc);
+                    acc = fmaf(xv[v].z, p.z, acc);
+                    acc = fmaf(xv[v].w, p.w, acc);
                 }
             }
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
             if (acc < best) {
                 best = acc;
                 bi = kp;
             }
         }
-        if (lane == 0) keys[i] = ((uint64_t)(uint32_t)bi << bits_n) | (uint64_t)i;
+        keys[i] = ((uint64_t)(uint32_t)bi << bits_n) | (uint64_t)i;
     }
 }
 
-__global__ void perm_from_keys_kernel(const uint64_t *__restrict__ keys, int64_t n, int bits_n,
-                                      int32_t *__restrict__ perm) {
-    const uint64_t mask = (1ull << bits_n) - 1;
+// Group sizes from the pivot keys (any order).
+__global__ void group_count_kernel(const uint64_t *__restrict__ keys, int64_t n, int bits_n, int32_t n_groups,
+                                   int32_t *__restrict__ count) {
+    extern __shared__ int32_t s_cnt[];
+    for (int g = threadIdx.x; g < n_groups; g += blockDim.x) s_cnt[g] = 0;
+    __syncthreads();
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
-        perm[p] = (int32_t)(keys[p] & mask);
+        atomicAdd(&s_cnt[(int)(keys[p] >> bits_n)], 1);
+    __syncthreads();
+    for (int g = threadIdx.x; g < n_groups; g += blockDim.x)
+        if (s_cnt[g]) atomicAdd(&count[g], s_cnt[g]);
 }
 
-// Per row block (internal order): centroid and radius of its points.
-// Float32 values rounded outward enough for the pruning test below.
-__global__ void block_bounds_kernel(const double *__restrict__ x, int64_t n, int d, const double *__restrict__ sum,
-                                    const int32_t *__restrict__ perm, float *__restrict__ centroid,
-                                    float *__restrict__ radius) {
+// Start of every group among the sorted keys and in the padded row order
+// (groups rounded up to whole 128-row blocks); [n_groups] holds the totals.
+__global__ void group_layout_kernel(const int32_t *__restrict__ count, int32_t n_groups, int64_t *__restrict__ start,
+                                    int64_t *__restrict__ pstart) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int64_t s = 0, ps = 0;
+    for (int g = 0; g < n_groups; ++g) {
+        start[g] = s;
+        pstart[g] = ps;
+        s += count[g];
+        ps += (count[g] + kTM - 1) / kTM * kTM;
+    }
+    start[n_groups] = s;
+    pstart[n_groups] = ps;
+}
+
+// Padded row -> point index (rows not written stay -1).
+__global__ void padded_perm_kernel(const uint64_t *__restrict__ keys, int64_t n, int bits_n,
+                                   const int64_t *__restrict__ start, const int64_t *__restrict__ pstart,
+                                   int32_t *__restrict__ perm) {
+    const uint64_t mask = (1ull << bits_n) - 1;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = keys[p];
+        const int g = (int)(k >> bits_n);
+        perm[pstart[g] + (p - start[g])] = (int32_t)(k & mask);
+    }
+}
+
+// Per row block (padded internal order): centroid and radius of its points
+// (empty rows skipped; every block holds at least one point).  Float32
+// values rounded outward enough for the pruning test below.
+__global__ void block_bounds_kernel(const double *__restrict__ x, int64_t n_rows, int64_t n, int d,
+                                    const double *__restrict__ mean, const int32_t *__restrict__ perm,
+                                    float *__restrict__ centroid, float *__restrict__ radius) {
     __shared__ double s_c[128];
     __shared__ double s_r[256];
+    __shared__ int32_t s_src[kTM];
+    __shared__ int s_rows;
     const int64_t I = blockIdx.x;
-    const int64_t r0 = I * kTM, r1 = min(n, r0 + kTM);
-    const int rows = (int)(r1 - r0);
+    const int64_t r0 = I * kTM, r1 = min(n_rows, r0 + kTM);
+    if (threadIdx.x == 0) {
+        int m = 0;
+        for (int64_t r = r0; r < r1; ++r)
+            if (perm[r] >= 0) s_src[m++] = perm[r];
+        s_rows = m;
+    }
+    __syncthreads();
+    const int rows = s_rows;
     for (int k = threadIdx.x; k < d; k += blockDim.x) {
         double c = 0;
-        for (int r = 0; r < rows; ++r) c += x[(int64_t)perm[r0 + r] * d + k] - sum[k] / (double)n;
-        s_c[k] = c / rows;
+        for (int r = 0; r < rows; ++r) c += x[(int64_t)s_src[r] * d + k] - mean[k];
+        s_c[k] = rows > 0 ? c / rows : 0.0;
         centroid[I * d + k] = (float)s_c[k];
     }
     __syncthreads();
     double m = 0;
     for (int r = threadIdx.x; r < rows; r += blockDim.x) {
         double s = 0;
-        const int64_t src = perm[r0 + r];
+        const int64_t src = s_src[r];
         for (int k = 0; k < d; ++k) {
             // distance to the float32 centroid actually used in the test
-            const double t = (x[src * d + k] - sum[k] / (double)n) - (double)(float)s_c[k];
+            const double t = (x[src * d + k] - mean[k]) - (double)(float)s_c[k];
             s += t * t;
         }
         m = fmax(m, s);
@@ -595,58 +669,93 @@ __global__ void block_bounds_kernel(const double *__restrict__ x, int64_t n, int
 // Can blocks I and J (J >= I) hold a pair within R?  |c_I - c_J| - rho_I -
 // rho_J > R means every pair is farther than R (triangle inequality); the
 // margin covers the float32 evaluation of the centroid distance.
-__device__ __forceinline__ bool blocks_may_touch(const float *__restrict__ centroid, const float *__restrict__ radius,
-                                                 int d, int64_t I, int64_t J, float R) {
-    if (I == J) return true;
-    const float *a = centroid + I * d, *b = centroid + J * d;
-    float s = 0.f, na = 0.f, nb = 0.f;
-    for (int k = 0; k < d; ++k) {
-        const float t = a[k] - b[k];
-        s = fmaf(t, t, s);
-        na = fmaf(a[k], a[k], na);
-        nb = fmaf(b[k], b[k], nb);
-    }
-    const float margin = 1e-5f * (sqrtf(na) + sqrtf(nb) + radius[I] + radius[J] + R);
-    return sqrtf(s) - radius[I] - radius[J] <= R + margin;
-}
+//
+// kListRows consecutive rows I per CTA: their centroids sit in shared memory
+// and every column centroid J is read once for all of them.  Pass 1 counts
+// the kept J per row, pass 2 writes them (order within a row is arbitrary).
+constexpr int kListRows = 8;
 
-// Row I of the tile triangle: count (pass 1) or write (pass 2) its kept J.
 template <bool kWrite>
-__global__ void tile_list_kernel(const float *__restrict__ centroid, const float *__restrict__ radius, int d,
-                                 int64_t nblk, float R, int32_t *__restrict__ row_count,
-                                 const int64_t *__restrict__ row_off, int2 *__restrict__ tiles) {
-    __shared__ int32_t s_cnt;
-    const int64_t I = blockIdx.x;
-    if (threadIdx.x == 0) s_cnt = 0;
+__global__ void __launch_bounds__(256) tile_list_kernel(const float *__restrict__ centroid,
+                                                        const float *__restrict__ radius, int d, int64_t nblk,
+                                                        float R, int32_t *__restrict__ row_count,
+                                                        const int64_t *__restrict__ row_off, int2 *__restrict__ tiles) {
+    __shared__ float s_a[kListRows][128];
+    __shared__ float s_na[kListRows], s_ra[kListRows];
+    __shared__ int32_t s_cnt[kListRows];
+    const int64_t I0 = (int64_t)blockIdx.x * kListRows;
+    const int rows = (int)min((int64_t)kListRows, nblk - I0);
+    const bool keep_all = !(R < INFINITY);  // no pruning (centroids unused; n_dim may exceed 128)
+    for (int e = threadIdx.x; e < kListRows * d && !keep_all; e += blockDim.x) {
+        const int r = e / d, k = e - r * d;
+        s_a[r][k] = r < rows ? centroid[(I0 + r) * d + k] : 0.f;
+    }
+    if (threadIdx.x < kListRows) {
+        s_cnt[threadIdx.x] = 0;
+        s_ra[threadIdx.x] = threadIdx.x < rows ? radius[I0 + threadIdx.x] : 0.f;
+    }
     __syncthreads();
-    for (int64_t J = I + threadIdx.x; J < nblk; J += blockDim.x) {
-        if (blocks_may_touch(centroid, radius, d, I, J, R)) {
-            const int32_t k = atomicAdd(&s_cnt, 1);
-            if (kWrite) tiles[row_off[I] + k] = make_int2((int32_t)I, (int32_t)J);
+    if (threadIdx.x < kListRows && !keep_all) {
+        float na = 0.f;
+        for (int k = 0; k < d; ++k) na = fmaf(s_a[threadIdx.x][k], s_a[threadIdx.x][k], na);
+        s_na[threadIdx.x] = sqrtf(na);
+    }
+    __syncthreads();
+    for (int64_t J = I0 + threadIdx.x; J < nblk; J += blockDim.x) {
+        const float *b = centroid + J * d;
+        float s[kListRows];
+#pragma unroll
+        for (int r = 0; r < kListRows; ++r) s[r] = 0.f;
+        float nb = 0.f;
+        for (int k = 0; k < d && !keep_all; ++k) {
+            const float bk = b[k];
+            nb = fmaf(bk, bk, nb);
+#pragma unroll
+            for (int r = 0; r < kListRows; ++r) {
+                const float t = s_a[r][k] - bk;
+                s[r] = fmaf(t, t, s[r]);
+            }
+        }
+        const float rb = keep_all ? 0.f : radius[J];
+        nb = sqrtf(nb);
+#pragma unroll
+        for (int r = 0; r < kListRows; ++r) {
+            const int64_t I = I0 + r;
+            if (r >= rows || J < I) continue;
+            const float margin = 1e-5f * (s_na[r] + nb + s_ra[r] + rb + R);
+            const bool touch = keep_all || J == I || sqrtf(s[r]) - s_ra[r] - rb <= R + margin;
+            if (touch) {
+                const int32_t k = atomicAdd(&s_cnt[r], 1);
+                if (kWrite) tiles[row_off[I] + k] = make_int2((int32_t)I, (int32_t)J);
+            }
         }
     }
     __syncthreads();
-    if (!kWrite && threadIdx.x == 0) row_count[I] = s_cnt;
+    if (!kWrite && threadIdx.x < rows) row_count[I0 + threadIdx.x] = s_cnt[threadIdx.x];
 }
 
-// internal indices -> point indices in the key lists (bit 63 kept)
+// internal indices -> point indices in a key list.  pack_bits > 0: write
+// (row << pack_bits | col), the sort key of the CSR; 0: keep (row << 32 |
+// col) and bit 63 (the band list).
 __global__ void map_keys_kernel(uint64_t *__restrict__ keys, const unsigned long long *__restrict__ count,
-                                int64_t cap, const int32_t *__restrict__ perm) {
+                                int64_t cap, const int32_t *__restrict__ perm, int pack_bits) {
     const int64_t nk = min((int64_t)*count, cap);
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nk; e += (int64_t)gridDim.x * blockDim.x) {
         const uint64_t k = keys[e];
         const uint64_t flag = k & (1ull << 63);
-        const uint64_t a = (k >> 32) & 0x7fffffffull, b = k & 0xffffffffull;
-        keys[e] = flag | ((uint64_t)(uint32_t)perm[a] << 32) | (uint64_t)(uint32_t)perm[b];
+        const uint64_t a = (uint32_t)perm[(k >> 32) & 0x7fffffffull], b = (uint32_t)perm[k & 0xffffffffull];
+        keys[e] = pack_bits > 0 ? (a << pack_bits) | b : flag | (a << 32) | b;
     }
 }
 
-// Band pairs in float64, reference order; hits appended to the key list.
+// Band pairs in float64, reference order; hits appended to the key list
+// as packed (row << pack_bits | col).
 __global__ void gram_recheck_kernel(const double *__restrict__ x, int d, const uint64_t *__restrict__ amb,
                                     const unsigned long long *__restrict__ namb, int64_t amb_cap, double rc,
                                     int metric, int fpmode, uint64_t *__restrict__ keys,
                                     unsigned long long *__restrict__ nkeys, int64_t key_cap,
-                                    const float *__restrict__ amb_d2, unsigned *__restrict__ max_err_bits) {
+                                    const float *__restrict__ amb_d2, unsigned *__restrict__ max_err_bits,
+                                    int pack_bits) {
     const int64_t total = min((int64_t)*namb, amb_cap);
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
         const uint64_t a = amb[e];
@@ -668,21 +777,33 @@ __global__ void gram_recheck_kernel(const double *__restrict__ x, int d, const u
         const double sv = metric == CNN_METRIC_EUCLIDEAN ? __dsqrt_rn(s) : s;
         if (sv <= rc) {
             const unsigned long long w = atomicAdd(nkeys, both ? 2ull : 1ull);
-            if (w < (unsigned long long)key_cap) keys[w] = ((uint64_t)i << 32) | (uint64_t)j;
-            if (both && w + 1 < (unsigned long long)key_cap) keys[w + 1] = ((uint64_t)j << 32) | (uint64_t)i;
+            if (w < (unsigned long long)key_cap) keys[w] = ((uint64_t)i << pack_bits) | (uint64_t)j;
+            if (both && w + 1 < (unsigned long long)key_cap) keys[w + 1] = ((uint64_t)j << pack_bits) | (uint64_t)i;
         }
         const float err = fabsf((float)(s - (double)amb_d2[e]));
         atomicMax(max_err_bits, __float_as_uint(err));
     }
 }
 
-__global__ void keys_rows_kernel(const uint64_t *__restrict__ keys, int64_t nk, int32_t *__restrict__ deg,
-                                 int32_t *__restrict__ cols) {
+// Sorted packed keys -> CSR: row starts at the key where the row changes
+// (rows without keys get the next start), column indices from the low bits.
+__global__ void keys_rows_kernel(const uint64_t *__restrict__ keys, int64_t nk, int pack_bits, int64_t n,
+                                 int64_t *__restrict__ row_off, int32_t *__restrict__ cols) {
+    const uint64_t mask = (1ull << pack_bits) - 1;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nk; e += (int64_t)gridDim.x * blockDim.x) {
         const uint64_t k = keys[e];
-        atomicAdd(&deg[(int64_t)(k >> 32)], 1);
-        cols[e] = (int32_t)(k & 0xffffffffull);
+        const int64_t r = (int64_t)(k >> pack_bits);
+        const int64_t rp = e == 0 ? -1 : (int64_t)(keys[e - 1] >> pack_bits);
+        for (int64_t q = rp + 1; q <= r; ++q) row_off[q] = e;
+        if (e == nk - 1)
+            for (int64_t q = r + 1; q <= n; ++q) row_off[q] = nk;
+        cols[e] = (int32_t)(k & mask);
     }
+}
+
+__global__ void degree_from_offsets_kernel(const int64_t *__restrict__ row_off, int64_t n, int32_t *__restrict__ deg) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p <= n; p += (int64_t)gridDim.x * blockDim.x)
+        deg[p] = p < n ? (int32_t)(row_off[p + 1] - row_off[p]) : 0;
 }
 
 typedef CUresult (*PFN_encodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -740,61 +861,95 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
 
     const int dp = (d + kKB - 1) / kKB * kKB;
     const int nkb = dp / kKB;
-    const int64_t nblk = (n + kTM - 1) / kTM;
     const double rc2 = metric == CNN_METRIC_EUCLIDEAN ? radius_cutoff * radius_cutoff : radius_cutoff;
-
-    // buffers: hi, lo (bf16 n x dp), norm2 (n), block norms, counters
-    CNN_TRY(ctx->ensure(ctx->gram_hi, sizeof(__nv_bfloat16) * (size_t)n * dp));
-    CNN_TRY(ctx->ensure(ctx->gram_lo, sizeof(__nv_bfloat16) * (size_t)n * dp));
-    CNN_TRY(ctx->ensure(ctx->gram_aux, sizeof(float) * (size_t)(n + 2 * nblk + 64) + sizeof(double) * (size_t)d + 256));
-    float *norm2 = ctx->gram_aux.as<float>();
-    unsigned *blk_norm_bits = reinterpret_cast<unsigned *>(norm2 + n);
-    unsigned *blk_norm2_bits = blk_norm_bits + nblk;
-    double *colsum = reinterpret_cast<double *>(
-        (reinterpret_cast<uintptr_t>(blk_norm2_bits + nblk + 16) + 15) & ~uintptr_t(15));
     unsigned long long *counters = ctx->counters.as<unsigned long long>();
     unsigned long long *nkeys = counters + 10, *namb = counters + 11;
     int *status = reinterpret_cast<int *>(counters + 12);
     int *nonfinite = reinterpret_cast<int *>(counters + 13);
     unsigned *max_err_bits = reinterpret_cast<unsigned *>(counters + 14);
     CNN_CUDA(ctx, cudaMemsetAsync(counters + 10, 0, 4 * sizeof(unsigned long long), st));
-    CNN_CUDA(ctx, cudaMemsetAsync(blk_norm_bits, 0, sizeof(unsigned) * 2 * (size_t)nblk, st));
+
+    // column sums (the centring) and the non-finite check
+    CNN_TRY(ctx->ensure(ctx->scratch_b, sizeof(double) * (size_t)d + 3 * sizeof(int64_t) * 1024 + 4096));
+    double *colsum = ctx->scratch_b.as<double>();
+    int32_t *gcount = reinterpret_cast<int32_t *>(colsum + d);
+    int64_t *gstart = reinterpret_cast<int64_t *>(
+        (reinterpret_cast<uintptr_t>(gcount + 1024) + 15) & ~uintptr_t(15));
+    int64_t *gpstart = gstart + 1024;
     CNN_CUDA(ctx, cudaMemsetAsync(colsum, 0, sizeof(double) * d, st));
     {
         const int blocks = (int)std::min<int64_t>(256, (n + 255) / 256);
-        column_sum_kernel<<<dim3(blocks, d), 256, 0, st>>>(ctx->x, n, d, colsum);
+        column_sum_kernel<<<dim3(blocks, d), 256, 0, st>>>(ctx->x, n, d, colsum, nonfinite);
+        CNN_LAUNCH_CHECK(ctx);
+        column_mean_kernel<<<1, 128, 0, st>>>(colsum, d, n);  // colsum holds the column means from here
         CNN_LAUNCH_CHECK(ctx);
     }
-    // internal order: points grouped by nearest pivot, so that 128-point
-    // blocks are compact and far-apart block pairs can be skipped
+    // internal order: points grouped by nearest pivot, every group starting
+    // on a block boundary, so that 128-row blocks are compact and far-apart
+    // block pairs can be skipped
     const int bits_n = [&] { int b = 1; while (b < 62 && (int64_t(1) << b) < n) ++b; return b; }();
     const bool prune = d <= 128 && n >= 8 * kTM;
-    int32_t *perm = ctx->perm.as<int32_t>();
+    int n_groups = 1;
     if (prune) {
-        const int n_pivots = (int)std::max<int64_t>(1, std::min<int64_t>({512, n / 1024, 98304 / (4 * d)}));
+        n_groups = (int)std::max<int64_t>(1, std::min<int64_t>({512, n / 1024, 98304 / (4 * ((d + 3) / 4 * 4))}));
         CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(uint64_t) * (size_t)n));
         uint64_t *pkeys = ctx->scratch_a.as<uint64_t>();
-        const size_t psmem = sizeof(float) * (size_t)n_pivots * d;
-        CNN_CUDA(ctx, cudaFuncSetAttribute(pivot_assign_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
-        pivot_assign_kernel<<<152 * 4, 256, psmem, st>>>(ctx->x, n, d, colsum, n_pivots, bits_n, pkeys);
-        CNN_LAUNCH_CHECK(ctx);
+        const size_t psmem = sizeof(float) * (size_t)n_groups * ((d + 3) / 4 * 4 + 1);
+        const unsigned pgrid = std::min<unsigned>(grid_for(n, 256), 152u * 8u);
+        auto launch_assign = [&](auto kern) -> cnn_status {
+            CNN_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+            kern<<<pgrid, 256, psmem, st>>>(ctx->x, n, d, colsum, n_groups, bits_n, pkeys);
+            CNN_LAUNCH_CHECK(ctx);
+            return CNN_OK;
+        };
+        if (d <= 32) CNN_TRY(launch_assign(pivot_assign_kernel<8>));
+        else if (d <= 64) CNN_TRY(launch_assign(pivot_assign_kernel<16>));
+        else if (d <= 96) CNN_TRY(launch_assign(pivot_assign_kernel<24>));
+        else CNN_TRY(launch_assign(pivot_assign_kernel<32>));
         int pb = 1;
-        while ((1 << pb) < n_pivots) ++pb;
+        while ((1 << pb) < n_groups) ++pb;
         CNN_TRY(radix_sort_u64(ctx, pkeys, n, bits_n + pb));
-        perm_from_keys_kernel<<<std::min<unsigned>(grid_for(n, 256), 4096u), 256, 0, st>>>(pkeys, n, bits_n, perm);
+        CNN_CUDA(ctx, cudaMemsetAsync(gcount, 0, sizeof(int32_t) * n_groups, st));
+        group_count_kernel<<<std::min<unsigned>(grid_for(n, 256), 152u * 2u), 256, sizeof(int32_t) * n_groups, st>>>(
+            pkeys, n, bits_n, n_groups, gcount);
+        CNN_LAUNCH_CHECK(ctx);
+        group_layout_kernel<<<1, 32, 0, st>>>(gcount, n_groups, gstart, gpstart);
+        CNN_LAUNCH_CHECK(ctx);
+    }
+    int64_t h_rows = n;
+    int h_nonfinite = 0;
+    if (prune) CNN_CUDA(ctx, cudaMemcpyAsync(&h_rows, gpstart + n_groups, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    CNN_CUDA(ctx, cudaMemcpyAsync(&h_nonfinite, nonfinite, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CNN_CUDA(ctx, cudaStreamSynchronize(st));
+    if (h_nonfinite) return CNN_OK;  // non-finite coordinates: the all-pairs path handles them
+    const int64_t n_rows = h_rows;   // padded internal rows (n without pruning)
+    if (n_rows >= (int64_t(1) << 31) - 256) return CNN_OK;
+    const int64_t nblk = (n_rows + kTM - 1) / kTM;
+
+    CNN_TRY(ctx->ensure(ctx->gram_perm, sizeof(int32_t) * (size_t)n_rows));
+    int32_t *perm = ctx->gram_perm.as<int32_t>();
+    if (prune) {
+        CNN_TRY(fill_i32(ctx, perm, n_rows, -1));
+        padded_perm_kernel<<<std::min<unsigned>(grid_for(n, 256), 4096u), 256, 0, st>>>(
+            ctx->scratch_a.as<uint64_t>(), n, bits_n, gstart, gpstart, perm);
         CNN_LAUNCH_CHECK(ctx);
     } else {
         CNN_TRY(iota_i32(ctx, perm, n));
     }
-    gram_prep_kernel<<<grid_for(n * 32, 256), 256, 0, st>>>(ctx->x, n, d, dp, colsum, perm,
-                                                            ctx->gram_hi.as<__nv_bfloat16>(),
-                                                            ctx->gram_lo.as<__nv_bfloat16>(), norm2, blk_norm_bits,
-                                                            blk_norm2_bits, nonfinite);
+
+    // hi, lo (bf16 n_rows x dp), norm2 (n_rows), block norms
+    CNN_TRY(ctx->ensure(ctx->gram_hi, sizeof(__nv_bfloat16) * (size_t)n_rows * dp));
+    CNN_TRY(ctx->ensure(ctx->gram_lo, sizeof(__nv_bfloat16) * (size_t)n_rows * dp));
+    CNN_TRY(ctx->ensure(ctx->gram_aux, sizeof(float) * (size_t)(n_rows + 2 * nblk + 64)));
+    float *norm2 = ctx->gram_aux.as<float>();
+    unsigned *blk_norm_bits = reinterpret_cast<unsigned *>(norm2 + n_rows);
+    unsigned *blk_norm2_bits = blk_norm_bits + nblk;
+    CNN_CUDA(ctx, cudaMemsetAsync(blk_norm_bits, 0, sizeof(unsigned) * 2 * (size_t)nblk, st));
+    gram_prep_kernel<<<grid_for(n_rows * 32, 256), 256, 0, st>>>(ctx->x, n_rows, n, d, dp, colsum, perm,
+                                                                 ctx->gram_hi.as<__nv_bfloat16>(),
+                                                                 ctx->gram_lo.as<__nv_bfloat16>(), norm2,
+                                                                 blk_norm_bits, blk_norm2_bits);
     CNN_LAUNCH_CHECK(ctx);
-    int h_nonfinite = 0;
-    CNN_CUDA(ctx, cudaMemcpyAsync(&h_nonfinite, nonfinite, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CNN_CUDA(ctx, cudaStreamSynchronize(st));
-    if (h_nonfinite) return CNN_OK;  // non-finite coordinates: the all-pairs path handles them
 
     // the list of block pairs (I, J >= I) that can hold a pair within R
     const double Rsearch = (metric == CNN_METRIC_EUCLIDEAN ? radius_cutoff : sqrt(radius_cutoff)) * (1.0 + 1e-6);
@@ -807,12 +962,13 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
         (reinterpret_cast<uintptr_t>(row_count + nblk + 1) + 15) & ~uintptr_t(15));
     const float Rf = prune ? (float)Rsearch : INFINITY;
     if (prune) {
-        block_bounds_kernel<<<(unsigned)nblk, 256, 0, st>>>(ctx->x, n, d, colsum, perm, centroid, bradius);
+        block_bounds_kernel<<<(unsigned)nblk, 256, 0, st>>>(ctx->x, n_rows, n, d, colsum, perm, centroid, bradius);
         CNN_LAUNCH_CHECK(ctx);
     } else {
         CNN_CUDA(ctx, cudaMemsetAsync(centroid, 0, sizeof(float) * (size_t)nblk * (d + 1), st));
     }
-    tile_list_kernel<false><<<(unsigned)nblk, 256, 0, st>>>(centroid, bradius, d, nblk, Rf, row_count, nullptr,
+    const unsigned lgrid = (unsigned)((nblk + kListRows - 1) / kListRows);
+    tile_list_kernel<false><<<lgrid, 256, 0, st>>>(centroid, bradius, d, nblk, Rf, row_count, nullptr,
                                                              nullptr);
     CNN_LAUNCH_CHECK(ctx);
     CNN_CUDA(ctx, cudaMemsetAsync(row_count + nblk, 0, sizeof(int32_t), st));
@@ -821,17 +977,17 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     CNN_CUDA(ctx, cudaMemcpyAsync(&ntiles, row_off + nblk, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     CNN_CUDA(ctx, cudaStreamSynchronize(st));
     CNN_TRY(ctx->ensure(ctx->gram_tiles, sizeof(int2) * (size_t)(ntiles > 0 ? ntiles : 1)));
-    tile_list_kernel<true><<<(unsigned)nblk, 256, 0, st>>>(centroid, bradius, d, nblk, Rf, nullptr, row_off,
+    tile_list_kernel<true><<<lgrid, 256, 0, st>>>(centroid, bradius, d, nblk, Rf, nullptr, row_off,
                                                             ctx->gram_tiles.as<int2>());
     CNN_LAUNCH_CHECK(ctx);
 
     CUtensorMap map_hi, map_lo;
-    if (!make_map(&map_hi, ctx->gram_hi.ptr, n, dp) || !make_map(&map_lo, ctx->gram_lo.ptr, n, dp))
+    if (!make_map(&map_hi, ctx->gram_hi.ptr, n_rows, dp) || !make_map(&map_lo, ctx->gram_lo.ptr, n_rows, dp))
         return CNN_OK;
 
     const double coef = gram_band_coef(dp);
     GramArgs a{};
-    a.n = n;
+    a.n = n_rows;
     a.nkb = nkb;
     a.nblk = (int32_t)nblk;
     a.ntiles = ntiles;
@@ -870,13 +1026,13 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
         CNN_LAUNCH_CHECK(ctx);
         stage_end(ctx, 9);
         // internal indices -> point indices (before the recheck appends more keys)
-        map_keys_kernel<<<152u * 8u, 256, 0, st>>>(a.keys, nkeys, key_cap, perm);
+        map_keys_kernel<<<152u * 8u, 256, 0, st>>>(a.keys, nkeys, key_cap, perm, bits_n);
         CNN_LAUNCH_CHECK(ctx);
-        map_keys_kernel<<<152u * 8u, 256, 0, st>>>(a.amb, namb, amb_cap, perm);
+        map_keys_kernel<<<152u * 8u, 256, 0, st>>>(a.amb, namb, amb_cap, perm, 0);
         CNN_LAUNCH_CHECK(ctx);
         gram_recheck_kernel<<<std::min<unsigned>(grid_for(amb_cap, 256), 152u * 8u), 256, 0, st>>>(
             ctx->x, d, a.amb, namb, amb_cap, radius_cutoff, metric, fpmode, a.keys, nkeys, key_cap, a.amb_d2,
-            max_err_bits);
+            max_err_bits, bits_n);
         CNN_LAUNCH_CHECK(ctx);
         unsigned long long hc[3];
         CNN_CUDA(ctx, cudaMemcpyAsync(hc, counters + 10, sizeof(hc), cudaMemcpyDeviceToHost, st));
@@ -889,22 +1045,25 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
             ctx->gram_key_hint = nk + nk / 8 + 1024;
             ctx->stats.n_exact = (int64_t)hc[1];
             unsigned me = 0;
-            CNN_CUDA(ctx, cudaMemcpy(&me, max_err_bits, sizeof(unsigned), cudaMemcpyDeviceToHost));
+            CNN_CUDA(ctx, cudaMemcpyAsync(&me, max_err_bits, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+            CNN_CUDA(ctx, cudaStreamSynchronize(st));
             float mef;
             memcpy(&mef, &me, sizeof(float));
             ctx->stats.max_abs_err = mef;
             ctx->stats.n_candidates = ntiles * kTM * kTM;
             ctx->stats.filter_band = std::max(coef, 0.0);
             ctx->stats.filter_enabled = 1;
-            // CSR: sort keys by (row, col), rows from the high half
-            CNN_TRY(radix_sort_u64(ctx, a.keys, nk, 32 + bits_n));
+            // CSR: sort the packed (row << bits_n | col) keys
+            CNN_TRY(radix_sort_u64(ctx, a.keys, nk, 2 * bits_n));
             CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nk > 0 ? nk : 1)));
-            int32_t *deg = ctx->deg.as<int32_t>();
-            CNN_CUDA(ctx, cudaMemsetAsync(deg, 0, sizeof(int32_t) * (size_t)(n + 1), st));
+            int64_t *row_off_csr = ctx->row_off.as<int64_t>();
+            if (nk == 0) CNN_CUDA(ctx, cudaMemsetAsync(row_off_csr, 0, sizeof(int64_t) * (size_t)(n + 1), st));
             keys_rows_kernel<<<std::min<unsigned>(grid_for(nk, 256), 152u * 16u), 256, 0, st>>>(
-                a.keys, nk, deg, ctx->cols.as<int32_t>());
+                a.keys, nk, bits_n, n, row_off_csr, ctx->cols.as<int32_t>());
             CNN_LAUNCH_CHECK(ctx);
-            CNN_TRY(scan_exclusive_i32_to_i64(ctx, deg, ctx->row_off.as<int64_t>(), n + 1));
+            degree_from_offsets_kernel<<<std::min<unsigned>(grid_for(n + 1, 256), 152u * 16u), 256, 0, st>>>(
+                row_off_csr, n, ctx->deg.as<int32_t>());
+            CNN_LAUNCH_CHECK(ctx);
             ctx->nnz = nk;
             *used = true;
             return CNN_OK;

@@ -535,6 +535,28 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     const bool radius_ok = radius_cutoff >= 0.0 && isfinite(radius_cutoff);
     const bool radius_inf = radius_cutoff == INFINITY;
 
+    if (d >= 16 && radius_ok) {
+        // tensor-core Gram search; declines (used = false) for non-finite
+        // data or when the float64 band would hold too many pairs
+        bool used = false;
+        stage_begin(ctx, 2);
+        CNN_TRY(gram_search_impl(ctx, radius_cutoff, metric, fpmode, &used));
+        stage_end(ctx, 2);
+        if (used) {
+            CNN_TRY(iota_i32(ctx, ctx->perm.as<int32_t>(), n));
+            CNN_TRY(iota_i32(ctx, ctx->inv.as<int32_t>(), n));
+            ctx->identity_perm = true;
+            ctx->stats.search_kind = 3;
+            ctx->stats.n_nonzero = ctx->nnz;
+            CNN_CUDA(ctx, cudaStreamSynchronize(st));
+            ctx->have_graph = true;
+            return CNN_OK;
+        }
+        CNN_CUDA(ctx, cudaMemsetAsync(ctx->counters.ptr, 0, 16 * sizeof(unsigned long long), st));
+        ctx->stats = cnn_stats{};
+        ctx->stats.n_points = n;
+    }
+
     stage_begin(ctx, 0);
     // ---- extents of finite points
     std::vector<double> lo(d), hi(d);
@@ -664,25 +686,6 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         stage_end(ctx, 2);
         ctx->identity_perm = false;
     } else {
-        if (d >= 16 && radius_ok) {
-            // tensor-core Gram search; declines (used = false) for non-finite
-            // data or when the float64 band would hold too many pairs
-            bool used = false;
-            stage_begin(ctx, 2);
-            CNN_TRY(gram_search_impl(ctx, radius_cutoff, metric, fpmode, &used));
-            stage_end(ctx, 2);
-            if (used) {
-                CNN_TRY(iota_i32(ctx, ctx->perm.as<int32_t>(), n));
-                CNN_TRY(iota_i32(ctx, ctx->inv.as<int32_t>(), n));
-                ctx->identity_perm = true;
-                ctx->stats.search_kind = 3;
-                ctx->stats.n_nonzero = ctx->nnz;
-                CNN_CUDA(ctx, cudaStreamSynchronize(st));
-                ctx->have_graph = true;
-                return CNN_OK;
-            }
-            CNN_CUDA(ctx, cudaMemsetAsync(ctx->counters.ptr, 0, 16 * sizeof(unsigned long long), st));
-        }
         stage_begin(ctx, 1);
         CNN_TRY(iota_i32(ctx, ctx->perm.as<int32_t>(), n));
         CNN_TRY(iota_i32(ctx, ctx->inv.as<int32_t>(), n));

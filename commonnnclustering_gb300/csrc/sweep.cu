@@ -155,6 +155,50 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
     for (int i = 1; i < n_radii; ++i)
         if (!(rcs[i] >= rcs[i - 1])) return ctx->fail(CNN_ERR_INVALID_ARG, "radius cutoffs must be ascending");
 
+    // Components only grow along the (radius, cut) lattice: a pair accepted
+    // at (r, sim, nmem) is accepted at any (r' >= r, 0 <= sim' <= sim,
+    // nmem' <= nmem) -- neighbourhoods, degrees and intersections only grow.
+    // So each fit starts from the finished components of up to two fits that
+    // refine it (the same cut at the previous radius, and a stricter cut at
+    // this radius); the lazy check then skips every pair already joined.
+    // The result is the same partition (the seeds only join points the fit
+    // itself would join), so labels equal those of a separate fit.
+    std::vector<int> order(n_cuts), seed_cut(n_cuts, -1);
+    for (int j = 0; j < n_cuts; ++j) order[j] = j;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return sim_cut[a] != sim_cut[b] ? sim_cut[a] > sim_cut[b] : member_cut[a] > member_cut[b];
+    });
+    for (int t = 0; t < n_cuts; ++t) {
+        const int j = order[t];
+        if (sim_cut[j] < 0) continue;  // a negative cutoff accepts no pair: nothing to seed
+        for (int u = 0; u < t; ++u) {
+            const int i = order[u];
+            if (sim_cut[i] >= sim_cut[j] && member_cut[i] >= member_cut[j] &&
+                (seed_cut[j] < 0 || sim_cut[i] < sim_cut[seed_cut[j]] ||
+                 (sim_cut[i] == sim_cut[seed_cut[j]] && member_cut[i] < member_cut[seed_cut[j]])))
+                seed_cut[j] = i;
+        }
+    }
+    CNN_TRY(ctx->ensure(ctx->sweep_forest, sizeof(int32_t) * (size_t)n * (size_t)n_cuts + 256));
+    int32_t *forest = ctx->sweep_forest.as<int32_t>();
+    std::vector<char> have(n_cuts, 0);  // slot j: the same cut at the previous radius
+    auto fit_cuts = [&](int32_t k, bool same_order_as_previous) -> cnn_status {
+        if (!same_order_as_previous) std::fill(have.begin(), have.end(), 0);
+        for (int t = 0; t < n_cuts; ++t) {
+            const int j = order[t];
+            const int32_t *sa = have[j] && sim_cut[j] >= 0 ? forest + (size_t)j * n : nullptr;
+            const int32_t *sb = seed_cut[j] >= 0 ? forest + (size_t)seed_cut[j] * n : nullptr;
+            CNN_TRY(fit_and_sort_into(ctx, sim_cut[j], member_cut[j], sort_member_cutoff, max_clusters,
+                                      labels_dev + ((int64_t)k * n_cuts + j) * n, sa, sb));
+            // after the fit the union-find array holds every node's root (-1 elsewhere)
+            if (n > 0)
+                CNN_CUDA(ctx, cudaMemcpyAsync(forest + (size_t)j * n, ctx->parent.ptr, sizeof(int32_t) * (size_t)n,
+                                              cudaMemcpyDeviceToDevice, st));
+            have[j] = 1;
+        }
+        return CNN_OK;
+    };
+
     // one search, at the largest radius (the same search cnn_build_neighbours runs)
     CNN_TRY(build_neighbours_impl(ctx, rcs.back(), metric, fpmode));
     const int64_t nnz = ctx->nnz;
@@ -168,12 +212,13 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
     if (!ladder) {
         // no cell-grid graph to filter (all-pairs or tensor-core search):
         // search every radius on its own, smallest first
+        bool prev_identity = false;
         for (int32_t k = 0; k < n_radii; ++k) {
             if (k < n_radii - 1) CNN_TRY(build_neighbours_impl(ctx, rcs[k], metric, fpmode));
             else if (n_radii > 1) CNN_TRY(build_neighbours_impl(ctx, rcs.back(), metric, fpmode));
-            for (int32_t j = 0; j < n_cuts; ++j)
-                CNN_TRY(fit_and_sort_into(ctx, sim_cut[j], member_cut[j], sort_member_cutoff, max_clusters,
-                                          labels_dev + ((int64_t)k * n_cuts + j) * n));
+            // seeds across radii need the same internal order (identity here)
+            CNN_TRY(fit_cuts(k, prev_identity && ctx->identity_perm));
+            prev_identity = ctx->identity_perm;
         }
         return CNN_OK;
     }
@@ -216,9 +261,7 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
             std::swap(ctx->deg, ctx->sweep_deg_max);
         }
         ctx->nnz = nnz_k;
-        for (int32_t j = 0; j < n_cuts; ++j)
-            CNN_TRY(fit_and_sort_into(ctx, sim_cut[j], member_cut[j], sort_member_cutoff, max_clusters,
-                                      labels_dev + ((int64_t)k * n_cuts + j) * n));
+        CNN_TRY(fit_cuts(k, true));  // every radius keeps the largest-radius internal order
     }
     return CNN_OK;
 }

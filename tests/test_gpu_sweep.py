@@ -61,3 +61,34 @@ def test_sweep_rejects_descending_radii(cnn):
     with pytest.raises(cnn.CNNError):
         ctx.sweep([0.04, 0.01], [(3, 2)])
     ctx.close()
+
+
+def fit_pair(cnn, ctx, x, rc, sim, nmem, member_cutoff):
+    labels = np.zeros(x.shape[0], dtype=np.int64)
+    consider = np.ones(x.shape[0], dtype=np.uint8)
+    ctx.set_points(x)
+    ctx.build_neighbours(rc)
+    ctx.fit(sim, nmem, 1, consider, labels)
+    ctx.sort_by_size(labels, member_cutoff, None)
+    return labels
+
+
+@pytest.mark.parametrize("d", [3, 5])
+def test_sweep_unordered_cut_pairs(cnn, d):
+    # (similarity_cutoff, n_member_cutoff) pairs in no particular order,
+    # including 0 (every pair passes) and -1 (no pair passes): fits may only
+    # start from fits that refine them
+    rng = np.random.default_rng(11 + d)
+    centres = rng.uniform(-3, 3, size=(12, d))
+    x = np.vstack([c + rng.normal(0, 0.25, size=(1500, d)) for c in centres])
+    rcs = [0.04, 0.09, 0.16] if d == 3 else [0.3, 0.5]
+    cuts = [(5, 2), (3, 8), (0, 4), (-1, 3), (7, 7), (5, 9), (12, 1), (3, 8)]
+    ctx = cnn.Context(0)
+    ctx.set_points(x)
+    got = ctx.sweep(rcs, cuts, member_cutoff=3)
+    alone = cnn.Context(0)
+    for k, rc in enumerate(rcs):
+        for j, (sim, nmem) in enumerate(cuts):
+            assert np.array_equal(got[k, j], fit_pair(cnn, alone, x, rc, sim, nmem, 3)), (rc, sim, nmem)
+    ctx.close()
+    alone.close()
