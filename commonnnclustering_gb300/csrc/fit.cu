@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(256) cross_filter_kernel(int64_t n, const int6
         const int32_t pa = parent[a];
         if (pa < 0) continue;
         const int64_t s = row_off[a], e = row_off[a + 1];
-        for (int64_t k0 = s; k0 < e; k0 += 32) {
+        for (int64_t k0 = warp_upper_bound(cols, s, e, a, lane); k0 < e; k0 += 32) {
             const int64_t k = k0 + lane;
             int32_t b = -1, pb = -1;
             if (k < e) {
@@ -342,7 +342,7 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     const unsigned check_blocks = std::min<unsigned>(grid_for(n, kCheckWarps), 152u * 8u);
     check_union_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(
         n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff, kHookEdges,
-        counters);
+        counters, seed_a, seed_b);
     CNN_LAUNCH_CHECK(ctx);
     root_store_kernel<<<blocks_for(n), 256, 0, st>>>(n, node, parent);
     CNN_LAUNCH_CHECK(ctx);

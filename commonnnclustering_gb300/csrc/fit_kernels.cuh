@@ -85,16 +85,38 @@ __global__ void node_kernel(const int32_t *__restrict__ deg, const int32_t *__re
     if ((threadIdx.x & 31) == 0 && local) atomicAdd(&counters[4], local);
 }
 
+// Index of the first entry > v in the ascending run cols[s, e), found by the
+// whole warp with 32-way probing (every lane returns the same value).
+// Invariant: entries before lo are <= v, entries from hi on are > v.
+__device__ __forceinline__ int64_t warp_upper_bound(const int32_t *__restrict__ cols, int64_t s, int64_t e, int32_t v,
+                                                    int lane) {
+    int64_t lo = s, hi = e;
+    while (hi - lo > 32) {
+        const int64_t step = (hi - lo + 31) / 32;
+        const int64_t p = lo + (int64_t)lane * step;
+        const int c = __popc(__ballot_sync(0xffffffffu, p < hi && cols[p] <= v));  // a prefix of the probes
+        if (c == 0) return lo;
+        const int64_t nlo = lo + (int64_t)(c - 1) * step + 1;
+        hi = min(hi, lo + (int64_t)c * step);
+        lo = nlo;
+    }
+    const int64_t p = lo + lane;
+    return lo + __popc(__ballot_sync(0xffffffffu, p < hi && cols[p] <= v));
+}
+
 // Persistent warps stride over nodes.  For node a, candidate edges (a, b)
 // with b > a and b a node (parent[b] >= 0) are taken 32 at a time; their
 // roots are resolved in parallel (one lane each) and re-resolved only after
 // this warp joined something: a stale "different" only costs an extra
 // check, never a wrong skip.  max_edges bounds the candidate edges one node
-// examines (the hook pass uses 2).
+// examines (the hook pass uses 2).  Rows are ascending, so the walk starts
+// at the first entry > a.  Nodes with skip_a[a] >= 0 or skip_b[a] >= 0
+// (already joined by seeds) are left to the cross-edge pass.
 __device__ __forceinline__ void check_union_body(
     int64_t n, const int64_t *__restrict__ row_off, const int32_t *__restrict__ cols,
     int32_t *__restrict__ parent, int32_t needed, int32_t max_edges,
-    unsigned long long *__restrict__ counters) {
+    unsigned long long *__restrict__ counters, const int32_t *__restrict__ skip_a = nullptr,
+    const int32_t *__restrict__ skip_b = nullptr) {
     const int lane = threadIdx.x & 31;
     const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -102,13 +124,14 @@ __device__ __forceinline__ void check_union_body(
     for (int64_t a64 = warp0; a64 < n; a64 += nwarps) {
         const int32_t a = (int32_t)a64;
         if (*(volatile int32_t *)&parent[a] < 0) continue;  // not a node
+        if ((skip_a && skip_a[a] >= 0) || (skip_b && skip_b[a] >= 0)) continue;
         const int64_t s = row_off[a], e = row_off[a + 1];
         const int32_t la = (int32_t)(e - s);
         const int32_t *A = cols + s;
         int32_t ra = -1;
         bool dirty = true;
         int32_t seen = 0;
-        for (int64_t k0 = s; k0 < e && seen < max_edges; k0 += 32) {
+        for (int64_t k0 = warp_upper_bound(cols, s, e, a, lane); k0 < e && seen < max_edges; k0 += 32) {
             const int64_t k = k0 + lane;
             int32_t b = -1, pb = -1;
             if (k < e) {
@@ -169,8 +192,9 @@ __device__ __forceinline__ void check_union_body(
 __global__ void __launch_bounds__(kCheckWarps * 32) check_union_kernel(
     int64_t n, const int64_t *__restrict__ row_off, const int32_t *__restrict__ cols,
     int32_t *__restrict__ parent, int32_t needed, int32_t max_edges,
-    unsigned long long *__restrict__ counters) {
-    check_union_body(n, row_off, cols, parent, needed, max_edges, counters);
+    unsigned long long *__restrict__ counters, const int32_t *__restrict__ skip_a,
+    const int32_t *__restrict__ skip_b) {
+    check_union_body(n, row_off, cols, parent, needed, max_edges, counters, skip_a, skip_b);
 }
 
 // Full path compression and per-component minimum point index.

@@ -141,10 +141,11 @@ extern "C" CNN_API cnn_status cnn_fit_csr_noalloc(const int64_t *offsets, const 
                                             sc->comp_min, counters);
     const unsigned check_blocks = std::min<unsigned>(grid_for(n, kCheckWarps), 152u * 8u);
     check_union_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(n, offsets, indices, sc->parent,
-                                                                   (int32_t)similarity_cutoff, 2, counters);
+                                                                   (int32_t)similarity_cutoff, 2, counters, nullptr, nullptr);
     root_store_kernel<<<nblocks(n), 256, 0, st>>>(n, sc->node, sc->parent);
     check_union_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(n, offsets, indices, sc->parent,
-                                                                   (int32_t)similarity_cutoff, INT32_MAX, counters);
+                                                                   (int32_t)similarity_cutoff, INT32_MAX, counters, nullptr,
+                                                                   nullptr);
     root_min_kernel<<<nblocks(n), 256, 0, st>>>(n, sc->node, sc->parent, sc->perm, sc->comp_min);
     root_store_kernel<<<nblocks(n), 256, 0, st>>>(n, sc->node, sc->parent);
     min_flag_kernel<<<nblocks(n), 256, 0, st>>>(n, sc->node, sc->parent, sc->comp_min, sc->flag);
