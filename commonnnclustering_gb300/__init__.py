@@ -11,7 +11,9 @@ the compute in hand-written sm_103a CUDA kernels behind the C ABI of
     clustering.labels
 """
 from ._abi import CNNError, Context, default_context
-from ._fit import Fitter, FitterGPU, FitterGPUNeighbourhoods
+from ._bundle import ReferenceIndices, bfs_leafs, isolate
+from ._fit import Fitter, FitterGPU, FitterGPUNeighbourhoods, HierarchicalFitter, HierarchicalFitterRepeatGPU
+from ._predict import Predictor, PredictorFirstmatchGPU
 from ._types import (ClusterParameters, DistanceGetterGPUMetric, InputData, InputDataGPUComponents,
                      InputDataGPUNeighbourhoods, Labels, MetricGPUEuclidean, MetricGPUEuclideanReduced,
                      NeighboursGetterGPUGrid, NeighboursGetterGPULookup, NeighboursGPU, QueueGPUUnionFind,
@@ -27,5 +29,7 @@ __all__ = [
     "ClusterParameters", "DistanceGetterGPUMetric", "InputData", "InputDataGPUComponents",
     "InputDataGPUNeighbourhoods", "Labels", "MetricGPUEuclidean", "MetricGPUEuclideanReduced",
     "NeighboursGetterGPUGrid", "NeighboursGetterGPULookup", "NeighboursGPU", "QueueGPUUnionFind",
-    "SimilarityCheckerGPU", "Bundle", "Clustering", "Record", "Summary", "sweep",
+    "SimilarityCheckerGPU", "Bundle", "Clustering", "Record", "Summary", "sweep", "HierarchicalFitter",
+    "HierarchicalFitterRepeatGPU", "Predictor", "PredictorFirstmatchGPU", "ReferenceIndices", "bfs_leafs",
+    "isolate",
 ]

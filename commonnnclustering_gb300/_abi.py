@@ -78,6 +78,9 @@ SIGNATURES = {
     "cnn_check_lists": (_INT, [_P, _P, _I64, _P, _I64, _I64, _P, _INT]),
     "cnn_fit_csr_noalloc": (_INT, [_P, _P, _I64, _I64, _I64, _I64, _P, _P, _P]),
     "cnn_sweep": (_INT, [_P, _P, _I32, _P, _P, _I32, _INT, _INT, _I64, _I64, _P, _INT]),
+    "cnn_sweep_pairs": (_INT, [_P, _P, _P, _P, _I32, _INT, _INT, _I32, _I64, _I64, _P, _INT]),
+    "cnn_predict": (_INT, [_P, _P, _INT, _I64, _I32, _P, _P, _I64, ctypes.c_double, _INT, _INT, _I64, _I64, _P, _P,
+                           _INT]),
 }
 
 _lib = None
@@ -319,6 +322,73 @@ class Context:
                                         sc.shape[0], int(metric), int(fpmode), int(member_cutoff), mx,
                                         ctypes.c_void_p(ptr), mem), "cnn_sweep")
         return out
+
+    def sweep_pairs(self, radius_cutoffs, cuts, member_cutoff: int = 2, max_clusters: Optional[int] = None,
+                    sort: bool = True, metric: int = METRIC_EUCLIDEAN_REDUCED, fpmode: int = FP_SEPARATE,
+                    labels_out=None):
+        """Fits for a list of steps on the current points.
+
+        radius_cutoffs: adjusted cutoff per step (any order, repeats allowed).
+        cuts: (similarity_cutoff, n_member_cutoff) per step.  Returns labels
+        of shape [n_steps, n_points] (host numpy array unless a CUDA tensor is
+        given as labels_out); row i equals the separate fit of step i.
+        """
+        rc = np.ascontiguousarray(radius_cutoffs, dtype=np.float64).reshape(-1)
+        if len(cuts) != rc.shape[0]:
+            raise ValueError("need one (similarity_cutoff, n_member_cutoff) per radius cutoff")
+        sc = np.ascontiguousarray([c[0] for c in cuts], dtype=np.int64)
+        nm = np.ascontiguousarray([c[1] for c in cuts], dtype=np.int64)
+        mx = -1 if max_clusters is None else int(max_clusters)
+        n = int(self._n_points)
+        if labels_out is not None and is_device_array(labels_out):
+            ptr, mem, out = device_pointer(labels_out, np.int64, writable=True), MEM_DEVICE, labels_out
+        else:
+            out = np.empty((rc.shape[0], n), dtype=np.int64)
+            ptr, mem = out.ctypes.data, MEM_HOST
+        self._check(self._lib.cnn_sweep_pairs(self._h, ctypes.c_void_p(rc.ctypes.data),
+                                              ctypes.c_void_p(sc.ctypes.data), ctypes.c_void_p(nm.ctypes.data),
+                                              rc.shape[0], int(metric), int(fpmode), 1 if sort else 0,
+                                              int(member_cutoff), mx, ctypes.c_void_p(ptr), mem), "cnn_sweep_pairs")
+        return out
+
+    def predict(self, other_points, labels, clusters, radius_cutoff: float, similarity_cutoff: int,
+                n_member_cutoff: int, other_labels, other_consider, metric: int = METRIC_EUCLIDEAN_REDUCED,
+                fpmode: int = FP_SEPARATE):
+        """First-match labels for other points from the current points' labels.
+
+        other_points: [m, n_dim] float64/float32; labels: [n_points] int64 of
+        the current points; clusters: labels that may be handed out.
+        other_labels (int64 [m]) and other_consider (uint8 [m]) are updated in
+        place.  All arrays on the host, or all CUDA tensors.
+        """
+        dev = is_device_array(other_points)
+        if dev:
+            dt = np.float32 if "float32" in str(other_points.dtype) else np.float64
+            shape = tuple(other_points.shape)
+            xp = device_pointer(other_points, dt)
+            lab_p = device_pointer(labels, np.int64)
+            out_l = device_pointer(other_labels, np.int64, writable=True)
+            out_c = device_pointer(other_consider, np.uint8, writable=True)
+            t = _torch()
+            cl = t.as_tensor(sorted({int(c) for c in clusters}), dtype=t.int64, device=other_points.device)
+            cl_p, n_cl, mem, keep = device_pointer(cl, np.int64), int(cl.shape[0]), MEM_DEVICE, cl
+        else:
+            xo = np.asarray(other_points)
+            dt = np.float32 if xo.dtype == np.float32 else np.float64
+            xo = host_array(xo.reshape(xo.shape[0], -1) if xo.ndim == 1 else xo, dt)
+            shape = xo.shape
+            lab = host_array(labels, np.int64)
+            ol = host_array(other_labels, np.int64, writable=True)
+            oc = host_array(other_consider, np.uint8, writable=True)
+            cl = np.ascontiguousarray(sorted({int(c) for c in clusters}), dtype=np.int64)
+            xp, lab_p, out_l, out_c = xo.ctypes.data, lab.ctypes.data, ol.ctypes.data, oc.ctypes.data
+            cl_p, n_cl, mem, keep = cl.ctypes.data, int(cl.shape[0]), MEM_HOST, (xo, lab, cl)
+        self._check(self._lib.cnn_predict(self._h, ctypes.c_void_p(xp), DTYPE_F32 if dt == np.float32 else DTYPE_F64,
+                                          int(shape[0]), int(shape[1]), ctypes.c_void_p(lab_p), ctypes.c_void_p(cl_p),
+                                          n_cl, float(radius_cutoff), int(metric), int(fpmode),
+                                          int(similarity_cutoff), int(n_member_cutoff), ctypes.c_void_p(out_l),
+                                          ctypes.c_void_p(out_c), mem), "cnn_predict")
+        del keep
 
     def check_lists(self, a, b, c: int) -> bool:
         a = host_array(a, np.int32)

@@ -176,4 +176,137 @@ class FitterGPUNeighbourhoods(FitterGPU):
         super().__init__(neighbours_getter, *args, **kwargs)
 
 
-__all__ = ["Fitter", "FitterGPU", "FitterGPUNeighbourhoods", "np"]
+class HierarchicalFitter(ABC):
+    """Hierarchical fitter interface (src/cnnclustering/_fit.pyx:88-126).
+
+    ``make_parameters`` reads ``self._neighbours_getter`` like the
+    reference's; a hierarchical fitter without that attribute (the repeat
+    fitter) passes (radius_cutoff, cnn_cutoff) through unchanged.
+    """
+
+    @abstractmethod
+    def fit(self, bundle, **kwargs):
+        """Generic hierarchical clustering"""
+
+    make_parameters = Fitter.make_parameters
+
+
+class HierarchicalFitterRepeatGPU(HierarchicalFitter):
+    """Drop-in for ``HierarchicalFitterRepeat`` (src/cnnclustering/_fit.pyx:1014-1187).
+
+    Every step (radius_cutoff[i], cnn_cutoff[i]) is a complete fit of all
+    points of the bundle from fresh labels; the labels of step i become
+    the labels of the step-(i-1) clusters' children, which are isolated
+    into child bundles.  With a ``FitterGPU`` on coordinates all steps run
+    as one batched device call (one largest-radius search per 16 radii,
+    fits seeded along the (radius, cut) lattice, ``cnn_sweep_pairs``);
+    any other fitter is called step by step.  The hierarchy bookkeeping
+    (:1146-1184) is host work.
+
+    As in the reference, the parameters come from this object's
+    ``make_parameters``: it has no neighbours getter, so the radius is not
+    adjusted by the metric and no self-counting offsets are added.
+    """
+
+    def __init__(self, fitter=None):
+        self._fitter = fitter if fitter is not None else FitterGPU()
+
+    def __str__(self):
+        return f"{type(self).__name__}(fitter={self._fitter})"
+
+    @classmethod
+    def get_builder_kwargs(cls):
+        return [("fitter", None)]
+
+    def fit(self, bundle, **kwargs):
+        self._fit(bundle, kwargs["radius_cutoff"], kwargs["cnn_cutoff"], kwargs.get("member_cutoff"),
+                  kwargs.get("max_clusters"), kwargs.get("cnn_offset"), kwargs.get("sort_by_size", True),
+                  kwargs.get("info", True), kwargs.get("v", True))
+
+    def step_labels(self, bundle, params, member_cutoff, max_clusters, sort_by_size):
+        """Labels of every step, shape [n_steps, n_points] (host)."""
+        from ._types import Labels
+        input_data = bundle._input_data
+        fitter = self._fitter
+        if isinstance(fitter, FitterGPU) and not _is_neighbourhood_input(input_data):
+            data = input_data.data
+            ctx = fitter.context_for(data)
+            fitter._sync_stream(ctx, data)
+            ctx.set_points(data)
+            fitter._graph_key = None
+            out = ctx.sweep_pairs([p.radius_cutoff for p in params],
+                                  [(p.similarity_cutoff, p.n_member_cutoff) for p in params],
+                                  member_cutoff=2 if member_cutoff is None else int(member_cutoff),
+                                  max_clusters=max_clusters, sort=sort_by_size, metric=fitter._metric_code(),
+                                  fpmode=fitter._fpmode_code())
+            return np.asarray(out)
+        n = input_data.n_points
+        rows = []
+        for p in params:
+            labels = Labels(np.zeros(n, order="C", dtype=np.int64))
+            fitter.fit(input_data, labels, p)
+            if sort_by_size:
+                labels.sort_by_size(member_cutoff, max_clusters)
+            rows.append(np.array(labels._host(), dtype=np.int64))
+        return np.stack(rows) if rows else np.zeros((0, n), dtype=np.int64)
+
+    def _fit(self, bundle, radius_cutoff, cnn_cutoff, member_cutoff=None, max_clusters=None, cnn_offset=None,
+             sort_by_size=True, info=True, v=True):
+        import weakref
+        from collections.abc import Iterable
+        from ._types import Labels
+
+        if not isinstance(radius_cutoff, Iterable):
+            radius_cutoff = [radius_cutoff]
+        radius_cutoff = [float(x) for x in radius_cutoff]
+        if not isinstance(cnn_cutoff, Iterable):
+            cnn_cutoff = [cnn_cutoff]
+        cnn_cutoff = [int(x) for x in cnn_cutoff]
+        if len(radius_cutoff) == 1:
+            radius_cutoff *= len(cnn_cutoff)
+        if len(cnn_cutoff) == 1:
+            cnn_cutoff *= len(radius_cutoff)
+        n_steps = len(radius_cutoff)
+        assert n_steps == len(cnn_cutoff)
+        if cnn_offset is None:
+            cnn_offset = 0
+        params = [self.make_parameters(radius_cutoff[i], cnn_cutoff[i] - cnn_offset, 1) for i in range(n_steps)]
+        if v:
+            for i in range(n_steps):
+                print(f"Running step {i:<5} (r = {radius_cutoff[i]}, c = {cnn_cutoff[i]})")
+        all_labels = self.step_labels(bundle, params, member_cutoff, max_clusters, sort_by_size)
+
+        n_points = bundle._input_data.n_points
+        previous = np.ones(n_points, dtype=np.int64)
+        terminal = {1: bundle}
+        for step in range(n_steps):
+            current = all_labels[step]
+            new_terminal = {}
+            # points of every parent cluster, in point order; parents in
+            # ascending label order
+            order = np.argsort(previous, kind="stable")
+            sorted_prev = previous[order]
+            values, starts = np.unique(sorted_prev, return_index=True)
+            ends = np.append(starts[1:], sorted_prev.shape[0])
+            for p_label, a, b in zip(values.tolist(), starts.tolist(), ends.tolist()):
+                if p_label == 0:
+                    continue
+                parent_clustering = terminal[p_label]
+                parent_clustering._labels = Labels.from_sequence(current[order[a:b]])
+                if info:
+                    label_params = {k: (radius_cutoff[step], cnn_cutoff[step])
+                                    for k in parent_clustering._labels.to_set() if k != 0}
+                    parent_clustering._labels.meta.update({"params": label_params,
+                                                           "reference": weakref.proxy(parent_clustering),
+                                                           "origin": "fit"})
+                parent_clustering.isolate(isolate_input_data=False)
+                for c_label, child in parent_clustering._children.items():
+                    if c_label == 0:
+                        continue
+                    new_terminal[c_label] = child
+            terminal = new_terminal
+            previous = current
+
+
+__all__ = ["Fitter", "FitterGPU", "FitterGPUNeighbourhoods", "HierarchicalFitter", "HierarchicalFitterRepeatGPU",
+           "np"]

@@ -228,6 +228,14 @@ class InputDataGPUComponents(InputData):
     def get_component(self, point: int, dimension: int) -> float:
         return float(self._data[point, dimension])
 
+    def get_subset(self, indices) -> "InputDataGPUComponents":
+        """The rows `indices` (src/cnnclustering/_types.pyx:1064-1086, coordinates)."""
+        idx = np.asarray(indices, dtype=np.int64)
+        if _abi.is_device_array(self._data):
+            import torch
+            return type(self)(self._data[torch.as_tensor(idx, device=self._data.device)].contiguous())
+        return type(self)(np.ascontiguousarray(self._data[idx]))
+
     def __str__(self):
         return f"{type(self).__name__}"
 
@@ -262,6 +270,16 @@ class InputDataGPUNeighbourhoods(InputData):
 
     def get_neighbour(self, point: int, member: int) -> int:
         return int(self._indices[self._offsets[point] + member])
+
+    def get_subset(self, indices) -> "InputDataGPUNeighbourhoods":
+        """Rows `indices`, each keeping only members in `indices`, member
+        values unchanged (src/cnnclustering/_types.pyx:1199-1217)."""
+        idx = np.asarray(indices, dtype=np.int64)
+        off, ind = (np.asarray(a) for a in (self._offsets, self._indices))
+        keep = np.zeros(max(self.n_points, int(ind.max()) + 1 if ind.size else 0), dtype=bool)
+        keep[idx] = True
+        rows = [ind[off[i]:off[i + 1]] for i in idx]
+        return type(self).from_sequence([r[keep[r]] for r in rows], meta=dict(self._meta))
 
 
 # ---------------------------------------------------------------------------

@@ -18,28 +18,10 @@ from typing import Optional
 import numpy as np
 
 from . import recipes
-from ._fit import Fitter
+from ._bundle import Bundle, bfs_leafs
+from ._fit import Fitter, HierarchicalFitter
 from ._types import InputData, Labels, P_AINDEX
 from .report import Record, Summary
-
-
-class Bundle:
-    """Input data, labels and fit records of one clustering
-    (the subset of src/cnnclustering/_bundle.pyx:20-272 the fit uses)."""
-
-    def __init__(self, input_data=None, labels=None, summary=None):
-        self._input_data = input_data
-        self._labels = labels
-        self._summary = Summary() if summary is None else summary
-        self._children = None
-
-    @property
-    def labels(self):
-        return None if self._labels is None else self._labels.labels
-
-    @labels.setter
-    def labels(self, value):
-        self._labels = value if isinstance(value, Labels) else Labels.from_sequence(value)
 
 
 def timed(function):
@@ -52,7 +34,8 @@ def timed(function):
 
 
 class Clustering:
-    def __init__(self, data=None, *, fitter=None, bundle_kwargs=None, recipe=None, **recipe_kwargs):
+    def __init__(self, data=None, *, fitter=None, hierarchical_fitter=None, predictor=None, bundle_kwargs=None,
+                 recipe=None, **recipe_kwargs):
         builder = recipes.Builder(recipe, **recipe_kwargs)
         bundle_kwargs = {} if bundle_kwargs is None else bundle_kwargs
         if data is None:
@@ -63,13 +46,28 @@ class Clustering:
             self._bundle = Bundle(data, **bundle_kwargs)
         else:
             self._bundle = Bundle(builder.make_input_data(data), **bundle_kwargs)
-        if isinstance(fitter, Fitter):
-            self._fitter = fitter
-        else:
-            if fitter is not None:
-                builder.recipe["fitter"] = fitter
-            made = builder.make_component("fitter")
-            self._fitter = None if made is object else made
+        from ._predict import Predictor
+        for kw, component_kw, kw_type in ((fitter, "fitter", Fitter),
+                                          (hierarchical_fitter, "hierarchical_fitter", HierarchicalFitter),
+                                          (predictor, "predictor", Predictor)):
+            if isinstance(kw, kw_type):
+                setattr(self, f"_{component_kw}", kw)
+                continue
+            if kw is not None:
+                builder.recipe[component_kw] = kw
+            made = builder.make_component(component_kw)
+            setattr(self, f"_{component_kw}", None if made is object else made)
+
+    @property
+    def root(self):
+        return self._bundle
+
+    @property
+    def children(self):
+        return self._bundle._children
+
+    def __getitem__(self, value):
+        return self._bundle.get_child(value)
 
     @property
     def labels(self):
@@ -103,9 +101,18 @@ class Clustering:
     def summary(self):
         return self._bundle._summary
 
+    @property
+    def hierarchical_fitter(self):
+        return self._hierarchical_fitter
+
+    @property
+    def predictor(self):
+        return self._predictor
+
     def __str__(self):
         inp = None if self._bundle is None else self._bundle._input_data
-        return f"{type(self).__name__}(input_data={inp}, fitter={self._fitter})"
+        return (f"{type(self).__name__}(input_data={inp}, fitter={self._fitter}, "
+                f"hfitter={self._hierarchical_fitter}, predictor={self._predictor})")
 
     def _fit(self, cluster_params, bundle=None):
         bundle = self._bundle if bundle is None else bundle
@@ -160,3 +167,91 @@ class Clustering:
             if v:
                 print(rec)
             bundle._summary.append(rec)
+
+    # -- hierarchy (src/cnnclustering/cluster.pyx:394-552) ------------------------------
+    def fit_hierarchical(self, purge=True, bundle=None, **fitter_kwargs):
+        """Run the hierarchical fitter (e.g. ``HierarchicalFitterRepeatGPU``) on a bundle."""
+        bundle = self._bundle if bundle is None else bundle
+        if purge or bundle._children is None:
+            bundle._children = {}
+        self._hierarchical_fitter.fit(bundle, **fitter_kwargs)
+
+    def isolate(self, purge: bool = True, isolate_input_data: bool = True, bundle=None):
+        """One child bundle per cluster label."""
+        bundle = self._bundle if bundle is None else bundle
+        bundle.isolate(purge, isolate_input_data)
+
+    def trim_shrinking_leafs(self, bundle=None):
+        bundle = self._bundle if bundle is None else bundle
+
+        def _trim_shrinking(b, new=True):
+            if not b._children:
+                splits = will_split = False
+            else:
+                label_set = b._labels.set
+                label_set.discard(0)
+                splits = len(label_set) > 1
+                will_split = any([_trim_shrinking(child, new=splits) for child in b._children.values()])
+            keep = new or will_split or splits
+            if not keep:
+                b._labels = None
+                b._children = {}
+            return keep
+
+        _trim_shrinking(bundle)
+
+    def trim_trivial_leafs(self, bundle=None):
+        """Reset labels and children of every all-noise clustering."""
+        bundle = self._bundle if bundle is None else bundle
+
+        def _trim_trivial(b):
+            if b._labels is None:
+                return
+            if b._labels.set == {0}:
+                b._labels = None
+                b._children = {}
+                return
+            for child in b._children.values():
+                _trim_trivial(child)
+
+        _trim_trivial(bundle)
+
+    def reel(self, depth: Optional[int] = None, bundle=None) -> None:
+        """Fold the labels of lower levels into their parents' labels."""
+        bundle = self._bundle if bundle is None else bundle
+        if depth is not None:
+            assert depth > 0
+
+        def _reel(parent, depth):
+            if not parent._children:
+                return
+            if depth is not None:
+                depth -= 1
+            parent._labels.meta["origin"] = "reel"
+            parent_labels = parent._labels.labels
+            for label, child in parent._children.items():
+                if child._labels is None:
+                    continue
+                if depth is None or depth > 0:
+                    _reel(child, depth)
+                n_clusters = int(max(parent_labels))
+                child_labels = np.asarray(child._labels.labels)
+                new = np.where(child_labels == 0, 0, child_labels + n_clusters)
+                parent_labels[np.asarray(child.parent_indices)] = new
+                parent._labels.meta.get("params", {}).pop(label, None)
+                for old_label, p in child._labels.meta.get("params", {}).items():
+                    parent._labels.meta.setdefault("params", {})[old_label + n_clusters] = p
+
+        _reel(bundle, depth)
+
+    def predict(self, other, radius_cutoff: float, cnn_cutoff: int, clusters=None, cnn_offset=None,
+                info: bool = True, record: bool = True, record_time: bool = True, v: bool = True,
+                purge: bool = False, bundle=None):
+        """Labels for the points of ``other`` from this clustering (see ``PredictorFirstmatchGPU``)."""
+        from ._predict import predict_into
+        bundle = self._bundle if bundle is None else bundle
+        return predict_into(self, bundle, other, radius_cutoff, cnn_cutoff, clusters, cnn_offset, info, record,
+                            record_time, v, purge)
+
+
+__all__ = ["Bundle", "Clustering", "bfs_leafs", "timed"]

@@ -4,7 +4,11 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
+#include <cmath>
 #include <new>
+#include <utility>
+#include <vector>
 
 #include "common.cuh"
 
@@ -103,7 +107,8 @@ CNN_API cnn_status cnn_destroy(cnn_context *ctx) {
                            &ctx->cols, &ctx->xf4, &ctx->cell_of, &ctx->cell_start, &ctx->node, &ctx->parent,
                            &ctx->comp_min, &ctx->flag, &ctx->counters, &ctx->stage_labels, &ctx->gram_hi,
                            &ctx->gram_lo, &ctx->gram_aux, &ctx->gram_keys, &ctx->gram_amb,
-                           &ctx->gram_blocks, &ctx->gram_tiles, &ctx->gram_perm,
+                           &ctx->gram_blocks, &ctx->gram_tiles, &ctx->gram_perm, &ctx->pred_off, &ctx->pred_cols,
+                           &ctx->pred_xoff, &ctx->pred_xcols, &ctx->pred_x, &ctx->pred_set,
                            &ctx->sweep_bucket, &ctx->sweep_row_off_max, &ctx->sweep_cols_max,
                            &ctx->sweep_deg_max, &ctx->sweep_consider, &ctx->sweep_forest,
                            &ctx->stage_consider, &ctx->stage_offsets, &ctx->stage_indices, &ctx->stage_misc,
@@ -338,6 +343,155 @@ CNN_API cnn_status cnn_sweep(cnn_context *ctx, const double *radius_cutoffs, int
         CNN_CUDA(ctx, cudaMemcpyAsync(labels_out, lab_dev, sizeof(int64_t) * (size_t)total, cudaMemcpyDeviceToHost,
                                       ctx->stream));
     CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return CNN_OK;
+}
+
+CNN_API cnn_status cnn_sweep_pairs(cnn_context *ctx, const double *radius_cutoffs,
+                                   const int64_t *similarity_cutoffs, const int64_t *n_member_cutoffs,
+                                   int32_t n_steps, cnn_metric metric, cnn_fpmode fpmode, int32_t sort,
+                                   int64_t member_cutoff, int64_t max_clusters, int64_t *labels_out,
+                                   cnn_memspace mem) {
+    CNN_TRY(check_ctx(ctx));
+    if (ctx->d < 1) return ctx->fail(CNN_ERR_STATE, "no points: call cnn_set_points first");
+    if (n_steps < 1 || !radius_cutoffs || !similarity_cutoffs || !n_member_cutoffs || !labels_out)
+        return ctx->fail(CNN_ERR_INVALID_ARG, "need >= 1 step and all arrays");
+    if (metric != CNN_METRIC_EUCLIDEAN_REDUCED && metric != CNN_METRIC_EUCLIDEAN)
+        return ctx->fail(CNN_ERR_INVALID_ARG, "unknown metric");
+    if (fpmode != CNN_FP_SEPARATE && fpmode != CNN_FP_FUSED) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown fpmode");
+    for (int32_t i = 0; i < n_steps; ++i)
+        if (std::isnan(radius_cutoffs[i])) return ctx->fail(CNN_ERR_INVALID_ARG, "NaN radius cutoff");
+    const int64_t n = ctx->n;
+    const int64_t total = (int64_t)n_steps * n;
+    int64_t *lab_dev = labels_out;
+    if (mem == CNN_MEM_HOST) {
+        CNN_TRY(ctx->ensure(ctx->stage_labels, sizeof(int64_t) * (size_t)(total > 0 ? total : 1)));
+        lab_dev = ctx->stage_labels.as<int64_t>();
+    }
+    // distinct radii (ascending) and distinct cuts; the first step of every
+    // distinct (radius, cut) pair is fitted, repeats are copied
+    std::vector<double> radii(radius_cutoffs, radius_cutoffs + n_steps);
+    std::sort(radii.begin(), radii.end());
+    radii.erase(std::unique(radii.begin(), radii.end()), radii.end());
+    std::vector<std::pair<int64_t, int64_t>> cuts;
+    for (int32_t i = 0; i < n_steps; ++i) cuts.emplace_back(similarity_cutoffs[i], n_member_cutoffs[i]);
+    std::sort(cuts.begin(), cuts.end());
+    cuts.erase(std::unique(cuts.begin(), cuts.end()), cuts.end());
+    const int32_t nr = (int32_t)radii.size(), nc = (int32_t)cuts.size();
+    std::vector<int32_t> first(static_cast<size_t>(nr) * nc, -1);
+    std::vector<int32_t> step_pair(n_steps);
+    for (int32_t i = 0; i < n_steps; ++i) {
+        const int32_t k = (int32_t)(std::lower_bound(radii.begin(), radii.end(), radius_cutoffs[i]) - radii.begin());
+        const int32_t j = (int32_t)(std::lower_bound(cuts.begin(), cuts.end(),
+                                                     std::make_pair(similarity_cutoffs[i], n_member_cutoffs[i])) -
+                                    cuts.begin());
+        step_pair[i] = k * nc + j;
+        if (first[step_pair[i]] < 0) first[step_pair[i]] = i;
+    }
+    std::vector<int64_t> sim(nc), mem_cut(nc);
+    for (int32_t j = 0; j < nc; ++j) {
+        sim[j] = cuts[j].first;
+        mem_cut[j] = cuts[j].second;
+    }
+    // at most 16 radii share one largest-radius search
+    for (int32_t k0 = 0; k0 < nr; k0 += 16) {
+        const int32_t kn = std::min<int32_t>(16, nr - k0);
+        CNN_TRY(sweep_impl(ctx, radii.data() + k0, kn, sim.data(), mem_cut.data(), nc, metric, fpmode, member_cutoff,
+                           max_clusters, lab_dev, first.data() + (size_t)k0 * nc, sort != 0));
+    }
+    for (int32_t i = 0; i < n_steps; ++i)
+        if (first[step_pair[i]] != i && n > 0)
+            CNN_CUDA(ctx, cudaMemcpyAsync(lab_dev + (int64_t)i * n, lab_dev + (int64_t)first[step_pair[i]] * n,
+                                          sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (mem == CNN_MEM_HOST && total > 0)
+        CNN_CUDA(ctx, cudaMemcpyAsync(labels_out, lab_dev, sizeof(int64_t) * (size_t)total, cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+    CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return CNN_OK;
+}
+
+CNN_API cnn_status cnn_predict(cnn_context *ctx, const void *other_points, cnn_dtype dtype, int64_t n_other,
+                               int32_t n_dim, const int64_t *labels, const int64_t *clusters, int64_t n_clusters,
+                               double radius_cutoff, cnn_metric metric, cnn_fpmode fpmode, int64_t similarity_cutoff,
+                               int64_t n_member_cutoff, int64_t *other_labels, uint8_t *other_consider,
+                               cnn_memspace mem) {
+    CNN_TRY(check_ctx(ctx));
+    if (ctx->d < 1 || !ctx->x) return ctx->fail(CNN_ERR_STATE, "no points: call cnn_set_points first");
+    if (n_dim != ctx->d) return ctx->fail(CNN_ERR_INVALID_ARG, "other points must have the same n_dim");
+    if (n_other < 0 || n_other > INT32_MAX - 2 || n_clusters < 0) return ctx->fail(CNN_ERR_INVALID_ARG, "bad sizes");
+    if (n_other > 0 && (!other_points || !other_labels || !other_consider))
+        return ctx->fail(CNN_ERR_INVALID_ARG, "other points, labels and consider are required");
+    if (ctx->n > 0 && !labels) return ctx->fail(CNN_ERR_INVALID_ARG, "labels of the clustered points are required");
+    if (n_clusters > 0 && !clusters) return ctx->fail(CNN_ERR_INVALID_ARG, "clusters missing");
+    if (dtype != CNN_DTYPE_F64 && dtype != CNN_DTYPE_F32) return ctx->fail(CNN_ERR_INVALID_ARG, "bad dtype");
+    if (metric != CNN_METRIC_EUCLIDEAN_REDUCED && metric != CNN_METRIC_EUCLIDEAN)
+        return ctx->fail(CNN_ERR_INVALID_ARG, "unknown metric");
+    if (fpmode != CNN_FP_SEPARATE && fpmode != CNN_FP_FUSED) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown fpmode");
+    if (mem != CNN_MEM_HOST && mem != CNN_MEM_DEVICE) return ctx->fail(CNN_ERR_INVALID_ARG, "bad memspace");
+    cudaStream_t st = ctx->stream;
+    const int64_t n = ctx->n, m = n_other, total = m * n_dim;
+    // other points as float64 on the device
+    const double *xq = nullptr;
+    if (dtype == CNN_DTYPE_F64 && mem == CNN_MEM_DEVICE) {
+        xq = static_cast<const double *>(other_points);
+    } else {
+        CNN_TRY(ctx->ensure(ctx->pred_x, sizeof(double) * (size_t)(total > 0 ? total : 1)));
+        if (dtype == CNN_DTYPE_F64) {
+            if (total > 0)
+                CNN_CUDA(ctx, cudaMemcpyAsync(ctx->pred_x.ptr, other_points, sizeof(double) * (size_t)total,
+                                              cudaMemcpyHostToDevice, st));
+        } else {
+            const float *src = static_cast<const float *>(other_points);
+            if (mem == CNN_MEM_HOST) {
+                CNN_TRY(ctx->ensure(ctx->stage_indices, sizeof(float) * (size_t)(total > 0 ? total : 1)));
+                if (total > 0)
+                    CNN_CUDA(ctx, cudaMemcpyAsync(ctx->stage_indices.ptr, other_points, sizeof(float) * (size_t)total,
+                                                  cudaMemcpyHostToDevice, st));
+                src = ctx->stage_indices.as<float>();
+            }
+            if (total > 0) {
+                widen_f32_kernel<<<grid_for(total, 256) > 4096 ? 4096 : grid_for(total, 256), 256, 0, st>>>(
+                    src, total, ctx->pred_x.as<double>());
+                CNN_LAUNCH_CHECK(ctx);
+            }
+        }
+        xq = ctx->pred_x.as<double>();
+    }
+    // clustered labels, the consider set (sorted, distinct), the other labels and flags
+    const int64_t *lab_dev = labels;
+    if (mem == CNN_MEM_HOST) CNN_TRY(stage_in<int64_t>(ctx, ctx->stage_labels, labels, n, mem, &lab_dev));
+    std::vector<int64_t> set(static_cast<size_t>(n_clusters));
+    if (n_clusters > 0) {
+        if (mem == CNN_MEM_HOST) {
+            memcpy(set.data(), clusters, sizeof(int64_t) * (size_t)n_clusters);
+        } else {
+            CNN_CUDA(ctx, cudaMemcpyAsync(set.data(), clusters, sizeof(int64_t) * (size_t)n_clusters,
+                                          cudaMemcpyDeviceToHost, st));
+            CNN_CUDA(ctx, cudaStreamSynchronize(st));
+        }
+    }
+    std::sort(set.begin(), set.end());
+    set.erase(std::unique(set.begin(), set.end()), set.end());
+    CNN_TRY(ctx->ensure(ctx->pred_set, sizeof(int64_t) * (set.size() + 1)));
+    if (!set.empty())
+        CNN_CUDA(ctx, cudaMemcpyAsync(ctx->pred_set.ptr, set.data(), sizeof(int64_t) * set.size(),
+                                      cudaMemcpyHostToDevice, st));
+    int64_t *olab = other_labels;
+    uint8_t *ocons = other_consider;
+    if (mem == CNN_MEM_HOST) {
+        const int64_t *l_in = nullptr;
+        const uint8_t *c_in = nullptr;
+        CNN_TRY(stage_in<int64_t>(ctx, ctx->stage_offsets, other_labels, m, mem, &l_in));
+        CNN_TRY(stage_in<uint8_t>(ctx, ctx->stage_consider, other_consider, m, mem, &c_in));
+        olab = const_cast<int64_t *>(l_in);
+        ocons = const_cast<uint8_t *>(c_in);
+    }
+    CNN_TRY(predict_impl(ctx, xq, m, lab_dev, ctx->pred_set.as<int64_t>(), (int64_t)set.size(), radius_cutoff,
+                         metric, fpmode, similarity_cutoff, n_member_cutoff, olab, ocons));
+    if (mem == CNN_MEM_HOST && m > 0) {
+        CNN_CUDA(ctx, cudaMemcpyAsync(other_labels, olab, sizeof(int64_t) * (size_t)m, cudaMemcpyDeviceToHost, st));
+        CNN_CUDA(ctx, cudaMemcpyAsync(other_consider, ocons, (size_t)m, cudaMemcpyDeviceToHost, st));
+    }
+    CNN_CUDA(ctx, cudaStreamSynchronize(st));
     return CNN_OK;
 }
 

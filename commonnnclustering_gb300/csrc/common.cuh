@@ -99,6 +99,9 @@ struct cnn_context {
 
     // tensor-core (Gram) search for n_dim >= 16
     cnn::DevBuf gram_hi, gram_lo, gram_aux, gram_keys, gram_amb, gram_blocks, gram_tiles, gram_perm;
+
+    // prediction: this set's graph in point order, the other points' rows
+    cnn::DevBuf pred_off, pred_cols, pred_xoff, pred_xcols, pred_x, pred_set;
     int64_t gram_key_hint = 0;
 
     // fit work arrays
@@ -168,6 +171,16 @@ cnn_status export_neighbours_impl(cnn_context *ctx, int64_t *offsets_dev, int32_
 cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev,
                                const int32_t *indices_dev, int64_t n);
 
+// rows of m other points (device float64 [m][d]) against the current points
+cnn_status cross_neighbours_impl(cnn_context *ctx, const double *xq, int64_t m, double radius_cutoff, int metric,
+                                 int fpmode, cnn::DevBuf &off_buf, cnn::DevBuf &cols_buf, int64_t *nnz_out);
+
+// predict.cu: first-match labels for other points
+cnn_status predict_impl(cnn_context *ctx, const double *xq, int64_t m, const int64_t *labels_dev,
+                        const int64_t *clusters_sorted_dev, int64_t n_clusters, double radius_cutoff, int metric,
+                        int fpmode, int64_t similarity_cutoff, int64_t n_member_cutoff, int64_t *other_labels_dev,
+                        uint8_t *other_consider_dev);
+
 // gram.cu: tensor-core search (n_dim >= 16); *used = false when it declined
 cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode, bool *used);
 
@@ -184,13 +197,14 @@ cnn_status check_lists_impl(cnn_context *ctx, const int32_t *a, int64_t na, cons
 // a fresh fit (labels 0, consider 1, current_start 1) and sort_by_size into labels_dev
 cnn_status fit_and_sort_into(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
                              int64_t sort_member_cutoff, int64_t max_clusters, int64_t *labels_dev,
-                             const int32_t *seed_a = nullptr, const int32_t *seed_b = nullptr);
+                             const int32_t *seed_a = nullptr, const int32_t *seed_b = nullptr, bool sort = true);
 
 // sweep.cu
 cnn_status sweep_impl(cnn_context *ctx, const double *radius_cutoffs, int32_t n_radii,
                       const int64_t *similarity_cutoffs, const int64_t *n_member_cutoffs, int32_t n_cuts,
                       int metric, int fpmode, int64_t sort_member_cutoff, int64_t max_clusters,
-                      int64_t *labels_dev);
+                      int64_t *labels_dev, const int32_t *out_slot = nullptr, bool sort = true);
+// out_slot (host, [n_radii][n_cuts]): output index of each pair in labels_dev, -1 = not wanted
 
 // timing helpers (cnngpu.cu): events only, no synchronisation
 void stage_begin(cnn_context *ctx, int slot);

@@ -485,7 +485,7 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64
 // current_start 1, the fit, then sort_by_size.
 cnn_status fit_and_sort_into(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
                              int64_t sort_member_cutoff, int64_t max_clusters, int64_t *labels_dev,
-                             const int32_t *seed_a, const int32_t *seed_b) {
+                             const int32_t *seed_a, const int32_t *seed_b, bool sort) {
     const int64_t n = ctx->n;
     cudaStream_t st = ctx->stream;
     if (n == 0) return CNN_OK;
@@ -494,7 +494,7 @@ cnn_status fit_and_sort_into(cnn_context *ctx, int64_t similarity_cutoff, int64_
     CNN_CUDA(ctx, cudaMemsetAsync(ctx->sweep_consider.ptr, 1, (size_t)n, st));
     CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, 1, ctx->sweep_consider.as<uint8_t>(), labels_dev,
                      seed_a, seed_b));
-    return sort_by_size_impl(ctx, labels_dev, n, sort_member_cutoff, max_clusters);
+    return sort ? sort_by_size_impl(ctx, labels_dev, n, sort_member_cutoff, max_clusters) : CNN_OK;
 }
 
 cnn_status check_lists_impl(cnn_context *ctx, const int32_t *a, int64_t na, const int32_t *b, int64_t nb,

@@ -388,6 +388,53 @@ __global__ void __launch_bounds__(kTileWarps * 32) tile_search_kernel(
     }
 }
 
+// Rows of other points (queries) against this set (candidates): the same
+// float32 test with the float64 band, candidates in ascending index order.
+// (NeighboursGetterExtBruteForce._get_other, src/cnnclustering/_types.pyx:1712-1731.)
+template <bool kFill>
+__global__ void __launch_bounds__(kTileWarps * 32) cross_tile_kernel(
+    const double *__restrict__ xq, const float *__restrict__ xqf, int64_t m, const double *__restrict__ x,
+    const float *__restrict__ xf, int64_t n, int d, SearchParams sp, int32_t *__restrict__ deg,
+    const int64_t *__restrict__ row_off, int32_t *__restrict__ cols) {
+    extern __shared__ float smem[];
+    const int ds = d + 1;
+    float *cand = smem;
+    float *qry = smem + kTileCand * ds;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t p = (int64_t)blockIdx.x * kTileWarps + wid;
+    const bool active = p < m;
+    for (int k = lane; k < d; k += 32) qry[wid * ds + k] = active ? xqf[p * d + k] : 0.f;
+    const unsigned lt = (1u << lane) - 1u;
+    int64_t w = (kFill && active) ? row_off[p] : 0;
+    int64_t cnt = 0;
+    for (int64_t j0 = 0; j0 < n; j0 += kTileCand) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < kTileCand * d; e += blockDim.x) {
+            const int r = e / d, k = e - r * d;
+            const int64_t j = j0 + r;
+            cand[r * ds + k] = j < n ? xf[j * d + k] : 0.f;
+        }
+        __syncthreads();
+        const int64_t j = j0 + lane;
+        bool in = false;
+        if (active && j < n) {
+            float sf = 0.f;
+            const float *cr = cand + lane * ds;
+            const float *qr = qry + wid * ds;
+            for (int k = 0; k < d; ++k) {
+                const float t = qr[k] - cr[k];
+                sf = fmaf(t, t, sf);
+            }
+            if (sf <= sp.thr_in) in = true;
+            else if (!(sf > sp.thr_out)) in = exact_in_radius(xq + p * d, x + j * d, d, sp);
+        }
+        const unsigned hit = __ballot_sync(0xffffffffu, in);
+        if (kFill && in) cols[w + cnt + __popc(hit & lt)] = (int32_t)j;
+        cnt += __popc(hit);
+    }
+    if (!kFill && active && lane == 0) deg[p] = (int32_t)cnt;
+}
+
 __global__ void to_f32_kernel(const double *__restrict__ x, int64_t n, int d, const double *__restrict__ lo,
                               float *__restrict__ xf) {
     const int64_t total = n * d;
@@ -775,6 +822,101 @@ cnn_status export_neighbours_impl(cnn_context *ctx, int64_t *offsets_dev, int32_
     keys_to_cols_kernel<<<std::min<unsigned>(grid_for(nnz, 256), 152u * 32u), 256, 0, st>>>(keys, nnz, bits_n,
                                                                                              indices_dev);
     CNN_LAUNCH_CHECK(ctx);
+    return CNN_OK;
+}
+
+// Neighbour rows of m other points (float64, device) against the current
+// points: offsets (m+1, int64) and ascending point indices.  Float32
+// coordinates relative to the lowest finite coordinate of both sets; the
+// float64 band decides the rest.
+cnn_status cross_neighbours_impl(cnn_context *ctx, const double *xq, int64_t m, double radius_cutoff, int metric,
+                                 int fpmode, cnn::DevBuf &off_buf, cnn::DevBuf &cols_buf, int64_t *nnz_out) {
+    const int64_t n = ctx->n;
+    const int d = ctx->d;
+    cudaStream_t st = ctx->stream;
+    CNN_TRY(ctx->ensure(off_buf, sizeof(int64_t) * (size_t)(m + 1)));
+    int64_t *off = off_buf.as<int64_t>();
+    *nnz_out = 0;
+    if (m == 0) {
+        CNN_CUDA(ctx, cudaMemsetAsync(off, 0, sizeof(int64_t), st));
+        return CNN_OK;
+    }
+    SearchParams sp;
+    sp.rc = radius_cutoff;
+    sp.metric = metric;
+    sp.fpmode = fpmode;
+    sp.thr_in = -1.f;
+    sp.thr_out = INFINITY;
+    const bool radius_ok = radius_cutoff >= 0.0 && isfinite(radius_cutoff);
+    std::vector<double> lo(d, INFINITY), hi(d, -INFINITY);
+    for (int set = 0; set < 2; ++set) {
+        const double *src = set == 0 ? ctx->x : xq;
+        const int64_t cnt = set == 0 ? n : m;
+        if (cnt == 0) continue;
+        const int blocks = (int)std::min<int64_t>(256, (cnt + 255) / 256);
+        CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(double) * (size_t)blocks * (size_t)d * 3 + 64));
+        extent_partial_kernel<<<dim3(blocks, d), 256, 0, st>>>(src, cnt, d, ctx->scratch_a.as<double>());
+        CNN_LAUNCH_CHECK(ctx);
+        std::vector<double> part((size_t)blocks * d * 3);
+        CNN_CUDA(ctx, cudaMemcpyAsync(part.data(), ctx->scratch_a.ptr, sizeof(double) * part.size(),
+                                      cudaMemcpyDeviceToHost, st));
+        CNN_CUDA(ctx, cudaStreamSynchronize(st));
+        for (int b = 0; b < blocks; ++b)
+            for (int k = 0; k < d; ++k) {
+                lo[k] = std::min(lo[k], part[((size_t)b * d + k) * 3]);
+                hi[k] = std::max(hi[k], part[((size_t)b * d + k) * 3 + 1]);
+            }
+    }
+    std::vector<double> ext(d);
+    for (int k = 0; k < d; ++k) {
+        if (!(lo[k] <= hi[k])) lo[k] = hi[k] = 0.0;
+        ext[k] = hi[k] - lo[k];
+    }
+    if (radius_ok) {
+        const double R = metric == CNN_METRIC_EUCLIDEAN ? radius_cutoff : sqrt(radius_cutoff);
+        const double rc2 = metric == CNN_METRIC_EUCLIDEAN ? radius_cutoff * radius_cutoff : radius_cutoff;
+        double band = 0;
+        if (!filter_thresholds(ext, R, rc2, &sp.thr_in, &sp.thr_out, &band)) {
+            sp.thr_in = -1.f;
+            sp.thr_out = INFINITY;  // every pair in float64
+        }
+    } else if (radius_cutoff != INFINITY) {
+        sp.thr_in = -1.f;
+        sp.thr_out = -1.f;  // a NaN or negative cutoff admits nothing
+    }
+    if (d > 1024) return ctx->fail(CNN_ERR_UNSUPPORTED, "n_dim > 1024 is not supported");
+    CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(double) * (size_t)d + 64));
+    CNN_TRY(ctx->ensure(ctx->scratch_b, sizeof(float) * (size_t)(n + m) * d + 64));
+    CNN_CUDA(ctx, cudaMemcpyAsync(ctx->scratch_a.ptr, lo.data(), sizeof(double) * d, cudaMemcpyHostToDevice, st));
+    float *xf = ctx->scratch_b.as<float>();
+    float *xqf = xf + (size_t)n * d;
+    if (n > 0) {
+        to_f32_kernel<<<std::min<unsigned>(grid_for(n * d, 256), 152u * 16u), 256, 0, st>>>(
+            ctx->x, n, d, ctx->scratch_a.as<double>(), xf);
+        CNN_LAUNCH_CHECK(ctx);
+    }
+    to_f32_kernel<<<std::min<unsigned>(grid_for(m * d, 256), 152u * 16u), 256, 0, st>>>(
+        xq, m, d, ctx->scratch_a.as<double>(), xqf);
+    CNN_LAUNCH_CHECK(ctx);
+    const size_t smem = sizeof(float) * (size_t)(kTileCand + kTileWarps) * (d + 1);
+    CNN_CUDA(ctx, cudaFuncSetAttribute(cross_tile_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CNN_CUDA(ctx, cudaFuncSetAttribute(cross_tile_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CNN_TRY(ctx->ensure(ctx->io_a, sizeof(int32_t) * (size_t)(m + 1)));
+    int32_t *deg = ctx->io_a.as<int32_t>();
+    const unsigned gq = grid_for(m, kTileWarps);
+    cross_tile_kernel<false><<<gq, kTileWarps * 32, smem, st>>>(xq, xqf, m, ctx->x, xf, n, d, sp, deg, nullptr,
+                                                                 nullptr);
+    CNN_LAUNCH_CHECK(ctx);
+    CNN_CUDA(ctx, cudaMemsetAsync(deg + m, 0, sizeof(int32_t), st));
+    CNN_TRY(scan_exclusive_i32_to_i64(ctx, deg, off, m + 1));
+    int64_t nnz = 0;
+    CNN_CUDA(ctx, cudaMemcpyAsync(&nnz, off + m, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    CNN_CUDA(ctx, cudaStreamSynchronize(st));
+    CNN_TRY(ctx->ensure(cols_buf, sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1)));
+    cross_tile_kernel<true><<<gq, kTileWarps * 32, smem, st>>>(xq, xqf, m, ctx->x, xf, n, d, sp, nullptr, off,
+                                                                cols_buf.as<int32_t>());
+    CNN_LAUNCH_CHECK(ctx);
+    *nnz_out = nnz;
     return CNN_OK;
 }
 

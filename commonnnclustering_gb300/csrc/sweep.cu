@@ -147,54 +147,59 @@ bool ladder_thresholds(const std::vector<double> &ext, const std::vector<double>
 
 cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, const int64_t *sim_cut,
                       const int64_t *member_cut, int32_t n_cuts, int metric, int fpmode, int64_t sort_member_cutoff,
-                      int64_t max_clusters, int64_t *labels_dev) {
+                      int64_t max_clusters, int64_t *labels_dev, const int32_t *out_slot, bool sort) {
     const int64_t n = ctx->n;
     const int d = ctx->d;
     cudaStream_t st = ctx->stream;
     std::vector<double> rcs(rcs_in, rcs_in + n_radii);
     for (int i = 1; i < n_radii; ++i)
         if (!(rcs[i] >= rcs[i - 1])) return ctx->fail(CNN_ERR_INVALID_ARG, "radius cutoffs must be ascending");
+    // output slot of (radius k, cut j); -1: not wanted
+    auto slot = [&](int32_t k, int j) -> int64_t {
+        return out_slot ? (int64_t)out_slot[(int64_t)k * n_cuts + j] : (int64_t)k * n_cuts + j;
+    };
 
     // Components only grow along the (radius, cut) lattice: a pair accepted
     // at (r, sim, nmem) is accepted at any (r' >= r, 0 <= sim' <= sim,
     // nmem' <= nmem) -- neighbourhoods, degrees and intersections only grow.
     // So each fit starts from the finished components of up to two fits that
-    // refine it (the same cut at the previous radius, and a stricter cut at
-    // this radius); the lazy check then skips every pair already joined.
-    // The result is the same partition (the seeds only join points the fit
-    // itself would join), so labels equal those of a separate fit.
-    std::vector<int> order(n_cuts), seed_cut(n_cuts, -1);
+    // refine it (the same cut at the last radius it ran at, and the closest
+    // stricter cut at this radius); the lazy check then skips every pair
+    // already joined.  The result is the same partition (the seeds only join
+    // points the fit itself would join), so labels equal a separate fit's.
+    std::vector<int> order(n_cuts);
     for (int j = 0; j < n_cuts; ++j) order[j] = j;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
         return sim_cut[a] != sim_cut[b] ? sim_cut[a] > sim_cut[b] : member_cut[a] > member_cut[b];
     });
-    for (int t = 0; t < n_cuts; ++t) {
-        const int j = order[t];
-        if (sim_cut[j] < 0) continue;  // a negative cutoff accepts no pair: nothing to seed
-        for (int u = 0; u < t; ++u) {
-            const int i = order[u];
-            if (sim_cut[i] >= sim_cut[j] && member_cut[i] >= member_cut[j] &&
-                (seed_cut[j] < 0 || sim_cut[i] < sim_cut[seed_cut[j]] ||
-                 (sim_cut[i] == sim_cut[seed_cut[j]] && member_cut[i] < member_cut[seed_cut[j]])))
-                seed_cut[j] = i;
-        }
-    }
+    auto refines = [&](int i, int j) {  // fit i's components refine fit j's (same radius or smaller)
+        return sim_cut[j] >= 0 && sim_cut[i] >= sim_cut[j] && member_cut[i] >= member_cut[j];
+    };
     CNN_TRY(ctx->ensure(ctx->sweep_forest, sizeof(int32_t) * (size_t)n * (size_t)n_cuts + 256));
     int32_t *forest = ctx->sweep_forest.as<int32_t>();
-    std::vector<char> have(n_cuts, 0);  // slot j: the same cut at the previous radius
+    std::vector<char> have(n_cuts, 0);  // slot j: cut j at the last radius it ran at
     auto fit_cuts = [&](int32_t k, bool same_order_as_previous) -> cnn_status {
         if (!same_order_as_previous) std::fill(have.begin(), have.end(), 0);
+        std::vector<int> done_here;
         for (int t = 0; t < n_cuts; ++t) {
             const int j = order[t];
+            const int64_t out = slot(k, j);
+            if (out < 0) continue;
+            int best = -1;
+            for (int i : done_here)
+                if (refines(i, j) && (best < 0 || sim_cut[i] < sim_cut[best] ||
+                                      (sim_cut[i] == sim_cut[best] && member_cut[i] < member_cut[best])))
+                    best = i;
             const int32_t *sa = have[j] && sim_cut[j] >= 0 ? forest + (size_t)j * n : nullptr;
-            const int32_t *sb = seed_cut[j] >= 0 ? forest + (size_t)seed_cut[j] * n : nullptr;
+            const int32_t *sb = best >= 0 ? forest + (size_t)best * n : nullptr;
             CNN_TRY(fit_and_sort_into(ctx, sim_cut[j], member_cut[j], sort_member_cutoff, max_clusters,
-                                      labels_dev + ((int64_t)k * n_cuts + j) * n, sa, sb));
+                                      labels_dev + out * n, sa, sb, sort));
             // after the fit the union-find array holds every node's root (-1 elsewhere)
             if (n > 0)
                 CNN_CUDA(ctx, cudaMemcpyAsync(forest + (size_t)j * n, ctx->parent.ptr, sizeof(int32_t) * (size_t)n,
                                               cudaMemcpyDeviceToDevice, st));
             have[j] = 1;
+            done_here.push_back(j);
         }
         return CNN_OK;
     };

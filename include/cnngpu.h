@@ -194,6 +194,40 @@ CNN_API cnn_status cnn_sweep(cnn_context *ctx, const double *radius_cutoffs, int
                              int64_t member_cutoff, int64_t max_clusters, int64_t *labels_out,
                              cnn_memspace mem);
 
+/* The step list of HierarchicalFitterRepeat._fit
+ * (src/cnnclustering/_fit.pyx:1131-1141): step i fits (radius_cutoffs[i],
+ * similarity_cutoffs[i], n_member_cutoffs[i]) from fresh labels
+ * (current_start 1) and, when sort != 0, sorts with (member_cutoff,
+ * max_clusters < 0: no limit), as :1143-1144 do.  Steps may come in any
+ * order and repeat; labels_out[i * n_points + p] equals the separate fit of
+ * step i.  Distinct radii share largest-radius searches (16 radii per
+ * search); fits are seeded along the (radius, cut) lattice as in cnn_sweep. */
+CNN_API cnn_status cnn_sweep_pairs(cnn_context *ctx, const double *radius_cutoffs,
+                                   const int64_t *similarity_cutoffs, const int64_t *n_member_cutoffs,
+                                   int32_t n_steps, cnn_metric metric, cnn_fpmode fpmode, int32_t sort,
+                                   int64_t member_cutoff, int64_t max_clusters, int64_t *labels_out,
+                                   cnn_memspace mem);
+
+/* Labels for other points from the clustering of the current points:
+ * PredictorFirstmatch.predict (src/cnnclustering/_fit.pyx:1235-1291) with
+ * NeighboursGetter.get_other (_types.pyx:1712-1731).  labels: the current
+ * points' labels [n_points]; clusters: the consider set (labels that may be
+ * handed out; any order).  radius_cutoff and the cutoffs as
+ * Predictor.make_parameters gives them.  For every other point p with
+ * other_consider[p] == 1 and more than n_member_cutoff neighbours among the
+ * current points, the first neighbour (in index order) whose label is in
+ * the set, whose own neighbourhood has more than n_member_cutoff members and
+ * that shares at least similarity_cutoff neighbours with p (0: always, < 0:
+ * never) gives p its label, and other_consider[p] becomes 0; other points
+ * keep their label.  other_points, labels, clusters, other_labels and
+ * other_consider all live in `mem`.  The current points' graph at this
+ * radius stays in the context afterwards. */
+CNN_API cnn_status cnn_predict(cnn_context *ctx, const void *other_points, cnn_dtype dtype, int64_t n_other,
+                               int32_t n_dim, const int64_t *labels, const int64_t *clusters, int64_t n_clusters,
+                               double radius_cutoff, cnn_metric metric, cnn_fpmode fpmode,
+                               int64_t similarity_cutoff, int64_t n_member_cutoff, int64_t *other_labels,
+                               uint8_t *other_consider, cnn_memspace mem);
+
 /* ---------------------------------------------------------------------
  * Fit without device memory allocation.  This entry point has no
  * counterpart in the reference.

@@ -15,6 +15,10 @@ and restates the pure-Python parts of the reference with numpy:
                             label initialisation / frozen labels,
                             parameters, fit, sort_by_size
                             (src/cnnclustering/cluster.pyx:256-392)
+* ``repeat_step_labels`` -- the step loop of HierarchicalFitterRepeat._fit
+                            (src/cnnclustering/_fit.pyx:1060-1144)
+* ``predict_firstmatch`` -- PredictorFirstmatch.predict
+                            (src/cnnclustering/_fit.pyx:1235-1291)
 """
 from __future__ import annotations
 
@@ -253,3 +257,74 @@ def clustering_fit(x, radius_cutoff: float, cnn_cutoff: int, member_cutoff=None,
     if sort:
         sort_by_size(labels, member_cutoff, max_clusters)
     return labels, info
+
+
+def other_row(x, q, radius_cutoff: float, metric=METRIC_EUCLIDEAN_REDUCED, fpmode=FP_SEPARATE) -> np.ndarray:
+    """Ascending indices of the points of x within the cutoff of the point q
+    (NeighboursGetterExtBruteForce._get_other, src/cnnclustering/_types.pyx:1712-1731)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    n, d = x.shape
+    q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1)
+    out = np.empty(n, dtype=np.int32)
+    c = lib().oracle_neighbour_row(_ptr(x), n, d, _ptr(q), float(radius_cutoff), metric, fpmode, _ptr(out))
+    return out[:c].copy()
+
+
+def predict_firstmatch(x, labels, y, radius_cutoff: float, similarity_cutoff: int, n_member_cutoff: int,
+                       clusters, other_labels=None, other_consider=None, metric=METRIC_EUCLIDEAN_REDUCED,
+                       fpmode=FP_SEPARATE):
+    """PredictorFirstmatch.predict (src/cnnclustering/_fit.pyx:1235-1291) with
+    brute-force getters; parameters as Predictor.make_parameters gives them.
+    Returns (other_labels, other_consider)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    m = y.shape[0]
+    out = np.zeros(m, dtype=np.int64) if other_labels is None else np.array(other_labels, dtype=np.int64)
+    cons = np.ones(m, dtype=np.uint8) if other_consider is None else np.array(other_consider, dtype=np.uint8)
+    clusters = set(int(c) for c in clusters)
+    offsets, indices = neighbourhoods(x, radius_cutoff, metric, fpmode, grid=False)
+    for p in range(m):
+        if cons[p] == 0:
+            continue
+        row = other_row(x, y[p], radius_cutoff, metric, fpmode)
+        if not row.shape[0] > n_member_cutoff:
+            continue
+        for i in row:
+            label = int(labels[i])
+            if label not in clusters:
+                continue
+            nb = indices[offsets[i]:offsets[i + 1]]
+            if not nb.shape[0] > n_member_cutoff:
+                continue
+            if check_sorted(row, nb, similarity_cutoff):
+                cons[p] = 0
+                out[p] = label
+                break
+    return out, cons
+
+
+def repeat_step_labels(x, radius_cutoffs, cnn_cutoffs, member_cutoff=None, max_clusters=None, cnn_offset=None,
+                       sort: bool = True, metric=METRIC_EUCLIDEAN_REDUCED, fpmode=FP_SEPARATE):
+    """Labels of every step of HierarchicalFitterRepeat._fit
+    (src/cnnclustering/_fit.pyx:1060-1144).  Its make_parameters finds no
+    neighbours getter on the hierarchical fitter, so each step compares with
+    radius_cutoff itself and uses similarity = n_member = cnn_cutoff."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    radius_cutoffs = [float(r) for r in np.atleast_1d(radius_cutoffs)]
+    cnn_cutoffs = [int(c) for c in np.atleast_1d(cnn_cutoffs)]
+    if len(radius_cutoffs) == 1:
+        radius_cutoffs *= len(cnn_cutoffs)
+    if len(cnn_cutoffs) == 1:
+        cnn_cutoffs *= len(radius_cutoffs)
+    offset = 0 if cnn_offset is None else cnn_offset
+    rows = []
+    for r, c in zip(radius_cutoffs, cnn_cutoffs):
+        c -= offset
+        labels = np.zeros(x.shape[0], dtype=np.int64)
+        consider = np.ones(x.shape[0], dtype=np.uint8)
+        off, ind = neighbourhoods(x, r, metric, fpmode)
+        fit_bfs_csr(off, ind, c, c, 1, consider, labels)
+        if sort:
+            sort_by_size(labels, member_cutoff, max_clusters)
+        rows.append(labels)
+    return np.stack(rows)

@@ -45,3 +45,42 @@ def fit_kwargs(g):
 @pytest.fixture(scope="session")
 def golden():
     return load_golden
+
+
+def golden_tree(g):
+    """Bundles of a stored hierarchy: {path tuple: (labels, root_indices, parent_indices)}."""
+    out = {}
+    for k, path in enumerate(g["paths"].tolist()):
+        key = tuple(int(p) for p in path.split(".")) if path else ()
+        lab = g["labels"][g["labels_off"][k]:g["labels_off"][k + 1]]
+        root = g["root"][g["root_off"][k]:g["root_off"][k + 1]]
+        parent = g["parent"][g["parent_off"][k]:g["parent_off"][k + 1]]
+        out[key] = (lab, root, parent)
+    return out
+
+
+def bundle_tree(bundle):
+    """The same mapping for a Bundle of this package (labels empty when None)."""
+    out = {}
+    stack = [((), bundle)]
+    while stack:
+        path, b = stack.pop()
+        lab = np.zeros(0, dtype=np.int64) if b._labels is None else np.asarray(b._labels._host(), dtype=np.int64)
+        root = np.zeros(0, dtype=np.int64) if b.root_indices is None else np.asarray(b.root_indices, dtype=np.int64)
+        parent = (np.zeros(0, dtype=np.int64) if b.parent_indices is None
+                  else np.asarray(b.parent_indices, dtype=np.int64))
+        out[path] = (lab, root, parent)
+        for label, child in b.children.items():
+            stack.append((path + (int(label),), child))
+    return out
+
+
+def predict_cases(g):
+    """(points, labels, other, radius_cutoff, cnn_cutoff, clusters or None, expected) per stored case."""
+    cases = []
+    for k in range(int(g["n_cases"])):
+        r, c = g[f"params_{k}"]
+        cl = g[f"clusters_{k}"]
+        cases.append((g["points"], g[f"labels_{k}"], g["other"], float(r), int(c),
+                      cl.tolist() if cl.size else None, g[f"predicted_{k}"]))
+    return cases

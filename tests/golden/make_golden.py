@@ -230,6 +230,105 @@ def main():
         r = float(np.quantile(np.sort(dist, axis=1)[:, 25], 0.5))
         fit_case(f"highdim_{d}.npz", xh, r, 5, fit_kwargs={"member_cutoff": 5})
 
+    # 12. HierarchicalFitterRepeat: a step list of fits, the bundle tree it
+    # builds (labels and reference indices per bundle) and reel()
+    hierarchy_case(rng)
+
+    # 13. PredictorFirstmatch on coordinates (brute-force getters)
+    predict_case(rng)
+
+
+def hierarchy_tree(root):
+    """Bundles of the tree, breadth first: path, labels, root/parent indices."""
+    from collections import deque
+    paths, labels, root_idx, parent_idx = [], [], [], []
+    q = deque([((), root)])
+    while q:
+        path, b = q.popleft()
+        paths.append(".".join(str(p) for p in path))
+        lab = b.labels
+        labels.append(np.asarray(lab, dtype=np.int64) if lab is not None else np.zeros(0, dtype=np.int64))
+        ri = b.root_indices
+        pi = b.parent_indices
+        root_idx.append(np.asarray(ri, dtype=np.int64) if ri is not None else np.zeros(0, dtype=np.int64))
+        parent_idx.append(np.asarray(pi, dtype=np.int64) if pi is not None else np.zeros(0, dtype=np.int64))
+        for label in sorted(b.children):
+            q.append((path + (label,), b.children[label]))
+
+    def pack(arrs):
+        off = np.zeros(len(arrs) + 1, dtype=np.int64)
+        off[1:] = np.cumsum([a.shape[0] for a in arrs])
+        return off, (np.concatenate(arrs) if arrs else np.zeros(0, dtype=np.int64))
+
+    lo, lv = pack(labels)
+    ro, rv = pack(root_idx)
+    po, pv = pack(parent_idx)
+    return {"paths": np.array(paths), "labels_off": lo, "labels": lv, "root_off": ro, "root": rv,
+            "parent_off": po, "parent": pv}
+
+
+def hierarchy_case(rng):
+    parents = rng.uniform(-6, 6, size=(5, 2))
+    kids = (parents[:, None, :] + rng.normal(0, 0.8, size=(5, 3, 2))).reshape(-1, 2)
+    x = np.vstack([k + rng.normal(0, 0.18, size=(120, 2)) for k in kids])
+    x = x[rng.permutation(x.shape[0])]
+    # the repeat fitter passes (radius_cutoff, cnn_cutoff) through unadjusted:
+    # the reduced metric compares squared distances with radius_cutoff itself
+    radii = np.array([0.5, 0.12, 0.05], dtype=np.float64)
+    cuts = np.array([4, 6, 8], dtype=np.int64)
+    recipe = {"input_data": "components_mview", "preparation_hook": "points_from_parts",
+              "hierarchical_fitter": "repeat", "hierarchical_fitter.fitter": "bfs",
+              "hierarchical_fitter.fitter.ngetter": "brute_force", "hierarchical_fitter.fitter.na": "vuset",
+              "hierarchical_fitter.fitter.checker": "switch", "hierarchical_fitter.fitter.queue": "fifo",
+              "hierarchical_fitter.fitter.ngetter.dgetter": "metric",
+              "hierarchical_fitter.fitter.ngetter.dgetter.metric": "euclidean_r"}
+    cl = cluster.Clustering(np.ascontiguousarray(x), recipe=recipe)
+    cl.fit_hierarchical(radius_cutoff=list(radii), cnn_cutoff=list(cuts), member_cutoff=5, v=False)
+    tree = hierarchy_tree(cl._bundle)
+    cl.reel()
+    reeled = np.asarray(cl._bundle.labels, dtype=np.int64)
+    save("hierarchy_repeat.npz", points=x, radii=radii, cuts=cuts, member_cutoff=np.int64(5), reeled=reeled,
+         **tree)
+
+
+def predict_case(rng):
+    centres = np.array([[0.0, 0.0], [2.5, 0.5], [1.0, 2.5]])
+    def sample(n):
+        return np.vstack([c + rng.normal(0, 0.45, size=(n, 2)) for c in centres] +
+                         [rng.uniform(-2, 4.5, size=(n // 5, 2))])
+    x = sample(300)
+    y = sample(450)
+    recipe = {
+        "input_data": _types.InputDataExtComponentsMemoryview,
+        "fitter": _fit.FitterExtBFS,
+        "fitter.ngetter": _types.NeighboursGetterExtBruteForce,
+        "fitter.na": _types.NeighboursExtVectorCPPUnorderedSet,
+        "fitter.checker": _types.SimilarityCheckerExtSwitchContains,
+        "fitter.queue": _types.QueueExtFIFOQueue,
+        "fitter.ngetter.dgetter": _types.DistanceGetterExtMetric,
+        "fitter.ngetter.dgetter.metric": _types.MetricExtEuclideanReduced,
+        "predictor": _fit.PredictorFirstmatch,
+        "predictor.ngetter": _types.NeighboursGetterExtBruteForce,
+        "predictor.ngetter.dgetter": _types.DistanceGetterExtMetric,
+        "predictor.ngetter.dgetter.metric": _types.MetricExtEuclideanReduced,
+        "predictor.ogetter": _types.NeighboursGetterExtBruteForce,
+        "predictor.ogetter.dgetter": _types.DistanceGetterExtMetric,
+        "predictor.ogetter.dgetter.metric": _types.MetricExtEuclideanReduced,
+        "predictor.na": _types.NeighboursExtVectorCPPUnorderedSet,
+        "predictor.checker": _types.SimilarityCheckerExtSwitchContains,
+    }
+    out = {"points": x, "other": y}
+    for k, (r, c, clusters) in enumerate([(0.3, 4, None), (0.25, 6, [1, 3]), (0.4, 2, None)]):
+        cl = cluster.Clustering(np.ascontiguousarray(x), recipe=recipe)
+        cl.fit(r, c, member_cutoff=5, v=False)
+        other = cluster.Clustering(np.ascontiguousarray(y), recipe=recipe)
+        cl.predict(other._bundle, r, c, clusters=clusters)
+        out[f"labels_{k}"] = np.asarray(cl.labels, dtype=np.int64)
+        out[f"predicted_{k}"] = np.asarray(other._bundle.labels, dtype=np.int64)
+        out[f"params_{k}"] = np.array([r, c], dtype=np.float64)
+        out[f"clusters_{k}"] = np.array(sorted(clusters) if clusters else [], dtype=np.int64)
+    save("predict_firstmatch.npz", n_cases=np.int64(3), **out)
+
 
 if __name__ == "__main__":
     main()

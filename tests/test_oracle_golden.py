@@ -111,3 +111,32 @@ def test_oracle_fused_mode_differs_only_by_rounding():
     b = o.neighbourhoods(x, r2, fpmode=o.FP_FUSED)
     da, db = np.diff(a[0]), np.diff(b[0])
     assert np.abs(da - db).sum() <= 4
+
+
+def test_oracle_predict_firstmatch_matches_reference():
+    from conftest import predict_cases
+    for x, labels, y, r, c, clusters, want in predict_cases(load_golden("predict_firstmatch.npz")):
+        prm = o.make_parameters(r, c, 0)
+        if clusters is None:
+            clusters = set(np.unique(labels).tolist()) - {0}
+        got, cons = o.predict_firstmatch(x, labels, y, prm["radius_cutoff"], prm["similarity_cutoff"],
+                                         prm["n_member_cutoff"], clusters)
+        assert np.array_equal(got, want)
+        assert np.array_equal(cons == 0, got != 0)
+
+
+def test_oracle_repeat_steps_match_reference_tree():
+    from conftest import golden_tree
+    g = load_golden("hierarchy_repeat.npz")
+    steps = o.repeat_step_labels(g["points"], g["radii"], g["cuts"], member_cutoff=int(g["member_cutoff"]))
+    tree = golden_tree(g)
+    checked = 0
+    for path, (lab, root, _) in tree.items():
+        depth = len(path)
+        if depth >= steps.shape[0]:
+            assert lab.shape[0] == 0  # leaves of the last step carry no labels
+            continue
+        idx = np.arange(g["points"].shape[0]) if depth == 0 else root
+        assert np.array_equal(lab, steps[depth][idx]), path
+        checked += 1
+    assert checked > 5
