@@ -14,10 +14,11 @@ from ._abi import CNNError, Context, default_context
 from ._bundle import ReferenceIndices, bfs_leafs, isolate
 from ._fit import Fitter, FitterGPU, FitterGPUNeighbourhoods, HierarchicalFitter, HierarchicalFitterRepeatGPU
 from ._predict import Predictor, PredictorFirstmatchGPU
-from ._types import (ClusterParameters, DistanceGetterGPUMetric, InputData, InputDataGPUComponents,
-                     InputDataGPUNeighbourhoods, Labels, MetricGPUEuclidean, MetricGPUEuclideanReduced,
-                     NeighboursGetterGPUGrid, NeighboursGetterGPULookup, NeighboursGPU, QueueGPUUnionFind,
-                     SimilarityCheckerGPU)
+from ._types import (ClusterParameters, DistanceGetterGPULookup, DistanceGetterGPUMetric, InputData,
+                     InputDataGPUComponents, InputDataGPUDistances, InputDataGPUDistancesLinear,
+                     InputDataGPUNeighbourhoods, Labels, MetricGPUEuclidean, MetricGPUEuclideanPeriodicReduced,
+                     MetricGPUEuclideanReduced, MetricGPUPrecomputed, NeighboursGetterGPUGrid,
+                     NeighboursGetterGPULookup, NeighboursGPU, QueueGPUUnionFind, SimilarityCheckerGPU)
 from .cluster import Bundle, Clustering
 from .report import Record, Summary
 from .sweep import sweep
@@ -31,5 +32,6 @@ __all__ = [
     "NeighboursGetterGPUGrid", "NeighboursGetterGPULookup", "NeighboursGPU", "QueueGPUUnionFind",
     "SimilarityCheckerGPU", "Bundle", "Clustering", "Record", "Summary", "sweep", "HierarchicalFitter",
     "HierarchicalFitterRepeatGPU", "Predictor", "PredictorFirstmatchGPU", "ReferenceIndices", "bfs_leafs",
-    "isolate",
+    "isolate", "DistanceGetterGPULookup", "InputDataGPUDistances", "InputDataGPUDistancesLinear",
+    "MetricGPUEuclideanPeriodicReduced", "MetricGPUPrecomputed",
 ]

@@ -25,6 +25,10 @@ _STATUS = {1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "timeo
 
 METRIC_EUCLIDEAN_REDUCED = 0
 METRIC_EUCLIDEAN = 1
+METRIC_PRECOMPUTED = 2
+METRIC_EUCLIDEAN_PERIODIC_REDUCED = 3
+DIST_SQUARE = 0
+DIST_LINEAR = 1
 FP_SEPARATE = 0
 FP_FUSED = 1
 DTYPE_F64 = 0
@@ -79,6 +83,8 @@ SIGNATURES = {
     "cnn_fit_csr_noalloc": (_INT, [_P, _P, _I64, _I64, _I64, _I64, _P, _P, _P]),
     "cnn_sweep": (_INT, [_P, _P, _I32, _P, _P, _I32, _INT, _INT, _I64, _I64, _P, _INT]),
     "cnn_sweep_pairs": (_INT, [_P, _P, _P, _P, _I32, _INT, _INT, _I32, _I64, _I64, _P, _INT]),
+    "cnn_set_distances": (_INT, [_P, _P, _INT, _I64, _INT]),
+    "cnn_set_periodic_bounds": (_INT, [_P, _P, _I32]),
     "cnn_predict": (_INT, [_P, _P, _INT, _I64, _I32, _P, _P, _I64, ctypes.c_double, _INT, _INT, _I64, _I64, _P, _P,
                            _INT]),
 }
@@ -182,6 +188,7 @@ class Context:
         self._h = h
         self.device = int(device)
         self.stream = stream
+        self._n_points = 0
 
     def close(self):
         if getattr(self, "_h", None):
@@ -214,6 +221,29 @@ class Context:
         return s.as_dict()
 
     # -- neighbour graph -------------------------------------------------------
+    def set_distances(self, distances, layout: int = DIST_SQUARE, n_points: Optional[int] = None):
+        """Precomputed distances (float64): [n, n] (DIST_SQUARE) or the
+        n(n-1)/2 upper triangle by rows (DIST_LINEAR)."""
+        if is_device_array(distances):
+            ptr, mem, keep = device_pointer(distances, np.float64), MEM_DEVICE, distances
+            size = int(np.prod(tuple(distances.shape)))
+        else:
+            arr = host_array(distances, np.float64)
+            ptr, mem, keep, size = arr.ctypes.data, MEM_HOST, arr, arr.size
+        if layout == DIST_SQUARE:
+            n = int(distances.shape[0])
+        else:
+            n = int(n_points) if n_points is not None else int(0.5 * (np.sqrt(8 * size + 1) + 1))
+        self._check(self._lib.cnn_set_distances(self._h, ctypes.c_void_p(ptr), int(layout), n, mem),
+                    "cnn_set_distances")
+        self._points_ref = keep
+        self._n_points = n
+
+    def set_periodic_bounds(self, bounds):
+        b = np.ascontiguousarray(bounds, dtype=np.float64).reshape(-1)
+        self._check(self._lib.cnn_set_periodic_bounds(self._h, ctypes.c_void_p(b.ctypes.data), b.shape[0]),
+                    "cnn_set_periodic_bounds")
+
     def set_points(self, points):
         """points: [n, d] float64/float32 numpy array or CUDA array."""
         if is_device_array(points):
@@ -256,14 +286,17 @@ class Context:
             self._check(self._lib.cnn_set_neighbours(self._h, ctypes.c_void_p(off.ctypes.data),
                                                      ctypes.c_void_p(idx.ctypes.data), n, MEM_HOST),
                         "cnn_set_neighbours")
+        self._n_points = n
 
     def neighbour_count(self) -> int:
         v = ctypes.c_int64()
         self._check(self._lib.cnn_neighbour_count(self._h, ctypes.byref(v)), "cnn_neighbour_count")
         return int(v.value)
 
-    def get_neighbours(self, n_points: int):
+    def get_neighbours(self, n_points: Optional[int] = None):
         """Sorted CSR (offsets int64[n+1], indices int32[nnz]) as numpy arrays."""
+        if n_points is None:
+            n_points = int(self._n_points)
         nnz = self.neighbour_count()
         off = np.empty(n_points + 1, dtype=np.int64)
         idx = np.empty(max(nnz, 1), dtype=np.int32)

@@ -19,9 +19,9 @@ from typing import Optional
 import numpy as np
 
 from . import _abi
-from ._types import (ClusterParameters, InputDataGPUNeighbourhoods, NeighboursGetterGPUGrid,
-                     NeighboursGetterGPULookup, SimilarityCheckerGPU, QueueGPUUnionFind, NeighboursGPU,
-                     _device_of)
+from ._types import (ClusterParameters, InputDataGPUDistances, InputDataGPUDistancesLinear,
+                     InputDataGPUNeighbourhoods, NeighboursGetterGPUGrid, NeighboursGetterGPULookup,
+                     SimilarityCheckerGPU, QueueGPUUnionFind, NeighboursGPU, _device_of)
 
 
 class Fitter(ABC):
@@ -51,6 +51,32 @@ class Fitter(ABC):
                 cnn_cutoff += 2
 
         return ClusterParameters(radius_cutoff, cnn_cutoff, cnn_cutoff, n_member_cutoff, current_start)
+
+
+def _distance_layout(input_data, metric_code: int):
+    """DIST_SQUARE / DIST_LINEAR for distance input, None for coordinates."""
+    if isinstance(input_data, InputDataGPUDistancesLinear):
+        return _abi.DIST_LINEAR
+    if isinstance(input_data, InputDataGPUDistances):
+        return _abi.DIST_SQUARE
+    meta = getattr(input_data, "meta", None) or {}
+    if meta.get("access_distances", False) or metric_code == _abi.METRIC_PRECOMPUTED:
+        shape = tuple(getattr(input_data.data, "shape", ()))
+        return _abi.DIST_LINEAR if len(shape) == 1 else _abi.DIST_SQUARE
+    return None
+
+
+def load_input(ctx: _abi.Context, input_data, neighbours_getter, metric_code: int) -> int:
+    """Points or distances of ``input_data`` onto the context; returns the
+    metric code the neighbour search uses."""
+    layout = _distance_layout(input_data, metric_code)
+    if layout is not None:
+        ctx.set_distances(input_data.data, layout, n_points=input_data.n_points)
+        return _abi.METRIC_PRECOMPUTED
+    ctx.set_points(input_data.data)
+    if metric_code == _abi.METRIC_EUCLIDEAN_PERIODIC_REDUCED:
+        ctx.set_periodic_bounds(neighbours_getter._distance_getter._metric.bounds)
+    return metric_code
 
 
 def _is_neighbourhood_input(input_data) -> bool:
@@ -142,13 +168,15 @@ class FitterGPU(Fitter):
         ctx = self.context_for(data)
         self._sync_stream(ctx, data)
         key = None
-        if self.reuse_graph and _abi.is_device_array(data) and hasattr(data, "_version"):
+        if (self.reuse_graph and _abi.is_device_array(data) and hasattr(data, "_version")
+                and _distance_layout(input_data, self._metric_code()) is None
+                and self._metric_code() != _abi.METRIC_EUCLIDEAN_PERIODIC_REDUCED):
             key = (id(data), int(data.data_ptr()), tuple(data.shape), int(data._version),
                    float(cluster_params.radius_cutoff), self._metric_code(), self._fpmode_code())
         if key is not None and key == self._graph_key:
             return ctx
-        ctx.set_points(data)
-        ctx.build_neighbours(cluster_params.radius_cutoff, self._metric_code(), self._fpmode_code())
+        metric = load_input(ctx, input_data, self._neighbours_getter, self._metric_code())
+        ctx.build_neighbours(cluster_params.radius_cutoff, metric, self._fpmode_code())
         self._graph_key = key
         return ctx
 
@@ -232,12 +260,12 @@ class HierarchicalFitterRepeatGPU(HierarchicalFitter):
             data = input_data.data
             ctx = fitter.context_for(data)
             fitter._sync_stream(ctx, data)
-            ctx.set_points(data)
+            metric = load_input(ctx, input_data, fitter._neighbours_getter, fitter._metric_code())
             fitter._graph_key = None
             out = ctx.sweep_pairs([p.radius_cutoff for p in params],
                                   [(p.similarity_cutoff, p.n_member_cutoff) for p in params],
                                   member_cutoff=2 if member_cutoff is None else int(member_cutoff),
-                                  max_clusters=max_clusters, sort=sort_by_size, metric=fitter._metric_code(),
+                                  max_clusters=max_clusters, sort=sort_by_size, metric=metric,
                                   fpmode=fitter._fpmode_code())
             return np.asarray(out)
         n = input_data.n_points

@@ -81,10 +81,13 @@ class PredictorFirstmatchGPU(Predictor):
             st = _abi.current_torch_stream(ctx.device)
             if st is not None and st != ctx.stream:
                 ctx.set_stream(st)
+        metric = self._metric_code()
         ctx.set_points(data)
+        if metric == _abi.METRIC_EUCLIDEAN_PERIODIC_REDUCED:
+            ctx.set_periodic_bounds(self._neighbours_getter._distance_getter._metric.bounds)
         ctx.predict(other, labels.labels, predictand_labels.consider_set, cluster_params.radius_cutoff,
                     cluster_params.similarity_cutoff, cluster_params.n_member_cutoff, predictand_labels.labels,
-                    predictand_labels.consider, metric=self._metric_code(),
+                    predictand_labels.consider, metric=metric,
                     fpmode=getattr(self._neighbours_getter, "fpmode_code", _abi.FP_SEPARATE))
 
 

@@ -240,6 +240,69 @@ class InputDataGPUComponents(InputData):
         return f"{type(self).__name__}"
 
 
+class InputDataGPUDistances(InputData):
+    """Precomputed distances as a square [n_points, n_points] float64 matrix
+    (the "distances" recipe's input, src/cnnclustering/recipes.py:329-339)."""
+
+    def __init__(self, data, *, meta=None):
+        if not _abi.is_device_array(data):
+            data = np.ascontiguousarray(data, dtype=P_AVALUE)
+        if len(data.shape) != 2 or data.shape[0] != data.shape[1]:
+            raise ValueError("distances must be a square [n_points, n_points] matrix")
+        self._data = data
+        self._meta = {"access_distances": True}
+        if meta:
+            self._meta.update(meta)
+
+    @property
+    def data(self):
+        return self._data
+
+    @property
+    def n_points(self) -> int:
+        return int(self._data.shape[0])
+
+    def get_distance(self, a: int, b: int) -> float:
+        return float(self._data[a, b])
+
+    def get_subset(self, indices) -> "InputDataGPUDistances":
+        idx = np.asarray(indices, dtype=np.int64)
+        if _abi.is_device_array(self._data):
+            import torch
+            t = torch.as_tensor(idx, device=self._data.device)
+            return type(self)(self._data[t][:, t].contiguous())
+        return type(self)(np.ascontiguousarray(self._data[np.ix_(idx, idx)]))
+
+
+class InputDataGPUDistancesLinear(InputData):
+    """Precomputed distances as the upper triangle by rows, n(n-1)/2 values
+    (InputDataExtDistancesLinearMemoryview, src/cnnclustering/_types.pyx:1112-1150)."""
+
+    def __init__(self, data, *, n_points=None, meta=None):
+        if not _abi.is_device_array(data):
+            data = np.ascontiguousarray(data, dtype=P_AVALUE).reshape(-1)
+        self._data = data
+        size = int(data.shape[0])
+        self._n_points = int(n_points) if n_points is not None else int(0.5 * (np.sqrt(8 * size + 1) + 1))
+        self._meta = {"access_distances": True}
+        if meta:
+            self._meta.update(meta)
+
+    @property
+    def data(self):
+        return self._data
+
+    @property
+    def n_points(self) -> int:
+        return self._n_points
+
+    def get_distance(self, a: int, b: int) -> float:
+        if a == b:
+            return 0.0
+        a, b = min(a, b), max(a, b)
+        return float(self._data[a * (self._n_points - 1) - (a * a - a) // 2 + b - a - 1])
+
+
 class InputDataGPUNeighbourhoods(InputData):
     """Precomputed neighbourhoods as CSR (offsets int64[n+1], indices int32)."""
 
@@ -304,6 +367,54 @@ class MetricGPUEuclidean:
 
     def adjust_radius(self, radius_cutoff: float) -> float:
         return radius_cutoff
+
+    def __str__(self):
+        return f"{type(self).__name__}"
+
+
+class MetricGPUPrecomputed:
+    """Distances given as input (MetricExtPrecomputed, src/cnnclustering/_types.pyx:
+    2108-2127): the stored value is compared with the radius as given."""
+
+    code = _abi.METRIC_PRECOMPUTED
+
+    def adjust_radius(self, radius_cutoff: float) -> float:
+        return radius_cutoff
+
+    def __str__(self):
+        return f"{type(self).__name__}"
+
+
+class MetricGPUEuclideanPeriodicReduced:
+    """Squared Euclidean distance with minimum images in a periodic box
+    (MetricExtEuclideanPeriodicReduced, src/cnnclustering/_types.pyx:2290-2348);
+    ``bounds`` per dimension, 0 = not periodic."""
+
+    code = _abi.METRIC_EUCLIDEAN_PERIODIC_REDUCED
+
+    def __init__(self, bounds):
+        self._bounds = np.ascontiguousarray(bounds, dtype=P_AVALUE).reshape(-1)
+
+    @property
+    def bounds(self):
+        return self._bounds
+
+    def adjust_radius(self, radius_cutoff: float) -> float:
+        return radius_cutoff ** 2
+
+    def __str__(self):
+        return f"{type(self).__name__}(bounds={self._bounds.tolist()})"
+
+
+class DistanceGetterGPULookup:
+    """Distances read from the input (DistanceGetterExtLookup,
+    src/cnnclustering/_types.pyx:2019-2037), e.g. InputDataGPUDistancesLinear."""
+
+    _metric = MetricGPUPrecomputed()
+
+    @classmethod
+    def get_builder_kwargs(cls):
+        return []
 
     def __str__(self):
         return f"{type(self).__name__}"

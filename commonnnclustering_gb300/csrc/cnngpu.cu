@@ -32,6 +32,21 @@ __global__ void widen_f32_kernel(const float *__restrict__ in, int64_t total, do
         out[e] = (double)in[e];
 }
 
+bool metric_known(int metric) {
+    return metric == CNN_METRIC_EUCLIDEAN_REDUCED || metric == CNN_METRIC_EUCLIDEAN ||
+           metric == CNN_METRIC_PRECOMPUTED || metric == CNN_METRIC_EUCLIDEAN_PERIODIC_REDUCED;
+}
+
+// The metric needs points (or, precomputed, distances) on the context.
+cnn_status check_source(cnn_context *ctx, int metric) {
+    if (metric == CNN_METRIC_PRECOMPUTED) {
+        if (!ctx->dist_set) return ctx->fail(CNN_ERR_STATE, "no distances: call cnn_set_distances first");
+        return CNN_OK;
+    }
+    if (ctx->d < 1) return ctx->fail(CNN_ERR_STATE, "no points: call cnn_set_points first");
+    return CNN_OK;
+}
+
 cnn_status check_ctx(cnn_context *ctx) {
     if (!ctx) return CNN_ERR_INVALID_ARG;
     cudaError_t e = cudaSetDevice(ctx->device);
@@ -182,6 +197,8 @@ CNN_API cnn_status cnn_set_points(cnn_context *ctx, const void *points, cnn_dtyp
     if (dtype != CNN_DTYPE_F64 && dtype != CNN_DTYPE_F32) return ctx->fail(CNN_ERR_INVALID_ARG, "bad dtype");
     if (mem != CNN_MEM_HOST && mem != CNN_MEM_DEVICE) return ctx->fail(CNN_ERR_INVALID_ARG, "bad memspace");
     ctx->have_graph = false;
+    ctx->dist = nullptr;
+    ctx->dist_set = false;
     ctx->n = n_points;
     ctx->d = n_dim;
     const int64_t total = n_points * n_dim;
@@ -215,13 +232,45 @@ CNN_API cnn_status cnn_set_points(cnn_context *ctx, const void *points, cnn_dtyp
     return CNN_OK;
 }
 
+CNN_API cnn_status cnn_set_distances(cnn_context *ctx, const double *distances, cnn_dist_layout layout,
+                                     int64_t n_points, cnn_memspace mem) {
+    CNN_TRY(check_ctx(ctx));
+    if (n_points < 0 || n_points > INT32_MAX - 1) return ctx->fail(CNN_ERR_INVALID_ARG, "n_points out of range");
+    if (layout != CNN_DIST_SQUARE && layout != CNN_DIST_LINEAR) return ctx->fail(CNN_ERR_INVALID_ARG, "bad layout");
+    if (mem != CNN_MEM_HOST && mem != CNN_MEM_DEVICE) return ctx->fail(CNN_ERR_INVALID_ARG, "bad memspace");
+    const int64_t count = layout == CNN_DIST_SQUARE ? n_points * n_points : n_points * (n_points - 1) / 2;
+    if (count > 0 && !distances) return ctx->fail(CNN_ERR_INVALID_ARG, "distances missing");
+    ctx->have_graph = false;
+    ctx->x = nullptr;
+    ctx->d = 0;
+    ctx->n = n_points;
+    ctx->dist_layout = layout;
+    if (mem == CNN_MEM_DEVICE || count == 0) {
+        ctx->dist = distances;
+    } else {
+        CNN_TRY(ctx->ensure(ctx->dist_own, sizeof(double) * (size_t)count));
+        CNN_CUDA(ctx, cudaMemcpyAsync(ctx->dist_own.ptr, distances, sizeof(double) * (size_t)count,
+                                      cudaMemcpyHostToDevice, ctx->stream));
+        ctx->dist = ctx->dist_own.as<double>();
+    }
+    ctx->dist_set = true;
+    CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return CNN_OK;
+}
+
+CNN_API cnn_status cnn_set_periodic_bounds(cnn_context *ctx, const double *bounds, int32_t n_dim) {
+    CNN_TRY(check_ctx(ctx));
+    if (n_dim < 0 || (n_dim > 0 && !bounds)) return ctx->fail(CNN_ERR_INVALID_ARG, "bad bounds");
+    ctx->periodic_bounds.assign(bounds, bounds + n_dim);
+    return CNN_OK;
+}
+
 CNN_API cnn_status cnn_build_neighbours(cnn_context *ctx, double radius_cutoff, cnn_metric metric,
                                         cnn_fpmode fpmode) {
     CNN_TRY(check_ctx(ctx));
-    if (metric != CNN_METRIC_EUCLIDEAN_REDUCED && metric != CNN_METRIC_EUCLIDEAN)
-        return ctx->fail(CNN_ERR_INVALID_ARG, "unknown metric");
+    if (!metric_known(metric)) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown metric");
     if (fpmode != CNN_FP_SEPARATE && fpmode != CNN_FP_FUSED) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown fpmode");
-    if (ctx->d < 1) return ctx->fail(CNN_ERR_STATE, "no points: call cnn_set_points first");
+    CNN_TRY(check_source(ctx, metric));
     return build_neighbours_impl(ctx, radius_cutoff, metric, fpmode);
 }
 
@@ -324,12 +373,11 @@ CNN_API cnn_status cnn_sweep(cnn_context *ctx, const double *radius_cutoffs, int
                              cnn_metric metric, cnn_fpmode fpmode, int64_t member_cutoff, int64_t max_clusters,
                              int64_t *labels_out, cnn_memspace mem) {
     CNN_TRY(check_ctx(ctx));
-    if (ctx->d < 1) return ctx->fail(CNN_ERR_STATE, "no points: call cnn_set_points first");
     if (n_radii < 1 || n_radii > 16 || n_cuts < 1 || !radius_cutoffs || !similarity_cutoffs || !n_member_cutoffs ||
         !labels_out)
         return ctx->fail(CNN_ERR_INVALID_ARG, "need 1..16 radii, >= 1 cut and all arrays");
-    if (metric != CNN_METRIC_EUCLIDEAN_REDUCED && metric != CNN_METRIC_EUCLIDEAN)
-        return ctx->fail(CNN_ERR_INVALID_ARG, "unknown metric");
+    if (!metric_known(metric)) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown metric");
+    CNN_TRY(check_source(ctx, metric));
     if (fpmode != CNN_FP_SEPARATE && fpmode != CNN_FP_FUSED) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown fpmode");
     const int64_t total = (int64_t)n_radii * n_cuts * ctx->n;
     int64_t *lab_dev = labels_out;
@@ -352,11 +400,10 @@ CNN_API cnn_status cnn_sweep_pairs(cnn_context *ctx, const double *radius_cutoff
                                    int64_t member_cutoff, int64_t max_clusters, int64_t *labels_out,
                                    cnn_memspace mem) {
     CNN_TRY(check_ctx(ctx));
-    if (ctx->d < 1) return ctx->fail(CNN_ERR_STATE, "no points: call cnn_set_points first");
     if (n_steps < 1 || !radius_cutoffs || !similarity_cutoffs || !n_member_cutoffs || !labels_out)
         return ctx->fail(CNN_ERR_INVALID_ARG, "need >= 1 step and all arrays");
-    if (metric != CNN_METRIC_EUCLIDEAN_REDUCED && metric != CNN_METRIC_EUCLIDEAN)
-        return ctx->fail(CNN_ERR_INVALID_ARG, "unknown metric");
+    if (!metric_known(metric)) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown metric");
+    CNN_TRY(check_source(ctx, metric));
     if (fpmode != CNN_FP_SEPARATE && fpmode != CNN_FP_FUSED) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown fpmode");
     for (int32_t i = 0; i < n_steps; ++i)
         if (std::isnan(radius_cutoffs[i])) return ctx->fail(CNN_ERR_INVALID_ARG, "NaN radius cutoff");
@@ -423,8 +470,9 @@ CNN_API cnn_status cnn_predict(cnn_context *ctx, const void *other_points, cnn_d
     if (ctx->n > 0 && !labels) return ctx->fail(CNN_ERR_INVALID_ARG, "labels of the clustered points are required");
     if (n_clusters > 0 && !clusters) return ctx->fail(CNN_ERR_INVALID_ARG, "clusters missing");
     if (dtype != CNN_DTYPE_F64 && dtype != CNN_DTYPE_F32) return ctx->fail(CNN_ERR_INVALID_ARG, "bad dtype");
-    if (metric != CNN_METRIC_EUCLIDEAN_REDUCED && metric != CNN_METRIC_EUCLIDEAN)
-        return ctx->fail(CNN_ERR_INVALID_ARG, "unknown metric");
+    if (metric == CNN_METRIC_PRECOMPUTED)
+        return ctx->fail(CNN_ERR_UNSUPPORTED, "prediction needs coordinates, not precomputed distances");
+    if (!metric_known(metric)) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown metric");
     if (fpmode != CNN_FP_SEPARATE && fpmode != CNN_FP_FUSED) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown fpmode");
     if (mem != CNN_MEM_HOST && mem != CNN_MEM_DEVICE) return ctx->fail(CNN_ERR_INVALID_ARG, "bad memspace");
     cudaStream_t st = ctx->stream;

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "cnngpu.h"
 
@@ -76,6 +77,16 @@ struct cnn_context {
     const double *x = nullptr;  // device pointer (borrowed or owned copy)
     cnn::DevBuf x_own;
     cnn::DevBuf x_f32_stage;    // float32 input staged before widening
+
+    // precomputed distances instead of points (cnn_set_distances)
+    const double *dist = nullptr;  // device pointer (borrowed or owned copy)
+    int dist_layout = 0;           // cnn_dist_layout
+    bool dist_set = false;
+    cnn::DevBuf dist_own;
+    // box lengths of the periodic metric (cnn_set_periodic_bounds), host copy
+    // and device copies (float64 then float32, per dimension)
+    std::vector<double> periodic_bounds;
+    cnn::DevBuf bounds_dev;
 
     // neighbour graph in internal (permuted) index space
     bool have_graph = false;

@@ -44,12 +44,42 @@ struct SearchParams {
     int fpmode;       // cnn_fpmode
     float thr_in;     // sf <= thr_in  -> neighbour
     float thr_out;    // sf >  thr_out -> not a neighbour; else float64
+    const double *bd = nullptr;  // periodic metric: box length per dimension (<= 0: not periodic)
+    const float *bf = nullptr;   // the same in float32
 };
+
+// Minimum-image difference of the periodic metric, reference order
+// (MetricExtEuclideanPeriodicReduced._calc_distance, _types.pyx:2303-2325):
+// d = |a - b|; if bound > 0: d = fmod(d, bound), d = bound - d if d > bound / 2.
+__device__ __forceinline__ double periodic_diff(double a, double b, double bound) {
+    double t = fabs(__dsub_rn(a, b));
+    if (bound > 0.0) {
+        t = fmod(t, bound);
+        if (t > bound / 2.0) t = __dsub_rn(bound, t);
+    }
+    return t;
+}
+
+__device__ __forceinline__ float periodic_diff_f(float a, float b, float bound) {
+    float t = fabsf(a - b);
+    if (bound > 0.f) {
+        t = fmodf(t, bound);
+        if (t > 0.5f * bound) t = bound - t;
+    }
+    return t;
+}
 
 // Exact float64 predicate in the reference's operation order.
 __device__ __forceinline__ bool exact_in_radius(const double *__restrict__ xa, const double *__restrict__ xb,
                                                 int d, const SearchParams &sp) {
     double s = 0.0;
+    if (sp.bd) {
+        for (int k = 0; k < d; ++k) {
+            const double t = periodic_diff(xa[k], xb[k], sp.bd[k]);
+            s = sp.fpmode == CNN_FP_FUSED ? __fma_rn(t, t, s) : __dadd_rn(s, __dmul_rn(t, t));
+        }
+        return s <= sp.rc;
+    }
     if (sp.fpmode == CNN_FP_FUSED) {
         for (int k = 0; k < d; ++k) {
             double t = __dsub_rn(xa[k], xb[k]);
@@ -365,9 +395,16 @@ __global__ void __launch_bounds__(kTileWarps * 32) tile_search_kernel(
             float sf = 0.f;
             const float *cr = cand + lane * ds;
             const float *qr = qry + wid * ds;
-            for (int k = 0; k < d; ++k) {
-                float t = qr[k] - cr[k];
-                sf = fmaf(t, t, sf);
+            if (sp.bf) {
+                for (int k = 0; k < d; ++k) {
+                    const float t = periodic_diff_f(qr[k], cr[k], sp.bf[k]);
+                    sf = fmaf(t, t, sf);
+                }
+            } else {
+                for (int k = 0; k < d; ++k) {
+                    float t = qr[k] - cr[k];
+                    sf = fmaf(t, t, sf);
+                }
             }
             if (sf <= sp.thr_in) {
                 in = true;
@@ -433,6 +470,48 @@ __global__ void __launch_bounds__(kTileWarps * 32) cross_tile_kernel(
         cnt += __popc(hit);
     }
     if (!kFill && active && lane == 0) deg[p] = (int32_t)cnt;
+}
+
+// Precomputed distances: row i keeps every j with distance(i, j) <= rc,
+// ascending (NeighboursGetterExtBruteForce._get over
+// MetricExtPrecomputed / DistanceGetterExtLookup, _types.pyx:1692-1710,
+// 2108-2127, 2019-2037).  Linear layout: the upper triangle by rows,
+// distance(a, b) for a < b at a (n - 1) - (a^2 - a) / 2 + b - a - 1, and 0
+// on the diagonal (_types.pyx:1127-1143).  One warp per row.
+template <bool kFill>
+__global__ void distance_rows_kernel(const double *__restrict__ dist, int layout, int64_t n, double rc,
+                                     int32_t *__restrict__ deg, const int64_t *__restrict__ row_off,
+                                     int32_t *__restrict__ cols) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = warp0; i < n; i += nwarps) {
+        int64_t w = kFill ? row_off[i] : 0;
+        int64_t cnt = 0;
+        const int64_t base_i = i * (n - 1) - (i * i - i) / 2;  // start of i's block (j > i)
+        for (int64_t j0 = 0; j0 < n; j0 += 32) {
+            const int64_t j = j0 + lane;
+            bool in = false;
+            if (j < n) {
+                double v;
+                if (layout == CNN_DIST_SQUARE) {
+                    v = dist[i * n + j];
+                } else if (j == i) {
+                    v = 0.0;
+                } else if (j > i) {
+                    v = dist[base_i + j - i - 1];
+                } else {
+                    v = dist[j * (n - 1) - (j * j - j) / 2 + i - j - 1];
+                }
+                in = v <= rc;
+            }
+            const unsigned hit = __ballot_sync(0xffffffffu, in);
+            if (kFill && in) cols[w + cnt + __popc(hit & lt)] = (int32_t)j;
+            cnt += __popc(hit);
+        }
+        if (!kFill && lane == 0) deg[i] = (int32_t)cnt;
+    }
 }
 
 __global__ void to_f32_kernel(const double *__restrict__ x, int64_t n, int d, const double *__restrict__ lo,
@@ -509,7 +588,7 @@ int bits_for(int64_t n) {
 // sf > rc2 + err + margin whenever the per-coordinate error is below
 // R/1000, which is required for the filter to be used at all.
 bool filter_thresholds(const std::vector<double> &ext, double R, double rc2, float *thr_in,
-                       float *thr_out, double *band) {
+                       float *thr_out, double *band, const std::vector<double> *bounds = nullptr) {
     const double u32 = ldexp(1.0, -24), u64 = ldexp(1.0, -53);
     const int d = (int)ext.size();
     double emax = 0;
@@ -523,6 +602,17 @@ bool filter_thresholds(const std::vector<double> &ext, double R, double rc2, flo
         if (delta > 1e-3 * R) return false;
         // |dx - D_k| <= 2 delta + u32 (|D_k| + 2 delta) with |D_k| <= 2R
         double eta = 2 * delta + u32 * (2 * R + 2 * delta);
+        const double L = bounds ? (*bounds)[k] : 0.0;
+        if (L > 0) {
+            // minimum image: |a - b| (float32, up to the extent), then fmod
+            // (exact) and bound - d.  The image map is 1-Lipschitz in the
+            // difference and moves by at most (E/L + 1)|L_f - L| with the
+            // float32 bound; the final subtraction rounds once more, and
+            // the float64 reference rounds its own difference.
+            eta = 2 * delta + u32 * (ext[k] + 2 * delta) + u32 * (ext[k] + L) + u32 * L * (1 + u32) +
+                  4 * u64 * (ext[k] + L);
+            if (eta > 1e-3 * R) return false;
+        }
         err += eta * (4 * R + eta);
     }
     // rounding of the float32 squares and sum (fma chain): gamma_{d+1}
@@ -575,14 +665,67 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         return CNN_OK;
     }
 
+    if (metric == CNN_METRIC_PRECOMPUTED) {
+        if (!ctx->dist_set) return ctx->fail(CNN_ERR_STATE, "precomputed metric: call cnn_set_distances first");
+        int32_t *deg = ctx->deg.as<int32_t>();
+        int64_t *row_off = ctx->row_off.as<int64_t>();
+        CNN_TRY(iota_i32(ctx, ctx->perm.as<int32_t>(), n));
+        CNN_TRY(iota_i32(ctx, ctx->inv.as<int32_t>(), n));
+        const unsigned blocks = std::min<unsigned>(grid_for(n * 32, 256), 152u * 16u);
+        stage_begin(ctx, 2);
+        distance_rows_kernel<false><<<blocks, 256, 0, st>>>(ctx->dist, ctx->dist_layout, n, radius_cutoff, deg, nullptr,
+                                                            nullptr);
+        CNN_LAUNCH_CHECK(ctx);
+        stage_end(ctx, 2);
+        set_last_zero_kernel<<<1, 1, 0, st>>>(deg, n);
+        CNN_LAUNCH_CHECK(ctx);
+        CNN_TRY(scan_exclusive_i32_to_i64(ctx, deg, row_off, n + 1));
+        int64_t nnz = 0;
+        CNN_CUDA(ctx, cudaMemcpyAsync(&nnz, row_off + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CNN_CUDA(ctx, cudaStreamSynchronize(st));
+        CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1)));
+        stage_begin(ctx, 4);
+        distance_rows_kernel<true><<<blocks, 256, 0, st>>>(ctx->dist, ctx->dist_layout, n, radius_cutoff, nullptr,
+                                                           row_off, ctx->cols.as<int32_t>());
+        CNN_LAUNCH_CHECK(ctx);
+        stage_end(ctx, 4);
+        CNN_CUDA(ctx, cudaStreamSynchronize(st));
+        ctx->identity_perm = true;
+        ctx->stats.search_kind = 4;
+        ctx->stats.n_candidates = n * n;
+        ctx->stats.n_nonzero = nnz;
+        ctx->nnz = nnz;
+        ctx->have_graph = true;
+        return CNN_OK;
+    }
+    if (!ctx->x) return ctx->fail(CNN_ERR_STATE, "no points: call cnn_set_points first");
+
     // search radius R in coordinate units.  A NaN or negative cutoff admits
     // no pair; +inf admits every pair whose distance is not NaN, which only
     // the all-pairs search with every pair decided in float64 can express.
     double R = metric == CNN_METRIC_EUCLIDEAN ? radius_cutoff : sqrt(radius_cutoff);
     const bool radius_ok = radius_cutoff >= 0.0 && isfinite(radius_cutoff);
     const bool radius_inf = radius_cutoff == INFINITY;
+    const bool periodic = metric == CNN_METRIC_EUCLIDEAN_PERIODIC_REDUCED;
+    if (periodic) {
+        // minimum-image distances: the all-pairs search with the periodic
+        // float32 test and float64 recheck
+        if ((int)ctx->periodic_bounds.size() != d)
+            return ctx->fail(CNN_ERR_INVALID_ARG, "periodic metric: call cnn_set_periodic_bounds with n_dim bounds");
+        CNN_TRY(ctx->ensure(ctx->bounds_dev, (sizeof(double) + sizeof(float)) * (size_t)d + 64));
+        std::vector<float> bf(d);
+        for (int k = 0; k < d; ++k) bf[k] = (float)ctx->periodic_bounds[k];
+        double *bd_dev = ctx->bounds_dev.as<double>();
+        float *bf_dev = reinterpret_cast<float *>(bd_dev + d);
+        CNN_CUDA(ctx, cudaMemcpyAsync(bd_dev, ctx->periodic_bounds.data(), sizeof(double) * d, cudaMemcpyHostToDevice,
+                                      st));
+        CNN_CUDA(ctx, cudaMemcpyAsync(bf_dev, bf.data(), sizeof(float) * d, cudaMemcpyHostToDevice, st));
+        CNN_CUDA(ctx, cudaStreamSynchronize(st));  // bf leaves scope
+        sp.bd = bd_dev;
+        sp.bf = bf_dev;
+    }
 
-    if (d >= 16 && radius_ok) {
+    if (d >= 16 && radius_ok && !periodic) {
         // tensor-core Gram search; declines (used = false) for non-finite
         // data or when the float64 band would hold too many pairs
         bool used = false;
@@ -638,9 +781,10 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     for (int k = 0; k < 3; ++k) ctx->grid_extent[k] = k < d ? ext[k] : 0.0;
     double band = 0;
     bool filt = false;
-    if (radius_ok && (metric == CNN_METRIC_EUCLIDEAN_REDUCED || metric == CNN_METRIC_EUCLIDEAN)) {
+    if (radius_ok && (metric == CNN_METRIC_EUCLIDEAN_REDUCED || metric == CNN_METRIC_EUCLIDEAN || periodic)) {
         const double rc2 = metric == CNN_METRIC_EUCLIDEAN ? radius_cutoff * radius_cutoff : radius_cutoff;
-        filt = filter_thresholds(ext, R, rc2, &sp.thr_in, &sp.thr_out, &band);
+        filt = filter_thresholds(ext, R, rc2, &sp.thr_in, &sp.thr_out, &band,
+                                 periodic ? &ctx->periodic_bounds : nullptr);
     }
     if (!radius_ok && !radius_inf) {
         // nothing satisfies `s <= NaN`; a negative cutoff admits nothing
@@ -653,7 +797,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
 
     // ---- choose the search
     GridGeom geo{};
-    bool use_grid = d <= 3 && radius_ok && R > 0 && isfinite(R);
+    bool use_grid = d <= 3 && radius_ok && R > 0 && isfinite(R) && !periodic;
     if (use_grid) {
         double h = R * (1.0 + 1e-6);
         // cells cost 12 bytes each (count + start); allow up to 64 per point
@@ -930,6 +1074,8 @@ cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev, con
     ctx->n = n;
     ctx->d = 0;
     ctx->x = nullptr;
+    ctx->dist = nullptr;
+    ctx->dist_set = false;
     CNN_TRY(ctx->ensure(ctx->counters, 16 * sizeof(unsigned long long)));
     CNN_CUDA(ctx, cudaMemsetAsync(ctx->counters.ptr, 0, 16 * sizeof(unsigned long long), st));
     CNN_TRY(ctx->ensure(ctx->deg, sizeof(int32_t) * (size_t)(n + 1)));

@@ -154,6 +154,17 @@ REGISTERED_RECIPES = {
     "none": {},
     "coordinates": dict(_GPU_POINTS),
     "gpu_coordinates": dict(_GPU_POINTS),
+    "distances": {
+        "input_data": "components_mview",
+        "preparation_hook": "points_from_parts",
+        "fitter": "gpu",
+        "fitter.ngetter": "grid",
+        "fitter.na": "gpu",
+        "fitter.checker": "gpu",
+        "fitter.queue": "union_find",
+        "fitter.ngetter.dgetter": "metric",
+        "fitter.ngetter.dgetter.metric": "precomputed",
+    },
     "neighbourhoods": {
         "input_data": "neighbourhoods_gpu",
         "preparation_hook": "neighbourhoods",
@@ -197,14 +208,18 @@ COMPONENT_NAME_TYPE_MAP = {
                          "pass": prepare_pass},
     "input_data": {"components_gpu": _types.InputDataGPUComponents,
                    "components_mview": _types.InputDataGPUComponents,
+                   "distances_gpu": _types.InputDataGPUDistances,
+                   "distances_linear_gpu": _types.InputDataGPUDistancesLinear,
                    "neighbourhoods_gpu": _types.InputDataGPUNeighbourhoods,
                    "neighbourhoods_mview": _types.InputDataGPUNeighbourhoods},
     "neighbours_getter": {"grid": _types.NeighboursGetterGPUGrid, "brute_force": _types.NeighboursGetterGPUGrid,
                           "lookup": _types.NeighboursGetterGPULookup},
-    "distance_getter": {"metric": _types.DistanceGetterGPUMetric},
+    "distance_getter": {"metric": _types.DistanceGetterGPUMetric, "lookup": _types.DistanceGetterGPULookup},
     "neighbours": {"gpu": _types.NeighboursGPU, "vector": _types.NeighboursGPU, "vuset": _types.NeighboursGPU},
     "metric": {"euclidean": _types.MetricGPUEuclidean, "euclidean_r": _types.MetricGPUEuclideanReduced,
-               "euclidean_reduced": _types.MetricGPUEuclideanReduced},
+               "euclidean_reduced": _types.MetricGPUEuclideanReduced, "precomputed": _types.MetricGPUPrecomputed,
+               "euclidean_periodic_r": _types.MetricGPUEuclideanPeriodicReduced,
+               "euclidean_periodic_reduced": _types.MetricGPUEuclideanPeriodicReduced},
     "similarity_checker": {"gpu": _types.SimilarityCheckerGPU, "screen": _types.SimilarityCheckerGPU,
                            "switch": _types.SimilarityCheckerGPU, "contains": _types.SimilarityCheckerGPU},
     "queue": {"union_find": _types.QueueGPUUnionFind, "fifo": _types.QueueGPUUnionFind},

@@ -68,8 +68,22 @@ typedef enum cnn_status {
 /* Which distance the getter compares with radius_cutoff. */
 typedef enum cnn_metric {
     CNN_METRIC_EUCLIDEAN_REDUCED = 0, /* sum of squares <= radius_cutoff (= r*r) */
-    CNN_METRIC_EUCLIDEAN = 1          /* sqrt(sum of squares) <= radius_cutoff (= r) */
+    CNN_METRIC_EUCLIDEAN = 1,         /* sqrt(sum of squares) <= radius_cutoff (= r) */
+    CNN_METRIC_PRECOMPUTED = 2,       /* stored distance <= radius_cutoff (= r), cnn_set_distances
+                                         (MetricExtPrecomputed, _types.pyx:2108-2127, and the
+                                         lookup getter, :2019-2037) */
+    CNN_METRIC_EUCLIDEAN_PERIODIC_REDUCED = 3 /* sum of squared minimum-image differences
+                                         <= radius_cutoff (= r*r), bounds from
+                                         cnn_set_periodic_bounds (_types.pyx:2290-2348) */
 } cnn_metric;
+
+/* Layout of precomputed distances (cnn_set_distances). */
+typedef enum cnn_dist_layout {
+    CNN_DIST_SQUARE = 0, /* [n][n] row-major: the "distances" recipe's
+                            InputDataExtComponentsMemoryview (_types.pyx:1034-1062) */
+    CNN_DIST_LINEAR = 1  /* upper triangle by rows, n(n-1)/2 values:
+                            InputDataExtDistancesLinearMemoryview (_types.pyx:1112-1150) */
+} cnn_dist_layout;
 
 /* How each term of the float64 distance sum is accumulated:
  * SEPARATE: total = total + (t*t), two roundings (reference built for
@@ -104,7 +118,8 @@ typedef struct cnn_stats {
     int64_t n_candidates;     /* candidate pairs tested by the search */
     int64_t n_clusters;       /* clusters found by the last fit */
     int32_t search_kind;      /* 1 = cell grid (d <= 3), 2 = tiled all-pairs float32,
-                                 3 = tensor-core Gram (d >= 16), 0 = precomputed */
+                                 3 = tensor-core Gram (d >= 16), 4 = precomputed distances,
+                                 0 = precomputed neighbourhoods */
     int32_t filter_enabled;   /* 1 when the float32 prefilter was usable */
     double filter_band;       /* half-width of the float64 recheck band on d^2 */
     float ms_bbox, ms_cells, ms_count, ms_scan, ms_fill;   /* neighbour build */
@@ -193,6 +208,21 @@ CNN_API cnn_status cnn_sweep(cnn_context *ctx, const double *radius_cutoffs, int
                              int32_t n_cuts, cnn_metric metric, cnn_fpmode fpmode,
                              int64_t member_cutoff, int64_t max_clusters, int64_t *labels_out,
                              cnn_memspace mem);
+
+/* Precomputed distances instead of points (layout above); device arrays
+ * are used in place.  The neighbour graph is then built with
+ * cnn_build_neighbours(ctx, radius_cutoff, CNN_METRIC_PRECOMPUTED, ...):
+ * N(i) = {j : distance(i, j) <= radius_cutoff}, the diagonal of the linear
+ * layout being 0, as NeighboursGetterExtBruteForce._get
+ * (src/cnnclustering/_types.pyx:1692-1710) collects them. */
+CNN_API cnn_status cnn_set_distances(cnn_context *ctx, const double *distances, cnn_dist_layout layout,
+                                     int64_t n_points, cnn_memspace mem);
+
+/* Box lengths per dimension for CNN_METRIC_EUCLIDEAN_PERIODIC_REDUCED
+ * (MetricExtEuclideanPeriodicReduced(bounds), _types.pyx:2290-2348): per
+ * dimension d = |a - b|, and when bound > 0, d = fmod(d, bound) and
+ * d = bound - d if d > bound / 2.  Host array of n_dim values. */
+CNN_API cnn_status cnn_set_periodic_bounds(cnn_context *ctx, const double *bounds, int32_t n_dim);
 
 /* The step list of HierarchicalFitterRepeat._fit
  * (src/cnnclustering/_fit.pyx:1131-1141): step i fits (radius_cutoffs[i],

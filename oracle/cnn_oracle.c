@@ -505,3 +505,34 @@ int oracle_neighbour_fill_grid(const double *x, int64_t n, int32_t d, double rad
     if (rc == 1) return oracle_neighbour_fill(x, n, d, radius_cutoff, metric, fpmode, nthreads, offsets, indices);
     return rc;
 }
+
+/* ------------------------------------------------------------------ */
+/* Periodic metric: MetricExtEuclideanPeriodicReduced._calc_distance   */
+/* (_types.pyx:2303-2325): per dimension d = |a - b|; when bound > 0,  */
+/* d = fmod(d, bound) and d = bound - d if d > bound / 2; total += d^2 */
+/* (separate or fused, like the plain metric).                         */
+/* ------------------------------------------------------------------ */
+double oracle_periodic_sqdist(const double *xa, const double *xb, int32_t d, const double *bounds, int fpmode)
+{
+    double total = 0.0;
+    for (int32_t k = 0; k < d; ++k) {
+        double t = fabs(xa[k] - xb[k]);
+        const double bound = bounds[k];
+        if (bound > 0) {
+            t = fmod(t, bound);
+            if (t > bound / 2) t = bound - t;
+        }
+        total = fpmode == 1 ? fma(t, t, total) : total + t * t;
+    }
+    return total;
+}
+
+/* Row of `query` among the n points under the periodic metric (ascending). */
+int64_t oracle_periodic_row(const double *x, int64_t n, int32_t d, const double *bounds, const double *query,
+                            double radius_cutoff, int fpmode, int32_t *out)
+{
+    int64_t c = 0;
+    for (int64_t i = 0; i < n; ++i)
+        if (oracle_periodic_sqdist(query, x + i * d, d, bounds, fpmode) <= radius_cutoff) out[c++] = (int32_t)i;
+    return c;
+}

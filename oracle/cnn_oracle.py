@@ -19,6 +19,11 @@ and restates the pure-Python parts of the reference with numpy:
                             (src/cnnclustering/_fit.pyx:1060-1144)
 * ``predict_firstmatch`` -- PredictorFirstmatch.predict
                             (src/cnnclustering/_fit.pyx:1235-1291)
+* ``periodic_neighbourhoods`` / ``distance_neighbourhoods`` -- the brute-force
+                            getter over MetricExtEuclideanPeriodicReduced and
+                            over precomputed distances (square or linear)
+                            (src/cnnclustering/_types.pyx:1692-1710, 2290-2348,
+                            2108-2127, 2019-2037, 1127-1143)
 """
 from __future__ import annotations
 
@@ -65,6 +70,10 @@ def lib():
         L.oracle_fit_bfs_csr.argtypes = [p, p, i64, i64, i64, i64, p, p]
         L.oracle_fit_bfs_points.restype = i64
         L.oracle_fit_bfs_points.argtypes = [p, i64, i32, dbl, i, i, i64, i64, i64, p, p]
+        L.oracle_periodic_sqdist.restype = dbl
+        L.oracle_periodic_sqdist.argtypes = [p, p, i32, p, i]
+        L.oracle_periodic_row.restype = i64
+        L.oracle_periodic_row.argtypes = [p, i64, i32, p, p, dbl, i, p]
         _lib = L
     return _lib
 
@@ -272,17 +281,23 @@ def other_row(x, q, radius_cutoff: float, metric=METRIC_EUCLIDEAN_REDUCED, fpmod
 
 def predict_firstmatch(x, labels, y, radius_cutoff: float, similarity_cutoff: int, n_member_cutoff: int,
                        clusters, other_labels=None, other_consider=None, metric=METRIC_EUCLIDEAN_REDUCED,
-                       fpmode=FP_SEPARATE):
+                       fpmode=FP_SEPARATE, periodic_bounds=None):
     """PredictorFirstmatch.predict (src/cnnclustering/_fit.pyx:1235-1291) with
     brute-force getters; parameters as Predictor.make_parameters gives them.
-    Returns (other_labels, other_consider)."""
+    With ``periodic_bounds`` the clustered points' rows use the periodic
+    metric while the other points' rows use the plain sum of squares, as
+    MetricExtEuclideanPeriodicReduced._calc_distance_other does
+    (_types.pyx:2327-2345).  Returns (other_labels, other_consider)."""
     x = np.ascontiguousarray(x, dtype=np.float64)
     y = np.ascontiguousarray(y, dtype=np.float64)
     m = y.shape[0]
     out = np.zeros(m, dtype=np.int64) if other_labels is None else np.array(other_labels, dtype=np.int64)
     cons = np.ones(m, dtype=np.uint8) if other_consider is None else np.array(other_consider, dtype=np.uint8)
     clusters = set(int(c) for c in clusters)
-    offsets, indices = neighbourhoods(x, radius_cutoff, metric, fpmode, grid=False)
+    if periodic_bounds is not None:
+        offsets, indices = periodic_neighbourhoods(x, periodic_bounds, radius_cutoff, fpmode)
+    else:
+        offsets, indices = neighbourhoods(x, radius_cutoff, metric, fpmode, grid=False)
     for p in range(m):
         if cons[p] == 0:
             continue
@@ -328,3 +343,63 @@ def repeat_step_labels(x, radius_cutoffs, cnn_cutoffs, member_cutoff=None, max_c
             sort_by_size(labels, member_cutoff, max_clusters)
         rows.append(labels)
     return np.stack(rows)
+
+
+def _rows_to_csr(rows):
+    offsets = np.zeros(len(rows) + 1, dtype=np.int64)
+    offsets[1:] = np.cumsum([r.shape[0] for r in rows])
+    indices = np.concatenate(rows).astype(np.int32) if rows else np.zeros(0, dtype=np.int32)
+    return offsets, indices
+
+
+def periodic_neighbourhoods(x, bounds, radius_cutoff: float, fpmode=FP_SEPARATE):
+    """Brute-force rows (self included, ascending) under the periodic metric;
+    radius_cutoff as compared (r**2)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    n, d = x.shape
+    b = np.ascontiguousarray(bounds, dtype=np.float64).reshape(-1)
+    out = np.empty(n, dtype=np.int32)
+    L = lib()
+    rows = []
+    for i in range(n):
+        c = L.oracle_periodic_row(_ptr(x), n, d, _ptr(b), _ptr(np.ascontiguousarray(x[i])), float(radius_cutoff),
+                                  fpmode, _ptr(out))
+        rows.append(out[:c].copy())
+    return _rows_to_csr(rows)
+
+
+def linear_distance(data, n: int, a: int, b: int) -> float:
+    """InputDataExtDistancesLinearMemoryview._get_distance (_types.pyx:1127-1143)."""
+    if a == b:
+        return 0.0
+    a, b = min(a, b), max(a, b)
+    return float(data[a * (n - 1) - (a * a - a) // 2 + b - a - 1])
+
+
+def distance_neighbourhoods(dist, radius_cutoff: float, linear: bool = False, n_points=None):
+    """Rows {j : distance(i, j) <= radius_cutoff} (ascending) from a square
+    matrix or the linear upper triangle."""
+    if linear:
+        dist = np.asarray(dist, dtype=np.float64).reshape(-1)
+        n = int(n_points) if n_points is not None else int(0.5 * (np.sqrt(8 * dist.shape[0] + 1) + 1))
+        sq = np.zeros((n, n), dtype=np.float64)
+        iu = np.triu_indices(n, 1)  # row-major upper triangle, the linear order
+        sq[iu] = dist
+        sq[(iu[1], iu[0])] = dist
+    else:
+        sq = np.asarray(dist, dtype=np.float64)
+    rows = [np.nonzero(sq[i] <= radius_cutoff)[0].astype(np.int32) for i in range(sq.shape[0])]
+    return _rows_to_csr(rows)
+
+
+def fit_from_neighbourhoods(offsets, indices, cnn_cutoff: int, member_cutoff=None, max_clusters=None,
+                            is_selfcounting: bool = True):
+    """Clustering.fit on given rows: parameters (c+2, c+1), fresh labels, sort_by_size."""
+    n = offsets.shape[0] - 1
+    labels = np.zeros(n, dtype=np.int64)
+    consider = np.ones(n, dtype=np.uint8)
+    sim = cnn_cutoff + 2 if is_selfcounting else cnn_cutoff
+    nmem = cnn_cutoff + 1 if is_selfcounting else cnn_cutoff
+    fit_bfs_csr(offsets, indices, sim, nmem, 1, consider, labels)
+    sort_by_size(labels, member_cutoff, max_clusters)
+    return labels

@@ -84,3 +84,9 @@ def predict_cases(g):
         cases.append((g["points"], g[f"labels_{k}"], g["other"], float(r), int(c),
                       cl.tolist() if cl.size else None, g[f"predicted_{k}"]))
     return cases
+
+
+def pairwise_distances(x):
+    """Square Euclidean distances, the expression tests/golden/make_golden.py used."""
+    x = np.asarray(x, dtype=np.float64)
+    return np.sqrt(((x[:, None, :] - x[None, :, :]) ** 2).sum(-1))

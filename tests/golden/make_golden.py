@@ -237,6 +237,9 @@ def main():
     # 13. PredictorFirstmatch on coordinates (brute-force getters)
     predict_case(rng)
 
+    # 14. the periodic metric and precomputed distances (square and linear)
+    metric_input_cases(rng)
+
 
 def hierarchy_tree(root):
     """Bundles of the tree, breadth first: path, labels, root/parent indices."""
@@ -328,6 +331,66 @@ def predict_case(rng):
         out[f"params_{k}"] = np.array([r, c], dtype=np.float64)
         out[f"clusters_{k}"] = np.array(sorted(clusters) if clusters else [], dtype=np.int64)
     save("predict_firstmatch.npz", n_cases=np.int64(3), **out)
+
+
+def metric_input_cases(rng):
+    # dihedral-like angles in [-180, 180): clusters that wrap around the box
+    centres = np.array([[-170.0, 60.0], [175.0, -160.0], [-60.0, -40.0], [60.0, 170.0]])
+    ang = np.vstack([c + rng.normal(0, 14.0, size=(700, 2)) for c in centres] +
+                    [rng.uniform(-180, 180, size=(300, 2))])
+    ang = (ang + 180.0) % 360.0 - 180.0
+    ang = ang[rng.permutation(ang.shape[0])]
+    bounds = np.array([360.0, 360.0])
+    metric = (_types.MetricExtEuclideanPeriodicReduced, (bounds,), {})
+    out = {"points": ang, "bounds": bounds}
+    for k, (r, c, mc) in enumerate([(10.0, 15, 50), (6.0, 5, 10)]):
+        cl = cluster.Clustering(np.ascontiguousarray(ang), fitter__getter__dgetter__metric=metric)
+        cl.fit(r, c, member_cutoff=mc, v=False)
+        out[f"labels_{k}"] = np.asarray(cl.labels, dtype=np.int64)
+        out[f"params_{k}"] = np.array([r, c, mc], dtype=np.float64)
+        off, ind = reference_periodic_rows(ang, bounds, r)
+        out[f"csr_sha256_{k}"] = np.array(csr_digest(off, ind))
+    save("periodic_dihedrals.npz", n_cases=np.int64(2), **out)
+
+    # precomputed distances of a small blob set
+    x = np.vstack([c + rng.normal(0, 0.4, size=(250, 2)) for c in ([0, 0], [3, 0], [1.5, 2.5])])
+    x = x[rng.permutation(x.shape[0])]
+    dist = pairwise_distances(x)
+    r, c = 0.35, 5
+    cl = cluster.Clustering(np.ascontiguousarray(dist), recipe="distances")
+    cl.fit(r, c, member_cutoff=5, v=False)
+    square = np.asarray(cl.labels, dtype=np.int64)
+    iu = np.triu_indices(x.shape[0], 1)
+    lin = np.ascontiguousarray(dist[iu])
+    recipe = {"input_data": _types.InputDataExtDistancesLinearMemoryview, "fitter": "bfs",
+              "fitter.ngetter": "brute_force", "fitter.na": "vuset", "fitter.checker": "switch",
+              "fitter.queue": "fifo", "fitter.ngetter.dgetter": "lookup"}
+    cl = cluster.Clustering(_types.InputDataExtDistancesLinearMemoryview(lin), recipe=recipe)
+    cl.fit(r, c, member_cutoff=5, v=False)
+    linear = np.asarray(cl.labels, dtype=np.int64)
+    # the distances are not stored: tests rebuild them with the same expression
+    save("precomputed_distances.npz", points=x, radius_cutoff=np.float64(r),
+         cnn_cutoff=np.int64(c), member_cutoff=np.int64(5), labels_square=square, labels_linear=linear)
+
+
+def pairwise_distances(x):
+    """Square Euclidean distance matrix (the expression the tests repeat)."""
+    return np.sqrt(((x[:, None, :] - x[None, :, :]) ** 2).sum(-1))
+
+
+def reference_periodic_rows(x, bounds, r):
+    m = _types.MetricExtEuclideanPeriodicReduced(np.asarray(bounds, dtype=np.float64))
+    getter = _types.NeighboursGetterExtBruteForce(_types.DistanceGetterExtMetric(m))
+    data = _types.InputDataExtComponentsMemoryview(np.ascontiguousarray(x, dtype=np.float64))
+    params = ClusterParameters(r * r)
+    nb = _types.NeighboursExtVector(64)
+    rows = []
+    for i in range(x.shape[0]):
+        getter.get(i, data, nb, params)
+        rows.append(np.array([nb.get_member(k) for k in range(nb.n_points)], dtype=np.int32))
+    offsets = np.zeros(x.shape[0] + 1, dtype=np.int64)
+    offsets[1:] = np.cumsum([len(a) for a in rows])
+    return offsets, np.concatenate(rows)
 
 
 if __name__ == "__main__":

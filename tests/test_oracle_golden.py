@@ -140,3 +140,25 @@ def test_oracle_repeat_steps_match_reference_tree():
         assert np.array_equal(lab, steps[depth][idx]), path
         checked += 1
     assert checked > 5
+
+
+def test_oracle_periodic_metric_matches_reference():
+    g = load_golden("periodic_dihedrals.npz")
+    for k in range(int(g["n_cases"])):
+        r, c, mc = g[f"params_{k}"]
+        off, idx = o.periodic_neighbourhoods(g["points"], g["bounds"], r * r)
+        assert digest(off, idx) == str(g[f"csr_sha256_{k}"])
+        labels = o.fit_from_neighbourhoods(off, idx, int(c), member_cutoff=int(mc))
+        assert np.array_equal(labels, g[f"labels_{k}"])
+
+
+def test_oracle_precomputed_distances_match_reference():
+    from conftest import pairwise_distances
+    g = load_golden("precomputed_distances.npz")
+    dist = pairwise_distances(g["points"])
+    iu = np.triu_indices(dist.shape[0], 1)
+    r, c, mc = float(g["radius_cutoff"]), int(g["cnn_cutoff"]), int(g["member_cutoff"])
+    sq = o.fit_from_neighbourhoods(*o.distance_neighbourhoods(dist, r), c, member_cutoff=mc)
+    lin = o.fit_from_neighbourhoods(*o.distance_neighbourhoods(dist[iu], r, linear=True), c, member_cutoff=mc)
+    assert np.array_equal(sq, g["labels_square"])
+    assert np.array_equal(lin, g["labels_linear"])
