@@ -13,6 +13,7 @@ the compute in hand-written sm_103a CUDA kernels behind the C ABI of
 from ._abi import CNNError, Context, default_context
 from ._bundle import ReferenceIndices, bfs_leafs, isolate
 from ._fit import Fitter, FitterGPU, FitterGPUNeighbourhoods, HierarchicalFitter, HierarchicalFitterRepeatGPU
+from ._mst import HierarchicalFitterMSTPrimGPU, WeightedGraph
 from ._predict import Predictor, PredictorFirstmatchGPU
 from ._types import (ClusterParameters, DistanceGetterGPULookup, DistanceGetterGPUMetric, InputData,
                      InputDataGPUComponents, InputDataGPUDistances, InputDataGPUDistancesLinear,
@@ -33,5 +34,5 @@ __all__ = [
     "SimilarityCheckerGPU", "Bundle", "Clustering", "Record", "Summary", "sweep", "HierarchicalFitter",
     "HierarchicalFitterRepeatGPU", "Predictor", "PredictorFirstmatchGPU", "ReferenceIndices", "bfs_leafs",
     "isolate", "DistanceGetterGPULookup", "InputDataGPUDistances", "InputDataGPUDistancesLinear",
-    "MetricGPUEuclideanPeriodicReduced", "MetricGPUPrecomputed",
+    "MetricGPUEuclideanPeriodicReduced", "MetricGPUPrecomputed", "HierarchicalFitterMSTPrimGPU", "WeightedGraph",
 ]

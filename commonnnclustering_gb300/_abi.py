@@ -84,6 +84,7 @@ SIGNATURES = {
     "cnn_sweep": (_INT, [_P, _P, _I32, _P, _P, _I32, _INT, _INT, _I64, _I64, _P, _INT]),
     "cnn_sweep_pairs": (_INT, [_P, _P, _P, _P, _I32, _INT, _INT, _I32, _I64, _I64, _P, _INT]),
     "cnn_set_distances": (_INT, [_P, _P, _INT, _I64, _INT]),
+    "cnn_mst_prim": (_INT, [_P, ctypes.c_double, _INT, _INT, _P, _P, _P, _I64, ctypes.POINTER(_I64)]),
     "cnn_set_periodic_bounds": (_INT, [_P, _P, _I32]),
     "cnn_predict": (_INT, [_P, _P, _INT, _I64, _I32, _P, _P, _I64, ctypes.c_double, _INT, _INT, _I64, _I64, _P, _P,
                            _INT]),
@@ -422,6 +423,19 @@ class Context:
                                           int(similarity_cutoff), int(n_member_cutoff), ctypes.c_void_p(out_l),
                                           ctypes.c_void_p(out_c), mem), "cnn_predict")
         del keep
+
+    def mst_prim(self, radius_cutoff: float, metric: int = METRIC_EUCLIDEAN_REDUCED, fpmode: int = FP_SEPARATE):
+        """Maximum spanning forest edges (a, b, weight) in Prim's tree-queue order."""
+        cap = max(int(self._n_points) - 1, 1)
+        a = np.empty(cap, dtype=np.int64)
+        b = np.empty(cap, dtype=np.int64)
+        w = np.empty(cap, dtype=np.int64)
+        ne = ctypes.c_int64()
+        self._check(self._lib.cnn_mst_prim(self._h, float(radius_cutoff), int(metric), int(fpmode),
+                                           ctypes.c_void_p(a.ctypes.data), ctypes.c_void_p(b.ctypes.data),
+                                           ctypes.c_void_p(w.ctypes.data), cap, ctypes.byref(ne)), "cnn_mst_prim")
+        k = int(ne.value)
+        return a[:k], b[:k], w[:k]
 
     def check_lists(self, a, b, c: int) -> bool:
         a = host_array(a, np.int32)

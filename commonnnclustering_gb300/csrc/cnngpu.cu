@@ -543,6 +543,27 @@ CNN_API cnn_status cnn_predict(cnn_context *ctx, const void *other_points, cnn_d
     return CNN_OK;
 }
 
+CNN_API cnn_status cnn_mst_prim(cnn_context *ctx, double radius_cutoff, cnn_metric metric, cnn_fpmode fpmode,
+                                int64_t *edges_a, int64_t *edges_b, int64_t *weights, int64_t capacity,
+                                int64_t *n_edges) {
+    CNN_TRY(check_ctx(ctx));
+    if (!n_edges) return ctx->fail(CNN_ERR_INVALID_ARG, "n_edges missing");
+    if (!metric_known(metric)) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown metric");
+    if (fpmode != CNN_FP_SEPARATE && fpmode != CNN_FP_FUSED) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown fpmode");
+    CNN_TRY(check_source(ctx, metric));
+    std::vector<int64_t> a, b, w;
+    CNN_TRY(mst_prim_impl(ctx, radius_cutoff, metric, fpmode, &a, &b, &w));
+    *n_edges = (int64_t)a.size();
+    if ((int64_t)a.size() > capacity || (!a.empty() && (!edges_a || !edges_b || !weights)))
+        return ctx->fail(CNN_ERR_INVALID_ARG, "edge arrays too small (n_points - 1 always suffice)");
+    if (!a.empty()) {
+        memcpy(edges_a, a.data(), sizeof(int64_t) * a.size());
+        memcpy(edges_b, b.data(), sizeof(int64_t) * b.size());
+        memcpy(weights, w.data(), sizeof(int64_t) * w.size());
+    }
+    return CNN_OK;
+}
+
 CNN_API cnn_status cnn_check_lists(cnn_context *ctx, const int32_t *a, int64_t na, const int32_t *b, int64_t nb,
                                    int64_t c, int32_t *result, cnn_memspace mem) {
     CNN_TRY(check_ctx(ctx));

@@ -192,6 +192,11 @@ cnn_status predict_impl(cnn_context *ctx, const double *xq, int64_t m, const int
                         int fpmode, int64_t similarity_cutoff, int64_t n_member_cutoff, int64_t *other_labels_dev,
                         uint8_t *other_consider_dev);
 
+// mst.cu: maximum spanning forest of the common-neighbour graph (Prim's
+// order); edges in the order the reference's tree queue pops them
+cnn_status mst_prim_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode, std::vector<int64_t> *ea,
+                         std::vector<int64_t> *eb, std::vector<int64_t> *ew);
+
 // gram.cu: tensor-core search (n_dim >= 16); *used = false when it declined
 cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode, bool *used);
 

@@ -15,7 +15,7 @@ from collections.abc import Iterable
 
 import numpy as np
 
-from . import _fit, _predict, _types
+from . import _fit, _mst, _predict, _types
 
 P_AINDEX = _types.P_AINDEX
 P_AVALUE = _types.P_AVALUE
@@ -224,7 +224,8 @@ COMPONENT_NAME_TYPE_MAP = {
                            "switch": _types.SimilarityCheckerGPU, "contains": _types.SimilarityCheckerGPU},
     "queue": {"union_find": _types.QueueGPUUnionFind, "fifo": _types.QueueGPUUnionFind},
     "fitter": {"gpu": _fit.FitterGPU, "bfs": _fit.FitterGPU},
-    "hierarchical_fitter": {"repeat": _fit.HierarchicalFitterRepeatGPU},
+    "hierarchical_fitter": {"repeat": _fit.HierarchicalFitterRepeatGPU, "mst": _mst.HierarchicalFitterMSTPrimGPU},
+    "priority_queue": {"maxheap": _mst.PriorityQueueMaxHeapGPU},
     "predictor": {"firstmatch": _predict.PredictorFirstmatchGPU},
 }
 

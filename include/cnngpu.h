@@ -258,6 +258,19 @@ CNN_API cnn_status cnn_predict(cnn_context *ctx, const void *other_points, cnn_d
                                int64_t similarity_cutoff, int64_t n_member_cutoff, int64_t *other_labels,
                                uint8_t *other_consider, cnn_memspace mem);
 
+/* Maximum spanning forest of the common-neighbour graph, as
+ * HierarchicalFitterMSTPrim._fit builds it (src/cnnclustering/_fit.pyx:
+ * 820-899): neighbourhoods at radius_cutoff (as compared: r*r for the
+ * reduced metric), every pair weighted by its full common-neighbour count
+ * (_types.pyx:2708-2753), Prim's algorithm from every unvisited point in
+ * index order with the reference's max-heap order (-weight, (a, b)).
+ * Output host arrays (capacity >= n_points - 1): the tree edges (a, b,
+ * weight) in the order the reference's tree queue pops them (weight
+ * descending, then a, then b).  The neighbour graph stays in the context. */
+CNN_API cnn_status cnn_mst_prim(cnn_context *ctx, double radius_cutoff, cnn_metric metric, cnn_fpmode fpmode,
+                                int64_t *edges_a, int64_t *edges_b, int64_t *weights, int64_t capacity,
+                                int64_t *n_edges);
+
 /* ---------------------------------------------------------------------
  * Fit without device memory allocation.  This entry point has no
  * counterpart in the reference.

@@ -403,3 +403,43 @@ def fit_from_neighbourhoods(offsets, indices, cnn_cutoff: int, member_cutoff=Non
     fit_bfs_csr(offsets, indices, sim, nmem, 1, consider, labels)
     sort_by_size(labels, member_cutoff, max_clusters)
     return labels
+
+
+def mst_prim_edges(x, radius_cutoff: float, metric=METRIC_EUCLIDEAN_REDUCED, fpmode=FP_SEPARATE, neighbours=None):
+    """Tree edges of HierarchicalFitterMSTPrim._fit (src/cnnclustering/_fit.pyx:
+    820-899) in the order its tree queue pops them: Prim's algorithm over the
+    neighbour graph from every unvisited point in index order, weights = the
+    full common-neighbour count (SimilarityCheckerExtScreensorted._get,
+    _types.pyx:2708-2753), a max-heap keyed (-weight, (a, b)).
+    ``radius_cutoff`` as compared (r**2 for the reduced metric).
+    Returns a list of (a, b, weight)."""
+    import heapq
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    n = x.shape[0]
+    if neighbours is None:
+        neighbours = neighbourhoods(x, radius_cutoff, metric, fpmode)
+    off, idx = neighbours
+    rows = [idx[off[i]:off[i + 1]] for i in range(n)]
+    visited = np.zeros(n, dtype=bool)
+    heap, tree = [], []
+    for point in range(n):
+        if visited[point]:
+            continue
+        visited[point] = True
+        for member in rows[point]:
+            if not visited[member]:
+                heapq.heappush(heap, (-count_common_sorted(rows[point], rows[member]), (point, int(member))))
+        while heap:
+            w, (a, b) = heapq.heappop(heap)
+            if visited[b]:
+                continue
+            visited[b] = True
+            heapq.heappush(tree, (w, (a, b)))
+            for member in rows[b]:
+                if not visited[member]:
+                    heapq.heappush(heap, (-count_common_sorted(rows[b], rows[member]), (b, int(member))))
+    out = []
+    while tree:
+        w, (a, b) = heapq.heappop(tree)
+        out.append((a, b, -w))
+    return out

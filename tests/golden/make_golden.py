@@ -240,6 +240,9 @@ def main():
     # 14. the periodic metric and precomputed distances (square and linear)
     metric_input_cases(rng)
 
+    # 15. HierarchicalFitterMSTPrim: the bundle tree of a maximum spanning forest
+    mst_case(rng)
+
 
 def hierarchy_tree(root):
     """Bundles of the tree, breadth first: path, labels, root/parent indices."""
@@ -391,6 +394,56 @@ def reference_periodic_rows(x, bounds, r):
     offsets = np.zeros(x.shape[0] + 1, dtype=np.int64)
     offsets[1:] = np.cumsum([len(a) for a in rows])
     return offsets, np.concatenate(rows)
+
+
+def mst_tree(root):
+    """Bundles breadth first: path, graph nodes, graph edges (a, b, weight), lambda."""
+    from collections import deque
+    paths, nodes, edges, lambdas = [], [], [], []
+    q = deque([((), root)])
+    while q:
+        path, b = q.popleft()
+        paths.append(".".join(str(p) for p in path))
+        g = b._graph
+        nodes.append(np.array(sorted(g.nodes), dtype=np.int64) if g is not None else np.zeros(0, dtype=np.int64))
+        e = sorted((min(u, v), max(u, v), float(d["weight"])) for u, v, d in g.edges(data=True)) if g is not None \
+            else []
+        edges.append(np.array(e, dtype=np.float64).reshape(-1, 3))
+        lambdas.append(float(b._lambda))
+        for label in sorted(b.children):
+            q.append((path + (label,), b.children[label]))
+    no = np.zeros(len(nodes) + 1, dtype=np.int64)
+    no[1:] = np.cumsum([a.shape[0] for a in nodes])
+    eo = np.zeros(len(edges) + 1, dtype=np.int64)
+    eo[1:] = np.cumsum([a.shape[0] for a in edges])
+    return {"paths": np.array(paths), "nodes_off": no, "nodes": np.concatenate(nodes), "edges_off": eo,
+            "edges": np.concatenate(edges) if edges else np.zeros((0, 3)), "lambdas": np.array(lambdas)}
+
+
+def mst_case(rng):
+    out = {}
+    cases = []
+    x1 = np.vstack([c + rng.normal(0, 0.25, size=(150, 2)) for c in ([0, 0], [1.6, 0.2], [0.8, 1.5])] +
+                   [rng.uniform(-1, 2.5, size=(40, 2))])
+    x1 = x1[rng.permutation(x1.shape[0])]
+    cases.append((x1, 0.3, 10))
+    x2 = np.vstack([c + rng.normal(0, 0.3, size=(120, 2)) for c in ([0, 0], [4, 4])])  # two components
+    cases.append((x2, 0.35, 5))
+    for k, (x, r, mc) in enumerate(cases):
+        recipe = {"input_data": "components_mview", "preparation_hook": "points_from_parts",
+                  "hierarchical_fitter": "mst", "hierarchical_fitter.ngetter": "brute_force",
+                  "hierarchical_fitter.ngetter.dgetter": "metric",
+                  "hierarchical_fitter.ngetter.dgetter.metric": "euclidean_r",
+                  "hierarchical_fitter.na": "vector", "hierarchical_fitter.checker": "screen",
+                  "hierarchical_fitter.pq": "maxheap"}
+        cl = cluster.Clustering(np.ascontiguousarray(x), recipe=recipe)
+        cl.fit_hierarchical(radius_cutoff=r, member_cutoff=mc, v=False)
+        tree = mst_tree(cl._bundle)
+        out[f"points_{k}"] = x
+        out[f"params_{k}"] = np.array([r, mc], dtype=np.float64)
+        for key, val in tree.items():
+            out[f"{key}_{k}"] = val
+    save("mst_prim.npz", n_cases=np.int64(len(cases)), **out)
 
 
 if __name__ == "__main__":
