@@ -100,6 +100,9 @@ struct cnn_context {
     cnn::DevBuf xf4;      // float4[n] permuted float32 coordinates (grid search)
     cnn::DevBuf cell_of;  // int32[n] cell id per point (original order)
     cnn::DevBuf cell_start;  // int32[ncells+2]
+    // one-pass grid search: per-cell slot offsets, the rows in their slots,
+    // each row's slot start
+    cnn::DevBuf grid_slot_base, grid_slot_cols, grid_qslot;
 
     // extents (max - min of finite points) per dimension of the last grid search
     double grid_extent[3] = {0.0, 0.0, 0.0};

@@ -208,8 +208,10 @@ __device__ __forceinline__ void tmem_wait_ld(uint32_t (&v)[32]) {
 
 // Emission for a 32-column chunk with at least one neighbour or band pair
 // somewhere in the warp: one warp-wide atomic per output list reserves the
-// slots, then each thread writes its pairs.  Fully unrolled so the
-// accumulator registers are never indexed dynamically.
+// slots, then each thread writes its own pairs, visiting only the set bits
+// of its masks.  A band pair's accumulator value is picked from the 32
+// registers with an unrolled select, so the registers are never indexed
+// dynamically (which would move them to local memory).
 __device__ __forceinline__ void epilogue_emit_masks(const GramArgs &args, const EpilogueTile &et,
                                                     const uint32_t (&v)[32], const float *norms, int col0, int lane,
                                                     uint32_t in_mask, uint32_t amb_mask) {
@@ -232,26 +234,28 @@ __device__ __forceinline__ void epilogue_emit_masks(const GramArgs &args, const 
     }
     unsigned long long wk = __shfl_sync(0xffffffffu, base_k, 31) + (unsigned long long)(inc_k - my_keys);
     unsigned long long wa = __shfl_sync(0xffffffffu, base_a, 31) + (unsigned long long)(inc_a - my_amb);
-    if (!(in_mask | amb_mask)) return;
     const uint64_t gi = (uint64_t)et.gi;
-#pragma unroll
-    for (int jj = 0; jj < 32; ++jj) {
-        const uint64_t gj = (uint64_t)et.J * kTM + (uint64_t)(col0 + jj);
-        if ((in_mask >> jj) & 1u) {
-            if (wk < (unsigned long long)args.key_cap) args.keys[wk] = (gi << 32) | gj;
+    const uint64_t gj0 = (uint64_t)et.J * kTM + (uint64_t)col0;
+    const unsigned long long kcap = (unsigned long long)args.key_cap, acap = (unsigned long long)args.amb_cap;
+    for (uint32_t m = in_mask; m; m &= m - 1) {
+        const uint64_t gj = gj0 + (uint64_t)(__ffs(m) - 1);
+        if (wk < kcap) args.keys[wk] = (gi << 32) | gj;
+        ++wk;
+        if (!et.diag) {
+            if (wk < kcap) args.keys[wk] = (gj << 32) | gi;
             ++wk;
-            if (!et.diag) {
-                if (wk < (unsigned long long)args.key_cap) args.keys[wk] = (gj << 32) | gi;
-                ++wk;
-            }
         }
-        if ((amb_mask >> jj) & 1u) {
-            if (wa < (unsigned long long)args.amb_cap) {
-                args.amb[wa] = (gi << 32) | gj | (et.diag ? 0ull : (1ull << 63));
-                args.amb_d2[wa] = fmaf(-2.f, __uint_as_float(v[jj]), et.ni + norms[jj]);
-            }
-            ++wa;
+    }
+    for (uint32_t m = amb_mask; m; m &= m - 1) {
+        const int jj = __ffs(m) - 1;
+        uint32_t acc = 0;
+#pragma unroll
+        for (int u = 0; u < 32; ++u) acc = u == jj ? v[u] : acc;
+        if (wa < acap) {
+            args.amb[wa] = (gi << 32) | (gj0 + (uint64_t)jj) | (et.diag ? 0ull : (1ull << 63));
+            args.amb_d2[wa] = fmaf(-2.f, __uint_as_float(acc), et.ni + norms[jj]);
         }
+        ++wa;
     }
 }
 

@@ -152,17 +152,24 @@ __global__ void __launch_bounds__(kRadixThreads) radix_hist_kernel(const uint64_
     hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
 }
 
-__global__ void __launch_bounds__(kRadixThreads) radix_scatter_kernel(const uint64_t *__restrict__ keys,
+// Stable scatter of one tile: keys are ranked by digit within the tile
+// (warp match_any ranks + per-warp digit counts), placed in digit order in
+// shared memory, then written out so that consecutive threads write
+// consecutive addresses of each digit's run (coalesced stores).
+__global__ void __launch_bounds__(kRadixThreads, 2) radix_scatter_kernel(const uint64_t *__restrict__ keys,
                                                                       uint64_t *__restrict__ out, int64_t n,
                                                                       int shift, int64_t ntiles,
                                                                       const int64_t *__restrict__ goff) {
     __shared__ int32_t wcount[kRadixWarps][256];
     __shared__ int64_t tile_off[256];
+    __shared__ int32_t digit_start[257];
+    __shared__ uint64_t staged[kRadixTile];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < kRadixWarps * 256; i += kRadixThreads) (&wcount[0][0])[i] = 0;
     tile_off[threadIdx.x] = goff[(int64_t)threadIdx.x * ntiles + blockIdx.x];
     __syncthreads();
-    const int64_t base = (int64_t)blockIdx.x * kRadixTile + (int64_t)w * (kRadixItems * 32);
+    const int64_t tile0 = (int64_t)blockIdx.x * kRadixTile;
+    const int64_t base = tile0 + (int64_t)w * (kRadixItems * 32);
     const unsigned lt = (1u << lane) - 1u;
     uint64_t k[kRadixItems];
     int32_t rank[kRadixItems];
@@ -183,8 +190,9 @@ __global__ void __launch_bounds__(kRadixThreads) radix_scatter_kernel(const uint
         dig[it] = valid ? d : -1;
     }
     __syncthreads();
+    int32_t digit_total;
     {
-        int t = threadIdx.x;  // one digit per thread
+        const int t = threadIdx.x;  // one digit per thread: offsets of the warps within the digit
         int32_t run = 0;
 #pragma unroll
         for (int ww = 0; ww < kRadixWarps; ++ww) {
@@ -192,14 +200,32 @@ __global__ void __launch_bounds__(kRadixThreads) radix_scatter_kernel(const uint
             wcount[ww][t] = run;
             run += c;
         }
+        digit_total = run;
+    }
+    // exclusive scan of the digit totals (256 threads, one digit each)
+    {
+        __shared__ int32_t scan_buf[256];
+        scan_buf[threadIdx.x] = digit_total;
+        __syncthreads();
+        for (int o = 1; o < 256; o <<= 1) {
+            const int32_t v = threadIdx.x >= o ? scan_buf[threadIdx.x - o] : 0;
+            __syncthreads();
+            scan_buf[threadIdx.x] += v;
+            __syncthreads();
+        }
+        digit_start[threadIdx.x] = scan_buf[threadIdx.x] - digit_total;
+        if (threadIdx.x == 255) digit_start[256] = scan_buf[255];
     }
     __syncthreads();
 #pragma unroll
-    for (int it = 0; it < kRadixItems; ++it) {
-        if (dig[it] >= 0) {
-            int64_t pos = tile_off[dig[it]] + wcount[w][dig[it]] + rank[it];
-            out[pos] = k[it];
-        }
+    for (int it = 0; it < kRadixItems; ++it)
+        if (dig[it] >= 0) staged[digit_start[dig[it]] + wcount[w][dig[it]] + rank[it]] = k[it];
+    __syncthreads();
+    const int valid_in_tile = digit_start[256];
+    for (int i = threadIdx.x; i < valid_in_tile; i += kRadixThreads) {
+        const uint64_t key = staged[i];
+        const int d = (int)((key >> shift) & 0xff);
+        out[tile_off[d] + (i - digit_start[d])] = key;
     }
 }
 

@@ -222,12 +222,65 @@ __global__ void item_fill_kernel(const int64_t *__restrict__ cell_start, int64_t
     }
 }
 
-template <bool kFill>
+// Candidate count of a cell: the points of the 3 x 3 x 3 cells around it
+// (the same 9 x-runs the search packs).
+__device__ __forceinline__ int64_t cell_candidates(int64_t cid, const GridGeom &geo,
+                                                   const int64_t *__restrict__ cell_start) {
+    const int32_t cx = (int32_t)(cid % geo.g[0]);
+    const int32_t cy = (int32_t)((cid / geo.g[0]) % geo.g[1]);
+    const int32_t cz = (int32_t)(cid / ((int64_t)geo.g[0] * geo.g[1]));
+    const int32_t xlo = cx > 0 ? cx - 1 : 0;
+    const int32_t xhi = cx + 1 < geo.g[0] ? cx + 1 : geo.g[0] - 1;
+    int64_t total = 0;
+    for (int dz = -1; dz <= 1; ++dz) {
+        const int32_t z = cz + dz;
+        if (z < 0 || z >= geo.g[2]) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int32_t y = cy + dy;
+            if (y < 0 || y >= geo.g[1]) continue;
+            const int64_t row = (int64_t)geo.g[0] * ((int64_t)y + (int64_t)geo.g[1] * z);
+            const int64_t rs = cell_start[row + xlo], re = cell_start[row + xhi + 1];
+            if (re > rs) total += re - rs;
+        }
+    }
+    return total;
+}
+
+// slots of a cell = its points x its candidate count (upper bound of every row)
+__global__ void cell_slots_kernel(const int64_t *__restrict__ cell_start, GridGeom geo,
+                                  int64_t *__restrict__ slots) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < geo.ncells;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = cell_start[c + 1] - cell_start[c];
+        slots[c] = q > 0 ? q * cell_candidates(c, geo, cell_start) : 0;
+    }
+}
+
+// rows from their slots to the CSR (one warp per row)
+__global__ void compact_rows_kernel(int64_t n, const int64_t *__restrict__ qslot, const int32_t *__restrict__ slot_cols,
+                                    const int64_t *__restrict__ row_off, int32_t *__restrict__ cols) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t q = warp0; q < n; q += nwarps) {
+        const int64_t src = qslot[q], dst = row_off[q], len = row_off[q + 1] - dst;
+        for (int64_t e = lane; e < len; e += 32) cols[dst + e] = slot_cols[src + e];
+    }
+}
+
+// kMode: kCount writes deg; kFill writes the rows at row_off; kSlots writes
+// each query's row into its slot (slot_base[cell] + rank in cell x the
+// cell's candidate count, an upper bound of the row), its length to deg
+// and the slot start to qslot -- one pass instead of count + fill when the
+// slots fit in memory.
+constexpr int kCount = 0, kFill = 1, kSlots = 2;
+
+template <int kMode>
 __global__ void __launch_bounds__(kGridWarps * 32) grid_search_kernel(
     const int2 *__restrict__ items, const double *__restrict__ x, int d, GridGeom geo, SearchParams sp,
     const int32_t *__restrict__ perm, const int64_t *__restrict__ cell_start, const float4 *__restrict__ xf4,
     int32_t *__restrict__ deg, const int64_t *__restrict__ row_off, int32_t *__restrict__ cols,
-    unsigned long long *__restrict__ counters) {
+    unsigned long long *__restrict__ counters, int64_t *__restrict__ qslot) {
     __shared__ float4 s_xf[kGridTile];
     __shared__ int32_t s_j[kGridTile];
     __shared__ int64_t s_rs[9];
@@ -282,7 +335,10 @@ __global__ void __launch_bounds__(kGridWarps * 32) grid_search_kernel(
         q[k] = q0 + (int64_t)wid * kQueriesPerWarp + k;
         const bool ok = q[k] < qend;
         qf[k] = ok ? xf4[q[k]] : make_float4(INFINITY, INFINITY, INFINITY, 0.f);
-        wpos[k] = (kFill && ok) ? row_off[q[k]] : 0;
+        if (kMode == kFill) wpos[k] = ok ? row_off[q[k]] : 0;
+        else if (kMode == kSlots) wpos[k] = ok ? row_off[cid] + (q[k] - cell_start[cid]) * (int64_t)total : 0;
+        else wpos[k] = 0;
+        if (kMode == kSlots && ok && lane == 0) qslot[q[k]] = wpos[k];
         cnt[k] = 0;
         if (!ok) q[k] = -1;
     }
@@ -332,7 +388,7 @@ __global__ void __launch_bounds__(kGridWarps * 32) grid_search_kernel(
             }
 #pragma unroll
             for (int k = 0; k < kQueriesPerWarp; ++k) {
-                if (kFill) {
+                if (kMode != kCount) {
                     const unsigned hit = __ballot_sync(0xffffffffu, in[k]);
                     if (in[k]) cols[wpos[k] + cnt[k] + __popc(hit & lt)] = s_j[t];
                     cnt[k] += __popc(hit);
@@ -342,10 +398,12 @@ __global__ void __launch_bounds__(kGridWarps * 32) grid_search_kernel(
             }
         }
     }
-    if (!kFill) {
+    if (kMode != kFill) {
+        if (kMode == kCount) {
 #pragma unroll
-        for (int k = 0; k < kQueriesPerWarp; ++k)
-            for (int o = 16; o > 0; o >>= 1) cnt[k] += __shfl_down_sync(0xffffffffu, cnt[k], o);
+            for (int k = 0; k < kQueriesPerWarp; ++k)
+                for (int o = 16; o > 0; o >>= 1) cnt[k] += __shfl_down_sync(0xffffffffu, cnt[k], o);
+        }
         if (lane == 0) {
 #pragma unroll
             for (int k = 0; k < kQueriesPerWarp; ++k)
@@ -823,6 +881,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     int32_t *deg = ctx->deg.as<int32_t>();
     int64_t *row_off = ctx->row_off.as<int64_t>();
     int64_t grid_items = 0;
+    bool use_slots = false;
     unsigned long long *counters = ctx->counters.as<unsigned long long>();
 
     if (use_grid) {
@@ -855,10 +914,28 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         CNN_LAUNCH_CHECK(ctx);
         CNN_CUDA(ctx, cudaMemsetAsync(ctx->io_a.as<int32_t>() + geo.ncells, 0, sizeof(int32_t), st));
         CNN_TRY(scan_exclusive_i32_to_i64(ctx, ctx->io_a.as<int32_t>(), ctx->io_b.as<int64_t>(), geo.ncells + 1));
-        int64_t nitems = 0;
-        CNN_CUDA(ctx, cudaMemcpyAsync(&nitems, ctx->io_b.as<int64_t>() + geo.ncells, sizeof(int64_t),
+        // slots: every row's upper bound (its cell's candidate count)
+        CNN_TRY(ctx->ensure(ctx->grid_slot_base, sizeof(int64_t) * (size_t)(geo.ncells + 2)));
+        int64_t *slot_base = ctx->grid_slot_base.as<int64_t>();
+        CNN_TRY(ctx->ensure(ctx->scratch_c, sizeof(int64_t) * (size_t)(geo.ncells + 2)));
+        CNN_CUDA(ctx, cudaMemsetAsync(ctx->scratch_c.as<int64_t>() + geo.ncells, 0, sizeof(int64_t), st));
+        cell_slots_kernel<<<std::min<unsigned>(grid_for(geo.ncells, 256), 152u * 16u), 256, 0, st>>>(
+            ctx->cell_start.as<int64_t>(), geo, ctx->scratch_c.as<int64_t>());
+        CNN_LAUNCH_CHECK(ctx);
+        CNN_TRY(scan_exclusive_i64(ctx, ctx->scratch_c.as<int64_t>(), slot_base, geo.ncells + 1));
+        int64_t hcounts[2] = {0, 0};
+        CNN_CUDA(ctx, cudaMemcpyAsync(&hcounts[0], ctx->io_b.as<int64_t>() + geo.ncells, sizeof(int64_t),
                                       cudaMemcpyDeviceToHost, st));
+        CNN_CUDA(ctx, cudaMemcpyAsync(&hcounts[1], slot_base + geo.ncells, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                      st));
         CNN_CUDA(ctx, cudaStreamSynchronize(st));
+        const int64_t nitems = hcounts[0];
+        // one pass into slots when they take at most 4 GiB, else count + fill
+        use_slots = hcounts[1] <= (int64_t(1) << 30);
+        if (use_slots) {
+            CNN_TRY(ctx->ensure(ctx->grid_slot_cols, sizeof(int32_t) * (size_t)(hcounts[1] > 0 ? hcounts[1] : 1)));
+            CNN_TRY(ctx->ensure(ctx->grid_qslot, sizeof(int64_t) * (size_t)n));
+        }
         CNN_TRY(ctx->ensure(ctx->io_c, sizeof(int2) * (size_t)(nitems > 0 ? nitems : 1)));
         item_fill_kernel<<<std::min<unsigned>(grid_for(geo.ncells, 256), 152u * 16u), 256, 0, st>>>(
             ctx->cell_start.as<int64_t>(), geo.ncells, ctx->io_b.as<int64_t>(), ctx->io_c.as<int2>());
@@ -868,10 +945,16 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
 
         stage_begin(ctx, 2);
         CNN_CUDA(ctx, cudaMemsetAsync(deg, 0, sizeof(int32_t) * (size_t)n, st));
-        if (nitems > 0) {
-            grid_search_kernel<false><<<(unsigned)nitems, kGridWarps * 32, 0, st>>>(
+        if (nitems > 0 && use_slots) {
+            grid_search_kernel<kSlots><<<(unsigned)nitems, kGridWarps * 32, 0, st>>>(
                 ctx->io_c.as<int2>(), ctx->x, d, geo, sp, ctx->perm.as<int32_t>(), ctx->cell_start.as<int64_t>(),
-                ctx->xf4.as<float4>(), deg, nullptr, nullptr, counters);
+                ctx->xf4.as<float4>(), deg, slot_base, ctx->grid_slot_cols.as<int32_t>(), counters,
+                ctx->grid_qslot.as<int64_t>());
+            CNN_LAUNCH_CHECK(ctx);
+        } else if (nitems > 0) {
+            grid_search_kernel<kCount><<<(unsigned)nitems, kGridWarps * 32, 0, st>>>(
+                ctx->io_c.as<int2>(), ctx->x, d, geo, sp, ctx->perm.as<int32_t>(), ctx->cell_start.as<int64_t>(),
+                ctx->xf4.as<float4>(), deg, nullptr, nullptr, counters, nullptr);
             CNN_LAUNCH_CHECK(ctx);
         }
         stage_end(ctx, 2);
@@ -913,10 +996,15 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
 
     stage_begin(ctx, 4);
     if (use_grid) {
-        if (grid_items > 0) {
-            grid_search_kernel<true><<<(unsigned)grid_items, kGridWarps * 32, 0, st>>>(
+        if (grid_items > 0 && use_slots) {
+            compact_rows_kernel<<<std::min<unsigned>(grid_for(n * 32, 256), 152u * 16u), 256, 0, st>>>(
+                n, ctx->grid_qslot.as<int64_t>(), ctx->grid_slot_cols.as<int32_t>(), row_off,
+                ctx->cols.as<int32_t>());
+            CNN_LAUNCH_CHECK(ctx);
+        } else if (grid_items > 0) {
+            grid_search_kernel<kFill><<<(unsigned)grid_items, kGridWarps * 32, 0, st>>>(
                 ctx->io_c.as<int2>(), ctx->x, d, geo, sp, ctx->perm.as<int32_t>(), ctx->cell_start.as<int64_t>(),
-                ctx->xf4.as<float4>(), deg, row_off, ctx->cols.as<int32_t>(), counters);
+                ctx->xf4.as<float4>(), deg, row_off, ctx->cols.as<int32_t>(), counters, nullptr);
             CNN_LAUNCH_CHECK(ctx);
         }
     } else {
