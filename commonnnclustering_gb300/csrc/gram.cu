@@ -753,40 +753,81 @@ __global__ void map_keys_kernel(uint64_t *__restrict__ keys, const unsigned long
 }
 
 // Band pairs in float64, reference order; hits appended to the key list
-// as packed (row << pack_bits | col).
-__global__ void gram_recheck_kernel(const double *__restrict__ x, int d, const uint64_t *__restrict__ amb,
-                                    const unsigned long long *__restrict__ namb, int64_t amb_cap, double rc,
-                                    int metric, int fpmode, uint64_t *__restrict__ keys,
-                                    unsigned long long *__restrict__ nkeys, int64_t key_cap,
-                                    const float *__restrict__ amb_d2, unsigned *__restrict__ max_err_bits,
-                                    int pack_bits) {
+// as packed (row << pack_bits | col).  One thread per pair keeps the
+// sequential sum of the reference; each warp stages its 32 pairs' rows in
+// shared memory kRecheckDims coordinates at a time, so the global loads are
+// 64-byte runs instead of 32 scattered words per instruction.  Keys and the
+// largest error are reserved / reduced once per warp.
+constexpr int kRecheckWarps = 8;
+constexpr int kRecheckDims = 8;
+
+__global__ void __launch_bounds__(kRecheckWarps * 32) gram_recheck_kernel(
+    const double *__restrict__ x, int d, const uint64_t *__restrict__ amb, const unsigned long long *__restrict__ namb,
+    int64_t amb_cap, double rc, int metric, int fpmode, uint64_t *__restrict__ keys,
+    unsigned long long *__restrict__ nkeys, int64_t key_cap, const float *__restrict__ amb_d2,
+    unsigned *__restrict__ max_err_bits, int pack_bits) {
+    __shared__ double s_a[kRecheckWarps][32][kRecheckDims + 1];
+    __shared__ double s_b[kRecheckWarps][32][kRecheckDims + 1];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
     const int64_t total = min((int64_t)*namb, amb_cap);
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-        const uint64_t a = amb[e];
+    float max_err = 0.f;
+    for (int64_t base = ((int64_t)blockIdx.x * kRecheckWarps + w) * 32; base < total;
+         base += (int64_t)gridDim.x * kRecheckWarps * 32) {
+        const int64_t e = base + lane;
+        const bool valid = e < total;
+        const uint64_t a = valid ? amb[e] : 0ull;
         const bool both = (a >> 63) & 1ull;
         const int64_t i = (int64_t)((a >> 32) & 0x7fffffffull), j = (int64_t)(a & 0xffffffffull);
         double s = 0.0;
-        const double *xa = x + i * d, *xb = x + j * d;
-        if (fpmode == CNN_FP_FUSED) {
-            for (int k = 0; k < d; ++k) {
-                const double t = __dsub_rn(xa[k], xb[k]);
-                s = __fma_rn(t, t, s);
+        for (int k0 = 0; k0 < d; k0 += kRecheckDims) {
+            // element m*32 + lane of the warp's 32 x kRecheckDims block: row r, coordinate c
+#pragma unroll
+            for (int m = 0; m < kRecheckDims; ++m) {
+                const int idx = m * 32 + lane;
+                const int r = idx / kRecheckDims, c = idx % kRecheckDims;
+                const int64_t ri = __shfl_sync(0xffffffffu, i, r), rj = __shfl_sync(0xffffffffu, j, r);
+                const bool rv = __shfl_sync(0xffffffffu, valid, r);
+                const int k = k0 + c;
+                s_a[w][r][c] = rv && k < d ? x[ri * d + k] : 0.0;
+                s_b[w][r][c] = rv && k < d ? x[rj * d + k] : 0.0;
             }
-        } else {
-            for (int k = 0; k < d; ++k) {
-                const double t = __dsub_rn(xa[k], xb[k]);
-                s = __dadd_rn(s, __dmul_rn(t, t));
+            __syncwarp();
+            const int kn = min(kRecheckDims, d - k0);
+            if (fpmode == CNN_FP_FUSED) {
+                for (int c = 0; c < kn; ++c) {
+                    const double t = __dsub_rn(s_a[w][lane][c], s_b[w][lane][c]);
+                    s = __fma_rn(t, t, s);
+                }
+            } else {
+                for (int c = 0; c < kn; ++c) {
+                    const double t = __dsub_rn(s_a[w][lane][c], s_b[w][lane][c]);
+                    s = __dadd_rn(s, __dmul_rn(t, t));
+                }
             }
+            __syncwarp();
         }
         const double sv = metric == CNN_METRIC_EUCLIDEAN ? __dsqrt_rn(s) : s;
-        if (sv <= rc) {
-            const unsigned long long w = atomicAdd(nkeys, both ? 2ull : 1ull);
-            if (w < (unsigned long long)key_cap) keys[w] = ((uint64_t)i << pack_bits) | (uint64_t)j;
-            if (both && w + 1 < (unsigned long long)key_cap) keys[w + 1] = ((uint64_t)j << pack_bits) | (uint64_t)i;
+        const bool hit = valid && sv <= rc;
+        const int mine = hit ? (both ? 2 : 1) : 0;
+        int inc = mine;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += u;
         }
-        const float err = fabsf((float)(s - (double)amb_d2[e]));
-        atomicMax(max_err_bits, __float_as_uint(err));
+        unsigned long long wbase = 0;
+        if (lane == 31 && inc) wbase = atomicAdd(nkeys, (unsigned long long)inc);
+        unsigned long long wpos = __shfl_sync(0xffffffffu, wbase, 31) + (unsigned long long)(inc - mine);
+        if (hit) {
+            if (wpos < (unsigned long long)key_cap) keys[wpos] = ((uint64_t)i << pack_bits) | (uint64_t)j;
+            if (both && wpos + 1 < (unsigned long long)key_cap)
+                keys[wpos + 1] = ((uint64_t)j << pack_bits) | (uint64_t)i;
+        }
+        if (valid) max_err = fmaxf(max_err, fabsf((float)(s - (double)amb_d2[e])));
+        (void)lt;
     }
+    for (int o = 16; o > 0; o >>= 1) max_err = fmaxf(max_err, __shfl_xor_sync(0xffffffffu, max_err, o));
+    if (lane == 0 && max_err > 0.f) atomicMax(max_err_bits, __float_as_uint(max_err));
 }
 
 // Sorted packed keys -> CSR: row starts at the key where the row changes
@@ -1034,7 +1075,7 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
         CNN_LAUNCH_CHECK(ctx);
         map_keys_kernel<<<152u * 8u, 256, 0, st>>>(a.amb, namb, amb_cap, perm, 0);
         CNN_LAUNCH_CHECK(ctx);
-        gram_recheck_kernel<<<std::min<unsigned>(grid_for(amb_cap, 256), 152u * 8u), 256, 0, st>>>(
+        gram_recheck_kernel<<<152u * 8u, kRecheckWarps * 32, 0, st>>>(
             ctx->x, d, a.amb, namb, amb_cap, radius_cutoff, metric, fpmode, a.keys, nkeys, key_cap, a.amb_d2,
             max_err_bits, bits_n);
         CNN_LAUNCH_CHECK(ctx);
