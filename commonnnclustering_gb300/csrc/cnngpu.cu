@@ -121,7 +121,7 @@ CNN_API cnn_status cnn_destroy(cnn_context *ctx) {
     cnn::DevBuf *bufs[] = {&ctx->x_own, &ctx->x_f32_stage, &ctx->perm, &ctx->inv, &ctx->deg, &ctx->row_off,
                            &ctx->cols, &ctx->xf4, &ctx->cell_of, &ctx->cell_start, &ctx->grid_slot_base,
                            &ctx->grid_slot_cols, &ctx->grid_qslot, &ctx->node, &ctx->parent,
-                           &ctx->comp_min, &ctx->flag, &ctx->counters, &ctx->stage_labels, &ctx->gram_hi,
+                           &ctx->comp_min, &ctx->flag, &ctx->counters, &ctx->stage_labels, &ctx->gram_hi, &ctx->gram_mid,
                            &ctx->gram_lo, &ctx->gram_aux, &ctx->gram_keys, &ctx->gram_amb,
                            &ctx->gram_blocks, &ctx->gram_tiles, &ctx->gram_perm, &ctx->pred_off, &ctx->pred_cols,
                            &ctx->pred_xoff, &ctx->pred_xcols, &ctx->pred_x, &ctx->pred_set,

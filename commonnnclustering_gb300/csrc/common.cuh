@@ -112,7 +112,7 @@ struct cnn_context {
     cnn::DevBuf sweep_bucket, sweep_row_off_max, sweep_cols_max, sweep_deg_max, sweep_consider, sweep_forest;
 
     // tensor-core (Gram) search for n_dim >= 16
-    cnn::DevBuf gram_hi, gram_lo, gram_aux, gram_keys, gram_amb, gram_blocks, gram_tiles, gram_perm;
+    cnn::DevBuf gram_hi, gram_mid, gram_lo, gram_aux, gram_keys, gram_amb, gram_blocks, gram_tiles, gram_perm;
 
     // prediction: this set's graph in point order, the other points' rows
     cnn::DevBuf pred_off, pred_cols, pred_xoff, pred_xcols, pred_x, pred_set;

@@ -3,20 +3,23 @@
 // Squared distances come from the Gram matrix: d2(i,j) = |x_i|^2 + |x_j|^2
 // - 2 x_i.x_j, on mean-centred coordinates.  x_i.x_j is computed on the 5th
 // generation tensor cores (tcgen05.mma, kind::f16) from a BF16 split of
-// every coordinate, x = hi + lo with hi = bf16(x), lo = bf16(x - hi):
-// x.y ~ hi.hi + hi.lo + lo.hi (three MMAs per 16-wide K slice), FP32
-// accumulation in tensor memory.  Per tile (128 x 128 pairs) a rigorous
+// every coordinate, x = hi + mid + lo with hi = bf16(x), mid = bf16(x - hi),
+// lo = bf16(x - hi - mid): x.y ~ hi.hi + (hi.mid + mid.hi + hi.lo + lo.hi +
+// mid.mid) (six MMAs per 16-wide K slice), FP32 accumulation in tensor
+// memory, hi.hi and the small cross terms in separate accumulators so that
+// the accumulation error scales with dp, not 6 dp.  Per tile (128 x 128 pairs) a rigorous
 // error bound gives a band around the cutoff: pairs below it are
 // neighbours, pairs above are not, pairs inside are recomputed in float64
 // with the reference's exact operation order (the only float64 step).
 //
 // Kernel structure (one persistent CTA per SM, 10 warps):
-//   warp 0  TMA producer: hi/lo tiles of the row block I and the column
+//   warp 0  TMA producer: hi/mid/lo tiles of the row block I and the column
 //           block J (cp.async.bulk.tensor, 128-byte swizzle) into a 2-stage
 //           shared-memory ring, completion counted on an mbarrier;
-//   warp 1  allocates 256 TMEM columns (two 128-column accumulators) and
-//           issues the MMAs from one thread; tcgen05.commit frees the
-//           shared stage and publishes the accumulator;
+//   warp 1  allocates 512 TMEM columns (two buffers, each a 128-column hi.hi
+//           accumulator and a 128-column cross-term accumulator) and issues
+//           the MMAs from one thread; tcgen05.commit frees the shared stage
+//           and publishes the accumulator;
 //   warps 2-9  epilogue, two per TMEM lane quadrant: each thread owns one
 //           tile row (its TMEM lane) and 64 of the columns, loads 32
 //           columns at a time with tcgen05.ld, compares, and appends hits /
@@ -42,9 +45,11 @@ constexpr int kTM = 128;              // tile rows (M) = tile columns (N)
 constexpr int kKB = 64;               // K block: 64 bf16 = 128 bytes per row
 constexpr int kStages = 2;
 constexpr int kTileBytes = kTM * kKB * 2;          // 16 KB: one operand tile
-constexpr int kStageBytes = 4 * kTileBytes;         // A_hi, A_lo, B_hi, B_lo
+constexpr int kSplits = 3;                          // x = hi + mid + lo (bf16 each)
+constexpr int kStageBytes = 2 * kSplits * kTileBytes;  // A_hi, A_mid, A_lo, B_hi, B_mid, B_lo: 96 KB
 constexpr int kGramThreads = 320;  // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
-constexpr uint32_t kTmemCols = 256;
+constexpr uint32_t kAccCols = 256;   // per accumulator buffer: hi.hi (128 columns), then the cross terms (128)
+constexpr uint32_t kTmemCols = 512;  // two buffers
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 
 struct GramArgs {
@@ -260,6 +265,7 @@ __device__ __forceinline__ void epilogue_emit_masks(const GramArgs &args, const 
 }
 
 __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __grid_constant__ CUtensorMap map_hi,
+                                                                      const __grid_constant__ CUtensorMap map_mid,
                                                                       const __grid_constant__ CUtensorMap map_lo,
                                                                       GramArgs args) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -321,9 +327,11 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
                     uint8_t *st = smem + s * kStageBytes;
                     mbar_expect_tx(&full_bar[s], kStageBytes);
                     tma_load_2d(st + 0 * kTileBytes, &map_hi, kb * kKB, I * kTM, &full_bar[s]);
-                    tma_load_2d(st + 1 * kTileBytes, &map_lo, kb * kKB, I * kTM, &full_bar[s]);
-                    tma_load_2d(st + 2 * kTileBytes, &map_hi, kb * kKB, J * kTM, &full_bar[s]);
-                    tma_load_2d(st + 3 * kTileBytes, &map_lo, kb * kKB, J * kTM, &full_bar[s]);
+                    tma_load_2d(st + 1 * kTileBytes, &map_mid, kb * kKB, I * kTM, &full_bar[s]);
+                    tma_load_2d(st + 2 * kTileBytes, &map_lo, kb * kKB, I * kTM, &full_bar[s]);
+                    tma_load_2d(st + 3 * kTileBytes, &map_hi, kb * kKB, J * kTM, &full_bar[s]);
+                    tma_load_2d(st + 4 * kTileBytes, &map_mid, kb * kKB, J * kTM, &full_bar[s]);
+                    tma_load_2d(st + 5 * kTileBytes, &map_lo, kb * kKB, J * kTM, &full_bar[s]);
                 }
             }
             if (!ok) {
@@ -345,7 +353,8 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
                 const uint32_t acc_ph = (uint32_t)((tl >> 1) & 1);
                 if (!mbar_wait(&acce_bar[b], acc_ph ^ 1u, abort_flag)) { ok = false; break; }
                 fence_after_sync();
-                const uint32_t d_tmem = tmem_base + (uint32_t)(b * kTM);
+                const uint32_t d_hh = tmem_base + (uint32_t)(b * kAccCols);  // hi.hi
+                const uint32_t d_x = d_hh + (uint32_t)kTM;                      // cross terms
                 for (int32_t kb = 0; kb < args.nkb; ++kb, ++it) {
                     const int s = (int)(it % kStages);
                     const uint32_t ph = (uint32_t)((it / kStages) & 1);
@@ -355,13 +364,19 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
 #pragma unroll
                     for (int kk = 0; kk < kKB / 16; ++kk) {
                         const uint32_t koff = (uint32_t)kk * 32u;  // 16 bf16 = 32 bytes along K
-                        const uint64_t a_hi = smem_desc(st + 0 * kTileBytes + koff);
-                        const uint64_t a_lo = smem_desc(st + 1 * kTileBytes + koff);
-                        const uint64_t b_hi = smem_desc(st + 2 * kTileBytes + koff);
-                        const uint64_t b_lo = smem_desc(st + 3 * kTileBytes + koff);
-                        umma(d_tmem, a_hi, b_hi, (kb > 0 || kk > 0) ? 1u : 0u);
-                        umma(d_tmem, a_hi, b_lo, 1u);
-                        umma(d_tmem, a_lo, b_hi, 1u);
+                        const uint64_t a_h = smem_desc(st + 0 * kTileBytes + koff);
+                        const uint64_t a_m = smem_desc(st + 1 * kTileBytes + koff);
+                        const uint64_t a_l = smem_desc(st + 2 * kTileBytes + koff);
+                        const uint64_t b_h = smem_desc(st + 3 * kTileBytes + koff);
+                        const uint64_t b_m = smem_desc(st + 4 * kTileBytes + koff);
+                        const uint64_t b_l = smem_desc(st + 5 * kTileBytes + koff);
+                        const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
+                        umma(d_hh, a_h, b_h, acc);
+                        umma(d_x, a_h, b_m, acc);
+                        umma(d_x, a_m, b_h, 1u);
+                        umma(d_x, a_h, b_l, 1u);
+                        umma(d_x, a_l, b_h, 1u);
+                        umma(d_x, a_m, b_m, 1u);
                     }
                     umma_commit(&empty_bar[s]);  // stage free once these MMAs are done
                 }
@@ -414,12 +429,16 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
             }
             __syncwarp();
             const uint32_t taddr =
-                tmem_base + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * kTM + half * 64);
+                tmem_base + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * kAccCols + half * 64);
 #pragma unroll 1
             for (int c = 0; c < 2; ++c) {
-                uint32_t v[32];
-                tmem_ld32_async(taddr + (uint32_t)(c * 32), v);
+                uint32_t v[32], vx[32];
+                tmem_ld32_async(taddr + (uint32_t)(c * 32), v);         // hi.hi
+                tmem_ld32_async(taddr + (uint32_t)(kTM + c * 32), vx);  // cross terms
                 tmem_wait_ld(v);
+                tmem_wait_ld(vx);
+#pragma unroll
+                for (int jj = 0; jj < 32; ++jj) v[jj] = __float_as_uint(__uint_as_float(v[jj]) + __uint_as_float(vx[jj]));
                 uint32_t in_mask = 0, amb_mask = 0;
 #pragma unroll
                 for (int jj = 0; jj < 32; ++jj) {
@@ -482,26 +501,30 @@ __global__ void column_mean_kernel(double *__restrict__ sum, int d, int64_t n) {
 // ordered int bits).  All coordinates are finite here.
 __global__ void gram_prep_kernel(const double *__restrict__ x, int64_t n_rows, int64_t n, int d, int dp,
                                  const double *__restrict__ mean, const int32_t *__restrict__ perm,
-                                 __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ lo,
-                                 float *__restrict__ norm2, unsigned *__restrict__ blk_norm_bits,
-                                 unsigned *__restrict__ blk_norm2_bits) {
+                                 __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ mid,
+                                 __nv_bfloat16 *__restrict__ lo, float *__restrict__ norm2,
+                                 unsigned *__restrict__ blk_norm_bits, unsigned *__restrict__ blk_norm2_bits) {
     const int lane = threadIdx.x & 31;
     const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (i >= n_rows) return;
     const int64_t src = perm[i];
     double s2 = 0;
     for (int k = lane; k < dp; k += 32) {
-        float h = 0.f, l = 0.f;
+        __nv_bfloat16 bh = __float2bfloat16_rn(0.f), bm = bh, bl = bh;
         if (k < d && src >= 0) {
+            // residuals in float64 are exact (Sterbenz): c - hi - mid - lo is the
+            // rounding of the last bf16 step, at most ~2^-24 |c|
             const double c = x[src * d + k] - mean[k];
-            const float cf = (float)c;
-            const __nv_bfloat16 hb = __float2bfloat16_rn(cf);
-            h = __bfloat162float(hb);
-            l = __bfloat162float(__float2bfloat16_rn((float)(c - (double)h)));
+            bh = __float2bfloat16_rn((float)c);
+            const double r1 = c - (double)__bfloat162float(bh);
+            bm = __float2bfloat16_rn((float)r1);
+            const double r2 = r1 - (double)__bfloat162float(bm);
+            bl = __float2bfloat16_rn((float)r2);
             s2 += c * c;
         }
-        hi[i * dp + k] = __float2bfloat16_rn(h);
-        lo[i * dp + k] = __float2bfloat16_rn(l);
+        hi[i * dp + k] = bh;
+        mid[i * dp + k] = bm;
+        lo[i * dp + k] = bl;
     }
     for (int o = 16; o > 0; o >>= 1) s2 += __shfl_down_sync(0xffffffffu, s2, o);
     if (lane == 0) {
@@ -882,12 +905,20 @@ bool make_map(CUtensorMap *map, void *base, int64_t rows, int dp) {
 
 }  // namespace
 
-// Error bound on |acc - x'.y'| relative to |x'||y'|: the split leaves at most
-// 2^-16 |x_k| per coordinate and drops lo.lo (<= 2^-16 |x_k||y_k|): about
-// 3.1 * 2^-16 overall; FP32 accumulation of 3*dp exact products adds at most
-// (3 dp + 8) 2^-23.  d2 uses 2*acc, so the band coefficient doubles both.
-// Taken with a safety factor of 2.
-double gram_band_coef(int dp) { return 2.0 * 2.0 * (3.2 * ldexp(1.0, -16) + (3.0 * dp + 8.0) * ldexp(1.0, -23)); }
+// Error bound on |acc - x'.y'| relative to |x'||y'| (Cauchy-Schwarz on the
+// per-coordinate bounds): the three-way split leaves at most ~2^-24 |x_k| per
+// coordinate, and the dropped mid.lo, lo.mid, lo.lo are at most ~2^-24
+// |x_k||y_k| together with those residuals: 6 * 2^-24 overall.  FP32
+// accumulation of the dp exact hi.hi products adds (dp + 8) 2^-23; the
+// cross-term accumulator (5 dp products, each below 2^-7 |x_k||y_k|) adds
+// (5 dp + 8) 2^-29, and summing the two accumulators 2 * 2^-24.  d2 uses
+// 2 * acc, so the band coefficient doubles the total; taken with a safety
+// factor of 2.
+double gram_band_coef(int dp) {
+    const double rel = 6.0 * ldexp(1.0, -24) + (dp + 8.0) * ldexp(1.0, -23) + (5.0 * dp + 8.0) * ldexp(1.0, -29) +
+                       2.0 * ldexp(1.0, -24);
+    return 2.0 * 2.0 * rel;
+}
 
 cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode, bool *used) {
     *used = false;
@@ -984,16 +1015,16 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
 
     // hi, lo (bf16 n_rows x dp), norm2 (n_rows), block norms
     CNN_TRY(ctx->ensure(ctx->gram_hi, sizeof(__nv_bfloat16) * (size_t)n_rows * dp));
+    CNN_TRY(ctx->ensure(ctx->gram_mid, sizeof(__nv_bfloat16) * (size_t)n_rows * dp));
     CNN_TRY(ctx->ensure(ctx->gram_lo, sizeof(__nv_bfloat16) * (size_t)n_rows * dp));
     CNN_TRY(ctx->ensure(ctx->gram_aux, sizeof(float) * (size_t)(n_rows + 2 * nblk + 64)));
     float *norm2 = ctx->gram_aux.as<float>();
     unsigned *blk_norm_bits = reinterpret_cast<unsigned *>(norm2 + n_rows);
     unsigned *blk_norm2_bits = blk_norm_bits + nblk;
     CNN_CUDA(ctx, cudaMemsetAsync(blk_norm_bits, 0, sizeof(unsigned) * 2 * (size_t)nblk, st));
-    gram_prep_kernel<<<grid_for(n_rows * 32, 256), 256, 0, st>>>(ctx->x, n_rows, n, d, dp, colsum, perm,
-                                                                 ctx->gram_hi.as<__nv_bfloat16>(),
-                                                                 ctx->gram_lo.as<__nv_bfloat16>(), norm2,
-                                                                 blk_norm_bits, blk_norm2_bits);
+    gram_prep_kernel<<<grid_for(n_rows * 32, 256), 256, 0, st>>>(
+        ctx->x, n_rows, n, d, dp, colsum, perm, ctx->gram_hi.as<__nv_bfloat16>(), ctx->gram_mid.as<__nv_bfloat16>(),
+        ctx->gram_lo.as<__nv_bfloat16>(), norm2, blk_norm_bits, blk_norm2_bits);
     CNN_LAUNCH_CHECK(ctx);
 
     // the list of block pairs (I, J >= I) that can hold a pair within R
@@ -1026,8 +1057,9 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
                                                             ctx->gram_tiles.as<int2>());
     CNN_LAUNCH_CHECK(ctx);
 
-    CUtensorMap map_hi, map_lo;
-    if (!make_map(&map_hi, ctx->gram_hi.ptr, n_rows, dp) || !make_map(&map_lo, ctx->gram_lo.ptr, n_rows, dp))
+    CUtensorMap map_hi, map_mid, map_lo;
+    if (!make_map(&map_hi, ctx->gram_hi.ptr, n_rows, dp) || !make_map(&map_mid, ctx->gram_mid.ptr, n_rows, dp) ||
+        !make_map(&map_lo, ctx->gram_lo.ptr, n_rows, dp))
         return CNN_OK;
 
     const double coef = gram_band_coef(dp);
@@ -1040,7 +1072,7 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     a.rc2 = (float)rc2;
     a.coef = (float)coef;
     a.slack_coef = (float)(8.0 * ldexp(1.0, -24));  // float32 rounding of |x|^2, |y|^2 and the fma
-    a.min_band = (float)(1e-3 * rc2);
+    a.min_band = (float)(1e-6 * rc2);  // float32 rounding of rc2 and of rc2 -/+ band
     a.norm2 = norm2;
     a.blk_norm = reinterpret_cast<const float *>(blk_norm_bits);
     a.blk_norm2 = reinterpret_cast<const float *>(blk_norm2_bits);
@@ -1067,7 +1099,7 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
         CNN_CUDA(ctx, cudaMemsetAsync(counters + 10, 0, 3 * sizeof(unsigned long long), st));
         CNN_CUDA(ctx, cudaMemsetAsync(max_err_bits, 0, sizeof(unsigned), st));
         stage_begin(ctx, 9);
-        gram_search_kernel<<<grid, kGramThreads, smem, st>>>(map_hi, map_lo, a);
+        gram_search_kernel<<<grid, kGramThreads, smem, st>>>(map_hi, map_mid, map_lo, a);
         CNN_LAUNCH_CHECK(ctx);
         stage_end(ctx, 9);
         // internal indices -> point indices (before the recheck appends more keys)
