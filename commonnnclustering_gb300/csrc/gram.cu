@@ -984,7 +984,7 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
         else CNN_TRY(launch_assign(pivot_assign_kernel<32>));
         int pb = 1;
         while ((1 << pb) < n_groups) ++pb;
-        CNN_TRY(radix_sort_u64(ctx, pkeys, n, bits_n + pb));
+        CNN_TRY(radix_sort_u64(ctx, pkeys, n, bits_n + pb, bits_n));  // built in point order
         CNN_CUDA(ctx, cudaMemsetAsync(gcount, 0, sizeof(int32_t) * n_groups, st));
         group_count_kernel<<<std::min<unsigned>(grid_for(n, 256), 152u * 2u), 256, sizeof(int32_t) * n_groups, st>>>(
             pkeys, n, bits_n, n_groups, gcount);

@@ -251,12 +251,49 @@ cnn_status scan_exclusive_i32_to_i64(cnn_context *ctx, const int32_t *in, int64_
     return scan_impl<int32_t>(ctx, in, out, n, 0);
 }
 
-// Sorts keys[0..n) ascending by their low `bits` bits (higher bits must be
-// zero).  Uses scratch_c/scratch_d and the scan temp.
-cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits) {
+// Up to kSmallSort keys: one block, bitonic sort in shared memory.
+constexpr int kSmallSort = 4096;
+
+__global__ void __launch_bounds__(1024) small_sort_kernel(uint64_t *__restrict__ keys, int n) {
+    __shared__ uint64_t s[kSmallSort];
+    int m = 1;
+    while (m < n) m <<= 1;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) s[i] = i < n ? keys[i] : ~0ull;
+    __syncthreads();
+    for (int k = 2; k <= m; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                const int p = i ^ j;
+                if (p > i) {
+                    const uint64_t a = s[i], b = s[p];
+                    const bool up = (i & k) == 0;
+                    if ((a > b) == up) {
+                        s[i] = b;
+                        s[p] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) keys[i] = s[i];
+}
+
+// Sorts keys[0..n) ascending by their bits [first_bit, bits) (higher bits
+// must be zero; bits below first_bit must already be in ascending order
+// within equal higher bits, which the stable passes keep -- e.g. an index
+// in the low bits of keys built in index order).  Uses scratch_c/scratch_d
+// and the scan temp.
+cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits, int first_bit) {
     if (n <= 1) return CNN_OK;
     if (bits < 1) bits = 1;
     if (bits > 64) bits = 64;
+    if (n <= kSmallSort) {  // every key distinct or not, a full sort gives the same order
+        small_sort_kernel<<<1, 1024, 0, ctx->stream>>>(keys, (int)n);
+        CNN_LAUNCH_CHECK(ctx);
+        return CNN_OK;
+    }
+    first_bit = first_bit < 0 ? 0 : (first_bit / 8) * 8;
     const int64_t ntiles = (n + kRadixTile - 1) / kRadixTile;
     const int64_t nh = 256 * ntiles;
     CNN_TRY(ctx->ensure(ctx->scratch_c, sizeof(uint64_t) * (size_t)n));
@@ -266,9 +303,9 @@ cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits)
     int64_t *goff = reinterpret_cast<int64_t *>(
         (reinterpret_cast<uintptr_t>(hist + nh) + 15) & ~uintptr_t(15));
     uint64_t *a = keys, *b = ctx->scratch_c.as<uint64_t>();
-    int passes = (bits + 7) / 8;
+    const int passes = (bits - first_bit + 7) / 8;
     for (int p = 0; p < passes; ++p) {
-        int shift = p * 8;
+        const int shift = first_bit + p * 8;
         radix_hist_kernel<<<(unsigned)ntiles, kRadixThreads, 0, ctx->stream>>>(a, n, shift, ntiles, hist);
         CNN_LAUNCH_CHECK(ctx);
         CNN_TRY(scan_impl<int32_t>(ctx, hist, goff, nh, 0));

@@ -901,7 +901,8 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         uint64_t *keys = ctx->scratch_a.as<uint64_t>();
         cell_key_kernel<<<gb, 256, 0, st>>>(ctx->cell_of.as<int32_t>(), n, bits_n, keys);
         CNN_LAUNCH_CHECK(ctx);
-        CNN_TRY(radix_sort_u64(ctx, keys, n, bits_n + bits_for(geo.ncells + 2)));
+        // keys are built in point order: sorting the cell bits alone keeps points ascending within a cell
+        CNN_TRY(radix_sort_u64(ctx, keys, n, bits_n + bits_for(geo.ncells + 2), bits_n));
         perm_gather_kernel<<<gb, 256, 0, st>>>(keys, n, bits_n, ctx->x, d, geo, ctx->perm.as<int32_t>(),
                                                 ctx->inv.as<int32_t>(), ctx->xf4.as<float4>());
         CNN_LAUNCH_CHECK(ctx);
