@@ -339,7 +339,20 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     stage_begin(ctx, 6);
     // hook: every node checks its first two candidate edges; compress; then
     // the full pass, where edges inside already joined sets cost one load
-    const unsigned check_blocks = std::min<unsigned>(grid_for(n, kCheckWarps), 152u * 8u);
+    // persistent warps: exactly the blocks that are resident at once, so
+    // that no block (and the nodes it strides over) waits for a second wave
+    auto resident = [&](const void *kernel, int threads) -> unsigned {
+        int per_sm = 0, sms = 0, dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            (void)cudaGetLastError();
+            per_sm = 8;
+            sms = 152;
+        }
+        return std::min<unsigned>(grid_for(n, kCheckWarps), (unsigned)std::max(1, per_sm * sms));
+    };
+    const unsigned check_blocks = resident((const void *)check_union_kernel, kCheckWarps * 32);
     check_union_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(
         n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff, kHookEdges,
         counters, seed_a, seed_b);
@@ -351,10 +364,10 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     CNN_TRY(ctx->ensure(ctx->io_c, sizeof(int2) * (size_t)wl_cap));
     unsigned long long *wl_count = counters + 8;
     CNN_CUDA(ctx, cudaMemsetAsync(wl_count, 0, sizeof(unsigned long long), st));
-    cross_filter_kernel<<<check_blocks, 256, 0, st>>>(n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent,
+    cross_filter_kernel<<<resident((const void *)cross_filter_kernel, 256), 256, 0, st>>>(n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent,
                                                       ctx->io_c.as<int2>(), wl_count, wl_cap);
     CNN_LAUNCH_CHECK(ctx);
-    edge_check_kernel<<<check_blocks, 256, 0, st>>>(ctx->io_c.as<int2>(), wl_count, wl_cap, ctx->row_off.as<int64_t>(),
+    edge_check_kernel<<<resident((const void *)edge_check_kernel, 256), 256, 0, st>>>(ctx->io_c.as<int2>(), wl_count, wl_cap, ctx->row_off.as<int64_t>(),
                                                     ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff,
                                                     counters);
     CNN_LAUNCH_CHECK(ctx);
