@@ -110,6 +110,7 @@ struct cnn_context {
     // batched (radius, cut) sweep: the largest-radius graph kept aside,
     // per-pair radius buckets, consider flags of the per-fit runs
     cnn::DevBuf sweep_bucket, sweep_row_off_max, sweep_cols_max, sweep_deg_max, sweep_consider, sweep_forest;
+    cnn::DevBuf sweep_open_a, sweep_open_b, sweep_open_count;  // open pairs of the last fit, two lists
 
     // tensor-core (Gram) search for n_dim >= 16
     cnn::DevBuf gram_hi, gram_mid, gram_lo, gram_aux, gram_keys, gram_amb, gram_blocks, gram_tiles, gram_perm;
@@ -208,7 +209,12 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
 // fit on the same graph order whose components refine this fit's (-1: none)
 cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
                     int64_t current_start, uint8_t *consider_dev, int64_t *labels_dev,
-                    const int32_t *seed_a = nullptr, const int32_t *seed_b = nullptr);
+                    const int32_t *seed_a = nullptr, const int32_t *seed_b = nullptr,
+                    const int2 *edge_list = nullptr, const unsigned long long *edge_count = nullptr);
+// edge_list (device, count on the device): the pairs (a, b > a) that can
+// still cross -- those a finished fit refining this one left open
+cnn_status open_pairs_impl(cnn_context *ctx, const int2 *in_list, const unsigned long long *in_count, int2 *out,
+                           unsigned long long *out_count, int64_t cap);
 cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels_dev, int64_t n,
                              int64_t member_cutoff, int64_t max_clusters);
 cnn_status check_lists_impl(cnn_context *ctx, const int32_t *a, int64_t na, const int32_t *b,
@@ -216,7 +222,8 @@ cnn_status check_lists_impl(cnn_context *ctx, const int32_t *a, int64_t na, cons
 // a fresh fit (labels 0, consider 1, current_start 1) and sort_by_size into labels_dev
 cnn_status fit_and_sort_into(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
                              int64_t sort_member_cutoff, int64_t max_clusters, int64_t *labels_dev,
-                             const int32_t *seed_a = nullptr, const int32_t *seed_b = nullptr, bool sort = true);
+                             const int32_t *seed_a = nullptr, const int32_t *seed_b = nullptr, bool sort = true,
+                             const int2 *edge_list = nullptr, const unsigned long long *edge_count = nullptr);
 
 // sweep.cu
 cnn_status sweep_impl(cnn_context *ctx, const double *radius_cutoffs, int32_t n_radii,

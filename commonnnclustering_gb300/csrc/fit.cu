@@ -82,6 +82,99 @@ __global__ void __launch_bounds__(256) cross_filter_kernel(int64_t n, const int6
     }
 }
 
+// The cross filter over an edge list (a, b > a) instead of the graph; the
+// list's length is read on the device.
+__global__ void __launch_bounds__(256) cross_filter_list_kernel(const int2 *__restrict__ edges,
+                                                                const unsigned long long *__restrict__ count,
+                                                                const int32_t *__restrict__ parent,
+                                                                int2 *__restrict__ wl,
+                                                                unsigned long long *__restrict__ wl_count,
+                                                                int64_t cap) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t total = (int64_t)*count;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
+        const int64_t e = base + lane;
+        int2 ed = make_int2(-1, -1);
+        bool cross = false;
+        if (e < total) {
+            ed = edges[e];
+            const int32_t pa = parent[ed.x], pb = parent[ed.y];
+            cross = pa >= 0 && pb >= 0 && pa != pb;
+        }
+        const unsigned mask = __ballot_sync(0xffffffffu, cross);
+        if (!mask) continue;
+        unsigned long long w = 0;
+        if (lane == 0) w = atomicAdd(wl_count, (unsigned long long)__popc(mask));
+        w = __shfl_sync(0xffffffffu, w, 0) + __popc(mask & lt);
+        if (cross && w < (unsigned long long)cap) wl[w] = ed;
+    }
+}
+
+// Pairs (a, b > a) a finished fit leaves open for a fit it refines: all
+// but those whose points are nodes with the same root (parent holds roots).
+__device__ __forceinline__ bool pair_open(const uint8_t *__restrict__ node, const int32_t *__restrict__ parent,
+                                          int32_t a, int32_t b) {
+    return !(node[a] && node[b] && parent[a] == parent[b]);
+}
+
+__global__ void __launch_bounds__(256) open_pairs_csr_kernel(int64_t n, const int64_t *__restrict__ row_off,
+                                                             const int32_t *__restrict__ cols,
+                                                             const uint8_t *__restrict__ node,
+                                                             const int32_t *__restrict__ parent,
+                                                             int2 *__restrict__ out,
+                                                             unsigned long long *__restrict__ out_count,
+                                                             int64_t cap) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t a64 = warp0; a64 < n; a64 += nwarps) {
+        const int32_t a = (int32_t)a64;
+        const int64_t s = row_off[a], e = row_off[a + 1];
+        for (int64_t k0 = warp_upper_bound(cols, s, e, a, lane); k0 < e; k0 += 32) {
+            const int64_t k = k0 + lane;
+            const int32_t b = k < e ? cols[k] : -1;
+            const bool keep = b > a && pair_open(node, parent, a, b);
+            const unsigned mask = __ballot_sync(0xffffffffu, keep);
+            if (!mask) continue;
+            unsigned long long w = 0;
+            if (lane == 0) w = atomicAdd(out_count, (unsigned long long)__popc(mask));
+            w = __shfl_sync(0xffffffffu, w, 0) + __popc(mask & lt);
+            if (keep && w < (unsigned long long)cap) out[w] = make_int2(a, b);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) open_pairs_list_kernel(const int2 *__restrict__ edges,
+                                                              const unsigned long long *__restrict__ count,
+                                                              const uint8_t *__restrict__ node,
+                                                              const int32_t *__restrict__ parent,
+                                                              int2 *__restrict__ out,
+                                                              unsigned long long *__restrict__ out_count,
+                                                              int64_t cap) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t total = (int64_t)*count;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
+        const int64_t e = base + lane;
+        int2 ed = make_int2(-1, -1);
+        bool keep = false;
+        if (e < total) {
+            ed = edges[e];
+            keep = pair_open(node, parent, ed.x, ed.y);
+        }
+        const unsigned mask = __ballot_sync(0xffffffffu, keep);
+        if (!mask) continue;
+        unsigned long long w = 0;
+        if (lane == 0) w = atomicAdd(out_count, (unsigned long long)__popc(mask));
+        w = __shfl_sync(0xffffffffu, w, 0) + __popc(mask & lt);
+        if (keep && w < (unsigned long long)cap) out[w] = ed;
+    }
+}
+
 __global__ void __launch_bounds__(256) edge_check_kernel(const int2 *__restrict__ wl,
                                                          const unsigned long long *__restrict__ wl_count,
                                                          int64_t cap, const int64_t *__restrict__ row_off,
@@ -306,7 +399,8 @@ __global__ void seed_union_kernel(int64_t n, const uint8_t *__restrict__ node, i
 }
 
 cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff, int64_t current_start,
-                    uint8_t *consider_dev, int64_t *labels_dev, const int32_t *seed_a, const int32_t *seed_b) {
+                    uint8_t *consider_dev, int64_t *labels_dev, const int32_t *seed_a, const int32_t *seed_b,
+                    const int2 *edge_list, const unsigned long long *edge_count) {
     if (!ctx->have_graph) return ctx->fail(CNN_ERR_STATE, "no neighbour graph: call cnn_build_neighbours first");
     const int64_t n = ctx->n;
     cudaStream_t st = ctx->stream;
@@ -337,8 +431,6 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     stage_end(ctx, 5);
 
     stage_begin(ctx, 6);
-    // hook: every node checks its first two candidate edges; compress; then
-    // the full pass, where edges inside already joined sets cost one load
     // persistent warps: exactly the blocks that are resident at once, so
     // that no block (and the nodes it strides over) waits for a second wave
     auto resident = [&](const void *kernel, int threads) -> unsigned {
@@ -353,6 +445,8 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
         return std::min<unsigned>(grid_for(n, kCheckWarps), (unsigned)std::max(1, per_sm * sms));
     };
     const unsigned check_blocks = resident((const void *)check_union_kernel, kCheckWarps * 32);
+    // hook: every node checks its first two candidate edges; compress; then
+    // the cross-root pairs only, where pairs inside joined sets cost one load
     check_union_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(
         n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff, kHookEdges,
         counters, seed_a, seed_b);
@@ -364,12 +458,18 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     CNN_TRY(ctx->ensure(ctx->io_c, sizeof(int2) * (size_t)wl_cap));
     unsigned long long *wl_count = counters + 8;
     CNN_CUDA(ctx, cudaMemsetAsync(wl_count, 0, sizeof(unsigned long long), st));
-    cross_filter_kernel<<<resident((const void *)cross_filter_kernel, 256), 256, 0, st>>>(n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent,
-                                                      ctx->io_c.as<int2>(), wl_count, wl_cap);
+    if (edge_list) {
+        // only pairs a finished fit that refines this one left open can cross
+        cross_filter_list_kernel<<<152u * 16u, 256, 0, st>>>(edge_list, edge_count, parent, ctx->io_c.as<int2>(),
+                                                             wl_count, wl_cap);
+    } else {
+        cross_filter_kernel<<<resident((const void *)cross_filter_kernel, 256), 256, 0, st>>>(
+            n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, ctx->io_c.as<int2>(), wl_count, wl_cap);
+    }
     CNN_LAUNCH_CHECK(ctx);
-    edge_check_kernel<<<resident((const void *)edge_check_kernel, 256), 256, 0, st>>>(ctx->io_c.as<int2>(), wl_count, wl_cap, ctx->row_off.as<int64_t>(),
-                                                    ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff,
-                                                    counters);
+    edge_check_kernel<<<resident((const void *)edge_check_kernel, 256), 256, 0, st>>>(
+        ctx->io_c.as<int2>(), wl_count, wl_cap, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent,
+        (int32_t)similarity_cutoff, counters);
     CNN_LAUNCH_CHECK(ctx);
     check_union_if_overflow_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(
         n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff, wl_count, wl_cap,
@@ -498,7 +598,8 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64
 // current_start 1, the fit, then sort_by_size.
 cnn_status fit_and_sort_into(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
                              int64_t sort_member_cutoff, int64_t max_clusters, int64_t *labels_dev,
-                             const int32_t *seed_a, const int32_t *seed_b, bool sort) {
+                             const int32_t *seed_a, const int32_t *seed_b, bool sort, const int2 *edge_list,
+                             const unsigned long long *edge_count) {
     const int64_t n = ctx->n;
     cudaStream_t st = ctx->stream;
     if (n == 0) return CNN_OK;
@@ -506,8 +607,28 @@ cnn_status fit_and_sort_into(cnn_context *ctx, int64_t similarity_cutoff, int64_
     CNN_CUDA(ctx, cudaMemsetAsync(labels_dev, 0, sizeof(int64_t) * (size_t)n, st));
     CNN_CUDA(ctx, cudaMemsetAsync(ctx->sweep_consider.ptr, 1, (size_t)n, st));
     CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, 1, ctx->sweep_consider.as<uint8_t>(), labels_dev,
-                     seed_a, seed_b));
+                     seed_a, seed_b, edge_list, edge_count));
     return sort ? sort_by_size_impl(ctx, labels_dev, n, sort_member_cutoff, max_clusters) : CNN_OK;
+}
+
+// The pairs the last fit left open, from the graph (in_list null) or from
+// the list that fit used; out_count is a device counter.
+cnn_status open_pairs_impl(cnn_context *ctx, const int2 *in_list, const unsigned long long *in_count, int2 *out,
+                           unsigned long long *out_count, int64_t cap) {
+    cudaStream_t st = ctx->stream;
+    const int64_t n = ctx->n;
+    CNN_CUDA(ctx, cudaMemsetAsync(out_count, 0, sizeof(unsigned long long), st));
+    if (n == 0) return CNN_OK;
+    if (in_list) {
+        open_pairs_list_kernel<<<152u * 16u, 256, 0, st>>>(in_list, in_count, ctx->node.as<uint8_t>(),
+                                                            ctx->parent.as<int32_t>(), out, out_count, cap);
+    } else {
+        open_pairs_csr_kernel<<<std::min<unsigned>(grid_for(n * 32, 256), 152u * 16u), 256, 0, st>>>(
+            n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), ctx->node.as<uint8_t>(),
+            ctx->parent.as<int32_t>(), out, out_count, cap);
+    }
+    CNN_LAUNCH_CHECK(ctx);
+    return CNN_OK;
 }
 
 cnn_status check_lists_impl(cnn_context *ctx, const int32_t *a, int64_t na, const int32_t *b, int64_t nb,

@@ -178,13 +178,35 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
     CNN_TRY(ctx->ensure(ctx->sweep_forest, sizeof(int32_t) * (size_t)n * (size_t)n_cuts + 256));
     int32_t *forest = ctx->sweep_forest.as<int32_t>();
     std::vector<char> have(n_cuts, 0);  // slot j: cut j at the last radius it ran at
+    // Within a radius the graph is fixed, so a fit only needs to look at the
+    // pairs the fit it starts from left open (not both in one component):
+    // the pairs inside its components are inside this fit's components too.
+    // Those open pairs are kept as a list (two alternating buffers) while
+    // fits follow each other at one radius.
     auto fit_cuts = [&](int32_t k, bool same_order_as_previous) -> cnn_status {
         if (!same_order_as_previous) std::fill(have.begin(), have.end(), 0);
+        std::vector<int> todo;
+        for (int t = 0; t < n_cuts; ++t)
+            if (slot(k, order[t]) >= 0) todo.push_back(order[t]);
+        const int64_t half = ctx->nnz / 2 + 1;
+        const bool lists = todo.size() > 1 && n > 0 && half * (int64_t)(2 * sizeof(int2)) <= (int64_t(24) << 30);
+        int2 *cur = nullptr, *nxt = nullptr;
+        unsigned long long *ccur = nullptr, *cnxt = nullptr;
+        if (lists) {
+            CNN_TRY(ctx->ensure(ctx->sweep_open_a, sizeof(int2) * (size_t)half));
+            CNN_TRY(ctx->ensure(ctx->sweep_open_b, sizeof(int2) * (size_t)half));
+            CNN_TRY(ctx->ensure(ctx->sweep_open_count, 2 * sizeof(unsigned long long)));
+            cur = ctx->sweep_open_a.as<int2>();
+            nxt = ctx->sweep_open_b.as<int2>();
+            ccur = ctx->sweep_open_count.as<unsigned long long>();
+            cnxt = ccur + 1;
+        }
         std::vector<int> done_here;
-        for (int t = 0; t < n_cuts; ++t) {
-            const int j = order[t];
+        int last = -1;            // the cut fitted last at this radius
+        bool list_valid = false;  // cur holds the pairs `last` left open
+        for (size_t t = 0; t < todo.size(); ++t) {
+            const int j = todo[t];
             const int64_t out = slot(k, j);
-            if (out < 0) continue;
             int best = -1;
             for (int i : done_here)
                 if (refines(i, j) && (best < 0 || sim_cut[i] < sim_cut[best] ||
@@ -192,14 +214,23 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
                     best = i;
             const int32_t *sa = have[j] && sim_cut[j] >= 0 ? forest + (size_t)j * n : nullptr;
             const int32_t *sb = best >= 0 ? forest + (size_t)best * n : nullptr;
+            const bool use_list = lists && list_valid && best == last;
             CNN_TRY(fit_and_sort_into(ctx, sim_cut[j], member_cut[j], sort_member_cutoff, max_clusters,
-                                      labels_dev + out * n, sa, sb, sort));
+                                      labels_dev + out * n, sa, sb, sort, use_list ? cur : nullptr,
+                                      use_list ? ccur : nullptr));
             // after the fit the union-find array holds every node's root (-1 elsewhere)
             if (n > 0)
                 CNN_CUDA(ctx, cudaMemcpyAsync(forest + (size_t)j * n, ctx->parent.ptr, sizeof(int32_t) * (size_t)n,
                                               cudaMemcpyDeviceToDevice, st));
+            if (lists && t + 1 < todo.size()) {
+                CNN_TRY(open_pairs_impl(ctx, use_list ? cur : nullptr, use_list ? ccur : nullptr, nxt, cnxt, half));
+                std::swap(cur, nxt);
+                std::swap(ccur, cnxt);
+                list_valid = true;
+            }
             have[j] = 1;
             done_here.push_back(j);
+            last = j;
         }
         return CNN_OK;
     };
