@@ -19,10 +19,13 @@
 //   2. one warp per node a walks its neighbours b > a.  An edge is checked
 //      only if find(a) != find(b) at that moment: edges inside an already
 //      joined set cannot change the components, so skipping them is exact.
-//      The check streams N(b) through the warp, each lane binary-searching
-//      one member in N(a) (held in shared memory), and stops as soon as the
-//      count reaches the cutoff or can no longer reach it.  Accepted edges
-//      are joined with a lock-free union-find (CAS on roots, path halving);
+//      The check merges N(a) and N(b) 32 entries at a time (each lane looks
+//      one member of N(b) up among 32 of N(a) by shuffles) and stops as soon
+//      as the count reaches the cutoff or can no longer reach it.  Accepted
+//      edges are joined with a lock-free union-find (CAS on roots, path
+//      halving).  A hook pass checks two edges per node; a read-only pass
+//      then lists the edges whose roots still differ and only those are
+//      checked;
 //   3. per component, the minimum point index; ranks of those minima give
 //      the labels (current_start + rank), written in point order.
 #include <climits>
@@ -175,7 +178,7 @@ __global__ void __launch_bounds__(256) open_pairs_list_kernel(const int2 *__rest
     }
 }
 
-__global__ void __launch_bounds__(256) edge_check_kernel(const int2 *__restrict__ wl,
+__global__ void __launch_bounds__(kCheckWarps * 32, CNN_CHECK_MIN_BLOCKS) edge_check_kernel(const int2 *__restrict__ wl,
                                                          const unsigned long long *__restrict__ wl_count,
                                                          int64_t cap, const int64_t *__restrict__ row_off,
                                                          const int32_t *__restrict__ cols,
@@ -357,6 +360,100 @@ __global__ void new_label_kernel(const uint64_t *__restrict__ keys, int64_t k, i
     }
 }
 
+// ---- sort_by_size for label ranges of up to kOrderSmall values -------------
+// One pass counts sizes and first occurrences per label value (lo..lo+r-1);
+// one block orders the clusters by (size descending, first occurrence
+// ascending) with a bitonic sort in shared memory and writes the new label
+// of every value; one pass applies it.
+constexpr int kOrderSmall = 4096;
+
+__global__ void init_count_first_kernel(int32_t *__restrict__ cnt, int32_t *__restrict__ first, int64_t r) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < r; i += (int64_t)gridDim.x * blockDim.x) {
+        cnt[i] = 0;
+        first[i] = INT32_MAX;
+    }
+}
+
+// Points in label order are often runs of one value: lanes with the same
+// value add their count with one atomic.
+__global__ void count_first_dense_kernel(const int64_t *__restrict__ labels, int64_t n, int64_t lo,
+                                         int32_t *__restrict__ cnt, int32_t *__restrict__ first) {
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+        const int64_t i = base + lane;
+        const int64_t v = i < n ? labels[i] : 0;
+        const int32_t id = v == 0 ? -1 : (int32_t)(v - lo);
+        const unsigned peers = __match_any_sync(0xffffffffu, id);
+        if (id >= 0 && lane == __ffs(peers) - 1) {
+            atomicAdd(&cnt[id], __popc(peers));
+            atomicMin(&first[id], (int32_t)i);  // the lowest lane holds the lowest index of its peers
+        }
+    }
+}
+
+__global__ void __launch_bounds__(1024) order_small_kernel(const int32_t *__restrict__ cnt,
+                                                           const int32_t *__restrict__ first, int r, int64_t n,
+                                                           int bits_n, int64_t member_cutoff, int64_t max_clusters,
+                                                           int64_t *__restrict__ newlab) {
+    __shared__ uint64_t s[kOrderSmall];
+    __shared__ int s_k;
+    int m = 1;
+    while (m < r) m <<= 1;
+    if (threadIdx.x == 0) s_k = 0;
+    __syncthreads();
+    int local = 0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const bool used = i < r && cnt[i] > 0;
+        // ascending key = size descending, then first occurrence (distinct
+        // per value, so the order is total)
+        s[i] = used ? (((uint64_t)(n - cnt[i]) << bits_n) | (uint64_t)first[i]) : ~0ull;
+        local += used;
+        if (i < r) newlab[i] = 0;
+    }
+    atomicAdd(&s_k, local);
+    __syncthreads();
+    for (int k = 2; k <= m; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                const int p = i ^ j;
+                if (p > i) {
+                    const uint64_t a = s[i], b = s[p];
+                    if ((a > b) == ((i & k) == 0)) {
+                        s[i] = b;
+                        s[p] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    const int k = s_k;
+    const int64_t maxc = max_clusters < 0 ? k : max_clusters;
+    // rank of every used value: its position in the sorted keys, found by
+    // binary search of its own key (keys are distinct)
+    for (int i = threadIdx.x; i < r; i += blockDim.x) {
+        if (cnt[i] <= 0) continue;
+        const uint64_t key = ((uint64_t)(n - cnt[i]) << bits_n) | (uint64_t)first[i];
+        int lo_q = 0, hi_q = k;
+        while (lo_q < hi_q) {
+            const int mid = (lo_q + hi_q) >> 1;
+            if (s[mid] < key) lo_q = mid + 1;
+            else hi_q = mid;
+        }
+        const int64_t rank = lo_q + 1;  // cluster_count in the reference loop
+        newlab[i] = rank > maxc ? 0 : ((int64_t)cnt[i] >= member_cutoff ? rank : 0);
+    }
+}
+
+__global__ void apply_dense_kernel(int64_t *__restrict__ labels, int64_t n, int64_t lo,
+                                   const int64_t *__restrict__ newlab) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = labels[i];
+        if (v != 0) labels[i] = newlab[v - lo];
+    }
+}
+
 __global__ void apply_label_kernel(int64_t *__restrict__ labels, const int32_t *__restrict__ ids, int64_t n,
                                    const int64_t *__restrict__ newlab) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -433,10 +530,10 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     stage_begin(ctx, 6);
     // persistent warps: exactly the blocks that are resident at once, so
     // that no block (and the nodes it strides over) waits for a second wave
-    auto resident = [&](const void *kernel, int threads) -> unsigned {
+    auto resident = [&](const void *kernel, int threads, size_t smem) -> unsigned {
         int per_sm = 0, sms = 0, dev = 0;
         cudaGetDevice(&dev);
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess ||
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess ||
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
             (void)cudaGetLastError();
             per_sm = 8;
@@ -444,7 +541,7 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
         }
         return std::min<unsigned>(grid_for(n, kCheckWarps), (unsigned)std::max(1, per_sm * sms));
     };
-    const unsigned check_blocks = resident((const void *)check_union_kernel, kCheckWarps * 32);
+    const unsigned check_blocks = resident((const void *)check_union_kernel, kCheckWarps * 32, 0);
     // hook: every node checks its first two candidate edges; compress; then
     // the cross-root pairs only, where pairs inside joined sets cost one load
     check_union_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(
@@ -463,11 +560,12 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
         cross_filter_list_kernel<<<152u * 16u, 256, 0, st>>>(edge_list, edge_count, parent, ctx->io_c.as<int2>(),
                                                              wl_count, wl_cap);
     } else {
-        cross_filter_kernel<<<resident((const void *)cross_filter_kernel, 256), 256, 0, st>>>(
+        cross_filter_kernel<<<resident((const void *)cross_filter_kernel, 256, 0), 256, 0, st>>>(
             n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, ctx->io_c.as<int2>(), wl_count, wl_cap);
     }
     CNN_LAUNCH_CHECK(ctx);
-    edge_check_kernel<<<resident((const void *)edge_check_kernel, 256), 256, 0, st>>>(
+    edge_check_kernel<<<resident((const void *)edge_check_kernel, kCheckWarps * 32, 0), kCheckWarps * 32,
+                        0, st>>>(
         ctx->io_c.as<int2>(), wl_count, wl_cap, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent,
         (int32_t)similarity_cutoff, counters);
     CNN_LAUNCH_CHECK(ctx);
@@ -527,6 +625,25 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64
         return CNN_OK;
     }
     const long long lo = hr[0], hi = hr[1];
+    if ((double)hi - (double)lo + 1.0 <= (double)kOrderSmall) {
+        // few label values: count, order in one block, apply (no further sync)
+        const int r = (int)(hi - lo + 1);
+        CNN_TRY(ctx->ensure(ctx->scratch_b, sizeof(int32_t) * (size_t)(2 * r) + sizeof(int64_t) * (size_t)r + 64));
+        int32_t *cnt = ctx->scratch_b.as<int32_t>();
+        int32_t *first = cnt + r;
+        int64_t *newlab = reinterpret_cast<int64_t *>((reinterpret_cast<uintptr_t>(first + r) + 15) & ~uintptr_t(15));
+        init_count_first_kernel<<<blocks_for(r), 256, 0, st>>>(cnt, first, r);
+        CNN_LAUNCH_CHECK(ctx);
+        count_first_dense_kernel<<<blocks_for(n), 256, 0, st>>>(labels, n, lo, cnt, first);
+        CNN_LAUNCH_CHECK(ctx);
+        order_small_kernel<<<1, 1024, 0, st>>>(cnt, first, r, n, bits_for_fit(n), member_cutoff, max_clusters,
+                                               newlab);
+        CNN_LAUNCH_CHECK(ctx);
+        apply_dense_kernel<<<blocks_for(n), 256, 0, st>>>(labels, n, lo, newlab);
+        CNN_LAUNCH_CHECK(ctx);
+        stage_end(ctx, 8);
+        return CNN_OK;
+    }
     CNN_TRY(ctx->ensure(ctx->io_a, sizeof(int32_t) * (size_t)n));
     int32_t *ids = ctx->io_a.as<int32_t>();
     // dense id space when the label values are compact enough

@@ -69,6 +69,20 @@ __device__ __forceinline__ bool warp_shares_at_least(const int32_t *__restrict__
     return false;
 }
 
+// Persistent check kernels: nodes are dealt to warps in contiguous chunks
+// (CNN_CHECK_CHUNKED=0 strides them), so that warps working at the same time
+// sit in different regions of the (cell-ordered) graph and rarely race on
+// one root, while each warp's own nodes share roots it has just resolved.
+// Seeded fits stride: their open nodes are few and clustered.
+#ifndef CNN_CHECK_CHUNKED
+#define CNN_CHECK_CHUNKED 1
+#endif
+// minimum resident blocks per SM asked of the compiler for the check kernels
+// (latency-bound: more resident warps keep more union-find chains in flight)
+#ifndef CNN_CHECK_MIN_BLOCKS
+#define CNN_CHECK_MIN_BLOCKS 7
+#endif
+
 __global__ void node_kernel(const int32_t *__restrict__ deg, const int32_t *__restrict__ perm,
                             const uint8_t *__restrict__ consider, int64_t n, int64_t n_member_cutoff,
                             uint8_t *__restrict__ node, int32_t *__restrict__ parent,
@@ -104,11 +118,11 @@ __device__ __forceinline__ int64_t warp_upper_bound(const int32_t *__restrict__ 
     return lo + __popc(__ballot_sync(0xffffffffu, p < hi && cols[p] <= v));
 }
 
-// Persistent warps stride over nodes.  For node a, candidate edges (a, b)
-// with b > a and b a node (parent[b] >= 0) are taken 32 at a time; their
-// roots are resolved in parallel (one lane each) and re-resolved only after
-// this warp joined something: a stale "different" only costs an extra
-// check, never a wrong skip.  max_edges bounds the candidate edges one node
+// Persistent warps over nodes.  For node a, candidate edges (a, b) with
+// b > a and b a node (parent[b] >= 0) are taken 32 at a time; their roots
+// are resolved in parallel (one lane each) and re-resolved only after this
+// warp joined something: a stale "different" only costs an extra check,
+// never a wrong skip.  max_edges bounds the candidate edges one node
 // examines (the hook pass uses 2).  Rows are ascending, so the walk starts
 // at the first entry > a.  Nodes with skip_a[a] >= 0 or skip_b[a] >= 0
 // (already joined by seeds) are left to the cross-edge pass.
@@ -121,7 +135,14 @@ __device__ __forceinline__ void check_union_body(
     const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     unsigned long long n_checks = 0, n_acc = 0;
-    for (int64_t a64 = warp0; a64 < n; a64 += nwarps) {
+    // contiguous chunks, or a stride when most nodes skip (seeded fits: the
+    // few open nodes cluster in space and would load a few warps only)
+    const bool chunked = CNN_CHECK_CHUNKED && !skip_a && !skip_b;
+    const int64_t per = chunked ? (n + nwarps - 1) / nwarps : 1;
+    const int64_t a_begin = chunked ? warp0 * per : warp0;
+    const int64_t a_end = chunked ? min(n, (warp0 + 1) * per) : n;
+    const int64_t a_step = chunked ? 1 : nwarps;
+    for (int64_t a64 = a_begin; a64 < a_end; a64 += a_step) {
         const int32_t a = (int32_t)a64;
         if (*(volatile int32_t *)&parent[a] < 0) continue;  // not a node
         if ((skip_a && skip_a[a] >= 0) || (skip_b && skip_b[a] >= 0)) continue;
@@ -189,7 +210,7 @@ __device__ __forceinline__ void check_union_body(
     if (lane == 0 && n_acc) atomicAdd(&counters[6], n_acc);
 }
 
-__global__ void __launch_bounds__(kCheckWarps * 32) check_union_kernel(
+__global__ void __launch_bounds__(kCheckWarps * 32, CNN_CHECK_MIN_BLOCKS) check_union_kernel(
     int64_t n, const int64_t *__restrict__ row_off, const int32_t *__restrict__ cols,
     int32_t *__restrict__ parent, int32_t needed, int32_t max_edges,
     unsigned long long *__restrict__ counters, const int32_t *__restrict__ skip_a,

@@ -139,7 +139,7 @@ extern "C" CNN_API cnn_status cnn_fit_csr_noalloc(const int64_t *offsets, const 
     noalloc_prepare_kernel<<<nblocks(n + 1), 256, 0, st>>>(offsets, n, sc);
     node_kernel<<<nblocks(n), 256, 0, st>>>(sc->deg, sc->perm, consider, n, n_member_cutoff, sc->node, sc->parent,
                                             sc->comp_min, counters);
-    const unsigned check_blocks = std::min<unsigned>(grid_for(n, kCheckWarps), 152u * 8u);
+    const unsigned check_blocks = std::min<unsigned>(grid_for(n, kCheckWarps), 152u * CNN_CHECK_MIN_BLOCKS);
     check_union_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(n, offsets, indices, sc->parent,
                                                                    (int32_t)similarity_cutoff, 2, counters, nullptr, nullptr);
     root_store_kernel<<<nblocks(n), 256, 0, st>>>(n, sc->node, sc->parent);

@@ -205,20 +205,23 @@ __device__ __forceinline__ bool exact_rows(const double *__restrict__ x, int d, 
     return exact_in_radius(xa, xb, d, sp);
 }
 
+// work items of kPer consecutive queries of one cell
+template <int kPer>
 __global__ void item_count_kernel(const int64_t *__restrict__ cell_start, int64_t ncells,
                                   int32_t *__restrict__ items_per_cell) {
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncells; c += (int64_t)gridDim.x * blockDim.x) {
         const int64_t q = cell_start[c + 1] - cell_start[c];
-        items_per_cell[c] = (int32_t)((q + kItemQueries - 1) / kItemQueries);
+        items_per_cell[c] = (int32_t)((q + kPer - 1) / kPer);
     }
 }
 
+template <int kPer>
 __global__ void item_fill_kernel(const int64_t *__restrict__ cell_start, int64_t ncells,
                                  const int64_t *__restrict__ item_off, int2 *__restrict__ items) {
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncells; c += (int64_t)gridDim.x * blockDim.x) {
         const int64_t b = item_off[c], e = item_off[c + 1];
         for (int64_t k = b; k < e; ++k)
-            items[k] = make_int2((int32_t)c, (int32_t)(cell_start[c] + (k - b) * kItemQueries));
+            items[k] = make_int2((int32_t)c, (int32_t)(cell_start[c] + (k - b) * kPer));
     }
 }
 
@@ -415,6 +418,156 @@ __global__ void __launch_bounds__(kGridWarps * 32) grid_search_kernel(
             const int64_t nq = (qend < q0 + kItemQueries ? qend : q0 + kItemQueries) - q0;
             atomicAdd(&counters[1], (unsigned long long)total * (unsigned long long)nq);
         }
+    }
+}
+
+// ---- warp-granular grid search ---------------------------------------------
+// Work unit = (cell, up to kUnitQueries consecutive queries of that cell), one
+// warp each, no block-wide staging: the warp reads its cell's 9 candidate
+// runs (3x3 (y,z) neighbours, each three x-cells long and contiguous in
+// internal order) straight from xf4, 32 candidates at a time over the runs'
+// concatenation, and tests each against its queries held in registers.
+// Sparse cells (most cells hold a few points) cost one warp, not a block;
+// the warps of a block work on neighbouring units and share candidates
+// through L1.  Concatenated run order = ascending internal index, so every
+// query's hits come out sorted.
+#ifndef CNN_UNIT_QUERIES
+#define CNN_UNIT_QUERIES 4
+#endif
+constexpr int kUnitQueries = CNN_UNIT_QUERIES;
+constexpr int kUnitWarps = 8;
+#ifndef CNN_GRID_UNITS
+#define CNN_GRID_UNITS 1
+#endif
+constexpr int kGridPer = CNN_GRID_UNITS ? kUnitQueries : kItemQueries;  // queries per work item
+
+#ifndef CNN_UNIT_MIN_BLOCKS
+#define CNN_UNIT_MIN_BLOCKS 4  // 64 registers: four blocks of eight warps per SM
+#endif
+
+template <int kMode>
+__global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_unit_kernel(
+    const int2 *__restrict__ units, int64_t nunits, const double *__restrict__ x, int d, GridGeom geo,
+    SearchParams sp, const int32_t *__restrict__ perm, const int64_t *__restrict__ cell_start,
+    const float4 *__restrict__ xf4, int32_t *__restrict__ deg, const int64_t *__restrict__ row_off,
+    int32_t *__restrict__ cols, unsigned long long *__restrict__ counters, int64_t *__restrict__ qslot) {
+    __shared__ int32_t s_rs[kUnitWarps][9];
+    __shared__ int32_t s_cum[kUnitWarps][10];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t u = (int64_t)blockIdx.x * kUnitWarps + wid;
+    if (u >= nunits) return;  // whole warps only: nothing below syncs the block
+    const int2 unit = units[u];
+    const int32_t cid = unit.x;
+    const int64_t q0 = unit.y;
+    const int64_t cs = cell_start[cid], qend = cell_start[cid + 1];
+    // run r = lane (r < 9): (dz, dy) = (r / 3 - 1, r % 3 - 1); empty when outside the grid
+    int32_t rs = 0, len = 0;
+    if (lane < 9) {
+        const int32_t cx = cid % geo.g[0];
+        const int32_t cy = (cid / geo.g[0]) % geo.g[1];
+        const int32_t cz = cid / (geo.g[0] * geo.g[1]);
+        const int32_t z = cz + lane / 3 - 1, y = cy + lane % 3 - 1;
+        if (z >= 0 && z < geo.g[2] && y >= 0 && y < geo.g[1]) {
+            const int32_t xlo = cx > 0 ? cx - 1 : 0;
+            const int32_t xhi = cx + 1 < geo.g[0] ? cx + 1 : geo.g[0] - 1;
+            const int64_t row = (int64_t)geo.g[0] * ((int64_t)y + (int64_t)geo.g[1] * z);
+            const int64_t b = cell_start[row + xlo], e = cell_start[row + xhi + 1];
+            rs = (int32_t)b;
+            len = e > b ? (int32_t)(e - b) : 0;
+        }
+    }
+    int32_t inc = len;  // inclusive prefix over the runs
+#pragma unroll
+    for (int o = 1; o < 16; o <<= 1) {
+        const int32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += v;
+    }
+    if (lane < 9) {
+        s_rs[wid][lane] = rs;
+        s_cum[wid][lane + 1] = inc;
+    }
+    if (lane == 0) s_cum[wid][0] = 0;
+    const int32_t total = __shfl_sync(0xffffffffu, inc, 8);
+    __syncwarp();
+
+    // query k: internal index (-1: none), coordinates, and for kFill/kSlots
+    // the running write position in its row (kCount: a per-lane count)
+    int32_t qi[kUnitQueries];
+    float qx[kUnitQueries], qy[kUnitQueries], qz[kUnitQueries];
+    int64_t wq[kUnitQueries];
+    int32_t cnt[kUnitQueries];
+    const int64_t slot0 = kMode == kSlots ? row_off[cid] + (q0 - cs) * (int64_t)total : 0;
+#pragma unroll
+    for (int k = 0; k < kUnitQueries; ++k) {
+        const int64_t qk = q0 + k;
+        const bool ok = qk < qend;
+        const float4 f = ok ? xf4[qk] : make_float4(INFINITY, INFINITY, INFINITY, 0.f);
+        qx[k] = f.x;
+        qy[k] = f.y;
+        qz[k] = f.z;
+        qi[k] = ok ? (int32_t)qk : -1;
+        wq[k] = kMode == kFill ? (ok ? row_off[qk] : 0) : slot0 + k * (int64_t)total;
+        if (kMode == kSlots && ok && lane == 0) qslot[qk] = wq[k];
+        cnt[k] = 0;
+    }
+    const unsigned lt = (1u << lane) - 1u;
+    unsigned long long n_exact = 0;
+    for (int32_t t0 = 0; t0 < total; t0 += 32) {
+        const int32_t t = t0 + lane;
+        int32_t j = -1;
+        float4 cf = make_float4(INFINITY, INFINITY, INFINITY, 0.f);  // +inf never matches
+        if (t < total) {
+            int r = 0;
+            while (s_cum[wid][r + 1] <= t) ++r;  // empty runs are passed over
+            j = s_rs[wid][r] + (t - s_cum[wid][r]);
+            cf = xf4[j];
+        }
+        bool in[kUnitQueries], amb[kUnitQueries];
+        bool any_amb = false;
+#pragma unroll
+        for (int k = 0; k < kUnitQueries; ++k) {
+            const float ex = qx[k] - cf.x, ey = qy[k] - cf.y, ez = qz[k] - cf.z;
+            const float sf = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+            in[k] = sf <= sp.thr_in;
+            amb[k] = !in[k] && sf <= sp.thr_out;
+            any_amb |= amb[k];
+        }
+        if (__any_sync(0xffffffffu, any_amb)) {  // rare: decide those pairs in float64
+#pragma unroll
+            for (int k = 0; k < kUnitQueries; ++k) {
+                if (amb[k]) {
+                    in[k] = exact_rows(x, d, perm[qi[k]], perm[j], sp);
+                    ++n_exact;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kUnitQueries; ++k) {
+            if (kMode != kCount) {
+                const unsigned hit = __ballot_sync(0xffffffffu, in[k]);
+                if (in[k]) cols[wq[k] + __popc(hit & lt)] = j;
+                wq[k] += __popc(hit);
+            } else {
+                cnt[k] += in[k];  // per-lane count, summed over the warp at the end
+            }
+        }
+    }
+    if (kMode != kFill) {
+        if (kMode == kCount) {
+#pragma unroll
+            for (int k = 0; k < kUnitQueries; ++k)
+                for (int o = 16; o > 0; o >>= 1) cnt[k] += __shfl_down_sync(0xffffffffu, cnt[k], o);
+        } else {
+#pragma unroll
+            for (int k = 0; k < kUnitQueries; ++k) cnt[k] = (int32_t)(wq[k] - (slot0 + k * (int64_t)total));
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < kUnitQueries; ++k)
+                if (qi[k] >= 0) deg[qi[k]] = cnt[k];
+        }
+        for (int o = 16; o > 0; o >>= 1) n_exact += __shfl_down_sync(0xffffffffu, n_exact, o);
+        if (lane == 0 && n_exact) atomicAdd(&counters[0], n_exact);
     }
 }
 
@@ -881,6 +1034,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     int32_t *deg = ctx->deg.as<int32_t>();
     int64_t *row_off = ctx->row_off.as<int64_t>();
     int64_t grid_items = 0;
+    int64_t n_candidates = -1;  // pairs looked at (grid path: from the slot sizes)
     bool use_slots = false;
     unsigned long long *counters = ctx->counters.as<unsigned long long>();
 
@@ -910,7 +1064,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         // work items: (cell, first query) for every 32 queries of a cell
         CNN_TRY(ctx->ensure(ctx->io_a, sizeof(int32_t) * (size_t)(geo.ncells + 1)));
         CNN_TRY(ctx->ensure(ctx->io_b, sizeof(int64_t) * (size_t)(geo.ncells + 1)));
-        item_count_kernel<<<std::min<unsigned>(grid_for(geo.ncells, 256), 152u * 16u), 256, 0, st>>>(
+        item_count_kernel<kGridPer><<<std::min<unsigned>(grid_for(geo.ncells, 256), 152u * 16u), 256, 0, st>>>(
             ctx->cell_start.as<int64_t>(), geo.ncells, ctx->io_a.as<int32_t>());
         CNN_LAUNCH_CHECK(ctx);
         CNN_CUDA(ctx, cudaMemsetAsync(ctx->io_a.as<int32_t>() + geo.ncells, 0, sizeof(int32_t), st));
@@ -938,7 +1092,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
             CNN_TRY(ctx->ensure(ctx->grid_qslot, sizeof(int64_t) * (size_t)n));
         }
         CNN_TRY(ctx->ensure(ctx->io_c, sizeof(int2) * (size_t)(nitems > 0 ? nitems : 1)));
-        item_fill_kernel<<<std::min<unsigned>(grid_for(geo.ncells, 256), 152u * 16u), 256, 0, st>>>(
+        item_fill_kernel<kGridPer><<<std::min<unsigned>(grid_for(geo.ncells, 256), 152u * 16u), 256, 0, st>>>(
             ctx->cell_start.as<int64_t>(), geo.ncells, ctx->io_b.as<int64_t>(), ctx->io_c.as<int2>());
         CNN_LAUNCH_CHECK(ctx);
         grid_items = nitems;
@@ -947,17 +1101,31 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         stage_begin(ctx, 2);
         CNN_CUDA(ctx, cudaMemsetAsync(deg, 0, sizeof(int32_t) * (size_t)n, st));
         if (nitems > 0 && use_slots) {
+#if CNN_GRID_UNITS
+            grid_unit_kernel<kSlots><<<(unsigned)((nitems + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
+                ctx->io_c.as<int2>(), nitems, ctx->x, d, geo, sp, ctx->perm.as<int32_t>(),
+                ctx->cell_start.as<int64_t>(), ctx->xf4.as<float4>(), deg, slot_base,
+                ctx->grid_slot_cols.as<int32_t>(), counters, ctx->grid_qslot.as<int64_t>());
+#else
             grid_search_kernel<kSlots><<<(unsigned)nitems, kGridWarps * 32, 0, st>>>(
                 ctx->io_c.as<int2>(), ctx->x, d, geo, sp, ctx->perm.as<int32_t>(), ctx->cell_start.as<int64_t>(),
                 ctx->xf4.as<float4>(), deg, slot_base, ctx->grid_slot_cols.as<int32_t>(), counters,
                 ctx->grid_qslot.as<int64_t>());
+#endif
             CNN_LAUNCH_CHECK(ctx);
         } else if (nitems > 0) {
+#if CNN_GRID_UNITS
+            grid_unit_kernel<kCount><<<(unsigned)((nitems + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
+                ctx->io_c.as<int2>(), nitems, ctx->x, d, geo, sp, ctx->perm.as<int32_t>(),
+                ctx->cell_start.as<int64_t>(), ctx->xf4.as<float4>(), deg, nullptr, nullptr, counters, nullptr);
+#else
             grid_search_kernel<kCount><<<(unsigned)nitems, kGridWarps * 32, 0, st>>>(
                 ctx->io_c.as<int2>(), ctx->x, d, geo, sp, ctx->perm.as<int32_t>(), ctx->cell_start.as<int64_t>(),
                 ctx->xf4.as<float4>(), deg, nullptr, nullptr, counters, nullptr);
+#endif
             CNN_LAUNCH_CHECK(ctx);
         }
+        n_candidates = hcounts[1];  // every query against its cell's candidate runs
         stage_end(ctx, 2);
         ctx->identity_perm = false;
     } else {
@@ -1003,9 +1171,16 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
                 ctx->cols.as<int32_t>());
             CNN_LAUNCH_CHECK(ctx);
         } else if (grid_items > 0) {
+#if CNN_GRID_UNITS
+            grid_unit_kernel<kFill><<<(unsigned)((grid_items + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
+                ctx->io_c.as<int2>(), grid_items, ctx->x, d, geo, sp, ctx->perm.as<int32_t>(),
+                ctx->cell_start.as<int64_t>(), ctx->xf4.as<float4>(), deg, row_off, ctx->cols.as<int32_t>(), counters,
+                nullptr);
+#else
             grid_search_kernel<kFill><<<(unsigned)grid_items, kGridWarps * 32, 0, st>>>(
                 ctx->io_c.as<int2>(), ctx->x, d, geo, sp, ctx->perm.as<int32_t>(), ctx->cell_start.as<int64_t>(),
                 ctx->xf4.as<float4>(), deg, row_off, ctx->cols.as<int32_t>(), counters, nullptr);
+#endif
             CNN_LAUNCH_CHECK(ctx);
         }
     } else {
@@ -1020,7 +1195,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     CNN_CUDA(ctx, cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
     CNN_CUDA(ctx, cudaStreamSynchronize(st));
     ctx->stats.n_exact = (int64_t)hc[0];
-    ctx->stats.n_candidates = (int64_t)hc[1];
+    ctx->stats.n_candidates = n_candidates >= 0 ? n_candidates : (int64_t)hc[1];
     ctx->stats.n_nonzero = nnz;
     ctx->nnz = nnz;
     ctx->have_graph = true;
