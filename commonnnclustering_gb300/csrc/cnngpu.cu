@@ -110,6 +110,10 @@ CNN_API cnn_status cnn_create(cnn_context **out, int device, void *stream) {
             return CNN_ERR_CUDA;
         }
     }
+    if (cudaMallocHost(&ctx->host_stats, 16 * sizeof(unsigned long long)) != cudaSuccess) {
+        (void)cudaGetLastError();
+        ctx->host_stats = nullptr;  // statistics are then read back with a sync
+    }
     *out = ctx;
     return CNN_OK;
 }
@@ -138,6 +142,7 @@ CNN_API cnn_status cnn_destroy(cnn_context *ctx) {
         if (ctx->ev_end[i]) cudaEventDestroy(ctx->ev_end[i]);
     }
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->host_stats) cudaFreeHost(ctx->host_stats);
     (void)cudaGetLastError();
     delete ctx;
     return CNN_OK;
@@ -185,6 +190,18 @@ CNN_API cnn_status cnn_get_stats(const cnn_context *cctx, cnn_stats *out) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, ctx->ev_begin[i], ctx->ev_end[i]) == cudaSuccess) *slot_field[i] = ms;
         (void)cudaGetLastError();
+    }
+    if (ctx->search_stats_pending) {
+        ctx->stats.n_exact = (int64_t)ctx->host_stats[0];
+        ctx->stats.n_candidates = ctx->pending_candidates >= 0 ? ctx->pending_candidates : (int64_t)ctx->host_stats[1];
+        ctx->search_stats_pending = false;
+    }
+    if (ctx->fit_stats_pending) {
+        ctx->stats.n_nodes = (int64_t)ctx->host_stats[4];
+        ctx->stats.n_checks = (int64_t)ctx->host_stats[5];
+        ctx->stats.n_accepted = (int64_t)ctx->host_stats[6];
+        ctx->stats.n_clusters = (int64_t)ctx->host_stats[8];
+        ctx->fit_stats_pending = false;
     }
     ctx->stats.n_launches = ctx->n_launches;
     *out = ctx->stats;

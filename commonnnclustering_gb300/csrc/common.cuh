@@ -70,6 +70,12 @@ struct cnn_context {
     int64_t n_launches = 0;
     std::string last_error;
     cnn_stats stats{};
+    // Counters of the last search and fit, copied back without a sync into
+    // pinned memory and read by cnn_get_stats (which syncs the stream).
+    unsigned long long *host_stats = nullptr;  // [0] exact, [1] candidates, [4..6] fit, [8] clusters
+    bool search_stats_pending = false;
+    bool fit_stats_pending = false;
+    int64_t pending_candidates = -1;  // >= 0: known on the host
 
     // points (original order, row-major float64)
     int64_t n = 0;

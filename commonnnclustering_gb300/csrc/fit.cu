@@ -501,6 +501,7 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     if (!ctx->have_graph) return ctx->fail(CNN_ERR_STATE, "no neighbour graph: call cnn_build_neighbours first");
     const int64_t n = ctx->n;
     cudaStream_t st = ctx->stream;
+    ctx->fit_stats_pending = false;
     if (n == 0) return CNN_OK;
     // no list is longer than 2^31-1; any negative cutoff rejects every pair
     if (similarity_cutoff > INT32_MAX) similarity_cutoff = INT32_MAX;
@@ -593,6 +594,13 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     CNN_CUDA(ctx, cudaMemsetAsync(consider_dev, 0, (size_t)n, st));
     stage_end(ctx, 7);
 
+    if (ctx->host_stats) {  // read by cnn_get_stats
+        CNN_CUDA(ctx, cudaMemcpyAsync(ctx->host_stats + 4, counters + 4, 3 * sizeof(unsigned long long),
+                                      cudaMemcpyDeviceToHost, st));
+        CNN_CUDA(ctx, cudaMemcpyAsync(ctx->host_stats + 8, rank + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        ctx->fit_stats_pending = true;
+        return CNN_OK;
+    }
     unsigned long long hc[4] = {0, 0, 0, 0};
     int64_t k = 0;
     CNN_CUDA(ctx, cudaMemcpyAsync(hc, counters + 4, sizeof(hc), cudaMemcpyDeviceToHost, st));

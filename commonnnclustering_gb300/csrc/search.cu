@@ -8,7 +8,8 @@
 // which pairs are looked at and how cheaply obvious ones are decided:
 //
 //  * Cell grid (d <= 3).  Points are bucketed into cubic cells of edge
-//    h >= R (R = search radius) and ordered by cell id (x fastest).  A
+//    h >= R (R = search radius) and ordered by cell id (x fastest; inside
+//    a cell, in the order of an atomic counter -- any order will do).  A
 //    point's candidates are the 3x3x3 cells around its own; for a fixed
 //    (dy, dz) the three x-cells are contiguous, so candidates form 9 runs of
 //    consecutive internal indices, visited in increasing order.  Rows come
@@ -142,8 +143,12 @@ __device__ __forceinline__ int32_t cell_coord(double v, double lo, double h, int
     return (int32_t)c;
 }
 
+// cell of every point and its slot among the points of that cell (the
+// order of the atomic increments: any order serves, rows are sorted by
+// internal index whatever the order inside a cell)
 __global__ void cell_assign_kernel(const double *__restrict__ x, int64_t n, int d, GridGeom geo,
-                                   int32_t *__restrict__ cell_of, int32_t *__restrict__ cell_count) {
+                                   int32_t *__restrict__ cell_of, int32_t *__restrict__ slot,
+                                   int32_t *__restrict__ cell_count) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         bool fin = true;
         for (int k = 0; k < d; ++k) fin = fin && isfinite(x[i * d + k]);
@@ -156,29 +161,23 @@ __global__ void cell_assign_kernel(const double *__restrict__ x, int64_t n, int 
             id = (int64_t)c[0] + (int64_t)geo.g[0] * ((int64_t)c[1] + (int64_t)geo.g[1] * c[2]);
         }
         cell_of[i] = (int32_t)id;
-        atomicAdd(&cell_count[id], 1);
+        slot[i] = atomicAdd(&cell_count[id], 1);
     }
 }
 
-// Sort key: cell id in the high bits, point index in the low bits, so the
-// permutation (cell order, ties by point index) is deterministic.
-__global__ void cell_key_kernel(const int32_t *__restrict__ cell_of, int64_t n, int bits_n,
-                                uint64_t *__restrict__ keys) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        keys[i] = ((uint64_t)(uint32_t)cell_of[i] << bits_n) | (uint64_t)i;
-}
-
-__global__ void perm_gather_kernel(const uint64_t *__restrict__ keys, int64_t n, int bits_n,
-                                   const double *__restrict__ x, int d, GridGeom geo,
-                                   int32_t *__restrict__ perm, int32_t *__restrict__ inv,
-                                   float4 *__restrict__ xf4) {
-    const uint64_t mask = (bits_n >= 64) ? ~0ull : ((1ull << bits_n) - 1);
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        int32_t i = (int32_t)(keys[p] & mask);
-        perm[p] = i;
-        inv[i] = (int32_t)p;
+// Internal order = cell order: point i goes to cell_start[cell] + slot;
+// perm/inv map between the orders and xf4 holds the float32 coordinates
+// relative to the grid origin in internal order.
+__global__ void place_kernel(const int32_t *__restrict__ cell_of, const int32_t *__restrict__ slot,
+                             const int64_t *__restrict__ cell_start, int64_t n, const double *__restrict__ x, int d,
+                             GridGeom geo, int32_t *__restrict__ perm, int32_t *__restrict__ inv,
+                             float4 *__restrict__ xf4) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t p = (int32_t)(cell_start[cell_of[i]] + slot[i]);
+        perm[p] = (int32_t)i;
+        inv[i] = p;
         float v[3] = {0.f, 0.f, 0.f};
-        for (int k = 0; k < d; ++k) v[k] = (float)__dsub_rn(x[(int64_t)i * d + k], geo.lo[k]);
+        for (int k = 0; k < d; ++k) v[k] = (float)__dsub_rn(x[i * d + k], geo.lo[k]);
         xf4[p] = make_float4(v[0], v[1], v[2], 0.f);
     }
 }
@@ -853,6 +852,8 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     cudaStream_t st = ctx->stream;
     ctx->have_graph = false;
     ctx->stats = cnn_stats{};
+    ctx->search_stats_pending = false;
+    ctx->fit_stats_pending = false;
     ctx->stats.n_points = n;
     CNN_TRY(ctx->ensure(ctx->counters, 16 * sizeof(unsigned long long)));
     CNN_CUDA(ctx, cudaMemsetAsync(ctx->counters.ptr, 0, 16 * sizeof(unsigned long long), st));
@@ -1040,25 +1041,21 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
 
     if (use_grid) {
         stage_begin(ctx, 1);
-        const int bits_n = bits_for(n);
         CNN_TRY(ctx->ensure(ctx->cell_of, sizeof(int32_t) * (size_t)n));
         CNN_TRY(ctx->ensure(ctx->cell_start, sizeof(int64_t) * (size_t)(geo.ncells + 2)));
         CNN_TRY(ctx->ensure(ctx->scratch_b, sizeof(int32_t) * (size_t)(geo.ncells + 2)));
-        CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(uint64_t) * (size_t)n));
+        CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(int32_t) * (size_t)n));
         CNN_TRY(ctx->ensure(ctx->xf4, sizeof(float4) * (size_t)n));
         int32_t *cell_count = ctx->scratch_b.as<int32_t>();
         CNN_CUDA(ctx, cudaMemsetAsync(cell_count, 0, sizeof(int32_t) * (size_t)(geo.ncells + 2), st));
         const unsigned gb = std::min<unsigned>(grid_for(n, 256), 152u * 16u);
-        cell_assign_kernel<<<gb, 256, 0, st>>>(ctx->x, n, d, geo, ctx->cell_of.as<int32_t>(), cell_count);
+        int32_t *slot = ctx->scratch_a.as<int32_t>();
+        cell_assign_kernel<<<gb, 256, 0, st>>>(ctx->x, n, d, geo, ctx->cell_of.as<int32_t>(), slot, cell_count);
         CNN_LAUNCH_CHECK(ctx);
         CNN_TRY(scan_exclusive_i32_to_i64(ctx, cell_count, ctx->cell_start.as<int64_t>(), geo.ncells + 2));
-        uint64_t *keys = ctx->scratch_a.as<uint64_t>();
-        cell_key_kernel<<<gb, 256, 0, st>>>(ctx->cell_of.as<int32_t>(), n, bits_n, keys);
-        CNN_LAUNCH_CHECK(ctx);
-        // keys are built in point order: sorting the cell bits alone keeps points ascending within a cell
-        CNN_TRY(radix_sort_u64(ctx, keys, n, bits_n + bits_for(geo.ncells + 2), bits_n));
-        perm_gather_kernel<<<gb, 256, 0, st>>>(keys, n, bits_n, ctx->x, d, geo, ctx->perm.as<int32_t>(),
-                                                ctx->inv.as<int32_t>(), ctx->xf4.as<float4>());
+        place_kernel<<<gb, 256, 0, st>>>(ctx->cell_of.as<int32_t>(), slot, ctx->cell_start.as<int64_t>(), n, ctx->x, d,
+                                         geo, ctx->perm.as<int32_t>(), ctx->inv.as<int32_t>(),
+                                         ctx->xf4.as<float4>());
         CNN_LAUNCH_CHECK(ctx);
 
         // work items: (cell, first query) for every 32 queries of a cell
@@ -1191,11 +1188,18 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     }
     stage_end(ctx, 4);
 
-    unsigned long long hc[2] = {0, 0};
-    CNN_CUDA(ctx, cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
-    CNN_CUDA(ctx, cudaStreamSynchronize(st));
-    ctx->stats.n_exact = (int64_t)hc[0];
-    ctx->stats.n_candidates = n_candidates >= 0 ? n_candidates : (int64_t)hc[1];
+    if (ctx->host_stats) {  // read by cnn_get_stats
+        CNN_CUDA(ctx, cudaMemcpyAsync(ctx->host_stats, counters, 2 * sizeof(unsigned long long),
+                                      cudaMemcpyDeviceToHost, st));
+        ctx->pending_candidates = n_candidates;
+        ctx->search_stats_pending = true;
+    } else {
+        unsigned long long hc[2] = {0, 0};
+        CNN_CUDA(ctx, cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
+        CNN_CUDA(ctx, cudaStreamSynchronize(st));
+        ctx->stats.n_exact = (int64_t)hc[0];
+        ctx->stats.n_candidates = n_candidates >= 0 ? n_candidates : (int64_t)hc[1];
+    }
     ctx->stats.n_nonzero = nnz;
     ctx->nnz = nnz;
     ctx->have_graph = true;
@@ -1334,6 +1338,8 @@ cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev, con
     cudaStream_t st = ctx->stream;
     ctx->have_graph = false;
     ctx->stats = cnn_stats{};
+    ctx->search_stats_pending = false;
+    ctx->fit_stats_pending = false;
     ctx->stats.n_points = n;
     ctx->n = n;
     ctx->d = 0;
