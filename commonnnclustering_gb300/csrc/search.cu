@@ -490,10 +490,10 @@ __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_uni
     __syncwarp();
 
     // query k: internal index (-1: none), coordinates, and for kFill/kSlots
-    // the running write position in its row (kCount: a per-lane count)
+    // its row in cols (kCount: a per-lane count)
     int32_t qi[kUnitQueries];
     float qx[kUnitQueries], qy[kUnitQueries], qz[kUnitQueries];
-    int64_t wq[kUnitQueries];
+    int32_t *rowp[kUnitQueries];
     int32_t cnt[kUnitQueries];
     const int64_t slot0 = kMode == kSlots ? row_off[cid] + (q0 - cs) * (int64_t)total : 0;
 #pragma unroll
@@ -505,22 +505,26 @@ __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_uni
         qy[k] = f.y;
         qz[k] = f.z;
         qi[k] = ok ? (int32_t)qk : -1;
-        wq[k] = kMode == kFill ? (ok ? row_off[qk] : 0) : slot0 + k * (int64_t)total;
-        if (kMode == kSlots && ok && lane == 0) qslot[qk] = wq[k];
+        const int64_t w = kMode == kFill ? (ok ? row_off[qk] : 0) : slot0 + k * (int64_t)total;
+        rowp[k] = kMode == kCount ? nullptr : cols + w;
+        if (kMode == kSlots && ok && lane == 0) qslot[qk] = w;
         cnt[k] = 0;
     }
     const unsigned lt = (1u << lane) - 1u;
     unsigned long long n_exact = 0;
-    for (int32_t t0 = 0; t0 < total; t0 += 32) {
-        const int32_t t = t0 + lane;
-        int32_t j = -1;
-        float4 cf = make_float4(INFINITY, INFINITY, INFINITY, 0.f);  // +inf never matches
-        if (t < total) {
-            int r = 0;
-            while (s_cum[wid][r + 1] <= t) ++r;  // empty runs are passed over
-            j = s_rs[wid][r] + (t - s_cum[wid][r]);
-            cf = xf4[j];
+    // this lane's run: t in [lo, hi) of the concatenation maps to j = base + t;
+    // t only grows, so the run index only moves forward (empty runs skipped)
+    int r = 0;
+    int32_t hi = s_cum[wid][1], base = s_rs[wid][0];
+    for (int32_t t = lane; t - lane < total; t += 32) {
+        while (t >= hi && r < 8) {
+            ++r;
+            base = s_rs[wid][r] - hi;
+            hi = s_cum[wid][r + 1];
         }
+        const bool valid = t < total;
+        const int32_t j = base + t;
+        const float4 cf = valid ? xf4[j] : make_float4(INFINITY, INFINITY, INFINITY, 0.f);  // +inf never matches
         bool in[kUnitQueries], amb[kUnitQueries];
         bool any_amb = false;
 #pragma unroll
@@ -544,8 +548,8 @@ __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_uni
         for (int k = 0; k < kUnitQueries; ++k) {
             if (kMode != kCount) {
                 const unsigned hit = __ballot_sync(0xffffffffu, in[k]);
-                if (in[k]) cols[wq[k] + __popc(hit & lt)] = j;
-                wq[k] += __popc(hit);
+                if (in[k]) rowp[k][cnt[k] + __popc(hit & lt)] = j;
+                cnt[k] += __popc(hit);
             } else {
                 cnt[k] += in[k];  // per-lane count, summed over the warp at the end
             }
@@ -556,9 +560,6 @@ __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_uni
 #pragma unroll
             for (int k = 0; k < kUnitQueries; ++k)
                 for (int o = 16; o > 0; o >>= 1) cnt[k] += __shfl_down_sync(0xffffffffu, cnt[k], o);
-        } else {
-#pragma unroll
-            for (int k = 0; k < kUnitQueries; ++k) cnt[k] = (int32_t)(wq[k] - (slot0 + k * (int64_t)total));
         }
         if (lane == 0) {
 #pragma unroll
