@@ -204,6 +204,8 @@ def roofline_entry(stats_list, nnz, n, peaks):
         "algorithmic_bytes": bytes_, "ms_per_launch": ms,
         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback 6800",
         "stage_ms": {k: round(v, 4) for k, v in means.items()},
+        "other_stage_ms": {k: round(statistics.mean(s.get(k, 0.0) for s in stats_list), 4)
+                           for k in ("ms_bbox", "ms_scan", "ms_nodes")},
     }
 
 

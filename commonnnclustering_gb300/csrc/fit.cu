@@ -23,7 +23,7 @@
 //      one member of N(b) up among 32 of N(a) by shuffles) and stops as soon
 //      as the count reaches the cutoff or can no longer reach it.  Accepted
 //      edges are joined with a lock-free union-find (CAS on roots, path
-//      halving).  A hook pass checks two edges per node; a read-only pass
+//      halving).  A hook pass checks three edges per node; a read-only pass
 //      then lists the edges whose roots still differ and only those are
 //      checked;
 //   3. per component, the minimum point index; ranks of those minima give
@@ -41,7 +41,7 @@ namespace {
 
 // candidate edges each node checks in the hook pass
 #ifndef CNN_HOOK_EDGES
-#define CNN_HOOK_EDGES 2
+#define CNN_HOOK_EDGES 3
 #endif
 constexpr int32_t kHookEdges = CNN_HOOK_EDGES;
 
@@ -543,7 +543,7 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
         return std::min<unsigned>(grid_for(n, kCheckWarps), (unsigned)std::max(1, per_sm * sms));
     };
     const unsigned check_blocks = resident((const void *)check_union_kernel, kCheckWarps * 32, 0);
-    // hook: every node checks its first two candidate edges; compress; then
+    // hook: every node checks its first kHookEdges candidate edges; compress; then
     // the cross-root pairs only, where pairs inside joined sets cost one load
     check_union_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(
         n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff, kHookEdges,

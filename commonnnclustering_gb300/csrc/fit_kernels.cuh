@@ -123,7 +123,7 @@ __device__ __forceinline__ int64_t warp_upper_bound(const int32_t *__restrict__ 
 // are resolved in parallel (one lane each) and re-resolved only after this
 // warp joined something: a stale "different" only costs an extra check,
 // never a wrong skip.  max_edges bounds the candidate edges one node
-// examines (the hook pass uses 2).  Rows are ascending, so the walk starts
+// examines (the hook pass uses 3).  Rows are ascending, so the walk starts
 // at the first entry > a.  Nodes with skip_a[a] >= 0 or skip_b[a] >= 0
 // (already joined by seeds) are left to the cross-edge pass.
 __device__ __forceinline__ void check_union_body(
@@ -144,12 +144,19 @@ __device__ __forceinline__ void check_union_body(
     const int64_t a_step = chunked ? 1 : nwarps;
     for (int64_t a64 = a_begin; a64 < a_end; a64 += a_step) {
         const int32_t a = (int32_t)a64;
-        if (*(volatile int32_t *)&parent[a] < 0) continue;  // not a node
+        // parent[a] and the row bounds in one round trip (lanes 0, 1, 2)
+        int64_t v = 0;
+        if (lane == 0) v = *(volatile int32_t *)&parent[a];
+        else if (lane < 3) v = row_off[a + lane - 1];
+        const int32_t pa = (int32_t)__shfl_sync(0xffffffffu, v, 0);
+        if (pa < 0) continue;  // not a node
         if ((skip_a && skip_a[a] >= 0) || (skip_b && skip_b[a] >= 0)) continue;
-        const int64_t s = row_off[a], e = row_off[a + 1];
+        const int64_t s = __shfl_sync(0xffffffffu, v, 1), e = __shfl_sync(0xffffffffu, v, 2);
         const int32_t la = (int32_t)(e - s);
         const int32_t *A = cols + s;
-        int32_t ra = -1;
+        // ra (and rx once set) are roots observed to hold a: equal roots mean
+        // one set, since sets only merge; a stale "different" costs a check
+        int32_t ra = -1, rx = -1;
         bool dirty = true;
         int32_t seen = 0;
         for (int64_t k0 = warp_upper_bound(cols, s, e, a, lane); k0 < e && seen < max_edges; k0 += 32) {
@@ -171,14 +178,16 @@ __device__ __forceinline__ void check_union_body(
             }
             seen += __popc(cmask);
             if (dirty) {
-                ra = uf_find(parent, a);
+                ra = (ra < 0 && pa == a) ? a : uf_find(parent, ra < 0 ? pa : a);  // parent pointers only rise
+                rx = -1;
                 dirty = false;
             }
             int32_t rb = cand ? uf_find(parent, pb) : -1;
-            unsigned mask = __ballot_sync(0xffffffffu, cand && rb != ra);
+            unsigned mask = __ballot_sync(0xffffffffu, cand && rb != ra && rb != rx);
             while (mask) {
                 if (dirty) {
                     ra = uf_find(parent, a);
+                    rx = -1;
                     const bool live = (mask >> lane) & 1u;
                     if (live) rb = uf_find(parent, rb);
                     mask = __ballot_sync(0xffffffffu, live && rb != ra);
@@ -198,10 +207,25 @@ __device__ __forceinline__ void check_union_body(
                     ++n_checks;
                 }
                 if (ok) {
-                    if (lane == 0) uf_unite(parent, a, bb);
-                    __syncwarp();
+                    // link the two observed roots directly (larger under
+                    // smaller, as uf_unite does); if the larger one is no
+                    // longer a root, take the general path and re-resolve
+                    const int32_t rbb = __shfl_sync(0xffffffffu, rb, src);
+                    const int32_t lo = min(ra, rbb), hi = max(ra, rbb);
+                    int direct = 0;
+                    if (lane == 0) {
+                        direct = atomicCAS(&parent[hi], hi, lo) == hi;
+                        if (!direct) uf_unite(parent, a, bb);
+                    }
+                    direct = __shfl_sync(0xffffffffu, direct, 0);
                     ++n_acc;
-                    dirty = true;
+                    if (direct) {
+                        ra = lo;
+                        rx = hi;
+                        mask = __ballot_sync(0xffffffffu, ((mask >> lane) & 1u) && rb != ra && rb != rx);
+                    } else {
+                        dirty = true;
+                    }
                 }
             }
         }
