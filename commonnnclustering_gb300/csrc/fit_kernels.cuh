@@ -252,10 +252,19 @@ __global__ void root_min_kernel(int64_t n, const uint8_t *__restrict__ node, int
     }
 }
 
+// Every node's parent becomes its root.  The walk writes nothing: with
+// path halving, another thread could store a not-yet-root ancestor into a
+// slot after its owner stored the root; here each slot is written once, by
+// its owner, with the root (no unions run at this point).
 __global__ void root_store_kernel(int64_t n, const uint8_t *__restrict__ node, int32_t *__restrict__ parent) {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
         if (!node[p]) continue;
-        parent[p] = uf_find(parent, (int32_t)p);
+        int32_t r = (int32_t)p, next = *(volatile int32_t *)&parent[r];
+        while (next != r) {
+            r = next;
+            next = *(volatile int32_t *)&parent[r];
+        }
+        parent[p] = r;
     }
 }
 
