@@ -177,10 +177,12 @@ def roofline_entry(stats_list, nnz, n, peaks):
         }
     stages = {
         # stage -> (kernel name, algorithmic bytes per launch)
-        "ms_fill": ("grid_search_kernel<fill>", n * d * 8 + 4 * nnz + 8 * (n + 1)),
-        "ms_count": ("grid_search_kernel<count>", n * d * 8 + 4 * n),
+        # one pass into per-row slots: float4 coordinates read, rows, lengths and slot starts written
+        "ms_count": ("grid_unit_kernel<slots>", 16 * n + 4 * nnz + 4 * n + 8 * n),
+        # slots -> compact CSR: rows read and written, offsets read
+        "ms_fill": ("compact_rows_kernel", 8 * nnz + 16 * (n + 1)),
         "ms_check": ("check_union_kernel", 4 * nnz + 8 * (n + 1) + n + 8 * n),
-        "ms_cells": ("cell binning + radix sort", 4 * 8 * n),
+        "ms_cells": ("cell binning (assign, scan, place)", 4 * 8 * n),
         "ms_label": ("labelling", 24 * n),
         "ms_sort": ("sort_by_size", 32 * n),
     }

@@ -251,7 +251,12 @@ __global__ void __launch_bounds__(kCheckWarps * 32) check_union_if_overflow_kern
 }
 
 // ---- sort_by_size ---------------------------------------------------------
-__global__ void label_range_kernel(const int64_t *__restrict__ labels, int64_t n, long long *__restrict__ out) {
+// Range and count of the nonzero labels: per block in shared memory, then
+// one set of atomics per block.
+__global__ void __launch_bounds__(256) label_range_kernel(const int64_t *__restrict__ labels, int64_t n,
+                                                          long long *__restrict__ out) {
+    __shared__ long long s_lo[8], s_hi[8];
+    __shared__ unsigned long long s_nz[8];
     long long lo = LLONG_MAX, hi = LLONG_MIN;
     unsigned long long nz = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -268,10 +273,24 @@ __global__ void label_range_kernel(const int64_t *__restrict__ labels, int64_t n
         lo = l2 < lo ? l2 : lo;
         hi = h2 > hi ? h2 : hi;
     }
-    if ((threadIdx.x & 31) == 0 && nz) {
-        atomicMin(&out[0], lo);
-        atomicMax(&out[1], hi);
-        atomicAdd((unsigned long long *)&out[2], nz);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_lo[w] = lo;
+        s_hi[w] = hi;
+        s_nz[w] = nz;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+            lo = s_lo[k] < lo ? s_lo[k] : lo;
+            hi = s_hi[k] > hi ? s_hi[k] : hi;
+            nz += s_nz[k];
+        }
+        if (nz) {
+            atomicMin(&out[0], lo);
+            atomicMax(&out[1], hi);
+            atomicAdd((unsigned long long *)&out[2], nz);
+        }
     }
 }
 
@@ -362,9 +381,8 @@ __global__ void new_label_kernel(const uint64_t *__restrict__ keys, int64_t k, i
 
 // ---- sort_by_size for label ranges of up to kOrderSmall values -------------
 // One pass counts sizes and first occurrences per label value (lo..lo+r-1);
-// one block orders the clusters by (size descending, first occurrence
-// ascending) with a bitonic sort in shared memory and writes the new label
-// of every value; one pass applies it.
+// one kernel ranks the clusters by (size descending, first occurrence
+// ascending) and writes the new label of every value; one pass applies it.
 constexpr int kOrderSmall = 4096;
 
 __global__ void init_count_first_kernel(int32_t *__restrict__ cnt, int32_t *__restrict__ first, int64_t r) {
@@ -392,58 +410,43 @@ __global__ void count_first_dense_kernel(const int64_t *__restrict__ labels, int
     }
 }
 
-__global__ void __launch_bounds__(1024) order_small_kernel(const int32_t *__restrict__ cnt,
-                                                           const int32_t *__restrict__ first, int r, int64_t n,
-                                                           int bits_n, int64_t member_cutoff, int64_t max_clusters,
-                                                           int64_t *__restrict__ newlab) {
+// New label of every value: its rank among the used values' keys (size
+// descending, first occurrence ascending; distinct per value).  Every block
+// holds all keys in shared memory; one warp per value counts the keys below
+// its own (the lanes stride over the keys).
+constexpr int kOrderWarps = 8;
+
+__global__ void __launch_bounds__(kOrderWarps * 32) order_small_kernel(
+    const int32_t *__restrict__ cnt, const int32_t *__restrict__ first, int r, int64_t n, int bits_n,
+    int64_t member_cutoff, int64_t max_clusters, int64_t *__restrict__ newlab) {
     __shared__ uint64_t s[kOrderSmall];
     __shared__ int s_k;
-    int m = 1;
-    while (m < r) m <<= 1;
     if (threadIdx.x == 0) s_k = 0;
     __syncthreads();
     int local = 0;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-        const bool used = i < r && cnt[i] > 0;
-        // ascending key = size descending, then first occurrence (distinct
-        // per value, so the order is total)
+    for (int i = threadIdx.x; i < r; i += blockDim.x) {
+        const bool used = cnt[i] > 0;
         s[i] = used ? (((uint64_t)(n - cnt[i]) << bits_n) | (uint64_t)first[i]) : ~0ull;
         local += used;
-        if (i < r) newlab[i] = 0;
     }
-    atomicAdd(&s_k, local);
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(&s_k, local);
     __syncthreads();
-    for (int k = 2; k <= m; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = threadIdx.x; i < m; i += blockDim.x) {
-                const int p = i ^ j;
-                if (p > i) {
-                    const uint64_t a = s[i], b = s[p];
-                    if ((a > b) == ((i & k) == 0)) {
-                        s[i] = b;
-                        s[p] = a;
-                    }
-                }
-            }
-            __syncthreads();
-        }
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * kOrderWarps + (threadIdx.x >> 5);
+    if (i >= r) return;
+    const uint64_t key = s[i];
+    int below = 0;
+    for (int j = lane; j < r; j += 32) below += s[j] < key;
+    below = __reduce_add_sync(0xffffffffu, below);
+    if (lane != 0) return;
+    if (key == ~0ull) {  // value not used
+        newlab[i] = 0;
+        return;
     }
-    const int k = s_k;
-    const int64_t maxc = max_clusters < 0 ? k : max_clusters;
-    // rank of every used value: its position in the sorted keys, found by
-    // binary search of its own key (keys are distinct)
-    for (int i = threadIdx.x; i < r; i += blockDim.x) {
-        if (cnt[i] <= 0) continue;
-        const uint64_t key = ((uint64_t)(n - cnt[i]) << bits_n) | (uint64_t)first[i];
-        int lo_q = 0, hi_q = k;
-        while (lo_q < hi_q) {
-            const int mid = (lo_q + hi_q) >> 1;
-            if (s[mid] < key) lo_q = mid + 1;
-            else hi_q = mid;
-        }
-        const int64_t rank = lo_q + 1;  // cluster_count in the reference loop
-        newlab[i] = rank > maxc ? 0 : ((int64_t)cnt[i] >= member_cutoff ? rank : 0);
-    }
+    const int64_t maxc = max_clusters < 0 ? s_k : max_clusters;
+    const int64_t rank = below + 1;  // cluster_count in the reference loop
+    newlab[i] = rank > maxc ? 0 : ((int64_t)cnt[i] >= member_cutoff ? rank : 0);
 }
 
 __global__ void apply_dense_kernel(int64_t *__restrict__ labels, int64_t n, int64_t lo,
@@ -644,8 +647,8 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64
         CNN_LAUNCH_CHECK(ctx);
         count_first_dense_kernel<<<blocks_for(n), 256, 0, st>>>(labels, n, lo, cnt, first);
         CNN_LAUNCH_CHECK(ctx);
-        order_small_kernel<<<1, 1024, 0, st>>>(cnt, first, r, n, bits_for_fit(n), member_cutoff, max_clusters,
-                                               newlab);
+        order_small_kernel<<<(unsigned)((r + kOrderWarps - 1) / kOrderWarps), kOrderWarps * 32, 0, st>>>(
+            cnt, first, r, n, bits_for_fit(n), member_cutoff, max_clusters, newlab);
         CNN_LAUNCH_CHECK(ctx);
         apply_dense_kernel<<<blocks_for(n), 256, 0, st>>>(labels, n, lo, newlab);
         CNN_LAUNCH_CHECK(ctx);

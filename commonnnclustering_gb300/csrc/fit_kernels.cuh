@@ -243,12 +243,20 @@ __global__ void __launch_bounds__(kCheckWarps * 32, CNN_CHECK_MIN_BLOCKS) check_
 }
 
 // Full path compression and per-component minimum point index.
+// Neighbouring internal indices mostly share a root: lanes with the same
+// root combine their minimum first and issue one atomic.
 __global__ void root_min_kernel(int64_t n, const uint8_t *__restrict__ node, int32_t *__restrict__ parent,
                                 const int32_t *__restrict__ perm, int32_t *__restrict__ comp_min) {
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        if (!node[p]) continue;
-        const int32_t r = uf_find(parent, (int32_t)p);
-        atomicMin(&comp_min[r], perm[p]);
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+        const int64_t p = base + lane;
+        const bool is_node = p < n && node[p];
+        const int32_t r = is_node ? uf_find(parent, (int32_t)p) : -1;
+        int32_t v = is_node ? perm[p] : INT_MAX;
+        const unsigned peers = __match_any_sync(0xffffffffu, r);
+        v = __reduce_min_sync(peers, v);
+        if (is_node && lane == __ffs(peers) - 1) atomicMin(&comp_min[r], v);
     }
 }
 

@@ -132,12 +132,17 @@ __global__ void extent_partial_kernel(const double *__restrict__ x, int64_t n, i
 struct GridGeom {
     double lo[3];
     double h;
+    double inv_h;      // 1 / h, rounded: cell coordinates are a monotone function of x
     int32_t g[3];      // cells per dimension (1 for unused dimensions)
     int64_t ncells;    // g0*g1*g2; bucket ncells holds non-finite points
 };
 
-__device__ __forceinline__ int32_t cell_coord(double v, double lo, double h, int32_t g) {
-    double c = floor(__ddiv_rn(__dsub_rn(v, lo), h));
+// floor((v - lo) / h) with the quotient taken as a product by the rounded
+// reciprocal: still monotone in v, and two values less than R apart land in
+// cells at most one apart (h exceeds R by a relative 1e-6, far above the
+// few ulps of relative rounding on (v - lo) / h for grids of <= 64M cells)
+__device__ __forceinline__ int32_t cell_coord(double v, double lo, double inv_h, int32_t g) {
+    double c = floor(__dmul_rn(__dsub_rn(v, lo), inv_h));
     if (!(c >= 0.0)) c = 0.0;
     if (c > (double)(g - 1)) c = (double)(g - 1);
     return (int32_t)c;
@@ -157,7 +162,7 @@ __global__ void cell_assign_kernel(const double *__restrict__ x, int64_t n, int 
             id = geo.ncells;
         } else {
             int32_t c[3] = {0, 0, 0};
-            for (int k = 0; k < d; ++k) c[k] = cell_coord(x[i * d + k], geo.lo[k], geo.h, geo.g[k]);
+            for (int k = 0; k < d; ++k) c[k] = cell_coord(x[i * d + k], geo.lo[k], geo.inv_h, geo.g[k]);
             id = (int64_t)c[0] + (int64_t)geo.g[0] * ((int64_t)c[1] + (int64_t)geo.g[1] * c[2]);
         }
         cell_of[i] = (int32_t)id;
@@ -1027,6 +1032,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
             h *= 1.25;
         }
         geo.h = h;
+        geo.inv_h = 1.0 / h;
         for (int k = 0; k < 3; ++k) geo.lo[k] = k < d ? lo[k] : 0.0;
         geo.ncells = (int64_t)geo.g[0] * geo.g[1] * geo.g[2];
         if (geo.ncells >= 0x7ffffff0LL) use_grid = false;
