@@ -41,6 +41,11 @@ namespace cnn {
 
 namespace {
 
+// Upper bound of the pivot groups that order the rows for tile pruning.  The
+// pivots are every (n / groups)-th point: too few of them leave natural
+// clusters without a pivot and the blocks loose; each costs n x d FMAs.
+constexpr int64_t kMaxGroups = 256;
+
 constexpr int kTM = 128;              // tile rows (M) = tile columns (N)
 constexpr int kKB = 64;               // K block: 64 bf16 = 128 bytes per row
 constexpr int kStages = 2;
@@ -967,7 +972,7 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     const bool prune = d <= 128 && n >= 8 * kTM;
     int n_groups = 1;
     if (prune) {
-        n_groups = (int)std::max<int64_t>(1, std::min<int64_t>({512, n / 1024, 98304 / (4 * ((d + 3) / 4 * 4))}));
+        n_groups = (int)std::max<int64_t>(1, std::min<int64_t>({kMaxGroups, n / 1024, 98304 / (4 * ((d + 3) / 4 * 4))}));
         CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(uint64_t) * (size_t)n));
         uint64_t *pkeys = ctx->scratch_a.as<uint64_t>();
         const size_t psmem = sizeof(float) * (size_t)n_groups * ((d + 3) / 4 * 4 + 1);
