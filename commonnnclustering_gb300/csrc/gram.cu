@@ -544,6 +544,116 @@ __global__ void gram_prep_kernel(const double *__restrict__ x, int64_t n_rows, i
     }
 }
 
+// One block per 128-row block of the padded internal order: every row split
+// as in gram_prep_kernel (float64 centring, exact residuals), its float32
+// norm, the block's norm maxima, and -- for the tile pruning -- the block's
+// float32 centroid and a radius that bounds the distance of every point of
+// the block to it: the float32 evaluation from the float32 coordinates,
+// inflated by its rounding ((d + 8) 2^-23 relative) and by the conversion
+// of the coordinates (2^-24 of the largest norm, taken twice).
+constexpr int kPrepWarps = 8;
+
+__global__ void __launch_bounds__(kPrepWarps * 32) gram_prep_bounds_kernel(
+    const double *__restrict__ x, int64_t n_rows, int d, int dp, const double *__restrict__ mean,
+    const int32_t *__restrict__ perm, __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ mid,
+    __nv_bfloat16 *__restrict__ lo, float *__restrict__ norm2, unsigned *__restrict__ blk_norm_bits,
+    unsigned *__restrict__ blk_norm2_bits, int bounds, float *__restrict__ centroid, float *__restrict__ radius) {
+    extern __shared__ float s_cf[];  // [kTM][d + 1] float32 coordinates, then [d] centroid
+    __shared__ float s_max[kPrepWarps][2];
+    __shared__ int s_used[kPrepWarps];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int ld = d + 1;
+    float *s_cent = s_cf + kTM * ld;
+    const int64_t I = blockIdx.x;
+    float wmax = 0.f, wmax2 = 0.f;
+    int used = 0;
+    for (int r = w; r < kTM; r += kPrepWarps) {
+        const int64_t i = I * kTM + r;
+        const int64_t src = i < n_rows ? perm[i] : -1;
+        double s2 = 0;
+        for (int k = lane; k < dp; k += 32) {
+            __nv_bfloat16 bh = __float2bfloat16_rn(0.f), bm = bh, bl = bh;
+            float cf = 0.f;
+            if (k < d && src >= 0) {
+                // residuals in float64 are exact (Sterbenz): c - hi - mid - lo is
+                // the rounding of the last bf16 step, at most ~2^-24 |c|
+                const double c = x[src * d + k] - mean[k];
+                bh = __float2bfloat16_rn((float)c);
+                const double r1 = c - (double)__bfloat162float(bh);
+                bm = __float2bfloat16_rn((float)r1);
+                const double r2 = r1 - (double)__bfloat162float(bm);
+                bl = __float2bfloat16_rn((float)r2);
+                s2 += c * c;
+                cf = (float)c;
+            }
+            if (i < n_rows) {
+                hi[i * dp + k] = bh;
+                mid[i * dp + k] = bm;
+                lo[i * dp + k] = bl;
+            }
+            if (k < d) s_cf[r * ld + k] = cf;
+        }
+        for (int o = 16; o > 0; o >>= 1) s2 += __shfl_down_sync(0xffffffffu, s2, o);
+        if (lane == 0) {
+            if (i < n_rows) norm2[i] = src < 0 ? INFINITY : (float)s2;
+            if (src >= 0) {
+                wmax = fmaxf(wmax, sqrtf((float)s2) * (1.f + 1e-6f));
+                wmax2 = fmaxf(wmax2, (float)s2 * (1.f + 1e-6f));
+                ++used;
+            }
+        }
+        if (lane == 0 && src < 0) s_cf[r * ld + d] = -1.f;  // marks an empty row
+        else if (lane == 0) s_cf[r * ld + d] = 1.f;
+    }
+    if (lane == 0) {
+        s_max[w][0] = wmax;
+        s_max[w][1] = wmax2;
+        s_used[w] = used;
+    }
+    __syncthreads();
+    float bmax = 0.f, bmax2 = 0.f;
+    int rows = 0;
+    for (int k = 0; k < kPrepWarps; ++k) {
+        bmax = fmaxf(bmax, s_max[k][0]);
+        bmax2 = fmaxf(bmax2, s_max[k][1]);
+        rows += s_used[k];
+    }
+    if (threadIdx.x == 0) {
+        blk_norm_bits[I] = __float_as_uint(bmax);
+        blk_norm2_bits[I] = __float_as_uint(bmax2);
+    }
+    if (!bounds) return;
+    // centroid of the block's points (any reference point serves)
+    for (int k = threadIdx.x; k < d; k += blockDim.x) {
+        float c = 0.f;
+        for (int r = 0; r < kTM; ++r)
+            if (s_cf[r * ld + d] > 0.f) c += s_cf[r * ld + k];
+        c = rows > 0 ? c / (float)rows : 0.f;
+        s_cent[k] = c;
+        centroid[I * d + k] = c;
+    }
+    __syncthreads();
+    float m = 0.f;
+    for (int r = threadIdx.x; r < kTM; r += blockDim.x) {
+        if (!(s_cf[r * ld + d] > 0.f)) continue;
+        float s = 0.f;
+        for (int k = 0; k < d; ++k) {
+            const float t = s_cf[r * ld + k] - s_cent[k];
+            s = fmaf(t, t, s);
+        }
+        m = fmaxf(m, s);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    __syncthreads();
+    if (lane == 0) s_max[w][0] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < kPrepWarps; ++k) m = fmaxf(m, s_max[k][0]);
+        const float rel = 1.f + (float)(d + 8) * 0x1p-23f;
+        radius[I] = sqrtf(m) * rel + 0x1p-22f * bmax + 1e-30f;
+    }
+}
+
 // ---- tile pruning ---------------------------------------------------------------
 // Points are grouped by their nearest pivot (float32, centred coordinates;
 // any grouping gives the same result, compact groups let more tiles go) and
@@ -649,53 +759,6 @@ __global__ void padded_perm_kernel(const uint64_t *__restrict__ keys, int64_t n,
         const int g = (int)(k >> bits_n);
         perm[pstart[g] + (p - start[g])] = (int32_t)(k & mask);
     }
-}
-
-// Per row block (padded internal order): centroid and radius of its points
-// (empty rows skipped; every block holds at least one point).  Float32
-// values rounded outward enough for the pruning test below.
-__global__ void block_bounds_kernel(const double *__restrict__ x, int64_t n_rows, int64_t n, int d,
-                                    const double *__restrict__ mean, const int32_t *__restrict__ perm,
-                                    float *__restrict__ centroid, float *__restrict__ radius) {
-    __shared__ double s_c[128];
-    __shared__ double s_r[256];
-    __shared__ int32_t s_src[kTM];
-    __shared__ int s_rows;
-    const int64_t I = blockIdx.x;
-    const int64_t r0 = I * kTM, r1 = min(n_rows, r0 + kTM);
-    if (threadIdx.x == 0) {
-        int m = 0;
-        for (int64_t r = r0; r < r1; ++r)
-            if (perm[r] >= 0) s_src[m++] = perm[r];
-        s_rows = m;
-    }
-    __syncthreads();
-    const int rows = s_rows;
-    for (int k = threadIdx.x; k < d; k += blockDim.x) {
-        double c = 0;
-        for (int r = 0; r < rows; ++r) c += x[(int64_t)s_src[r] * d + k] - mean[k];
-        s_c[k] = rows > 0 ? c / rows : 0.0;
-        centroid[I * d + k] = (float)s_c[k];
-    }
-    __syncthreads();
-    double m = 0;
-    for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-        double s = 0;
-        const int64_t src = s_src[r];
-        for (int k = 0; k < d; ++k) {
-            // distance to the float32 centroid actually used in the test
-            const double t = (x[src * d + k] - mean[k]) - (double)(float)s_c[k];
-            s += t * t;
-        }
-        m = fmax(m, s);
-    }
-    s_r[threadIdx.x] = m;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) s_r[threadIdx.x] = fmax(s_r[threadIdx.x], s_r[threadIdx.x + w]);
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) radius[I] = (float)(sqrt(s_r[0]) * (1.0 + 1e-6) + 1e-30);
 }
 
 // Can blocks I and J (J >= I) hold a pair within R?  |c_I - c_J| - rho_I -
@@ -1026,12 +1089,6 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     float *norm2 = ctx->gram_aux.as<float>();
     unsigned *blk_norm_bits = reinterpret_cast<unsigned *>(norm2 + n_rows);
     unsigned *blk_norm2_bits = blk_norm_bits + nblk;
-    CNN_CUDA(ctx, cudaMemsetAsync(blk_norm_bits, 0, sizeof(unsigned) * 2 * (size_t)nblk, st));
-    gram_prep_kernel<<<grid_for(n_rows * 32, 256), 256, 0, st>>>(
-        ctx->x, n_rows, n, d, dp, colsum, perm, ctx->gram_hi.as<__nv_bfloat16>(), ctx->gram_mid.as<__nv_bfloat16>(),
-        ctx->gram_lo.as<__nv_bfloat16>(), norm2, blk_norm_bits, blk_norm2_bits);
-    CNN_LAUNCH_CHECK(ctx);
-
     // the list of block pairs (I, J >= I) that can hold a pair within R
     const double Rsearch = (metric == CNN_METRIC_EUCLIDEAN ? radius_cutoff : sqrt(radius_cutoff)) * (1.0 + 1e-6);
     CNN_TRY(ctx->ensure(ctx->gram_blocks, sizeof(float) * (size_t)nblk * (d + 1) +
@@ -1042,10 +1099,21 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     int64_t *row_off = reinterpret_cast<int64_t *>(
         (reinterpret_cast<uintptr_t>(row_count + nblk + 1) + 15) & ~uintptr_t(15));
     const float Rf = prune ? (float)Rsearch : INFINITY;
-    if (prune) {
-        block_bounds_kernel<<<(unsigned)nblk, 256, 0, st>>>(ctx->x, n_rows, n, d, colsum, perm, centroid, bradius);
+    if (prune) {  // n_dim <= 128: the block's coordinates fit in shared memory
+        const size_t psmem = sizeof(float) * ((size_t)kTM * (d + 1) + d);
+        CNN_CUDA(ctx, cudaFuncSetAttribute(gram_prep_bounds_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)psmem));
+        gram_prep_bounds_kernel<<<(unsigned)nblk, kPrepWarps * 32, psmem, st>>>(
+            ctx->x, n_rows, d, dp, colsum, perm, ctx->gram_hi.as<__nv_bfloat16>(), ctx->gram_mid.as<__nv_bfloat16>(),
+            ctx->gram_lo.as<__nv_bfloat16>(), norm2, blk_norm_bits, blk_norm2_bits, 1, centroid, bradius);
         CNN_LAUNCH_CHECK(ctx);
     } else {
+        CNN_CUDA(ctx, cudaMemsetAsync(blk_norm_bits, 0, sizeof(unsigned) * 2 * (size_t)nblk, st));
+        gram_prep_kernel<<<grid_for(n_rows * 32, 256), 256, 0, st>>>(
+            ctx->x, n_rows, n, d, dp, colsum, perm, ctx->gram_hi.as<__nv_bfloat16>(),
+            ctx->gram_mid.as<__nv_bfloat16>(), ctx->gram_lo.as<__nv_bfloat16>(), norm2, blk_norm_bits,
+            blk_norm2_bits);
+        CNN_LAUNCH_CHECK(ctx);
         CNN_CUDA(ctx, cudaMemsetAsync(centroid, 0, sizeof(float) * (size_t)nblk * (d + 1), st));
     }
     const unsigned lgrid = (unsigned)((nblk + kListRows - 1) / kListRows);

@@ -188,19 +188,6 @@ __global__ void place_kernel(const int32_t *__restrict__ cell_of, const int32_t 
 }
 
 // ---- grid search -----------------------------------------------------------
-// Work item = (cell, up to kItemQueries consecutive queries of that cell).
-// The block packs the cell's 9 candidate runs (3x3 (y,z) neighbours, each
-// three x-cells long and contiguous in internal order) into shared-memory
-// tiles of kGridTile candidates; each warp owns kQueriesPerWarp queries
-// held in registers and tests every packed candidate of the tile against
-// all of them (lanes over candidates, one shared load per candidate).
-// Packed order = run order = ascending internal index, so each query's
-// hits come out sorted.
-constexpr int kGridWarps = 8;
-constexpr int kQueriesPerWarp = 4;
-constexpr int kItemQueries = kGridWarps * kQueriesPerWarp;  // 32
-constexpr int kGridTile = 1024;
-
 // Float64 predicate on rows of the original-order coordinate array.
 __device__ __forceinline__ bool exact_rows(const double *__restrict__ x, int d, int32_t ia, int32_t ib,
                                            const SearchParams &sp) {
@@ -282,149 +269,6 @@ __global__ void compact_rows_kernel(int64_t n, const int64_t *__restrict__ qslot
 // slots fit in memory.
 constexpr int kCount = 0, kFill = 1, kSlots = 2;
 
-template <int kMode>
-__global__ void __launch_bounds__(kGridWarps * 32) grid_search_kernel(
-    const int2 *__restrict__ items, const double *__restrict__ x, int d, GridGeom geo, SearchParams sp,
-    const int32_t *__restrict__ perm, const int64_t *__restrict__ cell_start, const float4 *__restrict__ xf4,
-    int32_t *__restrict__ deg, const int64_t *__restrict__ row_off, int32_t *__restrict__ cols,
-    unsigned long long *__restrict__ counters, int64_t *__restrict__ qslot) {
-    __shared__ float4 s_xf[kGridTile];
-    __shared__ int32_t s_j[kGridTile];
-    __shared__ int64_t s_rs[9];
-    __shared__ int32_t s_cum[10];
-    __shared__ int32_t s_nruns;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int2 item = items[blockIdx.x];
-    const int32_t cid = item.x;
-    const int64_t q0 = item.y;
-    const int64_t qend = cell_start[cid + 1];
-    if (threadIdx.x == 0) {
-        const int32_t cx = cid % geo.g[0];
-        const int32_t cy = (cid / geo.g[0]) % geo.g[1];
-        const int32_t cz = cid / (geo.g[0] * geo.g[1]);
-        const int32_t xlo = cx > 0 ? cx - 1 : 0;
-        const int32_t xhi = cx + 1 < geo.g[0] ? cx + 1 : geo.g[0] - 1;
-        int nr = 0;
-        int32_t cum = 0;
-        for (int dz = -1; dz <= 1; ++dz) {
-            const int32_t z = cz + dz;
-            if (z < 0 || z >= geo.g[2]) continue;
-            for (int dy = -1; dy <= 1; ++dy) {
-                const int32_t y = cy + dy;
-                if (y < 0 || y >= geo.g[1]) continue;
-                const int64_t row = (int64_t)geo.g[0] * ((int64_t)y + (int64_t)geo.g[1] * z);
-                const int64_t rs = cell_start[row + xlo];
-                const int64_t re = cell_start[row + xhi + 1];
-                if (re <= rs) continue;
-                s_rs[nr] = rs;
-                s_cum[nr] = cum;
-                cum += (int32_t)(re - rs);
-                ++nr;
-            }
-        }
-        s_cum[nr] = cum;
-        s_nruns = nr;
-    }
-    __syncthreads();
-    const int nruns = s_nruns;
-    const int32_t total = s_cum[nruns];
-
-    // this warp's queries: kQueriesPerWarp consecutive ones, so that short
-    // items leave whole warps idle instead of spreading one query per warp.
-    // Missing queries get +inf coordinates: they never match and are never
-    // ambiguous, so the inner loop needs no per-query branch.
-    int64_t q[kQueriesPerWarp];
-    float4 qf[kQueriesPerWarp];
-    int64_t wpos[kQueriesPerWarp];
-    int32_t cnt[kQueriesPerWarp];
-#pragma unroll
-    for (int k = 0; k < kQueriesPerWarp; ++k) {
-        q[k] = q0 + (int64_t)wid * kQueriesPerWarp + k;
-        const bool ok = q[k] < qend;
-        qf[k] = ok ? xf4[q[k]] : make_float4(INFINITY, INFINITY, INFINITY, 0.f);
-        if (kMode == kFill) wpos[k] = ok ? row_off[q[k]] : 0;
-        else if (kMode == kSlots) wpos[k] = ok ? row_off[cid] + (q[k] - cell_start[cid]) * (int64_t)total : 0;
-        else wpos[k] = 0;
-        if (kMode == kSlots && ok && lane == 0) qslot[q[k]] = wpos[k];
-        cnt[k] = 0;
-        if (!ok) q[k] = -1;
-    }
-    const bool warp_has_work = q[0] >= 0;
-    const unsigned lt = (1u << lane) - 1u;
-    unsigned long long n_exact = 0;
-    for (int32_t t0 = 0; t0 < total; t0 += kGridTile) {
-        const int32_t tlen = min(kGridTile, total - t0);
-        const int32_t tpad = (tlen + 31) & ~31;
-        __syncthreads();
-        // pack: warp w copies runs w, w+8, ... (their part inside this tile)
-        for (int r = wid; r < nruns; r += kGridWarps) {
-            const int32_t lo = max(s_cum[r], t0), hi = min(s_cum[r + 1], t0 + tlen);
-            for (int32_t pos = lo + lane; pos < hi; pos += 32) {
-                const int32_t j = (int32_t)(s_rs[r] + (pos - s_cum[r]));
-                s_j[pos - t0] = j;
-                s_xf[pos - t0] = xf4[j];
-            }
-        }
-        for (int32_t t = tlen + threadIdx.x; t < tpad; t += blockDim.x) {  // +inf never matches
-            s_j[t] = -1;
-            s_xf[t] = make_float4(INFINITY, INFINITY, INFINITY, 0.f);
-        }
-        __syncthreads();
-        if (!warp_has_work) continue;
-        for (int32_t c0 = 0; c0 < tpad; c0 += 32) {
-            const int32_t t = c0 + lane;
-            const float4 cf = s_xf[t];
-            bool in[kQueriesPerWarp], amb[kQueriesPerWarp];
-            bool any_amb = false;
-#pragma unroll
-            for (int k = 0; k < kQueriesPerWarp; ++k) {
-                const float ex = qf[k].x - cf.x, ey = qf[k].y - cf.y, ez = qf[k].z - cf.z;
-                const float sf = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
-                in[k] = sf <= sp.thr_in;
-                amb[k] = !in[k] && sf <= sp.thr_out;
-                any_amb |= amb[k];
-            }
-            if (__any_sync(0xffffffffu, any_amb)) {  // rare: decide those pairs in float64
-#pragma unroll
-                for (int k = 0; k < kQueriesPerWarp; ++k) {
-                    if (amb[k]) {
-                        in[k] = exact_rows(x, d, perm[q[k]], perm[s_j[t]], sp);
-                        ++n_exact;
-                    }
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < kQueriesPerWarp; ++k) {
-                if (kMode != kCount) {
-                    const unsigned hit = __ballot_sync(0xffffffffu, in[k]);
-                    if (in[k]) cols[wpos[k] + cnt[k] + __popc(hit & lt)] = s_j[t];
-                    cnt[k] += __popc(hit);
-                } else {
-                    cnt[k] += in[k];  // per-lane count, summed over the warp at the end
-                }
-            }
-        }
-    }
-    if (kMode != kFill) {
-        if (kMode == kCount) {
-#pragma unroll
-            for (int k = 0; k < kQueriesPerWarp; ++k)
-                for (int o = 16; o > 0; o >>= 1) cnt[k] += __shfl_down_sync(0xffffffffu, cnt[k], o);
-        }
-        if (lane == 0) {
-#pragma unroll
-            for (int k = 0; k < kQueriesPerWarp; ++k)
-                if (q[k] >= 0) deg[q[k]] = cnt[k];
-        }
-        for (int o = 16; o > 0; o >>= 1) n_exact += __shfl_down_sync(0xffffffffu, n_exact, o);
-        if (lane == 0 && n_exact) atomicAdd(&counters[0], n_exact);
-        if (threadIdx.x == 0) {
-            const int64_t nq = (qend < q0 + kItemQueries ? qend : q0 + kItemQueries) - q0;
-            atomicAdd(&counters[1], (unsigned long long)total * (unsigned long long)nq);
-        }
-    }
-}
-
 // ---- warp-granular grid search ---------------------------------------------
 // Work unit = (cell, up to kUnitQueries consecutive queries of that cell), one
 // warp each, no block-wide staging: the warp reads its cell's 9 candidate
@@ -440,10 +284,10 @@ __global__ void __launch_bounds__(kGridWarps * 32) grid_search_kernel(
 #endif
 constexpr int kUnitQueries = CNN_UNIT_QUERIES;
 constexpr int kUnitWarps = 8;
-#ifndef CNN_GRID_UNITS
-#define CNN_GRID_UNITS 1
+#ifndef CNN_UNIT_SUB
+#define CNN_UNIT_SUB 1  // two steps per iteration measured slower (register pressure)
 #endif
-constexpr int kGridPer = CNN_GRID_UNITS ? kUnitQueries : kItemQueries;  // queries per work item
+constexpr int kUnitSub = CNN_UNIT_SUB;  // 32-candidate steps per loop iteration
 
 #ifndef CNN_UNIT_MIN_BLOCKS
 #define CNN_UNIT_MIN_BLOCKS 4  // 64 registers: four blocks of eight warps per SM
@@ -517,46 +361,63 @@ __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_uni
     }
     const unsigned lt = (1u << lane) - 1u;
     unsigned long long n_exact = 0;
-    // this lane's run: t in [lo, hi) of the concatenation maps to j = base + t;
-    // t only grows, so the run index only moves forward (empty runs skipped)
-    int r = 0;
-    int32_t hi = s_cum[wid][1], base = s_rs[wid][0];
-    for (int32_t t = lane; t - lane < total; t += 32) {
-        while (t >= hi && r < 8) {
-            ++r;
-            base = s_rs[wid][r] - hi;
-            hi = s_cum[wid][r + 1];
-        }
-        const bool valid = t < total;
-        const int32_t j = base + t;
-        const float4 cf = valid ? xf4[j] : make_float4(INFINITY, INFINITY, INFINITY, 0.f);  // +inf never matches
-        bool in[kUnitQueries], amb[kUnitQueries];
+    // kUnitSub steps of 32 candidates per iteration (lane's candidates t and
+    // t + 32, ...).  Each step's lane keeps its run: t in [.., hi) of the
+    // concatenation maps to j = base + t; t only grows, so the run index only
+    // moves forward (empty runs skipped)
+    int r[kUnitSub];
+    int32_t hi[kUnitSub], base[kUnitSub];
+#pragma unroll
+    for (int u = 0; u < kUnitSub; ++u) {
+        r[u] = 0;
+        hi[u] = s_cum[wid][1];
+        base[u] = s_rs[wid][0];
+    }
+    for (int32_t t0 = lane; t0 - lane < total; t0 += 32 * kUnitSub) {
+        int32_t j[kUnitSub];
+        bool in[kUnitSub][kUnitQueries], amb[kUnitSub][kUnitQueries];
         bool any_amb = false;
 #pragma unroll
-        for (int k = 0; k < kUnitQueries; ++k) {
-            const float ex = qx[k] - cf.x, ey = qy[k] - cf.y, ez = qz[k] - cf.z;
-            const float sf = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
-            in[k] = sf <= sp.thr_in;
-            amb[k] = !in[k] && sf <= sp.thr_out;
-            any_amb |= amb[k];
+        for (int u = 0; u < kUnitSub; ++u) {
+            const int32_t t = t0 + 32 * u;
+            while (t >= hi[u] && r[u] < 8) {
+                ++r[u];
+                base[u] = s_rs[wid][r[u]] - hi[u];
+                hi[u] = s_cum[wid][r[u] + 1];
+            }
+            j[u] = base[u] + t;
+            const float4 cf = t < total ? xf4[j[u]] : make_float4(INFINITY, INFINITY, INFINITY, 0.f);  // +inf never matches
+#pragma unroll
+            for (int k = 0; k < kUnitQueries; ++k) {
+                const float ex = qx[k] - cf.x, ey = qy[k] - cf.y, ez = qz[k] - cf.z;
+                const float sf = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                in[u][k] = sf <= sp.thr_in;
+                amb[u][k] = !in[u][k] && sf <= sp.thr_out;
+                any_amb |= amb[u][k];
+            }
         }
         if (__any_sync(0xffffffffu, any_amb)) {  // rare: decide those pairs in float64
 #pragma unroll
-            for (int k = 0; k < kUnitQueries; ++k) {
-                if (amb[k]) {
-                    in[k] = exact_rows(x, d, perm[qi[k]], perm[j], sp);
-                    ++n_exact;
+            for (int u = 0; u < kUnitSub; ++u)
+#pragma unroll
+                for (int k = 0; k < kUnitQueries; ++k) {
+                    if (amb[u][k]) {
+                        in[u][k] = exact_rows(x, d, perm[qi[k]], perm[j[u]], sp);
+                        ++n_exact;
+                    }
                 }
-            }
         }
 #pragma unroll
         for (int k = 0; k < kUnitQueries; ++k) {
-            if (kMode != kCount) {
-                const unsigned hit = __ballot_sync(0xffffffffu, in[k]);
-                if (in[k]) rowp[k][cnt[k] + __popc(hit & lt)] = j;
-                cnt[k] += __popc(hit);
-            } else {
-                cnt[k] += in[k];  // per-lane count, summed over the warp at the end
+#pragma unroll
+            for (int u = 0; u < kUnitSub; ++u) {  // step u's candidates follow step u - 1's
+                if (kMode != kCount) {
+                    const unsigned hit = __ballot_sync(0xffffffffu, in[u][k]);
+                    if (in[u][k]) rowp[k][cnt[k] + __popc(hit & lt)] = j[u];
+                    cnt[k] += __popc(hit);
+                } else {
+                    cnt[k] += in[u][k];  // per-lane count, summed over the warp at the end
+                }
             }
         }
     }
@@ -1068,7 +929,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         // work items: (cell, first query) for every 32 queries of a cell
         CNN_TRY(ctx->ensure(ctx->io_a, sizeof(int32_t) * (size_t)(geo.ncells + 1)));
         CNN_TRY(ctx->ensure(ctx->io_b, sizeof(int64_t) * (size_t)(geo.ncells + 1)));
-        item_count_kernel<kGridPer><<<std::min<unsigned>(grid_for(geo.ncells, 256), 152u * 16u), 256, 0, st>>>(
+        item_count_kernel<kUnitQueries><<<std::min<unsigned>(grid_for(geo.ncells, 256), 152u * 16u), 256, 0, st>>>(
             ctx->cell_start.as<int64_t>(), geo.ncells, ctx->io_a.as<int32_t>());
         CNN_LAUNCH_CHECK(ctx);
         CNN_CUDA(ctx, cudaMemsetAsync(ctx->io_a.as<int32_t>() + geo.ncells, 0, sizeof(int32_t), st));
@@ -1096,7 +957,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
             CNN_TRY(ctx->ensure(ctx->grid_qslot, sizeof(int64_t) * (size_t)n));
         }
         CNN_TRY(ctx->ensure(ctx->io_c, sizeof(int2) * (size_t)(nitems > 0 ? nitems : 1)));
-        item_fill_kernel<kGridPer><<<std::min<unsigned>(grid_for(geo.ncells, 256), 152u * 16u), 256, 0, st>>>(
+        item_fill_kernel<kUnitQueries><<<std::min<unsigned>(grid_for(geo.ncells, 256), 152u * 16u), 256, 0, st>>>(
             ctx->cell_start.as<int64_t>(), geo.ncells, ctx->io_b.as<int64_t>(), ctx->io_c.as<int2>());
         CNN_LAUNCH_CHECK(ctx);
         grid_items = nitems;
@@ -1105,28 +966,15 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         stage_begin(ctx, 2);
         CNN_CUDA(ctx, cudaMemsetAsync(deg, 0, sizeof(int32_t) * (size_t)n, st));
         if (nitems > 0 && use_slots) {
-#if CNN_GRID_UNITS
             grid_unit_kernel<kSlots><<<(unsigned)((nitems + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
                 ctx->io_c.as<int2>(), nitems, ctx->x, d, geo, sp, ctx->perm.as<int32_t>(),
                 ctx->cell_start.as<int64_t>(), ctx->xf4.as<float4>(), deg, slot_base,
                 ctx->grid_slot_cols.as<int32_t>(), counters, ctx->grid_qslot.as<int64_t>());
-#else
-            grid_search_kernel<kSlots><<<(unsigned)nitems, kGridWarps * 32, 0, st>>>(
-                ctx->io_c.as<int2>(), ctx->x, d, geo, sp, ctx->perm.as<int32_t>(), ctx->cell_start.as<int64_t>(),
-                ctx->xf4.as<float4>(), deg, slot_base, ctx->grid_slot_cols.as<int32_t>(), counters,
-                ctx->grid_qslot.as<int64_t>());
-#endif
             CNN_LAUNCH_CHECK(ctx);
         } else if (nitems > 0) {
-#if CNN_GRID_UNITS
             grid_unit_kernel<kCount><<<(unsigned)((nitems + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
                 ctx->io_c.as<int2>(), nitems, ctx->x, d, geo, sp, ctx->perm.as<int32_t>(),
                 ctx->cell_start.as<int64_t>(), ctx->xf4.as<float4>(), deg, nullptr, nullptr, counters, nullptr);
-#else
-            grid_search_kernel<kCount><<<(unsigned)nitems, kGridWarps * 32, 0, st>>>(
-                ctx->io_c.as<int2>(), ctx->x, d, geo, sp, ctx->perm.as<int32_t>(), ctx->cell_start.as<int64_t>(),
-                ctx->xf4.as<float4>(), deg, nullptr, nullptr, counters, nullptr);
-#endif
             CNN_LAUNCH_CHECK(ctx);
         }
         n_candidates = hcounts[1];  // every query against its cell's candidate runs
@@ -1175,16 +1023,10 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
                 ctx->cols.as<int32_t>());
             CNN_LAUNCH_CHECK(ctx);
         } else if (grid_items > 0) {
-#if CNN_GRID_UNITS
             grid_unit_kernel<kFill><<<(unsigned)((grid_items + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
                 ctx->io_c.as<int2>(), grid_items, ctx->x, d, geo, sp, ctx->perm.as<int32_t>(),
                 ctx->cell_start.as<int64_t>(), ctx->xf4.as<float4>(), deg, row_off, ctx->cols.as<int32_t>(), counters,
                 nullptr);
-#else
-            grid_search_kernel<kFill><<<(unsigned)grid_items, kGridWarps * 32, 0, st>>>(
-                ctx->io_c.as<int2>(), ctx->x, d, geo, sp, ctx->perm.as<int32_t>(), ctx->cell_start.as<int64_t>(),
-                ctx->xf4.as<float4>(), deg, row_off, ctx->cols.as<int32_t>(), counters, nullptr);
-#endif
             CNN_LAUNCH_CHECK(ctx);
         }
     } else {
