@@ -655,68 +655,110 @@ __global__ void __launch_bounds__(kPrepWarps * 32) gram_prep_bounds_kernel(
 }
 
 // ---- tile pruning ---------------------------------------------------------------
-// Points are grouped by their nearest pivot (float32, centred coordinates;
-// any grouping gives the same result, compact groups let more tiles go) and
+// Points are grouped by their nearest pivot (centred coordinates; any
+// grouping gives the same result, compact groups let more tiles go) and
 // every group starts on a 128-row block boundary, so that no block mixes two
 // groups.  Rows left over at a group's end are empty (no point, infinite
 // norm): they never produce a pair.
 //
-// One thread per point, its coordinates in registers (n_dim <= 4 * kV4,
-// padded with zeros to a multiple of 4); pivots in shared memory as float4 rows
-// read by broadcast.  The score |p|^2 - 2 x.p ranks pivots like |x - p|^2.
-template <int kV4>
+// The score |p|^2 - 2 x.p ranks pivots like |x - p|^2.  Its products run on
+// the tensor cores in bf16 (a grouping heuristic needs no more): one warp
+// takes 16 points at a time as the A operand of mma.sync m16n8k16 (fp32
+// accumulation), the pivots sit in shared memory as the B operand (rows of
+// K = n_dim rounded up to 16, padded by 4 words so the fragment loads hit
+// distinct banks), 8 pivots per MMA column block.  Each thread keeps the best
+// pivot of its two rows over its two columns; the quad then agrees on the
+// minimum (lowest index on ties).
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+constexpr int kPivotMaxK = 128;  // n_dim of the pruned path
+
 __global__ void __launch_bounds__(256) pivot_assign_kernel(const double *__restrict__ x, int64_t n, int d,
                                                            const double *__restrict__ mean, int32_t n_pivots,
                                                            int bits_n, uint64_t *__restrict__ keys) {
-    extern __shared__ float4 s_piv4[];  // [n_pivots][nv4], then |p|^2 per pivot
-    const int nv4 = (d + 3) / 4;
-    float *s_pn = reinterpret_cast<float *>(s_piv4 + (size_t)n_pivots * nv4);
-    float *s_piv = reinterpret_cast<float *>(s_piv4);
+    extern __shared__ uint32_t s_piv[];  // [pad8(n_pivots)][ldw] bf16 pairs, then |p|^2 per pivot
+    const int dk = (d + 15) & ~15, ldw = dk / 2 + 4, ksteps = dk / 16;
+    const int np8 = (n_pivots + 7) & ~7;
+    float *s_pn = reinterpret_cast<float *>(s_piv + (size_t)np8 * ldw);
     const int64_t stride = n / n_pivots;
-    for (int e = threadIdx.x; e < n_pivots * nv4 * 4; e += blockDim.x) {
-        const int kp = e / (nv4 * 4), k = e - kp * nv4 * 4;
-        s_piv[e] = k < d ? (float)(x[(int64_t)kp * stride * d + k] - mean[k]) : 0.f;
+    for (int e = threadIdx.x; e < np8 * (dk / 2); e += blockDim.x) {
+        const int kp = e / (dk / 2), k = 2 * (e - kp * (dk / 2));
+        float v0 = 0.f, v1 = 0.f;
+        if (kp < n_pivots) {
+            const double *row = x + (int64_t)kp * stride * d;
+            if (k < d) v0 = (float)(row[k] - mean[k]);
+            if (k + 1 < d) v1 = (float)(row[k + 1] - mean[k + 1]);
+        }
+        s_piv[kp * ldw + k / 2] = pack_bf16x2(v0, v1);
     }
     __syncthreads();
-    for (int kp = threadIdx.x; kp < n_pivots; kp += blockDim.x) {
-        float s2 = 0.f;
-        for (int k = 0; k < nv4 * 4; ++k) s2 = fmaf(s_piv[kp * nv4 * 4 + k], s_piv[kp * nv4 * 4 + k], s2);
-        s_pn[kp] = s2;
+    for (int kp = threadIdx.x; kp < np8; kp += blockDim.x) {
+        float s2 = 0.f;  // of the bf16 values the products use
+        for (int w = 0; w < dk / 2; ++w) {
+            const __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162 *>(&s_piv[kp * ldw + w]);
+            const float2 f = __bfloat1622float2(v);
+            s2 = fmaf(f.x, f.x, fmaf(f.y, f.y, s2));
+        }
+        s_pn[kp] = kp < n_pivots ? s2 : INFINITY;
     }
     __syncthreads();
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        float4 xv[kV4];
+    const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row0 = warp0 * 16; row0 < n; row0 += nwarps * 16) {
+        const int64_t ra = row0 + g, rb = row0 + g + 8;
+        auto val = [&](int64_t r, int k) -> float {
+            return (r < n && k < d) ? (float)(x[r * d + k] - mean[k]) : 0.f;
+        };
+        uint32_t a[kPivotMaxK / 16][4];
 #pragma unroll
-        for (int v = 0; v < kV4; ++v) {
-            float c[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int k = 4 * v + q;
-                c[q] = k < d ? (float)(x[i * d + k] - mean[k]) : 0.f;
-            }
-            xv[v] = make_float4(-2.f * c[0], -2.f * c[1], -2.f * c[2], -2.f * c[3]);
-        }
-        float best = INFINITY;
-        int32_t bi = 0;
-        for (int kp = 0; kp < n_pivots; ++kp) {
-            const float4 *pv = s_piv4 + (size_t)kp * nv4;
-            float acc = s_pn[kp];
-#pragma unroll
-            for (int v = 0; v < kV4; ++v) {
-                if (v < nv4) {
-                    const float4 p = pv[v];
-                    acc = fmaf(xv[v].x, p.x, acc);
-                    acc = fmaf(xv[v].y, p.y, acc);
-                    acc = fmaf(xv[v].z, p.z, acc);
-                    acc = fmaf(xv[v].w, p.w, acc);
-                }
-            }
-            if (acc < best) {
-                best = acc;
-                bi = kp;
+        for (int ks = 0; ks < kPivotMaxK / 16; ++ks) {
+            if (ks < ksteps) {
+                const int k0 = ks * 16 + tig * 2;
+                a[ks][0] = pack_bf16x2(val(ra, k0), val(ra, k0 + 1));
+                a[ks][1] = pack_bf16x2(val(rb, k0), val(rb, k0 + 1));
+                a[ks][2] = pack_bf16x2(val(ra, k0 + 8), val(ra, k0 + 9));
+                a[ks][3] = pack_bf16x2(val(rb, k0 + 8), val(rb, k0 + 9));
             }
         }
-        keys[i] = ((uint64_t)(uint32_t)bi << bits_n) | (uint64_t)i;
+        float best_a = INFINITY, best_b = INFINITY;
+        int32_t bi_a = 0, bi_b = 0;
+        for (int nt = 0; nt < np8; nt += 8) {
+            float c[4] = {0.f, 0.f, 0.f, 0.f};
+            const uint32_t *prow = s_piv + (size_t)(nt + g) * ldw;
+#pragma unroll
+            for (int ks = 0; ks < kPivotMaxK / 16; ++ks)
+                if (ks < ksteps) mma_bf16_16816(c, a[ks], prow[ks * 8 + tig], prow[ks * 8 + 4 + tig]);
+            const int p0 = nt + tig * 2;
+            const float s0 = s_pn[p0] - 2.f * c[0], s1 = s_pn[p0 + 1] - 2.f * c[1];
+            const float s2 = s_pn[p0] - 2.f * c[2], s3 = s_pn[p0 + 1] - 2.f * c[3];
+            if (s0 < best_a) { best_a = s0; bi_a = p0; }
+            if (s1 < best_a) { best_a = s1; bi_a = p0 + 1; }
+            if (s2 < best_b) { best_b = s2; bi_b = p0; }
+            if (s3 < best_b) { best_b = s3; bi_b = p0 + 1; }
+        }
+#pragma unroll
+        for (int o = 1; o <= 2; o <<= 1) {
+            const float oa = __shfl_xor_sync(0xffffffffu, best_a, o), ob = __shfl_xor_sync(0xffffffffu, best_b, o);
+            const int32_t ia = __shfl_xor_sync(0xffffffffu, bi_a, o), ib = __shfl_xor_sync(0xffffffffu, bi_b, o);
+            if (oa < best_a || (oa == best_a && ia < bi_a)) { best_a = oa; bi_a = ia; }
+            if (ob < best_b || (ob == best_b && ib < bi_b)) { best_b = ob; bi_b = ib; }
+        }
+        if (tig == 0) {
+            if (ra < n) keys[ra] = ((uint64_t)(uint32_t)bi_a << bits_n) | (uint64_t)ra;
+            if (rb < n) keys[rb] = ((uint64_t)(uint32_t)bi_b << bits_n) | (uint64_t)rb;
+        }
     }
 }
 
@@ -1038,18 +1080,12 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
         n_groups = (int)std::max<int64_t>(1, std::min<int64_t>({kMaxGroups, n / 1024, 98304 / (4 * ((d + 3) / 4 * 4))}));
         CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(uint64_t) * (size_t)n));
         uint64_t *pkeys = ctx->scratch_a.as<uint64_t>();
-        const size_t psmem = sizeof(float) * (size_t)n_groups * ((d + 3) / 4 * 4 + 1);
-        const unsigned pgrid = std::min<unsigned>(grid_for(n, 256), 152u * 8u);
-        auto launch_assign = [&](auto kern) -> cnn_status {
-            CNN_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
-            kern<<<pgrid, 256, psmem, st>>>(ctx->x, n, d, colsum, n_groups, bits_n, pkeys);
-            CNN_LAUNCH_CHECK(ctx);
-            return CNN_OK;
-        };
-        if (d <= 32) CNN_TRY(launch_assign(pivot_assign_kernel<8>));
-        else if (d <= 64) CNN_TRY(launch_assign(pivot_assign_kernel<16>));
-        else if (d <= 96) CNN_TRY(launch_assign(pivot_assign_kernel<24>));
-        else CNN_TRY(launch_assign(pivot_assign_kernel<32>));
+        const int dk = (d + 15) & ~15, np8 = (n_groups + 7) & ~7;
+        const size_t psmem = sizeof(uint32_t) * (size_t)np8 * (dk / 2 + 4) + sizeof(float) * (size_t)np8;
+        CNN_CUDA(ctx, cudaFuncSetAttribute(pivot_assign_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)psmem));
+        pivot_assign_kernel<<<152u * 4u, 256, psmem, st>>>(ctx->x, n, d, colsum, n_groups, bits_n, pkeys);
+        CNN_LAUNCH_CHECK(ctx);
         int pb = 1;
         while ((1 << pb) < n_groups) ++pb;
         CNN_TRY(radix_sort_u64(ctx, pkeys, n, bits_n + pb, bits_n));  // built in point order
