@@ -182,7 +182,10 @@ namespace cnn {
 // prims.cu
 cnn_status scan_exclusive_i64(cnn_context *ctx, const int64_t *in, int64_t *out, int64_t n);
 cnn_status scan_exclusive_i32_to_i64(cnn_context *ctx, const int32_t *in, int64_t *out, int64_t n);
-cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits, int first_bit = 0);
+// sorted: if given, receives the buffer holding the result (keys or scratch_c,
+// valid until scratch_c is next used) and the final copy back is skipped
+cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits, int first_bit = 0,
+                          uint64_t **sorted = nullptr);
 cnn_status fill_i32(cnn_context *ctx, int32_t *p, int64_t n, int32_t v);
 cnn_status iota_i32(cnn_context *ctx, int32_t *p, int64_t n);
 

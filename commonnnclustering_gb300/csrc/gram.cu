@@ -477,22 +477,28 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
 }
 
 // ---- preparation: centring, BF16 split, norms ------------------------------------
-// Column sums of the finite coordinates; *nonfinite set if any coordinate is not.
+// Column sums of the finite coordinates; *nonfinite set if any coordinate is
+// not.  The array is read flat and coalesced: the block size is a multiple of
+// n_dim and so is the grid stride, so every thread stays on one column
+// (threadIdx.x % n_dim); the block adds its threads' sums per column.
 __global__ void column_sum_kernel(const double *__restrict__ x, int64_t n, int d, double *__restrict__ sum,
                                   int *__restrict__ nonfinite) {
-    const int k = blockIdx.y;
-    double s = 0;
+    extern __shared__ double s_part[];  // [blockDim.x]
+    const int64_t total = n * d;
+    double acc = 0;
     bool fin = true;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double v = x[i * d + k];
-        if (isfinite(v)) s += v;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const double v = x[e];
+        if (isfinite(v)) acc += v;
         else fin = false;
     }
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    fin = __all_sync(0xffffffffu, fin);
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(&sum[k], s);
-        if (!fin) atomicExch(nonfinite, 1);
+    s_part[threadIdx.x] = acc;
+    // block-wide (the block size need not be a multiple of 32); also the barrier for s_part
+    if (__syncthreads_or(!fin) && threadIdx.x == 0) atomicExch(nonfinite, 1);
+    for (int k = threadIdx.x; k < d; k += blockDim.x) {
+        double t = 0;
+        for (int i = k; i < (int)blockDim.x; i += d) t += s_part[i];
+        atomicAdd(&sum[k], t);
     }
 }
 
@@ -547,17 +553,18 @@ __global__ void gram_prep_kernel(const double *__restrict__ x, int64_t n_rows, i
 // One block per 128-row block of the padded internal order: every row split
 // as in gram_prep_kernel (float64 centring, exact residuals), its float32
 // norm, the block's norm maxima, and -- for the tile pruning -- the block's
-// float32 centroid and a radius that bounds the distance of every point of
+// float32 centroid (stored transposed, [d][nblk]) and a radius that bounds the distance of every point of
 // the block to it: the float32 evaluation from the float32 coordinates,
 // inflated by its rounding ((d + 8) 2^-23 relative) and by the conversion
 // of the coordinates (2^-24 of the largest norm, taken twice).
-constexpr int kPrepWarps = 8;
+constexpr int kPrepWarps = 16;
 
 __global__ void __launch_bounds__(kPrepWarps * 32) gram_prep_bounds_kernel(
     const double *__restrict__ x, int64_t n_rows, int d, int dp, const double *__restrict__ mean,
     const int32_t *__restrict__ perm, __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ mid,
     __nv_bfloat16 *__restrict__ lo, float *__restrict__ norm2, unsigned *__restrict__ blk_norm_bits,
-    unsigned *__restrict__ blk_norm2_bits, int bounds, float *__restrict__ centroid, float *__restrict__ radius) {
+    unsigned *__restrict__ blk_norm2_bits, int bounds, int64_t nblk, float *__restrict__ centroid_t,
+    float *__restrict__ radius) {
     extern __shared__ float s_cf[];  // [kTM][d + 1] float32 coordinates, then [d] centroid
     __shared__ float s_max[kPrepWarps][2];
     __shared__ int s_used[kPrepWarps];
@@ -630,7 +637,7 @@ __global__ void __launch_bounds__(kPrepWarps * 32) gram_prep_bounds_kernel(
             if (s_cf[r * ld + d] > 0.f) c += s_cf[r * ld + k];
         c = rows > 0 ? c / (float)rows : 0.f;
         s_cent[k] = c;
-        centroid[I * d + k] = c;
+        centroid_t[(int64_t)k * nblk + I] = c;
     }
     __syncthreads();
     float m = 0.f;
@@ -807,25 +814,33 @@ __global__ void padded_perm_kernel(const uint64_t *__restrict__ keys, int64_t n,
 // rho_J > R means every pair is farther than R (triangle inequality); the
 // margin covers the float32 evaluation of the centroid distance.
 //
-// kListRows consecutive rows I per CTA: their centroids sit in shared memory
-// and every column centroid J is read once for all of them.  Pass 1 counts
-// the kept J per row, pass 2 writes them (order within a row is arbitrary).
+// kListRows consecutive rows I per CTA and kListCols columns J (grid y):
+// the row centroids sit in shared memory, the column centroids are read
+// from the transposed array [d][nblk] (coalesced), once for all rows.  Pass
+// 1 counts the kept J per row, pass 2 writes them (order within a row is
+// arbitrary).
 constexpr int kListRows = 8;
 
+constexpr int kListCols = 1024;  // column blocks J per CTA (grid y)
+
 template <bool kWrite>
-__global__ void __launch_bounds__(256) tile_list_kernel(const float *__restrict__ centroid,
+__global__ void __launch_bounds__(256) tile_list_kernel(const float *__restrict__ centroid_t,
                                                         const float *__restrict__ radius, int d, int64_t nblk,
                                                         float R, int32_t *__restrict__ row_count,
-                                                        const int64_t *__restrict__ row_off, int2 *__restrict__ tiles) {
+                                                        const int64_t *__restrict__ row_off,
+                                                        int32_t *__restrict__ cursor, int2 *__restrict__ tiles) {
     __shared__ float s_a[kListRows][128];
     __shared__ float s_na[kListRows], s_ra[kListRows];
     __shared__ int32_t s_cnt[kListRows];
     const int64_t I0 = (int64_t)blockIdx.x * kListRows;
     const int rows = (int)min((int64_t)kListRows, nblk - I0);
+    const int64_t J0 = max(I0, (int64_t)blockIdx.y * kListCols);
+    const int64_t J1 = min(nblk, (int64_t)(blockIdx.y + 1) * kListCols);
+    if (J0 >= J1) return;  // the whole CTA: nothing of this column range is at or right of the diagonal
     const bool keep_all = !(R < INFINITY);  // no pruning (centroids unused; n_dim may exceed 128)
     for (int e = threadIdx.x; e < kListRows * d && !keep_all; e += blockDim.x) {
         const int r = e / d, k = e - r * d;
-        s_a[r][k] = r < rows ? centroid[(I0 + r) * d + k] : 0.f;
+        s_a[r][k] = r < rows ? centroid_t[(int64_t)k * nblk + I0 + r] : 0.f;
     }
     if (threadIdx.x < kListRows) {
         s_cnt[threadIdx.x] = 0;
@@ -838,14 +853,13 @@ __global__ void __launch_bounds__(256) tile_list_kernel(const float *__restrict_
         s_na[threadIdx.x] = sqrtf(na);
     }
     __syncthreads();
-    for (int64_t J = I0 + threadIdx.x; J < nblk; J += blockDim.x) {
-        const float *b = centroid + J * d;
+    for (int64_t J = J0 + threadIdx.x; J < J1; J += blockDim.x) {
         float s[kListRows];
 #pragma unroll
         for (int r = 0; r < kListRows; ++r) s[r] = 0.f;
         float nb = 0.f;
         for (int k = 0; k < d && !keep_all; ++k) {
-            const float bk = b[k];
+            const float bk = centroid_t[(int64_t)k * nblk + J];  // consecutive J: coalesced
             nb = fmaf(bk, bk, nb);
 #pragma unroll
             for (int r = 0; r < kListRows; ++r) {
@@ -862,13 +876,13 @@ __global__ void __launch_bounds__(256) tile_list_kernel(const float *__restrict_
             const float margin = 1e-5f * (s_na[r] + nb + s_ra[r] + rb + R);
             const bool touch = keep_all || J == I || sqrtf(s[r]) - s_ra[r] - rb <= R + margin;
             if (touch) {
-                const int32_t k = atomicAdd(&s_cnt[r], 1);
-                if (kWrite) tiles[row_off[I] + k] = make_int2((int32_t)I, (int32_t)J);
+                if (kWrite) tiles[row_off[I] + atomicAdd(&cursor[I], 1)] = make_int2((int32_t)I, (int32_t)J);
+                else atomicAdd(&s_cnt[r], 1);
             }
         }
     }
     __syncthreads();
-    if (!kWrite && threadIdx.x < rows) row_count[I0 + threadIdx.x] = s_cnt[threadIdx.x];
+    if (!kWrite && threadIdx.x < rows && s_cnt[threadIdx.x]) atomicAdd(&row_count[I0 + threadIdx.x], s_cnt[threadIdx.x]);
 }
 
 // internal indices -> point indices in a key list.  pack_bits > 0: write
@@ -1064,8 +1078,11 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     int64_t *gpstart = gstart + 1024;
     CNN_CUDA(ctx, cudaMemsetAsync(colsum, 0, sizeof(double) * d, st));
     {
-        const int blocks = (int)std::min<int64_t>(256, (n + 255) / 256);
-        column_sum_kernel<<<dim3(blocks, d), 256, 0, st>>>(ctx->x, n, d, colsum, nonfinite);
+        // block = a multiple of n_dim (at most 1024 threads); grid stride a multiple too
+        const int per = std::max(1, 256 / d), threads = d * per;
+        if (threads > 1024) return CNN_OK;  // n_dim > 1024: the all-pairs path takes it
+        const int blocks = (int)std::min<int64_t>(152 * 4, (n * d + threads - 1) / threads);
+        column_sum_kernel<<<blocks, threads, sizeof(double) * threads, st>>>(ctx->x, n, d, colsum, nonfinite);
         CNN_LAUNCH_CHECK(ctx);
         column_mean_kernel<<<1, 128, 0, st>>>(colsum, d, n);  // colsum holds the column means from here
         CNN_LAUNCH_CHECK(ctx);
@@ -1128,12 +1145,13 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     // the list of block pairs (I, J >= I) that can hold a pair within R
     const double Rsearch = (metric == CNN_METRIC_EUCLIDEAN ? radius_cutoff : sqrt(radius_cutoff)) * (1.0 + 1e-6);
     CNN_TRY(ctx->ensure(ctx->gram_blocks, sizeof(float) * (size_t)nblk * (d + 1) +
-                                              (sizeof(int32_t) + sizeof(int64_t)) * (size_t)(nblk + 1) + 256));
-    float *centroid = ctx->gram_blocks.as<float>();
+                                              (2 * sizeof(int32_t) + sizeof(int64_t)) * (size_t)(nblk + 1) + 256));
+    float *centroid = ctx->gram_blocks.as<float>();  // transposed: [d][nblk]
     float *bradius = centroid + nblk * d;
     int32_t *row_count = reinterpret_cast<int32_t *>(bradius + nblk);
+    int32_t *row_cursor = row_count + nblk + 1;
     int64_t *row_off = reinterpret_cast<int64_t *>(
-        (reinterpret_cast<uintptr_t>(row_count + nblk + 1) + 15) & ~uintptr_t(15));
+        (reinterpret_cast<uintptr_t>(row_cursor + nblk + 1) + 15) & ~uintptr_t(15));
     const float Rf = prune ? (float)Rsearch : INFINITY;
     if (prune) {  // n_dim <= 128: the block's coordinates fit in shared memory
         const size_t psmem = sizeof(float) * ((size_t)kTM * (d + 1) + d);
@@ -1141,7 +1159,7 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
                                            (int)psmem));
         gram_prep_bounds_kernel<<<(unsigned)nblk, kPrepWarps * 32, psmem, st>>>(
             ctx->x, n_rows, d, dp, colsum, perm, ctx->gram_hi.as<__nv_bfloat16>(), ctx->gram_mid.as<__nv_bfloat16>(),
-            ctx->gram_lo.as<__nv_bfloat16>(), norm2, blk_norm_bits, blk_norm2_bits, 1, centroid, bradius);
+            ctx->gram_lo.as<__nv_bfloat16>(), norm2, blk_norm_bits, blk_norm2_bits, 1, nblk, centroid, bradius);
         CNN_LAUNCH_CHECK(ctx);
     } else {
         CNN_CUDA(ctx, cudaMemsetAsync(blk_norm_bits, 0, sizeof(unsigned) * 2 * (size_t)nblk, st));
@@ -1152,18 +1170,18 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
         CNN_LAUNCH_CHECK(ctx);
         CNN_CUDA(ctx, cudaMemsetAsync(centroid, 0, sizeof(float) * (size_t)nblk * (d + 1), st));
     }
-    const unsigned lgrid = (unsigned)((nblk + kListRows - 1) / kListRows);
-    tile_list_kernel<false><<<lgrid, 256, 0, st>>>(centroid, bradius, d, nblk, Rf, row_count, nullptr,
-                                                             nullptr);
+    const dim3 lgrid((unsigned)((nblk + kListRows - 1) / kListRows), (unsigned)((nblk + kListCols - 1) / kListCols));
+    CNN_CUDA(ctx, cudaMemsetAsync(row_count, 0, sizeof(int32_t) * 2 * (size_t)(nblk + 1), st));  // counts, cursors
+    tile_list_kernel<false><<<lgrid, 256, 0, st>>>(centroid, bradius, d, nblk, Rf, row_count, nullptr, nullptr,
+                                                   nullptr);
     CNN_LAUNCH_CHECK(ctx);
-    CNN_CUDA(ctx, cudaMemsetAsync(row_count + nblk, 0, sizeof(int32_t), st));
     CNN_TRY(scan_exclusive_i32_to_i64(ctx, row_count, row_off, nblk + 1));
     int64_t ntiles = 0;
     CNN_CUDA(ctx, cudaMemcpyAsync(&ntiles, row_off + nblk, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     CNN_CUDA(ctx, cudaStreamSynchronize(st));
     CNN_TRY(ctx->ensure(ctx->gram_tiles, sizeof(int2) * (size_t)(ntiles > 0 ? ntiles : 1)));
-    tile_list_kernel<true><<<lgrid, 256, 0, st>>>(centroid, bradius, d, nblk, Rf, nullptr, row_off,
-                                                            ctx->gram_tiles.as<int2>());
+    tile_list_kernel<true><<<lgrid, 256, 0, st>>>(centroid, bradius, d, nblk, Rf, nullptr, row_off, row_cursor,
+                                                  ctx->gram_tiles.as<int2>());
     CNN_LAUNCH_CHECK(ctx);
 
     CUtensorMap map_hi, map_mid, map_lo;
@@ -1240,12 +1258,13 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
             ctx->stats.filter_band = std::max(coef, 0.0);
             ctx->stats.filter_enabled = 1;
             // CSR: sort the packed (row << bits_n | col) keys
-            CNN_TRY(radix_sort_u64(ctx, a.keys, nk, 2 * bits_n));
+            uint64_t *sorted = a.keys;
+            CNN_TRY(radix_sort_u64(ctx, a.keys, nk, 2 * bits_n, 0, &sorted));
             CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nk > 0 ? nk : 1)));
             int64_t *row_off_csr = ctx->row_off.as<int64_t>();
             if (nk == 0) CNN_CUDA(ctx, cudaMemsetAsync(row_off_csr, 0, sizeof(int64_t) * (size_t)(n + 1), st));
             keys_rows_kernel<<<std::min<unsigned>(grid_for(nk, 256), 152u * 16u), 256, 0, st>>>(
-                a.keys, nk, bits_n, n, row_off_csr, ctx->cols.as<int32_t>());
+                sorted, nk, bits_n, n, row_off_csr, ctx->cols.as<int32_t>());
             CNN_LAUNCH_CHECK(ctx);
             degree_from_offsets_kernel<<<std::min<unsigned>(grid_for(n + 1, 256), 152u * 16u), 256, 0, st>>>(
                 row_off_csr, n, ctx->deg.as<int32_t>());

@@ -284,7 +284,8 @@ __global__ void __launch_bounds__(1024) small_sort_kernel(uint64_t *__restrict__
 // within equal higher bits, which the stable passes keep -- e.g. an index
 // in the low bits of keys built in index order).  Uses scratch_c/scratch_d
 // and the scan temp.
-cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits, int first_bit) {
+cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits, int first_bit, uint64_t **sorted) {
+    if (sorted) *sorted = keys;
     if (n <= 1) return CNN_OK;
     if (bits < 1) bits = 1;
     if (bits > 64) bits = 64;
@@ -313,8 +314,11 @@ cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits,
         CNN_LAUNCH_CHECK(ctx);
         uint64_t *t = a; a = b; b = t;
     }
-    if (a != keys)
+    if (sorted) {
+        *sorted = a;  // the caller reads the result where the last pass left it
+    } else if (a != keys) {
         CNN_CUDA(ctx, cudaMemcpyAsync(keys, a, sizeof(uint64_t) * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
     return CNN_OK;
 }
 

@@ -1079,8 +1079,9 @@ cnn_status export_neighbours_impl(cnn_context *ctx, int64_t *offsets_dev, int32_
     export_keys_kernel<<<grid_for(n * 32, 256), 256, 0, st>>>(ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(),
                                                               ctx->perm.as<int32_t>(), n, bits_n, keys);
     CNN_LAUNCH_CHECK(ctx);
-    CNN_TRY(radix_sort_u64(ctx, keys, nnz, 2 * bits_n));
-    keys_to_cols_kernel<<<std::min<unsigned>(grid_for(nnz, 256), 152u * 32u), 256, 0, st>>>(keys, nnz, bits_n,
+    uint64_t *sorted = keys;
+    CNN_TRY(radix_sort_u64(ctx, keys, nnz, 2 * bits_n, 0, &sorted));
+    keys_to_cols_kernel<<<std::min<unsigned>(grid_for(nnz, 256), 152u * 32u), 256, 0, st>>>(sorted, nnz, bits_n,
                                                                                              indices_dev);
     CNN_LAUNCH_CHECK(ctx);
     return CNN_OK;
@@ -1229,9 +1230,10 @@ cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev, con
         CNN_CUDA(ctx, cudaStreamSynchronize(st));
         if (bad) return ctx->fail(CNN_ERR_INVALID_ARG, "neighbour index out of range");
         if (nnz > 0) {
-            CNN_TRY(radix_sort_u64(ctx, keys, nnz, 2 * bits_n));
+            uint64_t *sorted = keys;
+            CNN_TRY(radix_sort_u64(ctx, keys, nnz, 2 * bits_n, 0, &sorted));
             keys_to_cols_kernel<<<std::min<unsigned>(grid_for(nnz, 256), 152u * 32u), 256, 0, st>>>(
-                keys, nnz, bits_n, ctx->cols.as<int32_t>());
+                sorted, nnz, bits_n, ctx->cols.as<int32_t>());
             CNN_LAUNCH_CHECK(ctx);
         }
     }
