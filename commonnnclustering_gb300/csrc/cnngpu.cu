@@ -131,6 +131,7 @@ CNN_API cnn_status cnn_destroy(cnn_context *ctx) {
                            &ctx->pred_xoff, &ctx->pred_xcols, &ctx->pred_x, &ctx->pred_set,
                            &ctx->sweep_bucket, &ctx->sweep_row_off_max, &ctx->sweep_cols_max,
                            &ctx->sweep_deg_max, &ctx->sweep_consider, &ctx->sweep_forest, &ctx->sweep_open_a,
+                           &ctx->sweep_multi_deg, &ctx->sweep_multi_off, &ctx->sweep_multi_cols, &ctx->sweep_multi_base,
                            &ctx->sweep_open_b, &ctx->sweep_open_count,
                            &ctx->stage_consider, &ctx->stage_offsets, &ctx->stage_indices, &ctx->stage_misc,
                            &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->scratch_a, &ctx->scratch_b,

@@ -116,6 +116,7 @@ struct cnn_context {
     // batched (radius, cut) sweep: the largest-radius graph kept aside,
     // per-pair radius buckets, consider flags of the per-fit runs
     cnn::DevBuf sweep_bucket, sweep_row_off_max, sweep_cols_max, sweep_deg_max, sweep_consider, sweep_forest;
+    cnn::DevBuf sweep_multi_deg, sweep_multi_off, sweep_multi_cols, sweep_multi_base;  // every smaller radius's graph
     cnn::DevBuf sweep_open_a, sweep_open_b, sweep_open_count;  // open pairs of the last fit, two lists
 
     // tensor-core (Gram) search for n_dim >= 16

@@ -113,6 +113,72 @@ __global__ void filter_fill_kernel(int64_t n, const int64_t *__restrict__ row_of
     }
 }
 
+// Every radius below the largest at once: one pass over the r_max rows
+// counts, per row, the pairs of each radius (bucket <= k); a second pass
+// writes each radius's filtered rows (stable, so still sorted).  Radius k's
+// arrays sit at k * (n + 1) in deg_all / off_all and at base[k] in cols_all.
+constexpr int kMaxFiltered = kMaxRadii - 1;
+
+__global__ void __launch_bounds__(256) multi_count_kernel(int64_t n, const int64_t *__restrict__ row_off,
+                                                          const uint8_t *__restrict__ bucket, int kf,
+                                                          int32_t *__restrict__ deg_all) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t p = warp0; p <= n; p += nwarps) {
+        if (p == n) {  // the scans read n + 1 entries
+            if (lane < kf) deg_all[(int64_t)lane * (n + 1) + n] = 0;
+            continue;
+        }
+        int32_t c[kMaxFiltered];
+#pragma unroll
+        for (int k = 0; k < kMaxFiltered; ++k) c[k] = 0;
+        for (int64_t e = row_off[p] + lane; e < row_off[p + 1]; e += 32) {
+            const int b = bucket[e];
+#pragma unroll
+            for (int k = 0; k < kMaxFiltered; ++k) c[k] += b <= k;
+        }
+#pragma unroll
+        for (int k = 0; k < kMaxFiltered; ++k) {
+            if (k >= kf) break;
+            const int32_t t = __reduce_add_sync(0xffffffffu, c[k]);
+            if (lane == 0) deg_all[(int64_t)k * (n + 1) + p] = t;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) multi_fill_kernel(int64_t n, const int64_t *__restrict__ row_off,
+                                                         const int32_t *__restrict__ cols,
+                                                         const uint8_t *__restrict__ bucket, int kf,
+                                                         const int64_t *__restrict__ off_all,
+                                                         const int64_t *__restrict__ base,
+                                                         int32_t *__restrict__ cols_all) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t p = warp0; p < n; p += nwarps) {
+        int64_t w[kMaxFiltered];
+#pragma unroll
+        for (int k = 0; k < kMaxFiltered; ++k) w[k] = k < kf ? base[k] + off_all[(int64_t)k * (n + 1) + p] : 0;
+        const int64_t e1 = row_off[p + 1];
+        for (int64_t e0 = row_off[p]; e0 < e1; e0 += 32) {
+            const int64_t e = e0 + lane;
+            const bool valid = e < e1;
+            const int b = valid ? bucket[e] : 255;
+            const int32_t c = valid ? cols[e] : 0;
+#pragma unroll
+            for (int k = 0; k < kMaxFiltered; ++k) {
+                if (k >= kf) break;
+                const bool keep = b <= k;
+                const unsigned m = __ballot_sync(0xffffffffu, keep);
+                if (keep) cols_all[w[k] + __popc(m & lt)] = c;
+                w[k] += __popc(m);
+            }
+        }
+    }
+}
+
 __global__ void set_zero_tail_kernel(int32_t *deg, int64_t n) { deg[n] = 0; }
 
 bool ladder_thresholds(const std::vector<double> &ext, const std::vector<double> &rcs, int metric, Ladder *lad) {
@@ -274,6 +340,56 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
     const int32_t *cols_max = ctx->sweep_cols_max.as<int32_t>();
     CNN_TRY(ctx->ensure(ctx->row_off, sizeof(int64_t) * (size_t)(n + 1)));
     CNN_TRY(ctx->ensure(ctx->deg, sizeof(int32_t) * (size_t)(n + 1)));
+
+    // every smaller radius's graph in two passes, when they fit in 48 GB
+    const int kf = n_radii - 1;
+    if (kf > 0 && n > 0) {
+        CNN_TRY(ctx->ensure(ctx->sweep_multi_deg, sizeof(int32_t) * (size_t)kf * (size_t)(n + 1)));
+        CNN_TRY(ctx->ensure(ctx->sweep_multi_off, sizeof(int64_t) * (size_t)kf * (size_t)(n + 1)));
+        int32_t *deg_all = ctx->sweep_multi_deg.as<int32_t>();
+        int64_t *off_all = ctx->sweep_multi_off.as<int64_t>();
+        const unsigned mgrid = std::min<unsigned>(grid_for((n + 1) * 32, 256), 152u * 16u);
+        multi_count_kernel<<<mgrid, 256, 0, st>>>(n, off_max, bucket, kf, deg_all);
+        CNN_LAUNCH_CHECK(ctx);
+        for (int32_t k = 0; k < kf; ++k)
+            CNN_TRY(scan_exclusive_i32_to_i64(ctx, deg_all + (size_t)k * (n + 1), off_all + (size_t)k * (n + 1), n + 1));
+        std::vector<int64_t> nnz_k(kf), base(kf + 1, 0);
+        for (int32_t k = 0; k < kf; ++k)
+            CNN_CUDA(ctx, cudaMemcpyAsync(&nnz_k[k], off_all + (size_t)k * (n + 1) + n, sizeof(int64_t),
+                                          cudaMemcpyDeviceToHost, st));
+        CNN_CUDA(ctx, cudaStreamSynchronize(st));
+        for (int32_t k = 0; k < kf; ++k) base[k + 1] = base[k] + nnz_k[k];
+        if (base[kf] * (int64_t)sizeof(int32_t) <= (int64_t(48) << 30)) {
+            CNN_TRY(ctx->ensure(ctx->sweep_multi_cols, sizeof(int32_t) * (size_t)(base[kf] > 0 ? base[kf] : 1)));
+            CNN_TRY(ctx->ensure(ctx->sweep_multi_base, sizeof(int64_t) * (size_t)(kf + 1)));
+            CNN_CUDA(ctx, cudaMemcpyAsync(ctx->sweep_multi_base.ptr, base.data(), sizeof(int64_t) * (size_t)(kf + 1),
+                                          cudaMemcpyHostToDevice, st));
+            multi_fill_kernel<<<mgrid, 256, 0, st>>>(n, off_max, cols_max, bucket, kf, off_all,
+                                                     ctx->sweep_multi_base.as<int64_t>(),
+                                                     ctx->sweep_multi_cols.as<int32_t>());
+            CNN_LAUNCH_CHECK(ctx);
+            // the fits of radius k see views of its arrays as the graph
+            cnn::DevBuf own_off = ctx->row_off, own_cols = ctx->cols, own_deg = ctx->deg;
+            for (int32_t k = 0; k < kf; ++k) {
+                ctx->row_off = cnn::DevBuf{off_all + (size_t)k * (n + 1), sizeof(int64_t) * (size_t)(n + 1)};
+                ctx->deg = cnn::DevBuf{deg_all + (size_t)k * (n + 1), sizeof(int32_t) * (size_t)(n + 1)};
+                ctx->cols = cnn::DevBuf{ctx->sweep_multi_cols.as<int32_t>() + base[k],
+                                        sizeof(int32_t) * (size_t)(nnz_k[k] > 0 ? nnz_k[k] : 1)};
+                ctx->nnz = nnz_k[k];
+                const cnn_status fs = fit_cuts(k, true);
+                ctx->row_off = own_off;
+                ctx->cols = own_cols;
+                ctx->deg = own_deg;
+                CNN_TRY(fs);
+            }
+            // the largest radius is the kept graph itself
+            std::swap(ctx->row_off, ctx->sweep_row_off_max);
+            std::swap(ctx->cols, ctx->sweep_cols_max);
+            std::swap(ctx->deg, ctx->sweep_deg_max);
+            ctx->nnz = nnz;
+            return fit_cuts(kf, true);
+        }
+    }
     for (int32_t k = 0; k < n_radii; ++k) {
         int64_t nnz_k = nnz;
         if (k < n_radii - 1) {
