@@ -555,7 +555,11 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     root_store_kernel<<<blocks_for(n), 256, 0, st>>>(n, node, parent);
     CNN_LAUNCH_CHECK(ctx);
     // cross edges between the hooked sets -> worklist -> checks
-    const int64_t wl_cap = std::max<int64_t>(int64_t(1) << 20, ctx->nnz / 16);
+    // worklist capacity: a list-fed filter (pairs a finished fit left open)
+    // holds more cross pairs than the graph-fed one after its hook pass;
+    // overflow falls back to the full lazy pass (measured on the 1M-point
+    // sweep: nnz/4 for lists, nnz/16 for the graph)
+    const int64_t wl_cap = std::max<int64_t>(int64_t(1) << 20, ctx->nnz / (edge_list ? 4 : 16));
     CNN_TRY(ctx->ensure(ctx->io_c, sizeof(int2) * (size_t)wl_cap));
     unsigned long long *wl_count = counters + 8;
     CNN_CUDA(ctx, cudaMemsetAsync(wl_count, 0, sizeof(unsigned long long), st));
