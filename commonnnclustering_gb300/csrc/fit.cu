@@ -184,6 +184,8 @@ __global__ void __launch_bounds__(kCheckWarps * 32, CNN_CHECK_MIN_BLOCKS) edge_c
                                                          const int32_t *__restrict__ cols,
                                                          int32_t *__restrict__ parent, int32_t needed,
                                                          unsigned long long *__restrict__ counters) {
+    __shared__ int32_t s_wide[kCheckWarps][kWideChunk];
+    int32_t *sA = s_wide[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -224,8 +226,8 @@ __global__ void __launch_bounds__(kCheckWarps * 32, CNN_CHECK_MIN_BLOCKS) edge_c
                 ok = needed == 0;
             } else {
                 const int64_t as = row_off[aa], bs = row_off[bb];
-                ok = warp_shares_at_least(cols + as, (int32_t)(row_off[aa + 1] - as), cols + bs,
-                                          (int32_t)(row_off[bb + 1] - bs), needed, lane);
+                ok = warp_shares(cols + as, (int32_t)(row_off[aa + 1] - as), cols + bs, (int32_t)(row_off[bb + 1] - bs),
+                                 needed, lane, sA);
                 ++n_checks;
             }
             if (ok) {

@@ -69,6 +69,58 @@ __device__ __forceinline__ bool warp_shares_at_least(const int32_t *__restrict__
     return false;
 }
 
+// The same count for two long lists, 128 entries of each per step: A's
+// chunk goes to the warp's shared-memory slot sA (128 entries), B's stays
+// in registers (4 per lane), and each lane looks its 4 values up in A's
+// chunk by binary search.  Both chunks load together, so a list pair costs
+// a quarter of the dependent round trips of the 32-wide merge -- what a
+// rejected pair of long rows (scanned to the end) is bound by.
+constexpr int kWideChunk = 128;
+
+__device__ __forceinline__ bool warp_shares_at_least_wide(const int32_t *__restrict__ A, int32_t la,
+                                                          const int32_t *__restrict__ B, int32_t lb, int32_t needed,
+                                                          int lane, int32_t *sA) {
+    if (la < needed || lb < needed) return false;
+    int32_t ia = 0, ib = 0, count = 0;
+    while (ia < la && ib < lb) {
+        int32_t av[4], bv[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int32_t i = ia + j * 32 + lane, k = ib + j * 32 + lane;
+            av[j] = i < la ? __ldg(A + i) : INT_MAX;      // padding never matches:
+            bv[j] = k < lb ? __ldg(B + k) : INT_MAX - 1;  // A pads differ from B pads
+        }
+        __syncwarp();  // the previous step's lookups are done
+#pragma unroll
+        for (int j = 0; j < 4; ++j) sA[j * 32 + lane] = av[j];
+        __syncwarp();
+        const int32_t amax = sA[kWideChunk - 1];
+        const int32_t bmax = __shfl_sync(0xffffffffu, bv[3], 31);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int pos = 0;  // entries of the chunk below bv[j]
+#pragma unroll
+            for (int step = kWideChunk / 2; step > 0; step >>= 1)
+                if (sA[pos + step - 1] < bv[j]) pos += step;
+            const bool found = pos < kWideChunk && sA[pos] == bv[j];
+            count += __popc(__ballot_sync(0xffffffffu, found));
+        }
+        if (count >= needed) return true;
+        if (amax <= bmax) ia += kWideChunk;
+        if (bmax <= amax) ib += kWideChunk;
+        const int32_t rest = min(la - ia, lb - ib);
+        if (count + (rest > 0 ? rest : 0) < needed) return false;
+    }
+    return false;
+}
+
+// Either merge, by the lengths (both lists of at least one wide chunk).
+__device__ __forceinline__ bool warp_shares(const int32_t *__restrict__ A, int32_t la, const int32_t *__restrict__ B,
+                                            int32_t lb, int32_t needed, int lane, int32_t *sA) {
+    return (la >= kWideChunk && lb >= kWideChunk) ? warp_shares_at_least_wide(A, la, B, lb, needed, lane, sA)
+                                                  : warp_shares_at_least(A, la, B, lb, needed, lane);
+}
+
 // Persistent check kernels: nodes are dealt to warps in contiguous chunks
 // (CNN_CHECK_CHUNKED=0 strides them), so that warps working at the same time
 // sit in different regions of the (cell-ordered) graph and rarely race on
@@ -131,6 +183,8 @@ __device__ __forceinline__ void check_union_body(
     int32_t *__restrict__ parent, int32_t needed, int32_t max_edges,
     unsigned long long *__restrict__ counters, const int32_t *__restrict__ skip_a = nullptr,
     const int32_t *__restrict__ skip_b = nullptr) {
+    __shared__ int32_t s_wide[kCheckWarps][kWideChunk];
+    int32_t *sA = s_wide[(threadIdx.x >> 5) % kCheckWarps];
     const int lane = threadIdx.x & 31;
     const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -203,7 +257,7 @@ __device__ __forceinline__ void check_union_body(
                 } else {
                     const int64_t bs = row_off[bb];
                     const int32_t lb = (int32_t)(row_off[bb + 1] - bs);
-                    ok = warp_shares_at_least(A, la, cols + bs, lb, needed, lane);
+                    ok = warp_shares(A, la, cols + bs, lb, needed, lane, sA);
                     ++n_checks;
                 }
                 if (ok) {
