@@ -114,11 +114,17 @@ __device__ __forceinline__ bool warp_shares_at_least_wide(const int32_t *__restr
     return false;
 }
 
-// Either merge, by the lengths (both lists of at least one wide chunk).
+// Either merge, by the lengths: the wide one as soon as one list is at least
+// kWideMin long (a short row against a long one is walked 128 at a time).
+#ifndef CNN_WIDE_MIN
+#define CNN_WIDE_MIN 128
+#endif
+constexpr int kWideMin = CNN_WIDE_MIN;
+
 __device__ __forceinline__ bool warp_shares(const int32_t *__restrict__ A, int32_t la, const int32_t *__restrict__ B,
                                             int32_t lb, int32_t needed, int lane, int32_t *sA) {
-    return (la >= kWideChunk && lb >= kWideChunk) ? warp_shares_at_least_wide(A, la, B, lb, needed, lane, sA)
-                                                  : warp_shares_at_least(A, la, B, lb, needed, lane);
+    return (la >= kWideMin || lb >= kWideMin) ? warp_shares_at_least_wide(A, la, B, lb, needed, lane, sA)
+                                              : warp_shares_at_least(A, la, B, lb, needed, lane);
 }
 
 // Persistent check kernels: nodes are dealt to warps in contiguous chunks
