@@ -187,6 +187,8 @@ cnn_status scan_exclusive_i32_to_i64(cnn_context *ctx, const int32_t *in, int64_
 // valid until scratch_c is next used) and the final copy back is skipped
 cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits, int first_bit = 0,
                           uint64_t **sorted = nullptr);
+// raises a kernel's dynamic shared-memory limit to at least `bytes` (never lowers it)
+cnn_status allow_dynamic_smem(cnn_context *ctx, const void *kernel, size_t bytes);
 cnn_status fill_i32(cnn_context *ctx, int32_t *p, int64_t n, int32_t v);
 cnn_status iota_i32(cnn_context *ctx, int32_t *p, int64_t n);
 

@@ -1099,8 +1099,7 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
         uint64_t *pkeys = ctx->scratch_a.as<uint64_t>();
         const int dk = (d + 15) & ~15, np8 = (n_groups + 7) & ~7;
         const size_t psmem = sizeof(uint32_t) * (size_t)np8 * (dk / 2 + 4) + sizeof(float) * (size_t)np8;
-        CNN_CUDA(ctx, cudaFuncSetAttribute(pivot_assign_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)psmem));
+        CNN_TRY(allow_dynamic_smem(ctx, (const void *)pivot_assign_kernel, psmem));
         pivot_assign_kernel<<<152u * 4u, 256, psmem, st>>>(ctx->x, n, d, colsum, n_groups, bits_n, pkeys);
         CNN_LAUNCH_CHECK(ctx);
         int pb = 1;
@@ -1155,8 +1154,7 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     const float Rf = prune ? (float)Rsearch : INFINITY;
     if (prune) {  // n_dim <= 128: the block's coordinates fit in shared memory
         const size_t psmem = sizeof(float) * ((size_t)kTM * (d + 1) + d);
-        CNN_CUDA(ctx, cudaFuncSetAttribute(gram_prep_bounds_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)psmem));
+        CNN_TRY(allow_dynamic_smem(ctx, (const void *)gram_prep_bounds_kernel, psmem));
         gram_prep_bounds_kernel<<<(unsigned)nblk, kPrepWarps * 32, psmem, st>>>(
             ctx->x, n_rows, d, dp, colsum, perm, ctx->gram_hi.as<__nv_bfloat16>(), ctx->gram_mid.as<__nv_bfloat16>(),
             ctx->gram_lo.as<__nv_bfloat16>(), norm2, blk_norm_bits, blk_norm2_bits, 1, nblk, centroid, bradius);
@@ -1212,7 +1210,7 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, dev);
     const int grid = (int)std::min<int64_t>(ntiles, dev_sms > 0 ? dev_sms : sms);
     const size_t smem = (size_t)kStages * kStageBytes + 1024;
-    CNN_CUDA(ctx, cudaFuncSetAttribute(gram_search_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CNN_TRY(allow_dynamic_smem(ctx, (const void *)gram_search_kernel, smem));
     for (int attempt = 0; attempt < 2; ++attempt) {
         CNN_TRY(ctx->ensure(ctx->gram_keys, sizeof(uint64_t) * (size_t)key_cap));
         CNN_TRY(ctx->ensure(ctx->gram_amb, (sizeof(uint64_t) + sizeof(float)) * (size_t)amb_cap));

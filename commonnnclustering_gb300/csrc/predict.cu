@@ -43,6 +43,8 @@ __global__ void __launch_bounds__(256) predict_kernel(int64_t m, const int64_t *
                                                       const int64_t *__restrict__ set, int64_t nset, int64_t sim,
                                                       int64_t nmem, int64_t *__restrict__ olabels,
                                                       uint8_t *__restrict__ oconsider) {
+    __shared__ int32_t s_wide[8][kWideChunk];  // 256 threads: a slot per warp for the wide merge
+    int32_t *sA = s_wide[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -74,7 +76,7 @@ __global__ void __launch_bounds__(256) predict_kernel(int64_t m, const int64_t *
                     ok = sim == 0;
                 } else {
                     const int64_t bs = off[ii];
-                    ok = warp_shares_at_least(A, (int32_t)la, cols + bs, (int32_t)(off[ii + 1] - bs), needed, lane);
+                    ok = warp_shares(A, (int32_t)la, cols + bs, (int32_t)(off[ii + 1] - bs), needed, lane, sA);
                 }
                 if (ok) {
                     const int64_t l = __shfl_sync(0xffffffffu, lab, src);

@@ -3,6 +3,10 @@
 // Both are plain HBM-streaming kernels: a tile of 2048 elements per block
 // (256 threads x 8), staged through shared memory so that every global
 // access is coalesced.
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "common.cuh"
 
 namespace cnn {
@@ -319,6 +323,21 @@ cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits,
     } else if (a != keys) {
         CNN_CUDA(ctx, cudaMemcpyAsync(keys, a, sizeof(uint64_t) * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream));
     }
+    return CNN_OK;
+}
+
+// The dynamic shared-memory limit is a property of the kernel on a device,
+// shared by every thread and context of the process: it is only ever raised
+// (under a lock), so a launch sized under a limit set earlier stays valid
+// while another thread raises it for a bigger launch of the same kernel.
+cnn_status allow_dynamic_smem(cnn_context *ctx, const void *kernel, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, size_t> limit;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t &cur = limit[std::make_pair(ctx->device, kernel)];
+    if (bytes <= cur) return CNN_OK;
+    CNN_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cur = bytes;
     return CNN_OK;
 }
 

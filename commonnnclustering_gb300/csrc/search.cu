@@ -993,8 +993,8 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         stage_end(ctx, 1);
         if (d > 1024) return ctx->fail(CNN_ERR_UNSUPPORTED, "n_dim > 1024 is not supported");
         const size_t smem = sizeof(float) * (size_t)(kTileCand + kTileWarps) * (d + 1);
-        CNN_CUDA(ctx, cudaFuncSetAttribute(tile_search_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        CNN_CUDA(ctx, cudaFuncSetAttribute(tile_search_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CNN_TRY(allow_dynamic_smem(ctx, (const void *)tile_search_kernel<false>, smem));
+        CNN_TRY(allow_dynamic_smem(ctx, (const void *)tile_search_kernel<true>, smem));
         stage_begin(ctx, 2);
         const unsigned gq = grid_for(n, kTileWarps);
         tile_search_kernel<false><<<gq, kTileWarps * 32, smem, st>>>(ctx->x, ctx->scratch_b.as<float>(), d, n, sp, deg,
@@ -1161,8 +1161,8 @@ cnn_status cross_neighbours_impl(cnn_context *ctx, const double *xq, int64_t m, 
         xq, m, d, ctx->scratch_a.as<double>(), xqf);
     CNN_LAUNCH_CHECK(ctx);
     const size_t smem = sizeof(float) * (size_t)(kTileCand + kTileWarps) * (d + 1);
-    CNN_CUDA(ctx, cudaFuncSetAttribute(cross_tile_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CNN_CUDA(ctx, cudaFuncSetAttribute(cross_tile_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CNN_TRY(allow_dynamic_smem(ctx, (const void *)cross_tile_kernel<false>, smem));
+    CNN_TRY(allow_dynamic_smem(ctx, (const void *)cross_tile_kernel<true>, smem));
     CNN_TRY(ctx->ensure(ctx->io_a, sizeof(int32_t) * (size_t)(m + 1)));
     int32_t *deg = ctx->io_a.as<int32_t>();
     const unsigned gq = grid_for(m, kTileWarps);

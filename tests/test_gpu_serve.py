@@ -49,3 +49,51 @@ def test_admission_respects_the_memory_budget(serve):
         srv.close()
     assert all(j.error is None and j.labels is not None for j in jobs)
     assert srv.in_use == 0
+
+
+def test_gram_searches_of_different_widths_in_threads(serve):
+    """Concurrent contexts whose tensor-core searches need different
+    dynamic shared memory (n_dim 16 to 128) all succeed and match the same
+    searches run one after another."""
+    import threading
+    from commonnnclustering_gb300 import _abi
+    rng = np.random.default_rng(8)
+    cases = []
+    for t in range(16):
+        d = (16, 32, 64, 128)[t % 4]
+        centres = rng.normal(0, 3.0, size=(6, d))
+        x = np.vstack([c + rng.normal(0, 0.4, size=(700, d)) for c in centres])
+        cases.append((x, (0.35 * np.sqrt(2.0 * d)) ** 2))
+    ctx = _abi.Context(0)
+    want = []
+    for x, r2 in cases:
+        ctx.set_points(x)
+        ctx.build_neighbours(r2)
+        assert ctx.stats()["search_kind"] == 3  # the tensor-core path
+        want.append(ctx.get_neighbours())
+    ctx.close()
+    got = [None] * len(cases)
+    errors = []
+
+    def worker(w):
+        c = _abi.Context(0)
+        try:
+            for _ in range(3):
+                for i in range(w, len(cases), 4):
+                    x, r2 = cases[i]
+                    c.set_points(x)
+                    c.build_neighbours(r2)
+                    got[i] = c.get_neighbours()
+        except Exception as e:  # reported below
+            errors.append(repr(e))
+        finally:
+            c.close()
+
+    threads = [threading.Thread(target=worker, args=(w,)) for w in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for (wo, wi), (go, gi) in zip(want, got):
+        assert np.array_equal(wo, go) and np.array_equal(wi, gi)
