@@ -1002,16 +1002,18 @@ typedef CUresult (*PFN_encodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32
                                     const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                     CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+// looked up once per process (thread-safe initialisation of the static)
 PFN_encodeTiled get_encode_fn() {
-    static PFN_encodeTiled fn = nullptr;
-    if (!fn) {
+    static const PFN_encodeTiled fn = [] {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
+        PFN_encodeTiled f = nullptr;
         if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_encodeTiled>(p);
+            f = reinterpret_cast<PFN_encodeTiled>(p);
         (void)cudaGetLastError();
-    }
+        return f;
+    }();
     return fn;
 }
 
