@@ -12,6 +12,7 @@
 // fitted for every cut; every fit and sort is the same code cnn_fit and
 // cnn_sort_by_size run, so each result equals a separate fit.
 #include <math.h>
+#include <stdlib.h>
 
 #include <algorithm>
 #include <vector>
@@ -341,7 +342,7 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
     CNN_TRY(ctx->ensure(ctx->row_off, sizeof(int64_t) * (size_t)(n + 1)));
     CNN_TRY(ctx->ensure(ctx->deg, sizeof(int32_t) * (size_t)(n + 1)));
 
-    // every smaller radius's graph in two passes, when they fit in 48 GB
+    // every smaller radius's graph in two passes, when they fit in the budget
     const int kf = n_radii - 1;
     if (kf > 0 && n > 0) {
         CNN_TRY(ctx->ensure(ctx->sweep_multi_deg, sizeof(int32_t) * (size_t)kf * (size_t)(n + 1)));
@@ -359,7 +360,10 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
                                           cudaMemcpyDeviceToHost, st));
         CNN_CUDA(ctx, cudaStreamSynchronize(st));
         for (int32_t k = 0; k < kf; ++k) base[k + 1] = base[k] + nnz_k[k];
-        if (base[kf] * (int64_t)sizeof(int32_t) <= (int64_t(48) << 30)) {
+        // CNN_SWEEP_GRAPH_BUDGET (bytes) overrides the 48 GiB the graphs may take together
+        int64_t budget = int64_t(48) << 30;
+        if (const char *b = getenv("CNN_SWEEP_GRAPH_BUDGET")) budget = atoll(b);
+        if (base[kf] * (int64_t)sizeof(int32_t) <= budget) {
             CNN_TRY(ctx->ensure(ctx->sweep_multi_cols, sizeof(int32_t) * (size_t)(base[kf] > 0 ? base[kf] : 1)));
             CNN_TRY(ctx->ensure(ctx->sweep_multi_base, sizeof(int64_t) * (size_t)(kf + 1)));
             CNN_CUDA(ctx, cudaMemcpyAsync(ctx->sweep_multi_base.ptr, base.data(), sizeof(int64_t) * (size_t)(kf + 1),

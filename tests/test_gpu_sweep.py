@@ -92,3 +92,17 @@ def test_sweep_unordered_cut_pairs(cnn, d):
             assert np.array_equal(got[k, j], fit_pair(cnn, alone, x, rc, sim, nmem, 3)), (rc, sim, nmem)
     ctx.close()
     alone.close()
+
+
+def test_radius_by_radius_equals_all_radii_at_once(cnn, monkeypatch):
+    """The sweep builds every smaller radius's graph in one pass when they fit
+    in its memory budget, else one radius at a time: both give the same labels."""
+    from commonnnclustering_gb300 import workloads
+    x = workloads.nested3d(n=20000, seed=7, n_parents=5, box=3.0).astype(np.float64)
+    radii, cuts = [0.03, 0.06, 0.1], [2, 10, 40]
+    at_once = cnn.sweep(x, radii, cuts, member_cutoff=3)
+    monkeypatch.setenv("CNN_SWEEP_GRAPH_BUDGET", "0")
+    one_by_one = cnn.sweep(x, radii, cuts, member_cutoff=3)
+    assert np.array_equal(at_once, one_by_one)
+    for k, r in enumerate(radii):
+        assert np.array_equal(at_once[k, 1], separate_fit(cnn, x, r, cuts[1], 3)), r
