@@ -114,6 +114,10 @@ CNN_API cnn_status cnn_create(cnn_context **out, int device, void *stream) {
         (void)cudaGetLastError();
         ctx->host_stats = nullptr;  // statistics are then read back with a sync
     }
+    if (cudaMallocHost(&ctx->host_small, cnn_context::kHostSmall) != cudaSuccess) {
+        (void)cudaGetLastError();
+        ctx->host_small = nullptr;  // read-backs then go to pageable memory
+    }
     *out = ctx;
     return CNN_OK;
 }
@@ -144,6 +148,7 @@ CNN_API cnn_status cnn_destroy(cnn_context *ctx) {
     }
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->host_stats) cudaFreeHost(ctx->host_stats);
+    if (ctx->host_small) cudaFreeHost(ctx->host_small);
     (void)cudaGetLastError();
     delete ctx;
     return CNN_OK;

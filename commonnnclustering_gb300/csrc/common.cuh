@@ -73,6 +73,9 @@ struct cnn_context {
     // Counters of the last search and fit, copied back without a sync into
     // pinned memory and read by cnn_get_stats (which syncs the stream).
     unsigned long long *host_stats = nullptr;  // [0] exact, [1] candidates, [4..6] fit, [8] clusters
+    // pinned bounce buffer for the small read-backs the host waits on
+    static constexpr size_t kHostSmall = 64 << 10;
+    void *host_small = nullptr;
     bool search_stats_pending = false;
     bool fit_stats_pending = false;
     int64_t pending_candidates = -1;  // >= 0: known on the host
@@ -187,6 +190,9 @@ cnn_status scan_exclusive_i32_to_i64(cnn_context *ctx, const int32_t *in, int64_
 // valid until scratch_c is next used) and the final copy back is skipped
 cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits, int first_bit = 0,
                           uint64_t **sorted = nullptr);
+// Copies `bytes` from the device to `host` and waits (through the pinned
+// bounce buffer when it fits, else a plain copy).
+cnn_status read_back(cnn_context *ctx, void *host, const void *dev, size_t bytes);
 // raises a kernel's dynamic shared-memory limit to at least `bytes` (never lowers it)
 cnn_status allow_dynamic_smem(cnn_context *ctx, const void *kernel, size_t bytes);
 cnn_status fill_i32(cnn_context *ctx, int32_t *p, int64_t n, int32_t v);

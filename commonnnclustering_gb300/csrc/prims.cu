@@ -3,6 +3,8 @@
 // Both are plain HBM-streaming kernels: a tile of 2048 elements per block
 // (256 threads x 8), staged through shared memory so that every global
 // access is coalesced.
+#include <string.h>
+
 #include <map>
 #include <mutex>
 #include <utility>
@@ -323,6 +325,19 @@ cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits,
     } else if (a != keys) {
         CNN_CUDA(ctx, cudaMemcpyAsync(keys, a, sizeof(uint64_t) * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream));
     }
+    return CNN_OK;
+}
+
+cnn_status read_back(cnn_context *ctx, void *host, const void *dev, size_t bytes) {
+    if (bytes == 0) return CNN_OK;
+    if (ctx->host_small && bytes <= cnn_context::kHostSmall) {
+        CNN_CUDA(ctx, cudaMemcpyAsync(ctx->host_small, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        memcpy(host, ctx->host_small, bytes);
+        return CNN_OK;
+    }
+    CNN_CUDA(ctx, cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return CNN_OK;
 }
 

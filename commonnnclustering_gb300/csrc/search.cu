@@ -831,14 +831,12 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     std::vector<double> lo(d), hi(d);
     int64_t n_bad = 0;
     {
-        const int blocks = (int)std::min<int64_t>(256, (n + 255) / 256);
+        const int blocks = (int)std::min<int64_t>(128, (n + 255) / 256);
         CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(double) * (size_t)blocks * (size_t)d * 3 + 64));
         extent_partial_kernel<<<dim3(blocks, d), 256, 0, st>>>(ctx->x, n, d, ctx->scratch_a.as<double>());
         CNN_LAUNCH_CHECK(ctx);
         std::vector<double> part((size_t)blocks * d * 3);
-        CNN_CUDA(ctx, cudaMemcpyAsync(part.data(), ctx->scratch_a.ptr, sizeof(double) * part.size(),
-                                      cudaMemcpyDeviceToHost, st));
-        CNN_CUDA(ctx, cudaStreamSynchronize(st));
+        CNN_TRY(read_back(ctx, part.data(), ctx->scratch_a.ptr, sizeof(double) * part.size()));
         for (int k = 0; k < d; ++k) { lo[k] = INFINITY; hi[k] = -INFINITY; }
         double bad0 = 0;
         for (int b = 0; b < blocks; ++b)
@@ -928,7 +926,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
 
         // work items: (cell, first query) for every 32 queries of a cell
         CNN_TRY(ctx->ensure(ctx->io_a, sizeof(int32_t) * (size_t)(geo.ncells + 1)));
-        CNN_TRY(ctx->ensure(ctx->io_b, sizeof(int64_t) * (size_t)(geo.ncells + 1)));
+        CNN_TRY(ctx->ensure(ctx->io_b, sizeof(int64_t) * (size_t)(geo.ncells + 2)));  // + the slot total
         item_count_kernel<kUnitQueries><<<std::min<unsigned>(grid_for(geo.ncells, 256), 152u * 16u), 256, 0, st>>>(
             ctx->cell_start.as<int64_t>(), geo.ncells, ctx->io_a.as<int32_t>());
         CNN_LAUNCH_CHECK(ctx);
@@ -944,11 +942,9 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         CNN_LAUNCH_CHECK(ctx);
         CNN_TRY(scan_exclusive_i64(ctx, ctx->scratch_c.as<int64_t>(), slot_base, geo.ncells + 1));
         int64_t hcounts[2] = {0, 0};
-        CNN_CUDA(ctx, cudaMemcpyAsync(&hcounts[0], ctx->io_b.as<int64_t>() + geo.ncells, sizeof(int64_t),
-                                      cudaMemcpyDeviceToHost, st));
-        CNN_CUDA(ctx, cudaMemcpyAsync(&hcounts[1], slot_base + geo.ncells, sizeof(int64_t), cudaMemcpyDeviceToHost,
-                                      st));
-        CNN_CUDA(ctx, cudaStreamSynchronize(st));
+        CNN_CUDA(ctx, cudaMemcpyAsync(ctx->io_b.as<int64_t>() + geo.ncells + 1, slot_base + geo.ncells,
+                                      sizeof(int64_t), cudaMemcpyDeviceToDevice, st));  // both totals side by side
+        CNN_TRY(read_back(ctx, hcounts, ctx->io_b.as<int64_t>() + geo.ncells, 2 * sizeof(int64_t)));
         const int64_t nitems = hcounts[0];
         // one pass into slots when they take at most 4 GiB, else count + fill
         use_slots = hcounts[1] <= (int64_t(1) << 30);
@@ -1010,8 +1006,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     CNN_LAUNCH_CHECK(ctx);
     CNN_TRY(scan_exclusive_i32_to_i64(ctx, deg, row_off, n + 1));
     int64_t nnz = 0;
-    CNN_CUDA(ctx, cudaMemcpyAsync(&nnz, row_off + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-    CNN_CUDA(ctx, cudaStreamSynchronize(st));
+    CNN_TRY(read_back(ctx, &nnz, row_off + n, sizeof(int64_t)));
     stage_end(ctx, 3);
     CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1)));
 
