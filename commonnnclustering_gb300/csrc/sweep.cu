@@ -51,13 +51,19 @@ __device__ __forceinline__ double exact_s(const double *__restrict__ x, int d, i
 }
 
 // One warp per row of the r_max graph (internal order): bucket of each pair.
+// With deg_all, the same pass counts each row's pairs of every radius below
+// the largest (bucket <= k) into deg_all[k * (n + 1) + p] (entry n: 0).
 __global__ void bucket_kernel(const double *__restrict__ x, int d, int64_t n, const int32_t *__restrict__ perm,
                               const float4 *__restrict__ xf4, const int64_t *__restrict__ row_off,
                               const int32_t *__restrict__ cols, Ladder lad, uint8_t *__restrict__ bucket,
-                              unsigned long long *__restrict__ n_exact) {
+                              unsigned long long *__restrict__ n_exact, int kf, int32_t *__restrict__ deg_all) {
     const int lane = threadIdx.x & 31;
     const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (deg_all && p == 0 && lane < kf) deg_all[(int64_t)lane * (n + 1) + n] = 0;
     if (p >= n) return;
+    int32_t per_radius[kMaxRadii - 1];
+#pragma unroll
+    for (int k = 0; k < kMaxRadii - 1; ++k) per_radius[k] = 0;
     const float4 q = xf4[p];
     const int32_t ip = perm[p];
     unsigned long long ex = 0;
@@ -81,6 +87,16 @@ __global__ void bucket_kernel(const double *__restrict__ x, int d, int64_t n, co
             ++ex;
         }
         bucket[e] = (uint8_t)b;
+#pragma unroll
+        for (int k = 0; k < kMaxRadii - 1; ++k) per_radius[k] += b <= k;
+    }
+    if (deg_all) {
+#pragma unroll
+        for (int k = 0; k < kMaxRadii - 1; ++k) {
+            if (k >= kf) break;
+            const int32_t t = __reduce_add_sync(0xffffffffu, per_radius[k]);
+            if (lane == 0) deg_all[(int64_t)k * (n + 1) + p] = t;
+        }
     }
     for (int o = 16; o > 0; o >>= 1) ex += __shfl_down_sync(0xffffffffu, ex, o);
     if (lane == 0 && ex) atomicAdd(n_exact, ex);
@@ -114,39 +130,11 @@ __global__ void filter_fill_kernel(int64_t n, const int64_t *__restrict__ row_of
     }
 }
 
-// Every radius below the largest at once: one pass over the r_max rows
-// counts, per row, the pairs of each radius (bucket <= k); a second pass
-// writes each radius's filtered rows (stable, so still sorted).  Radius k's
-// arrays sit at k * (n + 1) in deg_all / off_all and at base[k] in cols_all.
+// Every radius below the largest at once: bucket_kernel counts, per row, the
+// pairs of each radius (bucket <= k); one pass writes each radius's filtered
+// rows (stable, so still sorted).  Radius k's arrays sit at k * (n + 1) in
+// deg_all / off_all and at base[k] in cols_all.
 constexpr int kMaxFiltered = kMaxRadii - 1;
-
-__global__ void __launch_bounds__(256) multi_count_kernel(int64_t n, const int64_t *__restrict__ row_off,
-                                                          const uint8_t *__restrict__ bucket, int kf,
-                                                          int32_t *__restrict__ deg_all) {
-    const int lane = threadIdx.x & 31;
-    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t p = warp0; p <= n; p += nwarps) {
-        if (p == n) {  // the scans read n + 1 entries
-            if (lane < kf) deg_all[(int64_t)lane * (n + 1) + n] = 0;
-            continue;
-        }
-        int32_t c[kMaxFiltered];
-#pragma unroll
-        for (int k = 0; k < kMaxFiltered; ++k) c[k] = 0;
-        for (int64_t e = row_off[p] + lane; e < row_off[p + 1]; e += 32) {
-            const int b = bucket[e];
-#pragma unroll
-            for (int k = 0; k < kMaxFiltered; ++k) c[k] += b <= k;
-        }
-#pragma unroll
-        for (int k = 0; k < kMaxFiltered; ++k) {
-            if (k >= kf) break;
-            const int32_t t = __reduce_add_sync(0xffffffffu, c[k]);
-            if (lane == 0) deg_all[(int64_t)k * (n + 1) + p] = t;
-        }
-    }
-}
 
 __global__ void __launch_bounds__(256) multi_fill_kernel(int64_t n, const int64_t *__restrict__ row_off,
                                                          const int32_t *__restrict__ cols,
@@ -330,9 +318,15 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
     CNN_TRY(ctx->ensure(ctx->sweep_bucket, (size_t)(nnz > 0 ? nnz : 1)));
     uint8_t *bucket = ctx->sweep_bucket.as<uint8_t>();
     unsigned long long *counters = ctx->counters.as<unsigned long long>();
+    const int kf = n_radii - 1;  // radii below the largest
+    int32_t *deg_all = nullptr;  // their row lengths, counted with the buckets
+    if (kf > 0 && n > 0) {
+        CNN_TRY(ctx->ensure(ctx->sweep_multi_deg, sizeof(int32_t) * (size_t)kf * (size_t)(n + 1)));
+        deg_all = ctx->sweep_multi_deg.as<int32_t>();
+    }
     bucket_kernel<<<grid_for(n * 32, 256), 256, 0, st>>>(ctx->x, d, n, ctx->perm.as<int32_t>(), ctx->xf4.as<float4>(),
                                                           ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), lad,
-                                                          bucket, counters + 15);
+                                                          bucket, counters + 15, kf, deg_all);
     CNN_LAUNCH_CHECK(ctx);
     std::swap(ctx->row_off, ctx->sweep_row_off_max);
     std::swap(ctx->cols, ctx->sweep_cols_max);
@@ -343,15 +337,10 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
     CNN_TRY(ctx->ensure(ctx->deg, sizeof(int32_t) * (size_t)(n + 1)));
 
     // every smaller radius's graph in two passes, when they fit in the budget
-    const int kf = n_radii - 1;
     if (kf > 0 && n > 0) {
-        CNN_TRY(ctx->ensure(ctx->sweep_multi_deg, sizeof(int32_t) * (size_t)kf * (size_t)(n + 1)));
         CNN_TRY(ctx->ensure(ctx->sweep_multi_off, sizeof(int64_t) * (size_t)kf * (size_t)(n + 1)));
-        int32_t *deg_all = ctx->sweep_multi_deg.as<int32_t>();
         int64_t *off_all = ctx->sweep_multi_off.as<int64_t>();
         const unsigned mgrid = std::min<unsigned>(grid_for((n + 1) * 32, 256), 152u * 16u);
-        multi_count_kernel<<<mgrid, 256, 0, st>>>(n, off_max, bucket, kf, deg_all);
-        CNN_LAUNCH_CHECK(ctx);
         for (int32_t k = 0; k < kf; ++k)
             CNN_TRY(scan_exclusive_i32_to_i64(ctx, deg_all + (size_t)k * (n + 1), off_all + (size_t)k * (n + 1), n + 1));
         std::vector<int64_t> nnz_k(kf), base(kf + 1, 0);
