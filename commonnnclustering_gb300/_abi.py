@@ -72,12 +72,14 @@ SIGNATURES = {
     "cnn_last_error": (ctypes.c_char_p, [_P]),
     "cnn_set_timing": (_INT, [_P, _INT]),
     "cnn_get_stats": (_INT, [_P, ctypes.POINTER(cnn_stats)]),
+    "cnn_set_wait_limit": (_INT, [_P, _I64]),
     "cnn_set_points": (_INT, [_P, _P, _INT, _I64, _I32, _INT]),
     "cnn_build_neighbours": (_INT, [_P, ctypes.c_double, _INT, _INT]),
     "cnn_set_neighbours": (_INT, [_P, _P, _P, _I64, _INT]),
     "cnn_neighbour_count": (_INT, [_P, ctypes.POINTER(_I64)]),
     "cnn_get_neighbours": (_INT, [_P, _P, _P, _INT]),
-    "cnn_fit": (_INT, [_P, _I64, _I64, _I64, _P, _P, _INT]),
+    "cnn_fit": (_INT, [_P, _I64, _I64, _I64, _P, _P, _I64, _INT]),
+    "cnn_graph_generation": (_INT, [_P, ctypes.POINTER(_I64)]),
     "cnn_sort_by_size": (_INT, [_P, _P, _I64, _I64, _I64, _INT]),
     "cnn_check_lists": (_INT, [_P, _P, _I64, _P, _I64, _I64, _P, _INT]),
     "cnn_fit_csr_noalloc": (_INT, [_P, _P, _I64, _I64, _I64, _I64, _P, _P, _P]),
@@ -216,6 +218,10 @@ class Context:
     def set_timing(self, enabled: bool):
         self._check(self._lib.cnn_set_timing(self._h, 1 if enabled else 0), "cnn_set_timing")
 
+    def set_wait_limit(self, limit_ns: int):
+        """Limit of the kernels' bounded waits (ns); <= 0: the default 2 s."""
+        self._check(self._lib.cnn_set_wait_limit(self._h, int(limit_ns)), "cnn_set_wait_limit")
+
     def stats(self) -> dict:
         s = cnn_stats()
         self._check(self._lib.cnn_get_stats(self._h, ctypes.byref(s)), "cnn_get_stats")
@@ -306,9 +312,24 @@ class Context:
                     "cnn_get_neighbours")
         return off, idx[:nnz]
 
+    def graph_generation(self) -> int:
+        """Changes whenever this context's points, distances, neighbourhoods
+        or neighbour graph are replaced (by any caller of the context)."""
+        v = ctypes.c_int64()
+        self._check(self._lib.cnn_graph_generation(self._h, ctypes.byref(v)), "cnn_graph_generation")
+        return int(v.value)
+
     # -- fit -------------------------------------------------------------------
     def fit(self, similarity_cutoff: int, n_member_cutoff: int, current_start: int, consider, labels):
-        """Cluster the current graph; labels/consider updated in place."""
+        """Cluster the current graph; labels/consider updated in place.
+
+        labels and consider must hold exactly one entry per point of the
+        current graph (ValueError otherwise, before the library is called).
+        """
+        n_lab, n_con = int(labels.shape[0]), int(consider.shape[0])
+        if n_lab != n_con or n_lab != int(self._n_points):
+            raise ValueError(f"labels ({n_lab}) and consider ({n_con}) must have one entry per point of the "
+                             f"current neighbour graph ({int(self._n_points)})")
         if is_device_array(labels):
             lp = device_pointer(labels, np.int64, writable=True)
             cp = device_pointer(consider, np.uint8, writable=True)
@@ -318,7 +339,7 @@ class Context:
             con = host_array(consider, np.uint8, writable=True)
             lp, cp, mem = lab.ctypes.data, con.ctypes.data, MEM_HOST
         self._check(self._lib.cnn_fit(self._h, int(similarity_cutoff), int(n_member_cutoff), int(current_start),
-                                      ctypes.c_void_p(cp), ctypes.c_void_p(lp), mem), "cnn_fit")
+                                      ctypes.c_void_p(cp), ctypes.c_void_p(lp), n_lab, mem), "cnn_fit")
 
     def sort_by_size(self, labels, member_cutoff: int, max_clusters: Optional[int]):
         mx = -1 if max_clusters is None else int(max_clusters)

@@ -99,8 +99,11 @@ class FitterGPU(Fitter):
             device).
         reuse_graph: keep the neighbour graph on the device between fits
             when the input is a CUDA tensor that has not been modified
-            (torch version counter) and the radius, metric and fpmode are
-            unchanged.  Host (numpy) inputs are always re-uploaded.
+            (torch version counter), the radius, metric and fpmode are
+            unchanged, and nothing else has replaced the graph of the
+            context since (the context's graph generation, which every other
+            user of a shared context changes).  Host (numpy) inputs are
+            always re-uploaded.
     """
 
     def __init__(self, neighbours_getter=None, neighbours=None, neighbour_neighbours=None,
@@ -114,7 +117,7 @@ class FitterGPU(Fitter):
         self._device = device
         self._context = context
         self.reuse_graph = reuse_graph
-        self._graph_key = None
+        self._graph_key = None  # (input identity, parameters, context, graph generation) of the last build
         self.last_stats: dict = {}
 
     def __str__(self):
@@ -173,11 +176,14 @@ class FitterGPU(Fitter):
                 and self._metric_code() != _abi.METRIC_EUCLIDEAN_PERIODIC_REDUCED):
             key = (id(data), int(data.data_ptr()), tuple(data.shape), int(data._version),
                    float(cluster_params.radius_cutoff), self._metric_code(), self._fpmode_code())
-        if key is not None and key == self._graph_key:
+        if (key is not None and self._graph_key is not None and self._graph_key[0] == key
+                and self._graph_key[1] is ctx and self._graph_key[2] == ctx.graph_generation()):
             return ctx
+        self._graph_key = None
         metric = load_input(ctx, input_data, self._neighbours_getter, self._metric_code())
         ctx.build_neighbours(cluster_params.radius_cutoff, metric, self._fpmode_code())
-        self._graph_key = key
+        if key is not None:
+            self._graph_key = (key, ctx, ctx.graph_generation())
         return ctx
 
     @staticmethod

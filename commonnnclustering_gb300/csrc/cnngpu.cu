@@ -90,10 +90,14 @@ CNN_API cnn_status cnn_create(cnn_context **out, int device, void *stream) {
     if (!ctx) return CNN_ERR_OOM;
     ctx->device = device;
     if (const char *pz = getenv("CNN_DEBUG_POISON")) ctx->poison = atoi(pz) & 0xff;
-    if (cudaSetDevice(device) != cudaSuccess) {
+    int sms = 0;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1) {
+        (void)cudaGetLastError();
         delete ctx;
         return CNN_ERR_CUDA;
     }
+    ctx->sm_count = (unsigned)sms;
     if (stream) {
         ctx->stream = static_cast<cudaStream_t>(stream);
     } else {
@@ -182,6 +186,12 @@ CNN_API cnn_status cnn_set_timing(cnn_context *ctx, int enabled) {
     return CNN_OK;
 }
 
+CNN_API cnn_status cnn_set_wait_limit(cnn_context *ctx, int64_t limit_ns) {
+    if (!ctx) return CNN_ERR_INVALID_ARG;
+    ctx->wait_limit_ns = limit_ns > 0 ? limit_ns : 0;
+    return CNN_OK;
+}
+
 CNN_API cnn_status cnn_get_stats(const cnn_context *cctx, cnn_stats *out) {
     cnn_context *ctx = const_cast<cnn_context *>(cctx);
     if (!ctx || !out) return CNN_ERR_INVALID_ARG;
@@ -222,6 +232,7 @@ CNN_API cnn_status cnn_set_points(cnn_context *ctx, const void *points, cnn_dtyp
     if (dtype != CNN_DTYPE_F64 && dtype != CNN_DTYPE_F32) return ctx->fail(CNN_ERR_INVALID_ARG, "bad dtype");
     if (mem != CNN_MEM_HOST && mem != CNN_MEM_DEVICE) return ctx->fail(CNN_ERR_INVALID_ARG, "bad memspace");
     ctx->have_graph = false;
+    ++ctx->graph_generation;
     ctx->dist = nullptr;
     ctx->dist_set = false;
     ctx->n = n_points;
@@ -266,6 +277,7 @@ CNN_API cnn_status cnn_set_distances(cnn_context *ctx, const double *distances, 
     const int64_t count = layout == CNN_DIST_SQUARE ? n_points * n_points : n_points * (n_points - 1) / 2;
     if (count > 0 && !distances) return ctx->fail(CNN_ERR_INVALID_ARG, "distances missing");
     ctx->have_graph = false;
+    ++ctx->graph_generation;
     ctx->x = nullptr;
     ctx->d = 0;
     ctx->n = n_points;
@@ -351,10 +363,15 @@ CNN_API cnn_status cnn_get_neighbours(cnn_context *ctx, int64_t *offsets, int32_
 }
 
 CNN_API cnn_status cnn_fit(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
-                           int64_t current_start, uint8_t *consider, int64_t *labels, cnn_memspace mem) {
+                           int64_t current_start, uint8_t *consider, int64_t *labels, int64_t n_points,
+                           cnn_memspace mem) {
     CNN_TRY(check_ctx(ctx));
     if (!ctx->have_graph) return ctx->fail(CNN_ERR_STATE, "no neighbour graph: build or set neighbours first");
     const int64_t n = ctx->n;
+    if (n_points != n)
+        return ctx->fail(CNN_ERR_INVALID_ARG, "labels/consider hold " + std::to_string(n_points) +
+                                                  " points, the neighbour graph " + std::to_string(n));
+    if (mem != CNN_MEM_HOST && mem != CNN_MEM_DEVICE) return ctx->fail(CNN_ERR_INVALID_ARG, "bad memspace");
     if (n > 0 && (!consider || !labels)) return ctx->fail(CNN_ERR_INVALID_ARG, "consider and labels are required");
     uint8_t *cons_dev = consider;
     int64_t *lab_dev = labels;
@@ -372,6 +389,12 @@ CNN_API cnn_status cnn_fit(cnn_context *ctx, int64_t similarity_cutoff, int64_t 
         CNN_CUDA(ctx, cudaMemcpyAsync(consider, cons_dev, (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
         CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     }
+    return CNN_OK;
+}
+
+CNN_API cnn_status cnn_graph_generation(const cnn_context *ctx, int64_t *generation) {
+    if (!ctx || !generation) return CNN_ERR_INVALID_ARG;
+    *generation = ctx->graph_generation;
     return CNN_OK;
 }
 

@@ -63,10 +63,12 @@ struct StageTimer {
 // The context behind the opaque cnn_context handle.
 struct cnn_context {
     int device = 0;
+    unsigned sm_count = 1;  // multiprocessors of `device` (cudaDevAttrMultiProcessorCount), sizes persistent grids
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     bool timing = false;
     int poison = -1;  // >= 0: fill every new workspace allocation with this byte (CNN_DEBUG_POISON)
+    int64_t wait_limit_ns = 0;  // > 0: limit of the bounded waits in the kernels (cnn_set_wait_limit)
     int64_t n_launches = 0;
     std::string last_error;
     cnn_stats stats{};
@@ -97,8 +99,10 @@ struct cnn_context {
     std::vector<double> periodic_bounds;
     cnn::DevBuf bounds_dev;
 
-    // neighbour graph in internal (permuted) index space
+    // neighbour graph in internal (permuted) index space; graph_generation
+    // changes with every replaced input or rebuilt graph (cnn_graph_generation)
     bool have_graph = false;
+    int64_t graph_generation = 0;
     bool identity_perm = true;
     int64_t nnz = 0;
     cnn::DevBuf perm;     // int32[n]: internal -> point index

@@ -39,12 +39,6 @@ namespace cnn {
 
 namespace {
 
-// candidate edges each node checks in the hook pass
-#ifndef CNN_HOOK_EDGES
-#define CNN_HOOK_EDGES 3
-#endif
-constexpr int32_t kHookEdges = CNN_HOOK_EDGES;
-
 // ---- cross-edge worklist ------------------------------------------------------
 // After the hook pass and a full compression, parent[] holds every node's
 // root.  A read-only pass streams the graph and keeps only candidate edges
@@ -478,7 +472,7 @@ __global__ void check_lists_kernel(const int32_t *__restrict__ a, int64_t na, co
     if (lane == 0) *result = r;
 }
 
-unsigned blocks_for(int64_t n) { return std::min<unsigned>(grid_for(n, 256), 152u * 16u); }
+unsigned blocks_for(const cnn_context *ctx, int64_t n) { return std::min<unsigned>(grid_for(n, 256), ctx->sm_count * 16u); }
 
 }  // namespace
 
@@ -524,11 +518,11 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     const int32_t *perm = ctx->perm.as<int32_t>();
 
     stage_begin(ctx, 5);
-    node_kernel<<<blocks_for(n), 256, 0, st>>>(ctx->deg.as<int32_t>(), perm, consider_dev, n, n_member_cutoff,
+    node_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(ctx->deg.as<int32_t>(), perm, consider_dev, n, n_member_cutoff,
                                                node, parent, comp_min, counters);
     CNN_LAUNCH_CHECK(ctx);
     if (seed_a || seed_b) {
-        seed_union_kernel<<<blocks_for(n), 256, 0, st>>>(n, node, parent, seed_a, seed_b);
+        seed_union_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(n, node, parent, seed_a, seed_b);
         CNN_LAUNCH_CHECK(ctx);
     }
     stage_end(ctx, 5);
@@ -543,7 +537,7 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
             (void)cudaGetLastError();
             per_sm = 8;
-            sms = 152;
+            sms = (int)ctx->sm_count;
         }
         return std::min<unsigned>(grid_for(n, kCheckWarps), (unsigned)std::max(1, per_sm * sms));
     };
@@ -554,7 +548,7 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
         n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff, kHookEdges,
         counters, seed_a, seed_b);
     CNN_LAUNCH_CHECK(ctx);
-    root_store_kernel<<<blocks_for(n), 256, 0, st>>>(n, node, parent);
+    root_store_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(n, node, parent);
     CNN_LAUNCH_CHECK(ctx);
     // cross edges between the hooked sets -> worklist -> checks
     // worklist capacity: a list-fed filter (pairs a finished fit left open)
@@ -567,7 +561,7 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     CNN_CUDA(ctx, cudaMemsetAsync(wl_count, 0, sizeof(unsigned long long), st));
     if (edge_list) {
         // only pairs a finished fit that refines this one left open can cross
-        cross_filter_list_kernel<<<152u * 16u, 256, 0, st>>>(edge_list, edge_count, parent, ctx->io_c.as<int2>(),
+        cross_filter_list_kernel<<<ctx->sm_count * 16u, 256, 0, st>>>(edge_list, edge_count, parent, ctx->io_c.as<int2>(),
                                                              wl_count, wl_cap);
     } else {
         cross_filter_kernel<<<resident((const void *)cross_filter_kernel, 256, 0), 256, 0, st>>>(
@@ -589,14 +583,14 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     int32_t *flag = ctx->flag.as<int32_t>();
     int64_t *rank = ctx->scratch_a.as<int64_t>();
     CNN_CUDA(ctx, cudaMemsetAsync(flag, 0, sizeof(int32_t) * (size_t)(n + 1), st));
-    root_min_kernel<<<blocks_for(n), 256, 0, st>>>(n, node, parent, perm, comp_min);
+    root_min_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(n, node, parent, perm, comp_min);
     CNN_LAUNCH_CHECK(ctx);
-    root_store_kernel<<<blocks_for(n), 256, 0, st>>>(n, node, parent);
+    root_store_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(n, node, parent);
     CNN_LAUNCH_CHECK(ctx);
-    min_flag_kernel<<<blocks_for(n), 256, 0, st>>>(n, node, parent, comp_min, flag);
+    min_flag_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(n, node, parent, comp_min, flag);
     CNN_LAUNCH_CHECK(ctx);
     CNN_TRY(scan_exclusive_i32_to_i64(ctx, flag, rank, n + 1));
-    label_kernel<<<blocks_for(n), 256, 0, st>>>(n, node, parent, comp_min, perm, rank, current_start, labels_dev);
+    label_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(n, node, parent, comp_min, perm, rank, current_start, labels_dev);
     CNN_LAUNCH_CHECK(ctx);
     // every point with consider == 1 is visited by the reference loop and
     // left at consider == 0; points already at 0 stay 0
@@ -632,7 +626,7 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64
     long long *range = ctx->io_c.as<long long>();
     init_range_kernel<<<1, 1, 0, st>>>(range);
     CNN_LAUNCH_CHECK(ctx);
-    label_range_kernel<<<blocks_for(n), 256, 0, st>>>(labels, n, range);
+    label_range_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(labels, n, range);
     CNN_LAUNCH_CHECK(ctx);
     long long hr[3];
     CNN_CUDA(ctx, cudaMemcpyAsync(hr, range, sizeof(hr), cudaMemcpyDeviceToHost, st));
@@ -649,14 +643,14 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64
         int32_t *cnt = ctx->scratch_b.as<int32_t>();
         int32_t *first = cnt + r;
         int64_t *newlab = reinterpret_cast<int64_t *>((reinterpret_cast<uintptr_t>(first + r) + 15) & ~uintptr_t(15));
-        init_count_first_kernel<<<blocks_for(r), 256, 0, st>>>(cnt, first, r);
+        init_count_first_kernel<<<blocks_for(ctx, r), 256, 0, st>>>(cnt, first, r);
         CNN_LAUNCH_CHECK(ctx);
-        count_first_dense_kernel<<<blocks_for(n), 256, 0, st>>>(labels, n, lo, cnt, first);
+        count_first_dense_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(labels, n, lo, cnt, first);
         CNN_LAUNCH_CHECK(ctx);
         order_small_kernel<<<(unsigned)((r + kOrderWarps - 1) / kOrderWarps), kOrderWarps * 32, 0, st>>>(
             cnt, first, r, n, bits_for_fit(n), member_cutoff, max_clusters, newlab);
         CNN_LAUNCH_CHECK(ctx);
-        apply_dense_kernel<<<blocks_for(n), 256, 0, st>>>(labels, n, lo, newlab);
+        apply_dense_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(labels, n, lo, newlab);
         CNN_LAUNCH_CHECK(ctx);
         stage_end(ctx, 8);
         return CNN_OK;
@@ -668,7 +662,7 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64
     int64_t r;
     if (span <= 4.0 * (double)n + 1024.0) {
         r = (int64_t)(hi - lo + 1);
-        dense_id_kernel<<<blocks_for(n), 256, 0, st>>>(labels, n, lo, ids);
+        dense_id_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(labels, n, lo, ids);
         CNN_LAUNCH_CHECK(ctx);
     } else {
         CNN_TRY(ctx->ensure(ctx->io_b, sizeof(uint64_t) * (size_t)n * 2 + 64));
@@ -676,21 +670,21 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64
         uint64_t *uniq = keys + n;
         CNN_TRY(ctx->ensure(ctx->flag, sizeof(int32_t) * (size_t)(n + 1)));
         CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(int64_t) * (size_t)(n + 1)));
-        label_keys_kernel<<<blocks_for(n), 256, 0, st>>>(labels, n, keys);
+        label_keys_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(labels, n, keys);
         CNN_LAUNCH_CHECK(ctx);
         CNN_TRY(radix_sort_u64(ctx, keys, n, 64));
         int32_t *flag = ctx->flag.as<int32_t>();
         int64_t *pos = ctx->scratch_a.as<int64_t>();
-        unique_flag_kernel<<<blocks_for(n), 256, 0, st>>>(keys, n, flag);
+        unique_flag_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(keys, n, flag);
         CNN_LAUNCH_CHECK(ctx);
         CNN_CUDA(ctx, cudaMemsetAsync(flag + n, 0, sizeof(int32_t), st));
         CNN_TRY(scan_exclusive_i32_to_i64(ctx, flag, pos, n + 1));
-        unique_compact_kernel<<<blocks_for(n), 256, 0, st>>>(keys, flag, pos, n, uniq);
+        unique_compact_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(keys, flag, pos, n, uniq);
         CNN_LAUNCH_CHECK(ctx);
         int64_t nu = 0;
         CNN_CUDA(ctx, cudaMemcpyAsync(&nu, pos + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
         CNN_CUDA(ctx, cudaStreamSynchronize(st));
-        sparse_id_kernel<<<blocks_for(n), 256, 0, st>>>(labels, n, uniq, nu, ids);
+        sparse_id_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(labels, n, uniq, nu, ids);
         CNN_LAUNCH_CHECK(ctx);
         r = nu;
     }
@@ -700,12 +694,12 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64
     int32_t *first = cnt + r;
     CNN_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (size_t)r, st));
     CNN_TRY(fill_i32(ctx, first, r, INT32_MAX));
-    count_first_kernel<<<blocks_for(n), 256, 0, st>>>(ids, n, cnt, first);
+    count_first_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(ids, n, cnt, first);
     CNN_LAUNCH_CHECK(ctx);
     CNN_TRY(ctx->ensure(ctx->scratch_d, sizeof(int32_t) * (size_t)(r + 1) + sizeof(int64_t) * (size_t)(r + 1) + 64));
     int32_t *cflag = ctx->scratch_d.as<int32_t>();
     int64_t *cpos = reinterpret_cast<int64_t *>((reinterpret_cast<uintptr_t>(cflag + r + 1) + 15) & ~uintptr_t(15));
-    cluster_flag_kernel<<<blocks_for(r + 1), 256, 0, st>>>(cnt, r, cflag);
+    cluster_flag_kernel<<<blocks_for(ctx, r + 1), 256, 0, st>>>(cnt, r, cflag);
     CNN_LAUNCH_CHECK(ctx);
     CNN_TRY(scan_exclusive_i32_to_i64(ctx, cflag, cpos, r + 1));
     int64_t k = 0;
@@ -715,13 +709,13 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64
     CNN_TRY(ctx->ensure(ctx->io_b, sizeof(uint64_t) * (size_t)(k + 1) + sizeof(int64_t) * (size_t)(r + 1) + 64));
     uint64_t *ckeys = ctx->io_b.as<uint64_t>();
     int64_t *newlab = reinterpret_cast<int64_t *>(ckeys + k + 1);
-    cluster_key_kernel<<<blocks_for(r), 256, 0, st>>>(cnt, first, cpos, r, n, bits_n, ckeys);
+    cluster_key_kernel<<<blocks_for(ctx, r), 256, 0, st>>>(cnt, first, cpos, r, n, bits_n, ckeys);
     CNN_LAUNCH_CHECK(ctx);
     CNN_TRY(radix_sort_u64(ctx, ckeys, k, bits_n + bits_for_fit(n + 1)));
     const int64_t maxc = max_clusters < 0 ? k : max_clusters;
-    new_label_kernel<<<blocks_for(k), 256, 0, st>>>(ckeys, k, n, bits_n, ids, member_cutoff, maxc, newlab);
+    new_label_kernel<<<blocks_for(ctx, k), 256, 0, st>>>(ckeys, k, n, bits_n, ids, member_cutoff, maxc, newlab);
     CNN_LAUNCH_CHECK(ctx);
-    apply_label_kernel<<<blocks_for(n), 256, 0, st>>>(labels, ids, n, newlab);
+    apply_label_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(labels, ids, n, newlab);
     CNN_LAUNCH_CHECK(ctx);
     stage_end(ctx, 8);
     return CNN_OK;
@@ -754,10 +748,10 @@ cnn_status open_pairs_impl(cnn_context *ctx, const int2 *in_list, const unsigned
     CNN_CUDA(ctx, cudaMemsetAsync(out_count, 0, sizeof(unsigned long long), st));
     if (n == 0) return CNN_OK;
     if (in_list) {
-        open_pairs_list_kernel<<<152u * 16u, 256, 0, st>>>(in_list, in_count, ctx->node.as<uint8_t>(),
+        open_pairs_list_kernel<<<ctx->sm_count * 16u, 256, 0, st>>>(in_list, in_count, ctx->node.as<uint8_t>(),
                                                             ctx->parent.as<int32_t>(), out, out_count, cap);
     } else {
-        open_pairs_csr_kernel<<<std::min<unsigned>(grid_for(n * 32, 256), 152u * 16u), 256, 0, st>>>(
+        open_pairs_csr_kernel<<<std::min<unsigned>(grid_for(n * 32, 256), ctx->sm_count * 16u), 256, 0, st>>>(
             n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), ctx->node.as<uint8_t>(),
             ctx->parent.as<int32_t>(), out, out_count, cap);
     }

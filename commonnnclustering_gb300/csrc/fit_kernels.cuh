@@ -12,6 +12,12 @@ namespace {
 
 constexpr int kCheckWarps = 8;
 
+// candidate edges each node checks in the hook pass
+#ifndef CNN_HOOK_EDGES
+#define CNN_HOOK_EDGES 3
+#endif
+constexpr int32_t kHookEdges = CNN_HOOK_EDGES;
+
 __device__ __forceinline__ int32_t uf_find(int32_t *parent, int32_t x) {
     int32_t cur = x;
     int32_t next = *(volatile int32_t *)&parent[cur];

@@ -55,7 +55,8 @@ constexpr int kStageBytes = 2 * kSplits * kTileBytes;  // A_hi, A_mid, A_lo, B_h
 constexpr int kGramThreads = 320;  // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
 constexpr uint32_t kAccCols = 256;   // per accumulator buffer: hi.hi (128 columns), then the cross terms (128)
 constexpr uint32_t kTmemCols = 512;  // two buffers
-constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
+constexpr unsigned long long kWaitNs = 2000000000ull;   // default limit of a pipeline wait (2 s)
+constexpr unsigned long long kDrainNs = 2000000000ull;  // limit of the drains before exit (copies, MMAs)
 
 struct GramArgs {
     int64_t n;
@@ -78,6 +79,7 @@ struct GramArgs {
     unsigned long long *namb;
     int64_t amb_cap;
     int *status;            // nonzero on a timed-out wait
+    unsigned long long wait_ns;  // limit of every pipeline wait (nanoseconds)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -115,17 +117,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait on an mbarrier phase.  Returns false on timeout or when
+// Bounded wait on an mbarrier phase.  Returns false after limit_ns or when
 // another warp has already given up (abort flag in shared memory).
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag) {
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
+                                          unsigned long long limit_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = globaltimer();
     for (;;) {
         if (mbar_try_wait(bar, parity)) return true;
         if (*abort_flag) return false;
-        if (globaltimer() - t0 > kWaitNs) return false;
+        if (globaltimer() - t0 > limit_ns) return false;
         __nanosleep(32);  // back off: waiting warps leave issue slots and shared-memory bandwidth
     }
+}
+
+// Wait for a phase that is certain to complete (copies already issued), also
+// after an abort: the CTA may not exit while a copy still writes its shared
+// memory.  Bounded by kDrainNs all the same.
+__device__ __forceinline__ void mbar_drain(uint64_t *bar, uint32_t parity) {
+    const uint64_t t0 = globaltimer();
+    while (!mbar_try_wait(bar, parity) && globaltimer() - t0 < kDrainNs) __nanosleep(32);
 }
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int c0, int c1, uint64_t *bar) {
@@ -328,7 +339,7 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
                 for (int32_t kb = 0; kb < args.nkb; ++kb, ++it) {
                     const int s = (int)(it % kStages);
                     const uint32_t ph = (uint32_t)((it / kStages) & 1);
-                    if (!mbar_wait(&empty_bar[s], ph ^ 1u, abort_flag)) { ok = false; break; }
+                    if (!mbar_wait(&empty_bar[s], ph ^ 1u, abort_flag, args.wait_ns)) { ok = false; break; }
                     uint8_t *st = smem + s * kStageBytes;
                     mbar_expect_tx(&full_bar[s], kStageBytes);
                     tma_load_2d(st + 0 * kTileBytes, &map_hi, kb * kKB, I * kTM, &full_bar[s]);
@@ -344,9 +355,10 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
                 *abort_flag = 1;
             }
             // drain: every issued stage must have landed before the CTA exits
+            // (not abortable: the copies complete whatever the other warps do)
             const int64_t issued = it;
             for (int64_t k = issued > kStages ? issued - kStages : 0; k < issued; ++k)
-                mbar_wait(&full_bar[(int)(k % kStages)], (uint32_t)((k / kStages) & 1), abort_flag);
+                mbar_drain(&full_bar[(int)(k % kStages)], (uint32_t)((k / kStages) & 1));
         }
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
@@ -356,14 +368,14 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
             for (int64_t tl = 0; tl < my_tiles && ok; ++tl) {
                 const int b = (int)(tl & 1);
                 const uint32_t acc_ph = (uint32_t)((tl >> 1) & 1);
-                if (!mbar_wait(&acce_bar[b], acc_ph ^ 1u, abort_flag)) { ok = false; break; }
+                if (!mbar_wait(&acce_bar[b], acc_ph ^ 1u, abort_flag, args.wait_ns)) { ok = false; break; }
                 fence_after_sync();
                 const uint32_t d_hh = tmem_base + (uint32_t)(b * kAccCols);  // hi.hi
                 const uint32_t d_x = d_hh + (uint32_t)kTM;                      // cross terms
                 for (int32_t kb = 0; kb < args.nkb; ++kb, ++it) {
                     const int s = (int)(it % kStages);
                     const uint32_t ph = (uint32_t)((it / kStages) & 1);
-                    if (!mbar_wait(&full_bar[s], ph, abort_flag)) { ok = false; break; }
+                    if (!mbar_wait(&full_bar[s], ph, abort_flag, args.wait_ns)) { ok = false; break; }
                     fence_after_sync();
                     const uint32_t st = smem_u32(smem + s * kStageBytes);
 #pragma unroll
@@ -393,9 +405,7 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
             }
             // every MMA this thread issued has finished before TMEM is freed
             umma_commit(&done_bar);
-            const uint64_t t0 = globaltimer();
-            while (!mbar_try_wait(&done_bar, 0) && globaltimer() - t0 < kWaitNs) {
-            }
+            mbar_drain(&done_bar, 0);
         }
     } else {
         // ---------------- epilogue (warps 2..9) ----------------
@@ -410,7 +420,7 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
             const int32_t I = tile.x, J = tile.y;
             const int b = (int)(tl & 1);
             const uint32_t acc_ph = (uint32_t)((tl >> 1) & 1);
-            if (!mbar_wait(&accf_bar[b], acc_ph, abort_flag)) {
+            if (!mbar_wait(&accf_bar[b], acc_ph, abort_flag, args.wait_ns)) {
                 atomicExch(args.status, 3);
                 *abort_flag = 1;
                 break;
@@ -1083,7 +1093,7 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
         // block = a multiple of n_dim (at most 1024 threads); grid stride a multiple too
         const int per = std::max(1, 256 / d), threads = d * per;
         if (threads > 1024) return CNN_OK;  // n_dim > 1024: the all-pairs path takes it
-        const int blocks = (int)std::min<int64_t>(152 * 4, (n * d + threads - 1) / threads);
+        const int blocks = (int)std::min<int64_t>((int64_t)ctx->sm_count * 4, (n * d + threads - 1) / threads);
         column_sum_kernel<<<blocks, threads, sizeof(double) * threads, st>>>(ctx->x, n, d, colsum, nonfinite);
         CNN_LAUNCH_CHECK(ctx);
         column_mean_kernel<<<1, 128, 0, st>>>(colsum, d, n);  // colsum holds the column means from here
@@ -1102,13 +1112,13 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
         const int dk = (d + 15) & ~15, np8 = (n_groups + 7) & ~7;
         const size_t psmem = sizeof(uint32_t) * (size_t)np8 * (dk / 2 + 4) + sizeof(float) * (size_t)np8;
         CNN_TRY(allow_dynamic_smem(ctx, (const void *)pivot_assign_kernel, psmem));
-        pivot_assign_kernel<<<152u * 4u, 256, psmem, st>>>(ctx->x, n, d, colsum, n_groups, bits_n, pkeys);
+        pivot_assign_kernel<<<ctx->sm_count * 4u, 256, psmem, st>>>(ctx->x, n, d, colsum, n_groups, bits_n, pkeys);
         CNN_LAUNCH_CHECK(ctx);
         int pb = 1;
         while ((1 << pb) < n_groups) ++pb;
         CNN_TRY(radix_sort_u64(ctx, pkeys, n, bits_n + pb, bits_n));  // built in point order
         CNN_CUDA(ctx, cudaMemsetAsync(gcount, 0, sizeof(int32_t) * n_groups, st));
-        group_count_kernel<<<std::min<unsigned>(grid_for(n, 256), 152u * 2u), 256, sizeof(int32_t) * n_groups, st>>>(
+        group_count_kernel<<<std::min<unsigned>(grid_for(n, 256), ctx->sm_count * 2u), 256, sizeof(int32_t) * n_groups, st>>>(
             pkeys, n, bits_n, n_groups, gcount);
         CNN_LAUNCH_CHECK(ctx);
         group_layout_kernel<<<1, 32, 0, st>>>(gcount, n_groups, gstart, gpstart);
@@ -1204,10 +1214,11 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     a.blk_norm = reinterpret_cast<const float *>(blk_norm_bits);
     a.blk_norm2 = reinterpret_cast<const float *>(blk_norm2_bits);
     a.status = status;
+    a.wait_ns = ctx->wait_limit_ns > 0 ? (unsigned long long)ctx->wait_limit_ns : kWaitNs;
     // the float32 threshold must itself be an upper/lower bound of rc2
     int64_t key_cap = std::max<int64_t>(ctx->gram_key_hint, std::min<int64_t>(n * 256, int64_t(1) << 31));
     const int64_t amb_cap = std::max<int64_t>(int64_t(1) << 22, n * 64);
-    const int sms = 152;
+    const int sms = (int)ctx->sm_count;
     int dev_sms = 0;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, dev);
     const int grid = (int)std::min<int64_t>(ntiles, dev_sms > 0 ? dev_sms : sms);
@@ -1230,11 +1241,11 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
         CNN_LAUNCH_CHECK(ctx);
         stage_end(ctx, 9);
         // internal indices -> point indices (before the recheck appends more keys)
-        map_keys_kernel<<<152u * 8u, 256, 0, st>>>(a.keys, nkeys, key_cap, perm, bits_n);
+        map_keys_kernel<<<ctx->sm_count * 8u, 256, 0, st>>>(a.keys, nkeys, key_cap, perm, bits_n);
         CNN_LAUNCH_CHECK(ctx);
-        map_keys_kernel<<<152u * 8u, 256, 0, st>>>(a.amb, namb, amb_cap, perm, 0);
+        map_keys_kernel<<<ctx->sm_count * 8u, 256, 0, st>>>(a.amb, namb, amb_cap, perm, 0);
         CNN_LAUNCH_CHECK(ctx);
-        gram_recheck_kernel<<<152u * 8u, kRecheckWarps * 32, 0, st>>>(
+        gram_recheck_kernel<<<ctx->sm_count * 8u, kRecheckWarps * 32, 0, st>>>(
             ctx->x, d, a.amb, namb, amb_cap, radius_cutoff, metric, fpmode, a.keys, nkeys, key_cap, a.amb_d2,
             max_err_bits, bits_n);
         CNN_LAUNCH_CHECK(ctx);
@@ -1263,10 +1274,10 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
             CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nk > 0 ? nk : 1)));
             int64_t *row_off_csr = ctx->row_off.as<int64_t>();
             if (nk == 0) CNN_CUDA(ctx, cudaMemsetAsync(row_off_csr, 0, sizeof(int64_t) * (size_t)(n + 1), st));
-            keys_rows_kernel<<<std::min<unsigned>(grid_for(nk, 256), 152u * 16u), 256, 0, st>>>(
+            keys_rows_kernel<<<std::min<unsigned>(grid_for(nk, 256), ctx->sm_count * 16u), 256, 0, st>>>(
                 sorted, nk, bits_n, n, row_off_csr, ctx->cols.as<int32_t>());
             CNN_LAUNCH_CHECK(ctx);
-            degree_from_offsets_kernel<<<std::min<unsigned>(grid_for(n + 1, 256), 152u * 16u), 256, 0, st>>>(
+            degree_from_offsets_kernel<<<std::min<unsigned>(grid_for(n + 1, 256), ctx->sm_count * 16u), 256, 0, st>>>(
                 row_off_csr, n, ctx->deg.as<int32_t>());
             CNN_LAUNCH_CHECK(ctx);
             ctx->nnz = nk;

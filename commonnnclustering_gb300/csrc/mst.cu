@@ -126,7 +126,7 @@ cnn_status mst_prim_impl(cnn_context *ctx, double radius_cutoff, int metric, int
     CNN_TRY(ctx->ensure(ctx->pred_xcols, sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1)));
     CNN_TRY(export_neighbours_impl(ctx, ctx->pred_off.as<int64_t>(), ctx->pred_cols.as<int32_t>()));
     int32_t *weight = ctx->pred_xcols.as<int32_t>();
-    const unsigned blocks = std::min<unsigned>(grid_for(n * 32, 256), 152u * 16u);
+    const unsigned blocks = std::min<unsigned>(grid_for(n * 32, 256), ctx->sm_count * 16u);
     pair_weight_kernel<<<blocks, 256, 0, st>>>(n, ctx->pred_off.as<int64_t>(), ctx->pred_cols.as<int32_t>(), weight);
     CNN_LAUNCH_CHECK(ctx);
     mirror_weight_kernel<<<blocks, 256, 0, st>>>(n, ctx->pred_off.as<int64_t>(), ctx->pred_cols.as<int32_t>(), weight);

@@ -114,7 +114,7 @@ cnn_status predict_impl(cnn_context *ctx, const double *xq, int64_t m, const int
     // _types.pyx:2327-2345, sums (a - b)^2): kept alike
     const int xmetric = metric == CNN_METRIC_EUCLIDEAN_PERIODIC_REDUCED ? CNN_METRIC_EUCLIDEAN_REDUCED : metric;
     CNN_TRY(cross_neighbours_impl(ctx, xq, m, radius_cutoff, xmetric, fpmode, ctx->pred_xoff, ctx->pred_xcols, &xnnz));
-    const unsigned blocks = std::min<unsigned>(grid_for(m * 32, 256), 152u * 16u);
+    const unsigned blocks = std::min<unsigned>(grid_for(m * 32, 256), ctx->sm_count * 16u);
     predict_kernel<<<blocks, 256, 0, st>>>(m, ctx->pred_xoff.as<int64_t>(), ctx->pred_xcols.as<int32_t>(),
                                            ctx->pred_off.as<int64_t>(), ctx->pred_cols.as<int32_t>(), labels_dev,
                                            clusters_sorted_dev, n_clusters, similarity_cutoff, n_member_cutoff,

@@ -718,6 +718,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     const int d = ctx->d;
     cudaStream_t st = ctx->stream;
     ctx->have_graph = false;
+    ++ctx->graph_generation;
     ctx->stats = cnn_stats{};
     ctx->search_stats_pending = false;
     ctx->fit_stats_pending = false;
@@ -750,7 +751,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         int64_t *row_off = ctx->row_off.as<int64_t>();
         CNN_TRY(iota_i32(ctx, ctx->perm.as<int32_t>(), n));
         CNN_TRY(iota_i32(ctx, ctx->inv.as<int32_t>(), n));
-        const unsigned blocks = std::min<unsigned>(grid_for(n * 32, 256), 152u * 16u);
+        const unsigned blocks = std::min<unsigned>(grid_for(n * 32, 256), ctx->sm_count * 16u);
         stage_begin(ctx, 2);
         distance_rows_kernel<false><<<blocks, 256, 0, st>>>(ctx->dist, ctx->dist_layout, n, radius_cutoff, deg, nullptr,
                                                             nullptr);
@@ -914,7 +915,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         CNN_TRY(ctx->ensure(ctx->xf4, sizeof(float4) * (size_t)n));
         int32_t *cell_count = ctx->scratch_b.as<int32_t>();
         CNN_CUDA(ctx, cudaMemsetAsync(cell_count, 0, sizeof(int32_t) * (size_t)(geo.ncells + 2), st));
-        const unsigned gb = std::min<unsigned>(grid_for(n, 256), 152u * 16u);
+        const unsigned gb = std::min<unsigned>(grid_for(n, 256), ctx->sm_count * 16u);
         int32_t *slot = ctx->scratch_a.as<int32_t>();
         cell_assign_kernel<<<gb, 256, 0, st>>>(ctx->x, n, d, geo, ctx->cell_of.as<int32_t>(), slot, cell_count);
         CNN_LAUNCH_CHECK(ctx);
@@ -927,7 +928,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         // work items: (cell, first query) for every 32 queries of a cell
         CNN_TRY(ctx->ensure(ctx->io_a, sizeof(int32_t) * (size_t)(geo.ncells + 1)));
         CNN_TRY(ctx->ensure(ctx->io_b, sizeof(int64_t) * (size_t)(geo.ncells + 2)));  // + the slot total
-        item_count_kernel<kUnitQueries><<<std::min<unsigned>(grid_for(geo.ncells, 256), 152u * 16u), 256, 0, st>>>(
+        item_count_kernel<kUnitQueries><<<std::min<unsigned>(grid_for(geo.ncells, 256), ctx->sm_count * 16u), 256, 0, st>>>(
             ctx->cell_start.as<int64_t>(), geo.ncells, ctx->io_a.as<int32_t>());
         CNN_LAUNCH_CHECK(ctx);
         CNN_CUDA(ctx, cudaMemsetAsync(ctx->io_a.as<int32_t>() + geo.ncells, 0, sizeof(int32_t), st));
@@ -937,7 +938,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         int64_t *slot_base = ctx->grid_slot_base.as<int64_t>();
         CNN_TRY(ctx->ensure(ctx->scratch_c, sizeof(int64_t) * (size_t)(geo.ncells + 2)));
         CNN_CUDA(ctx, cudaMemsetAsync(ctx->scratch_c.as<int64_t>() + geo.ncells, 0, sizeof(int64_t), st));
-        cell_slots_kernel<<<std::min<unsigned>(grid_for(geo.ncells, 256), 152u * 16u), 256, 0, st>>>(
+        cell_slots_kernel<<<std::min<unsigned>(grid_for(geo.ncells, 256), ctx->sm_count * 16u), 256, 0, st>>>(
             ctx->cell_start.as<int64_t>(), geo, ctx->scratch_c.as<int64_t>());
         CNN_LAUNCH_CHECK(ctx);
         CNN_TRY(scan_exclusive_i64(ctx, ctx->scratch_c.as<int64_t>(), slot_base, geo.ncells + 1));
@@ -953,7 +954,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
             CNN_TRY(ctx->ensure(ctx->grid_qslot, sizeof(int64_t) * (size_t)n));
         }
         CNN_TRY(ctx->ensure(ctx->io_c, sizeof(int2) * (size_t)(nitems > 0 ? nitems : 1)));
-        item_fill_kernel<kUnitQueries><<<std::min<unsigned>(grid_for(geo.ncells, 256), 152u * 16u), 256, 0, st>>>(
+        item_fill_kernel<kUnitQueries><<<std::min<unsigned>(grid_for(geo.ncells, 256), ctx->sm_count * 16u), 256, 0, st>>>(
             ctx->cell_start.as<int64_t>(), geo.ncells, ctx->io_b.as<int64_t>(), ctx->io_c.as<int2>());
         CNN_LAUNCH_CHECK(ctx);
         grid_items = nitems;
@@ -983,7 +984,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         CNN_TRY(ctx->ensure(ctx->scratch_b, sizeof(float) * (size_t)n * d));
         CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(double) * (size_t)d + 64));
         CNN_CUDA(ctx, cudaMemcpyAsync(ctx->scratch_a.ptr, lo.data(), sizeof(double) * d, cudaMemcpyHostToDevice, st));
-        const unsigned gb = std::min<unsigned>(grid_for(n * d, 256), 152u * 16u);
+        const unsigned gb = std::min<unsigned>(grid_for(n * d, 256), ctx->sm_count * 16u);
         to_f32_kernel<<<gb, 256, 0, st>>>(ctx->x, n, d, ctx->scratch_a.as<double>(), ctx->scratch_b.as<float>());
         CNN_LAUNCH_CHECK(ctx);
         stage_end(ctx, 1);
@@ -1013,7 +1014,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     stage_begin(ctx, 4);
     if (use_grid) {
         if (grid_items > 0 && use_slots) {
-            compact_rows_kernel<<<std::min<unsigned>(grid_for(n * 32, 256), 152u * 16u), 256, 0, st>>>(
+            compact_rows_kernel<<<std::min<unsigned>(grid_for(n * 32, 256), ctx->sm_count * 16u), 256, 0, st>>>(
                 n, ctx->grid_qslot.as<int64_t>(), ctx->grid_slot_cols.as<int32_t>(), row_off,
                 ctx->cols.as<int32_t>());
             CNN_LAUNCH_CHECK(ctx);
@@ -1076,7 +1077,7 @@ cnn_status export_neighbours_impl(cnn_context *ctx, int64_t *offsets_dev, int32_
     CNN_LAUNCH_CHECK(ctx);
     uint64_t *sorted = keys;
     CNN_TRY(radix_sort_u64(ctx, keys, nnz, 2 * bits_n, 0, &sorted));
-    keys_to_cols_kernel<<<std::min<unsigned>(grid_for(nnz, 256), 152u * 32u), 256, 0, st>>>(sorted, nnz, bits_n,
+    keys_to_cols_kernel<<<std::min<unsigned>(grid_for(nnz, 256), ctx->sm_count * 32u), 256, 0, st>>>(sorted, nnz, bits_n,
                                                                                              indices_dev);
     CNN_LAUNCH_CHECK(ctx);
     return CNN_OK;
@@ -1148,11 +1149,11 @@ cnn_status cross_neighbours_impl(cnn_context *ctx, const double *xq, int64_t m, 
     float *xf = ctx->scratch_b.as<float>();
     float *xqf = xf + (size_t)n * d;
     if (n > 0) {
-        to_f32_kernel<<<std::min<unsigned>(grid_for(n * d, 256), 152u * 16u), 256, 0, st>>>(
+        to_f32_kernel<<<std::min<unsigned>(grid_for(n * d, 256), ctx->sm_count * 16u), 256, 0, st>>>(
             ctx->x, n, d, ctx->scratch_a.as<double>(), xf);
         CNN_LAUNCH_CHECK(ctx);
     }
-    to_f32_kernel<<<std::min<unsigned>(grid_for(m * d, 256), 152u * 16u), 256, 0, st>>>(
+    to_f32_kernel<<<std::min<unsigned>(grid_for(m * d, 256), ctx->sm_count * 16u), 256, 0, st>>>(
         xq, m, d, ctx->scratch_a.as<double>(), xqf);
     CNN_LAUNCH_CHECK(ctx);
     const size_t smem = sizeof(float) * (size_t)(kTileCand + kTileWarps) * (d + 1);
@@ -1182,6 +1183,7 @@ cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev, con
                                int64_t n) {
     cudaStream_t st = ctx->stream;
     ctx->have_graph = false;
+    ++ctx->graph_generation;
     ctx->stats = cnn_stats{};
     ctx->search_stats_pending = false;
     ctx->fit_stats_pending = false;
@@ -1227,7 +1229,7 @@ cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev, con
         if (nnz > 0) {
             uint64_t *sorted = keys;
             CNN_TRY(radix_sort_u64(ctx, keys, nnz, 2 * bits_n, 0, &sorted));
-            keys_to_cols_kernel<<<std::min<unsigned>(grid_for(nnz, 256), 152u * 32u), 256, 0, st>>>(
+            keys_to_cols_kernel<<<std::min<unsigned>(grid_for(nnz, 256), ctx->sm_count * 32u), 256, 0, st>>>(
                 sorted, nnz, bits_n, ctx->cols.as<int32_t>());
             CNN_LAUNCH_CHECK(ctx);
         }

@@ -340,7 +340,7 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
     if (kf > 0 && n > 0) {
         CNN_TRY(ctx->ensure(ctx->sweep_multi_off, sizeof(int64_t) * (size_t)kf * (size_t)(n + 1)));
         int64_t *off_all = ctx->sweep_multi_off.as<int64_t>();
-        const unsigned mgrid = std::min<unsigned>(grid_for((n + 1) * 32, 256), 152u * 16u);
+        const unsigned mgrid = std::min<unsigned>(grid_for((n + 1) * 32, 256), ctx->sm_count * 16u);
         for (int32_t k = 0; k < kf; ++k)
             CNN_TRY(scan_exclusive_i32_to_i64(ctx, deg_all + (size_t)k * (n + 1), off_all + (size_t)k * (n + 1), n + 1));
         std::vector<int64_t> nnz_k(kf), base(kf + 1, 0);

@@ -51,7 +51,7 @@ extern "C" {
 #define CNN_API
 #endif
 
-#define CNN_ABI_VERSION 1
+#define CNN_ABI_VERSION 2
 
 typedef struct cnn_context cnn_context;
 
@@ -141,6 +141,14 @@ CNN_API const char *cnn_last_error(const cnn_context *ctx);
 CNN_API cnn_status cnn_set_timing(cnn_context *ctx, int enabled);
 CNN_API cnn_status cnn_get_stats(const cnn_context *ctx, cnn_stats *out);
 
+/* Limit, in nanoseconds, of every bounded wait inside the context's
+ * pipelined kernels (the tensor-core search's barrier waits); <= 0 restores
+ * the default of 2 s.  A wait that runs out stops the kernel cleanly (its
+ * copies drained, its tensor memory freed) and the call returns
+ * CNN_ERR_TIMEOUT; the context stays usable.  No reference counterpart: a
+ * testing and watchdog knob. */
+CNN_API cnn_status cnn_set_wait_limit(cnn_context *ctx, int64_t limit_ns);
+
 /* Points, row-major [n_points x n_dim].  Device arrays are used in place
  * (they must stay alive and unchanged until the next cnn_set_points);
  * host arrays are copied. */
@@ -174,10 +182,23 @@ CNN_API cnn_status cnn_get_neighbours(cnn_context *ctx, int64_t *offsets, int32_
  * neighbours are joined; each connected set of nodes gets one label,
  * numbered from current_start in the order of its lowest point index.
  * labels[] of nodes and consider[] of every visited point are written in
- * place as the reference does; other entries are left as they are. */
+ * place as the reference does; other entries are left as they are.
+ * n_points is the length of labels[] and consider[]: it must equal the
+ * point count of the current graph (the reference writes exactly
+ * input_data.n_points labels), else CNN_ERR_INVALID_ARG is returned
+ * before anything is copied or launched. */
 CNN_API cnn_status cnn_fit(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
                            int64_t current_start, uint8_t *consider, int64_t *labels,
-                           cnn_memspace mem);
+                           int64_t n_points, cnn_memspace mem);
+
+/* A counter of the graphs this context has held: it changes whenever the
+ * points, distances or neighbourhoods are replaced or a neighbour graph is
+ * built (cnn_set_points, cnn_set_distances, cnn_set_neighbours,
+ * cnn_build_neighbours, and the calls that build a graph on their own:
+ * cnn_sweep, cnn_sweep_pairs, cnn_predict, cnn_mst_prim).  A caller that
+ * keeps a graph for later fits compares it to tell whether the context still
+ * holds that graph. */
+CNN_API cnn_status cnn_graph_generation(const cnn_context *ctx, int64_t *generation);
 
 /* Labels.sort_by_size on labels[n] in place: renumber clusters by size
  * (descending, ties by first occurrence), zero clusters with fewer than
@@ -284,18 +305,27 @@ CNN_API cnn_status cnn_mst_prim(cnn_context *ctx, double radius_cutoff, cnn_metr
  * library (about 1.9 MB per GPU, held by every GPU that loads the library
  * until the process exits).
  *
- * Same result as cnn_set_neighbours + cnn_fit on the same graph.  All
- * pointers are device pointers; rows of `indices` must be ascending and the
- * neighbour relation symmetric (as produced by cnn_get_neighbours).  Work
- * is queued on `stream` (a cudaStream_t, NULL = legacy default stream) on
- * the current device; the call returns before it finishes.
+ * All pointers are device pointers.  The graph must be what
+ * cnn_get_neighbours produces: offsets int64[n_points + 1] from 0, rows of
+ * `indices` strictly ascending with values in [0, n_points), and the
+ * neighbour relation symmetric; for such a graph the labels equal those of
+ * cnn_set_neighbours + cnn_fit.  The offsets and rows are checked on the GPU
+ * before they are used; a graph that fails (decreasing offsets, an index out
+ * of range, a row out of order) is not fitted and labels and consider stay
+ * as they were -- a fitted call always leaves every consider entry 0.
+ * Symmetry is not checked: an asymmetric graph gives undefined labels.
+ * Work is queued on `stream` (a cudaStream_t, NULL = legacy default stream)
+ * on the current device; the call returns before it finishes.
  *
  * Limits and sharing: n_points above CNN_NOALLOC_MAX_POINTS returns
- * CNN_ERR_INVALID_ARG without touching the GPU.  All calls share the one
- * scratch block, so calls whose GPU work overlaps (other streams, other
- * host threads) race and must be serialised by the caller.  The first call
- * on a device looks up the scratch block's device address once (with that
- * device current); make that first call before any stream capture. */
+ * CNN_ERR_INVALID_ARG without touching the GPU; a CUDA error already
+ * pending when the call starts returns CNN_ERR_CUDA and is left pending.
+ * All calls share the one scratch block, so calls whose GPU work overlaps
+ * (other streams, other host threads) race and must be serialised by the
+ * caller.  The first call on a device looks up the scratch block's device
+ * address once (with that device current); make that first call before any
+ * stream capture, and do not call this entry point again after
+ * cudaDeviceReset in the same process. */
 #define CNN_NOALLOC_MAX_POINTS 65536
 
 CNN_API cnn_status cnn_fit_csr_noalloc(const int64_t *offsets, const int32_t *indices,

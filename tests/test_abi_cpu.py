@@ -40,7 +40,7 @@ def test_library_loads_and_reports_abi_version(lib_path):
     L = ctypes.CDLL(lib_path)
     for s in declared_symbols():
         assert hasattr(L, s), s
-    assert L.cnn_abi_version() == 1
+    assert L.cnn_abi_version() == 2
 
 
 def test_python_binding_covers_header():

@@ -281,3 +281,27 @@ def test_tensor_core_fit_labels(cnn, oracle):
     cl = cnn.Clustering(x)
     cl.fit(3.1, 5, v=False)
     assert np.array_equal(np.asarray(cl.labels), want)
+
+
+def test_tensor_core_wait_timeout_stops_cleanly(cnn, oracle):
+    """A barrier wait of the tensor-core search that runs out (limit 1 ns)
+    ends the kernel through its bounded-wait path: the call returns
+    CNN_ERR_TIMEOUT, and the same context then searches correctly with the
+    default limit (copies drained, tensor memory freed)."""
+    from commonnnclustering_gb300 import workloads
+    x = workloads.features(n=16000, d=64, seed=33, n_clusters=12)
+    r2 = 3.1 ** 2
+    want = oracle.neighbourhoods(x, r2, fpmode=0, grid=False)
+    ctx = cnn.Context(0)
+    ctx.set_points(x)
+    ctx.set_wait_limit(1)
+    with pytest.raises(cnn.CNNError) as err:
+        ctx.build_neighbours(r2)
+    assert err.value.status == 4  # CNN_ERR_TIMEOUT
+    ctx.set_wait_limit(0)
+    for _ in range(2):
+        ctx.build_neighbours(r2)
+        assert ctx.stats()["search_kind"] == 3
+        off, idx = ctx.get_neighbours(x.shape[0])
+        assert np.array_equal(off, want[0]) and np.array_equal(idx, want[1])
+    ctx.close()

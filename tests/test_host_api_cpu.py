@@ -96,3 +96,63 @@ def test_register_with_reference_package():
         assert p.radius_cutoff == 0.25 and p.similarity_cutoff == 4
     finally:
         sys.path.remove(ref)
+
+
+def test_context_fit_rejects_arrays_of_another_length_before_calling_the_library():
+    """Context.fit checks labels/consider against the graph's point count on
+    the host; nothing reaches the library (it is not even loaded here)."""
+    import numpy as np
+    from commonnnclustering_gb300 import _abi
+    ctx = object.__new__(_abi.Context)   # no device: only the Python check runs
+    ctx._lib = None
+    ctx._h = None
+    ctx._n_points = 100
+    with pytest.raises(ValueError):
+        ctx.fit(7, 6, 1, np.ones(100, dtype=np.uint8), np.zeros(99, dtype=np.int64))
+    with pytest.raises(ValueError):
+        ctx.fit(7, 6, 1, np.ones(101, dtype=np.uint8), np.zeros(101, dtype=np.int64))
+    with pytest.raises(ValueError):
+        ctx.fit(7, 6, 1, np.ones(99, dtype=np.uint8), np.zeros(100, dtype=np.int64))
+
+
+def test_fitter_graph_key_follows_the_context_generation():
+    """FitterGPU reuses a device graph only while the context's graph
+    generation is the one recorded at its own build."""
+    from commonnnclustering_gb300 import _fit
+
+    class FakeCtx:
+        def __init__(self):
+            self.gen, self.builds, self.device, self.stream = 0, 0, 0, None
+
+        def graph_generation(self):
+            return self.gen
+
+        def set_points(self, data):
+            self.gen += 1
+
+        def build_neighbours(self, *a):
+            self.gen += 1
+            self.builds += 1
+
+    class FakeTensor:
+        _version = 0
+        shape = (10, 3)
+        __cuda_array_interface__ = {"data": (1234, False), "shape": (10, 3), "typestr": "<f8"}
+
+        def data_ptr(self):
+            return 1234
+
+    class Inp:
+        data = FakeTensor()
+        meta = {}
+
+    ctx = FakeCtx()
+    f = _fit.FitterGPU(context=ctx)
+    f._sync_stream = lambda c, a: None
+    p = _fit.ClusterParameters(0.01, 12, 12, 11, 1)
+    f.prepare(Inp(), p)
+    f.prepare(Inp(), p)
+    assert ctx.builds == 1           # reused: nothing else touched the context
+    ctx.gen += 1                     # another user replaced the graph
+    f.prepare(Inp(), p)
+    assert ctx.builds == 2

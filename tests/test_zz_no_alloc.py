@@ -87,6 +87,36 @@ def test_noalloc_matches_allocating_path_on_consecutive_calls(env):
         assert len(set(got_l.tolist()) - {0, 9}) > 1
 
 
+def test_noalloc_leaves_outputs_untouched_for_an_invalid_graph(env):
+    """A bad graph is caught on the GPU before it is read: an index in
+    [n, CNN_NOALLOC_MAX_POINTS) (which would otherwise read stale scratch),
+    a row out of order, or decreasing offsets leave labels and consider as
+    they were; the next valid call is fitted as usual."""
+    torch, _abi = env
+    from commonnnclustering_gb300 import workloads
+    x = workloads.blobs2d(n=3000, seed=5)
+    off, idx = graph(_abi, x, 0.3 ** 2)
+    n = x.shape[0]
+    consider = np.ones(n, dtype=np.uint8)
+    labels = np.full(n, 7, dtype=np.int64)
+    row = int(np.argmax(np.diff(off)))          # a long row
+    s, e = int(off[row]), int(off[row + 1])
+    bad_index = idx.copy()
+    bad_index[e - 1] = n + 5                     # beyond the graph, inside the scratch block
+    bad_order = idx.copy()
+    bad_order[s], bad_order[s + 1] = bad_order[s + 1], bad_order[s]
+    bad_off = off.copy()
+    bad_off[row + 1] = bad_off[row] - 1          # a decreasing offset
+    for o, i in ((off, bad_index), (off, bad_order), (bad_off, idx)):
+        got_l, got_c = noalloc_fit(torch, _abi, o, i, 7, 6, 1, consider, labels)
+        assert np.array_equal(got_l, labels)
+        assert np.array_equal(got_c, consider)
+    want_l, want_c = allocating_fit(_abi, off, idx, 7, 6, 1, consider, labels)
+    got_l, got_c = noalloc_fit(torch, _abi, off, idx, 7, 6, 1, consider, labels)
+    assert np.array_equal(got_l, want_l) and np.array_equal(got_c, want_c)
+    assert not got_c.any()
+
+
 def test_noalloc_rejects_more_points_than_its_scratch_holds(env):
     torch, _abi = env
     lib = _abi.load()
