@@ -69,6 +69,13 @@ METRIC = "CommonNN fit points/s (bit-exact labels)"
 UNIT = "points/s"
 
 
+def fpmode_name() -> str:
+    """The float64 accumulation both arms use: the reference as built on this
+    host (fused multiply-add on aarch64, separate on x86-64)."""
+    from commonnnclustering_gb300 import _abi
+    return "fused" if _abi.host_fpmode() == _abi.FP_FUSED else "separate"
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -356,7 +363,7 @@ def run_gpu(args):
         "config": {"workload": W["name"], "n_points": n, "n_dim": W["d"], "radius_cutoff": W["radius_cutoff"],
                    "cnn_cutoff": W["cnn_cutoff"], "member_cutoff": W["member_cutoff"],
                    "neighbour_pairs": nnz, "l2": "flushed between steps (256 MiB write)",
-                   "parallelism": "replicas" if world > 1 else "single"},
+                   "parallelism": "replicas" if world > 1 else "single", "fpmode": fpmode_name()},
         "e2e": {"value": world * n / e2e_max, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches) * args.steps,
         "gpu_launches_per_step": int(launches),
@@ -562,7 +569,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean_s * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": f"synthetic (seeded {WORKLOAD['gen'][0]} generator)",
         "config": {"workload": W["name"], "n_points": n, "n_dim": W["d"], "radius_cutoff": W["radius_cutoff"],
-                   "cnn_cutoff": W["cnn_cutoff"], "member_cutoff": W["member_cutoff"]},
+                   "cnn_cutoff": W["cnn_cutoff"], "member_cutoff": W["member_cutoff"], "fpmode": fpmode_name()},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"full {W['name']} fit per step: neighbour lists restated on {cores} threads, "
                                    "the reference's BFS + sorted-merge check on 1 thread, sort_by_size"},

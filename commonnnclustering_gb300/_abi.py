@@ -37,6 +37,26 @@ MEM_HOST = 0
 MEM_DEVICE = 1
 
 
+def host_fpmode(fpmode: Optional[int] = None) -> int:
+    """The float64 accumulation of the distance sum; None: the one the
+    reference reproduces when it is built on this host.
+
+    The reference sums ``total += cpow(a - b, 2)`` (src/cnnclustering/
+    _types.pyx:2253-2267) and is compiled with its setup.py flags.  GCC on
+    x86-64 (no FMA in the baseline ISA) keeps the multiply and the add
+    (FP_SEPARATE); GCC on aarch64 (the GB300's Grace host) fuses each term
+    into one FMA (FP_FUSED), with the same flags.  ``CNN_FPMODE=separate`` or
+    ``fused`` in the environment chooses explicitly.
+    """
+    if fpmode is not None:
+        return int(fpmode)
+    env = os.environ.get("CNN_FPMODE", "").strip().lower()
+    if env in ("separate", "fused"):
+        return FP_FUSED if env == "fused" else FP_SEPARATE
+    import platform
+    return FP_FUSED if platform.machine().lower() in ("aarch64", "arm64") else FP_SEPARATE
+
+
 class CNNError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"{_STATUS.get(status, status)}: {message}")
@@ -275,8 +295,8 @@ class Context:
         return shape
 
     def build_neighbours(self, radius_cutoff: float, metric: int = METRIC_EUCLIDEAN_REDUCED,
-                         fpmode: int = FP_SEPARATE):
-        self._check(self._lib.cnn_build_neighbours(self._h, float(radius_cutoff), int(metric), int(fpmode)),
+                         fpmode: Optional[int] = None):
+        self._check(self._lib.cnn_build_neighbours(self._h, float(radius_cutoff), int(metric), host_fpmode(fpmode)),
                     "cnn_build_neighbours")
 
     def set_neighbours(self, offsets, indices):
@@ -354,7 +374,7 @@ class Context:
                     "cnn_sort_by_size")
 
     def sweep(self, radius_cutoffs, cuts, member_cutoff: int = 2, max_clusters: Optional[int] = None,
-              metric: int = METRIC_EUCLIDEAN_REDUCED, fpmode: int = FP_SEPARATE, labels_out=None):
+              metric: int = METRIC_EUCLIDEAN_REDUCED, fpmode: Optional[int] = None, labels_out=None):
         """Fits for every (radius, cut) pair on the current points.
 
         radius_cutoffs: adjusted cutoffs, ascending.  cuts: sequence of
@@ -374,12 +394,12 @@ class Context:
             ptr, mem = out.ctypes.data, MEM_HOST
         self._check(self._lib.cnn_sweep(self._h, ctypes.c_void_p(rc.ctypes.data), rc.shape[0],
                                         ctypes.c_void_p(sc.ctypes.data), ctypes.c_void_p(nm.ctypes.data),
-                                        sc.shape[0], int(metric), int(fpmode), int(member_cutoff), mx,
+                                        sc.shape[0], int(metric), host_fpmode(fpmode), int(member_cutoff), mx,
                                         ctypes.c_void_p(ptr), mem), "cnn_sweep")
         return out
 
     def sweep_pairs(self, radius_cutoffs, cuts, member_cutoff: int = 2, max_clusters: Optional[int] = None,
-                    sort: bool = True, metric: int = METRIC_EUCLIDEAN_REDUCED, fpmode: int = FP_SEPARATE,
+                    sort: bool = True, metric: int = METRIC_EUCLIDEAN_REDUCED, fpmode: Optional[int] = None,
                     labels_out=None):
         """Fits for a list of steps on the current points.
 
@@ -402,13 +422,13 @@ class Context:
             ptr, mem = out.ctypes.data, MEM_HOST
         self._check(self._lib.cnn_sweep_pairs(self._h, ctypes.c_void_p(rc.ctypes.data),
                                               ctypes.c_void_p(sc.ctypes.data), ctypes.c_void_p(nm.ctypes.data),
-                                              rc.shape[0], int(metric), int(fpmode), 1 if sort else 0,
+                                              rc.shape[0], int(metric), host_fpmode(fpmode), 1 if sort else 0,
                                               int(member_cutoff), mx, ctypes.c_void_p(ptr), mem), "cnn_sweep_pairs")
         return out
 
     def predict(self, other_points, labels, clusters, radius_cutoff: float, similarity_cutoff: int,
                 n_member_cutoff: int, other_labels, other_consider, metric: int = METRIC_EUCLIDEAN_REDUCED,
-                fpmode: int = FP_SEPARATE):
+                fpmode: Optional[int] = None):
         """First-match labels for other points from the current points' labels.
 
         other_points: [m, n_dim] float64/float32; labels: [n_points] int64 of
@@ -440,19 +460,19 @@ class Context:
             cl_p, n_cl, mem, keep = cl.ctypes.data, int(cl.shape[0]), MEM_HOST, (xo, lab, cl)
         self._check(self._lib.cnn_predict(self._h, ctypes.c_void_p(xp), DTYPE_F32 if dt == np.float32 else DTYPE_F64,
                                           int(shape[0]), int(shape[1]), ctypes.c_void_p(lab_p), ctypes.c_void_p(cl_p),
-                                          n_cl, float(radius_cutoff), int(metric), int(fpmode),
+                                          n_cl, float(radius_cutoff), int(metric), host_fpmode(fpmode),
                                           int(similarity_cutoff), int(n_member_cutoff), ctypes.c_void_p(out_l),
                                           ctypes.c_void_p(out_c), mem), "cnn_predict")
         del keep
 
-    def mst_prim(self, radius_cutoff: float, metric: int = METRIC_EUCLIDEAN_REDUCED, fpmode: int = FP_SEPARATE):
+    def mst_prim(self, radius_cutoff: float, metric: int = METRIC_EUCLIDEAN_REDUCED, fpmode: Optional[int] = None):
         """Maximum spanning forest edges (a, b, weight) in Prim's tree-queue order."""
         cap = max(int(self._n_points) - 1, 1)
         a = np.empty(cap, dtype=np.int64)
         b = np.empty(cap, dtype=np.int64)
         w = np.empty(cap, dtype=np.int64)
         ne = ctypes.c_int64()
-        self._check(self._lib.cnn_mst_prim(self._h, float(radius_cutoff), int(metric), int(fpmode),
+        self._check(self._lib.cnn_mst_prim(self._h, float(radius_cutoff), int(metric), host_fpmode(fpmode),
                                            ctypes.c_void_p(a.ctypes.data), ctypes.c_void_p(b.ctypes.data),
                                            ctypes.c_void_p(w.ctypes.data), cap, ctypes.byref(ne)), "cnn_mst_prim")
         k = int(ne.value)

@@ -153,7 +153,7 @@ class FitterGPU(Fitter):
             return _abi.METRIC_EUCLIDEAN_REDUCED
 
     def _fpmode_code(self) -> int:
-        return getattr(self._neighbours_getter, "fpmode_code", _abi.FP_SEPARATE)
+        return getattr(self._neighbours_getter, "fpmode_code", _abi.host_fpmode())
 
     def prepare(self, input_data, cluster_params: ClusterParameters) -> _abi.Context:
         """Put the neighbour graph of ``input_data`` on the device."""

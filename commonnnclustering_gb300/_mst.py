@@ -214,7 +214,7 @@ class HierarchicalFitterMSTPrimGPU(HierarchicalFitter):
         ctx = self._context
         metric = load_input(ctx, input_data, self._neighbours_getter, self._metric_code())
         a, b, w = ctx.mst_prim(radius_cutoff, metric=metric,
-                               fpmode=getattr(self._neighbours_getter, "fpmode_code", _abi.FP_SEPARATE))
+                               fpmode=getattr(self._neighbours_getter, "fpmode_code", _abi.host_fpmode()))
         return list(zip(a.tolist(), b.tolist(), w.tolist()))
 
     def fit(self, bundle, **kwargs):

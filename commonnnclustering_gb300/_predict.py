@@ -88,7 +88,7 @@ class PredictorFirstmatchGPU(Predictor):
         ctx.predict(other, labels.labels, predictand_labels.consider_set, cluster_params.radius_cutoff,
                     cluster_params.similarity_cutoff, cluster_params.n_member_cutoff, predictand_labels.labels,
                     predictand_labels.consider, metric=metric,
-                    fpmode=getattr(self._neighbours_getter, "fpmode_code", _abi.FP_SEPARATE))
+                    fpmode=getattr(self._neighbours_getter, "fpmode_code", _abi.host_fpmode()))
 
 
 def predict_into(clustering, bundle, other, radius_cutoff, cnn_cutoff, clusters=None, cnn_offset=None, info=True,

@@ -437,17 +437,21 @@ class NeighboursGetterGPUGrid:
     list ascending (cell grid for n_dim <= 3, tiled all-pairs otherwise).
 
     ``fpmode`` selects how the float64 sum of squares is accumulated:
-    ``"separate"`` (multiply, then add: the reference compiled without FMA
-    contraction, as on x86-64) or ``"fused"`` (one fused multiply-add per
-    term: the reference compiled with contraction, GCC's aarch64 default).
+    ``"separate"`` (multiply, then add: the reference as GCC builds it on
+    x86-64), ``"fused"`` (one fused multiply-add per term: the reference as
+    GCC builds it on aarch64, e.g. a GB300's Grace host) or ``"auto"`` (the
+    default): the mode of the reference built on this host
+    (``_abi.host_fpmode``, ``CNN_FPMODE`` overrides it).
     """
 
-    def __init__(self, distance_getter=None, fpmode: str = "separate"):
+    def __init__(self, distance_getter=None, fpmode: str = "auto"):
         self.is_sorted = True
         self.is_selfcounting = True
         self._distance_getter = distance_getter if distance_getter is not None else DistanceGetterGPUMetric()
-        if fpmode not in ("separate", "fused"):
-            raise ValueError("fpmode must be 'separate' or 'fused'")
+        if fpmode not in ("separate", "fused", "auto"):
+            raise ValueError("fpmode must be 'separate', 'fused' or 'auto'")
+        if fpmode == "auto":
+            fpmode = "fused" if _abi.host_fpmode() == _abi.FP_FUSED else "separate"
         self.fpmode = fpmode
 
     @classmethod

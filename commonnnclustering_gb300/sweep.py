@@ -20,7 +20,7 @@ from ._types import InputDataGPUComponents, MetricGPUEuclidean, MetricGPUEuclide
 
 def sweep(points, radius_cutoffs: Sequence[float], cnn_cutoffs: Sequence[int],
           member_cutoff: Optional[int] = None, max_clusters: Optional[int] = None,
-          metric=None, fpmode: str = "separate", is_selfcounting: bool = True,
+          metric=None, fpmode: str = "auto", is_selfcounting: bool = True,
           context: Optional[_abi.Context] = None, labels_out=None):
     """Labels of every (radius, cnn_cutoff) pair, shape [n_radii, n_cuts, n].
 
@@ -48,7 +48,7 @@ def sweep(points, radius_cutoffs: Sequence[float], cnn_cutoffs: Sequence[int],
             ctx.set_stream(st)
     ctx.set_points(data)
     code = _abi.METRIC_EUCLIDEAN if isinstance(metric, MetricGPUEuclidean) else _abi.METRIC_EUCLIDEAN_REDUCED
-    fp = _abi.FP_FUSED if fpmode == "fused" else _abi.FP_SEPARATE
+    fp = _abi.host_fpmode() if fpmode == "auto" else _abi.FP_FUSED if fpmode == "fused" else _abi.FP_SEPARATE
     return ctx.sweep(adjusted, cuts, member_cutoff=member_cutoff, max_clusters=max_clusters, metric=code,
                      fpmode=fp, labels_out=labels_out)
 

@@ -19,6 +19,7 @@
  *                              src/cnnclustering/_types.pyx:1676-1678)
  *   oracle_check_sorted      SimilarityCheckerExtScreensorted._check
  *                              src/cnnclustering/_types.pyx:2654-2706
+ *   oracle_pivot_run/_take   the same rows with an exact pivot prune
  *   oracle_fit_bfs_csr       FitterExtBFS._fit over precomputed sorted lists
  *                              src/cnnclustering/_fit.pyx:408-491 with
  *                              NeighboursGetterExtLookup._get :1806-1817,
@@ -505,6 +506,297 @@ int oracle_neighbour_fill_grid(const double *x, int64_t n, int32_t d, double rad
     if (rc == 1) return oracle_neighbour_fill(x, n, d, radius_cutoff, metric, fpmode, nthreads, offsets, indices);
     return rc;
 }
+
+/* ------------------------------------------------------------------ */
+/* Brute force with an exact pivot prune (high dimension, many points) */
+/* ------------------------------------------------------------------ */
+/* The predicate of oracle_neighbour_counts/fill, evaluated on fewer pairs.
+ * Shortcuts that cannot change a row:
+ *  - the float64 sum only grows (every term is >= 0 and rounding is
+ *    monotone), so a partial sum above the cutoff already means "out";
+ *  - triangle inequality, groups: points are grouped by their nearest of P
+ *    group pivots; with rad(G) the largest distance of a member of G to its
+ *    pivot g, no pair of G x H is closer than dist(g, h) - rad(G) - rad(H),
+ *    so group pairs above the radius are skipped;
+ *  - triangle inequality, pairs: with D(i, q) the distance to each of Q
+ *    bound pivots, |D(i,q) - D(p,q)| <= dist(i, p) skips single pairs.
+ * Every bound carries a relative margin of 1e-6, far above the rounding of
+ * the pivot distances and of the reference's own sum.  One pass: rows are
+ * gathered per thread, sorted ascending and handed out by
+ * oracle_pivot_take.  Finite coordinates only (-2: use the plain scan). */
+
+enum { kBoundPivots = 8 };
+
+typedef struct { int32_t *buf; int64_t len, cap; } pv_buf;
+
+typedef struct {
+    const double *x;
+    int64_t n;
+    int32_t d, P, Q;
+    double radius_cutoff, exit_above, reach;
+    int metric, fpmode;
+    int32_t *grp;      /* [n] group of each point (point order) */
+    double *od;        /* [n] distance to its group pivot (point order) */
+    double *bq;        /* [n][Q] distances to the bound pivots, group order */
+    double *xs;        /* [n][d] coordinates, group order */
+    int32_t *idx;      /* group order -> point index */
+    int64_t *gstart;   /* [P + 1] */
+    double *rad;       /* [P] */
+    double *pp;        /* [P][P] pivot-pivot distances */
+    int64_t *row_len;  /* [n] by point index */
+    int64_t *row_start;/* [n] start in the writing thread's buffer */
+    int32_t *row_tid;  /* [n] the writing thread */
+    int phase;         /* 0: groups and bounds per point, 1: pivot pairs, 2: rows */
+    int64_t next, total, block;
+    pthread_mutex_t mu;
+    int failed;
+} pv_state;
+
+static pv_state *g_pivot;  /* the result of the last oracle_pivot_run */
+static pv_buf *g_pivot_bufs;
+static int g_pivot_nbufs;
+
+/* The reference predicate, stopped as soon as the growing sum passes
+ * exit_above (past it the final sum cannot be within the cutoff). */
+static inline int in_radius_early(const double *xa, const double *xb, int32_t d, double radius_cutoff,
+                                  double exit_above, int metric, int fpmode)
+{
+    double total = 0.0;
+    for (int32_t k = 0; k < d; ++k) {
+        double t = xa[k] - xb[k];
+        if (fpmode) {
+            total = fma(t, t, total);
+        } else {
+            double sq = t * t;
+            total = total + sq;
+        }
+        if (total > exit_above) return 0;
+    }
+    if (metric == ORACLE_METRIC_EUCLIDEAN) total = sqrt(total);
+    return total <= radius_cutoff;
+}
+
+static double plain_dist(const double *a, const double *b, int32_t d)
+{
+    double t = 0;
+    for (int32_t k = 0; k < d; ++k) t += (a[k] - b[k]) * (a[k] - b[k]);
+    return sqrt(t);
+}
+
+static int pv_push(pv_buf *b, int32_t v)
+{
+    if (b->len == b->cap) {
+        int64_t cap = b->cap ? 2 * b->cap : 1 << 20;
+        int32_t *nb = (int32_t *)realloc(b->buf, sizeof(int32_t) * (size_t)cap);
+        if (!nb) return -1;
+        b->buf = nb;
+        b->cap = cap;
+    }
+    b->buf[b->len++] = v;
+    return 0;
+}
+
+typedef struct { pv_state *S; pv_buf *out; int32_t tid; } pv_arg;
+
+static int pv_rows_of_group(pv_state *S, int64_t G, pv_buf *out, int32_t tid, int32_t *near)
+{
+    const int32_t P = S->P, Q = S->Q, d = S->d;
+    const double reach = S->reach * (1.0 + 1e-6);
+    int32_t nh = 0;
+    for (int32_t H = 0; H < P; ++H) {
+        if (S->gstart[H] == S->gstart[H + 1]) continue;
+        const double gap = S->pp[G * P + H] - S->rad[G] - S->rad[H];
+        if (gap > reach + 1e-6 * (S->pp[G * P + H] + S->rad[G] + S->rad[H])) continue;
+        near[nh++] = H;
+    }
+    for (int64_t a = S->gstart[G]; a < S->gstart[G + 1]; ++a) {
+        const double *xp = S->xs + a * d, *dp = S->bq + a * Q;
+        const int64_t begin = out->len;
+        for (int32_t h = 0; h < nh; ++h) {
+            const int32_t H = near[h];
+            for (int64_t b = S->gstart[H]; b < S->gstart[H + 1]; ++b) {
+                const double *db = S->bq + b * Q;
+                int pruned = 0;
+                for (int32_t q = 0; q < Q && !pruned; ++q)
+                    pruned = fabs(db[q] - dp[q]) > reach + 1e-6 * (db[q] + dp[q]);
+                if (pruned) continue;
+                if (in_radius_early(xp, S->xs + b * d, d, S->radius_cutoff, S->exit_above, S->metric, S->fpmode))
+                    if (pv_push(out, S->idx[b]) != 0) return -1;
+            }
+        }
+        const int32_t p = S->idx[a];
+        qsort(out->buf + begin, (size_t)(out->len - begin), sizeof(int32_t), cmp_i32);
+        S->row_len[p] = out->len - begin;
+        S->row_start[p] = begin;
+        S->row_tid[p] = tid;
+    }
+    return 0;
+}
+
+static void *pv_worker(void *arg)
+{
+    pv_arg *A = (pv_arg *)arg;
+    pv_state *S = A->S;
+    const int32_t P = S->P, Q = S->Q, d = S->d;
+    int32_t *near = S->phase == 2 ? (int32_t *)malloc(sizeof(int32_t) * (size_t)P) : NULL;
+    if (S->phase == 2 && !near) { S->failed = 1; return NULL; }
+    const int64_t gstep = S->n / P, qstep = S->n / Q;
+    for (;;) {
+        pthread_mutex_lock(&S->mu);
+        const int64_t b = S->next;
+        S->next += S->block;
+        pthread_mutex_unlock(&S->mu);
+        if (b >= S->total) break;
+        const int64_t e = b + S->block < S->total ? b + S->block : S->total;
+        for (int64_t i = b; i < e; ++i) {
+            if (S->phase == 0) {  /* point i: nearest group pivot */
+                int32_t best = 0;
+                double bd = INFINITY;
+                for (int32_t v = 0; v < P; ++v) {
+                    const double dv = plain_dist(S->x + i * d, S->x + (int64_t)v * gstep * d, d);
+                    if (dv < bd) { bd = dv; best = v; }
+                }
+                S->grp[i] = best;
+                S->od[i] = bd;
+            } else if (S->phase == 1) {  /* pivot row i: distances to the other pivots */
+                for (int32_t v = 0; v < P; ++v)
+                    S->pp[i * P + v] = plain_dist(S->x + i * gstep * d, S->x + (int64_t)v * gstep * d, d);
+            } else if (S->phase == 3) {  /* group-order point i: bound-pivot distances */
+                for (int32_t q = 0; q < Q; ++q)
+                    S->bq[i * Q + q] = plain_dist(S->xs + i * d, S->x + (int64_t)q * qstep * d, d);
+            } else {
+                if (pv_rows_of_group(S, i, A->out, A->tid, near) != 0) { S->failed = 1; free(near); return NULL; }
+            }
+        }
+    }
+    free(near);
+    return NULL;
+}
+
+static int pv_phase(pv_state *S, int phase, int64_t total, int64_t block, pv_arg *args, int nthreads)
+{
+    pthread_t th[256];
+    S->phase = phase;
+    S->next = 0;
+    S->total = total;
+    S->block = block;
+    int started = 1;
+    for (int t = 1; t < nthreads; ++t, ++started)
+        if (pthread_create(&th[t], NULL, pv_worker, &args[t]) != 0) break;
+    pv_worker(&args[0]);
+    for (int t = 1; t < started; ++t) pthread_join(th[t], NULL);
+    return S->failed ? -1 : 0;
+}
+
+static void pivot_free(void)
+{
+    if (g_pivot) {
+        pv_state *S = g_pivot;
+        free(S->grp); free(S->od); free(S->bq); free(S->xs); free(S->idx); free(S->gstart); free(S->rad);
+        free(S->pp); free(S->row_len); free(S->row_start); free(S->row_tid);
+        free(S);
+        g_pivot = NULL;
+    }
+    for (int t = 0; t < g_pivot_nbufs; ++t) free(g_pivot_bufs[t].buf);
+    free(g_pivot_bufs);
+    g_pivot_bufs = NULL;
+    g_pivot_nbufs = 0;
+}
+
+/* Rows of every point; returns the total number of pairs (rows kept for
+ * oracle_pivot_take), -1 on allocation failure, -2 for non-finite input. */
+int64_t oracle_pivot_run(const double *x, int64_t n, int32_t d, double radius_cutoff, int metric, int fpmode,
+                         int nthreads)
+{
+    pivot_free();
+    for (int64_t e = 0; e < n * d; ++e)
+        if (!isfinite(x[e])) return -2;
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    pv_state *S = (pv_state *)calloc(1, sizeof(pv_state));
+    if (!S) return -1;
+    g_pivot = S;
+    S->x = x; S->n = n; S->d = d; S->radius_cutoff = radius_cutoff; S->metric = metric; S->fpmode = fpmode;
+    S->P = n >= 1024 * 64 ? 1024 : (int32_t)(n / 64 > 1 ? n / 64 : 1);
+    S->Q = S->P < kBoundPivots ? S->P : kBoundPivots;
+    const int32_t P = S->P, Q = S->Q;
+    const int ok_radius = radius_cutoff >= 0 && isfinite(radius_cutoff);
+    S->reach = !ok_radius ? INFINITY : metric == ORACLE_METRIC_EUCLIDEAN ? radius_cutoff : sqrt(radius_cutoff);
+    S->exit_above = !ok_radius ? INFINITY
+                    : metric == ORACLE_METRIC_EUCLIDEAN ? radius_cutoff * radius_cutoff * (1.0 + 1e-9) + 1e-300
+                                                        : radius_cutoff;
+    const size_t nn = (size_t)(n > 0 ? n : 1);
+    S->grp = (int32_t *)malloc(sizeof(int32_t) * nn);
+    S->od = (double *)malloc(sizeof(double) * nn);
+    S->bq = (double *)malloc(sizeof(double) * nn * Q);
+    S->xs = (double *)malloc(sizeof(double) * nn * d);
+    S->idx = (int32_t *)malloc(sizeof(int32_t) * nn);
+    S->gstart = (int64_t *)calloc((size_t)P + 1, sizeof(int64_t));
+    S->rad = (double *)calloc((size_t)P, sizeof(double));
+    S->pp = (double *)malloc(sizeof(double) * (size_t)P * P);
+    S->row_len = (int64_t *)calloc(nn, sizeof(int64_t));
+    S->row_start = (int64_t *)calloc(nn, sizeof(int64_t));
+    S->row_tid = (int32_t *)calloc(nn, sizeof(int32_t));
+    g_pivot_bufs = (pv_buf *)calloc((size_t)nthreads, sizeof(pv_buf));
+    pv_arg *args = (pv_arg *)calloc((size_t)nthreads, sizeof(pv_arg));
+    if (!S->grp || !S->od || !S->bq || !S->xs || !S->idx || !S->gstart || !S->rad || !S->pp || !S->row_len ||
+        !S->row_start || !S->row_tid || !g_pivot_bufs || !args) {
+        free(args);
+        pivot_free();
+        return -1;
+    }
+    g_pivot_nbufs = nthreads;
+    for (int t = 0; t < nthreads; ++t) { args[t].S = S; args[t].out = &g_pivot_bufs[t]; args[t].tid = t; }
+    pthread_mutex_init(&S->mu, NULL);
+    int rc = n == 0 ? 0 : pv_phase(S, 0, n, 256, args, nthreads);
+    if (rc == 0 && n > 0) rc = pv_phase(S, 1, P, 8, args, nthreads);
+    if (rc == 0 && n > 0) {
+        /* group order: counting sort by group, index order inside a group */
+        for (int64_t i = 0; i < n; ++i) S->gstart[S->grp[i] + 1]++;
+        for (int32_t v = 0; v < P; ++v) S->gstart[v + 1] += S->gstart[v];
+        int64_t *cur = (int64_t *)malloc(sizeof(int64_t) * (size_t)P);
+        if (!cur) {
+            rc = -1;
+        } else {
+            memcpy(cur, S->gstart, sizeof(int64_t) * (size_t)P);
+            for (int64_t i = 0; i < n; ++i) {
+                const int32_t G = S->grp[i];
+                const int64_t a = cur[G]++;
+                S->idx[a] = (int32_t)i;
+                memcpy(S->xs + a * d, x + i * d, sizeof(double) * (size_t)d);
+                if (S->od[i] > S->rad[G]) S->rad[G] = S->od[i];
+            }
+            free(cur);
+            rc = pv_phase(S, 3, n, 256, args, nthreads);
+        }
+    }
+    if (rc == 0 && n > 0) rc = pv_phase(S, 2, P, 1, args, nthreads);
+    free(args);
+    pthread_mutex_destroy(&S->mu);
+    if (rc != 0) { pivot_free(); return -1; }
+    int64_t total = 0;
+    for (int64_t p = 0; p < n; ++p) total += S->row_len[p];
+    return total;
+}
+
+/* The rows of the last oracle_pivot_run as CSR (offsets int64[n+1],
+ * indices int32[total]); frees them. */
+int oracle_pivot_take(int64_t *offsets, int32_t *indices)
+{
+    if (!g_pivot) return -1;
+    const pv_state *S = g_pivot;
+    offsets[0] = 0;
+    for (int64_t p = 0; p < S->n; ++p) {
+        offsets[p + 1] = offsets[p] + S->row_len[p];
+        if (S->row_len[p])
+            memcpy(indices + offsets[p], g_pivot_bufs[S->row_tid[p]].buf + S->row_start[p],
+                   sizeof(int32_t) * (size_t)S->row_len[p]);
+    }
+    pivot_free();
+    return 0;
+}
+
+void oracle_pivot_free(void) { pivot_free(); }
 
 /* ------------------------------------------------------------------ */
 /* Periodic metric: MetricExtEuclideanPeriodicReduced._calc_distance   */

@@ -40,6 +40,26 @@ METRIC_EUCLIDEAN = 1
 FP_SEPARATE = 0
 FP_FUSED = 1
 
+
+def host_fpmode(fpmode=None) -> int:
+    """The float64 accumulation a call uses; None: the reference's as built
+    on this host.
+
+    The reference compiles ``total += cpow(a - b, 2)`` (_types.pyx:2253-2267)
+    with its setup.py flags; measured with ``oracle/fma_probe.py``, GCC on
+    x86-64 (no FMA in the baseline ISA) keeps two roundings and GCC on aarch64
+    fuses each term into one FMA.  ``CNN_FPMODE=separate|fused`` in the
+    environment overrides the host's mode (the golden fixtures were made on
+    x86-64, so tests that compare with them set "separate").
+    """
+    if fpmode is not None:
+        return int(fpmode)
+    env = os.environ.get("CNN_FPMODE", "").strip().lower()
+    if env in ("separate", "fused"):
+        return FP_FUSED if env == "fused" else FP_SEPARATE
+    import platform
+    return FP_FUSED if platform.machine().lower() in ("aarch64", "arm64") else FP_SEPARATE
+
 _lib = None
 
 
@@ -60,6 +80,10 @@ def lib():
             f = getattr(L, name)
             f.restype = i
             f.argtypes = [p, i64, i32, dbl, i, i, i, p, p]
+        L.oracle_pivot_run.restype = i64
+        L.oracle_pivot_run.argtypes = [p, i64, i32, dbl, i, i, i]
+        L.oracle_pivot_take.restype = i
+        L.oracle_pivot_take.argtypes = [p, p]
         L.oracle_neighbour_row.restype = i64
         L.oracle_neighbour_row.argtypes = [p, i64, i32, p, dbl, i, i, p]
         L.oracle_check_sorted.restype = i
@@ -88,18 +112,20 @@ def _nthreads(nthreads: Optional[int]) -> int:
     return max(1, int(nthreads))
 
 
-def sqdist(xa, xb, fpmode=FP_SEPARATE) -> float:
+def sqdist(xa, xb, fpmode=None) -> float:
     xa = np.ascontiguousarray(xa, dtype=np.float64)
     xb = np.ascontiguousarray(xb, dtype=np.float64)
-    return lib().oracle_sqdist(_ptr(xa), _ptr(xb), xa.shape[0], fpmode)
+    return lib().oracle_sqdist(_ptr(xa), _ptr(xb), xa.shape[0], host_fpmode(fpmode))
 
 
 def neighbourhoods(x, radius_cutoff: float, metric=METRIC_EUCLIDEAN_REDUCED,
-                   fpmode=FP_SEPARATE, nthreads=None, grid: bool = True):
+                   fpmode=None, nthreads=None, grid=True):
     """Sorted CSR neighbourhoods (self included) of every point.
 
     ``radius_cutoff`` is the adjusted value the getter compares with
-    (r**2 for the reduced metric).  Returns (offsets int64[n+1],
+    (r**2 for the reduced metric).  ``grid``: True = cell grid (n_dim <= 3),
+    False = plain brute force, "pivot" = brute force with the exact pivot
+    prune (large sets in high dimension).  Returns (offsets int64[n+1],
     indices int32[nnz]).
     """
     x = np.ascontiguousarray(x, dtype=np.float64)
@@ -109,26 +135,39 @@ def neighbourhoods(x, radius_cutoff: float, metric=METRIC_EUCLIDEAN_REDUCED,
     counts = np.zeros(n, dtype=np.int64)
     L = lib()
     nt = _nthreads(nthreads)
+    fp = host_fpmode(fpmode)
+    if grid == "pivot":
+        nnz = L.oracle_pivot_run(_ptr(x), n, d, float(radius_cutoff), metric, fp, nt)
+        if nnz >= 0:
+            offsets = np.zeros(n + 1, dtype=np.int64)
+            indices = np.empty(max(int(nnz), 1), dtype=np.int32)
+            if L.oracle_pivot_take(_ptr(offsets), _ptr(indices)) != 0:
+                raise MemoryError("oracle pivot rows lost")
+            return offsets, indices[:int(nnz)]
+        if nnz == -1:
+            raise MemoryError("oracle pivot search failed")
+        grid = False  # non-finite coordinates: the plain scan
     fc = L.oracle_neighbour_counts_grid if grid else L.oracle_neighbour_counts
     ff = L.oracle_neighbour_fill_grid if grid else L.oracle_neighbour_fill
-    if fc(_ptr(x), n, d, float(radius_cutoff), metric, fpmode, nt, _ptr(counts)) != 0:
+    if fc(_ptr(x), n, d, float(radius_cutoff), metric, fp, nt, _ptr(counts)) != 0:
         raise MemoryError("oracle neighbour count failed")
     offsets = np.zeros(n + 1, dtype=np.int64)
     np.cumsum(counts, out=offsets[1:])
     indices = np.empty(int(offsets[-1]), dtype=np.int32)
-    if ff(_ptr(x), n, d, float(radius_cutoff), metric, fpmode, nt, _ptr(offsets), _ptr(indices)) != 0:
+    if ff(_ptr(x), n, d, float(radius_cutoff), metric, fp, nt, _ptr(offsets), _ptr(indices)) != 0:
         raise MemoryError("oracle neighbour fill failed")
     return offsets, indices
 
 
 def neighbour_row(x, i: int, radius_cutoff: float, metric=METRIC_EUCLIDEAN_REDUCED,
-                  fpmode=FP_SEPARATE) -> np.ndarray:
+                  fpmode=None) -> np.ndarray:
     """Ascending neighbour indices of point i (self included), brute force."""
     x = np.ascontiguousarray(x, dtype=np.float64)
     n, d = x.shape
     q = np.ascontiguousarray(x[i], dtype=np.float64)
     out = np.empty(n, dtype=np.int32)
-    c = lib().oracle_neighbour_row(_ptr(x), n, d, _ptr(q), float(radius_cutoff), metric, fpmode, _ptr(out))
+    c = lib().oracle_neighbour_row(_ptr(x), n, d, _ptr(q), float(radius_cutoff), metric, host_fpmode(fpmode),
+                                   _ptr(out))
     return out[:c].copy()
 
 
@@ -175,11 +214,11 @@ def fit_bfs_csr(offsets, indices, similarity_cutoff, n_member_cutoff, current_st
 
 
 def fit_bfs_points(x, radius_cutoff, similarity_cutoff, n_member_cutoff, current_start,
-                   consider, labels, metric=METRIC_EUCLIDEAN_REDUCED, fpmode=FP_SEPARATE) -> int:
+                   consider, labels, metric=METRIC_EUCLIDEAN_REDUCED, fpmode=None) -> int:
     """FitterExtBFS._fit with the brute-force getter (default recipe)."""
     x = np.ascontiguousarray(x, dtype=np.float64)
     n, d = x.shape
-    r = lib().oracle_fit_bfs_points(_ptr(x), n, d, float(radius_cutoff), metric, fpmode,
+    r = lib().oracle_fit_bfs_points(_ptr(x), n, d, float(radius_cutoff), metric, host_fpmode(fpmode),
                                     int(similarity_cutoff), int(n_member_cutoff),
                                     int(current_start), _ptr(consider), _ptr(labels))
     if r < 0:
@@ -226,7 +265,7 @@ def sort_by_size(labels: np.ndarray, member_cutoff: Optional[int] = None,
 
 def clustering_fit(x, radius_cutoff: float, cnn_cutoff: int, member_cutoff=None,
                    max_clusters=None, cnn_offset=None, sort: bool = True,
-                   metric=METRIC_EUCLIDEAN_REDUCED, fpmode=FP_SEPARATE,
+                   metric=METRIC_EUCLIDEAN_REDUCED, fpmode=None,
                    labels=None, consider=None, frozen: bool = False,
                    neighbours=None, brute_force: bool = False, nthreads=None):
     """Clustering.fit (src/cnnclustering/cluster.pyx:256-392) on the oracle.
@@ -268,20 +307,21 @@ def clustering_fit(x, radius_cutoff: float, cnn_cutoff: int, member_cutoff=None,
     return labels, info
 
 
-def other_row(x, q, radius_cutoff: float, metric=METRIC_EUCLIDEAN_REDUCED, fpmode=FP_SEPARATE) -> np.ndarray:
+def other_row(x, q, radius_cutoff: float, metric=METRIC_EUCLIDEAN_REDUCED, fpmode=None) -> np.ndarray:
     """Ascending indices of the points of x within the cutoff of the point q
     (NeighboursGetterExtBruteForce._get_other, src/cnnclustering/_types.pyx:1712-1731)."""
     x = np.ascontiguousarray(x, dtype=np.float64)
     n, d = x.shape
     q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1)
     out = np.empty(n, dtype=np.int32)
-    c = lib().oracle_neighbour_row(_ptr(x), n, d, _ptr(q), float(radius_cutoff), metric, fpmode, _ptr(out))
+    c = lib().oracle_neighbour_row(_ptr(x), n, d, _ptr(q), float(radius_cutoff), metric, host_fpmode(fpmode),
+                                   _ptr(out))
     return out[:c].copy()
 
 
 def predict_firstmatch(x, labels, y, radius_cutoff: float, similarity_cutoff: int, n_member_cutoff: int,
                        clusters, other_labels=None, other_consider=None, metric=METRIC_EUCLIDEAN_REDUCED,
-                       fpmode=FP_SEPARATE, periodic_bounds=None):
+                       fpmode=None, periodic_bounds=None):
     """PredictorFirstmatch.predict (src/cnnclustering/_fit.pyx:1235-1291) with
     brute-force getters; parameters as Predictor.make_parameters gives them.
     With ``periodic_bounds`` the clustered points' rows use the periodic
@@ -319,7 +359,7 @@ def predict_firstmatch(x, labels, y, radius_cutoff: float, similarity_cutoff: in
 
 
 def repeat_step_labels(x, radius_cutoffs, cnn_cutoffs, member_cutoff=None, max_clusters=None, cnn_offset=None,
-                       sort: bool = True, metric=METRIC_EUCLIDEAN_REDUCED, fpmode=FP_SEPARATE):
+                       sort: bool = True, metric=METRIC_EUCLIDEAN_REDUCED, fpmode=None):
     """Labels of every step of HierarchicalFitterRepeat._fit
     (src/cnnclustering/_fit.pyx:1060-1144).  Its make_parameters finds no
     neighbours getter on the hierarchical fitter, so each step compares with
@@ -352,7 +392,7 @@ def _rows_to_csr(rows):
     return offsets, indices
 
 
-def periodic_neighbourhoods(x, bounds, radius_cutoff: float, fpmode=FP_SEPARATE):
+def periodic_neighbourhoods(x, bounds, radius_cutoff: float, fpmode=None):
     """Brute-force rows (self included, ascending) under the periodic metric;
     radius_cutoff as compared (r**2)."""
     x = np.ascontiguousarray(x, dtype=np.float64)
@@ -363,7 +403,7 @@ def periodic_neighbourhoods(x, bounds, radius_cutoff: float, fpmode=FP_SEPARATE)
     rows = []
     for i in range(n):
         c = L.oracle_periodic_row(_ptr(x), n, d, _ptr(b), _ptr(np.ascontiguousarray(x[i])), float(radius_cutoff),
-                                  fpmode, _ptr(out))
+                                  host_fpmode(fpmode), _ptr(out))
         rows.append(out[:c].copy())
     return _rows_to_csr(rows)
 
@@ -405,7 +445,7 @@ def fit_from_neighbourhoods(offsets, indices, cnn_cutoff: int, member_cutoff=Non
     return labels
 
 
-def mst_prim_edges(x, radius_cutoff: float, metric=METRIC_EUCLIDEAN_REDUCED, fpmode=FP_SEPARATE, neighbours=None):
+def mst_prim_edges(x, radius_cutoff: float, metric=METRIC_EUCLIDEAN_REDUCED, fpmode=None, neighbours=None):
     """Tree edges of HierarchicalFitterMSTPrim._fit (src/cnnclustering/_fit.pyx:
     820-899) in the order its tree queue pops them: Prim's algorithm over the
     neighbour graph from every unvisited point in index order, weights = the

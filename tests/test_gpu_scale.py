@@ -1,12 +1,14 @@
-"""Parity at the benchmark sizes.
+"""Parity at the benchmark sizes, against the oracle on the whole workload.
 
 * 200,000 x 3 (cell grid): the whole CSR equals the oracle's and the
   labels equal the oracle's BFS + sort_by_size.
-* 500,000 x 64 (tensor cores): the oracle cannot build 2.5e11 pairs in a
-  test, so 64 sampled rows are compared against brute-force float64 rows,
-  the CSR is checked for size-independent properties (rows ascending,
-  symmetric, self included), and the labels equal the oracle's BFS run on
-  that checked CSR.
+* 500,000 x 64 (tensor cores): the whole CSR equals the oracle's exact
+  brute force (the pivot-pruned scan, which evaluates the reference's
+  predicate on every pair it cannot rule out by the triangle inequality),
+  and the labels equal the oracle's BFS on the oracle's own CSR.
+* 1,000,000 x 3 float32-stored, the 8 x 8 batched sweep: the 8 fits at
+  cnn_cutoff 10 and the 8 fits at the largest radius equal the oracle's
+  fits (grid neighbourhoods + BFS + sort_by_size) on all 1,000,000 points.
 """
 import numpy as np
 import pytest
@@ -61,21 +63,26 @@ def test_features_500k_d64_parity(cnn, oracle):
     r = 2.9
     off, idx, labels, st = fit_with_csr(cnn, x, r, 8, None)
     assert st["search_kind"] == 3, st
-    n = x.shape[0]
-    deg = np.diff(off)
-    assert deg.min() >= 1
-    rows = np.repeat(np.arange(n, dtype=np.int64), deg)
-    # ascending rows, self included
-    assert np.all((np.diff(idx.astype(np.int64)) > 0) | (np.diff(rows) != 0))
-    key = rows * n + idx
-    assert np.all(np.isin(np.arange(n, dtype=np.int64) * n + np.arange(n), key))
-    # symmetric
-    assert np.array_equal(np.sort(key), np.sort(idx.astype(np.int64) * n + rows))
-    # sampled rows against brute-force float64 rows
-    rng = np.random.default_rng(1)
-    for i in rng.choice(n, 64, replace=False):
-        want = oracle.neighbour_row(x, int(i), r * r)
-        assert np.array_equal(idx[off[i]:off[i + 1]], want), i
-    # labels: the oracle's BFS on the checked CSR
-    want, _ = oracle.clustering_fit(x, r, 8, neighbours=(off, idx))
+    want_off, want_idx = oracle.neighbourhoods(x, r * r, grid="pivot")
+    assert np.array_equal(off, want_off)
+    assert np.array_equal(idx, want_idx)
+    want, _ = oracle.clustering_fit(x, r, 8, neighbours=(want_off, want_idx))
     assert np.array_equal(labels, want)
+
+
+def test_nested3d_1m_sweep_against_oracle(cnn, oracle):
+    from commonnnclustering_gb300 import workloads
+    x = workloads.nested3d()  # float32-stored, widened exactly
+    x64 = x.astype(np.float64)
+    radii = [float(r) for r in np.linspace(0.03, 0.15, 8)]
+    cuts = [2, 5, 10, 20, 40, 80, 120, 160]
+    got = cnn.sweep(x, radii, cuts, member_cutoff=2)
+    assert got.shape == (8, 8, x.shape[0])
+    for k, r in enumerate(radii):
+        csr = oracle.neighbourhoods(x64, r * r)
+        for j, c in enumerate(cuts):
+            if c != 10 and k != len(radii) - 1:
+                continue
+            want, _ = oracle.clustering_fit(x64, r, c, member_cutoff=2, neighbours=csr)
+            assert np.array_equal(got[k, j], want), (r, c)
+        del csr
