@@ -212,6 +212,7 @@ class Context:
         self.device = int(device)
         self.stream = stream
         self._n_points = 0
+        self._points_set = False  # without points the library itself reports the missing graph
 
     def close(self):
         if getattr(self, "_h", None):
@@ -265,6 +266,7 @@ class Context:
                     "cnn_set_distances")
         self._points_ref = keep
         self._n_points = n
+        self._points_set = True
 
     def set_periodic_bounds(self, bounds):
         b = np.ascontiguousarray(bounds, dtype=np.float64).reshape(-1)
@@ -292,6 +294,7 @@ class Context:
                                              int(shape[0]), int(shape[1]), mem), "cnn_set_points")
         self._points_ref = keep
         self._n_points = int(shape[0])
+        self._points_set = True
         return shape
 
     def build_neighbours(self, radius_cutoff: float, metric: int = METRIC_EUCLIDEAN_REDUCED,
@@ -314,6 +317,7 @@ class Context:
                                                      ctypes.c_void_p(idx.ctypes.data), n, MEM_HOST),
                         "cnn_set_neighbours")
         self._n_points = n
+        self._points_set = True
 
     def neighbour_count(self) -> int:
         v = ctypes.c_int64()
@@ -347,7 +351,7 @@ class Context:
         current graph (ValueError otherwise, before the library is called).
         """
         n_lab, n_con = int(labels.shape[0]), int(consider.shape[0])
-        if n_lab != n_con or n_lab != int(self._n_points):
+        if n_lab != n_con or (self._points_set and n_lab != int(self._n_points)):
             raise ValueError(f"labels ({n_lab}) and consider ({n_con}) must have one entry per point of the "
                              f"current neighbour graph ({int(self._n_points)})")
         if is_device_array(labels):

@@ -107,6 +107,7 @@ def test_context_fit_rejects_arrays_of_another_length_before_calling_the_library
     ctx._lib = None
     ctx._h = None
     ctx._n_points = 100
+    ctx._points_set = True
     with pytest.raises(ValueError):
         ctx.fit(7, 6, 1, np.ones(100, dtype=np.uint8), np.zeros(99, dtype=np.int64))
     with pytest.raises(ValueError):
