@@ -1,9 +1,9 @@
-"""Benchmark: CommonNN fit points/s on the 200,000 x 3 MD-like workload.
+"""Benchmark: CommonNN fit points/s, headline on the 200,000 x 3 MD-like workload.
 
-One step = one complete fit of 200,000 points in 3D float64 (20
-anisotropic Gaussians + 5 % background, mean degree ~215): cell-grid
-radius search (r = 0.1) -> CSR, common-neighbour check (c = 10) +
-union-find, canonical labels, sort_by_size (member_cutoff = 50).
+One step of the headline = one complete fit of 200,000 points in 3D float64
+(20 anisotropic Gaussians + 5 % background, mean degree ~215): cell-grid
+radius search (r = 0.1) -> neighbour graph, common-neighbour check (c = 10)
++ union-find, canonical labels, sort_by_size (member_cutoff = 50).
 
 * ``value``  -- points/s with the points already resident in HBM (device
   pointers through the C ABI), CUDA events around each step on the
@@ -16,11 +16,19 @@ union-find, canonical labels, sort_by_size (member_cutoff = 50).
   its CUDA-event time (library stage events, same stream).
 * ``cpu_baseline`` -- the oracle port of the reference path on this
   host's cores (1 thread, like the reference).
+* ``workloads`` -- the other four workloads, each with its own value, e2e,
+  roofline, clocks and CPU baseline: ``blobs2d-5k`` (5,000 x 2),
+  ``features-500k-d64`` (tensor-core search, beside the plain float32
+  all-pairs search on the same points), ``nested3d-1m-sweep`` (64 (r, c)
+  fits in one batched call, beside the same fits one by one) and
+  ``serve-stream`` (continuous batching of a job stream, beside one job at
+  a time).  ``--headline-only`` skips them; ``--workload NAME`` runs one
+  workload as the only line.
 
 ``--impl reference`` times the reference's CPU path instead (the oracle
 port: grid-restated neighbour lists on all host threads, then the
 reference's BFS with the sorted-merge check on one thread, then
-sort_by_size), one full fit per step.
+sort_by_size), one full fit of the headline workload per step.
 
 With torchrun (N > 1) every rank fits its own replica of the workload on
 its own GPU (the fit does not shard); value = points of all ranks / the
@@ -51,20 +59,24 @@ WORKLOADS = {
                        gen=("blobs2d", {})),
     # 500,000 x 64 feature vectors, tensor-core Gram search (mean degree ~100)
     "features-500k-d64": dict(name="features-500k-d64", n=500_000, d=64, radius_cutoff=2.9, cnn_cutoff=8,
-                              member_cutoff=None, gen=("features", {})),
+                              member_cutoff=None, gen=("features", {}), max_steps=5),
     # 1,000,000 x 3 float32 nested blobs: 8 radii x 8 cnn_cutoffs in one batched sweep
     "nested3d-1m-sweep": dict(name="nested3d-1m-sweep", n=1_000_000, d=3, radius_cutoff=0.15, cnn_cutoff=None,
-                              member_cutoff=None, gen=("nested3d", {}), kind="sweep",
+                              member_cutoff=None, gen=("nested3d", {}), kind="sweep", max_steps=3,
                               radii=[float(r) for r in np.linspace(0.03, 0.15, 8)],
-                              cuts=[2, 5, 10, 20, 40, 80, 120, 160]),
+                              cuts=[2, 5, 10, 20, 40, 80, 120, 160], cpu_subsample=20),
     # served request stream: Poisson arrivals of jobs of uneven size and dimension
     "serve-stream": dict(name="serve-stream", n=None, d=None, radius_cutoff=None, cnn_cutoff=None,
                          member_cutoff=10, gen=None, kind="serve", n_jobs=2000, rates=[10.0, 100.0, 500.0]),
+    # the same stream shortened for the default run: 400 jobs at 100 and 500 jobs/s
+    "serve-stream-short": dict(name="serve-stream", n=None, d=None, radius_cutoff=None, cnn_cutoff=None,
+                               member_cutoff=10, gen=None, kind="serve", n_jobs=400, rates=[100.0, 500.0]),
     # the same generator at 100,000 points (small enough for a full ncu capture)
     "features-100k-d64": dict(name="features-100k-d64", n=100_000, d=64, radius_cutoff=2.9, cnn_cutoff=8,
                               member_cutoff=None, gen=("features", {})),
 }
-WORKLOAD = WORKLOADS["md3d-200k"]
+HEADLINE = "md3d-200k"
+SUB_WORKLOADS = ["blobs2d-5k", "features-500k-d64", "nested3d-1m-sweep", "serve-stream-short"]
 METRIC = "CommonNN fit points/s (bit-exact labels)"
 UNIT = "points/s"
 
@@ -104,6 +116,14 @@ def reduce_max(dist, v: float) -> float:
 def barrier(dist):
     if dist is not None:
         dist.barrier()
+
+
+def load_peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "_fallback": True}
 
 
 class ClockSampler:
@@ -153,35 +173,43 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def make_points():
+def make_points(W):
     from commonnnclustering_gb300 import workloads
-    name, kw = WORKLOAD["gen"]
-    return getattr(workloads, name)(n=WORKLOAD["n"], **kw)
+    name, kw = W["gen"]
+    return getattr(workloads, name)(n=W["n"], **kw)
 
 
-def roofline_entry(stats_list, nnz, n, peaks):
-    """Dominant kernel by mean stage time; algorithmic bytes per launch."""
-    d = WORKLOAD["d"]
-    if d >= 16:  # tensor-core Gram kernel: FLOPs of the 128 x 128 tiles it actually computed
-        ms = statistics.mean(s["ms_gram"] for s in stats_list)
-        nblk = (n + 127) // 128
-        all_pairs = nblk * (nblk + 1) // 2 * 128 * 128
-        pairs = statistics.mean(s["n_candidates"] for s in stats_list)  # tiles left after pruning x 128^2
-        dp = (d + 63) // 64 * 64
-        useful = 2.0 * pairs * dp
-        issued = 6.0 * useful  # three-way bf16 split: hi.hi + hi.mid + mid.hi + hi.lo + lo.hi + mid.mid
-        peak = peaks.get("bf16_tflops")
-        achieved = issued / (ms * 1e-3) / 1e12 if ms > 0 else None
-        return {
-            "kernel": "gram_search_kernel (tcgen05, three-way bf16 split)", "bound": "tensor", "achieved": achieved, "peak": peak,
-            "unit": "TFLOP/s", "frac": (achieved / peak) if (achieved and peak) else None, "traffic": None,
-            "algorithmic_flops_issued": issued, "algorithmic_flops_useful": useful,
-            "tile_pairs_computed": pairs, "tile_pairs_unpruned": all_pairs,
-            "useful_tflops": useful / (ms * 1e-3) / 1e12 if ms > 0 else None, "ms_per_launch": ms,
-            "peak_source": "MEASURED_PEAKS.json bf16_tflops (measured burst)" if peak else "fallback",
-            "stage_ms": {k: round(statistics.mean(s[k] for s in stats_list), 4)
-                         for k in ("ms_count", "ms_gram", "ms_check", "ms_label", "ms_sort")},
-        }
+# ---------------------------------------------------------------------------
+# rooflines
+# ---------------------------------------------------------------------------
+def tensor_roofline(W, stats_list, n, peaks):
+    """Gram kernel: FLOPs of the 128 x 128 tiles it computed (useful and issued)."""
+    d = W["d"]
+    ms = statistics.mean(s["ms_gram"] for s in stats_list)
+    nblk = (n + 127) // 128
+    all_pairs = nblk * (nblk + 1) // 2 * 128 * 128
+    pairs = statistics.mean(s["n_candidates"] for s in stats_list)  # tiles left after pruning x 128^2
+    dp = (d + 63) // 64 * 64
+    useful = 2.0 * pairs * dp
+    issued = 6.0 * useful  # three-way bf16 split: hi.hi + hi.mid + mid.hi + hi.lo + lo.hi + mid.mid
+    peak = peaks.get("bf16_tflops")
+    achieved = issued / (ms * 1e-3) / 1e12 if ms > 0 else None
+    return {
+        "kernel": "gram_search_kernel (tcgen05, three-way bf16 split)", "bound": "tensor", "achieved": achieved,
+        "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if (achieved and peak) else None, "traffic": None,
+        "algorithmic_flops_issued": issued, "algorithmic_flops_useful": useful,
+        "tile_pairs_computed": pairs, "tile_pairs_unpruned": all_pairs,
+        "useful_tflops": useful / (ms * 1e-3) / 1e12 if ms > 0 else None,
+        "useful_frac": (useful / (ms * 1e-3) / 1e12 / peak) if (ms > 0 and peak) else None,
+        "ms_per_launch": ms,
+        "peak_source": "MEASURED_PEAKS.json bf16_tflops (measured burst)" if not peaks.get("_fallback") else "fallback",
+        "stage_ms": {k: round(statistics.mean(s[k] for s in stats_list), 4)
+                     for k in ("ms_count", "ms_gram", "ms_check", "ms_label", "ms_sort")},
+    }
+
+
+def hbm_roofline(stats_list, nnz, n, peaks):
+    """Dominant stage by mean CUDA-event time; algorithmic bytes per launch."""
     stages = {
         # stage -> (kernel name, algorithmic bytes per launch)
         # one pass into per-row slots: float4 coordinates read, rows, lengths and slot starts written
@@ -211,16 +239,18 @@ def roofline_entry(stats_list, nnz, n, peaks):
         "kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
         "frac": (achieved / peak) if (achieved and peak) else None, "traffic": traffic,
         "algorithmic_bytes": bytes_, "ms_per_launch": ms,
-        "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback 6800",
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if not peaks.get("_fallback") else "fallback 6800",
         "stage_ms": {k: round(v, 4) for k, v in means.items()},
         "other_stage_ms": {k: round(statistics.mean(s.get(k, 0.0) for s in stats_list), 4)
                            for k in ("ms_bbox", "ms_scan", "ms_nodes")},
     }
 
 
-def cpu_baseline(x, budget_s=25.0):
+# ---------------------------------------------------------------------------
+# CPU baselines (the oracle port of the reference path; bounded samples)
+# ---------------------------------------------------------------------------
+def cpu_baseline(W, x, budget_s=25.0):
     from oracle import cnn_oracle
-    W = WORKLOAD
     if W["d"] >= 16:
         # all-pairs float64 rows on 1 thread for a sample of query points; the
         # full fit would take hours, so the rate is per query row, stated as such
@@ -260,16 +290,16 @@ def cpu_baseline(x, budget_s=25.0):
                       f"BFS with sorted-merge check + sort_by_size, 1 thread), best {best:.2f} s"}
 
 
-def run_gpu(args):
+# ---------------------------------------------------------------------------
+# one fit per step (md3d-200k, blobs2d-5k, features-500k-d64)
+# ---------------------------------------------------------------------------
+def fit_record(W, args, peaks, dist=None, world=1, local=0, rank=0, cpu=True):
     import torch
     from commonnnclustering_gb300 import _abi
 
-    rank, world, local = dist_env()
-    dist = init_dist(world)
-    torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    W = WORKLOAD
-    x = make_points()
+    steps = min(args.steps, W.get("max_steps", args.steps))
+    x = make_points(W)
     n = x.shape[0]
     stream = torch.cuda.Stream(device=dev)
     ctx = _abi.Context(local, stream=int(stream.cuda_stream))
@@ -296,13 +326,13 @@ def run_gpu(args):
         step()
     torch.cuda.synchronize()
     launches0 = ctx.stats()["n_launches"]
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     stats_list = []
     barrier(dist)
     torch.cuda.synchronize()
     t_wall = time.perf_counter()
     with ClockSampler(local) as clocks:
-        for i in range(args.steps):
+        for i in range(steps):
             with torch.cuda.stream(stream):
                 flush.zero_()  # 256 MiB write: evicts L2 between steps
             ev[i][0].record(stream)
@@ -315,9 +345,33 @@ def run_gpu(args):
     step_ms = [a.elapsed_time(b) for a, b in ev]
     mean_ms = statistics.mean(step_ms)
     max_ms = reduce_max(dist, mean_ms)
-    launches = (stats_list[-1]["n_launches"] - launches0) // max(args.steps, 1)
+    launches = (stats_list[-1]["n_launches"] - launches0) // max(steps, 1)
     nnz = stats_list[-1]["n_nonzero"]
     check_labels = labels.cpu().numpy()
+
+    # the plain float32 all-pairs search on the same points (tensor-core workloads)
+    plain = None
+    if W["d"] >= 16:
+        ctx.set_search(_abi.SEARCH_ALL_PAIRS)
+        plain_labels = torch.zeros(n, dtype=torch.int64, device=dev)
+        plain_cons = torch.ones(n, dtype=torch.uint8, device=dev)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a.record(stream)
+        ctx.set_points(xt)
+        ctx.build_neighbours(r2)
+        ctx.fit(sc, nm, 1, plain_cons, plain_labels)
+        ctx.sort_by_size(plain_labels, sort_cutoff, None)
+        b.record(stream)
+        torch.cuda.synchronize()
+        pst = ctx.stats()
+        ctx.set_search(_abi.SEARCH_AUTO)
+        plain_ms = a.elapsed_time(b)
+        plain = {"search": "tiled all-pairs float32 + float64 band (tile_search_kernel)", "ms_per_fit": plain_ms,
+                 "search_kind": pst["search_kind"], "identical_labels": bool(torch.equal(plain_labels, labels)),
+                 "identical_neighbour_count": pst["n_nonzero"] == nnz,
+                 "speedup_of_tensor_core_path": plain_ms / mean_ms}
 
     # e2e: host buffers through the C ABI (pinned), copies inside the timed region
     x_host = torch.from_numpy(x).pin_memory().numpy()
@@ -333,10 +387,10 @@ def run_gpu(args):
         e2e_ctx.fit(sc, nm, 1, con_host, lab_host)
         e2e_ctx.sort_by_size(lab_host, sort_cutoff, None)
 
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, min(args.warmup, 3))):
         e2e_step()
     e2e_times = []
-    for _ in range(args.steps):
+    for _ in range(steps):
         flush.zero_()
         torch.cuda.synchronize()
         t = time.perf_counter()
@@ -344,51 +398,75 @@ def run_gpu(args):
         e2e_times.append(time.perf_counter() - t)
     e2e_max = reduce_max(dist, statistics.mean(e2e_times))
     if not np.array_equal(lab_host, check_labels):
-        raise SystemExit("bench: host-buffer and device-buffer fits disagree")
+        raise SystemExit(f"bench: host-buffer and device-buffer fits of {W['name']} disagree")
+    e2e_ctx.close()
     h2d = n * W["d"] * 8 + n * 8 * 2 + n      # points, labels (fit + sort), consider
     d2h = n * 8 * 2 + n                       # labels (fit + sort), consider
-
+    ctx.close()
     if rank != 0:
-        return
-    peaks = {}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-    except Exception:
-        peaks = {"hbm_gbs": 6800.0}
-    line = {
+        return None
+    rec = {
         "metric": METRIC, "value": world * n / (max_ms * 1e-3), "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": max_ms, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": f"synthetic (seeded {WORKLOAD['gen'][0]} generator)",
+        "steps": steps, "warmup": args.warmup, "ms_per_step": max_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": f"synthetic (seeded {W['gen'][0]} generator)",
         "config": {"workload": W["name"], "n_points": n, "n_dim": W["d"], "radius_cutoff": W["radius_cutoff"],
                    "cnn_cutoff": W["cnn_cutoff"], "member_cutoff": W["member_cutoff"],
                    "neighbour_pairs": nnz, "l2": "flushed between steps (256 MiB write)",
                    "parallelism": "replicas" if world > 1 else "single", "fpmode": fpmode_name()},
         "e2e": {"value": world * n / e2e_max, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": int(launches) * args.steps,
+        "gpu_launches": int(launches) * steps,
         "gpu_launches_per_step": int(launches),
         "clocks": clocks.summary(),
-        "roofline": roofline_entry(stats_list, nnz, n, peaks),
+        "roofline": (tensor_roofline(W, stats_list, n, peaks) if W["d"] >= 16
+                     else hbm_roofline(stats_list, nnz, n, peaks)),
         "wall_s_timed_region": t_wall,
         "fit_stats": {k: stats_list[-1][k] for k in ("n_nodes", "n_checks", "n_accepted", "n_exact",
                                                      "n_candidates", "n_clusters", "filter_band", "max_abs_err",
                                                      "search_kind")},
     }
-    if world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(x)
-    print(json.dumps(line), flush=True)
+    if W["d"] >= 16:
+        rec["fit_stats"]["recheck_fraction"] = (stats_list[-1]["n_exact"] / stats_list[-1]["n_candidates"]
+                                                if stats_list[-1]["n_candidates"] else None)
+    if plain is not None:
+        rec["plain_gpu"] = plain
+    if cpu and world == 1 and not args.no_cpu_baseline:
+        rec["cpu_baseline"] = cpu_baseline(W, x)
+    return rec
 
 
-def run_sweep(args):
+# ---------------------------------------------------------------------------
+# batched sweep: 64 (radius, cut) fits per step
+# ---------------------------------------------------------------------------
+def sweep_cpu_baseline(W, x):
+    """The reference's way of scanning the 64 pairs (one full fit each) on a
+    documented subsample: every k-th point, oracle fits on 1 thread."""
+    from oracle import cnn_oracle
+    k = W["cpu_subsample"]
+    xs = np.ascontiguousarray(x[::k], dtype=np.float64)
+    t = time.perf_counter()
+    fits = 0
+    for r in W["radii"]:
+        for c in W["cuts"]:
+            if time.perf_counter() - t > 30.0:
+                break
+            cnn_oracle.clustering_fit(xs, r, c, member_cutoff=2, nthreads=1)
+            fits += 1
+    dt = time.perf_counter() - t
+    return {"value": xs.shape[0] * fits / dt, "unit": "points/s (summed over the fits)", "cores": 1, "kind": "port",
+            "sample": f"{fits} of the 64 (r, c) fits on every {k}th point ({xs.shape[0]} points, the same box, so "
+                      f"1/{k} of the density) with the oracle restatement (grid neighbour lists + BFS + "
+                      f"sort_by_size, 1 thread), {dt:.1f} s; not extrapolated to 1,000,000 points"}
+
+
+def sweep_record(W, args, peaks, dist=None, world=1, local=0, rank=0, cpu=True):
     """Batched sweep vs the same 64 fits run one by one (both on the GPU)."""
     import torch
     from commonnnclustering_gb300 import _abi
 
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    W = WORKLOAD
-    x = make_points()  # float32, widened exactly inside the library
+    steps = min(args.steps, W.get("max_steps", args.steps))
+    x = make_points(W)  # float32, widened exactly inside the library
     n = x.shape[0]
     radii, cuts = W["radii"], W["cuts"]
     r2 = [r * r for r in radii]
@@ -405,6 +483,7 @@ def run_sweep(args):
 
     lab = torch.zeros(n, dtype=torch.int64, device=dev)
     con = torch.ones(n, dtype=torch.uint8, device=dev)
+    nnz_by_radius = {}
 
     def one_by_one(check=None):
         for k, rr in enumerate(r2):
@@ -418,12 +497,13 @@ def run_sweep(args):
                 ctx.sort_by_size(lab, 2, None)
                 if check is not None:
                     stream.synchronize()  # the library writes lab on its own stream
-                if check is not None and not torch.equal(lab, check[k, j]):
-                    raise SystemExit(f"bench: sweep differs from the separate fit at r={radii[k]}, c={cuts[j]}")
+                    nnz_by_radius[k] = ctx.neighbour_count()
+                    if not torch.equal(lab, check[k, j]):
+                        raise SystemExit(f"bench: sweep differs from the separate fit at r={radii[k]}, c={cuts[j]}")
 
-    def timed(fn, steps):
+    def timed(fn, nsteps):
         ts = []
-        for _ in range(steps):
+        for _ in range(nsteps):
             with torch.cuda.stream(stream):
                 flush.zero_()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -434,39 +514,105 @@ def run_sweep(args):
             ts.append(a.elapsed_time(b))
         return statistics.mean(ts)
 
-    for _ in range(args.warmup):
+    for _ in range(max(1, min(args.warmup, 3))):
         batched()
     one_by_one(check=out)  # also the parity check: every pair equals its separate fit
     with ClockSampler(local) as clocks:
-        ms_batched = timed(batched, args.steps)
-        ms_plain = timed(one_by_one, max(1, min(args.steps, 2)))
+        ms_batched = timed(batched, steps)
+        ms_plain = timed(one_by_one, 1)
+    ms_batched = reduce_max(dist, ms_batched)
     fits = len(radii) * len(cuts)
     st = ctx.stats()
+
+    # e2e: host points in, host labels out, through the public sweep call
+    e2e_ctx = _abi.Context(local)
+    x_host = torch.from_numpy(x).pin_memory().numpy()
+    e2e_ctx.set_points(x_host)
+    got = e2e_ctx.sweep(r2, cut_pairs, member_cutoff=2)
+    e2e_times = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        e2e_ctx.set_points(x_host)
+        got = e2e_ctx.sweep(r2, cut_pairs, member_cutoff=2)
+        e2e_times.append(time.perf_counter() - t)
+    if not np.array_equal(got, out.cpu().numpy()):
+        raise SystemExit("bench: host-buffer and device-buffer sweeps disagree")
+    e2e_ctx.close()
+    e2e_s = reduce_max(dist, statistics.mean(e2e_times))
+    ctx.close()
     if rank != 0:
-        return
-    line = {
-        "metric": METRIC, "value": n * fits / (ms_batched * 1e-3), "unit": "points/s (summed over the fits)",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_batched,
+        return None
+    # whole-step algorithmic bytes: the largest-radius graph written once,
+    # every smaller radius's graph written once, and one pass of each fit
+    # over its graph (int32 entries + per-point offsets, flags and labels)
+    nnz_max = nnz_by_radius[len(radii) - 1]
+    bytes_step = 4 * nnz_max + sum(4 * nnz_by_radius[k] for k in range(len(radii) - 1)) + \
+        sum(len(cuts) * (4 * nnz_by_radius[k] + 24 * n) for k in range(len(radii)))
+    achieved = bytes_step / (ms_batched * 1e-3) / 1e9
+    peak = peaks.get("hbm_gbs")
+    rec = {
+        "metric": METRIC, "value": world * n * fits / (ms_batched * 1e-3), "unit": "points/s (summed over the fits)",
+        "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": ms_batched,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded nested3d generator, float32-stored)",
         "config": {"workload": W["name"], "n_points": n, "n_dim": 3, "radii": radii, "cnn_cutoffs": cuts,
                    "member_cutoff": 2, "fits_per_step": fits, "l2": "flushed between steps (256 MiB write)",
-                   "largest_radius_pairs": st["n_nonzero"]},
-        "plain_one_by_one_ms": ms_plain, "speedup_vs_one_by_one": ms_plain / ms_batched,
-        "fits_per_s": fits / (ms_batched * 1e-3), "clocks": clocks.summary(),
-        "gpu_launches_per_step": None,
+                   "largest_radius_pairs": nnz_max, "pairs_by_radius": [nnz_by_radius[k] for k in range(len(radii))],
+                   "fpmode": fpmode_name()},
+        "e2e": {"value": world * n * fits / e2e_s, "unit": "points/s (summed over the fits)",
+                "h2d_bytes_per_step": n * 3 * 4, "d2h_bytes_per_step": fits * n * 8},
+        "plain_gpu": {"path": "the same 64 fits one by one (search + fit + sort_by_size each)",
+                      "ms_per_step": ms_plain, "speedup_of_batched_sweep": ms_plain / ms_batched},
+        "fits_per_s": fits / (ms_batched * 1e-3),
+        "clocks": clocks.summary(),
+        "roofline": {"kernel": "whole sweep step (search at r_max, radius buckets, graphs of all radii, 64 fits)",
+                     "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if peak else None, "traffic": None,
+                     "algorithmic_bytes": bytes_step, "ms_per_launch": ms_batched,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+        "last_fit_stats": {k: st[k] for k in ("n_nodes", "n_checks", "n_accepted", "n_clusters")},
     }
-    print(json.dumps(line), flush=True)
+    if cpu and world == 1 and not args.no_cpu_baseline:
+        rec["cpu_baseline"] = sweep_cpu_baseline(W, x)
+    return rec
 
 
-def run_serve(args):
+# ---------------------------------------------------------------------------
+# served stream
+# ---------------------------------------------------------------------------
+def serve_cpu_baseline(raw, budget_s=20.0):
+    """Sequential per-job reference fits (the oracle restatement, 1 thread)."""
+    from oracle import cnn_oracle
+    t = time.perf_counter()
+    done, pts = 0, 0
+    for j in raw:
+        if time.perf_counter() - t > budget_s:
+            break
+        x = j["points"]
+        if x.shape[1] >= 16:
+            # the rows of a d >= 16 job come from the pivot-pruned exact scan;
+            # the reference itself would run its O(n^2) getter
+            csr = cnn_oracle.neighbourhoods(x, j["radius_cutoff"] ** 2, grid="pivot", nthreads=1)
+            cnn_oracle.clustering_fit(x, j["radius_cutoff"], j["cnn_cutoff"], member_cutoff=j["member_cutoff"],
+                                      neighbours=csr)
+        else:
+            cnn_oracle.clustering_fit(x, j["radius_cutoff"], j["cnn_cutoff"], member_cutoff=j["member_cutoff"],
+                                      nthreads=1)
+        done += 1
+        pts += x.shape[0]
+    dt = time.perf_counter() - t
+    return {"value": done / dt, "unit": "jobs/s", "cores": 1, "kind": "port",
+            "sample": f"the first {done} jobs of the stream ({pts} points) fitted one after another by the "
+                      f"oracle restatement (grid or pivot-pruned neighbour lists + BFS + sort_by_size, 1 thread), "
+                      f"{dt:.1f} s; {pts / dt:.0f} points/s"}
+
+
+def serve_record(W, args, peaks, dist=None, world=1, local=0, rank=0, cpu=True):
     """Served stream: continuous batching vs one job at a time, per arrival rate."""
-    import torch
     from commonnnclustering_gb300 import serve, workloads
 
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    W = WORKLOAD
     results = []
     t_gen = time.perf_counter()
     raw = workloads.job_stream(n_jobs=W["n_jobs"], rate=1.0, seed=11)
@@ -474,52 +620,104 @@ def run_serve(args):
     # arrival gaps of the trace at rate 1; each rate rescales them
     base = np.array([j["arrival"] for j in raw])
     srv = serve.Server(n_slots=args.slots, device=local)
+    clocks = ClockSampler(local)
     try:
         # warm-up: every slot sees the largest jobs once (device workspaces grown)
         big = sorted(raw, key=lambda j: -j["points"].shape[0] * j["points"].shape[1])[: 2 * args.slots]
         srv.serve([serve.Job(job_id=-1 - i, **dict(j, arrival=0.0)) for i, j in enumerate(big)], realtime=False)
         srv.done.clear()
-        for rate in W["rates"]:
-            n_jobs = W["n_jobs"] if rate >= 100 else min(W["n_jobs"], int(rate * 60))  # <= 60 s of arrivals
-            jobs = [serve.Job(job_id=i, **dict(raw[i], arrival=float(base[i] / rate))) for i in range(n_jobs)]
-            srv.done.clear()
-            srv.serve(jobs, realtime=True)
-            batched = serve.latency_summary(jobs)
-            plain_jobs = [serve.Job(job_id=i, **dict(raw[i], arrival=float(base[i] / rate))) for i in range(n_jobs)]
-            serve.serve_one_at_a_time(plain_jobs, device=local, realtime=True)
-            plain = serve.latency_summary(plain_jobs)
-            differ = [(a, b) for a, b in zip(jobs, plain_jobs)
-                      if a.labels is None or b.labels is None or not np.array_equal(a.labels, b.labels)]
-            detail = []
-            for a, b in differ[:5]:
-                from commonnnclustering_gb300 import _abi
-                c = _abi.Context(local)
-                alone = serve.run_job_alone(c, a)  # a fresh context decides which side is off
-                c.close()
-                detail.append({"job": a.job_id, "n": int(a.points.shape[0]), "d": int(a.points.shape[1]),
-                               "radius_cutoff": a.radius_cutoff, "cnn_cutoff": a.cnn_cutoff,
-                               "error_mix": a.error, "error_alone": b.error,
-                               "mix_equals_fresh": a.labels is not None and bool(np.array_equal(a.labels, alone)),
-                               "alone_equals_fresh": b.labels is not None and bool(np.array_equal(b.labels, alone))})
-            results.append({"rate_jobs_per_s": rate, "jobs": n_jobs, "continuous_batching": batched,
-                            "one_at_a_time": plain, "identical_labels": not differ,
-                            "jobs_differing": len(differ), "differing": detail,
-                            "max_jobs_in_flight": srv.max_in_flight})
+        with clocks:
+            for rate in W["rates"]:
+                n_jobs = W["n_jobs"] if rate >= 100 else min(W["n_jobs"], int(rate * 60))  # <= 60 s of arrivals
+                jobs = [serve.Job(job_id=i, **dict(raw[i], arrival=float(base[i] / rate))) for i in range(n_jobs)]
+                srv.done.clear()
+                srv.serve(jobs, realtime=True)
+                batched = serve.latency_summary(jobs)
+                plain_jobs = [serve.Job(job_id=i, **dict(raw[i], arrival=float(base[i] / rate)))
+                              for i in range(n_jobs)]
+                serve.serve_one_at_a_time(plain_jobs, device=local, realtime=True)
+                plain = serve.latency_summary(plain_jobs)
+                differ = [(a, b) for a, b in zip(jobs, plain_jobs)
+                          if a.labels is None or b.labels is None or not np.array_equal(a.labels, b.labels)]
+                results.append({"rate_jobs_per_s": rate, "jobs": n_jobs, "continuous_batching": batched,
+                                "one_at_a_time": plain, "identical_labels": not differ,
+                                "jobs_differing": len(differ),
+                                "errors": sorted({a.error for a, _ in differ if a.error} |
+                                                 {b.error for _, b in differ if b.error})[:3],
+                                "max_jobs_in_flight": srv.max_in_flight})
     finally:
         srv.close()
     if rank != 0:
-        return
+        return None
     top = results[-1]
-    line = {
+    sizes = np.array([j["points"].shape[0] for j in raw])
+    dims = np.array([j["points"].shape[1] for j in raw])
+    rec = {
         "metric": "served CommonNN fits: jobs/s and p50/p99 latency", "value": top["continuous_batching"]["jobs_per_s"],
         "unit": "jobs/s", "n_gpus": world, "steps": len(results), "warmup": 1, "ms_per_step": None,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded job stream: lognormal sizes, d in {2,3,16,64}, Poisson arrivals)",
         "config": {"workload": W["name"], "n_jobs": W["n_jobs"], "rates": W["rates"], "slots": args.slots,
-                   "trace_generation_s": t_gen},
+                   "trace_generation_s": t_gen, "points_per_job_median": float(np.median(sizes)),
+                   "points_per_job_max": int(sizes.max()),
+                   "jobs_by_dim": {str(d): int((dims == d).sum()) for d in (2, 3, 16, 64)},
+                   "fpmode": fpmode_name()},
+        # jobs arrive as host arrays and leave as host labels: the value is already end to end
+        "e2e": {"value": top["continuous_batching"]["jobs_per_s"], "unit": "jobs/s",
+                "h2d_bytes_per_step": int(sum(j["points"].nbytes for j in raw[:top["jobs"]])),
+                "d2h_bytes_per_step": int(sum(8 * j["points"].shape[0] for j in raw[:top["jobs"]]))},
+        "p50_ms": top["continuous_batching"]["p50_ms"], "p99_ms": top["continuous_batching"]["p99_ms"],
+        "plain_gpu": {"path": "one job at a time on one context", "jobs_per_s": top["one_at_a_time"]["jobs_per_s"],
+                      "p50_ms": top["one_at_a_time"]["p50_ms"], "p99_ms": top["one_at_a_time"]["p99_ms"],
+                      "speedup_of_continuous_batching": (top["continuous_batching"]["jobs_per_s"] /
+                                                         top["one_at_a_time"]["jobs_per_s"])},
         "per_rate": results,
+        "clocks": clocks.summary(),
+        "roofline": None,
+        "roofline_note": "a mix of jobs of every size and dimension; the kernels' rooflines are those of the fit "
+                         "workloads",
     }
-    print(json.dumps(line), flush=True)
+    if cpu and world == 1 and not args.no_cpu_baseline:
+        rec["cpu_baseline"] = serve_cpu_baseline(raw)
+    return rec
+
+
+def record_for(name, args, peaks, **kw):
+    W = WORKLOADS[name]
+    kind = W.get("kind")
+    if kind == "sweep":
+        return sweep_record(W, args, peaks, **kw)
+    if kind == "serve":
+        return serve_record(W, args, peaks, **kw)
+    return fit_record(W, args, peaks, **kw)
+
+
+def run_gpu(args):
+    import torch
+
+    rank, world, local = dist_env()
+    dist = init_dist(world)
+    torch.cuda.set_device(local)
+    peaks = load_peaks()
+    name = args.workload or HEADLINE
+    line = record_for(name, args, peaks, dist=dist, world=world, local=local, rank=rank)
+    if args.workload is None and not args.headline_only and world == 1:
+        subs = {}
+        for sub in SUB_WORKLOADS:
+            key = WORKLOADS[sub]["name"]
+            t = time.perf_counter()
+            try:
+                subs[key] = record_for(sub, args, peaks, dist=dist, world=world, local=local, rank=rank)
+            except SystemExit:
+                raise
+            except Exception as e:  # a failing sub-workload is reported; the headline still stands
+                subs[key] = {"error": f"{type(e).__name__}: {e}"}
+            if subs[key] is not None:
+                subs[key]["bench_wall_s"] = time.perf_counter() - t
+        if line is not None:
+            line["workloads"] = subs
+    if line is not None:
+        print(json.dumps(line), flush=True)
 
 
 def run_reference(args):
@@ -527,14 +725,19 @@ def run_reference(args):
     if rank != 0:
         return
     from oracle import cnn_oracle
-    W = WORKLOAD
-    x = make_points()
+    W = WORKLOADS[args.workload or HEADLINE]
+    if W.get("kind"):
+        print(json.dumps({"impl": "reference", "unavailable": f"the reference arm times the fit workloads; "
+                                                              f"{W['name']} reports its CPU baseline in its own "
+                                                              f"record"}), flush=True)
+        return
+    x = make_points(W)
     n = x.shape[0]
     cores = max(1, len(os.sched_getaffinity(0)))
     if W["d"] >= 16:
         # the reference's brute-force getter over all pairs is hours per fit
         # here; each step times a bounded sample of query rows on all cores
-        base = cpu_baseline(x)
+        base = cpu_baseline(W, x)
         rows_per_s = base["value"] * cores
         line = {
             "impl": "reference", "metric": METRIC, "value": rows_per_s, "unit": UNIT, "n_gpus": world,
@@ -542,7 +745,7 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded features generator)",
             "config": {"workload": W["name"], "n_points": n, "n_dim": W["d"], "radius_cutoff": W["radius_cutoff"],
-                       "cnn_cutoff": W["cnn_cutoff"]},
+                       "cnn_cutoff": W["cnn_cutoff"], "fpmode": fpmode_name()},
             "cpu_baseline": {"value": rows_per_s, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": base["sample"] + f"; scaled to {cores} threads; neighbour search only "
                                        "(an upper bound on the fit rate)"},
@@ -567,7 +770,7 @@ def run_reference(args):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean_s * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": f"synthetic (seeded {WORKLOAD['gen'][0]} generator)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": f"synthetic (seeded {W['gen'][0]} generator)",
         "config": {"workload": W["name"], "n_points": n, "n_dim": W["d"], "radius_cutoff": W["radius_cutoff"],
                    "cnn_cutoff": W["cnn_cutoff"], "member_cutoff": W["member_cutoff"], "fpmode": fpmode_name()},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
@@ -585,19 +788,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="md3d-200k", choices=sorted(WORKLOADS))
+    ap.add_argument("--headline-only", action="store_true", help="skip the other workloads' sub-records")
+    ap.add_argument("--workload", default=None, choices=sorted(WORKLOADS),
+                    help="run this workload alone as the only line (default: the headline plus sub-records)")
     ap.add_argument("--slots", type=int, default=4, help="concurrent jobs of the served stream")
     args = ap.parse_args()
-    global WORKLOAD
-    WORKLOAD = WORKLOADS[args.workload]
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
-    elif WORKLOAD.get("kind") == "sweep":
-        run_sweep(args)
-    elif WORKLOAD.get("kind") == "serve":
-        run_serve(args)
     else:
         run_gpu(args)
 

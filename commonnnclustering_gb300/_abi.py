@@ -35,6 +35,10 @@ DTYPE_F64 = 0
 DTYPE_F32 = 1
 MEM_HOST = 0
 MEM_DEVICE = 1
+SEARCH_AUTO = 0
+SEARCH_GRID = 1
+SEARCH_ALL_PAIRS = 2
+SEARCH_TENSOR = 3
 
 
 def host_fpmode(fpmode: Optional[int] = None) -> int:
@@ -93,6 +97,7 @@ SIGNATURES = {
     "cnn_set_timing": (_INT, [_P, _INT]),
     "cnn_get_stats": (_INT, [_P, ctypes.POINTER(cnn_stats)]),
     "cnn_set_wait_limit": (_INT, [_P, _I64]),
+    "cnn_set_search": (_INT, [_P, _INT]),
     "cnn_set_points": (_INT, [_P, _P, _INT, _I64, _I32, _INT]),
     "cnn_build_neighbours": (_INT, [_P, ctypes.c_double, _INT, _INT]),
     "cnn_set_neighbours": (_INT, [_P, _P, _P, _I64, _INT]),
@@ -238,6 +243,11 @@ class Context:
 
     def set_timing(self, enabled: bool):
         self._check(self._lib.cnn_set_timing(self._h, 1 if enabled else 0), "cnn_set_timing")
+
+    def set_search(self, search: int):
+        """Search preference of the following builds (SEARCH_AUTO,
+        SEARCH_GRID, SEARCH_ALL_PAIRS, SEARCH_TENSOR); same neighbour sets."""
+        self._check(self._lib.cnn_set_search(self._h, int(search)), "cnn_set_search")
 
     def set_wait_limit(self, limit_ns: int):
         """Limit of the kernels' bounded waits (ns); <= 0: the default 2 s."""

@@ -192,6 +192,13 @@ CNN_API cnn_status cnn_set_wait_limit(cnn_context *ctx, int64_t limit_ns) {
     return CNN_OK;
 }
 
+CNN_API cnn_status cnn_set_search(cnn_context *ctx, cnn_search search) {
+    if (!ctx) return CNN_ERR_INVALID_ARG;
+    if (search < CNN_SEARCH_AUTO || search > CNN_SEARCH_TENSOR) return ctx->fail(CNN_ERR_INVALID_ARG, "bad search");
+    ctx->search_pref = search;
+    return CNN_OK;
+}
+
 CNN_API cnn_status cnn_get_stats(const cnn_context *cctx, cnn_stats *out) {
     cnn_context *ctx = const_cast<cnn_context *>(cctx);
     if (!ctx || !out) return CNN_ERR_INVALID_ARG;

@@ -69,6 +69,7 @@ struct cnn_context {
     bool timing = false;
     int poison = -1;  // >= 0: fill every new workspace allocation with this byte (CNN_DEBUG_POISON)
     int64_t wait_limit_ns = 0;  // > 0: limit of the bounded waits in the kernels (cnn_set_wait_limit)
+    int search_pref = CNN_SEARCH_AUTO;  // cnn_set_search
     int64_t n_launches = 0;
     std::string last_error;
     cnn_stats stats{};

@@ -805,7 +805,8 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         sp.bf = bf_dev;
     }
 
-    if (d >= 16 && radius_ok && !periodic) {
+    const bool all_pairs = ctx->search_pref == CNN_SEARCH_ALL_PAIRS;
+    if (d >= 16 && radius_ok && !periodic && !all_pairs) {
         // tensor-core Gram search; declines (used = false) for non-finite
         // data or when the float64 band would hold too many pairs
         bool used = false;
@@ -875,7 +876,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
 
     // ---- choose the search
     GridGeom geo{};
-    bool use_grid = d <= 3 && radius_ok && R > 0 && isfinite(R) && !periodic;
+    bool use_grid = d <= 3 && radius_ok && R > 0 && isfinite(R) && !periodic && !all_pairs;
     if (use_grid) {
         double h = R * (1.0 + 1e-6);
         // cells cost 12 bytes each (count + start); allow up to 64 per point

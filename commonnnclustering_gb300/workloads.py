@@ -93,52 +93,58 @@ def mixture(n: int, d: int, n_components: int, seed: int, noise: float = 0.05) -
     return np.ascontiguousarray(x[rng.permutation(n)], dtype=np.float64)
 
 
-def degree_radius(x: np.ndarray, degree: float, seed: int = 0, queries: int = 128) -> float:
-    """Radius giving about `degree` neighbours per point (sampled estimate)."""
+def degree_radius(x: np.ndarray, degree, seed: int = 0, queries: int = 96, max_sample: int = 10000):
+    """Radius giving about `degree` neighbours per point (sampled estimate).
+
+    ``degree`` may be a sequence: then one radius per target, from one set
+    of sampled squared distances."""
+    many = np.ndim(degree) > 0
+    degrees = np.atleast_1d(np.asarray(degree, dtype=np.float64))
     rng = np.random.default_rng(seed)
     n = x.shape[0]
-    m = min(n, 20000)
+    m = min(n, max_sample)
     sample = x[rng.choice(n, m, replace=False)] if m < n else x
     q = x[rng.choice(n, min(queries, n), replace=False)]
-    k = max(2, int(round(degree * m / n)))
     d2 = (q * q).sum(1)[:, None] + (sample * sample).sum(1)[None] - 2.0 * q @ sample.T
-    kth = np.sort(d2, axis=1)[:, min(k, m - 1)]
-    r = float(np.sqrt(max(np.median(kth), 1e-12)))
-    if k > degree * m / n:  # the sample was too small for the target: shrink by volume
-        r *= (degree * m / n / k) ** (1.0 / x.shape[1])
-    return r
+    ks = [max(2, int(round(deg * m / n))) for deg in degrees]
+    kth = np.partition(d2, sorted({min(k, m - 1) for k in ks}), axis=1)
+    out = []
+    for deg, k in zip(degrees, ks):
+        r = float(np.sqrt(max(np.median(kth[:, min(k, m - 1)]), 1e-12)))
+        if k > deg * m / n:  # the sample was too small for the target: shrink by volume
+            r *= (deg * m / n / k) ** (1.0 / x.shape[1])
+        out.append(r)
+    return out if many else out[0]
 
 
-def job_stream(n_jobs: int = 2000, rate: float = 100.0, seed: int = 11, pool: int = 48,
-               max_points_tensor: int = 300_000):
+def job_stream(n_jobs: int = 2000, rate: float = 100.0, seed: int = 11, pool=None, max_points=2_000_000):
     """Served workload: Poisson arrivals of clustering jobs.
 
-    Point counts lognormal (median 20k, sigma 1.2) clipped to [1k, 2M]
-    (to `max_points_tensor` for d >= 16, which bounds the all-pairs tensor
-    work per job); d from {2, 3, 16, 64}; 5-200 Gaussian components + 5 %
-    uniform noise; a radius tuned for a mean degree in [50, 300];
-    cnn_cutoff in [3, 50]; member_cutoff 10.  Jobs draw their points from
-    a pool of `pool` generated datasets (generation is the host's cost,
-    not the server's) and their own degree target and cnn_cutoff.
-    Returns a list of dicts: arrival, points, radius_cutoff, cnn_cutoff,
-    member_cutoff, expected_degree.
+    Point counts lognormal (median 20k, sigma 1.2) clipped to [1k,
+    max_points = 2M]; d from {2, 3, 16, 64}; each job its own Gaussian
+    mixture of 5-200 components + 5 % uniform noise, its own radius (tuned
+    for a mean degree drawn from [50, 300]) and cnn_cutoff in [3, 50];
+    member_cutoff 10.  ``pool``: draw the jobs' points from that many shared
+    datasets instead (faster to generate; each job keeps its own degree
+    target and cnn_cutoff).  Returns a list of dicts: arrival, points,
+    radius_cutoff, cnn_cutoff, member_cutoff, expected_degree.
     """
     rng = np.random.default_rng(seed)
-    datasets = []
-    for p in range(pool):
+
+    def dataset(k: int):
         d = int(rng.choice([2, 3, 16, 64]))
-        n = int(np.clip(np.exp(rng.normal(np.log(20000.0), 1.2)), 1000, 2_000_000))
-        if d >= 16:
-            n = min(n, max_points_tensor)
-        k = int(rng.integers(5, 201))
-        x = mixture(n, d, k, seed=seed * 1000 + p)
-        radii = {deg: degree_radius(x, deg, seed=p) for deg in (50, 100, 200, 300)}
-        datasets.append((x, radii))
+        n = int(np.clip(np.exp(rng.normal(np.log(20000.0), 1.2)), 1000, max_points))
+        comps = int(rng.integers(5, 201))
+        x = mixture(n, d, comps, seed=seed * 100003 + k)
+        radii = dict(zip((50, 100, 200, 300), degree_radius(x, (50, 100, 200, 300), seed=k)))
+        return x, radii
+
+    datasets = [dataset(p) for p in range(pool)] if pool else None
     t = 0.0
     jobs = []
     for i in range(n_jobs):
         t += rng.exponential(1.0 / rate)
-        x, radii = datasets[int(rng.integers(0, pool))]
+        x, radii = datasets[int(rng.integers(0, pool))] if pool else dataset(i)
         deg = float(rng.uniform(50, 300))
         keys = sorted(radii)
         r = float(np.interp(deg, keys, [radii[k] for k in keys]))

@@ -132,6 +132,20 @@ typedef struct cnn_stats {
 
 CNN_API int cnn_abi_version(void);
 
+/* Which neighbour search cnn_build_neighbours runs (a preference: a search
+ * that does not apply to the points or the metric falls back to the
+ * automatic choice).  AUTO: cell grid for n_dim <= 3, tensor-core Gram
+ * search for n_dim >= 16, tiled all-pairs float32 otherwise; ALL_PAIRS: the
+ * tiled all-pairs float32 search with the float64 band for any n_dim (the
+ * plain GPU path the others are measured against).  The neighbour sets are
+ * the same whichever runs. */
+typedef enum cnn_search {
+    CNN_SEARCH_AUTO = 0,
+    CNN_SEARCH_GRID = 1,
+    CNN_SEARCH_ALL_PAIRS = 2,
+    CNN_SEARCH_TENSOR = 3
+} cnn_search;
+
 /* Create a context on `device`.  `stream` is a cudaStream_t (may be NULL:
  * the context creates its own non-blocking stream). */
 CNN_API cnn_status cnn_create(cnn_context **out, int device, void *stream);
@@ -148,6 +162,11 @@ CNN_API cnn_status cnn_get_stats(const cnn_context *ctx, cnn_stats *out);
  * CNN_ERR_TIMEOUT; the context stays usable.  No reference counterpart: a
  * testing and watchdog knob. */
 CNN_API cnn_status cnn_set_wait_limit(cnn_context *ctx, int64_t limit_ns);
+
+/* The search preference of the following cnn_build_neighbours calls (see
+ * cnn_search); no reference counterpart: the reference has one brute-force
+ * getter. */
+CNN_API cnn_status cnn_set_search(cnn_context *ctx, cnn_search search);
 
 /* Points, row-major [n_points x n_dim].  Device arrays are used in place
  * (they must stay alive and unchanged until the next cnn_set_points);

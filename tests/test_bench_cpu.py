@@ -17,11 +17,10 @@ def stats(**ms):
     return base
 
 
-def test_hbm_entry_takes_the_slowest_stage(bench, monkeypatch):
-    monkeypatch.setattr(bench, "WORKLOAD", bench.WORKLOADS["md3d-200k"])
+def test_hbm_entry_takes_the_slowest_stage(bench):
     n, nnz = 200_000, 43_000_000
     s = [stats(ms_count=0.30, ms_check=0.35, ms_fill=0.08), stats(ms_count=0.32, ms_check=0.33, ms_fill=0.08)]
-    e = bench.roofline_entry(s, nnz, n, {"hbm_gbs": 7000.0})
+    e = bench.hbm_roofline(s, nnz, n, {"hbm_gbs": 7000.0})
     assert e["bound"] == "hbm" and e["unit"] == "GB/s" and e["kernel"] == "check_union_kernel"
     assert e["ms_per_launch"] == pytest.approx(0.34)
     want_bytes = 4 * nnz + 8 * (n + 1) + n + 8 * n
@@ -31,12 +30,19 @@ def test_hbm_entry_takes_the_slowest_stage(bench, monkeypatch):
     assert set(e) >= {"bound", "achieved", "peak", "unit", "frac", "traffic"}
 
 
-def test_tensor_entry_counts_the_issued_mmas(bench, monkeypatch):
-    monkeypatch.setattr(bench, "WORKLOAD", bench.WORKLOADS["features-500k-d64"])
+def test_tensor_entry_counts_the_issued_mmas(bench):
     s = [stats(ms_gram=2.0, ms_count=5.0)]
-    e = bench.roofline_entry(s, 1000, 500_000, {"bf16_tflops": 2000.0})
+    e = bench.tensor_roofline(bench.WORKLOADS["features-500k-d64"], s, 500_000, {"bf16_tflops": 2000.0})
     useful = 2.0 * (1 << 20) * 64
     assert e["bound"] == "tensor" and e["unit"] == "TFLOP/s"
     assert e["algorithmic_flops_issued"] == pytest.approx(6 * useful)
     assert e["achieved"] == pytest.approx(6 * useful / 2.0e-3 / 1e12)
     assert e["frac"] == pytest.approx(e["achieved"] / 2000.0)
+
+
+def test_default_run_covers_every_workload(bench):
+    """The driver's default invocation measures the headline and the four
+    other workloads (sub-records of the same JSON line)."""
+    assert bench.HEADLINE == "md3d-200k"
+    names = {bench.WORKLOADS[w]["name"] for w in bench.SUB_WORKLOADS}
+    assert names == {"blobs2d-5k", "features-500k-d64", "nested3d-1m-sweep", "serve-stream"}

@@ -305,3 +305,22 @@ def test_tensor_core_wait_timeout_stops_cleanly(cnn, oracle):
         off, idx = ctx.get_neighbours(x.shape[0])
         assert np.array_equal(off, want[0]) and np.array_equal(idx, want[1])
     ctx.close()
+
+
+def test_search_preference_changes_the_search_not_the_sets(cnn, oracle):
+    """SEARCH_ALL_PAIRS (the plain float32 all-pairs search) and the
+    automatic choice (tensor cores at n_dim 16, the cell grid at 3) give the
+    oracle's neighbour sets."""
+    from commonnnclustering_gb300 import _abi, workloads
+    for x, r2, auto_kind in ((workloads.features(n=6000, d=16, seed=35, n_clusters=6), 1.6 ** 2, 3),
+                             (workloads.md3d(n=20000, seed=5, centre_spread=2.0), 0.1 ** 2, 1)):
+        want = oracle.neighbourhoods(x, r2, grid=x.shape[1] <= 3)
+        ctx = cnn.Context(0)
+        ctx.set_points(x)
+        for pref, kind in ((_abi.SEARCH_ALL_PAIRS, 2), (_abi.SEARCH_AUTO, auto_kind)):
+            ctx.set_search(pref)
+            ctx.build_neighbours(r2)
+            assert ctx.stats()["search_kind"] == kind
+            off, idx = ctx.get_neighbours(x.shape[0])
+            assert np.array_equal(off, want[0]) and np.array_equal(idx, want[1])
+        ctx.close()

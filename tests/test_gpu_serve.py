@@ -16,7 +16,7 @@ def serve():
 
 def make_jobs(serve_mod, n_jobs, rate, seed):
     from commonnnclustering_gb300 import workloads
-    raw = workloads.job_stream(n_jobs=n_jobs, rate=rate, seed=seed, pool=8, max_points_tensor=30000)
+    raw = workloads.job_stream(n_jobs=n_jobs, rate=rate, seed=seed, pool=8, max_points=30000)
     return [serve_mod.Job(job_id=i, **j) for i, j in enumerate(raw)]
 
 

@@ -50,8 +50,7 @@ def reference_rank_main(rank, world, port, out):
     os.environ.update({"RANK": str(rank), "WORLD_SIZE": str(world), "LOCAL_RANK": str(rank),
                        "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
     import bench
-    bench.WORKLOAD = bench.WORKLOADS["blobs2d-5k"]
-    args = type("A", (), {"steps": 1, "warmup": 0})()
+    args = type("A", (), {"steps": 1, "warmup": 0, "workload": "blobs2d-5k"})()
     buf = io.StringIO()
     with contextlib.redirect_stdout(buf):
         bench.run_reference(args)
