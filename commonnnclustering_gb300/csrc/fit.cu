@@ -379,7 +379,11 @@ __global__ void new_label_kernel(const uint64_t *__restrict__ keys, int64_t k, i
 // One pass counts sizes and first occurrences per label value (lo..lo+r-1);
 // one kernel ranks the clusters by (size descending, first occurrence
 // ascending) and writes the new label of every value; one pass applies it.
-constexpr int kOrderSmall = 4096;
+// The ranking block holds all r keys in shared memory (8 bytes each), so r
+// is bounded by the shared memory of a block.
+constexpr int kOrderSmall = 24576;
+constexpr int kOrderThreads = 1024;
+constexpr int kOrderPerBlock = 256;  // values ranked per block (8 per warp)
 
 __global__ void init_count_first_kernel(int32_t *__restrict__ cnt, int32_t *__restrict__ first, int64_t r) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < r; i += (int64_t)gridDim.x * blockDim.x) {
@@ -408,41 +412,40 @@ __global__ void count_first_dense_kernel(const int64_t *__restrict__ labels, int
 
 // New label of every value: its rank among the used values' keys (size
 // descending, first occurrence ascending; distinct per value).  Every block
-// holds all keys in shared memory; one warp per value counts the keys below
-// its own (the lanes stride over the keys).
-constexpr int kOrderWarps = 8;
-
-__global__ void __launch_bounds__(kOrderWarps * 32) order_small_kernel(
+// holds all keys in shared memory; each warp ranks its values in turn, the
+// lanes striding over the keys.
+__global__ void __launch_bounds__(kOrderThreads) order_small_kernel(
     const int32_t *__restrict__ cnt, const int32_t *__restrict__ first, int r, int64_t n, int bits_n,
     int64_t member_cutoff, int64_t max_clusters, int64_t *__restrict__ newlab) {
-    __shared__ uint64_t s[kOrderSmall];
+    extern __shared__ uint64_t s_keys[];  // [r]
     __shared__ int s_k;
     if (threadIdx.x == 0) s_k = 0;
     __syncthreads();
     int local = 0;
     for (int i = threadIdx.x; i < r; i += blockDim.x) {
         const bool used = cnt[i] > 0;
-        s[i] = used ? (((uint64_t)(n - cnt[i]) << bits_n) | (uint64_t)first[i]) : ~0ull;
+        s_keys[i] = used ? (((uint64_t)(n - cnt[i]) << bits_n) | (uint64_t)first[i]) : ~0ull;
         local += used;
     }
     for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
     if ((threadIdx.x & 31) == 0 && local) atomicAdd(&s_k, local);
     __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int i = blockIdx.x * kOrderWarps + (threadIdx.x >> 5);
-    if (i >= r) return;
-    const uint64_t key = s[i];
-    int below = 0;
-    for (int j = lane; j < r; j += 32) below += s[j] < key;
-    below = __reduce_add_sync(0xffffffffu, below);
-    if (lane != 0) return;
-    if (key == ~0ull) {  // value not used
-        newlab[i] = 0;
-        return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int v_end = min(r, (int)(blockIdx.x + 1) * kOrderPerBlock);
+    for (int i = (int)blockIdx.x * kOrderPerBlock + warp; i < v_end; i += nwarps) {
+        const uint64_t key = s_keys[i];
+        int below = 0;
+        for (int j = lane; j < r; j += 32) below += s_keys[j] < key;
+        below = __reduce_add_sync(0xffffffffu, below);
+        if (lane != 0) continue;
+        if (key == ~0ull) {  // value not used
+            newlab[i] = 0;
+            continue;
+        }
+        const int64_t maxc = max_clusters < 0 ? s_k : max_clusters;
+        const int64_t rank = below + 1;  // cluster_count in the reference loop
+        newlab[i] = rank > maxc ? 0 : ((int64_t)cnt[i] >= member_cutoff ? rank : 0);
     }
-    const int64_t maxc = max_clusters < 0 ? s_k : max_clusters;
-    const int64_t rank = below + 1;  // cluster_count in the reference loop
-    newlab[i] = rank > maxc ? 0 : ((int64_t)cnt[i] >= member_cutoff ? rank : 0);
 }
 
 __global__ void apply_dense_kernel(int64_t *__restrict__ labels, int64_t n, int64_t lo,
@@ -647,7 +650,9 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64
         CNN_LAUNCH_CHECK(ctx);
         count_first_dense_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(labels, n, lo, cnt, first);
         CNN_LAUNCH_CHECK(ctx);
-        order_small_kernel<<<(unsigned)((r + kOrderWarps - 1) / kOrderWarps), kOrderWarps * 32, 0, st>>>(
+        const size_t keys_smem = sizeof(uint64_t) * (size_t)r;
+        CNN_TRY(allow_dynamic_smem(ctx, (const void *)order_small_kernel, keys_smem));
+        order_small_kernel<<<(unsigned)((r + kOrderPerBlock - 1) / kOrderPerBlock), kOrderThreads, keys_smem, st>>>(
             cnt, first, r, n, bits_for_fit(n), member_cutoff, max_clusters, newlab);
         CNN_LAUNCH_CHECK(ctx);
         apply_dense_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(labels, n, lo, newlab);

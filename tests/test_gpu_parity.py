@@ -324,3 +324,22 @@ def test_search_preference_changes_the_search_not_the_sets(cnn, oracle):
             off, idx = ctx.get_neighbours(x.shape[0])
             assert np.array_equal(off, want[0]) and np.array_equal(idx, want[1])
         ctx.close()
+
+
+@pytest.mark.parametrize("n_values,span", [(3000, 1), (20000, 1), (24576, 1), (40000, 1), (5000, 1000)])
+def test_sort_by_size_many_label_values(cnn, oracle, n_values, span):
+    """sort_by_size over label ranges on both sides of the one-block ranking
+    (<= 24,576 values) and sparse label values (a span far above n)."""
+    rng = np.random.default_rng(n_values)
+    n = 200_000
+    values = (np.arange(1, n_values + 1, dtype=np.int64) * span)
+    sizes = rng.zipf(1.6, size=n_values).clip(1, 500)
+    lab = np.repeat(values, sizes)[:n]
+    lab = np.concatenate([lab, np.zeros(max(0, n - lab.shape[0]), dtype=np.int64)])
+    lab = lab[rng.permutation(lab.shape[0])]
+    for mc, mx in ((2, None), (5, 100), (1, None)):
+        want = lab.copy()
+        oracle.sort_by_size(want, mc, mx)
+        got = cnn.Labels(lab.copy())
+        got.sort_by_size(mc, mx)
+        assert np.array_equal(np.asarray(got.labels), want), (mc, mx)
