@@ -90,6 +90,7 @@ CNN_API cnn_status cnn_create(cnn_context **out, int device, void *stream) {
     if (!ctx) return CNN_ERR_OOM;
     ctx->device = device;
     if (const char *pz = getenv("CNN_DEBUG_POISON")) ctx->poison = atoi(pz) & 0xff;
+    if (const char *gf = getenv("CNN_GRAPH_FORM")) ctx->allow_mask = strcmp(gf, "lists") != 0;
     int sms = 0;
     if (cudaSetDevice(device) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1) {
@@ -142,6 +143,7 @@ CNN_API cnn_status cnn_destroy(cnn_context *ctx) {
                            &ctx->sweep_multi_deg, &ctx->sweep_multi_off, &ctx->sweep_multi_cols, &ctx->sweep_multi_base,
                            &ctx->sweep_open_b, &ctx->sweep_open_count,
                            &ctx->stage_consider, &ctx->stage_offsets, &ctx->stage_indices, &ctx->stage_misc,
+                           &ctx->pcell, &ctx->mbase, &ctx->masks, &ctx->dist_own, &ctx->bounds_dev,
                            &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->scratch_a, &ctx->scratch_b,
                            &ctx->scratch_c, &ctx->scratch_d, &ctx->scan_tmp};
     for (cnn::DevBuf *b : bufs)
@@ -315,7 +317,7 @@ CNN_API cnn_status cnn_build_neighbours(cnn_context *ctx, double radius_cutoff, 
     if (!metric_known(metric)) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown metric");
     if (fpmode != CNN_FP_SEPARATE && fpmode != CNN_FP_FUSED) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown fpmode");
     CNN_TRY(check_source(ctx, metric));
-    return build_neighbours_impl(ctx, radius_cutoff, metric, fpmode);
+    return build_neighbours_impl(ctx, radius_cutoff, metric, fpmode, /*want_mask=*/true);
 }
 
 CNN_API cnn_status cnn_set_neighbours(cnn_context *ctx, const int64_t *offsets, const int32_t *indices,
@@ -390,7 +392,10 @@ CNN_API cnn_status cnn_fit(cnn_context *ctx, int64_t similarity_cutoff, int64_t 
         cons_dev = const_cast<uint8_t *>(c_in);
         lab_dev = const_cast<int64_t *>(l_in);
     }
-    CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
+    if (ctx->graph_mask)
+        CNN_TRY(fit_mask_impl(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
+    else
+        CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
     if (mem == CNN_MEM_HOST && n > 0) {
         CNN_CUDA(ctx, cudaMemcpyAsync(labels, lab_dev, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
         CNN_CUDA(ctx, cudaMemcpyAsync(consider, cons_dev, (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));

@@ -53,6 +53,28 @@ struct DevBuf {
     template <typename T> T *as() const { return static_cast<T *>(ptr); }
 };
 
+// Cell grid of the d <= 3 search: cubic cells of edge h >= R, internal
+// order = points grouped by cell id (x fastest).
+struct GridGeom {
+    double lo[3];
+    double h;
+    double inv_h;      // 1 / h, rounded: cell coordinates are a monotone function of x
+    int32_t g[3];      // cells per dimension (1 for unused dimensions)
+    int64_t ncells;    // g0*g1*g2; bucket ncells holds non-finite points
+};
+
+// The cell-grid neighbour graph as bit masks (fit_mask.cu): a point of cell
+// c owns ceil(T_c / 32) words, one bit per candidate of the cell's candidate
+// sequence (the 9 runs of its 3 x 3 x 3 stencil, ascending), set for a
+// neighbour.  Kernel argument.
+struct MaskGraph {
+    const int64_t *cell_start;  // [ncells + 2] first internal index of each cell
+    const int32_t *pcell;       // [n] internal index -> cell
+    const int64_t *mbase;       // [ncells + 1] word offset of each cell's first row
+    const uint32_t *masks;      // the rows (+ one padding word at the end)
+    int32_t g0, g1, g2;         // cells per dimension
+};
+
 // Stage timer: CUDA events on the context stream.
 struct StageTimer {
     cudaEvent_t a = nullptr, b = nullptr;
@@ -120,6 +142,15 @@ struct cnn_context {
 
     // extents (max - min of finite points) per dimension of the last grid search
     double grid_extent[3] = {0.0, 0.0, 0.0};
+
+    // the graph in mask form (cell-grid searches of cnn_build_neighbours):
+    // graph_mask = the masks hold the graph; csr_valid = row_off/cols hold it
+    // too (built from the masks when a caller needs the lists)
+    bool graph_mask = false;
+    bool csr_valid = true;
+    bool allow_mask = true;  // CNN_GRAPH_FORM=lists at creation: always lists
+    cnn::GridGeom mask_geo{};
+    cnn::DevBuf pcell, mbase, masks;
 
     // batched (radius, cut) sweep: the largest-radius graph kept aside,
     // per-pair radius buckets, consider flags of the per-fit runs
@@ -204,7 +235,12 @@ cnn_status fill_i32(cnn_context *ctx, int32_t *p, int64_t n, int32_t v);
 cnn_status iota_i32(cnn_context *ctx, int32_t *p, int64_t n);
 
 // search.cu
-cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode);
+// want_mask: a cell-grid search stores the graph as masks (fit_mask.cu);
+// callers that walk the lists themselves pass false
+cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode,
+                                 bool want_mask = false);
+// row_off/cols of the current graph (materialised from the masks if needed)
+cnn_status ensure_lists(cnn_context *ctx);
 cnn_status export_neighbours_impl(cnn_context *ctx, int64_t *offsets_dev, int32_t *indices_dev);
 cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev,
                                const int32_t *indices_dev, int64_t n);
@@ -226,6 +262,12 @@ cnn_status mst_prim_impl(cnn_context *ctx, double radius_cutoff, int metric, int
 
 // gram.cu: tensor-core search (n_dim >= 16); *used = false when it declined
 cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode, bool *used);
+
+// fit_mask.cu: cnn_fit over the mask form
+cnn_status fit_mask_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
+                         int64_t current_start, uint8_t *consider_dev, int64_t *labels_dev);
+// lists from the masks: cols[row_off[p] ..] = the set bits of p's row, ascending
+cnn_status masks_to_lists(cnn_context *ctx);
 
 // fit.cu
 // seed_a / seed_b (optional, internal order): per point a node of a finished

@@ -501,6 +501,7 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
                     uint8_t *consider_dev, int64_t *labels_dev, const int32_t *seed_a, const int32_t *seed_b,
                     const int2 *edge_list, const unsigned long long *edge_count) {
     if (!ctx->have_graph) return ctx->fail(CNN_ERR_STATE, "no neighbour graph: call cnn_build_neighbours first");
+    CNN_TRY(ensure_lists(ctx));
     const int64_t n = ctx->n;
     cudaStream_t st = ctx->stream;
     ctx->fit_stats_pending = false;
@@ -748,6 +749,7 @@ cnn_status fit_and_sort_into(cnn_context *ctx, int64_t similarity_cutoff, int64_
 // the list that fit used; out_count is a device counter.
 cnn_status open_pairs_impl(cnn_context *ctx, const int2 *in_list, const unsigned long long *in_count, int2 *out,
                            unsigned long long *out_count, int64_t cap) {
+    CNN_TRY(ensure_lists(ctx));
     cudaStream_t st = ctx->stream;
     const int64_t n = ctx->n;
     CNN_CUDA(ctx, cudaMemsetAsync(out_count, 0, sizeof(unsigned long long), st));

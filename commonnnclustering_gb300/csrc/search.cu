@@ -128,14 +128,7 @@ __global__ void extent_partial_kernel(const double *__restrict__ x, int64_t n, i
     }
 }
 
-// ---- grid construction ---------------------------------------------------
-struct GridGeom {
-    double lo[3];
-    double h;
-    double inv_h;      // 1 / h, rounded: cell coordinates are a monotone function of x
-    int32_t g[3];      // cells per dimension (1 for unused dimensions)
-    int64_t ncells;    // g0*g1*g2; bucket ncells holds non-finite points
-};
+// ---- grid construction (GridGeom: common.cuh) -------------------------------
 
 // floor((v - lo) / h) with the quotient taken as a product by the rounded
 // reciprocal: still monotone in v, and two values less than R apart land in
@@ -176,11 +169,13 @@ __global__ void cell_assign_kernel(const double *__restrict__ x, int64_t n, int 
 __global__ void place_kernel(const int32_t *__restrict__ cell_of, const int32_t *__restrict__ slot,
                              const int64_t *__restrict__ cell_start, int64_t n, const double *__restrict__ x, int d,
                              GridGeom geo, int32_t *__restrict__ perm, int32_t *__restrict__ inv,
-                             float4 *__restrict__ xf4) {
+                             float4 *__restrict__ xf4, int32_t *__restrict__ pcell) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t p = (int32_t)(cell_start[cell_of[i]] + slot[i]);
+        const int32_t c = cell_of[i];
+        const int32_t p = (int32_t)(cell_start[c] + slot[i]);
         perm[p] = (int32_t)i;
         inv[i] = p;
+        if (pcell) pcell[p] = c;
         float v[3] = {0.f, 0.f, 0.f};
         for (int k = 0; k < d; ++k) v[k] = (float)__dsub_rn(x[i * d + k], geo.lo[k]);
         xf4[p] = make_float4(v[0], v[1], v[2], 0.f);
@@ -240,13 +235,16 @@ __device__ __forceinline__ int64_t cell_candidates(int64_t cid, const GridGeom &
     return total;
 }
 
-// slots of a cell = its points x its candidate count (upper bound of every row)
+// slots of a cell = its points x its candidate count (upper bound of every
+// row); kWords: its points x the 32-bit words of one mask row
+template <bool kWords>
 __global__ void cell_slots_kernel(const int64_t *__restrict__ cell_start, GridGeom geo,
                                   int64_t *__restrict__ slots) {
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < geo.ncells;
          c += (int64_t)gridDim.x * blockDim.x) {
         const int64_t q = cell_start[c + 1] - cell_start[c];
-        slots[c] = q > 0 ? q * cell_candidates(c, geo, cell_start) : 0;
+        const int64_t t = q > 0 ? cell_candidates(c, geo, cell_start) : 0;
+        slots[c] = q * (kWords ? (t + 31) / 32 : t);
     }
 }
 
@@ -266,8 +264,10 @@ __global__ void compact_rows_kernel(int64_t n, const int64_t *__restrict__ qslot
 // each query's row into its slot (slot_base[cell] + rank in cell x the
 // cell's candidate count, an upper bound of the row), its length to deg
 // and the slot start to qslot -- one pass instead of count + fill when the
-// slots fit in memory.
-constexpr int kCount = 0, kFill = 1, kSlots = 2;
+// slots fit in memory; kMask writes each query's row as bits, one 32-bit
+// word (the step's ballot) per 32 candidates, at mbase[cell] + rank in cell
+// x the words of the cell's rows, and its length to deg.
+constexpr int kCount = 0, kFill = 1, kSlots = 2, kMask = 3;
 
 // ---- warp-granular grid search ---------------------------------------------
 // Work unit = (cell, up to kUnitQueries consecutive queries of that cell), one
@@ -344,7 +344,8 @@ __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_uni
     float qx[kUnitQueries], qy[kUnitQueries], qz[kUnitQueries];
     int32_t *rowp[kUnitQueries];
     int32_t cnt[kUnitQueries];
-    const int64_t slot0 = kMode == kSlots ? row_off[cid] + (q0 - cs) * (int64_t)total : 0;
+    const int64_t row_len = kMode == kMask ? (int64_t)((total + 31) >> 5) : (int64_t)total;  // slot of one row
+    const int64_t slot0 = (kMode == kSlots || kMode == kMask) ? row_off[cid] + (q0 - cs) * row_len : 0;
 #pragma unroll
     for (int k = 0; k < kUnitQueries; ++k) {
         const int64_t qk = q0 + k;
@@ -354,7 +355,7 @@ __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_uni
         qy[k] = f.y;
         qz[k] = f.z;
         qi[k] = ok ? (int32_t)qk : -1;
-        const int64_t w = kMode == kFill ? (ok ? row_off[qk] : 0) : slot0 + k * (int64_t)total;
+        const int64_t w = kMode == kFill ? (ok ? row_off[qk] : 0) : slot0 + k * row_len;
         rowp[k] = kMode == kCount ? nullptr : cols + w;
         if (kMode == kSlots && ok && lane == 0) qslot[qk] = w;
         cnt[k] = 0;
@@ -411,7 +412,11 @@ __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_uni
         for (int k = 0; k < kUnitQueries; ++k) {
 #pragma unroll
             for (int u = 0; u < kUnitSub; ++u) {  // step u's candidates follow step u - 1's
-                if (kMode != kCount) {
+                if (kMode == kMask) {
+                    const unsigned hit = __ballot_sync(0xffffffffu, in[u][k]);
+                    if (lane == k && qi[k] >= 0) rowp[k][((t0 - lane) >> 5) + u] = (int32_t)hit;
+                    cnt[k] += __popc(hit);
+                } else if (kMode != kCount) {
                     const unsigned hit = __ballot_sync(0xffffffffu, in[u][k]);
                     if (in[u][k]) rowp[k][cnt[k] + __popc(hit & lt)] = j[u];
                     cnt[k] += __popc(hit);
@@ -434,6 +439,12 @@ __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_uni
         }
         for (int o = 16; o > 0; o >>= 1) n_exact += __shfl_down_sync(0xffffffffu, n_exact, o);
         if (lane == 0 && n_exact) atomicAdd(&counters[0], n_exact);
+        if (kMode == kMask && lane == 0) {  // candidate pairs looked at (statistics)
+            unsigned long long q = 0;
+#pragma unroll
+            for (int k = 0; k < kUnitQueries; ++k) q += qi[k] >= 0 ? 1 : 0;
+            atomicAdd(&counters[1], q * (unsigned long long)total);
+        }
     }
 }
 
@@ -713,11 +724,13 @@ bool filter_thresholds(const std::vector<double> &ext, double R, double rc2, flo
 }  // namespace
 
 // ---------------------------------------------------------------------------
-cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode) {
+cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode, bool want_mask) {
     const int64_t n = ctx->n;
     const int d = ctx->d;
     cudaStream_t st = ctx->stream;
     ctx->have_graph = false;
+    ctx->graph_mask = false;
+    ctx->csr_valid = true;
     ++ctx->graph_generation;
     ctx->stats = cnn_stats{};
     ctx->search_stats_pending = false;
@@ -905,6 +918,8 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     int64_t grid_items = 0;
     int64_t n_candidates = -1;  // pairs looked at (grid path: from the slot sizes)
     bool use_slots = false;
+    // the mask form: the rows as bits of the cells' candidate sequences
+    const bool use_mask = use_grid && want_mask && ctx->allow_mask;
     unsigned long long *counters = ctx->counters.as<unsigned long long>();
 
     if (use_grid) {
@@ -921,9 +936,10 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         cell_assign_kernel<<<gb, 256, 0, st>>>(ctx->x, n, d, geo, ctx->cell_of.as<int32_t>(), slot, cell_count);
         CNN_LAUNCH_CHECK(ctx);
         CNN_TRY(scan_exclusive_i32_to_i64(ctx, cell_count, ctx->cell_start.as<int64_t>(), geo.ncells + 2));
+        if (use_mask) CNN_TRY(ctx->ensure(ctx->pcell, sizeof(int32_t) * (size_t)n));
         place_kernel<<<gb, 256, 0, st>>>(ctx->cell_of.as<int32_t>(), slot, ctx->cell_start.as<int64_t>(), n, ctx->x, d,
                                          geo, ctx->perm.as<int32_t>(), ctx->inv.as<int32_t>(),
-                                         ctx->xf4.as<float4>());
+                                         ctx->xf4.as<float4>(), use_mask ? ctx->pcell.as<int32_t>() : nullptr);
         CNN_LAUNCH_CHECK(ctx);
 
         // work items: (cell, first query) for every 32 queries of a cell
@@ -934,13 +950,19 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         CNN_LAUNCH_CHECK(ctx);
         CNN_CUDA(ctx, cudaMemsetAsync(ctx->io_a.as<int32_t>() + geo.ncells, 0, sizeof(int32_t), st));
         CNN_TRY(scan_exclusive_i32_to_i64(ctx, ctx->io_a.as<int32_t>(), ctx->io_b.as<int64_t>(), geo.ncells + 1));
-        // slots: every row's upper bound (its cell's candidate count)
-        CNN_TRY(ctx->ensure(ctx->grid_slot_base, sizeof(int64_t) * (size_t)(geo.ncells + 2)));
-        int64_t *slot_base = ctx->grid_slot_base.as<int64_t>();
+        // slots: every row's upper bound (its cell's candidate count), or in
+        // the mask form every row's words
+        cnn::DevBuf &base_buf = use_mask ? ctx->mbase : ctx->grid_slot_base;
+        CNN_TRY(ctx->ensure(base_buf, sizeof(int64_t) * (size_t)(geo.ncells + 2)));
+        int64_t *slot_base = base_buf.as<int64_t>();
         CNN_TRY(ctx->ensure(ctx->scratch_c, sizeof(int64_t) * (size_t)(geo.ncells + 2)));
         CNN_CUDA(ctx, cudaMemsetAsync(ctx->scratch_c.as<int64_t>() + geo.ncells, 0, sizeof(int64_t), st));
-        cell_slots_kernel<<<std::min<unsigned>(grid_for(geo.ncells, 256), ctx->sm_count * 16u), 256, 0, st>>>(
-            ctx->cell_start.as<int64_t>(), geo, ctx->scratch_c.as<int64_t>());
+        if (use_mask)
+            cell_slots_kernel<true><<<std::min<unsigned>(grid_for(geo.ncells, 256), ctx->sm_count * 16u), 256, 0, st>>>(
+                ctx->cell_start.as<int64_t>(), geo, ctx->scratch_c.as<int64_t>());
+        else
+            cell_slots_kernel<false><<<std::min<unsigned>(grid_for(geo.ncells, 256), ctx->sm_count * 16u), 256, 0, st>>>(
+                ctx->cell_start.as<int64_t>(), geo, ctx->scratch_c.as<int64_t>());
         CNN_LAUNCH_CHECK(ctx);
         CNN_TRY(scan_exclusive_i64(ctx, ctx->scratch_c.as<int64_t>(), slot_base, geo.ncells + 1));
         int64_t hcounts[2] = {0, 0};
@@ -949,7 +971,12 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         CNN_TRY(read_back(ctx, hcounts, ctx->io_b.as<int64_t>() + geo.ncells, 2 * sizeof(int64_t)));
         const int64_t nitems = hcounts[0];
         // one pass into slots when they take at most 4 GiB, else count + fill
-        use_slots = hcounts[1] <= (int64_t(1) << 30);
+        use_slots = !use_mask && hcounts[1] <= (int64_t(1) << 30);
+        if (use_mask) {
+            // + 2 words: a row's last word may be read together with the next one
+            CNN_TRY(ctx->ensure(ctx->masks, sizeof(uint32_t) * (size_t)(hcounts[1] + 2)));
+            CNN_CUDA(ctx, cudaMemsetAsync(ctx->masks.as<uint32_t>() + hcounts[1], 0, 2 * sizeof(uint32_t), st));
+        }
         if (use_slots) {
             CNN_TRY(ctx->ensure(ctx->grid_slot_cols, sizeof(int32_t) * (size_t)(hcounts[1] > 0 ? hcounts[1] : 1)));
             CNN_TRY(ctx->ensure(ctx->grid_qslot, sizeof(int64_t) * (size_t)n));
@@ -963,7 +990,13 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
 
         stage_begin(ctx, 2);
         CNN_CUDA(ctx, cudaMemsetAsync(deg, 0, sizeof(int32_t) * (size_t)n, st));
-        if (nitems > 0 && use_slots) {
+        if (nitems > 0 && use_mask) {
+            grid_unit_kernel<kMask><<<(unsigned)((nitems + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
+                ctx->io_c.as<int2>(), nitems, ctx->x, d, geo, sp, ctx->perm.as<int32_t>(),
+                ctx->cell_start.as<int64_t>(), ctx->xf4.as<float4>(), deg, slot_base,
+                reinterpret_cast<int32_t *>(ctx->masks.as<uint32_t>()), counters, nullptr);
+            CNN_LAUNCH_CHECK(ctx);
+        } else if (nitems > 0 && use_slots) {
             grid_unit_kernel<kSlots><<<(unsigned)((nitems + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
                 ctx->io_c.as<int2>(), nitems, ctx->x, d, geo, sp, ctx->perm.as<int32_t>(),
                 ctx->cell_start.as<int64_t>(), ctx->xf4.as<float4>(), deg, slot_base,
@@ -975,7 +1008,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
                 ctx->cell_start.as<int64_t>(), ctx->xf4.as<float4>(), deg, nullptr, nullptr, counters, nullptr);
             CNN_LAUNCH_CHECK(ctx);
         }
-        n_candidates = hcounts[1];  // every query against its cell's candidate runs
+        n_candidates = use_mask ? -1 : hcounts[1];  // every query against its cell's candidate runs
         stage_end(ctx, 2);
         ctx->identity_perm = false;
     } else {
@@ -1010,10 +1043,15 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     int64_t nnz = 0;
     CNN_TRY(read_back(ctx, &nnz, row_off + n, sizeof(int64_t)));
     stage_end(ctx, 3);
-    CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1)));
+    if (!use_mask) CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1)));
 
     stage_begin(ctx, 4);
-    if (use_grid) {
+    if (use_mask) {
+        // the masks are the graph; lists are made from them on request
+        ctx->graph_mask = true;
+        ctx->csr_valid = false;
+        ctx->mask_geo = geo;
+    } else if (use_grid) {
         if (grid_items > 0 && use_slots) {
             compact_rows_kernel<<<std::min<unsigned>(grid_for(n * 32, 256), ctx->sm_count * 16u), 256, 0, st>>>(
                 n, ctx->grid_qslot.as<int64_t>(), ctx->grid_slot_cols.as<int32_t>(), row_off,
@@ -1052,8 +1090,17 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     return CNN_OK;
 }
 
+cnn_status ensure_lists(cnn_context *ctx) {
+    if (!ctx->have_graph || !ctx->graph_mask || ctx->csr_valid) return CNN_OK;
+    CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(ctx->nnz > 0 ? ctx->nnz : 1)));
+    CNN_TRY(masks_to_lists(ctx));
+    ctx->csr_valid = true;
+    return CNN_OK;
+}
+
 // Graph as CSR in point-index order (device output buffers).
 cnn_status export_neighbours_impl(cnn_context *ctx, int64_t *offsets_dev, int32_t *indices_dev) {
+    CNN_TRY(ensure_lists(ctx));
     const int64_t n = ctx->n, nnz = ctx->nnz;
     cudaStream_t st = ctx->stream;
     if (ctx->identity_perm) {
@@ -1184,6 +1231,8 @@ cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev, con
                                int64_t n) {
     cudaStream_t st = ctx->stream;
     ctx->have_graph = false;
+    ctx->graph_mask = false;
+    ctx->csr_valid = true;
     ++ctx->graph_generation;
     ctx->stats = cnn_stats{};
     ctx->search_stats_pending = false;
