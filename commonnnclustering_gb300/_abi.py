@@ -39,6 +39,9 @@ SEARCH_AUTO = 0
 SEARCH_GRID = 1
 SEARCH_ALL_PAIRS = 2
 SEARCH_TENSOR = 3
+INTERSECT_AUTO = 0
+INTERSECT_MERGE = 1
+INTERSECT_BITSET = 2
 
 
 def host_fpmode(fpmode: Optional[int] = None) -> int:
@@ -77,6 +80,8 @@ class cnn_stats(ctypes.Structure):
         ("ms_scan", ctypes.c_float), ("ms_fill", ctypes.c_float), ("ms_nodes", ctypes.c_float),
         ("ms_check", ctypes.c_float), ("ms_label", ctypes.c_float), ("ms_sort", ctypes.c_float),
         ("n_launches", ctypes.c_int64), ("ms_gram", ctypes.c_float), ("max_abs_err", ctypes.c_float),
+        ("intersection", ctypes.c_int32), ("tuned", ctypes.c_int32), ("tune_ms_merge", ctypes.c_float),
+        ("tune_ms_bitset", ctypes.c_float), ("ms_weights", ctypes.c_float),
     ]
 
     def as_dict(self):
@@ -98,6 +103,7 @@ SIGNATURES = {
     "cnn_get_stats": (_INT, [_P, ctypes.POINTER(cnn_stats)]),
     "cnn_set_wait_limit": (_INT, [_P, _I64]),
     "cnn_set_search": (_INT, [_P, _INT]),
+    "cnn_set_intersection": (_INT, [_P, _INT]),
     "cnn_set_points": (_INT, [_P, _P, _INT, _I64, _I32, _INT]),
     "cnn_build_neighbours": (_INT, [_P, ctypes.c_double, _INT, _INT]),
     "cnn_set_neighbours": (_INT, [_P, _P, _P, _I64, _INT]),
@@ -248,6 +254,12 @@ class Context:
         """Search preference of the following builds (SEARCH_AUTO,
         SEARCH_GRID, SEARCH_ALL_PAIRS, SEARCH_TENSOR); same neighbour sets."""
         self._check(self._lib.cnn_set_search(self._h, int(search)), "cnn_set_search")
+
+    def set_intersection(self, strategy: int):
+        """Intersection strategy of cell-grid fits (INTERSECT_AUTO: tuned per
+        workload profile, INTERSECT_MERGE: sorted lists, INTERSECT_BITSET:
+        bit masks); same labels."""
+        self._check(self._lib.cnn_set_intersection(self._h, int(strategy)), "cnn_set_intersection")
 
     def set_wait_limit(self, limit_ns: int):
         """Limit of the kernels' bounded waits (ns); <= 0: the default 2 s."""

@@ -90,7 +90,6 @@ CNN_API cnn_status cnn_create(cnn_context **out, int device, void *stream) {
     if (!ctx) return CNN_ERR_OOM;
     ctx->device = device;
     if (const char *pz = getenv("CNN_DEBUG_POISON")) ctx->poison = atoi(pz) & 0xff;
-    if (const char *gf = getenv("CNN_GRAPH_FORM")) ctx->allow_mask = strcmp(gf, "lists") != 0;
     int sms = 0;
     if (cudaSetDevice(device) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1) {
@@ -110,6 +109,13 @@ CNN_API cnn_status cnn_create(cnn_context **out, int device, void *stream) {
     }
     for (int i = 0; i < cnn_context::kSlots; ++i) {
         if (cudaEventCreate(&ctx->ev_begin[i]) != cudaSuccess || cudaEventCreate(&ctx->ev_end[i]) != cudaSuccess) {
+            (void)cudaGetLastError();
+            cnn_destroy(ctx);
+            return CNN_ERR_CUDA;
+        }
+    }
+    for (cudaEvent_t &e : ctx->tune_ev) {
+        if (cudaEventCreate(&e) != cudaSuccess) {
             (void)cudaGetLastError();
             cnn_destroy(ctx);
             return CNN_ERR_CUDA;
@@ -144,6 +150,7 @@ CNN_API cnn_status cnn_destroy(cnn_context *ctx) {
                            &ctx->sweep_open_b, &ctx->sweep_open_count,
                            &ctx->stage_consider, &ctx->stage_offsets, &ctx->stage_indices, &ctx->stage_misc,
                            &ctx->pcell, &ctx->mbase, &ctx->masks, &ctx->dist_own, &ctx->bounds_dev,
+                           &ctx->tune_consider, &ctx->tune_labels,
                            &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->scratch_a, &ctx->scratch_b,
                            &ctx->scratch_c, &ctx->scratch_d, &ctx->scan_tmp};
     for (cnn::DevBuf *b : bufs)
@@ -152,6 +159,8 @@ CNN_API cnn_status cnn_destroy(cnn_context *ctx) {
         if (ctx->ev_begin[i]) cudaEventDestroy(ctx->ev_begin[i]);
         if (ctx->ev_end[i]) cudaEventDestroy(ctx->ev_end[i]);
     }
+    for (cudaEvent_t e : ctx->tune_ev)
+        if (e) cudaEventDestroy(e);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->host_stats) cudaFreeHost(ctx->host_stats);
     if (ctx->host_small) cudaFreeHost(ctx->host_small);
@@ -194,6 +203,14 @@ CNN_API cnn_status cnn_set_wait_limit(cnn_context *ctx, int64_t limit_ns) {
     return CNN_OK;
 }
 
+CNN_API cnn_status cnn_set_intersection(cnn_context *ctx, cnn_intersection intersection) {
+    if (!ctx) return CNN_ERR_INVALID_ARG;
+    if (intersection < CNN_INTERSECT_AUTO || intersection > CNN_INTERSECT_BITSET)
+        return ctx->fail(CNN_ERR_INVALID_ARG, "bad intersection strategy");
+    ctx->intersect_pref = intersection;
+    return CNN_OK;
+}
+
 CNN_API cnn_status cnn_set_search(cnn_context *ctx, cnn_search search) {
     if (!ctx) return CNN_ERR_INVALID_ARG;
     if (search < CNN_SEARCH_AUTO || search > CNN_SEARCH_TENSOR) return ctx->fail(CNN_ERR_INVALID_ARG, "bad search");
@@ -209,7 +226,7 @@ CNN_API cnn_status cnn_get_stats(const cnn_context *cctx, cnn_stats *out) {
     float *slot_field[cnn_context::kSlots] = {
         &ctx->stats.ms_bbox, &ctx->stats.ms_cells, &ctx->stats.ms_count, &ctx->stats.ms_scan,
         &ctx->stats.ms_fill, &ctx->stats.ms_nodes, &ctx->stats.ms_check, &ctx->stats.ms_label,
-        &ctx->stats.ms_sort, &ctx->stats.ms_gram, nullptr, nullptr};
+        &ctx->stats.ms_sort, &ctx->stats.ms_gram, &ctx->stats.ms_weights, nullptr};
     for (int i = 0; i < cnn_context::kSlots; ++i) {
         if (!ctx->slot_pending[i] || !slot_field[i]) continue;
         float ms = 0.f;
@@ -317,7 +334,7 @@ CNN_API cnn_status cnn_build_neighbours(cnn_context *ctx, double radius_cutoff, 
     if (!metric_known(metric)) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown metric");
     if (fpmode != CNN_FP_SEPARATE && fpmode != CNN_FP_FUSED) return ctx->fail(CNN_ERR_INVALID_ARG, "unknown fpmode");
     CNN_TRY(check_source(ctx, metric));
-    return build_neighbours_impl(ctx, radius_cutoff, metric, fpmode, /*want_mask=*/true);
+    return build_neighbours_impl(ctx, radius_cutoff, metric, fpmode, kFormPref);
 }
 
 CNN_API cnn_status cnn_set_neighbours(cnn_context *ctx, const int64_t *offsets, const int32_t *indices,
@@ -392,10 +409,46 @@ CNN_API cnn_status cnn_fit(cnn_context *ctx, int64_t similarity_cutoff, int64_t 
         cons_dev = const_cast<uint8_t *>(c_in);
         lab_dev = const_cast<int64_t *>(l_in);
     }
-    if (ctx->graph_mask)
+    ctx->stats.tuned = 0;
+    ctx->stats.tune_ms_merge = ctx->stats.tune_ms_bitset = 0.f;
+    if (ctx->tune_pending && n > 0) {
+        // the graph is in both forms: fit it both ways from the same labels
+        // and consider, timed, and keep the faster strategy for this profile
+        cudaStream_t st = ctx->stream;
+        CNN_TRY(ctx->ensure(ctx->tune_consider, (size_t)n));
+        CNN_TRY(ctx->ensure(ctx->tune_labels, sizeof(int64_t) * (size_t)n));
+        CNN_CUDA(ctx, cudaMemcpyAsync(ctx->tune_consider.ptr, cons_dev, (size_t)n, cudaMemcpyDeviceToDevice, st));
+        CNN_CUDA(ctx, cudaMemcpyAsync(ctx->tune_labels.ptr, lab_dev, sizeof(int64_t) * (size_t)n,
+                                      cudaMemcpyDeviceToDevice, st));
+        CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[0], st));
         CNN_TRY(fit_mask_impl(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
-    else
+        CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[1], st));
+        CNN_CUDA(ctx, cudaMemcpyAsync(cons_dev, ctx->tune_consider.ptr, (size_t)n, cudaMemcpyDeviceToDevice, st));
+        CNN_CUDA(ctx, cudaMemcpyAsync(lab_dev, ctx->tune_labels.ptr, sizeof(int64_t) * (size_t)n,
+                                      cudaMemcpyDeviceToDevice, st));
+        CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[2], st));
         CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
+        CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[3], st));
+        CNN_CUDA(ctx, cudaEventSynchronize(ctx->tune_ev[3]));
+        float fm = 0.f, fl = 0.f;
+        CNN_CUDA(ctx, cudaEventElapsedTime(&fm, ctx->tune_ev[0], ctx->tune_ev[1]));
+        CNN_CUDA(ctx, cudaEventElapsedTime(&fl, ctx->tune_ev[2], ctx->tune_ev[3]));
+        const float bitset = ctx->tune_ms_mask + fm, merge = ctx->tune_ms_lists + fl;
+        const int choice = bitset < merge ? CNN_INTERSECT_BITSET : CNN_INTERSECT_MERGE;
+        tuner_store(ctx->tune_key, choice);
+        ctx->tune_pending = false;
+        ctx->graph_mask = choice == CNN_INTERSECT_BITSET;  // both forms stay valid for this graph
+        ctx->stats.tuned = 1;
+        ctx->stats.tune_ms_merge = merge;
+        ctx->stats.tune_ms_bitset = bitset;
+        ctx->stats.intersection = choice;
+    } else if (ctx->graph_mask) {
+        CNN_TRY(fit_mask_impl(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
+        ctx->stats.intersection = CNN_INTERSECT_BITSET;
+    } else {
+        CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
+        ctx->stats.intersection = CNN_INTERSECT_MERGE;
+    }
     if (mem == CNN_MEM_HOST && n > 0) {
         CNN_CUDA(ctx, cudaMemcpyAsync(labels, lab_dev, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
         CNN_CUDA(ctx, cudaMemcpyAsync(consider, cons_dev, (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));

@@ -148,9 +148,17 @@ struct cnn_context {
     // too (built from the masks when a caller needs the lists)
     bool graph_mask = false;
     bool csr_valid = true;
-    bool allow_mask = true;  // CNN_GRAPH_FORM=lists at creation: always lists
     cnn::GridGeom mask_geo{};
     cnn::DevBuf pcell, mbase, masks;
+    // intersection strategy of cnn_build_neighbours + cnn_fit
+    // (cnn_set_intersection); under AUTO the tuner (tuner.cu) picks per
+    // workload profile, timing both forms on the first fit of a new profile
+    int intersect_pref = CNN_INTERSECT_AUTO;
+    bool tune_pending = false;          // the graph is in both forms: the next fit times both
+    uint64_t tune_key = 0;
+    float tune_ms_mask = 0.f, tune_ms_lists = 0.f;  // search times of the two forms
+    cudaEvent_t tune_ev[5] = {};
+    cnn::DevBuf tune_consider, tune_labels;
 
     // batched (radius, cut) sweep: the largest-radius graph kept aside,
     // per-pair radius buckets, consider flags of the per-fit runs
@@ -235,10 +243,12 @@ cnn_status fill_i32(cnn_context *ctx, int32_t *p, int64_t n, int32_t v);
 cnn_status iota_i32(cnn_context *ctx, int32_t *p, int64_t n);
 
 // search.cu
-// want_mask: a cell-grid search stores the graph as masks (fit_mask.cu);
-// callers that walk the lists themselves pass false
+// form of a cell-grid graph: kFormLists (callers that walk the lists
+// themselves), kFormPref (cnn_build_neighbours: the context's intersection
+// strategy, tuned under AUTO), kFormMasks (the mask form, fit_mask.cu)
+constexpr int kFormLists = 0, kFormPref = 1, kFormMasks = 2;
 cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode,
-                                 bool want_mask = false);
+                                 int form = kFormLists);
 // row_off/cols of the current graph (materialised from the masks if needed)
 cnn_status ensure_lists(cnn_context *ctx);
 cnn_status export_neighbours_impl(cnn_context *ctx, int64_t *offsets_dev, int32_t *indices_dev);
@@ -263,11 +273,20 @@ cnn_status mst_prim_impl(cnn_context *ctx, double radius_cutoff, int metric, int
 // gram.cu: tensor-core search (n_dim >= 16); *used = false when it declined
 cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode, bool *used);
 
+// tuner.cu: per-process choice of the intersection strategy by workload
+// profile (grid search: point count and candidates per point, device)
+uint64_t tuner_key(const cnn_context *ctx, int64_t n, int64_t candidates);
+bool tuner_lookup(uint64_t key, int *choice);
+void tuner_store(uint64_t key, int choice);
+
 // fit_mask.cu: cnn_fit over the mask form
 cnn_status fit_mask_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
                          int64_t current_start, uint8_t *consider_dev, int64_t *labels_dev);
 // lists from the masks: cols[row_off[p] ..] = the set bits of p's row, ascending
 cnn_status masks_to_lists(cnn_context *ctx);
+// full common-neighbour counts of the pairs (p, q > p) of the point-order
+// lists off/cols, taken from the masks of the current graph
+cnn_status mask_pair_weights(cnn_context *ctx, const int64_t *off, const int32_t *cols, int32_t *weight);
 
 // fit.cu
 // seed_a / seed_b (optional, internal order): per point a node of a finished

@@ -383,7 +383,6 @@ __global__ void new_label_kernel(const uint64_t *__restrict__ keys, int64_t k, i
 // is bounded by the shared memory of a block.
 constexpr int kOrderSmall = 24576;
 constexpr int kOrderThreads = 1024;
-constexpr int kOrderPerBlock = 256;  // values ranked per block (8 per warp)
 
 __global__ void init_count_first_kernel(int32_t *__restrict__ cnt, int32_t *__restrict__ first, int64_t r) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < r; i += (int64_t)gridDim.x * blockDim.x) {
@@ -415,7 +414,7 @@ __global__ void count_first_dense_kernel(const int64_t *__restrict__ labels, int
 // holds all keys in shared memory; each warp ranks its values in turn, the
 // lanes striding over the keys.
 __global__ void __launch_bounds__(kOrderThreads) order_small_kernel(
-    const int32_t *__restrict__ cnt, const int32_t *__restrict__ first, int r, int64_t n, int bits_n,
+    const int32_t *__restrict__ cnt, const int32_t *__restrict__ first, int r, int per_block, int64_t n, int bits_n,
     int64_t member_cutoff, int64_t max_clusters, int64_t *__restrict__ newlab) {
     extern __shared__ uint64_t s_keys[];  // [r]
     __shared__ int s_k;
@@ -431,8 +430,8 @@ __global__ void __launch_bounds__(kOrderThreads) order_small_kernel(
     if ((threadIdx.x & 31) == 0 && local) atomicAdd(&s_k, local);
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const int v_end = min(r, (int)(blockIdx.x + 1) * kOrderPerBlock);
-    for (int i = (int)blockIdx.x * kOrderPerBlock + warp; i < v_end; i += nwarps) {
+    const int v_end = min(r, (int)(blockIdx.x + 1) * per_block);
+    for (int i = (int)blockIdx.x * per_block + warp; i < v_end; i += nwarps) {
         const uint64_t key = s_keys[i];
         int below = 0;
         for (int j = lane; j < r; j += 32) below += s_keys[j] < key;
@@ -653,8 +652,11 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64
         CNN_LAUNCH_CHECK(ctx);
         const size_t keys_smem = sizeof(uint64_t) * (size_t)r;
         CNN_TRY(allow_dynamic_smem(ctx, (const void *)order_small_kernel, keys_smem));
-        order_small_kernel<<<(unsigned)((r + kOrderPerBlock - 1) / kOrderPerBlock), kOrderThreads, keys_smem, st>>>(
-            cnt, first, r, n, bits_for_fit(n), member_cutoff, max_clusters, newlab);
+        // values per block: at least one per warp, about two blocks per SM
+        const int per_sm2 = (int)((r + 2 * ctx->sm_count - 1) / (2 * ctx->sm_count));
+        const int per_block = std::max(kOrderThreads / 32, (per_sm2 + 31) / 32 * 32);
+        order_small_kernel<<<(unsigned)((r + per_block - 1) / per_block), kOrderThreads, keys_smem, st>>>(
+            cnt, first, r, per_block, n, bits_for_fit(n), member_cutoff, max_clusters, newlab);
         CNN_LAUNCH_CHECK(ctx);
         apply_dense_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(labels, n, lo, newlab);
         CNN_LAUNCH_CHECK(ctx);

@@ -557,6 +557,37 @@ __global__ void __launch_bounds__(256) masks_to_lists_kernel(int64_t n, MaskGrap
     }
 }
 
+// Full common-neighbour count of every pair (p, q > p) of the point-order
+// lists (off, cols), from the masks (one warp per point p; inv maps point
+// index -> internal index).  The MST fitter's weights
+// (SimilarityCheckerExtScreensorted._get, src/cnnclustering/_types.pyx:
+// 2708-2753: the whole intersection, no early exit).
+__global__ void __launch_bounds__(256) mask_pair_weight_kernel(int64_t n, MaskGraph G,
+                                                               const int32_t *__restrict__ inv,
+                                                               const int64_t *__restrict__ off,
+                                                               const int32_t *__restrict__ cols,
+                                                               int32_t *__restrict__ weight) {
+    __shared__ RunTable s_ra[8], s_rb[8];
+    __shared__ SegTable s_sg[8];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    RunTable &RA = s_ra[wid];
+    RunTable &RB = s_rb[wid];
+    SegTable &SG = s_sg[wid];
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t p = warp0; p < n; p += nwarps) {
+        const int64_t s = off[p], e = off[p + 1];
+        const int64_t k0 = warp_upper_bound(cols, s, e, (int32_t)p, lane);
+        if (k0 >= e) continue;
+        load_runs(G, inv[p], RA, lane);
+        for (int64_t k = k0; k < e; ++k) {
+            load_runs(G, inv[cols[k]], RB, lane);
+            const int32_t w = mask_common(G, RA, RB, SG, lane);
+            if (lane == 0) weight[k] = w;
+        }
+    }
+}
+
 MaskGraph mask_graph(const cnn_context *ctx) {
     MaskGraph G;
     G.cell_start = ctx->cell_start.as<int64_t>();
@@ -579,6 +610,16 @@ unsigned resident_blocks(cnn_context *ctx, const void *kernel, int threads, int6
 }
 
 }  // namespace
+
+cnn_status mask_pair_weights(cnn_context *ctx, const int64_t *off, const int32_t *cols, int32_t *weight) {
+    const int64_t n = ctx->n;
+    if (!ctx->graph_mask) return ctx->fail(CNN_ERR_STATE, "no neighbour graph in mask form");
+    if (n == 0) return CNN_OK;
+    mask_pair_weight_kernel<<<std::min<unsigned>(grid_for(n * 32, 256), ctx->sm_count * 16u), 256, 0, ctx->stream>>>(
+        n, mask_graph(ctx), ctx->inv.as<int32_t>(), off, cols, weight);
+    CNN_LAUNCH_CHECK(ctx);
+    return CNN_OK;
+}
 
 cnn_status masks_to_lists(cnn_context *ctx) {
     const int64_t n = ctx->n;

@@ -119,7 +119,10 @@ cnn_status mst_prim_impl(cnn_context *ctx, double radius_cutoff, int metric, int
     eb->clear();
     ew->clear();
     if (n == 0) return CNN_OK;
-    CNN_TRY(build_neighbours_impl(ctx, radius_cutoff, metric, fpmode));
+    // the cell grid keeps the graph as masks unless the merge strategy is
+    // asked for: full counts (no early exit) are what the bitset path is for
+    CNN_TRY(build_neighbours_impl(ctx, radius_cutoff, metric, fpmode,
+                                  ctx->intersect_pref == CNN_INTERSECT_MERGE ? kFormLists : kFormMasks));
     const int64_t nnz = ctx->nnz;
     CNN_TRY(ctx->ensure(ctx->pred_off, sizeof(int64_t) * (size_t)(n + 1)));
     CNN_TRY(ctx->ensure(ctx->pred_cols, sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1)));
@@ -127,8 +130,17 @@ cnn_status mst_prim_impl(cnn_context *ctx, double radius_cutoff, int metric, int
     CNN_TRY(export_neighbours_impl(ctx, ctx->pred_off.as<int64_t>(), ctx->pred_cols.as<int32_t>()));
     int32_t *weight = ctx->pred_xcols.as<int32_t>();
     const unsigned blocks = std::min<unsigned>(grid_for(n * 32, 256), ctx->sm_count * 16u);
-    pair_weight_kernel<<<blocks, 256, 0, st>>>(n, ctx->pred_off.as<int64_t>(), ctx->pred_cols.as<int32_t>(), weight);
-    CNN_LAUNCH_CHECK(ctx);
+    stage_begin(ctx, 10);
+    if (ctx->graph_mask) {
+        CNN_TRY(mask_pair_weights(ctx, ctx->pred_off.as<int64_t>(), ctx->pred_cols.as<int32_t>(), weight));
+        ctx->stats.intersection = CNN_INTERSECT_BITSET;
+    } else {
+        pair_weight_kernel<<<blocks, 256, 0, st>>>(n, ctx->pred_off.as<int64_t>(), ctx->pred_cols.as<int32_t>(),
+                                                   weight);
+        CNN_LAUNCH_CHECK(ctx);
+        ctx->stats.intersection = CNN_INTERSECT_MERGE;
+    }
+    stage_end(ctx, 10);
     mirror_weight_kernel<<<blocks, 256, 0, st>>>(n, ctx->pred_off.as<int64_t>(), ctx->pred_cols.as<int32_t>(), weight);
     CNN_LAUNCH_CHECK(ctx);
     std::vector<int64_t> off(n + 1);

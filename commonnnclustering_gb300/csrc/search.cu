@@ -169,17 +169,23 @@ __global__ void cell_assign_kernel(const double *__restrict__ x, int64_t n, int 
 __global__ void place_kernel(const int32_t *__restrict__ cell_of, const int32_t *__restrict__ slot,
                              const int64_t *__restrict__ cell_start, int64_t n, const double *__restrict__ x, int d,
                              GridGeom geo, int32_t *__restrict__ perm, int32_t *__restrict__ inv,
-                             float4 *__restrict__ xf4, int32_t *__restrict__ pcell) {
+                             float4 *__restrict__ xf4) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t c = cell_of[i];
         const int32_t p = (int32_t)(cell_start[c] + slot[i]);
         perm[p] = (int32_t)i;
         inv[i] = p;
-        if (pcell) pcell[p] = c;
         float v[3] = {0.f, 0.f, 0.f};
         for (int k = 0; k < d; ++k) v[k] = (float)__dsub_rn(x[i * d + k], geo.lo[k]);
         xf4[p] = make_float4(v[0], v[1], v[2], 0.f);
     }
+}
+
+// cell of every point in internal order (the mask form's row geometry)
+__global__ void point_cell_kernel(const int32_t *__restrict__ cell_of, const int32_t *__restrict__ perm, int64_t n,
+                                  int32_t *__restrict__ pcell) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
+        pcell[p] = cell_of[perm[p]];
 }
 
 // ---- grid search -----------------------------------------------------------
@@ -724,13 +730,14 @@ bool filter_thresholds(const std::vector<double> &ext, double R, double rc2, flo
 }  // namespace
 
 // ---------------------------------------------------------------------------
-cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode, bool want_mask) {
+cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int metric, int fpmode, int form) {
     const int64_t n = ctx->n;
     const int d = ctx->d;
     cudaStream_t st = ctx->stream;
     ctx->have_graph = false;
     ctx->graph_mask = false;
     ctx->csr_valid = true;
+    ctx->tune_pending = false;
     ++ctx->graph_generation;
     ctx->stats = cnn_stats{};
     ctx->search_stats_pending = false;
@@ -918,8 +925,16 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     int64_t grid_items = 0;
     int64_t n_candidates = -1;  // pairs looked at (grid path: from the slot sizes)
     bool use_slots = false;
-    // the mask form: the rows as bits of the cells' candidate sequences
-    const bool use_mask = use_grid && want_mask && ctx->allow_mask;
+    // Which form the cell-grid graph takes: lists (the merge intersection),
+    // masks (the bitset intersection), or -- the first time a workload
+    // profile is seen under CNN_INTERSECT_AUTO -- both, so that the first fit
+    // can time the two and the tuner keep the faster (tuner.cu).
+    const int pref = form == kFormLists ? CNN_INTERSECT_MERGE
+                     : form == kFormMasks ? CNN_INTERSECT_BITSET
+                                          : ctx->intersect_pref;
+    bool use_mask = use_grid && pref == CNN_INTERSECT_BITSET;
+    bool use_lists = !use_mask;
+    bool calibrate = false;
     unsigned long long *counters = ctx->counters.as<unsigned long long>();
 
     if (use_grid) {
@@ -936,46 +951,65 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         cell_assign_kernel<<<gb, 256, 0, st>>>(ctx->x, n, d, geo, ctx->cell_of.as<int32_t>(), slot, cell_count);
         CNN_LAUNCH_CHECK(ctx);
         CNN_TRY(scan_exclusive_i32_to_i64(ctx, cell_count, ctx->cell_start.as<int64_t>(), geo.ncells + 2));
-        if (use_mask) CNN_TRY(ctx->ensure(ctx->pcell, sizeof(int32_t) * (size_t)n));
         place_kernel<<<gb, 256, 0, st>>>(ctx->cell_of.as<int32_t>(), slot, ctx->cell_start.as<int64_t>(), n, ctx->x, d,
                                          geo, ctx->perm.as<int32_t>(), ctx->inv.as<int32_t>(),
-                                         ctx->xf4.as<float4>(), use_mask ? ctx->pcell.as<int32_t>() : nullptr);
+                                         ctx->xf4.as<float4>());
         CNN_LAUNCH_CHECK(ctx);
 
         // work items: (cell, first query) for every 32 queries of a cell
         CNN_TRY(ctx->ensure(ctx->io_a, sizeof(int32_t) * (size_t)(geo.ncells + 1)));
-        CNN_TRY(ctx->ensure(ctx->io_b, sizeof(int64_t) * (size_t)(geo.ncells + 2)));  // + the slot total
+        CNN_TRY(ctx->ensure(ctx->io_b, sizeof(int64_t) * (size_t)(geo.ncells + 3)));  // + the slot and word totals
         item_count_kernel<kUnitQueries><<<std::min<unsigned>(grid_for(geo.ncells, 256), ctx->sm_count * 16u), 256, 0, st>>>(
             ctx->cell_start.as<int64_t>(), geo.ncells, ctx->io_a.as<int32_t>());
         CNN_LAUNCH_CHECK(ctx);
         CNN_CUDA(ctx, cudaMemsetAsync(ctx->io_a.as<int32_t>() + geo.ncells, 0, sizeof(int32_t), st));
         CNN_TRY(scan_exclusive_i32_to_i64(ctx, ctx->io_a.as<int32_t>(), ctx->io_b.as<int64_t>(), geo.ncells + 1));
-        // slots: every row's upper bound (its cell's candidate count), or in
-        // the mask form every row's words
-        cnn::DevBuf &base_buf = use_mask ? ctx->mbase : ctx->grid_slot_base;
-        CNN_TRY(ctx->ensure(base_buf, sizeof(int64_t) * (size_t)(geo.ncells + 2)));
-        int64_t *slot_base = base_buf.as<int64_t>();
+        // slots: every row's upper bound (its cell's candidate count), and
+        // for the mask form every row's words
+        CNN_TRY(ctx->ensure(ctx->grid_slot_base, sizeof(int64_t) * (size_t)(geo.ncells + 2)));
+        int64_t *slot_base = ctx->grid_slot_base.as<int64_t>();
         CNN_TRY(ctx->ensure(ctx->scratch_c, sizeof(int64_t) * (size_t)(geo.ncells + 2)));
         CNN_CUDA(ctx, cudaMemsetAsync(ctx->scratch_c.as<int64_t>() + geo.ncells, 0, sizeof(int64_t), st));
-        if (use_mask)
-            cell_slots_kernel<true><<<std::min<unsigned>(grid_for(geo.ncells, 256), ctx->sm_count * 16u), 256, 0, st>>>(
-                ctx->cell_start.as<int64_t>(), geo, ctx->scratch_c.as<int64_t>());
-        else
-            cell_slots_kernel<false><<<std::min<unsigned>(grid_for(geo.ncells, 256), ctx->sm_count * 16u), 256, 0, st>>>(
-                ctx->cell_start.as<int64_t>(), geo, ctx->scratch_c.as<int64_t>());
+        const unsigned cgrid = std::min<unsigned>(grid_for(geo.ncells, 256), ctx->sm_count * 16u);
+        cell_slots_kernel<false><<<cgrid, 256, 0, st>>>(ctx->cell_start.as<int64_t>(), geo, ctx->scratch_c.as<int64_t>());
         CNN_LAUNCH_CHECK(ctx);
         CNN_TRY(scan_exclusive_i64(ctx, ctx->scratch_c.as<int64_t>(), slot_base, geo.ncells + 1));
-        int64_t hcounts[2] = {0, 0};
+        int64_t hcounts[3] = {0, 0, 0};  // work items, candidate slots, mask words
         CNN_CUDA(ctx, cudaMemcpyAsync(ctx->io_b.as<int64_t>() + geo.ncells + 1, slot_base + geo.ncells,
                                       sizeof(int64_t), cudaMemcpyDeviceToDevice, st));  // both totals side by side
         CNN_TRY(read_back(ctx, hcounts, ctx->io_b.as<int64_t>() + geo.ncells, 2 * sizeof(int64_t)));
         const int64_t nitems = hcounts[0];
+        if (pref == CNN_INTERSECT_AUTO) {
+            int choice = CNN_INTERSECT_AUTO;
+            ctx->tune_key = tuner_key(ctx, n, hcounts[1]);
+            if (tuner_lookup(ctx->tune_key, &choice)) {
+                use_mask = choice == CNN_INTERSECT_BITSET;
+                use_lists = !use_mask;
+            } else {
+                calibrate = use_mask = use_lists = true;  // the first fit times both forms
+            }
+        }
+        int64_t *word_base = nullptr;
+        if (use_mask) {
+            // the mask form: every point's cell, every row's words
+            CNN_TRY(ctx->ensure(ctx->pcell, sizeof(int32_t) * (size_t)n));
+            point_cell_kernel<<<gb, 256, 0, st>>>(ctx->cell_of.as<int32_t>(), ctx->perm.as<int32_t>(), n,
+                                                  ctx->pcell.as<int32_t>());
+            CNN_LAUNCH_CHECK(ctx);
+            CNN_TRY(ctx->ensure(ctx->mbase, sizeof(int64_t) * (size_t)(geo.ncells + 2)));
+            word_base = ctx->mbase.as<int64_t>();
+            cell_slots_kernel<true><<<cgrid, 256, 0, st>>>(ctx->cell_start.as<int64_t>(), geo,
+                                                           ctx->scratch_c.as<int64_t>());
+            CNN_LAUNCH_CHECK(ctx);
+            CNN_TRY(scan_exclusive_i64(ctx, ctx->scratch_c.as<int64_t>(), word_base, geo.ncells + 1));
+            CNN_TRY(read_back(ctx, &hcounts[2], word_base + geo.ncells, sizeof(int64_t)));
+        }
         // one pass into slots when they take at most 4 GiB, else count + fill
-        use_slots = !use_mask && hcounts[1] <= (int64_t(1) << 30);
+        use_slots = use_lists && hcounts[1] <= (int64_t(1) << 30);
         if (use_mask) {
             // + 2 words: a row's last word may be read together with the next one
-            CNN_TRY(ctx->ensure(ctx->masks, sizeof(uint32_t) * (size_t)(hcounts[1] + 2)));
-            CNN_CUDA(ctx, cudaMemsetAsync(ctx->masks.as<uint32_t>() + hcounts[1], 0, 2 * sizeof(uint32_t), st));
+            CNN_TRY(ctx->ensure(ctx->masks, sizeof(uint32_t) * (size_t)(hcounts[2] + 2)));
+            CNN_CUDA(ctx, cudaMemsetAsync(ctx->masks.as<uint32_t>() + hcounts[2], 0, 2 * sizeof(uint32_t), st));
         }
         if (use_slots) {
             CNN_TRY(ctx->ensure(ctx->grid_slot_cols, sizeof(int32_t) * (size_t)(hcounts[1] > 0 ? hcounts[1] : 1)));
@@ -990,12 +1024,21 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
 
         stage_begin(ctx, 2);
         CNN_CUDA(ctx, cudaMemsetAsync(deg, 0, sizeof(int32_t) * (size_t)n, st));
+        if (calibrate) CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[0], st));
         if (nitems > 0 && use_mask) {
             grid_unit_kernel<kMask><<<(unsigned)((nitems + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
                 ctx->io_c.as<int2>(), nitems, ctx->x, d, geo, sp, ctx->perm.as<int32_t>(),
-                ctx->cell_start.as<int64_t>(), ctx->xf4.as<float4>(), deg, slot_base,
+                ctx->cell_start.as<int64_t>(), ctx->xf4.as<float4>(), deg, word_base,
                 reinterpret_cast<int32_t *>(ctx->masks.as<uint32_t>()), counters, nullptr);
             CNN_LAUNCH_CHECK(ctx);
+        }
+        if (calibrate) {
+            // the list search as well: the same rows and lengths, counted once
+            CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[1], st));
+            CNN_CUDA(ctx, cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned long long), st));
+        }
+        if (!use_lists) {
+            // masks only
         } else if (nitems > 0 && use_slots) {
             grid_unit_kernel<kSlots><<<(unsigned)((nitems + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
                 ctx->io_c.as<int2>(), nitems, ctx->x, d, geo, sp, ctx->perm.as<int32_t>(),
@@ -1008,7 +1051,8 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
                 ctx->cell_start.as<int64_t>(), ctx->xf4.as<float4>(), deg, nullptr, nullptr, counters, nullptr);
             CNN_LAUNCH_CHECK(ctx);
         }
-        n_candidates = use_mask ? -1 : hcounts[1];  // every query against its cell's candidate runs
+        if (calibrate) CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[2], st));
+        n_candidates = hcounts[1];  // every query against its cell's candidate runs
         stage_end(ctx, 2);
         ctx->identity_perm = false;
     } else {
@@ -1043,7 +1087,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     int64_t nnz = 0;
     CNN_TRY(read_back(ctx, &nnz, row_off + n, sizeof(int64_t)));
     stage_end(ctx, 3);
-    if (!use_mask) CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1)));
+    if (use_lists) CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1)));
 
     stage_begin(ctx, 4);
     if (use_mask) {
@@ -1051,7 +1095,9 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         ctx->graph_mask = true;
         ctx->csr_valid = false;
         ctx->mask_geo = geo;
-    } else if (use_grid) {
+    }
+    if (calibrate) CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[3], st));
+    if (use_grid && use_lists) {
         if (grid_items > 0 && use_slots) {
             compact_rows_kernel<<<std::min<unsigned>(grid_for(n * 32, 256), ctx->sm_count * 16u), 256, 0, st>>>(
                 n, ctx->grid_qslot.as<int64_t>(), ctx->grid_slot_cols.as<int32_t>(), row_off,
@@ -1064,13 +1110,26 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
                 nullptr);
             CNN_LAUNCH_CHECK(ctx);
         }
-    } else {
+        ctx->csr_valid = true;
+    } else if (!use_grid) {
         const size_t smem = sizeof(float) * (size_t)(kTileCand + kTileWarps) * (d + 1);
         tile_search_kernel<true><<<grid_for(n, kTileWarps), kTileWarps * 32, smem, st>>>(
             ctx->x, ctx->scratch_b.as<float>(), d, n, sp, deg, row_off, ctx->cols.as<int32_t>(), counters);
         CNN_LAUNCH_CHECK(ctx);
     }
     stage_end(ctx, 4);
+    if (calibrate) {
+        // search times of the two forms (the list form includes its compaction)
+        CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[4], st));
+        CNN_CUDA(ctx, cudaEventSynchronize(ctx->tune_ev[4]));
+        float m01 = 0.f, m12 = 0.f, m34 = 0.f;
+        CNN_CUDA(ctx, cudaEventElapsedTime(&m01, ctx->tune_ev[0], ctx->tune_ev[1]));
+        CNN_CUDA(ctx, cudaEventElapsedTime(&m12, ctx->tune_ev[1], ctx->tune_ev[2]));
+        CNN_CUDA(ctx, cudaEventElapsedTime(&m34, ctx->tune_ev[3], ctx->tune_ev[4]));
+        ctx->tune_ms_mask = m01;
+        ctx->tune_ms_lists = m12 + m34;
+        ctx->tune_pending = true;
+    }
 
     if (ctx->host_stats) {  // read by cnn_get_stats
         CNN_CUDA(ctx, cudaMemcpyAsync(ctx->host_stats, counters, 2 * sizeof(unsigned long long),
@@ -1233,6 +1292,7 @@ cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev, con
     ctx->have_graph = false;
     ctx->graph_mask = false;
     ctx->csr_valid = true;
+    ctx->tune_pending = false;
     ++ctx->graph_generation;
     ctx->stats = cnn_stats{};
     ctx->search_stats_pending = false;

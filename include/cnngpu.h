@@ -128,6 +128,11 @@ typedef struct cnn_stats {
     int64_t n_launches;       /* kernels launched by this context since creation */
     float ms_gram;            /* tensor-core distance kernel alone (n_dim >= 16) */
     float max_abs_err;        /* max |d^2 tensor-core - d^2 float64| over rechecked pairs */
+    int32_t intersection;     /* strategy of the last fit: CNN_INTERSECT_MERGE or _BITSET */
+    int32_t tuned;            /* 1: the last fit timed both strategies for the tuner */
+    float tune_ms_merge;      /* those times (search + fit), 0 otherwise */
+    float tune_ms_bitset;
+    float ms_weights;         /* cnn_mst_prim: the pair weights (full counts) */
 } cnn_stats;
 
 CNN_API int cnn_abi_version(void);
@@ -145,6 +150,19 @@ typedef enum cnn_search {
     CNN_SEARCH_ALL_PAIRS = 2,
     CNN_SEARCH_TENSOR = 3
 } cnn_search;
+
+/* How the common-neighbour counts of cell-grid graphs (n_dim <= 3) are
+ * taken.  MERGE: sorted neighbour lists, warp-wide merge with early exit;
+ * BITSET: rows stored as bit masks over each cell's stencil candidates,
+ * counts by AND + popcount of the overlapping runs; AUTO (default): the
+ * library's tuner times both on the first fit of each workload profile
+ * (point count and candidates per point) and keeps the faster for later
+ * graphs of that profile (per process).  Results are identical. */
+typedef enum cnn_intersection {
+    CNN_INTERSECT_AUTO = 0,
+    CNN_INTERSECT_MERGE = 1,
+    CNN_INTERSECT_BITSET = 2
+} cnn_intersection;
 
 /* Create a context on `device`.  `stream` is a cudaStream_t (may be NULL:
  * the context creates its own non-blocking stream). */
@@ -167,6 +185,10 @@ CNN_API cnn_status cnn_set_wait_limit(cnn_context *ctx, int64_t limit_ns);
  * cnn_search); no reference counterpart: the reference has one brute-force
  * getter. */
 CNN_API cnn_status cnn_set_search(cnn_context *ctx, cnn_search search);
+
+/* The intersection strategy of the following cnn_build_neighbours +
+ * cnn_fit calls (see cnn_intersection); no reference counterpart. */
+CNN_API cnn_status cnn_set_intersection(cnn_context *ctx, cnn_intersection intersection);
 
 /* Points, row-major [n_points x n_dim].  Device arrays are used in place
  * (they must stay alive and unchanged until the next cnn_set_points);

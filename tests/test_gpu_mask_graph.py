@@ -1,9 +1,8 @@
-"""The cell-grid neighbour graph in mask form (one bit per stencil candidate)
-against the same graph as sorted lists: identical neighbour lists, labels,
-consider flags and check counts, over dimensions, cutoffs and edge cases.
-
-Contexts created with CNN_GRAPH_FORM=lists in the environment keep the
-lists; the default stores masks for cell-grid searches.
+"""The cell-grid neighbour graph in mask form (one bit per stencil candidate,
+the bitset intersection) against the same graph as sorted lists (the merge
+intersection): identical neighbour lists, labels, consider flags and check
+counts, over dimensions, cutoffs and edge cases; the tuner that picks
+between them; the MST weights taken from the masks.
 """
 import numpy as np
 import pytest
@@ -21,11 +20,9 @@ def abi():
 
 
 def context(abi, monkeypatch, form):
-    if form == "lists":
-        monkeypatch.setenv("CNN_GRAPH_FORM", "lists")
-    else:
-        monkeypatch.delenv("CNN_GRAPH_FORM", raising=False)
-    return abi.Context(0)
+    ctx = abi.Context(0)
+    ctx.set_intersection(abi.INTERSECT_MERGE if form == "lists" else abi.INTERSECT_BITSET)
+    return ctx
 
 
 def fit(ctx, x, r2, sc, nm, consider=None, labels=None):
@@ -98,3 +95,50 @@ def test_masks_with_consider_and_non_finite_points(abi, monkeypatch):
     assert np.array_equal(off, want[0]) and np.array_equal(idx, want[1])
     a.close()
     b.close()
+
+
+def test_tuner_times_both_forms_once_per_profile(abi):
+    """Under INTERSECT_AUTO the first fit of a profile runs both strategies
+    (tuned = 1, labels as the merge gives them); later graphs of the same
+    profile are built in the chosen form only and fitted with it."""
+    from commonnnclustering_gb300 import workloads
+    x = workloads.md3d(n=37000, seed=17, centre_spread=2.0)
+    ref = abi.Context(0)
+    ref.set_intersection(abi.INTERSECT_MERGE)
+    want, wcon, _ = fit(ref, x, 0.1 ** 2, 12, 11)
+    ctx = abi.Context(0)
+    ctx.set_intersection(abi.INTERSECT_AUTO)
+    seen = []
+    for _ in range(3):
+        lab, con, st = fit(ctx, x, 0.1 ** 2, 12, 11)
+        assert np.array_equal(lab, want) and np.array_equal(con, wcon)
+        assert st["intersection"] in (abi.INTERSECT_MERGE, abi.INTERSECT_BITSET)
+        seen.append((st["tuned"], st["intersection"], st["tune_ms_merge"], st["tune_ms_bitset"]))
+    tuned = [t for t, *_ in seen]
+    assert tuned.count(1) <= 1 and tuned[1:] == [0, 0]  # the profile may be known from an earlier test
+    assert seen[1][1] == seen[2][1]
+    if tuned[0] == 1:
+        merge, bitset = seen[0][2], seen[0][3]
+        assert merge > 0 and bitset > 0
+        assert seen[1][1] == (abi.INTERSECT_BITSET if bitset < merge else abi.INTERSECT_MERGE)
+    ctx.close()
+    ref.close()
+
+
+def test_mst_weights_from_masks_equal_the_merge(abi):
+    from commonnnclustering_gb300 import workloads
+    from oracle import cnn_oracle
+    x = workloads.blobs2d(n=1000, seed=9)
+    out = {}
+    for strat in (abi.INTERSECT_MERGE, abi.INTERSECT_BITSET):
+        ctx = abi.Context(0)
+        ctx.set_intersection(strat)
+        ctx.set_points(x)
+        out[strat] = ctx.mst_prim(0.3 ** 2)
+        assert ctx.stats()["intersection"] == strat
+        ctx.close()
+    for a, b in zip(out[abi.INTERSECT_MERGE], out[abi.INTERSECT_BITSET]):
+        assert np.array_equal(a, b)
+    want = np.asarray(cnn_oracle.mst_prim_edges(x, 0.3 ** 2), dtype=np.int64).reshape(-1, 3)
+    got = np.stack(out[abi.INTERSECT_BITSET], axis=1)
+    assert np.array_equal(got, want)
