@@ -78,3 +78,54 @@ def test_trim_trivial_leafs():
     cl.children[1].labels = np.array([0, 0])
     cl.trim_trivial_leafs()
     assert cl.children[1]._labels is None
+
+
+def nonnested_points():
+    rng = np.random.default_rng(2024)
+    parents = rng.uniform(-6, 6, size=(6, 2))
+    kids = (parents[:, None, :] + rng.normal(0, 0.6, size=(6, 4, 2))).reshape(-1, 2)
+    x = np.vstack([k + rng.normal(0, 0.15, size=(90, 2)) for k in kids])
+    return np.ascontiguousarray(x[rng.permutation(x.shape[0])])
+
+
+NONNESTED = dict(radius_cutoff=[0.03, 0.1, 0.4, 0.9], cnn_cutoff=[10, 8, 5, 3], member_cutoff=5)
+
+
+def test_nonnested_step_list_raises_like_the_reference(monkeypatch):
+    """Step lists whose later clusters merge earlier ones (radius growing):
+    a step-k cluster spans several step-(k-1) clusters.  The reference's
+    repeat fitter then fails inside Bundle.isolate with an IndexError, and so
+    does this package's (the same isolate bookkeeping) -- the order in which
+    the parents are walked never shows in a result."""
+    import os
+    import sys
+    import commonnnclustering_gb300 as cnn
+    from conftest import ROOT
+    x = nonnested_points()
+
+    def oracle_steps(self, bundle, params, member_cutoff, max_clusters, sort_by_size):
+        return o.repeat_step_labels(bundle._input_data.data, [p.radius_cutoff for p in params],
+                                    [p.similarity_cutoff for p in params], member_cutoff=member_cutoff,
+                                    max_clusters=max_clusters, sort=sort_by_size)
+
+    monkeypatch.setattr(cnn.HierarchicalFitterRepeatGPU, "step_labels", oracle_steps)
+    cl = cnn.Clustering(x, hierarchical_fitter="repeat")
+    with pytest.raises(IndexError):
+        cl.fit_hierarchical(v=False, **NONNESTED)
+    ref = os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isdir(os.path.join(ref, "cnnclustering")):
+        pytest.skip("reference package not installed here")
+    sys.path.insert(0, ref)
+    try:
+        ref_cluster = pytest.importorskip("cnnclustering.cluster")
+        recipe = {"input_data": "components_mview", "preparation_hook": "points_from_parts",
+                  "hierarchical_fitter": "repeat", "hierarchical_fitter.fitter": "bfs",
+                  "hierarchical_fitter.fitter.ngetter": "brute_force", "hierarchical_fitter.fitter.na": "vuset",
+                  "hierarchical_fitter.fitter.checker": "switch", "hierarchical_fitter.fitter.queue": "fifo",
+                  "hierarchical_fitter.fitter.ngetter.dgetter": "metric",
+                  "hierarchical_fitter.fitter.ngetter.dgetter.metric": "euclidean_r"}
+        rcl = ref_cluster.Clustering(x, recipe=recipe)
+        with pytest.raises(IndexError):
+            rcl.fit_hierarchical(v=False, **NONNESTED)
+    finally:
+        sys.path.remove(ref)
