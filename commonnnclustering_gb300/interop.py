@@ -34,14 +34,31 @@ GPU_RECIPE = {
 }
 
 
+def reference_fitter_type():
+    """FitterGPU as the reference's Clustering needs it: the reference types
+    the parameters argument of its fit (``ClusterParameters cluster_params``,
+    src/cnnclustering/cluster.pyx:250-254), so make_parameters must hand out
+    the reference's own ClusterParameters; everything else is FitterGPU."""
+    import cnnclustering._types as ref_types
+
+    class FitterGPUForReference(_fit.FitterGPU):
+        def make_parameters(self, radius_cutoff, cnn_cutoff, current_start):
+            p = super().make_parameters(radius_cutoff, cnn_cutoff, current_start)
+            return ref_types.ClusterParameters(p.radius_cutoff, p.similarity_cutoff, p.similarity_cutoff_continuous,
+                                               p.n_member_cutoff, p.current_start)
+
+    return FitterGPUForReference
+
+
 def register_with_reference():
     """Register the GPU components with an importable cnnclustering."""
     import cnnclustering._fit as ref_fit
     import cnnclustering.recipes as ref_recipes
 
-    ref_fit.Fitter.register(_fit.FitterGPU)
+    fitter_type = reference_fitter_type()
+    ref_fit.Fitter.register(fitter_type)
     m = ref_recipes.COMPONENT_NAME_TYPE_MAP
-    m["fitter"]["gpu"] = _fit.FitterGPU
+    m["fitter"]["gpu"] = fitter_type
     m["neighbours_getter"]["grid"] = _types.NeighboursGetterGPUGrid
     m["neighbours"]["gpu"] = _types.NeighboursGPU
     m["similarity_checker"]["gpu"] = _types.SimilarityCheckerGPU

@@ -157,3 +157,57 @@ def test_fitter_graph_key_follows_the_context_generation():
     ctx.gen += 1                     # another user replaced the graph
     f.prepare(Inp(), p)
     assert ctx.builds == 2
+
+
+class _OracleContext:
+    """Stands in for the library context on a machine without a GPU: the
+    calls FitterGPU makes, computed by the oracle on the same arrays."""
+
+    def __init__(self):
+        self.device, self.stream, self._gen, self.x = 0, None, 0, None
+
+    def graph_generation(self):
+        return self._gen
+
+    def set_points(self, data):
+        self.x = np.asarray(data, dtype=np.float64)
+        self._gen += 1
+
+    def build_neighbours(self, radius_cutoff, metric=0, fpmode=None):
+        from oracle import cnn_oracle
+        self.csr = cnn_oracle.neighbourhoods(self.x, radius_cutoff, metric, fpmode)
+        self._gen += 1
+
+    def fit(self, similarity_cutoff, n_member_cutoff, current_start, consider, labels):
+        from oracle import cnn_oracle
+        cnn_oracle.fit_bfs_csr(self.csr[0], self.csr[1], similarity_cutoff, n_member_cutoff, current_start,
+                               np.asarray(consider), np.asarray(labels))
+
+
+def test_reference_clustering_fit_runs_through_the_gpu_fitter(monkeypatch):
+    """The reference's own Clustering.fit (cluster.pyx:256-392) with the
+    "gpu" recipe: its orchestration -- make_parameters through FitterGPU's
+    getter, fresh and frozen labels, cnn_offset, sort_by_size -- drives
+    FitterGPU.fit, whose library calls are answered by the oracle here.  The
+    labels equal the reference's default recipe on the same points."""
+    ref = os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isdir(os.path.join(ref, "cnnclustering")):
+        pytest.skip("reference package not installed here")
+    sys.path.insert(0, ref)
+    try:
+        pytest.importorskip("cnnclustering")
+        from cnnclustering import cluster as ref_cluster
+        from commonnnclustering_gb300 import _abi, interop, workloads
+        interop.register_with_reference()
+        fake = _OracleContext()
+        monkeypatch.setattr(_abi, "default_context", lambda device=0: fake)
+        x = workloads.blobs2d(n=1500, seed=4)
+        for kw in ({"member_cutoff": 10}, {"member_cutoff": 5, "cnn_offset": 2}, {"sort_by_size": False}):
+            gpu = ref_cluster.Clustering(x, recipe="gpu")
+            gpu.fit(0.3, 5, v=False, **kw)
+            plain = ref_cluster.Clustering(x)
+            plain.fit(0.3, 5, v=False, **kw)
+            assert isinstance(gpu._fitter, FitterGPU)
+            assert np.array_equal(np.asarray(gpu.labels), np.asarray(plain.labels)), kw
+    finally:
+        sys.path.remove(ref)
