@@ -150,7 +150,7 @@ CNN_API cnn_status cnn_destroy(cnn_context *ctx) {
                            &ctx->sweep_open_b, &ctx->sweep_open_count,
                            &ctx->stage_consider, &ctx->stage_offsets, &ctx->stage_indices, &ctx->stage_misc,
                            &ctx->pcell, &ctx->mbase, &ctx->masks, &ctx->dist_own, &ctx->bounds_dev,
-                           &ctx->tune_consider, &ctx->tune_labels,
+                           &ctx->tune_consider, &ctx->tune_labels, &ctx->split,
                            &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->scratch_a, &ctx->scratch_b,
                            &ctx->scratch_c, &ctx->scratch_d, &ctx->scan_tmp};
     for (cnn::DevBuf *b : bufs)

@@ -133,6 +133,8 @@ struct cnn_context {
     cnn::DevBuf deg;      // int32[n]
     cnn::DevBuf row_off;  // int64[n+1]
     cnn::DevBuf cols;     // int32[nnz], ascending internal indices per row
+    cnn::DevBuf split;    // int32[n]: entries <= p of row p (valid when split_valid)
+    bool split_valid = false;
     cnn::DevBuf xf4;      // float4[n] permuted float32 coordinates (grid search)
     cnn::DevBuf cell_of;  // int32[n] cell id per point (original order)
     cnn::DevBuf cell_start;  // int32[ncells+2]

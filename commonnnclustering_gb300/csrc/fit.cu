@@ -50,17 +50,23 @@ __global__ void __launch_bounds__(256) cross_filter_kernel(int64_t n, const int6
                                                            const int32_t *__restrict__ parent,
                                                            int2 *__restrict__ wl,
                                                            unsigned long long *__restrict__ wl_count,
-                                                           int64_t cap) {
+                                                           int64_t cap, const int32_t *__restrict__ split) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t a64 = warp0; a64 < n; a64 += nwarps) {
         const int32_t a = (int32_t)a64;
-        const int32_t pa = parent[a];
+        // parent[a], the row bounds and split[a] in one round trip
+        int64_t v = 0;
+        if (lane == 0) v = parent[a];
+        else if (lane < 3) v = row_off[a + lane - 1];
+        else if (lane == 3 && split) v = split[a];
+        const int32_t pa = (int32_t)__shfl_sync(0xffffffffu, v, 0);
         if (pa < 0) continue;
-        const int64_t s = row_off[a], e = row_off[a + 1];
-        for (int64_t k0 = warp_upper_bound(cols, s, e, a, lane); k0 < e; k0 += 32) {
+        const int64_t s = __shfl_sync(0xffffffffu, v, 1), e = __shfl_sync(0xffffffffu, v, 2);
+        const int64_t split_a = __shfl_sync(0xffffffffu, v, 3);
+        for (int64_t k0 = split ? s + split_a : warp_upper_bound(cols, s, e, a, lane); k0 < e; k0 += 32) {
             const int64_t k = k0 + lane;
             int32_t b = -1, pb = -1;
             if (k < e) {
@@ -547,9 +553,11 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     const unsigned check_blocks = resident((const void *)check_union_kernel, kCheckWarps * 32, 0);
     // hook: every node checks its first kHookEdges candidate edges; compress; then
     // the cross-root pairs only, where pairs inside joined sets cost one load
+    // rows ascending: the entries > a start at split[a] when the search recorded it
+    const int32_t *split = ctx->split_valid ? ctx->split.as<int32_t>() : nullptr;
     check_union_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(
         n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff, kHookEdges,
-        counters, seed_a, seed_b);
+        counters, seed_a, seed_b, split);
     CNN_LAUNCH_CHECK(ctx);
     root_store_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(n, node, parent);
     CNN_LAUNCH_CHECK(ctx);
@@ -568,7 +576,8 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
                                                              wl_count, wl_cap);
     } else {
         cross_filter_kernel<<<resident((const void *)cross_filter_kernel, 256, 0), 256, 0, st>>>(
-            n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, ctx->io_c.as<int2>(), wl_count, wl_cap);
+            n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, ctx->io_c.as<int2>(), wl_count, wl_cap,
+            split);
     }
     CNN_LAUNCH_CHECK(ctx);
     edge_check_kernel<<<resident((const void *)edge_check_kernel, kCheckWarps * 32, 0), kCheckWarps * 32,

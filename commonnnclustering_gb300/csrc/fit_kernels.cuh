@@ -188,13 +188,15 @@ __device__ __forceinline__ int64_t warp_upper_bound(const int32_t *__restrict__ 
 // warp joined something: a stale "different" only costs an extra check,
 // never a wrong skip.  max_edges bounds the candidate edges one node
 // examines (the hook pass uses 3).  Rows are ascending, so the walk starts
-// at the first entry > a.  Nodes with skip_a[a] >= 0 or skip_b[a] >= 0
-// (already joined by seeds) are left to the cross-edge pass.
+// at the first entry > a: split[a] (the number of entries <= a, when the
+// search recorded it) or a warp-wide binary search.  Nodes with
+// skip_a[a] >= 0 or skip_b[a] >= 0 (already joined by seeds) are left to
+// the cross-edge pass.
 __device__ __forceinline__ void check_union_body(
     int64_t n, const int64_t *__restrict__ row_off, const int32_t *__restrict__ cols,
     int32_t *__restrict__ parent, int32_t needed, int32_t max_edges,
     unsigned long long *__restrict__ counters, const int32_t *__restrict__ skip_a = nullptr,
-    const int32_t *__restrict__ skip_b = nullptr) {
+    const int32_t *__restrict__ skip_b = nullptr, const int32_t *__restrict__ split = nullptr) {
     __shared__ int32_t s_wide[kCheckWarps][kWideChunk];
     int32_t *sA = s_wide[(threadIdx.x >> 5) % kCheckWarps];
     const int lane = threadIdx.x & 31;
@@ -210,14 +212,16 @@ __device__ __forceinline__ void check_union_body(
     const int64_t a_step = chunked ? 1 : nwarps;
     for (int64_t a64 = a_begin; a64 < a_end; a64 += a_step) {
         const int32_t a = (int32_t)a64;
-        // parent[a] and the row bounds in one round trip (lanes 0, 1, 2)
+        // parent[a], the row bounds and split[a] in one round trip (lanes 0..3)
         int64_t v = 0;
         if (lane == 0) v = *(volatile int32_t *)&parent[a];
         else if (lane < 3) v = row_off[a + lane - 1];
+        else if (lane == 3 && split) v = split[a];
         const int32_t pa = (int32_t)__shfl_sync(0xffffffffu, v, 0);
         if (pa < 0) continue;  // not a node
         if ((skip_a && skip_a[a] >= 0) || (skip_b && skip_b[a] >= 0)) continue;
         const int64_t s = __shfl_sync(0xffffffffu, v, 1), e = __shfl_sync(0xffffffffu, v, 2);
+        const int64_t split_a = __shfl_sync(0xffffffffu, v, 3);
         const int32_t la = (int32_t)(e - s);
         const int32_t *A = cols + s;
         // ra (and rx once set) are roots observed to hold a: equal roots mean
@@ -225,7 +229,8 @@ __device__ __forceinline__ void check_union_body(
         int32_t ra = -1, rx = -1;
         bool dirty = true;
         int32_t seen = 0;
-        for (int64_t k0 = warp_upper_bound(cols, s, e, a, lane); k0 < e && seen < max_edges; k0 += 32) {
+        for (int64_t k0 = split ? s + split_a : warp_upper_bound(cols, s, e, a, lane); k0 < e && seen < max_edges;
+             k0 += 32) {
             const int64_t k = k0 + lane;
             int32_t b = -1, pb = -1;
             if (k < e) {
@@ -304,8 +309,8 @@ __global__ void __launch_bounds__(kCheckWarps * 32, CNN_CHECK_MIN_BLOCKS) check_
     int64_t n, const int64_t *__restrict__ row_off, const int32_t *__restrict__ cols,
     int32_t *__restrict__ parent, int32_t needed, int32_t max_edges,
     unsigned long long *__restrict__ counters, const int32_t *__restrict__ skip_a,
-    const int32_t *__restrict__ skip_b) {
-    check_union_body(n, row_off, cols, parent, needed, max_edges, counters, skip_a, skip_b);
+    const int32_t *__restrict__ skip_b, const int32_t *__restrict__ split = nullptr) {
+    check_union_body(n, row_off, cols, parent, needed, max_edges, counters, skip_a, skip_b, split);
 }
 
 // Full path compression and per-component minimum point index.

@@ -254,15 +254,28 @@ __global__ void cell_slots_kernel(const int64_t *__restrict__ cell_start, GridGe
     }
 }
 
-// rows from their slots to the CSR (one warp per row)
+// rows from their slots to the CSR (one warp per row); split[q] = the
+// entries <= q of row q (rows are ascending), so the fit's walks over the
+// entries > q start there
 __global__ void compact_rows_kernel(int64_t n, const int64_t *__restrict__ qslot, const int32_t *__restrict__ slot_cols,
-                                    const int64_t *__restrict__ row_off, int32_t *__restrict__ cols) {
+                                    const int64_t *__restrict__ row_off, int32_t *__restrict__ cols,
+                                    int32_t *__restrict__ split) {
     const int lane = threadIdx.x & 31;
     const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t q = warp0; q < n; q += nwarps) {
         const int64_t src = qslot[q], dst = row_off[q], len = row_off[q + 1] - dst;
-        for (int64_t e = lane; e < len; e += 32) cols[dst + e] = slot_cols[src + e];
+        int32_t le = 0;
+        for (int64_t e0 = 0; e0 < len; e0 += 32) {
+            const int64_t e = e0 + lane;
+            int32_t v = INT32_MAX;
+            if (e < len) {
+                v = slot_cols[src + e];
+                cols[dst + e] = v;
+            }
+            le += __popc(__ballot_sync(0xffffffffu, v <= (int32_t)q));
+        }
+        if (lane == 0) split[q] = le;
     }
 }
 
@@ -738,6 +751,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     ctx->graph_mask = false;
     ctx->csr_valid = true;
     ctx->tune_pending = false;
+    ctx->split_valid = false;
     ++ctx->graph_generation;
     ctx->stats = cnn_stats{};
     ctx->search_stats_pending = false;
@@ -1099,10 +1113,12 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     if (calibrate) CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[3], st));
     if (use_grid && use_lists) {
         if (grid_items > 0 && use_slots) {
+            CNN_TRY(ctx->ensure(ctx->split, sizeof(int32_t) * (size_t)n));
             compact_rows_kernel<<<std::min<unsigned>(grid_for(n * 32, 256), ctx->sm_count * 16u), 256, 0, st>>>(
                 n, ctx->grid_qslot.as<int64_t>(), ctx->grid_slot_cols.as<int32_t>(), row_off,
-                ctx->cols.as<int32_t>());
+                ctx->cols.as<int32_t>(), ctx->split.as<int32_t>());
             CNN_LAUNCH_CHECK(ctx);
+            ctx->split_valid = true;
         } else if (grid_items > 0) {
             grid_unit_kernel<kFill><<<(unsigned)((grid_items + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
                 ctx->io_c.as<int2>(), grid_items, ctx->x, d, geo, sp, ctx->perm.as<int32_t>(),
@@ -1293,6 +1309,7 @@ cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev, con
     ctx->graph_mask = false;
     ctx->csr_valid = true;
     ctx->tune_pending = false;
+    ctx->split_valid = false;
     ++ctx->graph_generation;
     ctx->stats = cnn_stats{};
     ctx->search_stats_pending = false;

@@ -292,6 +292,7 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
 
     // one search, at the largest radius (the same search cnn_build_neighbours runs)
     CNN_TRY(build_neighbours_impl(ctx, rcs.back(), metric, fpmode));
+    ctx->split_valid = false;  // the fits below see other graphs in the same arrays
     const int64_t nnz = ctx->nnz;
     Ladder lad{};
     lad.k = n_radii;
