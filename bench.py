@@ -78,6 +78,7 @@ WORKLOADS = {
 HEADLINE = "md3d-200k"
 SUB_WORKLOADS = ["blobs2d-5k", "features-500k-d64", "nested3d-1m-sweep", "serve-stream-short"]
 METRIC = "CommonNN fit points/s (bit-exact labels)"
+INTERSECTIONS = {"auto": 0, "merge": 1, "bitset": 2}  # cnn_intersection
 UNIT = "points/s"
 
 
@@ -304,6 +305,7 @@ def fit_record(W, args, peaks, dist=None, world=1, local=0, rank=0, cpu=True):
     stream = torch.cuda.Stream(device=dev)
     ctx = _abi.Context(local, stream=int(stream.cuda_stream))
     ctx.set_timing(True)
+    ctx.set_intersection(INTERSECTIONS[args.intersection])
     xt = torch.from_numpy(x).to(dev)
     labels = torch.zeros(n, dtype=torch.int64, device=dev)
     consider = torch.ones(n, dtype=torch.uint8, device=dev)
@@ -378,6 +380,7 @@ def fit_record(W, args, peaks, dist=None, world=1, local=0, rank=0, cpu=True):
     lab_host = torch.zeros(n, dtype=torch.int64).pin_memory().numpy()
     con_host = torch.ones(n, dtype=torch.uint8).pin_memory().numpy()
     e2e_ctx = _abi.Context(local)
+    e2e_ctx.set_intersection(INTERSECTIONS[args.intersection])
 
     def e2e_step():
         lab_host[:] = 0
@@ -424,6 +427,8 @@ def fit_record(W, args, peaks, dist=None, world=1, local=0, rank=0, cpu=True):
         "fit_stats": {k: stats_list[-1][k] for k in ("n_nodes", "n_checks", "n_accepted", "n_exact",
                                                      "n_candidates", "n_clusters", "filter_band", "max_abs_err",
                                                      "search_kind")},
+        "intersection": {"requested": args.intersection,
+                         "used": {1: "merge", 2: "bitset"}.get(stats_list[-1]["intersection"], "none")},
     }
     if W["d"] >= 16:
         rec["fit_stats"]["recheck_fraction"] = (stats_list[-1]["n_exact"] / stats_list[-1]["n_candidates"]
@@ -794,6 +799,8 @@ def main():
     ap.add_argument("--workload", default=None, choices=sorted(WORKLOADS),
                     help="run this workload alone as the only line (default: the headline plus sub-records)")
     ap.add_argument("--slots", type=int, default=4, help="concurrent jobs of the served stream")
+    ap.add_argument("--intersection", default="auto", choices=sorted(INTERSECTIONS),
+                    help="intersection strategy of the fit workloads (auto: the library's tuner picks)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3

@@ -266,14 +266,19 @@ __global__ void compact_rows_kernel(int64_t n, const int64_t *__restrict__ qslot
     for (int64_t q = warp0; q < n; q += nwarps) {
         const int64_t src = qslot[q], dst = row_off[q], len = row_off[q + 1] - dst;
         int32_t le = 0;
-        for (int64_t e0 = 0; e0 < len; e0 += 32) {
-            const int64_t e = e0 + lane;
-            int32_t v = INT32_MAX;
-            if (e < len) {
-                v = slot_cols[src + e];
-                cols[dst + e] = v;
+        for (int64_t e0 = 0; e0 < len; e0 += 128) {  // four independent loads in flight per lane
+            int32_t v[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int64_t e = e0 + j * 32 + lane;
+                v[j] = e < len ? slot_cols[src + e] : INT32_MAX;
             }
-            le += __popc(__ballot_sync(0xffffffffu, v <= (int32_t)q));
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int64_t e = e0 + j * 32 + lane;
+                if (e < len) cols[dst + e] = v[j];
+                le += __popc(__ballot_sync(0xffffffffu, v[j] <= (int32_t)q));
+            }
         }
         if (lane == 0) split[q] = le;
     }

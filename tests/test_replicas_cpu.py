@@ -50,7 +50,7 @@ def reference_rank_main(rank, world, port, out):
     os.environ.update({"RANK": str(rank), "WORLD_SIZE": str(world), "LOCAL_RANK": str(rank),
                        "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
     import bench
-    args = type("A", (), {"steps": 1, "warmup": 0, "workload": "blobs2d-5k"})()
+    args = type("A", (), {"steps": 1, "warmup": 0, "workload": "blobs2d-5k", "intersection": "auto"})()
     buf = io.StringIO()
     with contextlib.redirect_stdout(buf):
         bench.run_reference(args)
