@@ -90,6 +90,7 @@ CNN_API cnn_status cnn_create(cnn_context **out, int device, void *stream) {
     if (!ctx) return CNN_ERR_OOM;
     ctx->device = device;
     if (const char *pz = getenv("CNN_DEBUG_POISON")) ctx->poison = atoi(pz) & 0xff;
+    if (const char *gr = getenv("CNN_GRID_REACH")) ctx->grid_reach = atoi(gr) == 2 ? 2 : 1;
     int sms = 0;
     if (cudaSetDevice(device) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1) {

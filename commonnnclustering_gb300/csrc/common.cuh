@@ -61,6 +61,7 @@ struct GridGeom {
     double inv_h;      // 1 / h, rounded: cell coordinates are a monotone function of x
     int32_t g[3];      // cells per dimension (1 for unused dimensions)
     int64_t ncells;    // g0*g1*g2; bucket ncells holds non-finite points
+    int32_t reach;     // neighbours lie at most `reach` cells apart (h >= R / reach)
 };
 
 // The cell-grid neighbour graph as bit masks (fit_mask.cu): a point of cell
@@ -92,6 +93,7 @@ struct cnn_context {
     int poison = -1;  // >= 0: fill every new workspace allocation with this byte (CNN_DEBUG_POISON)
     int64_t wait_limit_ns = 0;  // > 0: limit of the bounded waits in the kernels (cnn_set_wait_limit)
     int search_pref = CNN_SEARCH_AUTO;  // cnn_set_search
+    int grid_reach = 1;  // cell edge R / grid_reach (CNN_GRID_REACH=1|2 at creation)
     int64_t n_launches = 0;
     std::string last_error;
     cnn_stats stats{};

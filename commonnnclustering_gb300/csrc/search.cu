@@ -217,20 +217,21 @@ __global__ void item_fill_kernel(const int64_t *__restrict__ cell_start, int64_t
     }
 }
 
-// Candidate count of a cell: the points of the 3 x 3 x 3 cells around it
-// (the same 9 x-runs the search packs).
+// Candidate count of a cell: the points of the (2 reach + 1)^3 cells around
+// it (the same x-runs the search packs).
 __device__ __forceinline__ int64_t cell_candidates(int64_t cid, const GridGeom &geo,
                                                    const int64_t *__restrict__ cell_start) {
     const int32_t cx = (int32_t)(cid % geo.g[0]);
     const int32_t cy = (int32_t)((cid / geo.g[0]) % geo.g[1]);
     const int32_t cz = (int32_t)(cid / ((int64_t)geo.g[0] * geo.g[1]));
-    const int32_t xlo = cx > 0 ? cx - 1 : 0;
-    const int32_t xhi = cx + 1 < geo.g[0] ? cx + 1 : geo.g[0] - 1;
+    const int S = geo.reach;
+    const int32_t xlo = cx > S - 1 ? cx - S : 0;
+    const int32_t xhi = cx + S < geo.g[0] ? cx + S : geo.g[0] - 1;
     int64_t total = 0;
-    for (int dz = -1; dz <= 1; ++dz) {
+    for (int dz = -S; dz <= S; ++dz) {
         const int32_t z = cz + dz;
         if (z < 0 || z >= geo.g[2]) continue;
-        for (int dy = -1; dy <= 1; ++dy) {
+        for (int dy = -S; dy <= S; ++dy) {
             const int32_t y = cy + dy;
             if (y < 0 || y >= geo.g[1]) continue;
             const int64_t row = (int64_t)geo.g[0] * ((int64_t)y + (int64_t)geo.g[1] * z);
@@ -295,10 +296,11 @@ constexpr int kCount = 0, kFill = 1, kSlots = 2, kMask = 3;
 
 // ---- warp-granular grid search ---------------------------------------------
 // Work unit = (cell, up to kUnitQueries consecutive queries of that cell), one
-// warp each, no block-wide staging: the warp reads its cell's 9 candidate
-// runs (3x3 (y,z) neighbours, each three x-cells long and contiguous in
-// internal order) straight from xf4, 32 candidates at a time over the runs'
-// concatenation, and tests each against its queries held in registers.
+// warp each, no block-wide staging: the warp reads its cell's candidate runs
+// ((2 reach + 1)^2 (y,z) neighbours, each 2 reach + 1 x-cells long and
+// contiguous in internal order) straight from xf4, 32 candidates at a time
+// over the runs' concatenation, and tests each against its queries held in
+// registers.
 // Sparse cells (most cells hold a few points) cost one warp, not a block;
 // the warps of a block work on neighbouring units and share candidates
 // through L1.  Concatenated run order = ascending internal index, so every
@@ -308,6 +310,7 @@ constexpr int kCount = 0, kFill = 1, kSlots = 2, kMask = 3;
 #endif
 constexpr int kUnitQueries = CNN_UNIT_QUERIES;
 constexpr int kUnitWarps = 8;
+constexpr int kMaxRuns = 25;  // (2 * reach + 1)^2 runs of a cell's stencil, reach <= 2
 #ifndef CNN_UNIT_SUB
 #define CNN_UNIT_SUB 1  // two steps per iteration measured slower (register pressure)
 #endif
@@ -323,8 +326,8 @@ __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_uni
     SearchParams sp, const int32_t *__restrict__ perm, const int64_t *__restrict__ cell_start,
     const float4 *__restrict__ xf4, int32_t *__restrict__ deg, const int64_t *__restrict__ row_off,
     int32_t *__restrict__ cols, unsigned long long *__restrict__ counters, int64_t *__restrict__ qslot) {
-    __shared__ int32_t s_rs[kUnitWarps][9];
-    __shared__ int32_t s_cum[kUnitWarps][10];
+    __shared__ int32_t s_rs[kUnitWarps][kMaxRuns];
+    __shared__ int32_t s_cum[kUnitWarps][kMaxRuns + 1];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t u = (int64_t)blockIdx.x * kUnitWarps + wid;
     if (u >= nunits) return;  // whole warps only: nothing below syncs the block
@@ -332,16 +335,17 @@ __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_uni
     const int32_t cid = unit.x;
     const int64_t q0 = unit.y;
     const int64_t cs = cell_start[cid], qend = cell_start[cid + 1];
-    // run r = lane (r < 9): (dz, dy) = (r / 3 - 1, r % 3 - 1); empty when outside the grid
+    // run r = lane (r < nruns): (dz, dy) = (r / W - S, r % W - S); empty when outside the grid
+    const int S = geo.reach, Wd = 2 * S + 1, nruns = Wd * Wd;
     int32_t rs = 0, len = 0;
-    if (lane < 9) {
+    if (lane < nruns) {
         const int32_t cx = cid % geo.g[0];
         const int32_t cy = (cid / geo.g[0]) % geo.g[1];
         const int32_t cz = cid / (geo.g[0] * geo.g[1]);
-        const int32_t z = cz + lane / 3 - 1, y = cy + lane % 3 - 1;
+        const int32_t z = cz + lane / Wd - S, y = cy + lane % Wd - S;
         if (z >= 0 && z < geo.g[2] && y >= 0 && y < geo.g[1]) {
-            const int32_t xlo = cx > 0 ? cx - 1 : 0;
-            const int32_t xhi = cx + 1 < geo.g[0] ? cx + 1 : geo.g[0] - 1;
+            const int32_t xlo = cx > S - 1 ? cx - S : 0;
+            const int32_t xhi = cx + S < geo.g[0] ? cx + S : geo.g[0] - 1;
             const int64_t row = (int64_t)geo.g[0] * ((int64_t)y + (int64_t)geo.g[1] * z);
             const int64_t b = cell_start[row + xlo], e = cell_start[row + xhi + 1];
             rs = (int32_t)b;
@@ -350,16 +354,16 @@ __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_uni
     }
     int32_t inc = len;  // inclusive prefix over the runs
 #pragma unroll
-    for (int o = 1; o < 16; o <<= 1) {
+    for (int o = 1; o < 32; o <<= 1) {
         const int32_t v = __shfl_up_sync(0xffffffffu, inc, o);
         if (lane >= o) inc += v;
     }
-    if (lane < 9) {
+    if (lane < nruns) {
         s_rs[wid][lane] = rs;
         s_cum[wid][lane + 1] = inc;
     }
     if (lane == 0) s_cum[wid][0] = 0;
-    const int32_t total = __shfl_sync(0xffffffffu, inc, 8);
+    const int32_t total = __shfl_sync(0xffffffffu, inc, nruns - 1);
     __syncwarp();
 
     // query k: internal index (-1: none), coordinates, and for kFill/kSlots
@@ -405,7 +409,7 @@ __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_uni
 #pragma unroll
         for (int u = 0; u < kUnitSub; ++u) {
             const int32_t t = t0 + 32 * u;
-            while (t >= hi[u] && r[u] < 8) {
+            while (t >= hi[u] && r[u] < nruns - 1) {
                 ++r[u];
                 base[u] = s_rs[wid][r[u]] - hi[u];
                 hi[u] = s_cum[wid][r[u] + 1];
@@ -917,7 +921,11 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     GridGeom geo{};
     bool use_grid = d <= 3 && radius_ok && R > 0 && isfinite(R) && !periodic && !all_pairs;
     if (use_grid) {
-        double h = R * (1.0 + 1e-6);
+        // cells of edge h >= R / reach: a qualifying pair lies at most `reach`
+        // cells apart in every dimension; reach 2 scans (5/2)^3 = 15.6 R^3
+        // around a point instead of 27 R^3 (fewer candidates per neighbour)
+        geo.reach = ctx->grid_reach;
+        double h = R / geo.reach * (1.0 + 1e-6);
         // cells cost 12 bytes each (count + start); allow up to 64 per point
         // (at most 64M) so sparse sets in large boxes keep cells of edge ~R
         const double max_cells = std::max<double>(std::min<double>(64.0 * (double)n, 67108864.0), 4096.0);
@@ -951,7 +959,8 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     const int pref = form == kFormLists ? CNN_INTERSECT_MERGE
                      : form == kFormMasks ? CNN_INTERSECT_BITSET
                                           : ctx->intersect_pref;
-    bool use_mask = use_grid && pref == CNN_INTERSECT_BITSET;
+    // the mask form reads rows through 3 x 3 x 3 stencils: cells of reach 1 only
+    bool use_mask = use_grid && pref == CNN_INTERSECT_BITSET && geo.reach == 1;
     bool use_lists = !use_mask;
     bool calibrate = false;
     unsigned long long *counters = ctx->counters.as<unsigned long long>();
@@ -998,7 +1007,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
                                       sizeof(int64_t), cudaMemcpyDeviceToDevice, st));  // both totals side by side
         CNN_TRY(read_back(ctx, hcounts, ctx->io_b.as<int64_t>() + geo.ncells, 2 * sizeof(int64_t)));
         const int64_t nitems = hcounts[0];
-        if (pref == CNN_INTERSECT_AUTO) {
+        if (pref == CNN_INTERSECT_AUTO && geo.reach == 1) {
             int choice = CNN_INTERSECT_AUTO;
             ctx->tune_key = tuner_key(ctx, n, hcounts[1]);
             if (tuner_lookup(ctx->tune_key, &choice)) {

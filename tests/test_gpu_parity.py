@@ -343,3 +343,30 @@ def test_sort_by_size_many_label_values(cnn, oracle, n_values, span):
         got = cnn.Labels(lab.copy())
         got.sort_by_size(mc, mx)
         assert np.array_equal(np.asarray(got.labels), want), (mc, mx)
+
+
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_grid_reach_two_gives_the_same_sets(cnn, oracle, monkeypatch, d):
+    """Cells of edge R/2 with a 5-cell stencil per dimension (CNN_GRID_REACH=2,
+    read when a context is created) scan fewer candidates and give the
+    oracle's neighbour sets and labels."""
+    from commonnnclustering_gb300 import _abi, workloads
+    monkeypatch.setenv("CNN_GRID_REACH", "2")
+    x = np.ascontiguousarray(workloads.md3d(n=20000, seed=9, centre_spread=2.0)[:, :d])
+    r2 = 0.1 ** 2 if d == 3 else 0.02 ** 2
+    want = oracle.neighbourhoods(x, r2, grid=True)
+    ctx = cnn.Context(0)
+    try:
+        ctx.set_points(x)
+        ctx.build_neighbours(r2)
+        assert ctx.stats()["search_kind"] == 1
+        off, idx = ctx.get_neighbours(x.shape[0])
+        assert np.array_equal(off, want[0]) and np.array_equal(idx, want[1])
+        labels = np.zeros(x.shape[0], dtype=np.int64)
+        consider = np.ones(x.shape[0], dtype=np.uint8)
+        ctx.fit(7, 6, 1, consider, labels)
+        ref_labels = np.zeros(x.shape[0], dtype=np.int64)
+        oracle.fit_bfs_csr(want[0], want[1], 7, 6, 1, np.ones(x.shape[0], dtype=np.uint8), ref_labels)
+        assert np.array_equal(labels, ref_labels)
+    finally:
+        ctx.close()
