@@ -209,8 +209,10 @@ def tensor_roofline(W, stats_list, n, peaks):
     }
 
 
-def hbm_roofline(stats_list, nnz, n, peaks):
-    """Dominant stage by mean CUDA-event time; algorithmic bytes per launch."""
+def hbm_roofline(stats_list, nnz, n, peaks, workload=None):
+    """Dominant stage by mean CUDA-event time; algorithmic bytes per launch.
+    `traffic` comes from the committed ncu capture, which holds one
+    workload's launches: other workloads report null."""
     stages = {
         # stage -> (kernel name, algorithmic bytes per launch)
         # one pass into per-row slots: float4 coordinates read, rows, lengths and slot starts written
@@ -233,7 +235,9 @@ def hbm_roofline(stats_list, nnz, n, peaks):
     if os.path.exists(tpath):
         try:
             with open(tpath) as f:
-                traffic = json.load(f).get(kname)
+                tj = json.load(f)
+            if tj.get("_workload") == workload:
+                traffic = tj.get(kname)
         except Exception:
             traffic = None
     return {
@@ -422,7 +426,7 @@ def fit_record(W, args, peaks, dist=None, world=1, local=0, rank=0, cpu=True):
         "gpu_launches_per_step": int(launches),
         "clocks": clocks.summary(),
         "roofline": (tensor_roofline(W, stats_list, n, peaks) if W["d"] >= 16
-                     else hbm_roofline(stats_list, nnz, n, peaks)),
+                     else hbm_roofline(stats_list, nnz, n, peaks, W["name"])),
         "wall_s_timed_region": t_wall,
         "fit_stats": {k: stats_list[-1][k] for k in ("n_nodes", "n_checks", "n_accepted", "n_exact",
                                                      "n_candidates", "n_clusters", "filter_band", "max_abs_err",
