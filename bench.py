@@ -525,6 +525,12 @@ def sweep_record(W, args, peaks, dist=None, world=1, local=0, rank=0, cpu=True):
 
     for _ in range(max(1, min(args.warmup, 3))):
         batched()
+    torch.cuda.synchronize()
+    l0 = ctx.stats()["n_launches"]
+    batched()
+    torch.cuda.synchronize()
+    sw = ctx.stats()  # this sweep's kernels and the CUDA graphs its fits ran as
+    kernels_per_step = int(sw["n_launches"] - l0)
     one_by_one(check=out)  # also the parity check: every pair equals its separate fit
     with ClockSampler(local) as clocks:
         ms_batched = timed(batched, steps)
@@ -533,18 +539,20 @@ def sweep_record(W, args, peaks, dist=None, world=1, local=0, rank=0, cpu=True):
     fits = len(radii) * len(cuts)
     st = ctx.stats()
 
-    # e2e: host points in, host labels out, through the public sweep call
+    # e2e: host points in, host labels out (pinned buffers), through the
+    # public sweep call
     e2e_ctx = _abi.Context(local)
     x_host = torch.from_numpy(x).pin_memory().numpy()
+    got = torch.empty((len(radii), len(cuts), n), dtype=torch.int64).pin_memory().numpy()
     e2e_ctx.set_points(x_host)
-    got = e2e_ctx.sweep(r2, cut_pairs, member_cutoff=2)
+    e2e_ctx.sweep(r2, cut_pairs, member_cutoff=2, labels_out=got)
     e2e_times = []
     for _ in range(steps):
         flush.zero_()
         torch.cuda.synchronize()
         t = time.perf_counter()
         e2e_ctx.set_points(x_host)
-        got = e2e_ctx.sweep(r2, cut_pairs, member_cutoff=2)
+        e2e_ctx.sweep(r2, cut_pairs, member_cutoff=2, labels_out=got)
         e2e_times.append(time.perf_counter() - t)
     if not np.array_equal(got, out.cpu().numpy()):
         raise SystemExit("bench: host-buffer and device-buffer sweeps disagree")
@@ -572,6 +580,13 @@ def sweep_record(W, args, peaks, dist=None, world=1, local=0, rank=0, cpu=True):
                    "fpmode": fpmode_name()},
         "e2e": {"value": world * n * fits / e2e_s, "unit": "points/s (summed over the fits)",
                 "h2d_bytes_per_step": n * 3 * 4, "d2h_bytes_per_step": fits * n * 8},
+        "gpu_launches": kernels_per_step * steps,
+        "gpu_launches_per_step": kernels_per_step,
+        "cuda_graph": {"graphs_per_step": sw["graphs"], "nodes_per_step": sw["graph_nodes"],
+                       "ms_capture_and_instantiate": round(sw["ms_graph_build"], 3),
+                       "note": "the 64 fits (with their sorts and open-pair lists) run as captured graphs; "
+                               "the searches, radius buckets and graph fills before them are plain launches"},
+        "e2e_ms_steps": [round(1e3 * t, 2) for t in e2e_times],
         "plain_gpu": {"path": "the same 64 fits one by one (search + fit + sort_by_size each)",
                       "ms_per_step": ms_plain, "speedup_of_batched_sweep": ms_plain / ms_batched},
         "fits_per_s": fits / (ms_batched * 1e-3),

@@ -82,6 +82,7 @@ class cnn_stats(ctypes.Structure):
         ("n_launches", ctypes.c_int64), ("ms_gram", ctypes.c_float), ("max_abs_err", ctypes.c_float),
         ("intersection", ctypes.c_int32), ("tuned", ctypes.c_int32), ("tune_ms_merge", ctypes.c_float),
         ("tune_ms_bitset", ctypes.c_float), ("ms_weights", ctypes.c_float),
+        ("graphs", ctypes.c_int32), ("graph_nodes", ctypes.c_int64), ("ms_graph_build", ctypes.c_float),
     ]
 
     def as_dict(self):
@@ -405,8 +406,9 @@ class Context:
 
         radius_cutoffs: adjusted cutoffs, ascending.  cuts: sequence of
         (similarity_cutoff, n_member_cutoff).  Returns labels of shape
-        [n_radii, n_cuts, n_points] (host numpy array unless a CUDA tensor
-        is given as labels_out).
+        [n_radii, n_cuts, n_points]: labels_out when given (a CUDA tensor,
+        or a C-contiguous int64 host array of that shape, e.g. in pinned
+        memory), else a new host numpy array.
         """
         rc = np.ascontiguousarray(radius_cutoffs, dtype=np.float64)
         sc = np.ascontiguousarray([c[0] for c in cuts], dtype=np.int64)
@@ -415,6 +417,13 @@ class Context:
         n = int(self._n_points)
         if labels_out is not None and is_device_array(labels_out):
             ptr, mem, out = device_pointer(labels_out, np.int64, writable=True), MEM_DEVICE, labels_out
+        elif labels_out is not None:
+            out = labels_out
+            if (not isinstance(out, np.ndarray) or out.dtype != np.int64 or not out.flags.c_contiguous
+                    or not out.flags.writeable or out.shape != (rc.shape[0], sc.shape[0], n)):
+                raise ValueError(f"labels_out: a writable C-contiguous int64 array of shape "
+                                 f"{(rc.shape[0], sc.shape[0], n)} is needed")
+            ptr, mem = out.ctypes.data, MEM_HOST
         else:
             out = np.empty((rc.shape[0], sc.shape[0], n), dtype=np.int64)
             ptr, mem = out.ctypes.data, MEM_HOST

@@ -91,6 +91,7 @@ CNN_API cnn_status cnn_create(cnn_context **out, int device, void *stream) {
     ctx->device = device;
     if (const char *pz = getenv("CNN_DEBUG_POISON")) ctx->poison = atoi(pz) & 0xff;
     if (const char *gr = getenv("CNN_GRID_REACH")) ctx->grid_reach = atoi(gr) == 2 ? 2 : 1;
+    if (const char *sg = getenv("CNN_SWEEP_GRAPH")) ctx->sweep_graphs = atoi(sg) != 0;
     int sms = 0;
     if (cudaSetDevice(device) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1) {
@@ -156,6 +157,8 @@ CNN_API cnn_status cnn_destroy(cnn_context *ctx) {
                            &ctx->scratch_c, &ctx->scratch_d, &ctx->scan_tmp};
     for (cnn::DevBuf *b : bufs)
         if (b->ptr) cudaFree(b->ptr);
+    for (void *p : ctx->deferred_free) cudaFree(p);
+    if (ctx->sweep_exec) cudaGraphExecDestroy(ctx->sweep_exec);
     for (int i = 0; i < cnn_context::kSlots; ++i) {
         if (ctx->ev_begin[i]) cudaEventDestroy(ctx->ev_begin[i]);
         if (ctx->ev_end[i]) cudaEventDestroy(ctx->ev_end[i]);

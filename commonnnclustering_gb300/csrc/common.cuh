@@ -94,6 +94,15 @@ struct cnn_context {
     int64_t wait_limit_ns = 0;  // > 0: limit of the bounded waits in the kernels (cnn_set_wait_limit)
     int search_pref = CNN_SEARCH_AUTO;  // cnn_set_search
     int grid_reach = 1;  // cell edge R / grid_reach (CNN_GRID_REACH=1|2 at creation)
+    // CUDA-graph capture of the sweep's fits (sweep.cu).  While capturing,
+    // a buffer that has to grow gets new memory and the old block is kept
+    // (captured work refers to it) until the graph has run.
+    bool sweep_graphs = true;  // CNN_SWEEP_GRAPH=0 at creation: plain launches
+    bool capturing = false;
+    std::vector<void *> deferred_free;
+    // the last sweep's instantiated graph: a sweep of the same shape updates
+    // its parameters (cudaGraphExecUpdate) instead of instantiating anew
+    cudaGraphExec_t sweep_exec = nullptr;
     int64_t n_launches = 0;
     std::string last_error;
     cnn_stats stats{};
@@ -202,9 +211,13 @@ struct cnn_context {
     cnn_status ensure(cnn::DevBuf &b, size_t bytes) {
         if (bytes <= b.cap) return CNN_OK;
         if (b.ptr) {
-            cudaError_t e = cudaStreamSynchronize(stream);
-            if (e != cudaSuccess) return fail(CNN_ERR_CUDA, cudaGetErrorString(e));
-            cudaFree(b.ptr);
+            if (capturing) {
+                deferred_free.push_back(b.ptr);  // freed after the captured graph has run
+            } else {
+                cudaError_t e = cudaStreamSynchronize(stream);
+                if (e != cudaSuccess) return fail(CNN_ERR_CUDA, cudaGetErrorString(e));
+                cudaFree(b.ptr);
+            }
             b.ptr = nullptr;
             b.cap = 0;
         }
@@ -235,9 +248,10 @@ namespace cnn {
 cnn_status scan_exclusive_i64(cnn_context *ctx, const int64_t *in, int64_t *out, int64_t n);
 cnn_status scan_exclusive_i32_to_i64(cnn_context *ctx, const int32_t *in, int64_t *out, int64_t n);
 // sorted: if given, receives the buffer holding the result (keys or scratch_c,
-// valid until scratch_c is next used) and the final copy back is skipped
+// valid until scratch_c is next used) and the final copy back is skipped;
+// n_dev: the key count read on the device (at most n; grids sized for n)
 cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits, int first_bit = 0,
-                          uint64_t **sorted = nullptr);
+                          uint64_t **sorted = nullptr, const int64_t *n_dev = nullptr);
 // Copies `bytes` from the device to `host` and waits (through the pinned
 // bounce buffer when it fits, else a plain copy).
 cnn_status read_back(cnn_context *ctx, void *host, const void *dev, size_t bytes);
@@ -303,6 +317,10 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
 // still cross -- those a finished fit refining this one left open
 cnn_status open_pairs_impl(cnn_context *ctx, const int2 *in_list, const unsigned long long *in_count, int2 *out,
                            unsigned long long *out_count, int64_t cap);
+// sort_by_size of the labels a fit from fresh labels just wrote (no host
+// round trip; fit.cu)
+cnn_status sort_fresh_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64_t member_cutoff,
+                           int64_t max_clusters);
 cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels_dev, int64_t n,
                              int64_t member_cutoff, int64_t max_clusters);
 cnn_status check_lists_impl(cnn_context *ctx, const int32_t *a, int64_t na, const int32_t *b,

@@ -461,6 +461,76 @@ __global__ void apply_dense_kernel(int64_t *__restrict__ labels, int64_t n, int6
     }
 }
 
+// ---- sort_by_size of fresh labels, without a host round trip --------------
+// After a fit from fresh labels (all 0, current_start 1) the clusters are
+// 1..k in order of their lowest point index, so the first occurrence order
+// is the label order and k is known on the device (the fit's rank total).
+// Sizes are counted per label; keys (n - size, label - 1) of labels 1..k are
+// radix-sorted on the size bits only (the label bits are ascending already);
+// key q gives its label the new label q + 1, or 0 past max_clusters or
+// below member_cutoff -- the same rule as new_label_kernel.
+__global__ void fresh_count_kernel(const int64_t *__restrict__ labels, int64_t n, int32_t *__restrict__ cnt) {
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+        const int64_t i = base + lane;
+        const int64_t v = i < n ? labels[i] : 0;
+        const unsigned peers = __match_any_sync(0xffffffffu, v);
+        if (v > 0 && v <= n && lane == __ffs(peers) - 1) atomicAdd(&cnt[v - 1], __popc(peers));
+    }
+}
+
+// Up to kOrderSmall labels: every block holds all keys in shared memory and
+// its warps rank a slice of the labels (as order_small_kernel does); the
+// count k_big for the radix path is k when k is larger, else 0.
+__global__ void __launch_bounds__(kOrderThreads) fresh_order_small_kernel(
+    const int32_t *__restrict__ cnt, const int64_t *__restrict__ k_dev, int64_t n, int bits_n, int64_t member_cutoff,
+    int64_t max_clusters, int64_t *__restrict__ newlab, int64_t *__restrict__ k_big) {
+    extern __shared__ uint64_t s_keys[];  // [min(n, kOrderSmall)]
+    const int64_t k = *k_dev < n ? *k_dev : n;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *k_big = k > kOrderSmall ? k : 0;
+    if (k > kOrderSmall || k <= 0) return;
+    const int kk = (int)k;
+    const int per_block = (kk + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int v0 = (int)blockIdx.x * per_block;
+    if (v0 >= kk) return;  // block-uniform
+    for (int i = threadIdx.x; i < kk; i += blockDim.x) s_keys[i] = ((uint64_t)(n - cnt[i]) << bits_n) | (uint64_t)i;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int v_end = min(kk, v0 + per_block);
+    const int64_t maxc = max_clusters < 0 ? k : max_clusters;
+    for (int i = v0 + warp; i < v_end; i += nwarps) {
+        const uint64_t key = s_keys[i];
+        int below = 0;
+        for (int j = lane; j < kk; j += 32) below += s_keys[j] < key;
+        below = __reduce_add_sync(0xffffffffu, below);
+        if (lane != 0) continue;
+        const int64_t rank = below + 1;
+        newlab[i] = rank > maxc ? 0 : ((int64_t)cnt[i] >= member_cutoff ? rank : 0);
+    }
+}
+
+__global__ void fresh_keys_kernel(const int32_t *__restrict__ cnt, const int64_t *__restrict__ k_dev, int64_t n,
+                                  int bits_n, uint64_t *__restrict__ keys) {
+    const int64_t k = *k_dev < n ? *k_dev : n;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < k; q += (int64_t)gridDim.x * blockDim.x)
+        keys[q] = ((uint64_t)(n - cnt[q]) << bits_n) | (uint64_t)q;
+}
+
+__global__ void fresh_new_label_kernel(const uint64_t *__restrict__ keys, const int64_t *__restrict__ k_dev, int64_t n,
+                                       int bits_n, int64_t member_cutoff, int64_t max_clusters,
+                                       int64_t *__restrict__ newlab) {
+    const int64_t k = *k_dev < n ? *k_dev : n;
+    const int64_t maxc = max_clusters < 0 ? k : max_clusters;
+    const uint64_t mask = (1ull << bits_n) - 1;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < k; q += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t key = keys[q];
+        const int64_t size = n - (int64_t)(key >> bits_n);
+        const int64_t rank = q + 1;
+        newlab[key & mask] = (rank > maxc) ? 0 : (size >= member_cutoff ? rank : 0);
+    }
+}
+
 __global__ void apply_label_kernel(int64_t *__restrict__ labels, const int32_t *__restrict__ ids, int64_t n,
                                    const int64_t *__restrict__ newlab) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -738,6 +808,48 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64
     return CNN_OK;
 }
 
+// sort_by_size_impl for the labels of a fit from fresh labels that has just
+// run on this context (its rank total, the cluster count, is still in
+// scratch_a[n]): the same result, and the same work enqueued whatever the
+// labels hold, so that a sequence of fits can be captured as a CUDA graph.
+cnn_status sort_fresh_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64_t member_cutoff,
+                           int64_t max_clusters) {
+    cudaStream_t st = ctx->stream;
+    if (n <= 0) return CNN_OK;
+    if (n > INT32_MAX) return ctx->fail(CNN_ERR_UNSUPPORTED, "more than 2^31-1 labels");
+    stage_begin(ctx, 8);
+    const int64_t *k_dev = ctx->scratch_a.as<int64_t>() + n;
+    const int bits_n = bits_for_fit(n);
+    CNN_TRY(ctx->ensure(ctx->flag, sizeof(int32_t) * (size_t)(n + 1)));
+    CNN_TRY(ctx->ensure(ctx->io_b, sizeof(uint64_t) * (size_t)(n + 1) + 64));
+    CNN_TRY(ctx->ensure(ctx->scratch_b, sizeof(int64_t) * (size_t)n + 64));
+    int32_t *cnt = ctx->flag.as<int32_t>();
+    uint64_t *keys = ctx->io_b.as<uint64_t>();
+    int64_t *k_big = reinterpret_cast<int64_t *>(keys + n);  // k when above kOrderSmall, else 0
+    int64_t *newlab = ctx->scratch_b.as<int64_t>();
+    CNN_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (size_t)n, st));
+    fresh_count_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(labels, n, cnt);
+    CNN_LAUNCH_CHECK(ctx);
+    // at most kOrderSmall labels: ranked in shared memory; more: radix sort
+    // (both enqueued, each does nothing when the other applies)
+    const size_t keys_smem = sizeof(uint64_t) * (size_t)std::min<int64_t>(n, kOrderSmall);
+    CNN_TRY(allow_dynamic_smem(ctx, (const void *)fresh_order_small_kernel, keys_smem));
+    fresh_order_small_kernel<<<2 * ctx->sm_count, kOrderThreads, keys_smem, st>>>(
+        cnt, k_dev, n, bits_n, member_cutoff, max_clusters, newlab, k_big);
+    CNN_LAUNCH_CHECK(ctx);
+    fresh_keys_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(cnt, k_big, n, bits_n, keys);
+    CNN_LAUNCH_CHECK(ctx);
+    uint64_t *sorted = keys;
+    CNN_TRY(radix_sort_u64(ctx, keys, n, bits_n + bits_for_fit(n + 1), bits_n, &sorted, k_big));
+    fresh_new_label_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(sorted, k_big, n, bits_n, member_cutoff, max_clusters,
+                                                              newlab);
+    CNN_LAUNCH_CHECK(ctx);
+    apply_dense_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(labels, n, 1, newlab);
+    CNN_LAUNCH_CHECK(ctx);
+    stage_end(ctx, 8);
+    return CNN_OK;
+}
+
 // What Clustering.fit does around the fitter for fresh labels
 // (src/cnnclustering/cluster.pyx:316-364): labels 0, consider 1,
 // current_start 1, the fit, then sort_by_size.
@@ -753,7 +865,7 @@ cnn_status fit_and_sort_into(cnn_context *ctx, int64_t similarity_cutoff, int64_
     CNN_CUDA(ctx, cudaMemsetAsync(ctx->sweep_consider.ptr, 1, (size_t)n, st));
     CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, 1, ctx->sweep_consider.as<uint8_t>(), labels_dev,
                      seed_a, seed_b, edge_list, edge_count));
-    return sort ? sort_by_size_impl(ctx, labels_dev, n, sort_member_cutoff, max_clusters) : CNN_OK;
+    return sort ? sort_fresh_impl(ctx, labels_dev, n, sort_member_cutoff, max_clusters) : CNN_OK;
 }
 
 // The pairs the last fit left open, from the graph (in_list null) or from

@@ -143,9 +143,18 @@ constexpr int kRadixItems = 8;
 constexpr int kRadixTile = kRadixThreads * kRadixItems;  // 2048
 constexpr int kRadixWarps = kRadixThreads / 32;
 
-__global__ void __launch_bounds__(kRadixThreads) radix_hist_kernel(const uint64_t *__restrict__ keys, int64_t n,
-                                                                   int shift, int64_t ntiles,
-                                                                   int32_t *__restrict__ hist) {
+// n_dev (optional): the key count on the device, at most n (grids are sized
+// for n; tiles past the count hold no keys)
+__device__ __forceinline__ int64_t key_count(int64_t n, const int64_t *n_dev) {
+    if (!n_dev) return n;
+    const int64_t m = *n_dev;
+    return m < 0 ? 0 : (m < n ? m : n);
+}
+
+__global__ void __launch_bounds__(kRadixThreads) radix_hist_kernel(const uint64_t *__restrict__ keys, int64_t n_max,
+                                                                   const int64_t *__restrict__ n_dev, int shift,
+                                                                   int64_t ntiles, int32_t *__restrict__ hist) {
+    const int64_t n = key_count(n_max, n_dev);
     __shared__ int32_t h[256];
     h[threadIdx.x] = 0;
     __syncthreads();
@@ -163,9 +172,11 @@ __global__ void __launch_bounds__(kRadixThreads) radix_hist_kernel(const uint64_
 // shared memory, then written out so that consecutive threads write
 // consecutive addresses of each digit's run (coalesced stores).
 __global__ void __launch_bounds__(kRadixThreads, 2) radix_scatter_kernel(const uint64_t *__restrict__ keys,
-                                                                      uint64_t *__restrict__ out, int64_t n,
-                                                                      int shift, int64_t ntiles,
+                                                                      uint64_t *__restrict__ out, int64_t n_max,
+                                                                      const int64_t *__restrict__ n_dev, int shift,
+                                                                      int64_t ntiles,
                                                                       const int64_t *__restrict__ goff) {
+    const int64_t n = key_count(n_max, n_dev);
     __shared__ int32_t wcount[kRadixWarps][256];
     __shared__ int64_t tile_off[256];
     __shared__ int32_t digit_start[257];
@@ -260,7 +271,9 @@ cnn_status scan_exclusive_i32_to_i64(cnn_context *ctx, const int32_t *in, int64_
 // Up to kSmallSort keys: one block, bitonic sort in shared memory.
 constexpr int kSmallSort = 4096;
 
-__global__ void __launch_bounds__(1024) small_sort_kernel(uint64_t *__restrict__ keys, int n) {
+__global__ void __launch_bounds__(1024) small_sort_kernel(uint64_t *__restrict__ keys, int n_max,
+                                                          const int64_t *__restrict__ n_dev) {
+    const int n = (int)key_count(n_max, n_dev);
     __shared__ uint64_t s[kSmallSort];
     int m = 1;
     while (m < n) m <<= 1;
@@ -290,13 +303,16 @@ __global__ void __launch_bounds__(1024) small_sort_kernel(uint64_t *__restrict__
 // within equal higher bits, which the stable passes keep -- e.g. an index
 // in the low bits of keys built in index order).  Uses scratch_c/scratch_d
 // and the scan temp.
-cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits, int first_bit, uint64_t **sorted) {
+// n_dev (optional): the key count is read on the device (at most n), so the
+// sort enqueues the same work whatever the count -- no host round trip.
+cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits, int first_bit, uint64_t **sorted,
+                          const int64_t *n_dev) {
     if (sorted) *sorted = keys;
     if (n <= 1) return CNN_OK;
     if (bits < 1) bits = 1;
     if (bits > 64) bits = 64;
     if (n <= kSmallSort) {  // every key distinct or not, a full sort gives the same order
-        small_sort_kernel<<<1, 1024, 0, ctx->stream>>>(keys, (int)n);
+        small_sort_kernel<<<1, 1024, 0, ctx->stream>>>(keys, (int)n, n_dev);
         CNN_LAUNCH_CHECK(ctx);
         return CNN_OK;
     }
@@ -313,10 +329,11 @@ cnn_status radix_sort_u64(cnn_context *ctx, uint64_t *keys, int64_t n, int bits,
     const int passes = (bits - first_bit + 7) / 8;
     for (int p = 0; p < passes; ++p) {
         const int shift = first_bit + p * 8;
-        radix_hist_kernel<<<(unsigned)ntiles, kRadixThreads, 0, ctx->stream>>>(a, n, shift, ntiles, hist);
+        radix_hist_kernel<<<(unsigned)ntiles, kRadixThreads, 0, ctx->stream>>>(a, n, n_dev, shift, ntiles, hist);
         CNN_LAUNCH_CHECK(ctx);
         CNN_TRY(scan_impl<int32_t>(ctx, hist, goff, nh, 0));
-        radix_scatter_kernel<<<(unsigned)ntiles, kRadixThreads, 0, ctx->stream>>>(a, b, n, shift, ntiles, goff);
+        radix_scatter_kernel<<<(unsigned)ntiles, kRadixThreads, 0, ctx->stream>>>(a, b, n, n_dev, shift, ntiles,
+                                                                                 goff);
         CNN_LAUNCH_CHECK(ctx);
         uint64_t *t = a; a = b; b = t;
     }

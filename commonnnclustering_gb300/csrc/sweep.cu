@@ -15,6 +15,7 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <chrono>
 #include <vector>
 
 #include "common.cuh"
@@ -198,6 +199,75 @@ bool ladder_thresholds(const std::vector<double> &ext, const std::vector<double>
     return true;
 }
 
+// Runs `body` -- host logic that only enqueues work on the context stream --
+// as one CUDA graph: captured (relaxed mode: buffers may still grow, see
+// cnn_context::ensure), instantiated and launched.  With `keep`, the
+// instantiated graph stays with the context and the next call whose graph
+// has the same shape only updates its parameters (no new instantiation or
+// upload).  Where the stream cannot be captured or capture fails, nothing
+// captured has run and `body` runs again with plain launches; it must
+// therefore be repeatable from the same host state.
+template <class F>
+cnn_status run_as_graph(cnn_context *ctx, bool keep, F &&body) {
+    cudaStream_t st = ctx->stream;
+    if (!ctx->sweep_graphs || st == nullptr || st == cudaStreamLegacy || st == cudaStreamPerThread) return body();
+    const auto t0 = std::chrono::steady_clock::now();
+    const bool timing = ctx->timing;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return body();
+    }
+    ctx->capturing = true;
+    ctx->timing = false;  // stage events are not recorded inside a graph
+    const int64_t launches0 = ctx->n_launches;
+    const cnn_status s = body();
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(st, &graph);
+    ctx->capturing = false;
+    ctx->timing = timing;
+    cudaGraphExec_t exec = nullptr;
+    size_t nodes = 0;
+    bool ok = s == CNN_OK && e == cudaSuccess && graph != nullptr &&
+              cudaGraphGetNodes(graph, nullptr, &nodes) == cudaSuccess;
+    if (ok && keep && ctx->sweep_exec) {
+        cudaGraphExecUpdateResultInfo info{};
+        if (cudaGraphExecUpdate(ctx->sweep_exec, graph, &info) == cudaSuccess) {
+            exec = ctx->sweep_exec;  // same shape: parameters updated in place
+        } else {
+            (void)cudaGetLastError();
+            cudaGraphExecDestroy(ctx->sweep_exec);
+        }
+        ctx->sweep_exec = nullptr;
+    }
+    if (ok && !exec) ok = cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+    if (graph) cudaGraphDestroy(graph);
+    if (!ok) {
+        (void)cudaGetLastError();
+        if (exec) cudaGraphExecDestroy(exec);
+        for (void *p : ctx->deferred_free) cudaFree(p);  // nothing captured has run
+        ctx->deferred_free.clear();
+        ctx->n_launches = launches0;
+        return body();
+    }
+    const cudaError_t le = cudaGraphLaunch(exec, st);
+    if (keep && le == cudaSuccess) ctx->sweep_exec = exec;
+    else cudaGraphExecDestroy(exec);  // released once the launch completes
+    ctx->stats.graphs += 1;
+    ctx->stats.graph_nodes += (int64_t)nodes;
+    ctx->stats.ms_graph_build +=
+        std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (le != cudaSuccess) {
+        (void)cudaGetLastError();
+        return ctx->fail(CNN_ERR_CUDA, std::string("cudaGraphLaunch: ") + cudaGetErrorString(le));
+    }
+    if (!ctx->deferred_free.empty()) {  // the blocks replaced during capture
+        CNN_CUDA(ctx, cudaStreamSynchronize(st));
+        for (void *p : ctx->deferred_free) cudaFree(p);
+        ctx->deferred_free.clear();
+    }
+    return CNN_OK;
+}
+
 }  // namespace
 
 cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, const int64_t *sim_cut,
@@ -290,6 +360,21 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
         return CNN_OK;
     };
 
+    // The fits of one or more radii as one CUDA graph: every fit, its sort
+    // and the open-pair lists between fits enqueue the same work whatever
+    // the data (counts stay on the device), so the host logic of fit_cuts
+    // runs once at capture; a fallback repeats it from the same state.
+    ctx->stats.graphs = 0;
+    ctx->stats.graph_nodes = 0;
+    ctx->stats.ms_graph_build = 0.f;
+    auto fits_as_graph = [&](bool keep, auto &&fits) -> cnn_status {
+        const std::vector<char> have0 = have;
+        return run_as_graph(ctx, keep, [&]() -> cnn_status {
+            have = have0;
+            return fits();
+        });
+    };
+
     // one search, at the largest radius (the same search cnn_build_neighbours runs)
     CNN_TRY(build_neighbours_impl(ctx, rcs.back(), metric, fpmode));
     ctx->split_valid = false;  // the fits below see other graphs in the same arrays
@@ -309,7 +394,8 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
             if (k < n_radii - 1) CNN_TRY(build_neighbours_impl(ctx, rcs[k], metric, fpmode));
             else if (n_radii > 1) CNN_TRY(build_neighbours_impl(ctx, rcs.back(), metric, fpmode));
             // seeds across radii need the same internal order (identity here)
-            CNN_TRY(fit_cuts(k, prev_identity && ctx->identity_perm));
+            const bool same = prev_identity && ctx->identity_perm;
+            CNN_TRY(fits_as_graph(false, [&] { return fit_cuts(k, same); }));
             prev_identity = ctx->identity_perm;
         }
         return CNN_OK;
@@ -362,26 +448,40 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
                                                      ctx->sweep_multi_base.as<int64_t>(),
                                                      ctx->sweep_multi_cols.as<int32_t>());
             CNN_LAUNCH_CHECK(ctx);
-            // the fits of radius k see views of its arrays as the graph
-            cnn::DevBuf own_off = ctx->row_off, own_cols = ctx->cols, own_deg = ctx->deg;
-            for (int32_t k = 0; k < kf; ++k) {
-                ctx->row_off = cnn::DevBuf{off_all + (size_t)k * (n + 1), sizeof(int64_t) * (size_t)(n + 1)};
-                ctx->deg = cnn::DevBuf{deg_all + (size_t)k * (n + 1), sizeof(int32_t) * (size_t)(n + 1)};
-                ctx->cols = cnn::DevBuf{ctx->sweep_multi_cols.as<int32_t>() + base[k],
-                                        sizeof(int32_t) * (size_t)(nnz_k[k] > 0 ? nnz_k[k] : 1)};
-                ctx->nnz = nnz_k[k];
-                const cnn_status fs = fit_cuts(k, true);
+            // the fits of radius k see views of its arrays as the graph, the
+            // largest radius the kept graph itself; all 64 fits, one graph
+            const cnn::DevBuf own_off = ctx->row_off, own_cols = ctx->cols, own_deg = ctx->deg;
+            const cnn::DevBuf max_off = ctx->sweep_row_off_max, max_cols = ctx->sweep_cols_max,
+                              max_deg = ctx->sweep_deg_max;
+            auto all_fits = [&]() -> cnn_status {
+                cnn_status fs = CNN_OK;
+                for (int32_t k = 0; k < kf && fs == CNN_OK; ++k) {
+                    ctx->row_off = cnn::DevBuf{off_all + (size_t)k * (n + 1), sizeof(int64_t) * (size_t)(n + 1)};
+                    ctx->deg = cnn::DevBuf{deg_all + (size_t)k * (n + 1), sizeof(int32_t) * (size_t)(n + 1)};
+                    ctx->cols = cnn::DevBuf{ctx->sweep_multi_cols.as<int32_t>() + base[k],
+                                            sizeof(int32_t) * (size_t)(nnz_k[k] > 0 ? nnz_k[k] : 1)};
+                    ctx->nnz = nnz_k[k];
+                    fs = fit_cuts(k, true);
+                }
+                if (fs == CNN_OK) {
+                    ctx->row_off = max_off;
+                    ctx->cols = max_cols;
+                    ctx->deg = max_deg;
+                    ctx->nnz = nnz;
+                    fs = fit_cuts(kf, true);
+                }
                 ctx->row_off = own_off;
                 ctx->cols = own_cols;
                 ctx->deg = own_deg;
-                CNN_TRY(fs);
-            }
-            // the largest radius is the kept graph itself
+                return fs;
+            };
+            CNN_TRY(fits_as_graph(true, all_fits));
+            // the context keeps the largest-radius graph
             std::swap(ctx->row_off, ctx->sweep_row_off_max);
             std::swap(ctx->cols, ctx->sweep_cols_max);
             std::swap(ctx->deg, ctx->sweep_deg_max);
             ctx->nnz = nnz;
-            return fit_cuts(kf, true);
+            return CNN_OK;
         }
     }
     for (int32_t k = 0; k < n_radii; ++k) {
@@ -407,7 +507,8 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
             std::swap(ctx->deg, ctx->sweep_deg_max);
         }
         ctx->nnz = nnz_k;
-        CNN_TRY(fit_cuts(k, true));  // every radius keeps the largest-radius internal order
+        // every radius keeps the largest-radius internal order
+        CNN_TRY(fits_as_graph(false, [&] { return fit_cuts(k, true); }));
     }
     return CNN_OK;
 }

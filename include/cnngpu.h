@@ -133,6 +133,10 @@ typedef struct cnn_stats {
     float tune_ms_merge;      /* those times (search + fit), 0 otherwise */
     float tune_ms_bitset;
     float ms_weights;         /* cnn_mst_prim: the pair weights (full counts) */
+    int32_t graphs;           /* cnn_sweep / cnn_sweep_pairs: CUDA graphs the fits ran as
+                                 (0: launched one by one) */
+    int64_t graph_nodes;      /* kernels, copies and memsets in those graphs */
+    float ms_graph_build;     /* host time to capture and instantiate them */
 } cnn_stats;
 
 CNN_API int cnn_abi_version(void);

@@ -106,3 +106,47 @@ def test_radius_by_radius_equals_all_radii_at_once(cnn, monkeypatch):
     assert np.array_equal(at_once, one_by_one)
     for k, r in enumerate(radii):
         assert np.array_equal(at_once[k, 1], separate_fit(cnn, x, r, cuts[1], 3)), r
+
+
+@pytest.mark.parametrize("max_clusters", [None, 3])
+def test_sweep_as_cuda_graph_equals_plain_launches(cnn, monkeypatch, max_clusters):
+    """The sweep's fits run as captured CUDA graphs (the sort of each fit
+    enqueues the same work whatever the labels hold); with capture switched
+    off (CNN_SWEEP_GRAPH=0 at context creation) the same labels come out."""
+    from commonnnclustering_gb300 import _abi, workloads
+    x = workloads.nested3d(n=40000, seed=8, n_parents=8, box=3.0).astype(np.float64)
+    x2 = workloads.nested3d(n=40000, seed=11, n_parents=5, box=3.0).astype(np.float64)
+    r2 = [r * r for r in (0.03, 0.05, 0.08, 0.11)]
+    cuts = [(c + 2, c + 1) for c in (2, 5, 20, 60)]
+    out = {}
+    for graph in ("1", "0"):
+        monkeypatch.setenv("CNN_SWEEP_GRAPH", graph)
+        ctx = _abi.Context(0)
+        try:
+            # the second sweep on the same context reuses the instantiated
+            # graph with updated parameters (other points, other graph sizes)
+            for key, pts in ((graph, x), (graph + "b", x2)):
+                ctx.set_points(pts)
+                out[key] = ctx.sweep(r2, cuts, member_cutoff=5, max_clusters=max_clusters)
+                st = ctx.stats()
+                if graph == "1":
+                    assert st["graphs"] >= 1 and st["graph_nodes"] > 100
+                else:
+                    assert st["graphs"] == 0
+        finally:
+            ctx.close()
+    assert np.array_equal(out["1"], out["0"])
+    assert np.array_equal(out["1b"], out["0b"])
+    # and each equals a plain fit + sort_by_size on the same context type
+    ctx = _abi.Context(0)
+    try:
+        ctx.set_points(x)
+        for k, rc in enumerate(r2):
+            ctx.build_neighbours(rc)
+            for j, (sc, nm) in enumerate(cuts):
+                labels = np.zeros(x.shape[0], dtype=np.int64)
+                ctx.fit(sc, nm, 1, np.ones(x.shape[0], dtype=np.uint8), labels)
+                ctx.sort_by_size(labels, 5, max_clusters)
+                assert np.array_equal(out["1"][k, j], labels), (k, j)
+    finally:
+        ctx.close()
