@@ -268,7 +268,12 @@ CNN_API cnn_status cnn_check_lists(cnn_context *ctx, const int32_t *a, int64_t n
  * Every pair is fitted from fresh labels (current_start 1) and sorted with
  * (member_cutoff, max_clusters < 0: no limit); labels_out[(k * n_cuts + j) *
  * n_points + i] then equals what cnn_fit + cnn_sort_by_size give at radius
- * k and cut j.  The context keeps the largest-radius graph afterwards. */
+ * k and cut j.  The context keeps the largest-radius graph afterwards.
+ * The fits (with their sorts) enqueue no host round trip and run as one
+ * CUDA graph captured on the context's stream (kept by the context and
+ * updated for the next sweep of the same shape); CNN_SWEEP_GRAPH=0 in the
+ * environment at cnn_create runs them as plain launches.  cnn_stats.graphs,
+ * graph_nodes and ms_graph_build report it. */
 CNN_API cnn_status cnn_sweep(cnn_context *ctx, const double *radius_cutoffs, int32_t n_radii,
                              const int64_t *similarity_cutoffs, const int64_t *n_member_cutoffs,
                              int32_t n_cuts, cnn_metric metric, cnn_fpmode fpmode,
