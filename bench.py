@@ -651,12 +651,10 @@ def serve_record(W, args, peaks, dist=None, world=1, local=0, rank=0, cpu=True):
         # warm-up: every slot sees the largest jobs once (device workspaces grown)
         big = sorted(raw, key=lambda j: -j["points"].shape[0] * j["points"].shape[1])[: 2 * args.slots]
         srv.serve([serve.Job(job_id=-1 - i, **dict(j, arrival=0.0)) for i, j in enumerate(big)], realtime=False)
-        srv.done.clear()
         with clocks:
             for rate in W["rates"]:
                 n_jobs = W["n_jobs"] if rate >= 100 else min(W["n_jobs"], int(rate * 60))  # <= 60 s of arrivals
                 jobs = [serve.Job(job_id=i, **dict(raw[i], arrival=float(base[i] / rate))) for i in range(n_jobs)]
-                srv.done.clear()
                 srv.serve(jobs, realtime=True)
                 batched = serve.latency_summary(jobs)
                 plain_jobs = [serve.Job(job_id=i, **dict(raw[i], arrival=float(base[i] / rate)))
@@ -670,7 +668,9 @@ def serve_record(W, args, peaks, dist=None, world=1, local=0, rank=0, cpu=True):
                                 "jobs_differing": len(differ),
                                 "errors": sorted({a.error for a, _ in differ if a.error} |
                                                  {b.error for _, b in differ if b.error})[:3],
-                                "max_jobs_in_flight": srv.max_in_flight})
+                                "max_jobs_in_flight": srv.max_in_flight,
+                                "server": {k: srv.stats[k] for k in ("budget_bytes", "peak_held_bytes", "requeued",
+                                                                     "released", "failed")}})
     finally:
         srv.close()
     if rank != 0:

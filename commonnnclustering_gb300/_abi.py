@@ -20,6 +20,7 @@ import numpy as np
 from . import _build
 
 CNN_OK = 0
+CNN_ERR_INVALID_ARG, CNN_ERR_OOM, CNN_ERR_CUDA, CNN_ERR_TIMEOUT, CNN_ERR_UNSUPPORTED, CNN_ERR_STATE = 1, 2, 3, 4, 5, 6
 _STATUS = {1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "timeout",
            5: "unsupported", 6: "bad state"}
 
@@ -94,6 +95,41 @@ _P = ctypes.c_void_p
 _I64 = ctypes.c_int64
 _I32 = ctypes.c_int32
 _INT = ctypes.c_int
+class cnn_job(ctypes.Structure):
+    _fields_ = [
+        ("points", ctypes.c_void_p), ("dtype", ctypes.c_int), ("n_points", ctypes.c_int64),
+        ("n_dim", ctypes.c_int32), ("metric", ctypes.c_int), ("fpmode", ctypes.c_int),
+        ("radius_cutoff", ctypes.c_double), ("similarity_cutoff", ctypes.c_int64),
+        ("n_member_cutoff", ctypes.c_int64), ("member_cutoff", ctypes.c_int64), ("max_clusters", ctypes.c_int64),
+        ("labels", ctypes.c_void_p), ("reserve_bytes", ctypes.c_int64),
+    ]
+
+
+class cnn_job_info(ctypes.Structure):
+    _fields_ = [
+        ("state", ctypes.c_int), ("result", ctypes.c_int), ("slot", ctypes.c_int32), ("attempts", ctypes.c_int32),
+        ("reserved_bytes", ctypes.c_int64), ("t_submit", ctypes.c_double), ("t_start", ctypes.c_double),
+        ("t_done", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class cnn_server_stats(ctypes.Structure):
+    _fields_ = [
+        ("submitted", ctypes.c_int64), ("done", ctypes.c_int64), ("failed", ctypes.c_int64),
+        ("requeued", ctypes.c_int64), ("released", ctypes.c_int64), ("running", ctypes.c_int32),
+        ("queued", ctypes.c_int32), ("max_running", ctypes.c_int32), ("budget_bytes", ctypes.c_int64),
+        ("committed_bytes", ctypes.c_int64), ("held_bytes", ctypes.c_int64), ("peak_held_bytes", ctypes.c_int64),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+JOB_QUEUED, JOB_RUNNING, JOB_DONE = 0, 1, 2
+
 SIGNATURES = {
     "cnn_abi_version": (_INT, []),
     "cnn_create": (_INT, [ctypes.POINTER(_P), _INT, _P]),
@@ -122,6 +158,14 @@ SIGNATURES = {
     "cnn_set_periodic_bounds": (_INT, [_P, _P, _I32]),
     "cnn_predict": (_INT, [_P, _P, _INT, _I64, _I32, _P, _P, _I64, ctypes.c_double, _INT, _INT, _I64, _I64, _P, _P,
                            _INT]),
+    "cnn_server_create": (_INT, [ctypes.POINTER(_P), _INT, _I32, _I64]),
+    "cnn_server_destroy": (_INT, [_P]),
+    "cnn_submit": (_INT, [_P, ctypes.POINTER(cnn_job), ctypes.POINTER(_I64)]),
+    "cnn_poll": (_INT, [_P, _I64, ctypes.POINTER(cnn_job_info)]),
+    "cnn_wait": (_INT, [_P, _I64, _I64, ctypes.POINTER(cnn_job_info)]),
+    "cnn_job_error": (_INT, [_P, _I64, ctypes.c_char_p, _I64]),
+    "cnn_job_release": (_INT, [_P, _I64]),
+    "cnn_server_get_stats": (_INT, [_P, ctypes.POINTER(cnn_server_stats)]),
 }
 
 _lib = None
@@ -521,6 +565,93 @@ class Context:
                                               ctypes.c_void_p(b.ctypes.data), b.shape[0], int(c),
                                               ctypes.c_void_p(r.ctypes.data), MEM_HOST), "cnn_check_lists")
         return bool(r[0])
+
+
+class NativeServer:
+    """The library's job server (cnn_server_*): n_slots contexts with their
+    own streams and worker threads, admission under a device-memory budget
+    that bounds the bytes the workspaces really hold."""
+
+    def __init__(self, device: int = 0, n_slots: int = 4, budget_bytes: int = 32 << 30):
+        self._lib = load()
+        h = ctypes.c_void_p()
+        st = self._lib.cnn_server_create(ctypes.byref(h), int(device), int(n_slots), int(budget_bytes))
+        if st != CNN_OK:
+            raise CNNError(st, f"cnn_server_create(device={device}, n_slots={n_slots}) failed")
+        self._h = h
+        self._keep = {}  # job id -> the host arrays the job reads and writes
+
+    def submit(self, points, radius_cutoff: float, similarity_cutoff: int, n_member_cutoff: int,
+               member_cutoff: int = 2, max_clusters: Optional[int] = None, metric: int = METRIC_EUCLIDEAN_REDUCED,
+               fpmode: Optional[int] = None, reserve_bytes: int = 0, labels=None) -> int:
+        x = np.ascontiguousarray(points)
+        if x.dtype not in (np.float64, np.float32):
+            x = x.astype(np.float64)
+        if x.ndim != 2:
+            raise ValueError("points: a 2-D array [n_points, n_dim] is needed")
+        n = x.shape[0]
+        lab = np.empty(n, dtype=np.int64) if labels is None else labels
+        if lab.dtype != np.int64 or lab.shape != (n,) or not lab.flags.c_contiguous:
+            raise ValueError("labels: a C-contiguous int64 array of n_points entries is needed")
+        job = cnn_job(points=x.ctypes.data, dtype=DTYPE_F64 if x.dtype == np.float64 else DTYPE_F32, n_points=n,
+                      n_dim=x.shape[1], metric=int(metric), fpmode=host_fpmode(fpmode),
+                      radius_cutoff=float(radius_cutoff), similarity_cutoff=int(similarity_cutoff),
+                      n_member_cutoff=int(n_member_cutoff), member_cutoff=int(member_cutoff),
+                      max_clusters=-1 if max_clusters is None else int(max_clusters),
+                      labels=lab.ctypes.data, reserve_bytes=int(reserve_bytes))
+        jid = ctypes.c_int64()
+        st = self._lib.cnn_submit(self._h, ctypes.byref(job), ctypes.byref(jid))
+        if st != CNN_OK:
+            raise CNNError(st, "cnn_submit: invalid job")
+        self._keep[jid.value] = (x, lab)
+        return jid.value
+
+    def poll(self, job_id: int) -> dict:
+        info = cnn_job_info()
+        st = self._lib.cnn_poll(self._h, int(job_id), ctypes.byref(info))
+        if st != CNN_OK:
+            raise CNNError(st, f"cnn_poll({job_id})")
+        return info.as_dict()
+
+    def wait(self, job_id: int, timeout_s: Optional[float] = None):
+        """Blocks until the job is done; returns (labels, info).  A failed
+        job raises CNNError with its message."""
+        info = cnn_job_info()
+        ns = -1 if timeout_s is None else int(timeout_s * 1e9)
+        st = self._lib.cnn_wait(self._h, int(job_id), ns, ctypes.byref(info))
+        if st != CNN_OK:
+            raise CNNError(st, f"cnn_wait({job_id})")
+        d = info.as_dict()
+        if d["result"] != CNN_OK:
+            buf = ctypes.create_string_buffer(512)
+            self._lib.cnn_job_error(self._h, int(job_id), buf, 512)
+            self._lib.cnn_job_release(self._h, int(job_id))
+            self._keep.pop(job_id, None)
+            err = CNNError(d["result"], f"job {job_id}: {buf.value.decode()}")
+            err.info = d  # the job's times and slot
+            raise err
+        _, lab = self._keep.pop(job_id)
+        self._lib.cnn_job_release(self._h, int(job_id))
+        return lab, d
+
+    def stats(self) -> dict:
+        s = cnn_server_stats()
+        st = self._lib.cnn_server_get_stats(self._h, ctypes.byref(s))
+        if st != CNN_OK:
+            raise CNNError(st, "cnn_server_get_stats")
+        return s.as_dict()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.cnn_server_destroy(self._h)
+            self._h = None
+            self._keep.clear()
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 _tls = threading.local()

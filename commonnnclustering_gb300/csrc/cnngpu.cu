@@ -74,6 +74,59 @@ cnn_status stage_in(cnn_context *ctx, cnn::DevBuf &buf, const T *src, int64_t co
 
 using namespace cnn;
 
+namespace cnn {
+namespace {
+
+std::vector<DevBuf *> workspace_buffers(cnn_context *ctx) {
+    return {&ctx->x_own, &ctx->x_f32_stage, &ctx->perm, &ctx->inv, &ctx->deg, &ctx->row_off,
+                           &ctx->cols, &ctx->xf4, &ctx->cell_of, &ctx->cell_start, &ctx->grid_slot_base,
+                           &ctx->grid_slot_cols, &ctx->grid_qslot, &ctx->node, &ctx->parent,
+                           &ctx->comp_min, &ctx->flag, &ctx->counters, &ctx->stage_labels, &ctx->gram_hi, &ctx->gram_mid,
+                           &ctx->gram_lo, &ctx->gram_aux, &ctx->gram_keys, &ctx->gram_amb,
+                           &ctx->gram_blocks, &ctx->gram_tiles, &ctx->gram_perm, &ctx->pred_off, &ctx->pred_cols,
+                           &ctx->pred_xoff, &ctx->pred_xcols, &ctx->pred_x, &ctx->pred_set,
+                           &ctx->sweep_bucket, &ctx->sweep_row_off_max, &ctx->sweep_cols_max,
+                           &ctx->sweep_deg_max, &ctx->sweep_consider, &ctx->sweep_forest, &ctx->sweep_open_a,
+                           &ctx->sweep_multi_deg, &ctx->sweep_multi_off, &ctx->sweep_multi_cols, &ctx->sweep_multi_base,
+                           &ctx->sweep_open_b, &ctx->sweep_open_count,
+                           &ctx->stage_consider, &ctx->stage_offsets, &ctx->stage_indices, &ctx->stage_misc,
+                           &ctx->pcell, &ctx->mbase, &ctx->masks, &ctx->dist_own, &ctx->bounds_dev,
+                           &ctx->tune_consider, &ctx->tune_labels, &ctx->split,
+                           &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->scratch_a, &ctx->scratch_b,
+                           &ctx->scratch_c, &ctx->scratch_d, &ctx->scan_tmp};
+}
+
+}  // namespace
+
+cnn_status release_workspace(cnn_context *ctx) {
+    CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (DevBuf *b : workspace_buffers(ctx)) {
+        if (b->ptr) cudaFree(b->ptr);
+        *b = DevBuf{};
+    }
+    for (void *p : ctx->deferred_free) cudaFree(p);
+    ctx->deferred_free.clear();
+    if (ctx->sweep_exec) {
+        cudaGraphExecDestroy(ctx->sweep_exec);
+        ctx->sweep_exec = nullptr;
+    }
+    ctx->mem_held = 0;
+    ctx->have_graph = false;
+    ctx->graph_mask = false;
+    ctx->csr_valid = true;
+    ctx->split_valid = false;
+    ctx->tune_pending = false;
+    ++ctx->graph_generation;
+    ctx->x = nullptr;
+    ctx->n = 0;
+    ctx->d = 0;
+    ctx->dist = nullptr;
+    ctx->dist_set = false;
+    return CNN_OK;
+}
+
+}  // namespace cnn
+
 extern "C" {
 
 CNN_API int cnn_abi_version(void) { return CNN_ABI_VERSION; }
@@ -139,23 +192,7 @@ CNN_API cnn_status cnn_destroy(cnn_context *ctx) {
     if (!ctx) return CNN_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    cnn::DevBuf *bufs[] = {&ctx->x_own, &ctx->x_f32_stage, &ctx->perm, &ctx->inv, &ctx->deg, &ctx->row_off,
-                           &ctx->cols, &ctx->xf4, &ctx->cell_of, &ctx->cell_start, &ctx->grid_slot_base,
-                           &ctx->grid_slot_cols, &ctx->grid_qslot, &ctx->node, &ctx->parent,
-                           &ctx->comp_min, &ctx->flag, &ctx->counters, &ctx->stage_labels, &ctx->gram_hi, &ctx->gram_mid,
-                           &ctx->gram_lo, &ctx->gram_aux, &ctx->gram_keys, &ctx->gram_amb,
-                           &ctx->gram_blocks, &ctx->gram_tiles, &ctx->gram_perm, &ctx->pred_off, &ctx->pred_cols,
-                           &ctx->pred_xoff, &ctx->pred_xcols, &ctx->pred_x, &ctx->pred_set,
-                           &ctx->sweep_bucket, &ctx->sweep_row_off_max, &ctx->sweep_cols_max,
-                           &ctx->sweep_deg_max, &ctx->sweep_consider, &ctx->sweep_forest, &ctx->sweep_open_a,
-                           &ctx->sweep_multi_deg, &ctx->sweep_multi_off, &ctx->sweep_multi_cols, &ctx->sweep_multi_base,
-                           &ctx->sweep_open_b, &ctx->sweep_open_count,
-                           &ctx->stage_consider, &ctx->stage_offsets, &ctx->stage_indices, &ctx->stage_misc,
-                           &ctx->pcell, &ctx->mbase, &ctx->masks, &ctx->dist_own, &ctx->bounds_dev,
-                           &ctx->tune_consider, &ctx->tune_labels, &ctx->split,
-                           &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->scratch_a, &ctx->scratch_b,
-                           &ctx->scratch_c, &ctx->scratch_d, &ctx->scan_tmp};
-    for (cnn::DevBuf *b : bufs)
+    for (cnn::DevBuf *b : cnn::workspace_buffers(ctx))
         if (b->ptr) cudaFree(b->ptr);
     for (void *p : ctx->deferred_free) cudaFree(p);
     if (ctx->sweep_exec) cudaGraphExecDestroy(ctx->sweep_exec);

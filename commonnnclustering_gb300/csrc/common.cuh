@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -103,6 +104,13 @@ struct cnn_context {
     // the last sweep's instantiated graph: a sweep of the same shape updates
     // its parameters (cudaGraphExecUpdate) instead of instantiating anew
     cudaGraphExec_t sweep_exec = nullptr;
+    // device bytes the workspace holds, and an optional limit on them (a
+    // served job's reservation): a growth past mem_cap fails with
+    // CNN_ERR_OOM before cudaMalloc and sets cap_hit
+    std::atomic<int64_t> mem_held{0};  // read by a server's dispatcher while the slot runs
+    int64_t mem_cap = 0;                // 0: no limit
+    bool cap_hit = false;
+    int64_t cap_need = 0;               // the holding the refused growth asked for
     int64_t n_launches = 0;
     std::string last_error;
     cnn_stats stats{};
@@ -210,7 +218,17 @@ struct cnn_context {
     }
     cnn_status ensure(cnn::DevBuf &b, size_t bytes) {
         if (bytes <= b.cap) return CNN_OK;
+        size_t want = bytes < 256 ? 256 : bytes;
+        want = (want + 255) & ~size_t(255);
+        const int64_t after = mem_held.load() - (int64_t)b.cap + (int64_t)want;
+        if (mem_cap > 0 && after > mem_cap) {
+            cap_hit = true;
+            cap_need = after;
+            return fail(CNN_ERR_OOM, "workspace limit: " + std::to_string(after) + " bytes needed, " +
+                                         std::to_string(mem_cap) + " allowed");
+        }
         if (b.ptr) {
+            mem_held -= (int64_t)b.cap;
             if (capturing) {
                 deferred_free.push_back(b.ptr);  // freed after the captured graph has run
             } else {
@@ -221,8 +239,6 @@ struct cnn_context {
             b.ptr = nullptr;
             b.cap = 0;
         }
-        size_t want = bytes < 256 ? 256 : bytes;
-        want = (want + 255) & ~size_t(255);
         cudaError_t e = cudaMalloc(&b.ptr, want);
         if (e != cudaSuccess) {
             (void)cudaGetLastError();
@@ -231,6 +247,7 @@ struct cnn_context {
                         std::string("cudaMalloc(") + std::to_string(want) + "): " + cudaGetErrorString(e));
         }
         b.cap = want;
+        mem_held += (int64_t)want;
         if (poison >= 0) {
             // debugging aid: stale workspace contents must never change a result
             e = cudaMemsetAsync(b.ptr, poison, want, stream);
@@ -259,6 +276,11 @@ cnn_status read_back(cnn_context *ctx, void *host, const void *dev, size_t bytes
 cnn_status allow_dynamic_smem(cnn_context *ctx, const void *kernel, size_t bytes);
 cnn_status fill_i32(cnn_context *ctx, int32_t *p, int64_t n, int32_t v);
 cnn_status iota_i32(cnn_context *ctx, int32_t *p, int64_t n);
+
+// cnngpu.cu
+// Frees every workspace buffer of the context (after its stream is idle):
+// the graph and the points are gone, mem_held is 0.
+cnn_status release_workspace(cnn_context *ctx);
 
 // search.cu
 // form of a cell-grid graph: kFormLists (callers that walk the lists

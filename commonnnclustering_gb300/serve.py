@@ -1,14 +1,15 @@
 """A served stream of clustering jobs with continuous batching.
 
 Jobs (points + radius_cutoff, cnn_cutoff, member_cutoff) arrive over time.
-The server owns ``n_slots`` library contexts, each with its own CUDA stream
-and device-resident workspace that persists across jobs.  A dispatcher
-admits a waiting job as soon as a slot is free AND its estimated HBM
-footprint fits the remaining budget -- the oldest job first, and when the
-oldest does not fit yet, any later job that does (backfill), so small jobs
-keep flowing past a large one.  Admitted jobs run concurrently on their
-slots' streams; the host threads release the GIL inside every library call,
-so their copies and kernels overlap on the device.
+The library's job server (cnn_server_create / cnn_submit / cnn_wait, in
+csrc/server.cu) owns ``n_slots`` contexts, each with its own CUDA stream,
+device-resident workspace that persists across jobs, and a native worker
+thread.  It admits a waiting job as soon as a slot is free AND its
+reservation fits the budget -- the oldest job first, and when the oldest does
+not fit yet, any later job that does (backfill, bounded by aging), so small
+jobs keep flowing past a large one.  A running job's context cannot grow
+past its reservation, so the budget bounds the device memory really held,
+not an estimate.  Admitted jobs run concurrently on their slots' streams.
 
 Each job is one ``Clustering.fit`` (fresh labels, current_start 1, then
 sort_by_size) through the C ABI with host buffers, so its result does not
@@ -17,10 +18,8 @@ job alone against the same job in the mix.
 """
 from __future__ import annotations
 
-import collections
-import threading
 import time
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from typing import Callable, List, Optional
 
 import numpy as np
@@ -79,6 +78,12 @@ def run_job_alone(ctx: _abi.Context, job: Job) -> np.ndarray:
 
 
 class Server:
+    """Continuous batching through the library's job server (cnn_submit /
+    cnn_wait): ``n_slots`` contexts with their own streams and native worker
+    threads; admission under ``hbm_budget_bytes``, which bounds the device
+    bytes the slots' workspaces really hold (a job that outgrows its
+    estimate runs again alone with the whole budget)."""
+
     def __init__(self, n_slots: int = 4, hbm_budget_bytes: Optional[int] = None, device: int = 0,
                  backfill: bool = True):
         if hbm_budget_bytes is None:
@@ -89,74 +94,46 @@ class Server:
             except Exception:
                 hbm_budget_bytes = 32 << 30
         self.budget = int(hbm_budget_bytes)
-        self.in_use = 0
-        self.backfill = backfill
-        self.contexts = [_abi.Context(device) for _ in range(n_slots)]
-        self.free_slots = collections.deque(range(n_slots))
-        self.waiting: collections.deque = collections.deque()
-        self.cv = threading.Condition()
-        self.done: List[Job] = []
-        self.t0 = 0.0
+        self.backfill = backfill  # the library always backfills (bounded by aging)
+        self.native = _abi.NativeServer(device, n_slots, self.budget)
         self.max_in_flight = 0
-        self._in_flight = 0
-
-    def _admit_locked(self):
-        """Start every waiting job that fits (oldest first, then backfill)."""
-        started = True
-        while started and self.free_slots and self.waiting:
-            started = False
-            for idx, job in enumerate(self.waiting):
-                need = footprint_bytes(job.points.shape[0], job.points.shape[1], job.expected_degree)
-                if need <= self.budget - self.in_use or (self.in_use == 0 and need > self.budget):
-                    del self.waiting[idx]
-                    self.in_use += need
-                    slot = self.free_slots.popleft()
-                    job.slot = slot
-                    job.t_admit = time.perf_counter() - self.t0
-                    self._in_flight += 1
-                    self.max_in_flight = max(self.max_in_flight, self._in_flight)
-                    threading.Thread(target=self._run, args=(job, need), daemon=True).start()
-                    started = True
-                    break
-                if not self.backfill:
-                    break
-
-    def _run(self, job: Job, need: int):
-        try:
-            job.labels = run_job_alone(self.contexts[job.slot], job)
-        except Exception as e:  # the job fails alone; the server keeps going
-            job.error = f"{type(e).__name__}: {e}"
-        job.t_done = time.perf_counter() - self.t0
-        with self.cv:
-            self.in_use -= need
-            self.free_slots.append(job.slot)
-            self._in_flight -= 1
-            self.done.append(job)
-            self._admit_locked()
-            self.cv.notify_all()
+        self.stats = {}
 
     def serve(self, jobs: List[Job], realtime: bool = True, on_done: Optional[Callable] = None) -> List[Job]:
         """Feed jobs at their arrival times; return them when all are done."""
         jobs = sorted(jobs, key=lambda j: j.arrival)
-        self.t0 = time.perf_counter()
+        t0 = time.perf_counter()
+        ids = []
         for job in jobs:
             if realtime:
-                delay = job.arrival - (time.perf_counter() - self.t0)
+                delay = job.arrival - (time.perf_counter() - t0)
                 if delay > 0:
                     time.sleep(delay)
             else:
-                job.arrival = time.perf_counter() - self.t0
-            with self.cv:
-                self.waiting.append(job)
-                self._admit_locked()
-        with self.cv:
-            while len(self.done) < len(jobs):
-                self.cv.wait(timeout=1.0)
+                job.arrival = time.perf_counter() - t0
+            x = np.ascontiguousarray(job.points)
+            ids.append(self.native.submit(
+                x, job.radius_cutoff ** 2, job.cnn_cutoff + 2, job.cnn_cutoff + 1,
+                member_cutoff=2 if job.member_cutoff is None else job.member_cutoff,
+                reserve_bytes=footprint_bytes(x.shape[0], x.shape[1], job.expected_degree)))
+        for job, jid in zip(jobs, ids):
+            try:
+                job.labels, info = self.native.wait(jid)
+            except _abi.CNNError as e:  # the job fails alone; the server keeps going
+                job.error = str(e)
+                info = e.info
+            # the library's clock: start and end relative to the submission
+            job.slot = info.get("slot")
+            job.t_admit = job.arrival + (info["t_start"] - info["t_submit"])
+            job.t_done = job.arrival + (info["t_done"] - info["t_submit"])
+            if on_done is not None:
+                on_done(job)
+        self.stats = self.native.stats()
+        self.max_in_flight = self.stats["max_running"]
         return jobs
 
     def close(self):
-        for c in self.contexts:
-            c.close()
+        self.native.close()
 
 
 def serve_one_at_a_time(jobs: List[Job], device: int = 0, realtime: bool = True) -> List[Job]:

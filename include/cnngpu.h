@@ -383,6 +383,93 @@ CNN_API cnn_status cnn_fit_csr_noalloc(const int64_t *offsets, const int32_t *in
                                        int64_t n_member_cutoff, int64_t current_start,
                                        uint8_t *consider, int64_t *labels, void *stream);
 
+/* ---- Served job stream (continuous batching) ------------------------------
+ * A server runs many Clustering.fit jobs concurrently on one device
+ * (src/cnnclustering/cluster.pyx:256-392 per job, fresh labels): n_slots
+ * contexts, each with its own stream and workspace kept between jobs, and
+ * one host worker thread per slot.  cnn_submit queues a job and returns at
+ * once; jobs start oldest first as slots free up, and later jobs pass one
+ * that does not fit the memory budget yet (up to 64 times, then it waits at
+ * the head until it fits).  Each job's labels equal cnn_set_points +
+ * cnn_build_neighbours + cnn_fit (fresh labels, current_start 1) +
+ * cnn_sort_by_size run alone.
+ *
+ * Memory: the device bytes the slots' workspaces hold never exceed
+ * budget_bytes.  A running job holds a reservation its context cannot grow
+ * past (checked before any allocation): what its slot already holds plus
+ * the job's need; idle slots count with what they hold and are released
+ * when a waiting job needs the room.  The need starts from
+ * job->reserve_bytes (or an estimate from n_points and n_dim when 0),
+ * scaled by what earlier jobs of the same kind (n_dim <= 3, < 16, >= 16)
+ * needed beyond their estimates.  A job that outgrows its reservation is
+ * queued again at the head with at least twice the need
+ * (cnn_job_info.attempts counts the starts); once the need reaches the
+ * budget the job runs alone, and fails with CNN_ERR_OOM only if the whole
+ * budget is too small.
+ *
+ * Host buffers: points and labels are host memory owned by the caller and
+ * must stay valid until the job is done; labels[n_points] is written by the
+ * job.  Threads: every entry point may be called from any thread. */
+typedef struct cnn_server cnn_server;
+
+typedef struct cnn_job {
+    const void *points;          /* host, row-major [n_points x n_dim] */
+    cnn_dtype dtype;
+    int64_t n_points;
+    int32_t n_dim;
+    cnn_metric metric;           /* EUCLIDEAN_REDUCED or EUCLIDEAN */
+    cnn_fpmode fpmode;
+    double radius_cutoff;        /* adjusted, as make_parameters gives it */
+    int64_t similarity_cutoff;   /* as make_parameters gives them */
+    int64_t n_member_cutoff;
+    int64_t member_cutoff;       /* sort_by_size; < 0: labels left unsorted */
+    int64_t max_clusters;        /* sort_by_size; < 0: no limit */
+    int64_t *labels;             /* host [n_points], written when the job is done */
+    int64_t reserve_bytes;       /* first reservation; 0: estimated */
+} cnn_job;
+
+typedef enum cnn_job_state {
+    CNN_JOB_QUEUED = 0,
+    CNN_JOB_RUNNING = 1,
+    CNN_JOB_DONE = 2
+} cnn_job_state;
+
+typedef struct cnn_job_info {
+    cnn_job_state state;
+    cnn_status result;           /* of a done job */
+    int32_t slot;                /* of the last start, -1 before */
+    int32_t attempts;            /* starts: 2 when the job outgrew its first reservation */
+    int64_t reserved_bytes;      /* reservation of the last start */
+    double t_submit, t_start, t_done;  /* seconds since cnn_server_create */
+} cnn_job_info;
+
+typedef struct cnn_server_stats {
+    int64_t submitted, done, failed;
+    int64_t requeued;            /* jobs that outgrew their first reservation */
+    int64_t released;            /* idle workspaces released to make room */
+    int32_t running, queued, max_running;
+    int64_t budget_bytes;
+    int64_t committed_bytes;     /* running reservations + idle holdings, now */
+    int64_t held_bytes;          /* device bytes the slots' workspaces hold, now */
+    int64_t peak_held_bytes;     /* largest held_bytes seen (at job ends and here) */
+} cnn_server_stats;
+
+CNN_API cnn_status cnn_server_create(cnn_server **out, int device, int32_t n_slots,
+                                     int64_t budget_bytes);
+/* Waits for every submitted job, then frees the server. */
+CNN_API cnn_status cnn_server_destroy(cnn_server *srv);
+CNN_API cnn_status cnn_submit(cnn_server *srv, const cnn_job *job, int64_t *job_id);
+CNN_API cnn_status cnn_poll(cnn_server *srv, int64_t job_id, cnn_job_info *info);
+/* Blocks until the job is done (timeout_ns < 0: no limit); CNN_ERR_TIMEOUT
+ * when the limit passes first (info then holds the current state). */
+CNN_API cnn_status cnn_wait(cnn_server *srv, int64_t job_id, int64_t timeout_ns,
+                            cnn_job_info *info);
+/* The message of a failed job (empty when it succeeded). */
+CNN_API cnn_status cnn_job_error(cnn_server *srv, int64_t job_id, char *buf, int64_t size);
+/* Forgets a done job (its id is invalid afterwards). */
+CNN_API cnn_status cnn_job_release(cnn_server *srv, int64_t job_id);
+CNN_API cnn_status cnn_server_get_stats(cnn_server *srv, cnn_server_stats *out);
+
 #ifdef __cplusplus
 }
 #endif
