@@ -63,6 +63,12 @@ struct GridGeom {
     int32_t g[3];      // cells per dimension (1 for unused dimensions)
     int64_t ncells;    // g0*g1*g2; bucket ncells holds non-finite points
     int32_t reach;     // neighbours lie at most `reach` cells apart (h >= R / reach)
+    // periodic metric: bit k of `wrap` = dimension k wraps around its box
+    // length L[k]; its coordinates are binned as x - L floor(x / L) into
+    // g[k] >= 3 cells of edge L / g[k] >= h, neighbouring cyclically
+    int32_t wrap;
+    double L[3];
+    double inv_hk[3];  // cell coordinate = floor(v * inv_hk[k]) (v = x - lo, or the wrapped x)
 };
 
 // The cell-grid neighbour graph as bit masks (fit_mask.cu): a point of cell

@@ -28,6 +28,7 @@
 // (perm: internal -> point index).  Intersections and connected
 // components are invariant under that relabelling; export to point order
 // happens only on request (cnn_get_neighbours).
+#include <limits.h>
 #include <math.h>
 
 #include <algorithm>
@@ -47,6 +48,10 @@ struct SearchParams {
     float thr_out;    // sf >  thr_out -> not a neighbour; else float64
     const double *bd = nullptr;  // periodic metric: box length per dimension (<= 0: not periodic)
     const float *bf = nullptr;   // the same in float32
+    // wrapped cell grid: float32 box length and half length per dimension
+    // (0 and +inf for dimensions that do not wrap)
+    float wl[3] = {0.f, 0.f, 0.f};
+    float whalf[3] = {INFINITY, INFINITY, INFINITY};
 };
 
 // Minimum-image difference of the periodic metric, reference order
@@ -141,6 +146,22 @@ __device__ __forceinline__ int32_t cell_coord(double v, double lo, double inv_h,
     return (int32_t)c;
 }
 
+// A coordinate of a wrapping dimension mapped into the box [0, L): the
+// minimum-image difference of two points equals the cyclic distance of
+// their mapped coordinates (up to a few ulps of max(|x|, L)).
+__device__ __forceinline__ double wrap_coord(double v, double L) { return v - L * floor(v / L); }
+
+// Cell coordinate of dimension k (wrapping or not), clamped to the grid.
+__device__ __forceinline__ int32_t cell_coord_k(double v, const GridGeom &geo, int k) {
+    if ((geo.wrap >> k) & 1) {
+        double c = floor(wrap_coord(v, geo.L[k]) * geo.inv_hk[k]);
+        if (!(c >= 0.0)) c = 0.0;
+        if (c > (double)(geo.g[k] - 1)) c = (double)(geo.g[k] - 1);
+        return (int32_t)c;
+    }
+    return cell_coord(v, geo.lo[k], geo.inv_hk[k], geo.g[k]);
+}
+
 // cell of every point and its slot among the points of that cell (the
 // order of the atomic increments: any order serves, rows are sorted by
 // internal index whatever the order inside a cell)
@@ -155,7 +176,7 @@ __global__ void cell_assign_kernel(const double *__restrict__ x, int64_t n, int 
             id = geo.ncells;
         } else {
             int32_t c[3] = {0, 0, 0};
-            for (int k = 0; k < d; ++k) c[k] = cell_coord(x[i * d + k], geo.lo[k], geo.inv_h, geo.g[k]);
+            for (int k = 0; k < d; ++k) c[k] = cell_coord_k(x[i * d + k], geo, k);
             id = (int64_t)c[0] + (int64_t)geo.g[0] * ((int64_t)c[1] + (int64_t)geo.g[1] * c[2]);
         }
         cell_of[i] = (int32_t)id;
@@ -176,7 +197,9 @@ __global__ void place_kernel(const int32_t *__restrict__ cell_of, const int32_t 
         perm[p] = (int32_t)i;
         inv[i] = p;
         float v[3] = {0.f, 0.f, 0.f};
-        for (int k = 0; k < d; ++k) v[k] = (float)__dsub_rn(x[i * d + k], geo.lo[k]);
+        for (int k = 0; k < d; ++k)
+            v[k] = (geo.wrap >> k) & 1 ? (float)wrap_coord(x[i * d + k], geo.L[k])
+                                       : (float)__dsub_rn(x[i * d + k], geo.lo[k]);
         xf4[p] = make_float4(v[0], v[1], v[2], 0.f);
     }
 }
@@ -219,11 +242,51 @@ __global__ void item_fill_kernel(const int64_t *__restrict__ cell_start, int64_t
 
 // Candidate count of a cell: the points of the (2 reach + 1)^3 cells around
 // it (the same x-runs the search packs).
+// The runs of the stencil row (y, z) around x-cell cx on a wrapped grid
+// (reach 1): one run, or two where the three x-cells wrap around.
+__device__ __forceinline__ int wrapped_x_runs(int32_t cx, int32_t g0, bool wrap_x, int32_t *a, int32_t *b) {
+    if (wrap_x && cx == 0) {
+        a[0] = 0; b[0] = 1; a[1] = g0 - 1; b[1] = g0 - 1;
+        return 2;
+    }
+    if (wrap_x && cx == g0 - 1) {
+        a[0] = g0 - 2; b[0] = g0 - 1; a[1] = 0; b[1] = 0;
+        return 2;
+    }
+    a[0] = cx > 0 ? cx - 1 : 0;
+    b[0] = cx + 1 < g0 ? cx + 1 : g0 - 1;
+    return 1;
+}
+
+// neighbour row/plane index of c + dc, cyclic when the dimension wraps;
+// -1 outside a grid that does not
+__device__ __forceinline__ int32_t stencil_coord(int32_t c, int dc, int32_t g, bool wrap) {
+    int32_t v = c + dc;
+    if (wrap) return v < 0 ? v + g : (v >= g ? v - g : v);
+    return v < 0 || v >= g ? -1 : v;
+}
+
 __device__ __forceinline__ int64_t cell_candidates(int64_t cid, const GridGeom &geo,
                                                    const int64_t *__restrict__ cell_start) {
     const int32_t cx = (int32_t)(cid % geo.g[0]);
     const int32_t cy = (int32_t)((cid / geo.g[0]) % geo.g[1]);
     const int32_t cz = (int32_t)(cid / ((int64_t)geo.g[0] * geo.g[1]));
+    if (geo.wrap) {  // reach 1 (a wrapped grid is built with reach 1 only)
+        int32_t a[2], b[2];
+        const int nx = wrapped_x_runs(cx, geo.g[0], geo.wrap & 1, a, b);
+        int64_t total = 0;
+        for (int dz = -1; dz <= 1; ++dz) {
+            const int32_t z = stencil_coord(cz, dz, geo.g[2], (geo.wrap >> 2) & 1);
+            if (z < 0) continue;
+            for (int dy = -1; dy <= 1; ++dy) {
+                const int32_t y = stencil_coord(cy, dy, geo.g[1], (geo.wrap >> 1) & 1);
+                if (y < 0) continue;
+                const int64_t row = (int64_t)geo.g[0] * ((int64_t)y + (int64_t)geo.g[1] * z);
+                for (int r = 0; r < nx; ++r) total += cell_start[row + b[r] + 1] - cell_start[row + a[r]];
+            }
+        }
+        return total;
+    }
     const int S = geo.reach;
     const int32_t xlo = cx > S - 1 ? cx - S : 0;
     const int32_t xhi = cx + S < geo.g[0] ? cx + S : geo.g[0] - 1;
@@ -320,7 +383,10 @@ constexpr int kUnitSub = CNN_UNIT_SUB;  // 32-candidate steps per loop iteration
 #define CNN_UNIT_MIN_BLOCKS 4  // 64 registers: four blocks of eight warps per SM
 #endif
 
-template <int kMode>
+// kWrap: a wrapped grid (periodic metric, reach 1): up to 18 runs (a 3-cell
+// x-run splits in two where it wraps), sorted by start so that the
+// concatenation stays ascending, and minimum-image float32 differences.
+template <int kMode, bool kWrap = false>
 __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_unit_kernel(
     const int2 *__restrict__ units, int64_t nunits, const double *__restrict__ x, int d, GridGeom geo,
     SearchParams sp, const int32_t *__restrict__ perm, const int64_t *__restrict__ cell_start,
@@ -336,9 +402,60 @@ __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_uni
     const int64_t q0 = unit.y;
     const int64_t cs = cell_start[cid], qend = cell_start[cid + 1];
     // run r = lane (r < nruns): (dz, dy) = (r / W - S, r % W - S); empty when outside the grid
-    const int S = geo.reach, Wd = 2 * S + 1, nruns = Wd * Wd;
+    const int S = geo.reach, Wd = 2 * S + 1;
+    const int nruns = kWrap ? 18 : Wd * Wd;
     int32_t rs = 0, len = 0;
-    if (lane < nruns) {
+    if (kWrap) {
+        // lanes 0..8 hold the (dz, dy) rows' runs, two where x wraps; every
+        // non-empty run goes to its rank by start (runs are disjoint), the
+        // rest of the 18 slots are empty
+        int32_t a0 = 0, l0 = 0, a1 = 0, l1 = 0;
+        if (lane < 9) {
+            const int32_t cx = cid % geo.g[0];
+            const int32_t cy = (cid / geo.g[0]) % geo.g[1];
+            const int32_t cz = cid / (geo.g[0] * geo.g[1]);
+            const int32_t z = stencil_coord(cz, lane / 3 - 1, geo.g[2], (geo.wrap >> 2) & 1);
+            const int32_t y = stencil_coord(cy, lane % 3 - 1, geo.g[1], (geo.wrap >> 1) & 1);
+            if (z >= 0 && y >= 0) {
+                int32_t xa[2], xb[2];
+                const int nx = wrapped_x_runs(cx, geo.g[0], geo.wrap & 1, xa, xb);
+                const int64_t row = (int64_t)geo.g[0] * ((int64_t)y + (int64_t)geo.g[1] * z);
+                a0 = (int32_t)cell_start[row + xa[0]];
+                l0 = (int32_t)(cell_start[row + xb[0] + 1] - a0);
+                if (nx > 1) {
+                    a1 = (int32_t)cell_start[row + xa[1]];
+                    l1 = (int32_t)(cell_start[row + xb[1] + 1] - a1);
+                }
+            }
+        }
+        const int32_t k0 = l0 > 0 ? a0 : INT_MAX, k1 = l1 > 0 ? a1 : INT_MAX;
+        int r0 = 0, r1 = 0;
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            const int32_t o0 = __shfl_sync(0xffffffffu, k0, j), o1 = __shfl_sync(0xffffffffu, k1, j);
+            r0 += (o0 < k0) + (o1 < k0);
+            r1 += (o0 < k1) + (o1 < k1);
+        }
+        if (lane < 18) {
+            s_rs[wid][lane] = 0;
+            s_cum[wid][lane + 1] = 0;  // lengths, in rank order, until the scan below
+        }
+        __syncwarp();
+        if (lane < 9 && l0 > 0) {
+            s_rs[wid][r0] = a0;
+            s_cum[wid][r0 + 1] = l0;
+        }
+        if (lane < 9 && l1 > 0) {
+            s_rs[wid][r1] = a1;
+            s_cum[wid][r1 + 1] = l1;
+        }
+        __syncwarp();
+        if (lane < 18) {
+            rs = s_rs[wid][lane];
+            len = s_cum[wid][lane + 1];
+        }
+        __syncwarp();
+    } else if (lane < nruns) {
         const int32_t cx = cid % geo.g[0];
         const int32_t cy = (cid / geo.g[0]) % geo.g[1];
         const int32_t cz = cid / (geo.g[0] * geo.g[1]);
@@ -418,7 +535,15 @@ __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_uni
             const float4 cf = t < total ? xf4[j[u]] : make_float4(INFINITY, INFINITY, INFINITY, 0.f);  // +inf never matches
 #pragma unroll
             for (int k = 0; k < kUnitQueries; ++k) {
-                const float ex = qx[k] - cf.x, ey = qy[k] - cf.y, ez = qz[k] - cf.z;
+                float ex = qx[k] - cf.x, ey = qy[k] - cf.y, ez = qz[k] - cf.z;
+                if (kWrap) {  // minimum image of wrapped coordinates (both in [0, L))
+                    ex = fabsf(ex);
+                    ey = fabsf(ey);
+                    ez = fabsf(ez);
+                    if (ex > sp.whalf[0]) ex = sp.wl[0] - ex;
+                    if (ey > sp.whalf[1]) ey = sp.wl[1] - ey;
+                    if (ez > sp.whalf[2]) ez = sp.wl[2] - ez;
+                }
                 const float sf = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
                 in[u][k] = sf <= sp.thr_in;
                 amb[u][k] = !in[u][k] && sf <= sp.thr_out;
@@ -901,11 +1026,21 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     std::vector<double> ext(d);
     for (int k = 0; k < d; ++k) ext[k] = std::max(std::fabs(hi[k] - lo[k]), 0.0);
     for (int k = 0; k < 3; ++k) ctx->grid_extent[k] = k < d ? ext[k] : 0.0;
+    // periodic dimensions: the float32 values are either x - lo (all-pairs
+    // search) or x mapped into [0, L) (wrapped grid; mapping error a few
+    // ulps of max |x|): the bound takes the larger magnitude of the two
+    std::vector<double> ext_f = ext;
+    if (periodic)
+        for (int k = 0; k < d; ++k) {
+            const double L = ctx->periodic_bounds[k];
+            if (L > 0)
+                ext_f[k] = std::max(ext[k], L + ldexp(std::max(std::fabs(lo[k]), std::fabs(hi[k])), -28));
+        }
     double band = 0;
     bool filt = false;
     if (radius_ok && (metric == CNN_METRIC_EUCLIDEAN_REDUCED || metric == CNN_METRIC_EUCLIDEAN || periodic)) {
         const double rc2 = metric == CNN_METRIC_EUCLIDEAN ? radius_cutoff * radius_cutoff : radius_cutoff;
-        filt = filter_thresholds(ext, R, rc2, &sp.thr_in, &sp.thr_out, &band,
+        filt = filter_thresholds(ext_f, R, rc2, &sp.thr_in, &sp.thr_out, &band,
                                  periodic ? &ctx->periodic_bounds : nullptr);
     }
     if (!radius_ok && !radius_inf) {
@@ -919,29 +1054,52 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
 
     // ---- choose the search
     GridGeom geo{};
-    bool use_grid = d <= 3 && radius_ok && R > 0 && isfinite(R) && !periodic && !all_pairs;
+    bool use_grid = d <= 3 && radius_ok && R > 0 && isfinite(R) && !all_pairs;
+    if (use_grid && periodic) {
+        // a wrapped grid (reach 1): every periodic dimension's mapping into
+        // [0, L) must be exact to far below the 1e-6 R by which cells exceed
+        // R, and each needs at least 3 cells (checked below)
+        for (int k = 0; k < d; ++k) {
+            const double L = ctx->periodic_bounds[k];
+            if (L > 0 && (!(L < 1e30) || !(ldexp(std::max(std::fabs(lo[k]), std::fabs(hi[k])) + L, -50) < 1e-7 * R)))
+                use_grid = false;
+        }
+    }
     if (use_grid) {
         // cells of edge h >= R / reach: a qualifying pair lies at most `reach`
         // cells apart in every dimension; reach 2 scans (5/2)^3 = 15.6 R^3
         // around a point instead of 27 R^3 (fewer candidates per neighbour)
-        geo.reach = ctx->grid_reach;
+        geo.reach = periodic ? 1 : ctx->grid_reach;
         double h = R / geo.reach * (1.0 + 1e-6);
+        auto wraps = [&](int k) { return periodic && k < d && ctx->periodic_bounds[k] > 0; };
         // cells cost 12 bytes each (count + start); allow up to 64 per point
         // (at most 64M) so sparse sets in large boxes keep cells of edge ~R
         const double max_cells = std::max<double>(std::min<double>(64.0 * (double)n, 67108864.0), 4096.0);
         for (int attempt = 0; attempt < 200; ++attempt) {
             double cells = 1;
             for (int k = 0; k < 3; ++k) {
-                double g = k < d ? floor(ext[k] / h) + 1.0 : 1.0;
-                geo.g[k] = (int32_t)std::min(g, 2.0e9);
-                cells *= g;
+                // a wrapping dimension: floor(L / h) cells of edge L / g >= h
+                double g = k >= d ? 1.0 : wraps(k) ? floor(ctx->periodic_bounds[k] / h) : floor(ext[k] / h) + 1.0;
+                geo.g[k] = (int32_t)std::max(1.0, std::min(g, 2.0e9));
+                cells *= std::max(g, 1.0);
             }
             if (cells <= max_cells && cells < 2.0e9) break;
             h *= 1.25;
         }
         geo.h = h;
         geo.inv_h = 1.0 / h;
-        for (int k = 0; k < 3; ++k) geo.lo[k] = k < d ? lo[k] : 0.0;
+        for (int k = 0; k < 3; ++k) {
+            geo.lo[k] = k < d && !wraps(k) ? lo[k] : 0.0;
+            geo.inv_hk[k] = geo.inv_h;
+            if (wraps(k)) {
+                geo.wrap |= 1 << k;
+                geo.L[k] = ctx->periodic_bounds[k];
+                geo.inv_hk[k] = (double)geo.g[k] / geo.L[k];
+                sp.wl[k] = (float)geo.L[k];
+                sp.whalf[k] = 0.5f * sp.wl[k];
+                if (geo.g[k] < 3) use_grid = false;  // a 3-cell stencil would meet a cell twice
+            }
+        }
         geo.ncells = (int64_t)geo.g[0] * geo.g[1] * geo.g[2];
         if (geo.ncells >= 0x7ffffff0LL) use_grid = false;
     }
@@ -960,7 +1118,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
                      : form == kFormMasks ? CNN_INTERSECT_BITSET
                                           : ctx->intersect_pref;
     // the mask form reads rows through 3 x 3 x 3 stencils: cells of reach 1 only
-    bool use_mask = use_grid && pref == CNN_INTERSECT_BITSET && geo.reach == 1;
+    bool use_mask = use_grid && pref == CNN_INTERSECT_BITSET && geo.reach == 1 && !geo.wrap;
     bool use_lists = !use_mask;
     bool calibrate = false;
     unsigned long long *counters = ctx->counters.as<unsigned long long>();
@@ -1007,7 +1165,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
                                       sizeof(int64_t), cudaMemcpyDeviceToDevice, st));  // both totals side by side
         CNN_TRY(read_back(ctx, hcounts, ctx->io_b.as<int64_t>() + geo.ncells, 2 * sizeof(int64_t)));
         const int64_t nitems = hcounts[0];
-        if (pref == CNN_INTERSECT_AUTO && geo.reach == 1) {
+        if (pref == CNN_INTERSECT_AUTO && geo.reach == 1 && !geo.wrap) {
             int choice = CNN_INTERSECT_AUTO;
             ctx->tune_key = tuner_key(ctx, n, hcounts[1]);
             if (tuner_lookup(ctx->tune_key, &choice)) {
@@ -1068,13 +1226,13 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         if (!use_lists) {
             // masks only
         } else if (nitems > 0 && use_slots) {
-            grid_unit_kernel<kSlots><<<(unsigned)((nitems + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
+            (geo.wrap ? grid_unit_kernel<kSlots, true> : grid_unit_kernel<kSlots, false>)<<<(unsigned)((nitems + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
                 ctx->io_c.as<int2>(), nitems, ctx->x, d, geo, sp, ctx->perm.as<int32_t>(),
                 ctx->cell_start.as<int64_t>(), ctx->xf4.as<float4>(), deg, slot_base,
                 ctx->grid_slot_cols.as<int32_t>(), counters, ctx->grid_qslot.as<int64_t>());
             CNN_LAUNCH_CHECK(ctx);
         } else if (nitems > 0) {
-            grid_unit_kernel<kCount><<<(unsigned)((nitems + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
+            (geo.wrap ? grid_unit_kernel<kCount, true> : grid_unit_kernel<kCount, false>)<<<(unsigned)((nitems + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
                 ctx->io_c.as<int2>(), nitems, ctx->x, d, geo, sp, ctx->perm.as<int32_t>(),
                 ctx->cell_start.as<int64_t>(), ctx->xf4.as<float4>(), deg, nullptr, nullptr, counters, nullptr);
             CNN_LAUNCH_CHECK(ctx);
@@ -1134,7 +1292,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
             CNN_LAUNCH_CHECK(ctx);
             ctx->split_valid = true;
         } else if (grid_items > 0) {
-            grid_unit_kernel<kFill><<<(unsigned)((grid_items + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
+            (geo.wrap ? grid_unit_kernel<kFill, true> : grid_unit_kernel<kFill, false>)<<<(unsigned)((grid_items + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
                 ctx->io_c.as<int2>(), grid_items, ctx->x, d, geo, sp, ctx->perm.as<int32_t>(),
                 ctx->cell_start.as<int64_t>(), ctx->xf4.as<float4>(), deg, row_off, ctx->cols.as<int32_t>(), counters,
                 nullptr);

@@ -383,7 +383,9 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
     lad.k = n_radii;
     lad.metric = metric;
     lad.fpmode = fpmode;
+    // the radius buckets use plain differences: not for the periodic metric
     const bool ladder = ctx->stats.search_kind == 1 && n_radii > 1 && n > 0 &&
+                        metric != CNN_METRIC_EUCLIDEAN_PERIODIC_REDUCED &&
                         ladder_thresholds(std::vector<double>(ctx->grid_extent, ctx->grid_extent + d), rcs, metric,
                                           &lad);
     if (!ladder) {

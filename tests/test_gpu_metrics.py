@@ -151,3 +151,54 @@ def test_periodic_predict_against_oracle(cnn):
     other = cnn.Clustering(y)
     cl.predict(other._bundle, r, c)
     assert np.array_equal(np.asarray(other.labels), want)
+
+
+@pytest.mark.parametrize("fpmode", ["separate", "fused"])
+def test_periodic_wrapped_grid_against_oracle(cnn, fpmode):
+    """The periodic metric runs on a wrapped cell grid (n_dim <= 3, at least 3
+    cells per periodic dimension): coordinates far outside the box, points
+    on the box edges and at half a box, and a lattice whose minimum-image
+    distances hit the cutoff exactly give the oracle's neighbour sets."""
+    from commonnnclustering_gb300 import _abi
+    rng = np.random.default_rng(7)
+    bounds = np.array([360.0, 360.0])
+    x = rng.uniform(-900.0, 900.0, size=(12000, 2))            # several box lengths out
+    x[:3000] = rng.normal(0.0, 8.0, size=(3000, 2)) + 180.0     # a cluster across the +-180 edge
+    x[3000:3010] = [[0, 0], [360, 0], [-360, 360], [180, -180], [540, 180],
+                    [-180, 0], [179.999999, 0], [-179.999999, 0], [720, 720], [0, 180]]
+    lat = np.stack(np.meshgrid(np.arange(-180.0, 180.0, 10.0), np.arange(-180.0, 180.0, 10.0)), -1).reshape(-1, 2)
+    x = np.vstack([x, lat])
+    fp = 1 if fpmode == "fused" else 0
+    for r in (10.0, 14.0):  # the lattice spacing: ties s == r^2 at r = 10
+        off, idx = o.periodic_neighbourhoods(x, bounds, r * r, fp)
+        ctx = _abi.Context(0)
+        try:
+            ctx.set_points(x)
+            ctx.set_periodic_bounds(bounds)
+            ctx.build_neighbours(r * r, metric=_abi.METRIC_EUCLIDEAN_PERIODIC_REDUCED, fpmode=fp)
+            assert ctx.stats()["search_kind"] == 1  # the wrapped grid
+            got_off, got_idx = ctx.get_neighbours()
+            assert np.array_equal(got_off, off) and np.array_equal(got_idx, idx)
+        finally:
+            ctx.close()
+
+
+def test_periodic_mixed_dimensions_on_the_grid(cnn):
+    """3-D with one dimension not periodic and two periodic ones of
+    different box lengths; a box too small for 3 cells falls back to the
+    all-pairs search with the same sets."""
+    from commonnnclustering_gb300 import _abi
+    rng = np.random.default_rng(8)
+    x = rng.uniform(-20.0, 20.0, size=(15000, 3))
+    for bounds, kind in ((np.array([10.0, 0.0, 7.5]), 1), (np.array([1.5, 10.0, 10.0]), 2)):
+        off, idx = o.periodic_neighbourhoods(x, bounds, 0.6 ** 2, 0)
+        ctx = _abi.Context(0)
+        try:
+            ctx.set_points(x)
+            ctx.set_periodic_bounds(bounds)
+            ctx.build_neighbours(0.6 ** 2, metric=_abi.METRIC_EUCLIDEAN_PERIODIC_REDUCED, fpmode=0)
+            assert ctx.stats()["search_kind"] == kind
+            got_off, got_idx = ctx.get_neighbours()
+            assert np.array_equal(got_off, off) and np.array_equal(got_idx, idx)
+        finally:
+            ctx.close()
