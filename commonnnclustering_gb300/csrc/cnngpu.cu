@@ -93,7 +93,11 @@ std::vector<DevBuf *> workspace_buffers(cnn_context *ctx) {
                            &ctx->pcell, &ctx->mbase, &ctx->masks, &ctx->dist_own, &ctx->bounds_dev,
                            &ctx->tune_consider, &ctx->tune_labels, &ctx->split,
                            &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->scratch_a, &ctx->scratch_b,
-                           &ctx->scratch_c, &ctx->scratch_d, &ctx->scan_tmp};
+                           &ctx->scratch_c, &ctx->scratch_d, &ctx->scan_tmp,
+                           &ctx->cross_cell_of, &ctx->cross_slot, &ctx->cross_count, &ctx->cross_start,
+                           &ctx->cross_perm, &ctx->cross_inv, &ctx->cross_xf4, &ctx->cross_units_n,
+                           &ctx->cross_units_off, &ctx->cross_units, &ctx->cross_deg, &ctx->cross_row_off,
+                           &ctx->cross_keys};
 }
 
 }  // namespace

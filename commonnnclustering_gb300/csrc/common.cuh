@@ -198,6 +198,12 @@ struct cnn_context {
 
     // prediction: this set's graph in point order, the other points' rows
     cnn::DevBuf pred_off, pred_cols, pred_xoff, pred_xcols, pred_x, pred_set;
+    // the cell grid of the last grid search (valid with the graph it built)
+    // and the other points binned into it (cross rows on the grid)
+    cnn::GridGeom grid_geo{};
+    bool grid_geo_valid = false;
+    cnn::DevBuf cross_cell_of, cross_slot, cross_count, cross_start, cross_perm, cross_inv, cross_xf4;
+    cnn::DevBuf cross_units_n, cross_units_off, cross_units, cross_deg, cross_row_off, cross_keys;
     int64_t gram_key_hint = 0;
 
     // fit work arrays

@@ -666,6 +666,125 @@ __global__ void __launch_bounds__(kTileWarps * 32) tile_search_kernel(
     }
 }
 
+// Rows of other points against this set on this set's cell grid
+// (NeighboursGetterExtBruteForce._get_other, src/cnnclustering/_types.pyx:
+// 1712-1731, for n_dim <= 3): the other points are binned into the same
+// cells (clamped to the grid: a point outside it has its neighbours, if
+// any, in the boundary cells); one warp per (cell, up to kUnitQueries other
+// points of that cell) scans the cell's stencil runs of this set's xf4 as
+// grid_unit_kernel does.  kCount: row lengths; kFill: keys (other point
+// index, this set's point index) for a radix sort into ascending rows.
+template <bool kFill>
+__global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) cross_unit_kernel(
+    const int2 *__restrict__ units, int64_t nunits, const double *__restrict__ xq, const double *__restrict__ x, int d,
+    GridGeom geo, SearchParams sp, const int32_t *__restrict__ qperm, const int64_t *__restrict__ qcell_start,
+    const float4 *__restrict__ qxf4, const int32_t *__restrict__ perm, const int64_t *__restrict__ cell_start,
+    const float4 *__restrict__ xf4, int bits_n, int32_t *__restrict__ qdeg, const int64_t *__restrict__ qrow_off,
+    uint64_t *__restrict__ keys, unsigned long long *__restrict__ counters) {
+    __shared__ int32_t s_rs[kUnitWarps][kMaxRuns];
+    __shared__ int32_t s_cum[kUnitWarps][kMaxRuns + 1];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t u = (int64_t)blockIdx.x * kUnitWarps + wid;
+    if (u >= nunits) return;  // whole warps only
+    const int2 unit = units[u];
+    const int32_t cid = unit.x;
+    const int64_t q0 = unit.y, qend = qcell_start[cid + 1];
+    const int S = geo.reach, Wd = 2 * S + 1, nruns = Wd * Wd;
+    int32_t rs = 0, len = 0;
+    if (lane < nruns) {
+        const int32_t cx = cid % geo.g[0];
+        const int32_t cy = (cid / geo.g[0]) % geo.g[1];
+        const int32_t cz = cid / (geo.g[0] * geo.g[1]);
+        const int32_t z = cz + lane / Wd - S, y = cy + lane % Wd - S;
+        if (z >= 0 && z < geo.g[2] && y >= 0 && y < geo.g[1]) {
+            const int32_t xlo = cx > S - 1 ? cx - S : 0;
+            const int32_t xhi = cx + S < geo.g[0] ? cx + S : geo.g[0] - 1;
+            const int64_t row = (int64_t)geo.g[0] * ((int64_t)y + (int64_t)geo.g[1] * z);
+            const int64_t b = cell_start[row + xlo], e = cell_start[row + xhi + 1];
+            rs = (int32_t)b;
+            len = e > b ? (int32_t)(e - b) : 0;
+        }
+    }
+    int32_t inc = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += v;
+    }
+    if (lane < nruns) {
+        s_rs[wid][lane] = rs;
+        s_cum[wid][lane + 1] = inc;
+    }
+    if (lane == 0) s_cum[wid][0] = 0;
+    const int32_t total = __shfl_sync(0xffffffffu, inc, nruns - 1);
+    __syncwarp();
+
+    int32_t qi[kUnitQueries];
+    float qx[kUnitQueries], qy[kUnitQueries], qz[kUnitQueries];
+    int64_t w[kUnitQueries];
+    uint64_t qkey[kUnitQueries];
+    int32_t cnt[kUnitQueries];
+#pragma unroll
+    for (int k = 0; k < kUnitQueries; ++k) {
+        const int64_t qk = q0 + k;
+        const bool ok = qk < qend;
+        const float4 f = ok ? qxf4[qk] : make_float4(INFINITY, INFINITY, INFINITY, 0.f);
+        qx[k] = f.x;
+        qy[k] = f.y;
+        qz[k] = f.z;
+        qi[k] = ok ? qperm[qk] : -1;  // the other point's index
+        w[k] = kFill && ok ? qrow_off[qk] : 0;
+        qkey[k] = ok ? (uint64_t)(uint32_t)qi[k] << bits_n : 0;
+        cnt[k] = 0;
+    }
+    const unsigned lt = (1u << lane) - 1u;
+    unsigned long long n_exact = 0;
+    int r = 0;
+    int32_t hi = s_cum[wid][1], base = s_rs[wid][0];
+    for (int32_t t = lane; t - lane < total; t += 32) {
+        while (t >= hi && r < nruns - 1) {
+            ++r;
+            base = s_rs[wid][r] - hi;
+            hi = s_cum[wid][r + 1];
+        }
+        const int32_t j = base + t;
+        const float4 cf = t < total ? xf4[j] : make_float4(INFINITY, INFINITY, INFINITY, 0.f);
+        bool in[kUnitQueries], amb[kUnitQueries];
+        bool any_amb = false;
+#pragma unroll
+        for (int k = 0; k < kUnitQueries; ++k) {
+            const float ex = qx[k] - cf.x, ey = qy[k] - cf.y, ez = qz[k] - cf.z;
+            const float sf = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+            in[k] = sf <= sp.thr_in;
+            amb[k] = !in[k] && sf <= sp.thr_out && t < total && qi[k] >= 0;
+            any_amb |= amb[k];
+        }
+        if (__any_sync(0xffffffffu, any_amb)) {
+#pragma unroll
+            for (int k = 0; k < kUnitQueries; ++k)
+                if (amb[k]) {
+                    in[k] = exact_in_radius(xq + (int64_t)qi[k] * d, x + (int64_t)perm[j] * d, d, sp);
+                    ++n_exact;
+                }
+        }
+#pragma unroll
+        for (int k = 0; k < kUnitQueries; ++k) {
+            const unsigned hit = __ballot_sync(0xffffffffu, in[k]);
+            if (kFill && in[k]) keys[w[k] + cnt[k] + __popc(hit & lt)] = qkey[k] | (uint64_t)(uint32_t)perm[j];
+            cnt[k] += __popc(hit);
+        }
+    }
+    if (!kFill && lane == 0) {
+#pragma unroll
+        for (int k = 0; k < kUnitQueries; ++k)
+            if (q0 + k < qend) qdeg[q0 + k] = cnt[k];
+    }
+    if (!kFill) {
+        for (int o = 16; o > 0; o >>= 1) n_exact += __shfl_down_sync(0xffffffffu, n_exact, o);
+        if (lane == 0 && n_exact) atomicAdd(&counters[0], n_exact);
+    }
+}
+
 // Rows of other points (queries) against this set (candidates): the same
 // float32 test with the float64 band, candidates in ascending index order.
 // (NeighboursGetterExtBruteForce._get_other, src/cnnclustering/_types.pyx:1712-1731.)
@@ -882,6 +1001,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     const int d = ctx->d;
     cudaStream_t st = ctx->stream;
     ctx->have_graph = false;
+    ctx->grid_geo_valid = false;
     ctx->graph_mask = false;
     ctx->csr_valid = true;
     ctx->tune_pending = false;
@@ -1104,6 +1224,8 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         if (geo.ncells >= 0x7ffffff0LL) use_grid = false;
     }
     ctx->stats.search_kind = use_grid ? 1 : 2;
+    ctx->grid_geo = geo;
+    ctx->grid_geo_valid = use_grid;
 
     int32_t *deg = ctx->deg.as<int32_t>();
     int64_t *row_off = ctx->row_off.as<int64_t>();
@@ -1436,6 +1558,103 @@ cnn_status cross_neighbours_impl(cnn_context *ctx, const double *xq, int64_t m, 
     } else if (radius_cutoff != INFINITY) {
         sp.thr_in = -1.f;
         sp.thr_out = -1.f;  // a NaN or negative cutoff admits nothing
+    }
+    // this set's cell grid, when its graph was built on one for a radius at
+    // least this large (the other points are binned into the same cells)
+    const GridGeom &geo = ctx->grid_geo;
+    const double R = metric == CNN_METRIC_EUCLIDEAN ? radius_cutoff : sqrt(radius_cutoff);
+    if (ctx->have_graph && ctx->grid_geo_valid && !geo.wrap && d <= 3 && radius_ok && R > 0 &&
+        (metric == CNN_METRIC_EUCLIDEAN_REDUCED || metric == CNN_METRIC_EUCLIDEAN) &&
+        geo.h * geo.reach >= R * (1.0 + 1e-6) && n > 0) {
+        // float32 values relative to the grid origin: the bound takes the
+        // largest magnitude either set reaches
+        std::vector<double> ext_g(d);
+        for (int k = 0; k < d; ++k) ext_g[k] = std::max(std::fabs(hi[k] - geo.lo[k]), std::fabs(lo[k] - geo.lo[k]));
+        const double rc2 = metric == CNN_METRIC_EUCLIDEAN ? radius_cutoff * radius_cutoff : radius_cutoff;
+        double band = 0;
+        if (!filter_thresholds(ext_g, R, rc2, &sp.thr_in, &sp.thr_out, &band)) {
+            sp.thr_in = -1.f;
+            sp.thr_out = INFINITY;  // every candidate pair in float64
+        }
+        const int64_t ncells = geo.ncells;
+        CNN_TRY(ctx->ensure(ctx->cross_cell_of, sizeof(int32_t) * (size_t)m));
+        CNN_TRY(ctx->ensure(ctx->cross_slot, sizeof(int32_t) * (size_t)m));
+        CNN_TRY(ctx->ensure(ctx->cross_count, sizeof(int32_t) * (size_t)(ncells + 2)));
+        CNN_TRY(ctx->ensure(ctx->cross_start, sizeof(int64_t) * (size_t)(ncells + 2)));
+        CNN_TRY(ctx->ensure(ctx->cross_perm, sizeof(int32_t) * (size_t)m));
+        CNN_TRY(ctx->ensure(ctx->cross_inv, sizeof(int32_t) * (size_t)m));
+        CNN_TRY(ctx->ensure(ctx->cross_xf4, sizeof(float4) * (size_t)m));
+        int32_t *qcount = ctx->cross_count.as<int32_t>();
+        int64_t *qstart = ctx->cross_start.as<int64_t>();
+        CNN_CUDA(ctx, cudaMemsetAsync(qcount, 0, sizeof(int32_t) * (size_t)(ncells + 2), st));
+        const unsigned gb = std::min<unsigned>(grid_for(m, 256), ctx->sm_count * 16u);
+        cell_assign_kernel<<<gb, 256, 0, st>>>(xq, m, d, geo, ctx->cross_cell_of.as<int32_t>(),
+                                               ctx->cross_slot.as<int32_t>(), qcount);
+        CNN_LAUNCH_CHECK(ctx);
+        CNN_TRY(scan_exclusive_i32_to_i64(ctx, qcount, qstart, ncells + 2));
+        place_kernel<<<gb, 256, 0, st>>>(ctx->cross_cell_of.as<int32_t>(), ctx->cross_slot.as<int32_t>(), qstart, m, xq,
+                                         d, geo, ctx->cross_perm.as<int32_t>(), ctx->cross_inv.as<int32_t>(),
+                                         ctx->cross_xf4.as<float4>());
+        CNN_LAUNCH_CHECK(ctx);
+        // units: (cell, up to kUnitQueries other points); the bucket of
+        // non-finite points (cell ncells) has no neighbours
+        CNN_TRY(ctx->ensure(ctx->cross_units_n, sizeof(int32_t) * (size_t)(ncells + 1)));
+        CNN_TRY(ctx->ensure(ctx->cross_units_off, sizeof(int64_t) * (size_t)(ncells + 1)));
+        const unsigned cg = std::min<unsigned>(grid_for(ncells, 256), ctx->sm_count * 16u);
+        item_count_kernel<kUnitQueries><<<cg, 256, 0, st>>>(qstart, ncells, ctx->cross_units_n.as<int32_t>());
+        CNN_LAUNCH_CHECK(ctx);
+        CNN_CUDA(ctx, cudaMemsetAsync(ctx->cross_units_n.as<int32_t>() + ncells, 0, sizeof(int32_t), st));
+        CNN_TRY(scan_exclusive_i32_to_i64(ctx, ctx->cross_units_n.as<int32_t>(), ctx->cross_units_off.as<int64_t>(),
+                                          ncells + 1));
+        int64_t nunits = 0;
+        CNN_TRY(read_back(ctx, &nunits, ctx->cross_units_off.as<int64_t>() + ncells, sizeof(int64_t)));
+        CNN_TRY(ctx->ensure(ctx->cross_units, sizeof(int2) * (size_t)(nunits > 0 ? nunits : 1)));
+        if (nunits > 0) {
+            item_fill_kernel<kUnitQueries><<<cg, 256, 0, st>>>(qstart, ncells, ctx->cross_units_off.as<int64_t>(),
+                                                               ctx->cross_units.as<int2>());
+            CNN_LAUNCH_CHECK(ctx);
+        }
+        // row lengths (in binned order), offsets, keys, sort, rows
+        CNN_TRY(ctx->ensure(ctx->cross_deg, sizeof(int32_t) * (size_t)(m + 1)));
+        CNN_TRY(ctx->ensure(ctx->cross_row_off, sizeof(int64_t) * (size_t)(m + 1)));
+        int32_t *qdeg = ctx->cross_deg.as<int32_t>();
+        CNN_CUDA(ctx, cudaMemsetAsync(qdeg, 0, sizeof(int32_t) * (size_t)(m + 1), st));
+        unsigned long long *counters = ctx->counters.as<unsigned long long>();
+        const int bits_n = bits_for(n);
+        const unsigned ug = (unsigned)((nunits + kUnitWarps - 1) / kUnitWarps);
+        if (nunits > 0) {
+            cross_unit_kernel<false><<<ug, kUnitWarps * 32, 0, st>>>(
+                ctx->cross_units.as<int2>(), nunits, xq, ctx->x, d, geo, sp, ctx->cross_perm.as<int32_t>(), qstart,
+                ctx->cross_xf4.as<float4>(), ctx->perm.as<int32_t>(), ctx->cell_start.as<int64_t>(),
+                ctx->xf4.as<float4>(), bits_n, qdeg, nullptr, nullptr, counters);
+            CNN_LAUNCH_CHECK(ctx);
+        }
+        CNN_TRY(scan_exclusive_i32_to_i64(ctx, qdeg, ctx->cross_row_off.as<int64_t>(), m + 1));
+        int64_t nnz = 0;
+        CNN_TRY(read_back(ctx, &nnz, ctx->cross_row_off.as<int64_t>() + m, sizeof(int64_t)));
+        // offsets in the other points' order
+        CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(int64_t) * (size_t)(m + 1)));
+        deg_by_point_kernel<<<std::min<unsigned>(grid_for(m + 1, 256), 4096u), 256, 0, st>>>(
+            qdeg, ctx->cross_inv.as<int32_t>(), m, ctx->scratch_a.as<int64_t>());
+        CNN_LAUNCH_CHECK(ctx);
+        CNN_TRY(scan_exclusive_i64(ctx, ctx->scratch_a.as<int64_t>(), off, m + 1));
+        CNN_TRY(ctx->ensure(cols_buf, sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1)));
+        if (nnz > 0) {
+            CNN_TRY(ctx->ensure(ctx->cross_keys, sizeof(uint64_t) * (size_t)nnz));
+            uint64_t *keys = ctx->cross_keys.as<uint64_t>();
+            cross_unit_kernel<true><<<ug, kUnitWarps * 32, 0, st>>>(
+                ctx->cross_units.as<int2>(), nunits, xq, ctx->x, d, geo, sp, ctx->cross_perm.as<int32_t>(), qstart,
+                ctx->cross_xf4.as<float4>(), ctx->perm.as<int32_t>(), ctx->cell_start.as<int64_t>(),
+                ctx->xf4.as<float4>(), bits_n, nullptr, ctx->cross_row_off.as<int64_t>(), keys, counters);
+            CNN_LAUNCH_CHECK(ctx);
+            uint64_t *sorted = keys;
+            CNN_TRY(radix_sort_u64(ctx, keys, nnz, bits_n + bits_for(m), 0, &sorted));
+            keys_to_cols_kernel<<<std::min<unsigned>(grid_for(nnz, 256), ctx->sm_count * 32u), 256, 0, st>>>(
+                sorted, nnz, bits_n, cols_buf.as<int32_t>());
+            CNN_LAUNCH_CHECK(ctx);
+        }
+        *nnz_out = nnz;
+        return CNN_OK;
     }
     if (d > 1024) return ctx->fail(CNN_ERR_UNSUPPORTED, "n_dim > 1024 is not supported");
     CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(double) * (size_t)d + 64));

@@ -158,3 +158,39 @@ def test_predict_edge_cases(cnn):
         ctx.predict(np.zeros((3, 3)), labels, [1], 0.25, 3, 2, np.zeros(3, dtype=np.int64),
                     np.ones(3, dtype=np.uint8))
     ctx.close()
+
+
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_predict_on_the_cell_grid_against_oracle(cnn, d):
+    """Other points binned into this set's cell grid (n_dim <= 3): points
+    far outside the grid, just outside its edge, non-finite ones and
+    duplicates of clustered points get the oracle's labels."""
+    rng = np.random.default_rng(300 + d)
+    centres = rng.uniform(-3, 3, size=(5, d))
+    x = np.vstack([cc + rng.normal(0, 0.45, size=(3000, d)) for cc in centres])
+    y = np.vstack([cc + rng.normal(0, 0.6, size=(2500, d)) for cc in centres])
+    lo, hi = x.min(0), x.max(0)
+    y[:20] = hi + 0.1                      # just outside the grid's edge
+    y[20:40] = lo - 0.15
+    y[40:60] = hi + 50.0                   # far outside
+    y[60:80] = x[100:120]                  # duplicates of clustered points
+    y[80, 0] = np.nan
+    y[81, -1] = np.inf
+    r = 0.35 if d > 1 else 0.02
+    prm = o.make_parameters(r, 4, 0)
+    ref_labels, _ = o.clustering_fit(x, r, 4, member_cutoff=3)
+    clusters = sorted(set(ref_labels.tolist()) - {0})
+    want, want_cons = o.predict_firstmatch(x, ref_labels, y, prm["radius_cutoff"], prm["similarity_cutoff"],
+                                           prm["n_member_cutoff"], clusters)
+    ctx = cnn.Context(0)
+    try:
+        ctx.set_points(x)
+        got = np.zeros(y.shape[0], dtype=np.int64)
+        got_cons = np.ones(y.shape[0], dtype=np.uint8)
+        ctx.predict(y, ref_labels, clusters, prm["radius_cutoff"], prm["similarity_cutoff"], prm["n_member_cutoff"],
+                    got, got_cons)
+        assert ctx.stats()["search_kind"] == 1  # this set's graph (and the cross rows) on the grid
+        assert np.array_equal(got, want)
+        assert np.array_equal(got_cons, want_cons)
+    finally:
+        ctx.close()
