@@ -194,7 +194,8 @@ struct cnn_context {
     cnn::DevBuf sweep_open_a, sweep_open_b, sweep_open_count;  // open pairs of the last fit, two lists
 
     // tensor-core (Gram) search for n_dim >= 16
-    cnn::DevBuf gram_hi, gram_mid, gram_lo, gram_aux, gram_keys, gram_amb, gram_blocks, gram_tiles, gram_perm;
+    cnn::DevBuf gram_hi, gram_mid, gram_lo, gram_aux, gram_amb, gram_blocks, gram_tiles, gram_perm;
+    cnn::DevBuf gram_masks, gram_tkeys, gram_low, gram_pad2c;  // tile hit masks, tile order, lower tiles, row map
 
     // prediction: this set's graph in point order, the other points' rows
     cnn::DevBuf pred_off, pred_cols, pred_xoff, pred_xcols, pred_x, pred_set;
@@ -204,7 +205,6 @@ struct cnn_context {
     bool grid_geo_valid = false;
     cnn::DevBuf cross_cell_of, cross_slot, cross_count, cross_start, cross_perm, cross_inv, cross_xf4;
     cnn::DevBuf cross_units_n, cross_units_off, cross_units, cross_deg, cross_row_off, cross_keys;
-    int64_t gram_key_hint = 0;
 
     // fit work arrays
     cnn::DevBuf node;     // uint8[n]

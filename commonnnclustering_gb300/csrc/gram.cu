@@ -47,6 +47,7 @@ namespace {
 constexpr int64_t kMaxGroups = 256;
 
 constexpr int kTM = 128;              // tile rows (M) = tile columns (N)
+constexpr int kMaskWords = kTM * kTM / 32;  // a tile's hit mask: row r, column c = word r * 4 + c / 32, bit c % 32
 constexpr int kKB = 64;               // K block: 64 bf16 = 128 bytes per row
 constexpr int kStages = 2;
 constexpr int kTileBytes = kTM * kKB * 2;          // 16 KB: one operand tile
@@ -71,10 +72,8 @@ struct GramArgs {
     const float *norm2;     // |x'_i|^2 (float)
     const float *blk_norm;  // max |x'_i| per row block
     const float *blk_norm2; // max |x'_i|^2 per row block
-    uint64_t *keys;         // (row << 32 | col) of neighbours
-    unsigned long long *nkeys;
-    int64_t key_cap;
-    uint64_t *amb;          // band pairs; bit 63 = emit both directions
+    uint32_t *masks;        // per listed tile: 128 rows x 4 words, bit = neighbour (kMaskWords per tile)
+    uint64_t *amb;          // band pairs (padded row << 32 | padded col); bit 63: off-diagonal tile
     float *amb_d2;          // their float32 squared distance
     unsigned long long *namb;
     int64_t amb_cap;
@@ -227,46 +226,28 @@ __device__ __forceinline__ void tmem_wait_ld(uint32_t (&v)[32]) {
                  : "memory");
 }
 
-// Emission for a 32-column chunk with at least one neighbour or band pair
-// somewhere in the warp: one warp-wide atomic per output list reserves the
-// slots, then each thread writes its own pairs, visiting only the set bits
-// of its masks.  A band pair's accumulator value is picked from the 32
-// registers with an unrolled select, so the registers are never indexed
-// dynamically (which would move them to local memory).
-__device__ __forceinline__ void epilogue_emit_masks(const GramArgs &args, const EpilogueTile &et,
-                                                    const uint32_t (&v)[32], const float *norms, int col0, int lane,
-                                                    uint32_t in_mask, uint32_t amb_mask) {
-    const int per_hit = et.diag ? 1 : 2;
-    const int my_keys = __popc(in_mask) * per_hit, my_amb = __popc(amb_mask);
-    int inc_k = my_keys, inc_a = my_amb;
+// Band pairs of a 32-column chunk with at least one somewhere in the warp:
+// one warp-wide atomic reserves the slots, then each thread writes its own,
+// visiting only the set bits of its mask.  A band pair's accumulator value
+// is picked from the 32 registers with an unrolled select, so the registers
+// are never indexed dynamically (which would move them to local memory).
+// Neighbours need no list: the chunk's hit bits go to the tile mask.
+__device__ __forceinline__ void epilogue_emit_band(const GramArgs &args, const EpilogueTile &et,
+                                                   const uint32_t (&v)[32], const float *norms, int col0, int lane,
+                                                   uint32_t amb_mask) {
+    const int my_amb = __popc(amb_mask);
+    int inc_a = my_amb;
     for (int o = 1; o < 32; o <<= 1) {
-        const int uk = __shfl_up_sync(0xffffffffu, inc_k, o);
         const int ua = __shfl_up_sync(0xffffffffu, inc_a, o);
-        if (lane >= o) {
-            inc_k += uk;
-            inc_a += ua;
-        }
+        if (lane >= o) inc_a += ua;
     }
-    const int tot_k = __shfl_sync(0xffffffffu, inc_k, 31), tot_a = __shfl_sync(0xffffffffu, inc_a, 31);
-    unsigned long long base_k = 0, base_a = 0;
-    if (lane == 31) {
-        if (tot_k) base_k = atomicAdd(args.nkeys, (unsigned long long)tot_k);
-        if (tot_a) base_a = atomicAdd(args.namb, (unsigned long long)tot_a);
-    }
-    unsigned long long wk = __shfl_sync(0xffffffffu, base_k, 31) + (unsigned long long)(inc_k - my_keys);
+    const int tot_a = __shfl_sync(0xffffffffu, inc_a, 31);
+    unsigned long long base_a = 0;
+    if (lane == 31 && tot_a) base_a = atomicAdd(args.namb, (unsigned long long)tot_a);
     unsigned long long wa = __shfl_sync(0xffffffffu, base_a, 31) + (unsigned long long)(inc_a - my_amb);
     const uint64_t gi = (uint64_t)et.gi;
     const uint64_t gj0 = (uint64_t)et.J * kTM + (uint64_t)col0;
-    const unsigned long long kcap = (unsigned long long)args.key_cap, acap = (unsigned long long)args.amb_cap;
-    for (uint32_t m = in_mask; m; m &= m - 1) {
-        const uint64_t gj = gj0 + (uint64_t)(__ffs(m) - 1);
-        if (wk < kcap) args.keys[wk] = (gi << 32) | gj;
-        ++wk;
-        if (!et.diag) {
-            if (wk < kcap) args.keys[wk] = (gj << 32) | gi;
-            ++wk;
-        }
-    }
+    const unsigned long long acap = (unsigned long long)args.amb_cap;
     for (uint32_t m = amb_mask; m; m &= m - 1) {
         const int jj = __ffs(m) - 1;
         uint32_t acc = 0;
@@ -466,9 +447,10 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_search_kernel(const __gr
                     in_mask = 0;
                     amb_mask = 0;
                 }
-                if (__any_sync(0xffffffffu, (in_mask | amb_mask) != 0))
-                    epilogue_emit_masks(args, et, v, my_norms + c * 32, half * 64 + c * 32, lane, in_mask,
-                                        amb_mask);
+                // every word of every listed tile's mask is written here
+                args.masks[(size_t)(t_begin + tl) * kMaskWords + row_in_tile * 4 + half * 2 + c] = in_mask;
+                if (__any_sync(0xffffffffu, amb_mask != 0))
+                    epilogue_emit_band(args, et, v, my_norms + c * 32, half * 64 + c * 32, lane, amb_mask);
             }
             __syncwarp();
             fence_before_sync();
@@ -895,38 +877,80 @@ __global__ void __launch_bounds__(256) tile_list_kernel(const float *__restrict_
     if (!kWrite && threadIdx.x < rows && s_cnt[threadIdx.x]) atomicAdd(&row_count[I0 + threadIdx.x], s_cnt[threadIdx.x]);
 }
 
-// internal indices -> point indices in a key list.  pack_bits > 0: write
-// (row << pack_bits | col), the sort key of the CSR; 0: keep (row << 32 |
-// col) and bit 63 (the band list).
-__global__ void map_keys_kernel(uint64_t *__restrict__ keys, const unsigned long long *__restrict__ count,
-                                int64_t cap, const int32_t *__restrict__ perm, int pack_bits) {
-    const int64_t nk = min((int64_t)*count, cap);
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nk; e += (int64_t)gridDim.x * blockDim.x) {
-        const uint64_t k = keys[e];
-        const uint64_t flag = k & (1ull << 63);
-        const uint64_t a = (uint32_t)perm[(k >> 32) & 0x7fffffffull], b = (uint32_t)perm[k & 0xffffffffull];
-        keys[e] = pack_bits > 0 ? (a << pack_bits) | b : flag | (a << 32) | b;
+// Tile list -> sort keys (I, J) of every tile, and (J, I) of the tiles
+// below the diagonal's mirror (J > I), counted per column block J.
+__global__ void tile_keys_kernel(const int2 *__restrict__ tiles, int64_t ntiles, uint64_t *__restrict__ keys,
+                                 uint64_t *__restrict__ ckeys, unsigned long long *__restrict__ nlow,
+                                 int32_t *__restrict__ col_count) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntiles; t += (int64_t)gridDim.x * blockDim.x) {
+        const int2 tl = tiles[t];
+        keys[t] = ((uint64_t)(uint32_t)tl.x << 32) | (uint32_t)tl.y;
+        if (tl.y > tl.x) {
+            ckeys[atomicAdd(nlow, 1ull)] = ((uint64_t)(uint32_t)tl.y << 32) | (uint32_t)tl.x;
+            atomicAdd(&col_count[tl.y], 1);
+        }
     }
 }
 
-// Band pairs in float64, reference order; hits appended to the key list
-// as packed (row << pack_bits | col).  One thread per pair keeps the
+__global__ void tiles_from_keys_kernel(const uint64_t *__restrict__ keys, int64_t ntiles, int2 *__restrict__ tiles) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntiles; t += (int64_t)gridDim.x * blockDim.x)
+        tiles[t] = make_int2((int32_t)(keys[t] >> 32), (int32_t)(keys[t] & 0xffffffffull));
+}
+
+// Index of tile (I, J) in the list (sorted by I, then J; every listed pair
+// has J >= I); -1 when not listed.
+__device__ __forceinline__ int64_t find_tile(const int2 *__restrict__ tiles, const int64_t *__restrict__ tile_off,
+                                             int32_t I, int32_t J) {
+    int64_t lo = tile_off[I], hi = tile_off[I + 1];
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (tiles[mid].y < J) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo < tile_off[I + 1] && tiles[lo].y == J ? lo : -1;
+}
+
+// Padded rows -> compact internal index (rows of points in padded order,
+// padding rows removed): the neighbour graph is kept in this order, so a
+// tile's columns come out ascending with no sort.
+__global__ void real_flag_kernel(const int32_t *__restrict__ perm, int64_t n_rows, int32_t *__restrict__ flag) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p <= n_rows; p += (int64_t)gridDim.x * blockDim.x)
+        flag[p] = p < n_rows && perm[p] >= 0 ? 1 : 0;
+}
+
+__global__ void compact_order_kernel(const int32_t *__restrict__ perm_pad, const int64_t *__restrict__ pos,
+                                     int64_t n_rows, int32_t *__restrict__ pad2c, int32_t *__restrict__ perm,
+                                     int32_t *__restrict__ inv) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n_rows; p += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t pt = perm_pad[p];
+        if (pt < 0) {
+            pad2c[p] = -1;
+            continue;
+        }
+        const int32_t c = (int32_t)pos[p];
+        pad2c[p] = c;
+        perm[c] = pt;
+        inv[pt] = c;
+    }
+}
+
+// Band pairs in float64, reference order; a pair within the radius sets
+// its bit in the mask of its tile.  One thread per pair keeps the
 // sequential sum of the reference; each warp stages its 32 pairs' rows in
 // shared memory kRecheckDims coordinates at a time, so the global loads are
-// 64-byte runs instead of 32 scattered words per instruction.  Keys and the
-// largest error are reserved / reduced once per warp.
+// 64-byte runs instead of 32 scattered words per instruction.  The largest
+// error is reduced once per warp.
 constexpr int kRecheckWarps = 8;
 constexpr int kRecheckDims = 8;
 
 __global__ void __launch_bounds__(kRecheckWarps * 32) gram_recheck_kernel(
     const double *__restrict__ x, int d, const uint64_t *__restrict__ amb, const unsigned long long *__restrict__ namb,
-    int64_t amb_cap, double rc, int metric, int fpmode, uint64_t *__restrict__ keys,
-    unsigned long long *__restrict__ nkeys, int64_t key_cap, const float *__restrict__ amb_d2,
-    unsigned *__restrict__ max_err_bits, int pack_bits) {
+    int64_t amb_cap, double rc, int metric, int fpmode, const int32_t *__restrict__ perm_pad,
+    const int2 *__restrict__ tiles, const int64_t *__restrict__ tile_off, uint32_t *__restrict__ masks,
+    const float *__restrict__ amb_d2, unsigned *__restrict__ max_err_bits) {
     __shared__ double s_a[kRecheckWarps][32][kRecheckDims + 1];
     __shared__ double s_b[kRecheckWarps][32][kRecheckDims + 1];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const unsigned lt = (1u << lane) - 1u;
     const int64_t total = min((int64_t)*namb, amb_cap);
     float max_err = 0.f;
     for (int64_t base = ((int64_t)blockIdx.x * kRecheckWarps + w) * 32; base < total;
@@ -934,8 +958,8 @@ __global__ void __launch_bounds__(kRecheckWarps * 32) gram_recheck_kernel(
         const int64_t e = base + lane;
         const bool valid = e < total;
         const uint64_t a = valid ? amb[e] : 0ull;
-        const bool both = (a >> 63) & 1ull;
-        const int64_t i = (int64_t)((a >> 32) & 0x7fffffffull), j = (int64_t)(a & 0xffffffffull);
+        const int64_t pi = (int64_t)((a >> 32) & 0x7fffffffull), pj = (int64_t)(a & 0xffffffffull);  // padded rows
+        const int64_t i = valid ? perm_pad[pi] : 0, j = valid ? perm_pad[pj] : 0;                    // points
         double s = 0.0;
         for (int k0 = 0; k0 < d; k0 += kRecheckDims) {
             // element m*32 + lane of the warp's 32 x kRecheckDims block: row r, coordinate c
@@ -965,47 +989,76 @@ __global__ void __launch_bounds__(kRecheckWarps * 32) gram_recheck_kernel(
             __syncwarp();
         }
         const double sv = metric == CNN_METRIC_EUCLIDEAN ? __dsqrt_rn(s) : s;
-        const bool hit = valid && sv <= rc;
-        const int mine = hit ? (both ? 2 : 1) : 0;
-        int inc = mine;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int u = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += u;
-        }
-        unsigned long long wbase = 0;
-        if (lane == 31 && inc) wbase = atomicAdd(nkeys, (unsigned long long)inc);
-        unsigned long long wpos = __shfl_sync(0xffffffffu, wbase, 31) + (unsigned long long)(inc - mine);
-        if (hit) {
-            if (wpos < (unsigned long long)key_cap) keys[wpos] = ((uint64_t)i << pack_bits) | (uint64_t)j;
-            if (both && wpos + 1 < (unsigned long long)key_cap)
-                keys[wpos + 1] = ((uint64_t)j << pack_bits) | (uint64_t)i;
+        if (valid && sv <= rc) {
+            const int64_t t = find_tile(tiles, tile_off, (int32_t)(pi / kTM), (int32_t)(pj / kTM));
+            if (t >= 0)  // always: the pair came from that tile
+                atomicOr(&masks[t * kMaskWords + (pi % kTM) * 4 + (pj % kTM) / 32], 1u << (pj % 32));
         }
         if (valid) max_err = fmaxf(max_err, fabsf((float)(s - (double)amb_d2[e])));
-        (void)lt;
     }
     for (int o = 16; o > 0; o >>= 1) max_err = fmaxf(max_err, __shfl_xor_sync(0xffffffffu, max_err, o));
     if (lane == 0 && max_err > 0.f) atomicMax(max_err_bits, __float_as_uint(max_err));
 }
 
-// Sorted packed keys -> CSR: row starts at the key where the row changes
-// (rows without keys get the next start), column indices from the low bits.
-__global__ void keys_rows_kernel(const uint64_t *__restrict__ keys, int64_t nk, int pack_bits, int64_t n,
-                                 int64_t *__restrict__ row_off, int32_t *__restrict__ cols) {
-    const uint64_t mask = (1ull << pack_bits) - 1;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nk; e += (int64_t)gridDim.x * blockDim.x) {
-        const uint64_t k = keys[e];
-        const int64_t r = (int64_t)(k >> pack_bits);
-        const int64_t rp = e == 0 ? -1 : (int64_t)(keys[e - 1] >> pack_bits);
-        for (int64_t q = rp + 1; q <= r; ++q) row_off[q] = e;
-        if (e == nk - 1)
-            for (int64_t q = r + 1; q <= n; ++q) row_off[q] = nk;
-        cols[e] = (int32_t)(k & mask);
+// Rows of the neighbour graph from the tile masks, in the compact internal
+// order: one warp per 32 rows of a row block I (lane = row).  Columns come
+// in ascending order: first the tiles (J', I) with J' < I, read as columns
+// of their masks (a word of such a mask holds one column's bits for the
+// warp's 32 rows), then the tiles (I, J >= I), read as rows.  kFill = false
+// counts, kFill = true writes.
+template <bool kFill>
+__global__ void __launch_bounds__(256) gram_rows_kernel(
+    int64_t nblk, const int2 *__restrict__ tiles, const int64_t *__restrict__ tile_off,
+    const uint64_t *__restrict__ low_keys, const int64_t *__restrict__ low_off, const uint32_t *__restrict__ masks,
+    const int32_t *__restrict__ pad2c, int32_t *__restrict__ deg, const int64_t *__restrict__ row_off,
+    int32_t *__restrict__ cols) {
+    const int lane = threadIdx.x & 31;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (gw >= nblk * 4) return;
+    const int32_t I = (int32_t)(gw >> 2);
+    const int q = (int)(gw & 3);
+    const int lr = q * 32 + lane;
+    const int32_t me = pad2c[(int64_t)I * kTM + lr];  // -1: a padding row (never a neighbour)
+    int64_t w = kFill && me >= 0 ? row_off[me] : 0;
+    int32_t cnt = 0;
+    // tiles (J', I), J' < I: bits of column block I = this block's rows
+    for (int64_t e = low_off[I]; e < low_off[I + 1]; ++e) {
+        const int32_t Jp = (int32_t)(low_keys[e] & 0xffffffffull);
+        const int64_t t = find_tile(tiles, tile_off, Jp, I);
+        if (t < 0) continue;  // not reached: every lower entry is a listed tile
+        const uint32_t *mt = masks + t * kMaskWords;
+        for (int g = 0; g < kTM / 32; ++g) {
+            const uint32_t word = mt[(g * 32 + lane) * 4 + q];  // column g*32+lane of tile (J', I), this warp's rows
+            const int32_t col = pad2c[(int64_t)Jp * kTM + g * 32 + lane];
+#pragma unroll 4
+            for (int k = 0; k < 32; ++k) {
+                const uint32_t wk = __shfl_sync(0xffffffffu, word, k);
+                const int32_t ck = __shfl_sync(0xffffffffu, col, k);
+                if ((wk >> lane) & 1u) {  // never on a padding row: it has no bits
+                    if (kFill && me >= 0) cols[w + cnt] = ck;
+                    ++cnt;
+                }
+            }
+        }
     }
-}
-
-__global__ void degree_from_offsets_kernel(const int64_t *__restrict__ row_off, int64_t n, int32_t *__restrict__ deg) {
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p <= n; p += (int64_t)gridDim.x * blockDim.x)
-        deg[p] = p < n ? (int32_t)(row_off[p + 1] - row_off[p]) : 0;
+    // tiles (I, J), J >= I: this row's words
+    for (int64_t t = tile_off[I]; t < tile_off[I + 1]; ++t) {
+        const int32_t J = tiles[t].y;
+        const uint4 rw = *reinterpret_cast<const uint4 *>(masks + t * kMaskWords + lr * 4);
+        const uint32_t words[4] = {rw.x, rw.y, rw.z, rw.w};
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            if (!kFill) {
+                cnt += __popc(words[g]);
+                continue;
+            }
+            for (uint32_t m = words[g]; m; m &= m - 1) {
+                if (me >= 0) cols[w + cnt] = pad2c[(int64_t)J * kTM + g * 32 + __ffs(m) - 1];
+                ++cnt;
+            }
+        }
+    }
+    if (!kFill && me >= 0) deg[me] = cnt;
 }
 
 typedef CUresult (*PFN_encodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -1189,10 +1242,35 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     int64_t ntiles = 0;
     CNN_CUDA(ctx, cudaMemcpyAsync(&ntiles, row_off + nblk, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     CNN_CUDA(ctx, cudaStreamSynchronize(st));
+    // a 2 KB hit mask per listed tile: decline past 64 GiB of them
+    if (ntiles > (int64_t(64) << 30) / (int64_t)(kMaskWords * sizeof(uint32_t))) return CNN_OK;
     CNN_TRY(ctx->ensure(ctx->gram_tiles, sizeof(int2) * (size_t)(ntiles > 0 ? ntiles : 1)));
+    int2 *tiles = ctx->gram_tiles.as<int2>();
     tile_list_kernel<true><<<lgrid, 256, 0, st>>>(centroid, bradius, d, nblk, Rf, nullptr, row_off, row_cursor,
-                                                  ctx->gram_tiles.as<int2>());
+                                                  tiles);
     CNN_LAUNCH_CHECK(ctx);
+    // the list sorted by (I, J); the tiles (J', I) with J' < I by column
+    // block I, then J' (the lower half of every row's columns)
+    const int bits_blk = [&] { int b = 1; while (b < 31 && (int64_t(1) << b) <= nblk) ++b; return b; }();
+    CNN_TRY(ctx->ensure(ctx->gram_tkeys, sizeof(uint64_t) * (size_t)(2 * ntiles + 2)));
+    CNN_TRY(ctx->ensure(ctx->gram_low, (sizeof(int32_t) + sizeof(int64_t)) * (size_t)(nblk + 1) + 64));
+    uint64_t *tkeys = ctx->gram_tkeys.as<uint64_t>();
+    uint64_t *lkeys = tkeys + ntiles;
+    int32_t *low_count = ctx->gram_low.as<int32_t>();
+    int64_t *low_off = reinterpret_cast<int64_t *>(
+        (reinterpret_cast<uintptr_t>(low_count + nblk + 1) + 15) & ~uintptr_t(15));
+    unsigned long long *nlow = counters + 10;
+    CNN_CUDA(ctx, cudaMemsetAsync(low_count, 0, sizeof(int32_t) * (size_t)(nblk + 1), st));
+    CNN_CUDA(ctx, cudaMemsetAsync(nlow, 0, sizeof(unsigned long long), st));
+    const unsigned tg = std::min<unsigned>(grid_for(ntiles, 256), ctx->sm_count * 8u);
+    tile_keys_kernel<<<tg, 256, 0, st>>>(tiles, ntiles, tkeys, lkeys, nlow, low_count);
+    CNN_LAUNCH_CHECK(ctx);
+    CNN_TRY(radix_sort_u64(ctx, tkeys, ntiles, 32 + bits_blk));
+    tiles_from_keys_kernel<<<tg, 256, 0, st>>>(tkeys, ntiles, tiles);
+    CNN_LAUNCH_CHECK(ctx);
+    CNN_TRY(scan_exclusive_i32_to_i64(ctx, low_count, low_off, nblk + 1));
+    // the count of lower tiles stays on the device (at most ntiles)
+    CNN_TRY(radix_sort_u64(ctx, lkeys, ntiles, 32 + bits_blk, 0, nullptr, reinterpret_cast<const int64_t *>(nlow)));
 
     CUtensorMap map_hi, map_mid, map_lo;
     if (!make_map(&map_hi, ctx->gram_hi.ptr, n_rows, dp) || !make_map(&map_mid, ctx->gram_mid.ptr, n_rows, dp) ||
@@ -1205,7 +1283,7 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     a.nkb = nkb;
     a.nblk = (int32_t)nblk;
     a.ntiles = ntiles;
-    a.tiles = ctx->gram_tiles.as<int2>();
+    a.tiles = tiles;
     a.rc2 = (float)rc2;
     a.coef = (float)coef;
     a.slack_coef = (float)(8.0 * ldexp(1.0, -24));  // float32 rounding of |x|^2, |y|^2 and the fma
@@ -1215,8 +1293,6 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     a.blk_norm2 = reinterpret_cast<const float *>(blk_norm2_bits);
     a.status = status;
     a.wait_ns = ctx->wait_limit_ns > 0 ? (unsigned long long)ctx->wait_limit_ns : kWaitNs;
-    // the float32 threshold must itself be an upper/lower bound of rc2
-    int64_t key_cap = std::max<int64_t>(ctx->gram_key_hint, std::min<int64_t>(n * 256, int64_t(1) << 31));
     const int64_t amb_cap = std::max<int64_t>(int64_t(1) << 22, n * 64);
     const int sms = (int)ctx->sm_count;
     int dev_sms = 0;
@@ -1224,68 +1300,71 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     const int grid = (int)std::min<int64_t>(ntiles, dev_sms > 0 ? dev_sms : sms);
     const size_t smem = (size_t)kStages * kStageBytes + 1024;
     CNN_TRY(allow_dynamic_smem(ctx, (const void *)gram_search_kernel, smem));
-    for (int attempt = 0; attempt < 2; ++attempt) {
-        CNN_TRY(ctx->ensure(ctx->gram_keys, sizeof(uint64_t) * (size_t)key_cap));
-        CNN_TRY(ctx->ensure(ctx->gram_amb, (sizeof(uint64_t) + sizeof(float)) * (size_t)amb_cap));
-        a.keys = ctx->gram_keys.as<uint64_t>();
-        a.key_cap = key_cap;
-        a.amb = ctx->gram_amb.as<uint64_t>();
-        a.amb_d2 = reinterpret_cast<float *>(a.amb + amb_cap);
-        a.amb_cap = amb_cap;
-        a.nkeys = nkeys;
-        a.namb = namb;
-        CNN_CUDA(ctx, cudaMemsetAsync(counters + 10, 0, 3 * sizeof(unsigned long long), st));
-        CNN_CUDA(ctx, cudaMemsetAsync(max_err_bits, 0, sizeof(unsigned), st));
-        stage_begin(ctx, 9);
-        gram_search_kernel<<<grid, kGramThreads, smem, st>>>(map_hi, map_mid, map_lo, a);
-        CNN_LAUNCH_CHECK(ctx);
-        stage_end(ctx, 9);
-        // internal indices -> point indices (before the recheck appends more keys)
-        map_keys_kernel<<<ctx->sm_count * 8u, 256, 0, st>>>(a.keys, nkeys, key_cap, perm, bits_n);
-        CNN_LAUNCH_CHECK(ctx);
-        map_keys_kernel<<<ctx->sm_count * 8u, 256, 0, st>>>(a.amb, namb, amb_cap, perm, 0);
-        CNN_LAUNCH_CHECK(ctx);
-        gram_recheck_kernel<<<ctx->sm_count * 8u, kRecheckWarps * 32, 0, st>>>(
-            ctx->x, d, a.amb, namb, amb_cap, radius_cutoff, metric, fpmode, a.keys, nkeys, key_cap, a.amb_d2,
-            max_err_bits, bits_n);
-        CNN_LAUNCH_CHECK(ctx);
-        unsigned long long hc[3];
-        CNN_CUDA(ctx, cudaMemcpyAsync(hc, counters + 10, sizeof(hc), cudaMemcpyDeviceToHost, st));
-        CNN_CUDA(ctx, cudaStreamSynchronize(st));
-        int h_status = (int)(hc[2] & 0xffffffffull);
-        if (h_status != 0) return ctx->fail(CNN_ERR_TIMEOUT, "tensor-core distance kernel timed out on a barrier");
-        if ((int64_t)hc[1] > amb_cap) return CNN_OK;  // too many band pairs: the all-pairs path decides
-        if ((int64_t)hc[0] <= key_cap) {
-            const int64_t nk = (int64_t)hc[0];
-            ctx->gram_key_hint = nk + nk / 8 + 1024;
-            ctx->stats.n_exact = (int64_t)hc[1];
-            unsigned me = 0;
-            CNN_CUDA(ctx, cudaMemcpyAsync(&me, max_err_bits, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-            CNN_CUDA(ctx, cudaStreamSynchronize(st));
-            float mef;
-            memcpy(&mef, &me, sizeof(float));
-            ctx->stats.max_abs_err = mef;
-            ctx->stats.n_candidates = ntiles * kTM * kTM;
-            ctx->stats.filter_band = std::max(coef, 0.0);
-            ctx->stats.filter_enabled = 1;
-            // CSR: sort the packed (row << bits_n | col) keys
-            uint64_t *sorted = a.keys;
-            CNN_TRY(radix_sort_u64(ctx, a.keys, nk, 2 * bits_n, 0, &sorted));
-            CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nk > 0 ? nk : 1)));
-            int64_t *row_off_csr = ctx->row_off.as<int64_t>();
-            if (nk == 0) CNN_CUDA(ctx, cudaMemsetAsync(row_off_csr, 0, sizeof(int64_t) * (size_t)(n + 1), st));
-            keys_rows_kernel<<<std::min<unsigned>(grid_for(nk, 256), ctx->sm_count * 16u), 256, 0, st>>>(
-                sorted, nk, bits_n, n, row_off_csr, ctx->cols.as<int32_t>());
-            CNN_LAUNCH_CHECK(ctx);
-            degree_from_offsets_kernel<<<std::min<unsigned>(grid_for(n + 1, 256), ctx->sm_count * 16u), 256, 0, st>>>(
-                row_off_csr, n, ctx->deg.as<int32_t>());
-            CNN_LAUNCH_CHECK(ctx);
-            ctx->nnz = nk;
-            *used = true;
-            return CNN_OK;
-        }
-        key_cap = (int64_t)hc[0] + 1024;  // exact size now known: run once more
-    }
+    CNN_TRY(ctx->ensure(ctx->gram_masks, sizeof(uint32_t) * (size_t)kMaskWords * (size_t)ntiles));
+    CNN_TRY(ctx->ensure(ctx->gram_amb, (sizeof(uint64_t) + sizeof(float)) * (size_t)amb_cap));
+    a.masks = ctx->gram_masks.as<uint32_t>();
+    a.amb = ctx->gram_amb.as<uint64_t>();
+    a.amb_d2 = reinterpret_cast<float *>(a.amb + amb_cap);
+    a.amb_cap = amb_cap;
+    a.namb = namb;
+    CNN_CUDA(ctx, cudaMemsetAsync(counters + 11, 0, 2 * sizeof(unsigned long long), st));
+    CNN_CUDA(ctx, cudaMemsetAsync(max_err_bits, 0, sizeof(unsigned), st));
+    stage_begin(ctx, 9);
+    gram_search_kernel<<<grid, kGramThreads, smem, st>>>(map_hi, map_mid, map_lo, a);
+    CNN_LAUNCH_CHECK(ctx);
+    stage_end(ctx, 9);
+    gram_recheck_kernel<<<ctx->sm_count * 8u, kRecheckWarps * 32, 0, st>>>(
+        ctx->x, d, a.amb, namb, amb_cap, radius_cutoff, metric, fpmode, perm, tiles, row_off, a.masks, a.amb_d2,
+        max_err_bits);
+    CNN_LAUNCH_CHECK(ctx);
+    unsigned long long hc[3];
+    CNN_CUDA(ctx, cudaMemcpyAsync(hc, counters + 10, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    CNN_CUDA(ctx, cudaStreamSynchronize(st));
+    const int h_status = (int)(hc[2] & 0xffffffffull);
+    if (h_status != 0) return ctx->fail(CNN_ERR_TIMEOUT, "tensor-core distance kernel timed out on a barrier");
+    if ((int64_t)hc[1] > amb_cap) return CNN_OK;  // too many band pairs: the all-pairs path decides
+    ctx->stats.n_exact = (int64_t)hc[1];
+    unsigned me = 0;
+    CNN_CUDA(ctx, cudaMemcpyAsync(&me, max_err_bits, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+
+    // the compact internal order (padded rows without padding) and the
+    // rows from the masks
+    CNN_TRY(ctx->ensure(ctx->gram_pad2c, sizeof(int32_t) * (size_t)(nblk * kTM + 1)));
+    CNN_TRY(ctx->ensure(ctx->scratch_c, sizeof(int64_t) * (size_t)(n_rows + 1) + sizeof(int32_t) * (size_t)(n_rows + 1) + 64));
+    int32_t *pad2c = ctx->gram_pad2c.as<int32_t>();
+    int64_t *pos = ctx->scratch_c.as<int64_t>();
+    int32_t *rflag = reinterpret_cast<int32_t *>(pos + n_rows + 1);
+    CNN_TRY(fill_i32(ctx, pad2c, nblk * kTM, -1));
+    real_flag_kernel<<<std::min<unsigned>(grid_for(n_rows + 1, 256), ctx->sm_count * 16u), 256, 0, st>>>(perm, n_rows,
+                                                                                                    rflag);
+    CNN_LAUNCH_CHECK(ctx);
+    CNN_TRY(scan_exclusive_i32_to_i64(ctx, rflag, pos, n_rows + 1));
+    compact_order_kernel<<<std::min<unsigned>(grid_for(n_rows, 256), ctx->sm_count * 16u), 256, 0, st>>>(
+        perm, pos, n_rows, pad2c, ctx->perm.as<int32_t>(), ctx->inv.as<int32_t>());
+    CNN_LAUNCH_CHECK(ctx);
+    int32_t *deg = ctx->deg.as<int32_t>();
+    int64_t *row_off_csr = ctx->row_off.as<int64_t>();
+    CNN_CUDA(ctx, cudaMemsetAsync(deg, 0, sizeof(int32_t) * (size_t)(n + 1), st));
+    const unsigned rg = (unsigned)((nblk * 4 * 32 + 255) / 256);
+    gram_rows_kernel<false><<<rg, 256, 0, st>>>(nblk, tiles, row_off, lkeys, low_off, a.masks, pad2c, deg, nullptr,
+                                                nullptr);
+    CNN_LAUNCH_CHECK(ctx);
+    CNN_TRY(scan_exclusive_i32_to_i64(ctx, deg, row_off_csr, n + 1));
+    int64_t nk = 0;
+    CNN_TRY(read_back(ctx, &nk, row_off_csr + n, sizeof(int64_t)));
+    CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nk > 0 ? nk : 1)));
+    gram_rows_kernel<true><<<rg, 256, 0, st>>>(nblk, tiles, row_off, lkeys, low_off, a.masks, pad2c, nullptr,
+                                               row_off_csr, ctx->cols.as<int32_t>());
+    CNN_LAUNCH_CHECK(ctx);
+    float mef;
+    memcpy(&mef, &me, sizeof(float));
+    ctx->stats.max_abs_err = mef;
+    ctx->stats.n_candidates = ntiles * kTM * kTM;
+    ctx->stats.filter_band = std::max(coef, 0.0);
+    ctx->stats.filter_enabled = 1;
+    ctx->nnz = nk;
+    ctx->identity_perm = !prune;  // without pruning the rows are the points in order
+    *used = true;
     return CNN_OK;
 }
 

@@ -1101,10 +1101,7 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         stage_begin(ctx, 2);
         CNN_TRY(gram_search_impl(ctx, radius_cutoff, metric, fpmode, &used));
         stage_end(ctx, 2);
-        if (used) {
-            CNN_TRY(iota_i32(ctx, ctx->perm.as<int32_t>(), n));
-            CNN_TRY(iota_i32(ctx, ctx->inv.as<int32_t>(), n));
-            ctx->identity_perm = true;
+        if (used) {  // the graph in the search's internal order (perm / inv set by it)
             ctx->stats.search_kind = 3;
             ctx->stats.n_nonzero = ctx->nnz;
             CNN_CUDA(ctx, cudaStreamSynchronize(st));
