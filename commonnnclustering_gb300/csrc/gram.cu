@@ -1001,64 +1001,117 @@ __global__ void __launch_bounds__(kRecheckWarps * 32) gram_recheck_kernel(
 }
 
 // Rows of the neighbour graph from the tile masks, in the compact internal
-// order: one warp per 32 rows of a row block I (lane = row).  Columns come
-// in ascending order: first the tiles (J', I) with J' < I, read as columns
-// of their masks (a word of such a mask holds one column's bits for the
-// warp's 32 rows), then the tiles (I, J >= I), read as rows.  kFill = false
-// counts, kFill = true writes.
+// order.  Row block B's columns come from a sequence of tiles: first the
+// tiles (J', B) with J' < B (ascending J', read as columns of their masks:
+// a word of such a mask holds one column's bits for 32 rows of B), then the
+// tiles (B, J), J >= B (ascending J, read as rows).  The sequence is cut
+// into chunks of kRowChunk tiles, and every (row block, 32-row quadrant,
+// chunk) is one warp's work (lane = row), so that row blocks with many
+// tiles spread over many warps.  The count pass stores each (chunk, row)
+// count and adds it to the row's degree; the fill pass starts each chunk of
+// a row after the chunks before it.
+constexpr int kRowChunk = 8;
+
+// the lower tiles' list indices (sorted keys (B << 32 | J') -> tile of (J', B))
+__global__ void lower_tiles_kernel(const uint64_t *__restrict__ lkeys, const unsigned long long *__restrict__ nlow,
+                                   const int2 *__restrict__ tiles, const int64_t *__restrict__ tile_off,
+                                   int64_t *__restrict__ ltile) {
+    const int64_t m = (int64_t)*nlow;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = lkeys[e];
+        ltile[e] = find_tile(tiles, tile_off, (int32_t)(k & 0xffffffffull), (int32_t)(k >> 32));
+    }
+}
+
+// chunks of every row block's tile sequence
+__global__ void row_chunks_kernel(int64_t nblk, const int64_t *__restrict__ tile_off,
+                                  const int64_t *__restrict__ low_off, int32_t *__restrict__ nchunk) {
+    for (int64_t B = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; B <= nblk; B += (int64_t)gridDim.x * blockDim.x) {
+        if (B == nblk) {
+            nchunk[B] = 0;
+            continue;
+        }
+        const int64_t L = (low_off[B + 1] - low_off[B]) + (tile_off[B + 1] - tile_off[B]);
+        nchunk[B] = (int32_t)((L + kRowChunk - 1) / kRowChunk);
+    }
+}
+
 template <bool kFill>
 __global__ void __launch_bounds__(256) gram_rows_kernel(
-    int64_t nblk, const int2 *__restrict__ tiles, const int64_t *__restrict__ tile_off,
-    const uint64_t *__restrict__ low_keys, const int64_t *__restrict__ low_off, const uint32_t *__restrict__ masks,
-    const int32_t *__restrict__ pad2c, int32_t *__restrict__ deg, const int64_t *__restrict__ row_off,
-    int32_t *__restrict__ cols) {
+    int64_t nblk, int64_t nwork, const int64_t *__restrict__ chunk_base, const int2 *__restrict__ tiles,
+    const int64_t *__restrict__ tile_off, const int64_t *__restrict__ ltile, const int64_t *__restrict__ low_off,
+    const uint32_t *__restrict__ masks, const int32_t *__restrict__ pad2c, int32_t *__restrict__ chunk_cnt,
+    int32_t *__restrict__ deg, const int64_t *__restrict__ row_off, int32_t *__restrict__ cols) {
     const int lane = threadIdx.x & 31;
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (gw >= nblk * 4) return;
-    const int32_t I = (int32_t)(gw >> 2);
-    const int q = (int)(gw & 3);
+    if (gw >= nwork) return;
+    // the row block: 4 * chunk_base[B] <= gw < 4 * chunk_base[B + 1]
+    int64_t lo = 0, hi = nblk;
+    while (hi - lo > 1) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (4 * chunk_base[mid] <= gw) lo = mid;
+        else hi = mid;
+    }
+    const int32_t B = (int32_t)lo;
+    const int64_t nch = chunk_base[B + 1] - chunk_base[B];
+    const int64_t r = gw - 4 * chunk_base[B];
+    const int q = (int)(r / nch);
+    const int64_t k = r - (int64_t)q * nch;
     const int lr = q * 32 + lane;
-    const int32_t me = pad2c[(int64_t)I * kTM + lr];  // -1: a padding row (never a neighbour)
-    int64_t w = kFill && me >= 0 ? row_off[me] : 0;
+    const int32_t me = pad2c[(int64_t)B * kTM + lr];  // -1: a padding row (never a neighbour)
+    const int64_t item0 = 4 * chunk_base[B] + (int64_t)q * nch;  // chunk 0 of this (block, quadrant)
+    int64_t w = 0;
+    if (kFill && me >= 0) {
+        w = row_off[me];
+        for (int64_t kk = 0; kk < k; ++kk) w += chunk_cnt[(item0 + kk) * 32 + lane];
+    }
+    const int64_t nlow = low_off[B + 1] - low_off[B];
+    const int64_t L = nlow + (tile_off[B + 1] - tile_off[B]);
+    const int64_t s1 = min(L, (k + 1) * kRowChunk);
     int32_t cnt = 0;
-    // tiles (J', I), J' < I: bits of column block I = this block's rows
-    for (int64_t e = low_off[I]; e < low_off[I + 1]; ++e) {
-        const int32_t Jp = (int32_t)(low_keys[e] & 0xffffffffull);
-        const int64_t t = find_tile(tiles, tile_off, Jp, I);
-        if (t < 0) continue;  // not reached: every lower entry is a listed tile
-        const uint32_t *mt = masks + t * kMaskWords;
-        for (int g = 0; g < kTM / 32; ++g) {
-            const uint32_t word = mt[(g * 32 + lane) * 4 + q];  // column g*32+lane of tile (J', I), this warp's rows
-            const int32_t col = pad2c[(int64_t)Jp * kTM + g * 32 + lane];
+    for (int64_t sidx = k * kRowChunk; sidx < s1; ++sidx) {
+        if (sidx < nlow) {
+            // tile (J', B): column lr of its mask
+            const int64_t t = ltile[low_off[B] + sidx];
+            if (t < 0) continue;  // not reached: every lower entry is a listed tile
+            const int32_t Jp = tiles[t].x;
+            const uint32_t *mt = masks + t * kMaskWords;
+            for (int g = 0; g < kTM / 32; ++g) {
+                const uint32_t word = mt[(g * 32 + lane) * 4 + q];  // row g*32+lane of (J', B): bits of this warp's rows
+                const int32_t col = pad2c[(int64_t)Jp * kTM + g * 32 + lane];
 #pragma unroll 4
-            for (int k = 0; k < 32; ++k) {
-                const uint32_t wk = __shfl_sync(0xffffffffu, word, k);
-                const int32_t ck = __shfl_sync(0xffffffffu, col, k);
-                if ((wk >> lane) & 1u) {  // never on a padding row: it has no bits
-                    if (kFill && me >= 0) cols[w + cnt] = ck;
+                for (int kk = 0; kk < 32; ++kk) {
+                    const uint32_t wk = __shfl_sync(0xffffffffu, word, kk);
+                    const int32_t ck = __shfl_sync(0xffffffffu, col, kk);
+                    if ((wk >> lane) & 1u) {  // never on a padding row: it has no bits
+                        if (kFill && me >= 0) cols[w + cnt] = ck;
+                        ++cnt;
+                    }
+                }
+            }
+        } else {
+            // tile (B, J), J >= B: this row's words
+            const int64_t t = tile_off[B] + (sidx - nlow);
+            const int32_t J = tiles[t].y;
+            const uint4 rw = *reinterpret_cast<const uint4 *>(masks + t * kMaskWords + lr * 4);
+            const uint32_t words[4] = {rw.x, rw.y, rw.z, rw.w};
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+                if (!kFill) {
+                    cnt += __popc(words[g]);
+                    continue;
+                }
+                for (uint32_t m = words[g]; m; m &= m - 1) {
+                    if (me >= 0) cols[w + cnt] = pad2c[(int64_t)J * kTM + g * 32 + __ffs(m) - 1];
                     ++cnt;
                 }
             }
         }
     }
-    // tiles (I, J), J >= I: this row's words
-    for (int64_t t = tile_off[I]; t < tile_off[I + 1]; ++t) {
-        const int32_t J = tiles[t].y;
-        const uint4 rw = *reinterpret_cast<const uint4 *>(masks + t * kMaskWords + lr * 4);
-        const uint32_t words[4] = {rw.x, rw.y, rw.z, rw.w};
-#pragma unroll
-        for (int g = 0; g < 4; ++g) {
-            if (!kFill) {
-                cnt += __popc(words[g]);
-                continue;
-            }
-            for (uint32_t m = words[g]; m; m &= m - 1) {
-                if (me >= 0) cols[w + cnt] = pad2c[(int64_t)J * kTM + g * 32 + __ffs(m) - 1];
-                ++cnt;
-            }
-        }
+    if (!kFill) {
+        chunk_cnt[(item0 + k) * 32 + lane] = cnt;
+        if (me >= 0 && cnt) atomicAdd(&deg[me], cnt);
     }
-    if (!kFill && me >= 0) deg[me] = cnt;
 }
 
 typedef CUresult (*PFN_encodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -1342,20 +1395,41 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     compact_order_kernel<<<std::min<unsigned>(grid_for(n_rows, 256), ctx->sm_count * 16u), 256, 0, st>>>(
         perm, pos, n_rows, pad2c, ctx->perm.as<int32_t>(), ctx->inv.as<int32_t>());
     CNN_LAUNCH_CHECK(ctx);
+    // work items of the row builder: (row block, quadrant, chunk of tiles)
+    CNN_TRY(ctx->ensure(ctx->gram_rowwork, sizeof(int64_t) * (size_t)(ntiles + nblk + 2) +
+                                               sizeof(int32_t) * (size_t)(nblk + 1) + 64));
+    int64_t *ltile = ctx->gram_rowwork.as<int64_t>();
+    int64_t *chunk_base = ltile + ntiles;
+    int32_t *nchunk = reinterpret_cast<int32_t *>(chunk_base + nblk + 2);
+    lower_tiles_kernel<<<tg, 256, 0, st>>>(lkeys, nlow, tiles, row_off, ltile);
+    CNN_LAUNCH_CHECK(ctx);
+    row_chunks_kernel<<<std::min<unsigned>(grid_for(nblk + 1, 256), ctx->sm_count * 8u), 256, 0, st>>>(
+        nblk, row_off, low_off, nchunk);
+    CNN_LAUNCH_CHECK(ctx);
+    CNN_TRY(scan_exclusive_i32_to_i64(ctx, nchunk, chunk_base, nblk + 1));
+    int64_t nchunks = 0;
+    CNN_TRY(read_back(ctx, &nchunks, chunk_base + nblk, sizeof(int64_t)));
+    const int64_t nwork = 4 * nchunks;
+    CNN_TRY(ctx->ensure(ctx->gram_chunkcnt, sizeof(int32_t) * 32 * (size_t)(nwork > 0 ? nwork : 1)));
     int32_t *deg = ctx->deg.as<int32_t>();
     int64_t *row_off_csr = ctx->row_off.as<int64_t>();
     CNN_CUDA(ctx, cudaMemsetAsync(deg, 0, sizeof(int32_t) * (size_t)(n + 1), st));
-    const unsigned rg = (unsigned)((nblk * 4 * 32 + 255) / 256);
-    gram_rows_kernel<false><<<rg, 256, 0, st>>>(nblk, tiles, row_off, lkeys, low_off, a.masks, pad2c, deg, nullptr,
-                                                nullptr);
-    CNN_LAUNCH_CHECK(ctx);
+    const unsigned rg = (unsigned)((nwork * 32 + 255) / 256);
+    if (nwork > 0) {
+        gram_rows_kernel<false><<<rg, 256, 0, st>>>(nblk, nwork, chunk_base, tiles, row_off, ltile, low_off, a.masks,
+                                                    pad2c, ctx->gram_chunkcnt.as<int32_t>(), deg, nullptr, nullptr);
+        CNN_LAUNCH_CHECK(ctx);
+    }
     CNN_TRY(scan_exclusive_i32_to_i64(ctx, deg, row_off_csr, n + 1));
     int64_t nk = 0;
     CNN_TRY(read_back(ctx, &nk, row_off_csr + n, sizeof(int64_t)));
     CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nk > 0 ? nk : 1)));
-    gram_rows_kernel<true><<<rg, 256, 0, st>>>(nblk, tiles, row_off, lkeys, low_off, a.masks, pad2c, nullptr,
-                                               row_off_csr, ctx->cols.as<int32_t>());
-    CNN_LAUNCH_CHECK(ctx);
+    if (nwork > 0) {
+        gram_rows_kernel<true><<<rg, 256, 0, st>>>(nblk, nwork, chunk_base, tiles, row_off, ltile, low_off, a.masks,
+                                                   pad2c, ctx->gram_chunkcnt.as<int32_t>(), nullptr, row_off_csr,
+                                                   ctx->cols.as<int32_t>());
+        CNN_LAUNCH_CHECK(ctx);
+    }
     float mef;
     memcpy(&mef, &me, sizeof(float));
     ctx->stats.max_abs_err = mef;
