@@ -1002,15 +1002,40 @@ __global__ void __launch_bounds__(kRecheckWarps * 32) gram_recheck_kernel(
 
 // Rows of the neighbour graph from the tile masks, in the compact internal
 // order.  Row block B's columns come from a sequence of tiles: first the
-// tiles (J', B) with J' < B (ascending J', read as columns of their masks:
-// a word of such a mask holds one column's bits for 32 rows of B), then the
-// tiles (B, J), J >= B (ascending J, read as rows).  The sequence is cut
+// tiles (J', B) with J' < B (ascending J', rows of their transposed masks),
+// then the tiles (B, J), J >= B (ascending J, rows of their masks).  The sequence is cut
 // into chunks of kRowChunk tiles, and every (row block, 32-row quadrant,
 // chunk) is one warp's work (lane = row), so that row blocks with many
 // tiles spread over many warps.  The count pass stores each (chunk, row)
 // count and adds it to the row's degree; the fill pass starts each chunk of
 // a row after the chunks before it.
 constexpr int kRowChunk = 8;
+
+// Transposed masks of the tiles off the diagonal, so that rows of column
+// block J read their bits of tile (I, J) as rows too: one block of 4 warps
+// per tile, warp w holds rows 32w..32w+31 (a lane each); the ballot of
+// column c over the warp is word w of the transposed row c.
+__global__ void __launch_bounds__(128) transpose_masks_kernel(const int2 *__restrict__ tiles, int64_t ntiles,
+                                                              const uint32_t *__restrict__ masks,
+                                                              uint32_t *__restrict__ masks_t) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int2 tl = tiles[t];
+        if (tl.x == tl.y) continue;  // the diagonal tile holds both halves already (block-uniform)
+        const uint4 rw = *reinterpret_cast<const uint4 *>(masks + t * kMaskWords + (w * 32 + lane) * 4);
+        const uint32_t words[4] = {rw.x, rw.y, rw.z, rw.w};
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            uint32_t mine = 0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const uint32_t b = __ballot_sync(0xffffffffu, (words[g] >> j) & 1u);
+                mine = lane == j ? b : mine;
+            }
+            masks_t[t * kMaskWords + (g * 32 + lane) * 4 + w] = mine;
+        }
+    }
+}
 
 // the lower tiles' list indices (sorted keys (B << 32 | J') -> tile of (J', B))
 __global__ void lower_tiles_kernel(const uint64_t *__restrict__ lkeys, const unsigned long long *__restrict__ nlow,
@@ -1040,7 +1065,8 @@ template <bool kFill>
 __global__ void __launch_bounds__(256) gram_rows_kernel(
     int64_t nblk, int64_t nwork, const int64_t *__restrict__ chunk_base, const int2 *__restrict__ tiles,
     const int64_t *__restrict__ tile_off, const int64_t *__restrict__ ltile, const int64_t *__restrict__ low_off,
-    const uint32_t *__restrict__ masks, const int32_t *__restrict__ pad2c, int32_t *__restrict__ chunk_cnt,
+    const uint32_t *__restrict__ masks, const uint32_t *__restrict__ masks_t, const int32_t *__restrict__ pad2c,
+    int32_t *__restrict__ chunk_cnt,
     int32_t *__restrict__ deg, const int64_t *__restrict__ row_off, int32_t *__restrict__ cols) {
     const int lane = threadIdx.x & 31;
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -1070,30 +1096,24 @@ __global__ void __launch_bounds__(256) gram_rows_kernel(
     const int64_t s1 = min(L, (k + 1) * kRowChunk);
     int32_t cnt = 0;
     for (int64_t sidx = k * kRowChunk; sidx < s1; ++sidx) {
+        // tile (J', B), J' < B: row lr of its transposed mask; tile (B, J),
+        // J >= B: row lr of its mask.  Either way 128 bits over the other
+        // block's rows.
+        int64_t t;
+        int32_t J;
+        const uint32_t *src;
         if (sidx < nlow) {
-            // tile (J', B): column lr of its mask
-            const int64_t t = ltile[low_off[B] + sidx];
+            t = ltile[low_off[B] + sidx];
             if (t < 0) continue;  // not reached: every lower entry is a listed tile
-            const int32_t Jp = tiles[t].x;
-            const uint32_t *mt = masks + t * kMaskWords;
-            for (int g = 0; g < kTM / 32; ++g) {
-                const uint32_t word = mt[(g * 32 + lane) * 4 + q];  // row g*32+lane of (J', B): bits of this warp's rows
-                const int32_t col = pad2c[(int64_t)Jp * kTM + g * 32 + lane];
-#pragma unroll 4
-                for (int kk = 0; kk < 32; ++kk) {
-                    const uint32_t wk = __shfl_sync(0xffffffffu, word, kk);
-                    const int32_t ck = __shfl_sync(0xffffffffu, col, kk);
-                    if ((wk >> lane) & 1u) {  // never on a padding row: it has no bits
-                        if (kFill && me >= 0) cols[w + cnt] = ck;
-                        ++cnt;
-                    }
-                }
-            }
+            J = tiles[t].x;
+            src = masks_t;
         } else {
-            // tile (B, J), J >= B: this row's words
-            const int64_t t = tile_off[B] + (sidx - nlow);
-            const int32_t J = tiles[t].y;
-            const uint4 rw = *reinterpret_cast<const uint4 *>(masks + t * kMaskWords + lr * 4);
+            t = tile_off[B] + (sidx - nlow);
+            J = tiles[t].y;
+            src = masks;
+        }
+        {
+            const uint4 rw = *reinterpret_cast<const uint4 *>(src + t * kMaskWords + lr * 4);
             const uint32_t words[4] = {rw.x, rw.y, rw.z, rw.w};
 #pragma unroll
             for (int g = 0; g < 4; ++g) {
@@ -1403,6 +1423,11 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     int32_t *nchunk = reinterpret_cast<int32_t *>(chunk_base + nblk + 2);
     lower_tiles_kernel<<<tg, 256, 0, st>>>(lkeys, nlow, tiles, row_off, ltile);
     CNN_LAUNCH_CHECK(ctx);
+    CNN_TRY(ctx->ensure(ctx->gram_masks_t, sizeof(uint32_t) * (size_t)kMaskWords * (size_t)ntiles));
+    uint32_t *masks_t = ctx->gram_masks_t.as<uint32_t>();
+    transpose_masks_kernel<<<(unsigned)std::min<int64_t>(ntiles, (int64_t)ctx->sm_count * 16), 128, 0, st>>>(
+        tiles, ntiles, a.masks, masks_t);
+    CNN_LAUNCH_CHECK(ctx);
     row_chunks_kernel<<<std::min<unsigned>(grid_for(nblk + 1, 256), ctx->sm_count * 8u), 256, 0, st>>>(
         nblk, row_off, low_off, nchunk);
     CNN_LAUNCH_CHECK(ctx);
@@ -1417,7 +1442,8 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     const unsigned rg = (unsigned)((nwork * 32 + 255) / 256);
     if (nwork > 0) {
         gram_rows_kernel<false><<<rg, 256, 0, st>>>(nblk, nwork, chunk_base, tiles, row_off, ltile, low_off, a.masks,
-                                                    pad2c, ctx->gram_chunkcnt.as<int32_t>(), deg, nullptr, nullptr);
+                                                    masks_t, pad2c, ctx->gram_chunkcnt.as<int32_t>(), deg, nullptr,
+                                                    nullptr);
         CNN_LAUNCH_CHECK(ctx);
     }
     CNN_TRY(scan_exclusive_i32_to_i64(ctx, deg, row_off_csr, n + 1));
@@ -1426,8 +1452,8 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nk > 0 ? nk : 1)));
     if (nwork > 0) {
         gram_rows_kernel<true><<<rg, 256, 0, st>>>(nblk, nwork, chunk_base, tiles, row_off, ltile, low_off, a.masks,
-                                                   pad2c, ctx->gram_chunkcnt.as<int32_t>(), nullptr, row_off_csr,
-                                                   ctx->cols.as<int32_t>());
+                                                   masks_t, pad2c, ctx->gram_chunkcnt.as<int32_t>(), nullptr,
+                                                   row_off_csr, ctx->cols.as<int32_t>());
         CNN_LAUNCH_CHECK(ctx);
     }
     float mef;
