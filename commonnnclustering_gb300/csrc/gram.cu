@@ -502,6 +502,21 @@ __global__ void column_mean_kernel(double *__restrict__ sum, int d, int64_t n) {
 // for an empty row): split x - mean into hi/lo bf16 (K padded with zeros to
 // dp), float32 squared norm (+inf for an empty row), per-block max norm (as
 // ordered int bits).  All coordinates are finite here.
+// Three-way bf16 split of a centred coordinate c, in float32: cf = (float)c
+// is within 2^-24 |c|; hi = bf16(cf) and the residuals cf - hi and
+// (cf - hi) - mid are exact in float32 (each operand pair within a factor
+// of 2), so hi + mid + lo misses cf by the last bf16 rounding only,
+// 2^-9 |(cf - hi) - mid| <= 2^-27 |cf|.  One float64 operation per
+// coordinate remains (the centring); GB300's float64 rate is low.
+__device__ __forceinline__ void split3(double c, __nv_bfloat16 &bh, __nv_bfloat16 &bm, __nv_bfloat16 &bl) {
+    const float cf = (float)c;
+    bh = __float2bfloat16_rn(cf);
+    const float r1 = cf - __bfloat162float(bh);
+    bm = __float2bfloat16_rn(r1);
+    const float r2 = r1 - __bfloat162float(bm);
+    bl = __float2bfloat16_rn(r2);
+}
+
 __global__ void gram_prep_kernel(const double *__restrict__ x, int64_t n_rows, int64_t n, int d, int dp,
                                  const double *__restrict__ mean, const int32_t *__restrict__ perm,
                                  __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ mid,
@@ -515,15 +530,9 @@ __global__ void gram_prep_kernel(const double *__restrict__ x, int64_t n_rows, i
     for (int k = lane; k < dp; k += 32) {
         __nv_bfloat16 bh = __float2bfloat16_rn(0.f), bm = bh, bl = bh;
         if (k < d && src >= 0) {
-            // residuals in float64 are exact (Sterbenz): c - hi - mid - lo is the
-            // rounding of the last bf16 step, at most ~2^-24 |c|
             const double c = x[src * d + k] - mean[k];
-            bh = __float2bfloat16_rn((float)c);
-            const double r1 = c - (double)__bfloat162float(bh);
-            bm = __float2bfloat16_rn((float)r1);
-            const double r2 = r1 - (double)__bfloat162float(bm);
-            bl = __float2bfloat16_rn((float)r2);
-            s2 += c * c;
+            split3(c, bh, bm, bl);
+            s2 = fma(c, c, s2);
         }
         hi[i * dp + k] = bh;
         mid[i * dp + k] = bm;
@@ -574,15 +583,9 @@ __global__ void __launch_bounds__(kPrepWarps * 32) gram_prep_bounds_kernel(
             __nv_bfloat16 bh = __float2bfloat16_rn(0.f), bm = bh, bl = bh;
             float cf = 0.f;
             if (k < d && src >= 0) {
-                // residuals in float64 are exact (Sterbenz): c - hi - mid - lo is
-                // the rounding of the last bf16 step, at most ~2^-24 |c|
                 const double c = x[src * d + k] - mean[k];
-                bh = __float2bfloat16_rn((float)c);
-                const double r1 = c - (double)__bfloat162float(bh);
-                bm = __float2bfloat16_rn((float)r1);
-                const double r2 = r1 - (double)__bfloat162float(bm);
-                bl = __float2bfloat16_rn((float)r2);
-                s2 += c * c;
+                split3(c, bh, bm, bl);
+                s2 = fma(c, c, s2);
                 cf = (float)c;
             }
             if (i < n_rows) {
@@ -1168,9 +1171,10 @@ bool make_map(CUtensorMap *map, void *base, int64_t rows, int dp) {
 }  // namespace
 
 // Error bound on |acc - x'.y'| relative to |x'||y'| (Cauchy-Schwarz on the
-// per-coordinate bounds): the three-way split leaves at most ~2^-24 |x_k| per
-// coordinate, and the dropped mid.lo, lo.mid, lo.lo are at most ~2^-24
-// |x_k||y_k| together with those residuals: 6 * 2^-24 overall.  FP32
+// per-coordinate bounds): the three-way split (split3) leaves at most
+// (1 + 2^-3) 2^-24 |x_k| per coordinate, so the residuals of both operands
+// add at most 2.25 * 2^-24 |x_k||y_k|, and the dropped mid.lo, lo.mid,
+// lo.lo at most 2^-26 |x_k||y_k|: below 2.5 * 2^-24, counted as 6 * 2^-24.  FP32
 // accumulation of the dp exact hi.hi products adds (dp + 8) 2^-23; the
 // cross-term accumulator (5 dp products, each below 2^-7 |x_k||y_k|) adds
 // (5 dp + 8) 2^-29, and summing the two accumulators 2 * 2^-24.  d2 uses
