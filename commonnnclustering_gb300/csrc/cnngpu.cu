@@ -82,7 +82,7 @@ std::vector<DevBuf *> workspace_buffers(cnn_context *ctx) {
                            &ctx->cols, &ctx->xf4, &ctx->cell_of, &ctx->cell_start, &ctx->grid_slot_base,
                            &ctx->grid_slot_cols, &ctx->grid_qslot, &ctx->node, &ctx->parent,
                            &ctx->comp_min, &ctx->flag, &ctx->counters, &ctx->stage_labels, &ctx->gram_hi, &ctx->gram_mid,
-                           &ctx->gram_lo, &ctx->gram_aux, &ctx->gram_masks, &ctx->gram_tkeys, &ctx->gram_low, &ctx->gram_pad2c, &ctx->gram_rowwork, &ctx->gram_chunkcnt, &ctx->gram_masks_t, &ctx->gram_amb,
+                           &ctx->gram_lo, &ctx->gram_aux, &ctx->gram_masks, &ctx->gram_tkeys, &ctx->gram_low, &ctx->gram_pad2c, &ctx->gram_rowwork, &ctx->gram_chunkcnt, &ctx->gram_amb,
                            &ctx->gram_blocks, &ctx->gram_tiles, &ctx->gram_perm, &ctx->pred_off, &ctx->pred_cols,
                            &ctx->pred_xoff, &ctx->pred_xcols, &ctx->pred_x, &ctx->pred_set,
                            &ctx->sweep_bucket, &ctx->sweep_row_off_max, &ctx->sweep_cols_max,

@@ -196,7 +196,7 @@ struct cnn_context {
     // tensor-core (Gram) search for n_dim >= 16
     cnn::DevBuf gram_hi, gram_mid, gram_lo, gram_aux, gram_amb, gram_blocks, gram_tiles, gram_perm;
     cnn::DevBuf gram_masks, gram_tkeys, gram_low, gram_pad2c;  // tile hit masks, tile order, lower tiles, row map
-    cnn::DevBuf gram_rowwork, gram_chunkcnt, gram_masks_t;     // row builder's work items, chunk counts, transposed masks
+    cnn::DevBuf gram_rowwork, gram_chunkcnt;                   // the row builder's work items and chunk counts
 
     // prediction: this set's graph in point order, the other points' rows
     cnn::DevBuf pred_off, pred_cols, pred_xoff, pred_xcols, pred_x, pred_set;

@@ -1005,8 +1005,9 @@ __global__ void __launch_bounds__(kRecheckWarps * 32) gram_recheck_kernel(
 
 // Rows of the neighbour graph from the tile masks, in the compact internal
 // order.  Row block B's columns come from a sequence of tiles: first the
-// tiles (J', B) with J' < B (ascending J', rows of their transposed masks),
-// then the tiles (B, J), J >= B (ascending J, rows of their masks).  The sequence is cut
+// tiles (J', B) with J' < B (ascending J', columns of their masks,
+// transposed in the warp), then the tiles (B, J), J >= B (ascending J, rows
+// of their masks).  The sequence is cut
 // into chunks of kRowChunk tiles, and every (row block, 32-row quadrant,
 // chunk) is one warp's work (lane = row), so that row blocks with many
 // tiles spread over many warps.  The count pass stores each (chunk, row)
@@ -1014,30 +1015,23 @@ __global__ void __launch_bounds__(kRecheckWarps * 32) gram_recheck_kernel(
 // a row after the chunks before it.
 constexpr int kRowChunk = 8;
 
-// Transposed masks of the tiles off the diagonal, so that rows of column
-// block J read their bits of tile (I, J) as rows too: one block of 4 warps
-// per tile, warp w holds rows 32w..32w+31 (a lane each); the ballot of
-// column c over the warp is word w of the transposed row c.
-__global__ void __launch_bounds__(128) transpose_masks_kernel(const int2 *__restrict__ tiles, int64_t ntiles,
-                                                              const uint32_t *__restrict__ masks,
-                                                              uint32_t *__restrict__ masks_t) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const int2 tl = tiles[t];
-        if (tl.x == tl.y) continue;  // the diagonal tile holds both halves already (block-uniform)
-        const uint4 rw = *reinterpret_cast<const uint4 *>(masks + t * kMaskWords + (w * 32 + lane) * 4);
-        const uint32_t words[4] = {rw.x, rw.y, rw.z, rw.w};
-#pragma unroll
-        for (int g = 0; g < 4; ++g) {
-            uint32_t mine = 0;
-#pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                const uint32_t b = __ballot_sync(0xffffffffu, (words[g] >> j) & 1u);
-                mine = lane == j ? b : mine;
-            }
-            masks_t[t * kMaskWords + (g * 32 + lane) * 4 + w] = mine;
-        }
+// 32 x 32 bit transpose across a warp: lane r holds row r (bit c = column
+// c); afterwards lane c holds column c (bit r = row r).  Five butterfly
+// stages swap the off-diagonal blocks of size 16, 8, 4, 2, 1.
+__device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
+    const uint32_t m16 = 0x0000ffffu, m8 = 0x00ff00ffu, m4 = 0x0f0f0f0fu, m2 = 0x33333333u, m1 = 0x55555555u;
+#define CNN_T32_STAGE(S, M)                                               \
+    {                                                                     \
+        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, S);            \
+        x = (lane & S) ? ((x & ~M) | ((y >> S) & M)) : ((x & M) | ((y & M) << S)); \
     }
+    CNN_T32_STAGE(16, m16)
+    CNN_T32_STAGE(8, m8)
+    CNN_T32_STAGE(4, m4)
+    CNN_T32_STAGE(2, m2)
+    CNN_T32_STAGE(1, m1)
+#undef CNN_T32_STAGE
+    return x;
 }
 
 // the lower tiles' list indices (sorted keys (B << 32 | J') -> tile of (J', B))
@@ -1068,8 +1062,7 @@ template <bool kFill>
 __global__ void __launch_bounds__(256) gram_rows_kernel(
     int64_t nblk, int64_t nwork, const int64_t *__restrict__ chunk_base, const int2 *__restrict__ tiles,
     const int64_t *__restrict__ tile_off, const int64_t *__restrict__ ltile, const int64_t *__restrict__ low_off,
-    const uint32_t *__restrict__ masks, const uint32_t *__restrict__ masks_t, const int32_t *__restrict__ pad2c,
-    int32_t *__restrict__ chunk_cnt,
+    const uint32_t *__restrict__ masks, const int32_t *__restrict__ pad2c, int32_t *__restrict__ chunk_cnt,
     int32_t *__restrict__ deg, const int64_t *__restrict__ row_off, int32_t *__restrict__ cols) {
     const int lane = threadIdx.x & 31;
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -1099,25 +1092,29 @@ __global__ void __launch_bounds__(256) gram_rows_kernel(
     const int64_t s1 = min(L, (k + 1) * kRowChunk);
     int32_t cnt = 0;
     for (int64_t sidx = k * kRowChunk; sidx < s1; ++sidx) {
-        // tile (J', B), J' < B: row lr of its transposed mask; tile (B, J),
-        // J >= B: row lr of its mask.  Either way 128 bits over the other
-        // block's rows.
+        // tile (J', B), J' < B: column lr of its mask, transposed in the
+        // warp from word q of its rows; tile (B, J), J >= B: row lr of its
+        // mask.  Either way 128 bits over the other block's rows.
         int64_t t;
         int32_t J;
-        const uint32_t *src;
+        uint32_t words[4];
         if (sidx < nlow) {
             t = ltile[low_off[B] + sidx];
-            if (t < 0) continue;  // not reached: every lower entry is a listed tile
+            if (t < 0) continue;  // not reached: every lower entry is a listed tile (warp-uniform)
             J = tiles[t].x;
-            src = masks_t;
+            const uint32_t *mt = masks + t * kMaskWords;
+#pragma unroll
+            for (int g = 0; g < 4; ++g) words[g] = transpose32(mt[(g * 32 + lane) * 4 + q], lane);
         } else {
             t = tile_off[B] + (sidx - nlow);
             J = tiles[t].y;
-            src = masks;
+            const uint4 rw = *reinterpret_cast<const uint4 *>(masks + t * kMaskWords + lr * 4);
+            words[0] = rw.x;
+            words[1] = rw.y;
+            words[2] = rw.z;
+            words[3] = rw.w;
         }
         {
-            const uint4 rw = *reinterpret_cast<const uint4 *>(src + t * kMaskWords + lr * 4);
-            const uint32_t words[4] = {rw.x, rw.y, rw.z, rw.w};
 #pragma unroll
             for (int g = 0; g < 4; ++g) {
                 if (!kFill) {
@@ -1427,11 +1424,6 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     int32_t *nchunk = reinterpret_cast<int32_t *>(chunk_base + nblk + 2);
     lower_tiles_kernel<<<tg, 256, 0, st>>>(lkeys, nlow, tiles, row_off, ltile);
     CNN_LAUNCH_CHECK(ctx);
-    CNN_TRY(ctx->ensure(ctx->gram_masks_t, sizeof(uint32_t) * (size_t)kMaskWords * (size_t)ntiles));
-    uint32_t *masks_t = ctx->gram_masks_t.as<uint32_t>();
-    transpose_masks_kernel<<<(unsigned)std::min<int64_t>(ntiles, (int64_t)ctx->sm_count * 16), 128, 0, st>>>(
-        tiles, ntiles, a.masks, masks_t);
-    CNN_LAUNCH_CHECK(ctx);
     row_chunks_kernel<<<std::min<unsigned>(grid_for(nblk + 1, 256), ctx->sm_count * 8u), 256, 0, st>>>(
         nblk, row_off, low_off, nchunk);
     CNN_LAUNCH_CHECK(ctx);
@@ -1446,8 +1438,7 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     const unsigned rg = (unsigned)((nwork * 32 + 255) / 256);
     if (nwork > 0) {
         gram_rows_kernel<false><<<rg, 256, 0, st>>>(nblk, nwork, chunk_base, tiles, row_off, ltile, low_off, a.masks,
-                                                    masks_t, pad2c, ctx->gram_chunkcnt.as<int32_t>(), deg, nullptr,
-                                                    nullptr);
+                                                    pad2c, ctx->gram_chunkcnt.as<int32_t>(), deg, nullptr, nullptr);
         CNN_LAUNCH_CHECK(ctx);
     }
     CNN_TRY(scan_exclusive_i32_to_i64(ctx, deg, row_off_csr, n + 1));
@@ -1456,8 +1447,8 @@ cnn_status gram_search_impl(cnn_context *ctx, double radius_cutoff, int metric, 
     CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(nk > 0 ? nk : 1)));
     if (nwork > 0) {
         gram_rows_kernel<true><<<rg, 256, 0, st>>>(nblk, nwork, chunk_base, tiles, row_off, ltile, low_off, a.masks,
-                                                   masks_t, pad2c, ctx->gram_chunkcnt.as<int32_t>(), nullptr,
-                                                   row_off_csr, ctx->cols.as<int32_t>());
+                                                   pad2c, ctx->gram_chunkcnt.as<int32_t>(), nullptr, row_off_csr,
+                                                   ctx->cols.as<int32_t>());
         CNN_LAUNCH_CHECK(ctx);
     }
     float mef;
