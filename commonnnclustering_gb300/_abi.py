@@ -147,6 +147,7 @@ SIGNATURES = {
     "cnn_neighbour_count": (_INT, [_P, ctypes.POINTER(_I64)]),
     "cnn_get_neighbours": (_INT, [_P, _P, _P, _INT]),
     "cnn_fit": (_INT, [_P, _I64, _I64, _I64, _P, _P, _I64, _INT]),
+    "cnn_fit_fresh": (_INT, [_P, _I64, _I64, _I32, _I64, _I64, _P, _P, _I64, _INT]),
     "cnn_graph_generation": (_INT, [_P, ctypes.POINTER(_I64)]),
     "cnn_sort_by_size": (_INT, [_P, _P, _I64, _I64, _I64, _INT]),
     "cnn_check_lists": (_INT, [_P, _P, _I64, _P, _I64, _I64, _P, _INT]),
@@ -431,6 +432,34 @@ class Context:
             lp, cp, mem = lab.ctypes.data, con.ctypes.data, MEM_HOST
         self._check(self._lib.cnn_fit(self._h, int(similarity_cutoff), int(n_member_cutoff), int(current_start),
                                       ctypes.c_void_p(cp), ctypes.c_void_p(lp), n_lab, mem), "cnn_fit")
+
+    def fit_fresh(self, similarity_cutoff: int, n_member_cutoff: int, sort: bool = True, member_cutoff: int = 2,
+                  max_clusters: Optional[int] = None, labels=None, consider=None):
+        """Clustering.fit from fresh labels (current_start 1), then
+        sort_by_size when ``sort``, in one library call (cnn_fit_fresh).
+        ``labels``: output array (host or CUDA, one int64 per point), a new
+        host array when None; ``consider``: optional output (all 0 after).
+        Returns labels."""
+        n = int(self._n_points)
+        if labels is None:
+            labels = np.empty(n, dtype=np.int64)
+        if int(labels.shape[0]) != n or (consider is not None and int(consider.shape[0]) != n):
+            raise ValueError(f"labels/consider must have one entry per point of the current neighbour graph ({n})")
+        mx = -1 if max_clusters is None else int(max_clusters)
+        if mx < -1:
+            mx = 0  # a negative limit keeps no cluster (every rank exceeds it)
+        if is_device_array(labels):
+            lp = device_pointer(labels, np.int64, writable=True)
+            cp = device_pointer(consider, np.uint8, writable=True) if consider is not None else 0
+            mem = MEM_DEVICE
+        else:
+            lab = host_array(labels, np.int64, writable=True)
+            con = host_array(consider, np.uint8, writable=True) if consider is not None else None
+            lp, cp, mem = lab.ctypes.data, (con.ctypes.data if con is not None else 0), MEM_HOST
+        self._check(self._lib.cnn_fit_fresh(self._h, int(similarity_cutoff), int(n_member_cutoff), 1 if sort else 0,
+                                            int(member_cutoff), mx, ctypes.c_void_p(lp), ctypes.c_void_p(cp or None),
+                                            n, mem), "cnn_fit_fresh")
+        return labels
 
     def sort_by_size(self, labels, member_cutoff: int, max_clusters: Optional[int]):
         mx = -1 if max_clusters is None else int(max_clusters)

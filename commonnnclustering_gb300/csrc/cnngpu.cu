@@ -129,6 +129,56 @@ cnn_status release_workspace(cnn_context *ctx) {
     return CNN_OK;
 }
 
+// The fit of cnn_fit on device arrays: the strategy of the graph's form,
+// or -- the first fit of a new workload profile under CNN_INTERSECT_AUTO --
+// both strategies from the same labels and consider, timed, the faster kept
+// by the tuner.  Either way the cluster count is left in scratch_a[n].
+cnn_status fit_dispatch(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff, int64_t current_start,
+                        uint8_t *cons_dev, int64_t *lab_dev) {
+    const int64_t n = ctx->n;
+    ctx->stats.tuned = 0;
+    ctx->stats.tune_ms_merge = ctx->stats.tune_ms_bitset = 0.f;
+    if (ctx->tune_pending && n > 0) {
+        // the graph is in both forms: fit it both ways from the same labels
+        // and consider, timed, and keep the faster strategy for this profile
+        cudaStream_t st = ctx->stream;
+        CNN_TRY(ctx->ensure(ctx->tune_consider, (size_t)n));
+        CNN_TRY(ctx->ensure(ctx->tune_labels, sizeof(int64_t) * (size_t)n));
+        CNN_CUDA(ctx, cudaMemcpyAsync(ctx->tune_consider.ptr, cons_dev, (size_t)n, cudaMemcpyDeviceToDevice, st));
+        CNN_CUDA(ctx, cudaMemcpyAsync(ctx->tune_labels.ptr, lab_dev, sizeof(int64_t) * (size_t)n,
+                                      cudaMemcpyDeviceToDevice, st));
+        CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[0], st));
+        CNN_TRY(fit_mask_impl(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
+        CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[1], st));
+        CNN_CUDA(ctx, cudaMemcpyAsync(cons_dev, ctx->tune_consider.ptr, (size_t)n, cudaMemcpyDeviceToDevice, st));
+        CNN_CUDA(ctx, cudaMemcpyAsync(lab_dev, ctx->tune_labels.ptr, sizeof(int64_t) * (size_t)n,
+                                      cudaMemcpyDeviceToDevice, st));
+        CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[2], st));
+        CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
+        CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[3], st));
+        CNN_CUDA(ctx, cudaEventSynchronize(ctx->tune_ev[3]));
+        float fm = 0.f, fl = 0.f;
+        CNN_CUDA(ctx, cudaEventElapsedTime(&fm, ctx->tune_ev[0], ctx->tune_ev[1]));
+        CNN_CUDA(ctx, cudaEventElapsedTime(&fl, ctx->tune_ev[2], ctx->tune_ev[3]));
+        const float bitset = ctx->tune_ms_mask + fm, merge = ctx->tune_ms_lists + fl;
+        const int choice = bitset < merge ? CNN_INTERSECT_BITSET : CNN_INTERSECT_MERGE;
+        tuner_store(ctx->tune_key, choice);
+        ctx->tune_pending = false;
+        ctx->graph_mask = choice == CNN_INTERSECT_BITSET;  // both forms stay valid for this graph
+        ctx->stats.tuned = 1;
+        ctx->stats.tune_ms_merge = merge;
+        ctx->stats.tune_ms_bitset = bitset;
+        ctx->stats.intersection = choice;
+    } else if (ctx->graph_mask) {
+        CNN_TRY(fit_mask_impl(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
+        ctx->stats.intersection = CNN_INTERSECT_BITSET;
+    } else {
+        CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
+        ctx->stats.intersection = CNN_INTERSECT_MERGE;
+    }
+    return CNN_OK;
+}
+
 }  // namespace cnn
 
 extern "C" {
@@ -454,50 +504,48 @@ CNN_API cnn_status cnn_fit(cnn_context *ctx, int64_t similarity_cutoff, int64_t 
         cons_dev = const_cast<uint8_t *>(c_in);
         lab_dev = const_cast<int64_t *>(l_in);
     }
-    ctx->stats.tuned = 0;
-    ctx->stats.tune_ms_merge = ctx->stats.tune_ms_bitset = 0.f;
-    if (ctx->tune_pending && n > 0) {
-        // the graph is in both forms: fit it both ways from the same labels
-        // and consider, timed, and keep the faster strategy for this profile
-        cudaStream_t st = ctx->stream;
-        CNN_TRY(ctx->ensure(ctx->tune_consider, (size_t)n));
-        CNN_TRY(ctx->ensure(ctx->tune_labels, sizeof(int64_t) * (size_t)n));
-        CNN_CUDA(ctx, cudaMemcpyAsync(ctx->tune_consider.ptr, cons_dev, (size_t)n, cudaMemcpyDeviceToDevice, st));
-        CNN_CUDA(ctx, cudaMemcpyAsync(ctx->tune_labels.ptr, lab_dev, sizeof(int64_t) * (size_t)n,
-                                      cudaMemcpyDeviceToDevice, st));
-        CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[0], st));
-        CNN_TRY(fit_mask_impl(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
-        CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[1], st));
-        CNN_CUDA(ctx, cudaMemcpyAsync(cons_dev, ctx->tune_consider.ptr, (size_t)n, cudaMemcpyDeviceToDevice, st));
-        CNN_CUDA(ctx, cudaMemcpyAsync(lab_dev, ctx->tune_labels.ptr, sizeof(int64_t) * (size_t)n,
-                                      cudaMemcpyDeviceToDevice, st));
-        CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[2], st));
-        CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
-        CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[3], st));
-        CNN_CUDA(ctx, cudaEventSynchronize(ctx->tune_ev[3]));
-        float fm = 0.f, fl = 0.f;
-        CNN_CUDA(ctx, cudaEventElapsedTime(&fm, ctx->tune_ev[0], ctx->tune_ev[1]));
-        CNN_CUDA(ctx, cudaEventElapsedTime(&fl, ctx->tune_ev[2], ctx->tune_ev[3]));
-        const float bitset = ctx->tune_ms_mask + fm, merge = ctx->tune_ms_lists + fl;
-        const int choice = bitset < merge ? CNN_INTERSECT_BITSET : CNN_INTERSECT_MERGE;
-        tuner_store(ctx->tune_key, choice);
-        ctx->tune_pending = false;
-        ctx->graph_mask = choice == CNN_INTERSECT_BITSET;  // both forms stay valid for this graph
-        ctx->stats.tuned = 1;
-        ctx->stats.tune_ms_merge = merge;
-        ctx->stats.tune_ms_bitset = bitset;
-        ctx->stats.intersection = choice;
-    } else if (ctx->graph_mask) {
-        CNN_TRY(fit_mask_impl(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
-        ctx->stats.intersection = CNN_INTERSECT_BITSET;
-    } else {
-        CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
-        ctx->stats.intersection = CNN_INTERSECT_MERGE;
-    }
+    CNN_TRY(cnn::fit_dispatch(ctx, similarity_cutoff, n_member_cutoff, current_start, cons_dev, lab_dev));
     if (mem == CNN_MEM_HOST && n > 0) {
         CNN_CUDA(ctx, cudaMemcpyAsync(labels, lab_dev, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
         CNN_CUDA(ctx, cudaMemcpyAsync(consider, cons_dev, (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
         CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return CNN_OK;
+}
+
+CNN_API cnn_status cnn_fit_fresh(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff, int32_t sort,
+                                 int64_t member_cutoff, int64_t max_clusters, int64_t *labels, uint8_t *consider,
+                                 int64_t n_points, cnn_memspace mem) {
+    CNN_TRY(check_ctx(ctx));
+    if (!ctx->have_graph) return ctx->fail(CNN_ERR_STATE, "no neighbour graph: build or set neighbours first");
+    const int64_t n = ctx->n;
+    if (n_points != n)
+        return ctx->fail(CNN_ERR_INVALID_ARG, "labels hold " + std::to_string(n_points) +
+                                                  " points, the neighbour graph " + std::to_string(n));
+    if (mem != CNN_MEM_HOST && mem != CNN_MEM_DEVICE) return ctx->fail(CNN_ERR_INVALID_ARG, "bad memspace");
+    if (n > 0 && !labels) return ctx->fail(CNN_ERR_INVALID_ARG, "labels are required");
+    if (n > INT32_MAX) return ctx->fail(CNN_ERR_UNSUPPORTED, "more than 2^31-1 labels");
+    if (n == 0) return CNN_OK;
+    cudaStream_t st = ctx->stream;
+    // fresh labels and consider flags are made on the device: nothing is copied in
+    int64_t *lab_dev = labels;
+    if (mem == CNN_MEM_HOST) {
+        CNN_TRY(ctx->ensure(ctx->stage_labels, sizeof(int64_t) * (size_t)n));
+        lab_dev = ctx->stage_labels.as<int64_t>();
+    }
+    uint8_t *cons_dev = consider;
+    if (mem == CNN_MEM_HOST || !consider) {
+        CNN_TRY(ctx->ensure(ctx->stage_consider, (size_t)n));
+        cons_dev = ctx->stage_consider.as<uint8_t>();
+    }
+    CNN_CUDA(ctx, cudaMemsetAsync(lab_dev, 0, sizeof(int64_t) * (size_t)n, st));
+    CNN_CUDA(ctx, cudaMemsetAsync(cons_dev, 1, (size_t)n, st));
+    CNN_TRY(cnn::fit_dispatch(ctx, similarity_cutoff, n_member_cutoff, 1, cons_dev, lab_dev));
+    if (sort) CNN_TRY(cnn::sort_fresh_impl(ctx, lab_dev, n, member_cutoff, max_clusters, ctx->capturing));
+    if (mem == CNN_MEM_HOST) {
+        CNN_CUDA(ctx, cudaMemcpyAsync(labels, lab_dev, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost, st));
+        CNN_CUDA(ctx, cudaStreamSynchronize(st));
+        if (consider) memset(consider, 0, (size_t)n);  // the fit visits every point
     }
     return CNN_OK;
 }

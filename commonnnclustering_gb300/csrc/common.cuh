@@ -291,6 +291,10 @@ cnn_status fill_i32(cnn_context *ctx, int32_t *p, int64_t n, int32_t v);
 cnn_status iota_i32(cnn_context *ctx, int32_t *p, int64_t n);
 
 // cnngpu.cu
+// cnn_fit on device arrays (with the intersection tuner); the cluster count
+// stays in scratch_a[n]
+cnn_status fit_dispatch(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff, int64_t current_start,
+                        uint8_t *cons_dev, int64_t *lab_dev);
 // Frees every workspace buffer of the context (after its stream is idle):
 // the graph and the points are gone, mem_held is 0.
 cnn_status release_workspace(cnn_context *ctx);
@@ -354,8 +358,10 @@ cnn_status open_pairs_impl(cnn_context *ctx, const int2 *in_list, const unsigned
                            unsigned long long *out_count, int64_t cap);
 // sort_by_size of the labels a fit from fresh labels just wrote (no host
 // round trip; fit.cu)
+// device_count: read the cluster count on the device only (graph capture);
+// otherwise one read-back picks the path and sizes its launches
 cnn_status sort_fresh_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64_t member_cutoff,
-                           int64_t max_clusters);
+                           int64_t max_clusters, bool device_count);
 cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels_dev, int64_t n,
                              int64_t member_cutoff, int64_t max_clusters);
 cnn_status check_lists_impl(cnn_context *ctx, const int32_t *a, int64_t na, const int32_t *b,

@@ -813,7 +813,7 @@ cnn_status sort_by_size_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64
 // scratch_a[n]): the same result, and the same work enqueued whatever the
 // labels hold, so that a sequence of fits can be captured as a CUDA graph.
 cnn_status sort_fresh_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64_t member_cutoff,
-                           int64_t max_clusters) {
+                           int64_t max_clusters, bool device_count) {
     cudaStream_t st = ctx->stream;
     if (n <= 0) return CNN_OK;
     if (n > INT32_MAX) return ctx->fail(CNN_ERR_UNSUPPORTED, "more than 2^31-1 labels");
@@ -827,11 +827,48 @@ cnn_status sort_fresh_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64_t
     uint64_t *keys = ctx->io_b.as<uint64_t>();
     int64_t *k_big = reinterpret_cast<int64_t *>(keys + n);  // k when above kOrderSmall, else 0
     int64_t *newlab = ctx->scratch_b.as<int64_t>();
-    CNN_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (size_t)n, st));
+    // outside a graph capture one read of the cluster count picks the path
+    // and sizes its launches (no idle launches of the other path)
+    int64_t k_host = -1;
+    if (!device_count) {
+        CNN_TRY(read_back(ctx, &k_host, k_dev, sizeof(int64_t)));
+        if (k_host <= 0) {
+            stage_end(ctx, 8);
+            return CNN_OK;  // only noise
+        }
+    }
+    CNN_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (size_t)(k_host >= 0 ? k_host : n), st));
     fresh_count_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(labels, n, cnt);
     CNN_LAUNCH_CHECK(ctx);
-    // at most kOrderSmall labels: ranked in shared memory; more: radix sort
-    // (both enqueued, each does nothing when the other applies)
+    if (k_host >= 0 && k_host <= kOrderSmall) {
+        const size_t smem = sizeof(uint64_t) * (size_t)k_host;
+        CNN_TRY(allow_dynamic_smem(ctx, (const void *)fresh_order_small_kernel, smem));
+        const unsigned blocks = (unsigned)std::min<int64_t>(2 * (int64_t)ctx->sm_count, (k_host + 31) / 32);
+        fresh_order_small_kernel<<<blocks, kOrderThreads, smem, st>>>(cnt, k_dev, n, bits_n, member_cutoff,
+                                                                      max_clusters, newlab, k_big);
+        CNN_LAUNCH_CHECK(ctx);
+        apply_dense_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(labels, n, 1, newlab);
+        CNN_LAUNCH_CHECK(ctx);
+        stage_end(ctx, 8);
+        return CNN_OK;
+    }
+    if (k_host > kOrderSmall) {  // the radix path with the count known here
+        CNN_CUDA(ctx, cudaMemcpyAsync(k_big, k_dev, sizeof(int64_t), cudaMemcpyDeviceToDevice, st));
+        fresh_keys_kernel<<<blocks_for(ctx, k_host), 256, 0, st>>>(cnt, k_big, n, bits_n, keys);
+        CNN_LAUNCH_CHECK(ctx);
+        uint64_t *sorted = keys;
+        CNN_TRY(radix_sort_u64(ctx, keys, k_host, bits_n + bits_for_fit(n + 1), bits_n, &sorted));
+        fresh_new_label_kernel<<<blocks_for(ctx, k_host), 256, 0, st>>>(sorted, k_big, n, bits_n, member_cutoff,
+                                                                       max_clusters, newlab);
+        CNN_LAUNCH_CHECK(ctx);
+        apply_dense_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(labels, n, 1, newlab);
+        CNN_LAUNCH_CHECK(ctx);
+        stage_end(ctx, 8);
+        return CNN_OK;
+    }
+    // device count (a graph capture): at most kOrderSmall labels ranked in
+    // shared memory, more by a radix sort -- both enqueued, each does
+    // nothing when the other applies
     const size_t keys_smem = sizeof(uint64_t) * (size_t)std::min<int64_t>(n, kOrderSmall);
     CNN_TRY(allow_dynamic_smem(ctx, (const void *)fresh_order_small_kernel, keys_smem));
     fresh_order_small_kernel<<<2 * ctx->sm_count, kOrderThreads, keys_smem, st>>>(
@@ -865,7 +902,7 @@ cnn_status fit_and_sort_into(cnn_context *ctx, int64_t similarity_cutoff, int64_
     CNN_CUDA(ctx, cudaMemsetAsync(ctx->sweep_consider.ptr, 1, (size_t)n, st));
     CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, 1, ctx->sweep_consider.as<uint8_t>(), labels_dev,
                      seed_a, seed_b, edge_list, edge_count));
-    return sort ? sort_fresh_impl(ctx, labels_dev, n, sort_member_cutoff, max_clusters) : CNN_OK;
+    return sort ? sort_fresh_impl(ctx, labels_dev, n, sort_member_cutoff, max_clusters, true) : CNN_OK;
 }
 
 // The pairs the last fit left open, from the graph (in_list null) or from

@@ -25,6 +25,8 @@
  *                           _types.pyx:1408-1411, 2580-2610, 2654-2706
  *   cnn_sort_by_size      Labels.sort_by_size
  *                           src/cnnclustering/_types.pyx:212-286
+ *   cnn_fit_fresh         Clustering.fit with fresh labels + sort_by_size
+ *                           src/cnnclustering/cluster.pyx:316-364
  *   cnn_check_lists       SimilarityCheckerExtScreensorted._check
  *                           src/cnnclustering/_types.pyx:2654-2706
  *
@@ -235,6 +237,18 @@ CNN_API cnn_status cnn_get_neighbours(cnn_context *ctx, int64_t *offsets, int32_
 CNN_API cnn_status cnn_fit(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
                            int64_t current_start, uint8_t *consider, int64_t *labels,
                            int64_t n_points, cnn_memspace mem);
+
+/* Clustering.fit from fresh labels (src/cnnclustering/cluster.pyx:316-364
+ * with no labels yet: labels 0, consider 1, current_start 1), then, when
+ * sort != 0, Labels.sort_by_size(member_cutoff, max_clusters) -- in one
+ * call: the fresh arrays are made on the device and the sort reads the
+ * cluster count there, so nothing is copied in and only labels[n] (and
+ * consider[n], all 0 afterwards, if not NULL) come back.  Same labels as
+ * cnn_fit + cnn_sort_by_size on fresh arrays.  n_points as for cnn_fit. */
+CNN_API cnn_status cnn_fit_fresh(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
+                                 int32_t sort, int64_t member_cutoff, int64_t max_clusters,
+                                 int64_t *labels, uint8_t *consider, int64_t n_points,
+                                 cnn_memspace mem);
 
 /* A counter of the graphs this context has held: it changes whenever the
  * points, distances or neighbourhoods are replaced or a neighbour graph is

@@ -370,3 +370,40 @@ def test_grid_reach_two_gives_the_same_sets(cnn, oracle, monkeypatch, d):
         assert np.array_equal(labels, ref_labels)
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("mem", ["host", "device"])
+@pytest.mark.parametrize("strategy", ["auto", "merge", "bitset"])
+def test_fit_fresh_equals_fit_then_sort(cnn, mem, strategy):
+    """cnn_fit_fresh (fresh labels made on the device, the sort reading the
+    cluster count there) gives the labels of cnn_fit + cnn_sort_by_size on
+    fresh arrays, with the intersection tuner's calibration fit, either
+    strategy, a cluster limit and no sort."""
+    import torch
+    from commonnnclustering_gb300 import _abi, workloads
+    x = workloads.md3d(n=30000, seed=13, centre_spread=2.0)
+    ctx = cnn.Context(0)
+    try:
+        ctx.set_intersection({"auto": _abi.INTERSECT_AUTO, "merge": _abi.INTERSECT_MERGE,
+                              "bitset": _abi.INTERSECT_BITSET}[strategy])
+        ctx.set_points(x)
+        for (sc, nm, mc, mx, sort) in ((12, 11, 5, None, True), (7, 6, 2, 3, True), (12, 11, 5, None, False)):
+            ctx.build_neighbours(0.1 ** 2)
+            want = np.zeros(x.shape[0], dtype=np.int64)
+            cons = np.ones(x.shape[0], dtype=np.uint8)
+            ctx.fit(sc, nm, 1, cons, want)
+            if sort:
+                ctx.sort_by_size(want, mc, mx)
+            ctx.build_neighbours(0.1 ** 2)
+            if mem == "host":
+                got_cons = np.ones(x.shape[0], dtype=np.uint8)
+                got = ctx.fit_fresh(sc, nm, sort, mc, mx, consider=got_cons)
+                assert not got_cons.any()
+            else:
+                lt = torch.full((x.shape[0],), -5, dtype=torch.int64, device="cuda")
+                ctx.fit_fresh(sc, nm, sort, mc, mx, labels=lt)
+                torch.cuda.synchronize()
+                got = lt.cpu().numpy()
+            assert np.array_equal(got, want), (sc, nm, mc, mx, sort)
+    finally:
+        ctx.close()
