@@ -99,14 +99,87 @@ struct HeapEdge {
     int32_t a, b;
 };
 
-// max-heap order of (-weight, (a, b)) in a min-heap: larger weight first,
-// then smaller a, then smaller b
-struct HeapAfter {
-    bool operator()(const HeapEdge &x, const HeapEdge &y) const {
-        if (x.w != y.w) return x.w < y.w;
-        if (x.a != y.a) return x.a > y.a;
-        return x.b > y.b;
+// The reference's heap order of (-weight, (a, b)): larger weight first,
+// then smaller a, then smaller b.
+inline bool edge_before(const HeapEdge &x, const HeapEdge &y) {
+    if (x.w != y.w) return x.w > y.w;
+    if (x.a != y.a) return x.a < y.a;
+    return x.b < y.b;
+}
+
+// Prim's frontier as an indexed heap with one entry per point not yet in
+// the tree: its best edge (w, a) from the tree, ordered by edge_before of
+// (w, a, b).  The reference's lazy heap holds every pushed (a, b) and pops
+// the first by the same order among those whose b is not in the tree; that
+// entry is the first over b of b's best entry, so popping this heap visits
+// the points and picks the tree edges exactly as the reference does, with
+// at most n entries instead of one per pair.
+class Frontier {
+  public:
+    explicit Frontier(int64_t n) : pos_((size_t)n, -1), key_((size_t)n) {}
+    bool empty() const { return heap_.empty(); }
+    // b's entry becomes (w, a) if that comes first by the heap order
+    void offer(int32_t b, int64_t w, int32_t a) {
+        const HeapEdge e{w, a, b};
+        int64_t i = pos_[b];
+        if (i < 0) {
+            key_[b] = e;
+            i = (int64_t)heap_.size();
+            heap_.push_back(b);
+            pos_[b] = i;
+        } else if (edge_before(e, key_[b])) {
+            key_[b] = e;
+        } else {
+            return;
+        }
+        up(i);
     }
+    HeapEdge pop() {
+        const int32_t b = heap_[0];
+        const HeapEdge e = key_[b];
+        pos_[b] = -2;  // in the tree
+        const int32_t last = heap_.back();
+        heap_.pop_back();
+        if (!heap_.empty()) {
+            heap_[0] = last;
+            pos_[last] = 0;
+            down(0);
+        }
+        return e;
+    }
+
+  private:
+    bool before(int32_t x, int32_t y) const { return edge_before(key_[x], key_[y]); }
+    void up(int64_t i) {
+        const int32_t b = heap_[i];
+        while (i > 0) {
+            const int64_t p = (i - 1) >> 1;
+            if (!before(b, heap_[p])) break;
+            heap_[i] = heap_[p];
+            pos_[heap_[i]] = i;
+            i = p;
+        }
+        heap_[i] = b;
+        pos_[b] = i;
+    }
+    void down(int64_t i) {
+        const int32_t b = heap_[i];
+        const int64_t m = (int64_t)heap_.size();
+        for (;;) {
+            int64_t c = 2 * i + 1;
+            if (c >= m) break;
+            if (c + 1 < m && before(heap_[c + 1], heap_[c])) ++c;
+            if (!before(heap_[c], b)) break;
+            heap_[i] = heap_[c];
+            pos_[heap_[i]] = i;
+            i = c;
+        }
+        heap_[i] = b;
+        pos_[b] = i;
+    }
+    std::vector<int64_t> pos_;  // index in heap_, -1 never offered, -2 in the tree
+    std::vector<HeapEdge> key_;
+    std::vector<int32_t> heap_;
 };
 
 }  // namespace
@@ -154,32 +227,32 @@ cnn_status mst_prim_impl(cnn_context *ctx, double radius_cutoff, int metric, int
     }
     CNN_CUDA(ctx, cudaStreamSynchronize(st));
 
-    // Prim, exactly the reference's loop and heap order
+    // Prim, the reference's loop and heap order (Frontier); the tree edges
+    // then leave in the tree queue's order, the same heap order
     std::vector<uint8_t> visited((size_t)n, 0);
-    std::priority_queue<HeapEdge, std::vector<HeapEdge>, HeapAfter> heap, tree;
-    auto push_row = [&](int64_t p) {
+    Frontier frontier(n);
+    std::vector<HeapEdge> tree;
+    tree.reserve((size_t)(n > 0 ? n - 1 : 0));
+    auto offer_row = [&](int64_t p) {
         for (int64_t k = off[p]; k < off[p + 1]; ++k)
-            if (!visited[cols[k]]) heap.push(HeapEdge{w[k], (int32_t)p, cols[k]});
+            if (!visited[cols[k]]) frontier.offer(cols[k], w[k], (int32_t)p);
     };
     for (int64_t point = 0; point < n; ++point) {
         if (visited[point]) continue;
         visited[point] = 1;
-        push_row(point);
-        while (!heap.empty()) {
-            const HeapEdge top = heap.top();
-            heap.pop();
-            if (visited[top.b]) continue;
+        offer_row(point);
+        while (!frontier.empty()) {
+            const HeapEdge top = frontier.pop();
             visited[top.b] = 1;
-            tree.push(top);
-            push_row(top.b);
+            tree.push_back(top);
+            offer_row(top.b);
         }
     }
+    std::sort(tree.begin(), tree.end(), edge_before);
     ea->reserve(tree.size());
     eb->reserve(tree.size());
     ew->reserve(tree.size());
-    while (!tree.empty()) {
-        const HeapEdge e = tree.top();
-        tree.pop();
+    for (const HeapEdge &e : tree) {
         ea->push_back(e.a);
         eb->push_back(e.b);
         ew->push_back(e.w);
