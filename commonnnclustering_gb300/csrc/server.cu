@@ -207,7 +207,6 @@ struct cnn_server {
 
     void run_slot(int s) {
         cnn_context *c = ctx[s];
-        std::vector<uint8_t> consider;
         for (;;) {
             int64_t id;
             cnn_job job;
@@ -227,14 +226,10 @@ struct cnn_server {
             const int64_t n = job.n_points;
             if (r == CNN_OK) r = cnn_set_points(c, job.points, job.dtype, n, job.n_dim, CNN_MEM_HOST);
             if (r == CNN_OK) r = cnn_build_neighbours(c, job.radius_cutoff, job.metric, job.fpmode);
-            if (r == CNN_OK) {
-                memset(job.labels, 0, sizeof(int64_t) * (size_t)n);
-                consider.assign((size_t)n, 1);
-                r = cnn_fit(c, job.similarity_cutoff, job.n_member_cutoff, 1, consider.data(), job.labels, n,
-                            CNN_MEM_HOST);
-            }
-            if (r == CNN_OK && job.member_cutoff >= 0)
-                r = cnn_sort_by_size(c, job.labels, n, job.member_cutoff, job.max_clusters, CNN_MEM_HOST);
+            // fresh labels, the fit and sort_by_size in one call: only the labels come back
+            if (r == CNN_OK)
+                r = cnn_fit_fresh(c, job.similarity_cutoff, job.n_member_cutoff, job.member_cutoff >= 0 ? 1 : 0,
+                                  job.member_cutoff, job.max_clusters, job.labels, nullptr, n, CNN_MEM_HOST);
             const bool outgrew = r == CNN_ERR_OOM && c->cap_hit;
             const std::string err = r == CNN_OK ? std::string() : std::string(cnn_last_error(c));
             // what the job added to the slot's holding (a lower bound of its

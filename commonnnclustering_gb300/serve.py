@@ -65,16 +65,13 @@ def footprint_bytes(n: int, d: int, expected_degree: float) -> int:
 
 
 def run_job_alone(ctx: _abi.Context, job: Job) -> np.ndarray:
-    """One job exactly as Clustering.fit runs it (host buffers)."""
+    """One job as Clustering.fit runs it from fresh labels, then
+    sort_by_size (host buffers; cnn_fit_fresh, the call the server makes)."""
     x = np.ascontiguousarray(job.points)
-    n = x.shape[0]
-    labels = np.zeros(n, dtype=np.int64)
-    consider = np.ones(n, dtype=np.uint8)
     ctx.set_points(x)
     ctx.build_neighbours(job.radius_cutoff ** 2)
-    ctx.fit(job.cnn_cutoff + 2, job.cnn_cutoff + 1, 1, consider, labels)
-    ctx.sort_by_size(labels, 2 if job.member_cutoff is None else job.member_cutoff, None)
-    return labels
+    return ctx.fit_fresh(job.cnn_cutoff + 2, job.cnn_cutoff + 1, True,
+                         2 if job.member_cutoff is None else job.member_cutoff, None)
 
 
 class Server:
