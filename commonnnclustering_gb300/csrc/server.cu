@@ -371,17 +371,18 @@ CNN_API cnn_status cnn_poll(cnn_server *srv, int64_t job_id, cnn_job_info *info)
 CNN_API cnn_status cnn_wait(cnn_server *srv, int64_t job_id, int64_t timeout_ns, cnn_job_info *info) {
     if (!srv) return CNN_ERR_INVALID_ARG;
     std::unique_lock<std::mutex> lk(srv->mu);
+    if (srv->jobs.find(job_id) == srv->jobs.end()) return CNN_ERR_INVALID_ARG;
+    // done, or released by another thread meanwhile (then the id is gone)
+    auto done = [&] {
+        auto it = srv->jobs.find(job_id);
+        return it == srv->jobs.end() || it->second.state == CNN_JOB_DONE;
+    };
+    const bool finished = timeout_ns < 0 ? (srv->cv_done.wait(lk, done), true)
+                                         : srv->cv_done.wait_for(lk, std::chrono::nanoseconds(timeout_ns), done);
     auto it = srv->jobs.find(job_id);
     if (it == srv->jobs.end()) return CNN_ERR_INVALID_ARG;
-    auto done = [&] { return srv->jobs[job_id].state == CNN_JOB_DONE; };
-    if (timeout_ns < 0) {
-        srv->cv_done.wait(lk, done);
-    } else if (!srv->cv_done.wait_for(lk, std::chrono::nanoseconds(timeout_ns), done)) {
-        fill_info(srv->jobs[job_id], info);
-        return CNN_ERR_TIMEOUT;
-    }
-    fill_info(srv->jobs[job_id], info);
-    return CNN_OK;
+    fill_info(it->second, info);
+    return finished ? CNN_OK : CNN_ERR_TIMEOUT;
 }
 
 CNN_API cnn_status cnn_job_error(cnn_server *srv, int64_t job_id, char *buf, int64_t size) {
@@ -403,6 +404,7 @@ CNN_API cnn_status cnn_job_release(cnn_server *srv, int64_t job_id) {
     if (it == srv->jobs.end()) return CNN_ERR_INVALID_ARG;
     if (it->second.state != CNN_JOB_DONE) return CNN_ERR_STATE;
     srv->jobs.erase(it);
+    srv->cv_done.notify_all();  // a waiter on this id returns
     return CNN_OK;
 }
 
