@@ -159,3 +159,38 @@ def test_gram_searches_of_different_widths_in_threads(serve):
     assert not errors, errors
     for (wo, wi), (go, gi) in zip(want, got):
         assert np.array_equal(wo, go) and np.array_equal(wi, gi)
+
+
+def test_job_states_wait_timeout_and_release(serve):
+    """cnn_poll / cnn_wait / cnn_job_release semantics: a job is QUEUED or
+    RUNNING until DONE, a zero wait limit returns CNN_ERR_TIMEOUT or the
+    done job, a job cannot be released before it is done and its id is
+    invalid after."""
+    import ctypes
+    from commonnnclustering_gb300 import _abi, workloads
+    srv = _abi.NativeServer(0, 1, 8 << 30)
+    try:
+        xs = [workloads.md3d(n=60000, seed=s) for s in range(3)]
+        ids = [srv.submit(x, 0.1 ** 2, 12, 11, member_cutoff=50) for x in xs]
+        states = [srv.poll(i)["state"] for i in ids]
+        assert all(s in (_abi.JOB_QUEUED, _abi.JOB_RUNNING, _abi.JOB_DONE) for s in states)
+        info = _abi.cnn_job_info()
+        st = srv._lib.cnn_wait(srv._h, ids[-1], 0, ctypes.byref(info))
+        assert st in (_abi.CNN_OK, _abi.CNN_ERR_TIMEOUT)
+        if st == _abi.CNN_ERR_TIMEOUT:
+            assert info.state != _abi.JOB_DONE
+            assert srv._lib.cnn_job_release(srv._h, ids[-1]) == _abi.CNN_ERR_STATE
+        assert srv._lib.cnn_wait(srv._h, ids[-1], -1, ctypes.byref(info)) == _abi.CNN_OK
+        assert info.state == _abi.JOB_DONE and info.result == _abi.CNN_OK
+        assert info.t_submit <= info.t_start <= info.t_done
+        for i in ids[:-1]:
+            labels, inf = srv.wait(i)      # waits, then releases the record
+            assert inf["state"] == _abi.JOB_DONE
+            assert srv._lib.cnn_poll(srv._h, i, ctypes.byref(info)) == _abi.CNN_ERR_INVALID_ARG
+        assert srv._lib.cnn_job_release(srv._h, ids[-1]) == _abi.CNN_OK
+        assert srv._lib.cnn_job_release(srv._h, ids[-1]) == _abi.CNN_ERR_INVALID_ARG
+        st = srv.stats()
+        assert st["done"] == 3 and st["failed"] == 0 and st["max_running"] == 1
+    finally:
+        srv._keep.clear()
+        srv.close()
