@@ -351,9 +351,12 @@ cnn_status mask_pair_weights(cnn_context *ctx, const int64_t *off, const int32_t
 cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
                     int64_t current_start, uint8_t *consider_dev, int64_t *labels_dev,
                     const int32_t *seed_a = nullptr, const int32_t *seed_b = nullptr,
-                    const int2 *edge_list = nullptr, const unsigned long long *edge_count = nullptr);
+                    const int2 *edge_list = nullptr, const unsigned long long *edge_count = nullptr,
+                    int2 *wl_buf = nullptr, int64_t wl_buf_cap = 0);
 // edge_list (device, count on the device): the pairs (a, b > a) that can
-// still cross -- those a finished fit refining this one left open
+// still cross -- those a finished fit refining this one left open.
+// wl_buf (optional): the cross-pair worklist with room for wl_buf_cap pairs
+// (at least the pairs a pass can emit: no overflow pass)
 cnn_status open_pairs_impl(cnn_context *ctx, const int2 *in_list, const unsigned long long *in_count, int2 *out,
                            unsigned long long *out_count, int64_t cap);
 // sort_by_size of the labels a fit from fresh labels just wrote (no host
@@ -370,7 +373,8 @@ cnn_status check_lists_impl(cnn_context *ctx, const int32_t *a, int64_t na, cons
 cnn_status fit_and_sort_into(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
                              int64_t sort_member_cutoff, int64_t max_clusters, int64_t *labels_dev,
                              const int32_t *seed_a = nullptr, const int32_t *seed_b = nullptr, bool sort = true,
-                             const int2 *edge_list = nullptr, const unsigned long long *edge_count = nullptr);
+                             const int2 *edge_list = nullptr, const unsigned long long *edge_count = nullptr,
+                             int2 *wl_buf = nullptr, int64_t wl_buf_cap = 0);
 
 // sweep.cu
 cnn_status sweep_impl(cnn_context *ctx, const double *radius_cutoffs, int32_t n_radii,

@@ -469,14 +469,36 @@ __global__ void apply_dense_kernel(int64_t *__restrict__ labels, int64_t n, int6
 // radix-sorted on the size bits only (the label bits are ascending already);
 // key q gives its label the new label q + 1, or 0 past max_clusters or
 // below member_cutoff -- the same rule as new_label_kernel.
-__global__ void fresh_count_kernel(const int64_t *__restrict__ labels, int64_t n, int32_t *__restrict__ cnt) {
+// Up to kFreshSmemBins labels (the count read on the device) each block
+// counts in shared memory and adds its nonzero bins once; more labels go to
+// global atomics directly.  Either way warps first merge equal labels.
+constexpr int kFreshSmemBins = 2048;
+
+__global__ void __launch_bounds__(256) fresh_count_kernel(const int64_t *__restrict__ labels, int64_t n,
+                                                          const int64_t *__restrict__ k_dev,
+                                                          int32_t *__restrict__ cnt) {
+    __shared__ int32_t s_cnt[kFreshSmemBins];
+    const int64_t k = *k_dev < n ? *k_dev : n;
+    const bool local = k <= kFreshSmemBins;  // block-uniform
+    if (local) {
+        for (int i = threadIdx.x; i < (int)k; i += blockDim.x) s_cnt[i] = 0;
+        __syncthreads();
+    }
     const int lane = threadIdx.x & 31;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
         const int64_t i = base + lane;
         const int64_t v = i < n ? labels[i] : 0;
         const unsigned peers = __match_any_sync(0xffffffffu, v);
-        if (v > 0 && v <= n && lane == __ffs(peers) - 1) atomicAdd(&cnt[v - 1], __popc(peers));
+        if (v > 0 && v <= k && lane == __ffs(peers) - 1) {
+            if (local) atomicAdd(&s_cnt[v - 1], __popc(peers));
+            else atomicAdd(&cnt[v - 1], __popc(peers));
+        }
+    }
+    if (local) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < (int)k; i += blockDim.x)
+            if (s_cnt[i]) atomicAdd(&cnt[i], s_cnt[i]);
     }
 }
 
@@ -574,7 +596,8 @@ __global__ void seed_union_kernel(int64_t n, const uint8_t *__restrict__ node, i
 
 cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff, int64_t current_start,
                     uint8_t *consider_dev, int64_t *labels_dev, const int32_t *seed_a, const int32_t *seed_b,
-                    const int2 *edge_list, const unsigned long long *edge_count) {
+                    const int2 *edge_list, const unsigned long long *edge_count, int2 *wl_buf,
+                    int64_t wl_buf_cap) {
     if (!ctx->have_graph) return ctx->fail(CNN_ERR_STATE, "no neighbour graph: call cnn_build_neighbours first");
     CNN_TRY(ensure_lists(ctx));
     const int64_t n = ctx->n;
@@ -636,23 +659,30 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     // holds more cross pairs than the graph-fed one after its hook pass;
     // overflow falls back to the full lazy pass (measured on the 1M-point
     // sweep: nnz/4 for lists, nnz/16 for the graph)
-    const int64_t wl_cap = std::max<int64_t>(int64_t(1) << 20, ctx->nnz / (edge_list ? 4 : 16));
-    CNN_TRY(ctx->ensure(ctx->io_c, sizeof(int2) * (size_t)wl_cap));
+    int64_t wl_cap = std::max<int64_t>(int64_t(1) << 20, ctx->nnz / (edge_list ? 4 : 16));
+    int2 *wl = nullptr;
+    if (wl_buf && wl_buf_cap > 0) {  // the caller's room: every pair the filter can emit
+        wl = wl_buf;
+        wl_cap = wl_buf_cap;
+    } else {
+        CNN_TRY(ctx->ensure(ctx->io_c, sizeof(int2) * (size_t)wl_cap));
+        wl = ctx->io_c.as<int2>();
+    }
     unsigned long long *wl_count = counters + 8;
     CNN_CUDA(ctx, cudaMemsetAsync(wl_count, 0, sizeof(unsigned long long), st));
     if (edge_list) {
         // only pairs a finished fit that refines this one left open can cross
-        cross_filter_list_kernel<<<ctx->sm_count * 16u, 256, 0, st>>>(edge_list, edge_count, parent, ctx->io_c.as<int2>(),
+        cross_filter_list_kernel<<<ctx->sm_count * 16u, 256, 0, st>>>(edge_list, edge_count, parent, wl,
                                                              wl_count, wl_cap);
     } else {
         cross_filter_kernel<<<resident((const void *)cross_filter_kernel, 256, 0), 256, 0, st>>>(
-            n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, ctx->io_c.as<int2>(), wl_count, wl_cap,
+            n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, wl, wl_count, wl_cap,
             split);
     }
     CNN_LAUNCH_CHECK(ctx);
     edge_check_kernel<<<resident((const void *)edge_check_kernel, kCheckWarps * 32, 0), kCheckWarps * 32,
                         0, st>>>(
-        ctx->io_c.as<int2>(), wl_count, wl_cap, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent,
+        wl, wl_count, wl_cap, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent,
         (int32_t)similarity_cutoff, counters);
     CNN_LAUNCH_CHECK(ctx);
     check_union_if_overflow_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(
@@ -838,7 +868,8 @@ cnn_status sort_fresh_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64_t
         }
     }
     CNN_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (size_t)(k_host >= 0 ? k_host : n), st));
-    fresh_count_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(labels, n, cnt);
+    fresh_count_kernel<<<std::min<unsigned>(blocks_for(ctx, n), 2 * ctx->sm_count), 256, 0, st>>>(labels, n, k_dev,
+                                                                                            cnt);
     CNN_LAUNCH_CHECK(ctx);
     if (k_host >= 0 && k_host <= kOrderSmall) {
         const size_t smem = sizeof(uint64_t) * (size_t)k_host;
@@ -893,7 +924,7 @@ cnn_status sort_fresh_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64_t
 cnn_status fit_and_sort_into(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff,
                              int64_t sort_member_cutoff, int64_t max_clusters, int64_t *labels_dev,
                              const int32_t *seed_a, const int32_t *seed_b, bool sort, const int2 *edge_list,
-                             const unsigned long long *edge_count) {
+                             const unsigned long long *edge_count, int2 *wl_buf, int64_t wl_buf_cap) {
     const int64_t n = ctx->n;
     cudaStream_t st = ctx->stream;
     if (n == 0) return CNN_OK;
@@ -901,7 +932,7 @@ cnn_status fit_and_sort_into(cnn_context *ctx, int64_t similarity_cutoff, int64_
     CNN_CUDA(ctx, cudaMemsetAsync(labels_dev, 0, sizeof(int64_t) * (size_t)n, st));
     CNN_CUDA(ctx, cudaMemsetAsync(ctx->sweep_consider.ptr, 1, (size_t)n, st));
     CNN_TRY(fit_impl(ctx, similarity_cutoff, n_member_cutoff, 1, ctx->sweep_consider.as<uint8_t>(), labels_dev,
-                     seed_a, seed_b, edge_list, edge_count));
+                     seed_a, seed_b, edge_list, edge_count, wl_buf, wl_buf_cap));
     return sort ? sort_fresh_impl(ctx, labels_dev, n, sort_member_cutoff, max_clusters, true) : CNN_OK;
 }
 

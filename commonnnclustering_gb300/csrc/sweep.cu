@@ -340,9 +340,11 @@ cnn_status sweep_impl(cnn_context *ctx, const double *rcs_in, int32_t n_radii, c
             const int32_t *sa = have[j] && sim_cut[j] >= 0 ? forest + (size_t)j * n : nullptr;
             const int32_t *sb = best >= 0 ? forest + (size_t)best * n : nullptr;
             const bool use_list = lists && list_valid && best == last;
+            // the next open-pairs list is written after the fit: its buffer
+            // (room for every pair b > a) holds this fit's cross-pair worklist
             CNN_TRY(fit_and_sort_into(ctx, sim_cut[j], member_cut[j], sort_member_cutoff, max_clusters,
                                       labels_dev + out * n, sa, sb, sort, use_list ? cur : nullptr,
-                                      use_list ? ccur : nullptr));
+                                      use_list ? ccur : nullptr, lists ? nxt : nullptr, lists ? half : 0));
             // after the fit the union-find array holds every node's root (-1 elsewhere)
             if (n > 0)
                 CNN_CUDA(ctx, cudaMemcpyAsync(forest + (size_t)j * n, ctx->parent.ptr, sizeof(int32_t) * (size_t)n,
