@@ -54,48 +54,65 @@ __device__ __forceinline__ double exact_s(const double *__restrict__ x, int d, i
 // One warp per row of the r_max graph (internal order): bucket of each pair.
 // With deg_all, the same pass counts each row's pairs of every radius below
 // the largest (bucket <= k) into deg_all[k * (n + 1) + p] (entry n: 0).
-__global__ void bucket_kernel(const double *__restrict__ x, int d, int64_t n, const int32_t *__restrict__ perm,
-                              const float4 *__restrict__ xf4, const int64_t *__restrict__ row_off,
-                              const int32_t *__restrict__ cols, Ladder lad, uint8_t *__restrict__ bucket,
-                              unsigned long long *__restrict__ n_exact, int kf, int32_t *__restrict__ deg_all) {
-    const int lane = threadIdx.x & 31;
+// The ladder sits in shared memory (lanes index it by their own radius) and
+// every lane counts its pairs per bucket in its own shared-memory column.
+__global__ void __launch_bounds__(256) bucket_kernel(const double *__restrict__ x, int d, int64_t n,
+                                                     const int32_t *__restrict__ perm,
+                                                     const float4 *__restrict__ xf4,
+                                                     const int64_t *__restrict__ row_off,
+                                                     const int32_t *__restrict__ cols, Ladder lad,
+                                                     uint8_t *__restrict__ bucket,
+                                                     unsigned long long *__restrict__ n_exact, int kf,
+                                                     int32_t *__restrict__ deg_all) {
+    __shared__ float s_in[kMaxRadii], s_out[kMaxRadii];
+    __shared__ double s_rc[kMaxRadii];
+    __shared__ int32_t s_cnt[8][kMaxRadii][32];  // [warp][bucket][lane]
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x < kMaxRadii) {
+        s_in[threadIdx.x] = threadIdx.x < lad.k ? lad.thr_in[threadIdx.x] : INFINITY;
+        s_out[threadIdx.x] = threadIdx.x < lad.k ? lad.thr_out[threadIdx.x] : INFINITY;
+        s_rc[threadIdx.x] = threadIdx.x < lad.k ? lad.rc[threadIdx.x] : INFINITY;
+    }
+#pragma unroll
+    for (int b = 0; b < kMaxRadii; ++b) s_cnt[w][b][lane] = 0;
+    __syncthreads();
     const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (deg_all && p == 0 && lane < kf) deg_all[(int64_t)lane * (n + 1) + n] = 0;
-    if (p >= n) return;
-    int32_t per_radius[kMaxRadii - 1];
-#pragma unroll
-    for (int k = 0; k < kMaxRadii - 1; ++k) per_radius[k] = 0;
+    if (p >= n) return;  // whole warps (nothing below syncs the block)
     const float4 q = xf4[p];
     const int32_t ip = perm[p];
     unsigned long long ex = 0;
+    const int kl = lad.k - 1;
     for (int64_t e = row_off[p] + lane; e < row_off[p + 1]; e += 32) {
         const int32_t j = cols[e];
         const float4 c = xf4[j];
         const float dx = q.x - c.x, dy = q.y - c.y, dz = q.z - c.z;
         const float sf = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        // radii that are certainly too small (the thresholds ascend)
         int k = 0;
-        while (k < lad.k - 1 && sf > lad.thr_out[k]) ++k;  // radii that are certainly too small
+#pragma unroll
+        for (int kk = 0; kk < kMaxRadii - 1; ++kk) k += (kk < kl) & (sf > s_out[kk]);
         int b = k;
-        if (!(sf <= lad.thr_in[k])) {  // inside the band of radius k: decide in float64
+        if (!(sf <= s_in[k])) {  // inside the band of radius k: decide in float64
             double s = exact_s(x, d, ip, perm[j], lad.fpmode);
             if (lad.metric == CNN_METRIC_EUCLIDEAN) s = __dsqrt_rn(s);
             b = lad.k - 1;
             for (int kk = k; kk < lad.k; ++kk)
-                if (s <= lad.rc[kk]) {
+                if (s <= s_rc[kk]) {
                     b = kk;
                     break;
                 }
             ++ex;
         }
         bucket[e] = (uint8_t)b;
-#pragma unroll
-        for (int k = 0; k < kMaxRadii - 1; ++k) per_radius[k] += b <= k;
+        ++s_cnt[w][b][lane];
     }
     if (deg_all) {
-#pragma unroll
-        for (int k = 0; k < kMaxRadii - 1; ++k) {
-            if (k >= kf) break;
-            const int32_t t = __reduce_add_sync(0xffffffffu, per_radius[k]);
+        __syncwarp();
+        int32_t run = 0;  // this lane's pairs of buckets <= k
+        for (int k = 0; k < kf; ++k) {
+            run += s_cnt[w][k][lane];
+            const int32_t t = __reduce_add_sync(0xffffffffu, run);
             if (lane == 0) deg_all[(int64_t)k * (n + 1) + p] = t;
         }
     }
