@@ -41,8 +41,8 @@ def test_tensor_entry_counts_the_issued_mmas(bench):
 
 
 def test_default_run_covers_every_workload(bench):
-    """The driver's default invocation measures the headline and the four
-    other workloads (sub-records of the same JSON line)."""
+    """bench.py without arguments measures the headline and the four other
+    workloads (sub-records of the same JSON line)."""
     assert bench.HEADLINE == "md3d-200k"
     names = {bench.WORKLOADS[w]["name"] for w in bench.SUB_WORKLOADS}
     assert names == {"blobs2d-5k", "features-500k-d64", "nested3d-1m-sweep", "serve-stream"}
