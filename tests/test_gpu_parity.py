@@ -407,3 +407,33 @@ def test_fit_fresh_equals_fit_then_sort(cnn, mem, strategy):
             assert np.array_equal(got, want), (sc, nm, mc, mx, sort)
     finally:
         ctx.close()
+
+
+def test_fit_fresh_on_other_graphs(cnn):
+    """cnn_fit_fresh after the tensor-core search (n_dim 16, the graph in the
+    search's pivot-grouped order), after precomputed neighbourhoods
+    (cnn_set_neighbours) and with only noise: the labels of cnn_fit +
+    cnn_sort_by_size."""
+    from commonnnclustering_gb300 import workloads
+    x = workloads.features(n=6000, d=16, seed=21, n_clusters=6)
+    ctx = cnn.Context(0)
+    try:
+        ctx.set_points(x)
+        for r2, sc, nm in ((1.6 ** 2, 7, 6), (1.6 ** 2, 2000, 1999)):  # the second: no node, all noise
+            ctx.build_neighbours(r2)
+            assert ctx.stats()["search_kind"] == 3
+            want = np.zeros(x.shape[0], dtype=np.int64)
+            ctx.fit(sc, nm, 1, np.ones(x.shape[0], dtype=np.uint8), want)
+            ctx.sort_by_size(want, 5, None)
+            ctx.build_neighbours(r2)
+            got = ctx.fit_fresh(sc, nm, True, 5, None)
+            assert np.array_equal(got, want), (sc, nm)
+        off, idx = ctx.get_neighbours()
+        ctx.set_neighbours(off, idx)
+        want = np.zeros(x.shape[0], dtype=np.int64)
+        ctx.fit(7, 6, 1, np.ones(x.shape[0], dtype=np.uint8), want)
+        ctx.sort_by_size(want, 3, 4)
+        got = ctx.fit_fresh(7, 6, True, 3, 4)
+        assert np.array_equal(got, want)
+    finally:
+        ctx.close()
