@@ -177,6 +177,9 @@ def lib_path() -> str:
     return _build.LIB
 
 
+ABI_VERSION = 2  # CNN_ABI_VERSION of include/cnngpu.h
+
+
 def load(build_if_missing: bool = True):
     """Load libcnngpu.so (building it first when it is missing or stale)."""
     global _lib
@@ -193,6 +196,9 @@ def load(build_if_missing: bool = True):
                 f = getattr(L, name)
                 f.restype = res
                 f.argtypes = args
+            if L.cnn_abi_version() != ABI_VERSION:  # the structs below mirror this version's header
+                raise ImportError(f"{path} has ABI version {L.cnn_abi_version()}, this binding expects "
+                                  f"{ABI_VERSION}: rebuild it")
             _lib = L
     return _lib
 
