@@ -40,6 +40,11 @@ namespace cnn {
 namespace {
 
 // ---- cross-edge worklist ------------------------------------------------------
+#ifndef CNN_FILTER_UNROLL
+#define CNN_FILTER_UNROLL 4
+#endif
+constexpr int kFilterUnroll = CNN_FILTER_UNROLL;  // row entries per lane per step of the pair filters
+
 // After the hook pass and a full compression, parent[] holds every node's
 // root.  A read-only pass streams the graph and keeps only candidate edges
 // (a, b > a, both nodes) whose roots differ; everything else is already
@@ -66,21 +71,35 @@ __global__ void __launch_bounds__(256) cross_filter_kernel(int64_t n, const int6
         if (pa < 0) continue;
         const int64_t s = __shfl_sync(0xffffffffu, v, 1), e = __shfl_sync(0xffffffffu, v, 2);
         const int64_t split_a = __shfl_sync(0xffffffffu, v, 3);
-        for (int64_t k0 = split ? s + split_a : warp_upper_bound(cols, s, e, a, lane); k0 < e; k0 += 32) {
-            const int64_t k = k0 + lane;
-            int32_t b = -1, pb = -1;
-            if (k < e) {
-                b = cols[k];
-                if (b > a) pb = parent[b];
+        // 128 entries per step, four per lane: the column loads, then the
+        // parent loads, are in flight together; one worklist atomic per step
+        for (int64_t k0 = split ? s + split_a : warp_upper_bound(cols, s, e, a, lane); k0 < e;
+             k0 += kFilterUnroll * 32) {
+            int32_t b[kFilterUnroll], pb[kFilterUnroll];
+#pragma unroll
+            for (int u = 0; u < kFilterUnroll; ++u) {
+                const int64_t k = k0 + u * 32 + lane;
+                b[u] = k < e ? cols[k] : -1;
             }
-            const bool cross = pb >= 0 && pb != pa;
-            const unsigned mask = __ballot_sync(0xffffffffu, cross);
-            if (!mask) continue;
+#pragma unroll
+            for (int u = 0; u < kFilterUnroll; ++u) pb[u] = b[u] > a ? parent[b[u]] : -1;
+            unsigned mask[kFilterUnroll];
+            int total = 0;
+#pragma unroll
+            for (int u = 0; u < kFilterUnroll; ++u) {
+                mask[u] = __ballot_sync(0xffffffffu, pb[u] >= 0 && pb[u] != pa);
+                total += __popc(mask[u]);
+            }
+            if (!total) continue;
             unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(wl_count, (unsigned long long)__popc(mask));
+            if (lane == 0) base = atomicAdd(wl_count, (unsigned long long)total);
             base = __shfl_sync(0xffffffffu, base, 0);
-            const unsigned long long idx = base + __popc(mask & lt);
-            if (cross && idx < (unsigned long long)cap) wl[idx] = make_int2(a, b);
+#pragma unroll
+            for (int u = 0; u < kFilterUnroll; ++u) {
+                const unsigned long long idx = base + __popc(mask[u] & lt);
+                if (((mask[u] >> lane) & 1u) && idx < (unsigned long long)cap) wl[idx] = make_int2(a, b[u]);
+                base += __popc(mask[u]);
+            }
         }
     }
 }
@@ -136,16 +155,37 @@ __global__ void __launch_bounds__(256) open_pairs_csr_kernel(int64_t n, const in
     for (int64_t a64 = warp0; a64 < n; a64 += nwarps) {
         const int32_t a = (int32_t)a64;
         const int64_t s = row_off[a], e = row_off[a + 1];
-        for (int64_t k0 = warp_upper_bound(cols, s, e, a, lane); k0 < e; k0 += 32) {
-            const int64_t k = k0 + lane;
-            const int32_t b = k < e ? cols[k] : -1;
-            const bool keep = b > a && pair_open(node, parent, a, b);
-            const unsigned mask = __ballot_sync(0xffffffffu, keep);
-            if (!mask) continue;
+        // pair_open(a, b) with a's node flag and root read once per row
+        const bool na = node[a] != 0;
+        const int32_t ra = parent[a];
+        for (int64_t k0 = warp_upper_bound(cols, s, e, a, lane); k0 < e; k0 += kFilterUnroll * 32) {
+            int32_t b[kFilterUnroll];
+#pragma unroll
+            for (int u = 0; u < kFilterUnroll; ++u) {  // four entries per lane in flight
+                const int64_t k = k0 + u * 32 + lane;
+                b[u] = k < e ? cols[k] : -1;
+            }
+            bool keep[kFilterUnroll];
+#pragma unroll
+            for (int u = 0; u < kFilterUnroll; ++u)
+                keep[u] = b[u] > a && !(na && node[b[u]] && ra == parent[b[u]]);
+            unsigned mask[kFilterUnroll];
+            int total = 0;
+#pragma unroll
+            for (int u = 0; u < kFilterUnroll; ++u) {
+                mask[u] = __ballot_sync(0xffffffffu, keep[u]);
+                total += __popc(mask[u]);
+            }
+            if (!total) continue;
             unsigned long long w = 0;
-            if (lane == 0) w = atomicAdd(out_count, (unsigned long long)__popc(mask));
-            w = __shfl_sync(0xffffffffu, w, 0) + __popc(mask & lt);
-            if (keep && w < (unsigned long long)cap) out[w] = make_int2(a, b);
+            if (lane == 0) w = atomicAdd(out_count, (unsigned long long)total);
+            w = __shfl_sync(0xffffffffu, w, 0);
+#pragma unroll
+            for (int u = 0; u < kFilterUnroll; ++u) {
+                const unsigned long long idx = w + __popc(mask[u] & lt);
+                if (keep[u] && idx < (unsigned long long)cap) out[idx] = make_int2(a, b[u]);
+                w += __popc(mask[u]);
+            }
         }
     }
 }

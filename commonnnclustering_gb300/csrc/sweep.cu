@@ -25,6 +25,13 @@ namespace cnn {
 namespace {
 
 constexpr int kMaxRadii = 16;
+#ifndef CNN_BUCKET_UNROLL
+#define CNN_BUCKET_UNROLL 4
+#endif
+constexpr int kBucketUnroll = CNN_BUCKET_UNROLL;  // row entries per lane per step of the per-row passes
+#ifndef CNN_BUCKET_MIN_BLOCKS
+#define CNN_BUCKET_MIN_BLOCKS 4  // 64 registers (a few bytes spilled) for four blocks per SM
+#endif
 
 struct Ladder {
     int32_t k;                  // number of radii
@@ -56,7 +63,7 @@ __device__ __forceinline__ double exact_s(const double *__restrict__ x, int d, i
 // the largest (bucket <= k) into deg_all[k * (n + 1) + p] (entry n: 0).
 // The ladder sits in shared memory (lanes index it by their own radius) and
 // every lane counts its pairs per bucket in its own shared-memory column.
-__global__ void __launch_bounds__(256) bucket_kernel(const double *__restrict__ x, int d, int64_t n,
+__global__ void __launch_bounds__(256, CNN_BUCKET_MIN_BLOCKS) bucket_kernel(const double *__restrict__ x, int d, int64_t n,
                                                      const int32_t *__restrict__ perm,
                                                      const float4 *__restrict__ xf4,
                                                      const int64_t *__restrict__ row_off,
@@ -83,29 +90,44 @@ __global__ void __launch_bounds__(256) bucket_kernel(const double *__restrict__ 
     const int32_t ip = perm[p];
     unsigned long long ex = 0;
     const int kl = lad.k - 1;
-    for (int64_t e = row_off[p] + lane; e < row_off[p + 1]; e += 32) {
-        const int32_t j = cols[e];
-        const float4 c = xf4[j];
-        const float dx = q.x - c.x, dy = q.y - c.y, dz = q.z - c.z;
-        const float sf = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        // radii that are certainly too small (the thresholds ascend)
-        int k = 0;
+    const int64_t e_end = row_off[p + 1];
+    // 128 entries per step, four per lane: their column loads, then their
+    // coordinate gathers, are in flight together
+    for (int64_t e0 = row_off[p]; e0 < e_end; e0 += kBucketUnroll * 32) {
+        int32_t jv[kBucketUnroll];
+        float4 cv[kBucketUnroll];
 #pragma unroll
-        for (int kk = 0; kk < kMaxRadii - 1; ++kk) k += (kk < kl) & (sf > s_out[kk]);
-        int b = k;
-        if (!(sf <= s_in[k])) {  // inside the band of radius k: decide in float64
-            double s = exact_s(x, d, ip, perm[j], lad.fpmode);
-            if (lad.metric == CNN_METRIC_EUCLIDEAN) s = __dsqrt_rn(s);
-            b = lad.k - 1;
-            for (int kk = k; kk < lad.k; ++kk)
-                if (s <= s_rc[kk]) {
-                    b = kk;
-                    break;
-                }
-            ++ex;
+        for (int u = 0; u < kBucketUnroll; ++u) {
+            const int64_t e = e0 + u * 32 + lane;
+            jv[u] = e < e_end ? cols[e] : -1;
         }
-        bucket[e] = (uint8_t)b;
-        ++s_cnt[w][b][lane];
+#pragma unroll
+        for (int u = 0; u < kBucketUnroll; ++u) cv[u] = jv[u] >= 0 ? xf4[jv[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < kBucketUnroll; ++u) {
+            if (jv[u] < 0) continue;
+            const int64_t e = e0 + u * 32 + lane;
+            const float dx = q.x - cv[u].x, dy = q.y - cv[u].y, dz = q.z - cv[u].z;
+            const float sf = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            // radii that are certainly too small (the thresholds ascend)
+            int k = 0;
+#pragma unroll
+            for (int kk = 0; kk < kMaxRadii - 1; ++kk) k += (kk < kl) & (sf > s_out[kk]);
+            int b = k;
+            if (!(sf <= s_in[k])) {  // inside the band of radius k: decide in float64
+                double s = exact_s(x, d, ip, perm[jv[u]], lad.fpmode);
+                if (lad.metric == CNN_METRIC_EUCLIDEAN) s = __dsqrt_rn(s);
+                b = lad.k - 1;
+                for (int kk = k; kk < lad.k; ++kk)
+                    if (s <= s_rc[kk]) {
+                        b = kk;
+                        break;
+                    }
+                ++ex;
+            }
+            bucket[e] = (uint8_t)b;
+            ++s_cnt[w][b][lane];
+        }
     }
     if (deg_all) {
         __syncwarp();
@@ -169,18 +191,26 @@ __global__ void __launch_bounds__(256) multi_fill_kernel(int64_t n, const int64_
 #pragma unroll
         for (int k = 0; k < kMaxFiltered; ++k) w[k] = k < kf ? base[k] + off_all[(int64_t)k * (n + 1) + p] : 0;
         const int64_t e1 = row_off[p + 1];
-        for (int64_t e0 = row_off[p]; e0 < e1; e0 += 32) {
-            const int64_t e = e0 + lane;
-            const bool valid = e < e1;
-            const int b = valid ? bucket[e] : 255;
-            const int32_t c = valid ? cols[e] : 0;
+        for (int64_t e0 = row_off[p]; e0 < e1; e0 += kBucketUnroll * 32) {
+            int bv[kBucketUnroll];
+            int32_t cv[kBucketUnroll];
 #pragma unroll
-            for (int k = 0; k < kMaxFiltered; ++k) {
-                if (k >= kf) break;
-                const bool keep = b <= k;
-                const unsigned m = __ballot_sync(0xffffffffu, keep);
-                if (keep) cols_all[w[k] + __popc(m & lt)] = c;
-                w[k] += __popc(m);
+            for (int u = 0; u < kBucketUnroll; ++u) {  // four entries per lane in flight
+                const int64_t e = e0 + u * 32 + lane;
+                const bool valid = e < e1;
+                bv[u] = valid ? bucket[e] : 255;
+                cv[u] = valid ? cols[e] : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < kBucketUnroll; ++u) {  // in entry order: the rows stay sorted
+#pragma unroll
+                for (int k = 0; k < kMaxFiltered; ++k) {
+                    if (k >= kf) break;
+                    const bool keep = bv[u] <= k;
+                    const unsigned m = __ballot_sync(0xffffffffu, keep);
+                    if (keep) cols_all[w[k] + __popc(m & lt)] = cv[u];
+                    w[k] += __popc(m);
+                }
             }
         }
     }
