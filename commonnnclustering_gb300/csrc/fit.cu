@@ -40,10 +40,17 @@ namespace cnn {
 namespace {
 
 // ---- cross-edge worklist ------------------------------------------------------
+// row entries per lane per step of the pair filters: 4 for the cross filter
+// every fit runs (rows of a few hundred entries b > a), 8 for the sweep's
+// passes over long rows and flat edge lists
 #ifndef CNN_FILTER_UNROLL
 #define CNN_FILTER_UNROLL 4
 #endif
-constexpr int kFilterUnroll = CNN_FILTER_UNROLL;  // row entries per lane per step of the pair filters
+#ifndef CNN_LIST_UNROLL
+#define CNN_LIST_UNROLL 8
+#endif
+constexpr int kFilterUnroll = CNN_FILTER_UNROLL;
+constexpr int kListUnroll = CNN_LIST_UNROLL;
 
 // After the hook pass and a full compression, parent[] holds every node's
 // root.  A read-only pass streams the graph and keeps only candidate edges
@@ -71,8 +78,9 @@ __global__ void __launch_bounds__(256) cross_filter_kernel(int64_t n, const int6
         if (pa < 0) continue;
         const int64_t s = __shfl_sync(0xffffffffu, v, 1), e = __shfl_sync(0xffffffffu, v, 2);
         const int64_t split_a = __shfl_sync(0xffffffffu, v, 3);
-        // 128 entries per step, four per lane: the column loads, then the
-        // parent loads, are in flight together; one worklist atomic per step
+        // 32 kFilterUnroll entries per step, kFilterUnroll per lane: the column
+        // loads, then the parent loads, are in flight together; one worklist
+        // atomic per step
         for (int64_t k0 = split ? s + split_a : warp_upper_bound(cols, s, e, a, lane); k0 < e;
              k0 += kFilterUnroll * 32) {
             int32_t b[kFilterUnroll], pb[kFilterUnroll];
@@ -115,22 +123,40 @@ __global__ void __launch_bounds__(256) cross_filter_list_kernel(const int2 *__re
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int64_t total = (int64_t)*count;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
-        const int64_t e = base + lane;
-        int2 ed = make_int2(-1, -1);
-        bool cross = false;
-        if (e < total) {
-            ed = edges[e];
-            const int32_t pa = parent[ed.x], pb = parent[ed.y];
-            cross = pa >= 0 && pb >= 0 && pa != pb;
+    // each warp takes 32 kListUnroll consecutive edges per step, kListUnroll
+    // per lane: the edge loads, then the parent loads, are in flight together
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x * kListUnroll;
+    for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31)) * kListUnroll; base < total;
+         base += stride) {
+        int2 ed[kListUnroll];
+#pragma unroll
+        for (int u = 0; u < kListUnroll; ++u) {
+            const int64_t e = base + u * 32 + lane;
+            ed[u] = e < total ? edges[e] : make_int2(-1, -1);
         }
-        const unsigned mask = __ballot_sync(0xffffffffu, cross);
-        if (!mask) continue;
+        int32_t pa[kListUnroll], pb[kListUnroll];
+#pragma unroll
+        for (int u = 0; u < kListUnroll; ++u) {
+            pa[u] = ed[u].x >= 0 ? parent[ed[u].x] : -1;
+            pb[u] = ed[u].x >= 0 ? parent[ed[u].y] : -1;
+        }
+        unsigned mask[kListUnroll];
+        int n_cross = 0;
+#pragma unroll
+        for (int u = 0; u < kListUnroll; ++u) {
+            mask[u] = __ballot_sync(0xffffffffu, pa[u] >= 0 && pb[u] >= 0 && pa[u] != pb[u]);
+            n_cross += __popc(mask[u]);
+        }
+        if (!n_cross) continue;
         unsigned long long w = 0;
-        if (lane == 0) w = atomicAdd(wl_count, (unsigned long long)__popc(mask));
-        w = __shfl_sync(0xffffffffu, w, 0) + __popc(mask & lt);
-        if (cross && w < (unsigned long long)cap) wl[w] = ed;
+        if (lane == 0) w = atomicAdd(wl_count, (unsigned long long)n_cross);
+        w = __shfl_sync(0xffffffffu, w, 0);
+#pragma unroll
+        for (int u = 0; u < kListUnroll; ++u) {
+            const unsigned long long idx = w + __popc(mask[u] & lt);
+            if (((mask[u] >> lane) & 1u) && idx < (unsigned long long)cap) wl[idx] = ed[u];
+            w += __popc(mask[u]);
+        }
     }
 }
 
@@ -158,21 +184,21 @@ __global__ void __launch_bounds__(256) open_pairs_csr_kernel(int64_t n, const in
         // pair_open(a, b) with a's node flag and root read once per row
         const bool na = node[a] != 0;
         const int32_t ra = parent[a];
-        for (int64_t k0 = warp_upper_bound(cols, s, e, a, lane); k0 < e; k0 += kFilterUnroll * 32) {
-            int32_t b[kFilterUnroll];
+        for (int64_t k0 = warp_upper_bound(cols, s, e, a, lane); k0 < e; k0 += kListUnroll * 32) {
+            int32_t b[kListUnroll];
 #pragma unroll
-            for (int u = 0; u < kFilterUnroll; ++u) {  // four entries per lane in flight
+            for (int u = 0; u < kListUnroll; ++u) {  // kListUnroll entries per lane in flight
                 const int64_t k = k0 + u * 32 + lane;
                 b[u] = k < e ? cols[k] : -1;
             }
-            bool keep[kFilterUnroll];
+            bool keep[kListUnroll];
 #pragma unroll
-            for (int u = 0; u < kFilterUnroll; ++u)
+            for (int u = 0; u < kListUnroll; ++u)
                 keep[u] = b[u] > a && !(na && node[b[u]] && ra == parent[b[u]]);
-            unsigned mask[kFilterUnroll];
+            unsigned mask[kListUnroll];
             int total = 0;
 #pragma unroll
-            for (int u = 0; u < kFilterUnroll; ++u) {
+            for (int u = 0; u < kListUnroll; ++u) {
                 mask[u] = __ballot_sync(0xffffffffu, keep[u]);
                 total += __popc(mask[u]);
             }
@@ -181,7 +207,7 @@ __global__ void __launch_bounds__(256) open_pairs_csr_kernel(int64_t n, const in
             if (lane == 0) w = atomicAdd(out_count, (unsigned long long)total);
             w = __shfl_sync(0xffffffffu, w, 0);
 #pragma unroll
-            for (int u = 0; u < kFilterUnroll; ++u) {
+            for (int u = 0; u < kListUnroll; ++u) {
                 const unsigned long long idx = w + __popc(mask[u] & lt);
                 if (keep[u] && idx < (unsigned long long)cap) out[idx] = make_int2(a, b[u]);
                 w += __popc(mask[u]);
@@ -200,21 +226,33 @@ __global__ void __launch_bounds__(256) open_pairs_list_kernel(const int2 *__rest
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int64_t total = (int64_t)*count;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
-        const int64_t e = base + lane;
-        int2 ed = make_int2(-1, -1);
-        bool keep = false;
-        if (e < total) {
-            ed = edges[e];
-            keep = pair_open(node, parent, ed.x, ed.y);
+    // 32 kListUnroll consecutive edges per warp step, kListUnroll per lane in flight
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x * kListUnroll;
+    for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31)) * kListUnroll; base < total;
+         base += stride) {
+        int2 ed[kListUnroll];
+#pragma unroll
+        for (int u = 0; u < kListUnroll; ++u) {
+            const int64_t e = base + u * 32 + lane;
+            ed[u] = e < total ? edges[e] : make_int2(-1, -1);
         }
-        const unsigned mask = __ballot_sync(0xffffffffu, keep);
-        if (!mask) continue;
+        unsigned mask[kListUnroll];
+        int n_keep = 0;
+#pragma unroll
+        for (int u = 0; u < kListUnroll; ++u) {
+            mask[u] = __ballot_sync(0xffffffffu, ed[u].x >= 0 && pair_open(node, parent, ed[u].x, ed[u].y));
+            n_keep += __popc(mask[u]);
+        }
+        if (!n_keep) continue;
         unsigned long long w = 0;
-        if (lane == 0) w = atomicAdd(out_count, (unsigned long long)__popc(mask));
-        w = __shfl_sync(0xffffffffu, w, 0) + __popc(mask & lt);
-        if (keep && w < (unsigned long long)cap) out[w] = ed;
+        if (lane == 0) w = atomicAdd(out_count, (unsigned long long)n_keep);
+        w = __shfl_sync(0xffffffffu, w, 0);
+#pragma unroll
+        for (int u = 0; u < kListUnroll; ++u) {
+            const unsigned long long idx = w + __popc(mask[u] & lt);
+            if (((mask[u] >> lane) & 1u) && idx < (unsigned long long)cap) out[idx] = ed[u];
+            w += __popc(mask[u]);
+        }
     }
 }
 
