@@ -18,6 +18,7 @@ namespace {
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
+constexpr int64_t kScanSumMax = 1024;  // blocks up to which a scan takes two launches
 
 __device__ __forceinline__ int64_t warp_incl_scan(int64_t v) {
     int lane = threadIdx.x & 31;
@@ -80,19 +81,37 @@ __global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const TIn *__
     }
 }
 
-template <typename TIn>
+// kSum: offs holds the blocks' unscanned sums and each block adds up those
+// before it (a few KB from L2 for at most kScanSumMax blocks) -- one launch
+// fewer than scanning the sums first.
+template <typename TIn, bool kSum = false>
 __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const TIn *__restrict__ in, int64_t n,
                                                                   const int64_t *__restrict__ offs,
                                                                   int64_t *__restrict__ out) {
     __shared__ int64_t s[kScanTile];
+    __shared__ int64_t s_off[kScanThreads / 32];
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
+    int64_t before = 0;
+    if (kSum)
+        for (int i = threadIdx.x; i < (int)blockIdx.x; i += kScanThreads) before += offs[i];
     for (int i = threadIdx.x; i < kScanTile; i += kScanThreads) {
         int64_t g = base + i;
         s[i] = g < n ? (int64_t)in[g] : 0;
     }
+    if (kSum) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) before += __shfl_down_sync(0xffffffffu, before, o);
+        if ((threadIdx.x & 31) == 0) s_off[threadIdx.x >> 5] = before;
+    }
     __syncthreads();
-    block_scan_tile(s);
-    const int64_t off = offs ? offs[blockIdx.x] : 0;
+    block_scan_tile(s);  // synchronises the block, so s_off is complete
+    int64_t off = 0;
+    if (kSum) {
+#pragma unroll
+        for (int w = 0; w < kScanThreads / 32; ++w) off += s_off[w];
+    } else if (offs) {
+        off = offs[blockIdx.x];
+    }
     for (int i = threadIdx.x; i < kScanTile; i += kScanThreads) {
         int64_t g = base + i;
         if (g < n) out[g] = s[i] + off;
@@ -116,6 +135,11 @@ cnn_status scan_impl(cnn_context *ctx, const TIn *in, int64_t *out, int64_t n, s
     int64_t *partial_scan = partial + nb;
     scan_reduce_kernel<TIn><<<(unsigned)nb, kScanThreads, 0, ctx->stream>>>(in, n, partial);
     CNN_LAUNCH_CHECK(ctx);
+    if (nb <= kScanSumMax) {  // every block adds up the sums before it
+        scan_apply_kernel<TIn, true><<<(unsigned)nb, kScanThreads, 0, ctx->stream>>>(in, n, partial, out);
+        CNN_LAUNCH_CHECK(ctx);
+        return CNN_OK;
+    }
     size_t next_off = tmp_off + sizeof(int64_t) * (size_t)(2 * nb);
     next_off = (next_off + 255) & ~size_t(255);
     CNN_TRY(scan_impl<int64_t>(ctx, partial, partial_scan, nb, next_off));

@@ -318,6 +318,24 @@ __global__ void cell_slots_kernel(const int64_t *__restrict__ cell_start, GridGe
     }
 }
 
+// Per cell its work items (kPer consecutive queries each) and its slots
+// (points x candidate count, the upper bound of each row); the entries at
+// ncells are the zero tails of the two exclusive scans.
+template <int kPer>
+__global__ void cell_units_kernel(const int64_t *__restrict__ cell_start, GridGeom geo, int32_t *__restrict__ items,
+                                  int64_t *__restrict__ slots) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < geo.ncells;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = cell_start[c + 1] - cell_start[c];
+        items[c] = (int32_t)((q + kPer - 1) / kPer);
+        slots[c] = q > 0 ? q * cell_candidates(c, geo, cell_start) : 0;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        items[geo.ncells] = 0;
+        slots[geo.ncells] = 0;
+    }
+}
+
 // rows from their slots to the CSR (one warp per row); split[q] = the
 // entries <= q of row q (rows are ascending), so the fit's walks over the
 // entries > q start there
@@ -1261,23 +1279,19 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
                                          ctx->xf4.as<float4>());
         CNN_LAUNCH_CHECK(ctx);
 
-        // work items: (cell, first query) for every 32 queries of a cell
+        // work items: (cell, first query) for every kUnitQueries queries of a
+        // cell; slots: every row's upper bound (its cell's candidate count),
+        // and for the mask form every row's words
         CNN_TRY(ctx->ensure(ctx->io_a, sizeof(int32_t) * (size_t)(geo.ncells + 1)));
         CNN_TRY(ctx->ensure(ctx->io_b, sizeof(int64_t) * (size_t)(geo.ncells + 3)));  // + the slot and word totals
-        item_count_kernel<kUnitQueries><<<std::min<unsigned>(grid_for(geo.ncells, 256), ctx->sm_count * 16u), 256, 0, st>>>(
-            ctx->cell_start.as<int64_t>(), geo.ncells, ctx->io_a.as<int32_t>());
-        CNN_LAUNCH_CHECK(ctx);
-        CNN_CUDA(ctx, cudaMemsetAsync(ctx->io_a.as<int32_t>() + geo.ncells, 0, sizeof(int32_t), st));
-        CNN_TRY(scan_exclusive_i32_to_i64(ctx, ctx->io_a.as<int32_t>(), ctx->io_b.as<int64_t>(), geo.ncells + 1));
-        // slots: every row's upper bound (its cell's candidate count), and
-        // for the mask form every row's words
         CNN_TRY(ctx->ensure(ctx->grid_slot_base, sizeof(int64_t) * (size_t)(geo.ncells + 2)));
         int64_t *slot_base = ctx->grid_slot_base.as<int64_t>();
         CNN_TRY(ctx->ensure(ctx->scratch_c, sizeof(int64_t) * (size_t)(geo.ncells + 2)));
-        CNN_CUDA(ctx, cudaMemsetAsync(ctx->scratch_c.as<int64_t>() + geo.ncells, 0, sizeof(int64_t), st));
         const unsigned cgrid = std::min<unsigned>(grid_for(geo.ncells, 256), ctx->sm_count * 16u);
-        cell_slots_kernel<false><<<cgrid, 256, 0, st>>>(ctx->cell_start.as<int64_t>(), geo, ctx->scratch_c.as<int64_t>());
+        cell_units_kernel<kUnitQueries><<<cgrid, 256, 0, st>>>(ctx->cell_start.as<int64_t>(), geo,
+                                                               ctx->io_a.as<int32_t>(), ctx->scratch_c.as<int64_t>());
         CNN_LAUNCH_CHECK(ctx);
+        CNN_TRY(scan_exclusive_i32_to_i64(ctx, ctx->io_a.as<int32_t>(), ctx->io_b.as<int64_t>(), geo.ncells + 1));
         CNN_TRY(scan_exclusive_i64(ctx, ctx->scratch_c.as<int64_t>(), slot_base, geo.ncells + 1));
         int64_t hcounts[3] = {0, 0, 0};  // work items, candidate slots, mask words
         CNN_CUDA(ctx, cudaMemcpyAsync(ctx->io_b.as<int64_t>() + geo.ncells + 1, slot_base + geo.ncells,
@@ -1328,7 +1342,8 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         stage_end(ctx, 1);
 
         stage_begin(ctx, 2);
-        CNN_CUDA(ctx, cudaMemsetAsync(deg, 0, sizeof(int32_t) * (size_t)n, st));
+        // deg[n] = 0 as well: the tail of the row-offset scan
+        CNN_CUDA(ctx, cudaMemsetAsync(deg, 0, sizeof(int32_t) * (size_t)(n + 1), st));
         if (calibrate) CNN_CUDA(ctx, cudaEventRecord(ctx->tune_ev[0], st));
         if (nitems > 0 && use_mask) {
             grid_unit_kernel<kMask><<<(unsigned)((nitems + kUnitWarps - 1) / kUnitWarps), kUnitWarps * 32, 0, st>>>(
@@ -1386,8 +1401,10 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
 
     // ---- offsets
     stage_begin(ctx, 3);
-    set_last_zero_kernel<<<1, 1, 0, st>>>(deg, n);
-    CNN_LAUNCH_CHECK(ctx);
+    if (!use_grid) {  // the grid path cleared deg[n] with deg
+        set_last_zero_kernel<<<1, 1, 0, st>>>(deg, n);
+        CNN_LAUNCH_CHECK(ctx);
+    }
     CNN_TRY(scan_exclusive_i32_to_i64(ctx, deg, row_off, n + 1));
     int64_t nnz = 0;
     CNN_TRY(read_back(ctx, &nnz, row_off + n, sizeof(int64_t)));
