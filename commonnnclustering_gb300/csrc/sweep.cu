@@ -63,6 +63,12 @@ __device__ __forceinline__ double exact_s(const double *__restrict__ x, int d, i
 // the largest (bucket <= k) into deg_all[k * (n + 1) + p] (entry n: 0).
 // The ladder sits in shared memory (lanes index it by their own radius) and
 // every lane counts its pairs per bucket in its own shared-memory column.
+// In-band pairs wait in a per-warp queue and are decided in float64 32 at a
+// time, one per lane: decided where they are found, each would stall its
+// whole warp on a dependent gather (about one 32-entry step in two holds one
+// on a wide box, where the float32 bands are wide).
+constexpr int kBandQueue = 64;
+
 __global__ void __launch_bounds__(256, CNN_BUCKET_MIN_BLOCKS) bucket_kernel(const double *__restrict__ x, int d, int64_t n,
                                                      const int32_t *__restrict__ perm,
                                                      const float4 *__restrict__ xf4,
@@ -74,7 +80,11 @@ __global__ void __launch_bounds__(256, CNN_BUCKET_MIN_BLOCKS) bucket_kernel(cons
     __shared__ float s_in[kMaxRadii], s_out[kMaxRadii];
     __shared__ double s_rc[kMaxRadii];
     __shared__ int32_t s_cnt[8][kMaxRadii][32];  // [warp][bucket][lane]
+    __shared__ int64_t s_qe[8][kBandQueue];       // queued in-band pairs: entry,
+    __shared__ int32_t s_qj[8][kBandQueue];       // other point (internal index),
+    __shared__ int32_t s_qk[8][kBandQueue];       // lowest possible bucket
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
     if (threadIdx.x < kMaxRadii) {
         s_in[threadIdx.x] = threadIdx.x < lad.k ? lad.thr_in[threadIdx.x] : INFINITY;
         s_out[threadIdx.x] = threadIdx.x < lad.k ? lad.thr_out[threadIdx.x] : INFINITY;
@@ -91,8 +101,28 @@ __global__ void __launch_bounds__(256, CNN_BUCKET_MIN_BLOCKS) bucket_kernel(cons
     unsigned long long ex = 0;
     const int kl = lad.k - 1;
     const int64_t e_end = row_off[p + 1];
-    // 128 entries per step, four per lane: their column loads, then their
-    // coordinate gathers, are in flight together
+    int qn = 0;  // queued pairs (warp-uniform)
+    // lanes < count decide queue entries [0, count) in float64
+    auto decide = [&](int count) {
+        __syncwarp();
+        if (lane < count) {
+            const int64_t e = s_qe[w][lane];
+            double s = exact_s(x, d, ip, perm[s_qj[w][lane]], lad.fpmode);
+            if (lad.metric == CNN_METRIC_EUCLIDEAN) s = __dsqrt_rn(s);
+            int b = lad.k - 1;
+            for (int kk = s_qk[w][lane]; kk < lad.k; ++kk)
+                if (s <= s_rc[kk]) {
+                    b = kk;
+                    break;
+                }
+            bucket[e] = (uint8_t)b;
+            ++s_cnt[w][b][lane];
+            ++ex;
+        }
+        __syncwarp();
+    };
+    // 32 kBucketUnroll entries per step, kBucketUnroll per lane: their column
+    // loads, then their coordinate gathers, are in flight together
     for (int64_t e0 = row_off[p]; e0 < e_end; e0 += kBucketUnroll * 32) {
         int32_t jv[kBucketUnroll];
         float4 cv[kBucketUnroll];
@@ -105,7 +135,7 @@ __global__ void __launch_bounds__(256, CNN_BUCKET_MIN_BLOCKS) bucket_kernel(cons
         for (int u = 0; u < kBucketUnroll; ++u) cv[u] = jv[u] >= 0 ? xf4[jv[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int u = 0; u < kBucketUnroll; ++u) {
-            if (jv[u] < 0) continue;
+            const bool valid = jv[u] >= 0;
             const int64_t e = e0 + u * 32 + lane;
             const float dx = q.x - cv[u].x, dy = q.y - cv[u].y, dz = q.z - cv[u].z;
             const float sf = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
@@ -113,22 +143,30 @@ __global__ void __launch_bounds__(256, CNN_BUCKET_MIN_BLOCKS) bucket_kernel(cons
             int k = 0;
 #pragma unroll
             for (int kk = 0; kk < kMaxRadii - 1; ++kk) k += (kk < kl) & (sf > s_out[kk]);
-            int b = k;
-            if (!(sf <= s_in[k])) {  // inside the band of radius k: decide in float64
-                double s = exact_s(x, d, ip, perm[jv[u]], lad.fpmode);
-                if (lad.metric == CNN_METRIC_EUCLIDEAN) s = __dsqrt_rn(s);
-                b = lad.k - 1;
-                for (int kk = k; kk < lad.k; ++kk)
-                    if (s <= s_rc[kk]) {
-                        b = kk;
-                        break;
-                    }
-                ++ex;
+            const bool band = valid && !(sf <= s_in[k]);  // inside the band of radius k
+            const unsigned bm = __ballot_sync(0xffffffffu, band);
+            if (band) {  // queue it (qn <= 31 here, so the queue has room for 32)
+                const int slot = qn + __popc(bm & lt);
+                s_qe[w][slot] = e;
+                s_qj[w][slot] = jv[u];
+                s_qk[w][slot] = k;
+            } else if (valid) {
+                bucket[e] = (uint8_t)k;
+                ++s_cnt[w][k][lane];
             }
-            bucket[e] = (uint8_t)b;
-            ++s_cnt[w][b][lane];
+            qn += __popc(bm);
+            if (qn >= 32) {
+                decide(32);
+                if (lane < qn - 32) {  // move the rest (fewer than 32) to the front
+                    s_qe[w][lane] = s_qe[w][lane + 32];
+                    s_qj[w][lane] = s_qj[w][lane + 32];
+                    s_qk[w][lane] = s_qk[w][lane + 32];
+                }
+                qn -= 32;
+            }
         }
     }
+    if (qn > 0) decide(qn);
     if (deg_all) {
         __syncwarp();
         int32_t run = 0;  // this lane's pairs of buckets <= k
