@@ -129,6 +129,7 @@ struct cnn_context {
     bool search_stats_pending = false;
     bool fit_stats_pending = false;
     int64_t pending_candidates = -1;  // >= 0: known on the host
+    const int64_t *counted_labels = nullptr;  // labels whose counts the last fit left in flag
 
     // points (original order, row-major float64)
     int64_t n = 0;

@@ -676,6 +676,7 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
                     uint8_t *consider_dev, int64_t *labels_dev, const int32_t *seed_a, const int32_t *seed_b,
                     const int2 *edge_list, const unsigned long long *edge_count, int2 *wl_buf,
                     int64_t wl_buf_cap) {
+    ctx->counted_labels = nullptr;  // set by the label stage
     if (!ctx->have_graph) return ctx->fail(CNN_ERR_STATE, "no neighbour graph: call cnn_build_neighbours first");
     CNN_TRY(ensure_lists(ctx));
     const int64_t n = ctx->n;
@@ -688,7 +689,7 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     CNN_TRY(ctx->ensure(ctx->node, (size_t)n));
     CNN_TRY(ctx->ensure(ctx->parent, sizeof(int32_t) * (size_t)n));
     CNN_TRY(ctx->ensure(ctx->comp_min, sizeof(int32_t) * (size_t)n));
-    CNN_TRY(ctx->ensure(ctx->flag, sizeof(int32_t) * (size_t)(n + 1)));
+    CNN_TRY(ctx->ensure(ctx->flag, sizeof(int32_t) * (size_t)(2 * n + 1)));  // + the component sizes
     CNN_TRY(ctx->ensure(ctx->scratch_a, sizeof(int64_t) * (size_t)(n + 1)));
     unsigned long long *counters = ctx->counters.as<unsigned long long>();
     CNN_CUDA(ctx, cudaMemsetAsync(counters + 4, 0, 5 * sizeof(unsigned long long), st));
@@ -770,18 +771,25 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     stage_end(ctx, 6);
 
     stage_begin(ctx, 7);
+    // flag[0..n] for the cluster ranks, then (fresh labels) comp_size[0..n):
+    // the component sizes, which become the label counts sort_by_size reads
+    // (in flag, once the ranks are scanned)
     int32_t *flag = ctx->flag.as<int32_t>();
     int64_t *rank = ctx->scratch_a.as<int64_t>();
-    CNN_CUDA(ctx, cudaMemsetAsync(flag, 0, sizeof(int32_t) * (size_t)(n + 1), st));
-    root_min_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(n, node, parent, perm, comp_min);
+    const bool count = current_start == 1;
+    int32_t *comp_size = count ? flag + (n + 1) : nullptr;
+    CNN_CUDA(ctx, cudaMemsetAsync(flag, 0, sizeof(int32_t) * (size_t)(count ? 2 * n + 1 : n + 1), st));
+    root_min_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(n, node, parent, perm, comp_min, comp_size);
     CNN_LAUNCH_CHECK(ctx);
     root_store_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(n, node, parent);
     CNN_LAUNCH_CHECK(ctx);
     min_flag_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(n, node, parent, comp_min, flag);
     CNN_LAUNCH_CHECK(ctx);
     CNN_TRY(scan_exclusive_i32_to_i64(ctx, flag, rank, n + 1));
-    label_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(n, node, parent, comp_min, perm, rank, current_start, labels_dev);
+    label_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(n, node, parent, comp_min, perm, rank, current_start, labels_dev,
+                                                     comp_size, count ? flag : nullptr);
     CNN_LAUNCH_CHECK(ctx);
+    ctx->counted_labels = count ? labels_dev : nullptr;
     // every point with consider == 1 is visited by the reference loop and
     // left at consider == 0; points already at 0 stay 0
     CNN_CUDA(ctx, cudaMemsetAsync(consider_dev, 0, (size_t)n, st));
@@ -933,6 +941,9 @@ cnn_status sort_fresh_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64_t
     CNN_TRY(ctx->ensure(ctx->scratch_b, sizeof(int64_t) * (size_t)n + 64));
     int32_t *cnt = ctx->flag.as<int32_t>();
     uint64_t *keys = ctx->io_b.as<uint64_t>();
+    // the fit that wrote these labels left their counts in cnt (its label stage)
+    const bool counted = ctx->counted_labels == labels;
+    ctx->counted_labels = nullptr;
     int64_t *k_big = reinterpret_cast<int64_t *>(keys + n);  // k when above kOrderSmall, else 0
     int64_t *newlab = ctx->scratch_b.as<int64_t>();
     // outside a graph capture one read of the cluster count picks the path
@@ -945,10 +956,12 @@ cnn_status sort_fresh_impl(cnn_context *ctx, int64_t *labels, int64_t n, int64_t
             return CNN_OK;  // only noise
         }
     }
-    CNN_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (size_t)(k_host >= 0 ? k_host : n), st));
-    fresh_count_kernel<<<std::min<unsigned>(blocks_for(ctx, n), 2 * ctx->sm_count), 256, 0, st>>>(labels, n, k_dev,
-                                                                                            cnt);
-    CNN_LAUNCH_CHECK(ctx);
+    if (!counted) {
+        CNN_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (size_t)(k_host >= 0 ? k_host : n), st));
+        fresh_count_kernel<<<std::min<unsigned>(blocks_for(ctx, n), 2 * ctx->sm_count), 256, 0, st>>>(labels, n,
+                                                                                                k_dev, cnt);
+        CNN_LAUNCH_CHECK(ctx);
+    }
     if (k_host >= 0 && k_host <= kOrderSmall) {
         const size_t smem = sizeof(uint64_t) * (size_t)k_host;
         CNN_TRY(allow_dynamic_smem(ctx, (const void *)fresh_order_small_kernel, smem));

@@ -316,8 +316,10 @@ __global__ void __launch_bounds__(kCheckWarps * 32, CNN_CHECK_MIN_BLOCKS) check_
 // Full path compression and per-component minimum point index.
 // Neighbouring internal indices mostly share a root: lanes with the same
 // root combine their minimum first and issue one atomic.
+// comp_size (optional): the nodes of each component, counted the same way.
 __global__ void root_min_kernel(int64_t n, const uint8_t *__restrict__ node, int32_t *__restrict__ parent,
-                                const int32_t *__restrict__ perm, int32_t *__restrict__ comp_min) {
+                                const int32_t *__restrict__ perm, int32_t *__restrict__ comp_min,
+                                int32_t *__restrict__ comp_size = nullptr) {
     const int lane = threadIdx.x & 31;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
@@ -327,7 +329,10 @@ __global__ void root_min_kernel(int64_t n, const uint8_t *__restrict__ node, int
         int32_t v = is_node ? perm[p] : INT_MAX;
         const unsigned peers = __match_any_sync(0xffffffffu, r);
         v = __reduce_min_sync(peers, v);
-        if (is_node && lane == __ffs(peers) - 1) atomicMin(&comp_min[r], v);
+        if (is_node && lane == __ffs(peers) - 1) {
+            atomicMin(&comp_min[r], v);
+            if (comp_size) atomicAdd(&comp_size[r], __popc(peers));
+        }
     }
 }
 
@@ -355,13 +360,18 @@ __global__ void min_flag_kernel(int64_t n, const uint8_t *__restrict__ node, con
     }
 }
 
+// label_cnt (optional): at each root, the size of its component as the count
+// of label current_start + rank (entry rank), what sort_by_size counts.
 __global__ void label_kernel(int64_t n, const uint8_t *__restrict__ node, const int32_t *__restrict__ parent,
                              const int32_t *__restrict__ comp_min, const int32_t *__restrict__ perm,
-                             const int64_t *__restrict__ rank, int64_t current_start, int64_t *__restrict__ labels) {
+                             const int64_t *__restrict__ rank, int64_t current_start, int64_t *__restrict__ labels,
+                             const int32_t *__restrict__ comp_size = nullptr, int32_t *__restrict__ label_cnt = nullptr) {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
         if (!node[p]) continue;
-        const int32_t m = comp_min[parent[p]];
-        labels[perm[p]] = current_start + rank[m];
+        const int32_t r = parent[p];
+        const int64_t lab = rank[comp_min[r]];
+        labels[perm[p]] = current_start + lab;
+        if (label_cnt && r == (int32_t)p) label_cnt[lab] = comp_size[p];
     }
 }
 

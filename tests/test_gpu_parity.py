@@ -409,6 +409,34 @@ def test_fit_fresh_equals_fit_then_sort(cnn, mem, strategy):
         ctx.close()
 
 
+@pytest.mark.parametrize("n_blobs", [3000, 9000])
+def test_fit_fresh_many_clusters(cnn, n_blobs):
+    """Thousands of small clusters (beyond the 4,096 labels ranked in shared
+    memory for 9,000 blobs): the fresh fit's label counts, taken from the
+    component sizes of its union-find, order the clusters as cnn_sort_by_size
+    counting the labels does, with a member cutoff that drops some and a
+    cluster limit."""
+    rng = np.random.default_rng(31)
+    centres = rng.uniform(0, 1000, size=(n_blobs, 3))
+    sizes = rng.integers(3, 12, size=n_blobs)
+    x = np.ascontiguousarray(np.vstack([c + rng.normal(0, 0.05, size=(k, 3)) for c, k in zip(centres, sizes)]))
+    x = x[rng.permutation(x.shape[0])]
+    ctx = cnn.Context(0)
+    try:
+        ctx.set_points(x)
+        for (mc, mx) in ((2, None), (6, None), (2, n_blobs // 3)):
+            ctx.build_neighbours(0.3 ** 2)
+            want = np.zeros(x.shape[0], dtype=np.int64)
+            ctx.fit(2, 1, 1, np.ones(x.shape[0], dtype=np.uint8), want)
+            assert want.max() > 2000
+            ctx.sort_by_size(want, mc, mx)
+            ctx.build_neighbours(0.3 ** 2)
+            got = ctx.fit_fresh(2, 1, True, mc, mx)
+            assert np.array_equal(got, want), (mc, mx)
+    finally:
+        ctx.close()
+
+
 def test_fit_fresh_on_other_graphs(cnn):
     """cnn_fit_fresh after the tensor-core search (n_dim 16, the graph in the
     search's pivot-grouped order), after precomputed neighbourhoods
