@@ -25,6 +25,22 @@ void stage_end(cnn_context *ctx, int slot) {
     ctx->slot_pending[slot] = true;
 }
 
+// the cnn_stats field each stage slot's events time
+static float *stage_field(cnn_context *ctx, int slot) {
+    float *f[cnn_context::kSlots] = {
+        &ctx->stats.ms_bbox, &ctx->stats.ms_cells, &ctx->stats.ms_count, &ctx->stats.ms_scan,
+        &ctx->stats.ms_fill, &ctx->stats.ms_nodes, &ctx->stats.ms_check, &ctx->stats.ms_label,
+        &ctx->stats.ms_sort, &ctx->stats.ms_gram, &ctx->stats.ms_weights, nullptr};
+    return slot >= 0 && slot < cnn_context::kSlots ? f[slot] : nullptr;
+}
+
+void stages_reset(cnn_context *ctx, int first, int last) {
+    for (int i = first; i <= last && i < cnn_context::kSlots; ++i) {
+        ctx->slot_pending[i] = false;  // a stage this call skips reports 0, not an older time
+        if (float *f = stage_field(ctx, i)) *f = 0.f;
+    }
+}
+
 namespace {
 
 __global__ void widen_f32_kernel(const float *__restrict__ in, int64_t total, double *__restrict__ out) {
@@ -80,7 +96,7 @@ namespace {
 std::vector<DevBuf *> workspace_buffers(cnn_context *ctx) {
     return {&ctx->x_own, &ctx->x_f32_stage, &ctx->perm, &ctx->inv, &ctx->deg, &ctx->row_off,
                            &ctx->cols, &ctx->xf4, &ctx->cell_of, &ctx->cell_start, &ctx->grid_slot_base,
-                           &ctx->grid_slot_cols, &ctx->grid_qslot, &ctx->node, &ctx->parent,
+                           &ctx->grid_slot_cols, &ctx->grid_qslot, &ctx->grid_qend, &ctx->node, &ctx->parent,
                            &ctx->comp_min, &ctx->flag, &ctx->counters, &ctx->stage_labels, &ctx->gram_hi, &ctx->gram_mid,
                            &ctx->gram_lo, &ctx->gram_aux, &ctx->gram_masks, &ctx->gram_tkeys, &ctx->gram_low, &ctx->gram_pad2c, &ctx->gram_rowwork, &ctx->gram_chunkcnt, &ctx->gram_amb,
                            &ctx->gram_blocks, &ctx->gram_tiles, &ctx->gram_perm, &ctx->pred_off, &ctx->pred_cols,
@@ -118,6 +134,8 @@ cnn_status release_workspace(cnn_context *ctx) {
     ctx->have_graph = false;
     ctx->graph_mask = false;
     ctx->csr_valid = true;
+    ctx->graph_slots = false;
+    ctx->nnz_pending = false;
     ctx->split_valid = false;
     ctx->tune_pending = false;
     ++ctx->graph_generation;
@@ -318,16 +336,14 @@ CNN_API cnn_status cnn_get_stats(const cnn_context *cctx, cnn_stats *out) {
     if (!ctx || !out) return CNN_ERR_INVALID_ARG;
     CNN_TRY(check_ctx(ctx));
     CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    float *slot_field[cnn_context::kSlots] = {
-        &ctx->stats.ms_bbox, &ctx->stats.ms_cells, &ctx->stats.ms_count, &ctx->stats.ms_scan,
-        &ctx->stats.ms_fill, &ctx->stats.ms_nodes, &ctx->stats.ms_check, &ctx->stats.ms_label,
-        &ctx->stats.ms_sort, &ctx->stats.ms_gram, &ctx->stats.ms_weights, nullptr};
     for (int i = 0; i < cnn_context::kSlots; ++i) {
-        if (!ctx->slot_pending[i] || !slot_field[i]) continue;
+        float *field = stage_field(ctx, i);
+        if (!ctx->slot_pending[i] || !field) continue;
         float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, ctx->ev_begin[i], ctx->ev_end[i]) == cudaSuccess) *slot_field[i] = ms;
+        if (cudaEventElapsedTime(&ms, ctx->ev_begin[i], ctx->ev_end[i]) == cudaSuccess) *field = ms;
         (void)cudaGetLastError();
     }
+    CNN_TRY(resolve_nnz(ctx));  // the stream is idle: no wait
     if (ctx->search_stats_pending) {
         ctx->stats.n_exact = (int64_t)ctx->host_stats[0];
         ctx->stats.n_candidates = ctx->pending_candidates >= 0 ? ctx->pending_candidates : (int64_t)ctx->host_stats[1];
@@ -454,6 +470,7 @@ CNN_API cnn_status cnn_neighbour_count(cnn_context *ctx, int64_t *nnz) {
     CNN_TRY(check_ctx(ctx));
     if (!nnz) return ctx->fail(CNN_ERR_INVALID_ARG, "null output");
     if (!ctx->have_graph) return ctx->fail(CNN_ERR_STATE, "no neighbour graph");
+    CNN_TRY(resolve_nnz(ctx));
     *nnz = ctx->nnz;
     return CNN_OK;
 }
@@ -461,6 +478,7 @@ CNN_API cnn_status cnn_neighbour_count(cnn_context *ctx, int64_t *nnz) {
 CNN_API cnn_status cnn_get_neighbours(cnn_context *ctx, int64_t *offsets, int32_t *indices, cnn_memspace mem) {
     CNN_TRY(check_ctx(ctx));
     if (!ctx->have_graph) return ctx->fail(CNN_ERR_STATE, "no neighbour graph");
+    CNN_TRY(ensure_csr(ctx));
     if (!offsets || (ctx->nnz > 0 && !indices)) return ctx->fail(CNN_ERR_INVALID_ARG, "null output");
     const int64_t n = ctx->n, nnz = ctx->nnz;
     int64_t *off_dev = offsets;

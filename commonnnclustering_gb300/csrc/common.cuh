@@ -122,7 +122,7 @@ struct cnn_context {
     cnn_stats stats{};
     // Counters of the last search and fit, copied back without a sync into
     // pinned memory and read by cnn_get_stats (which syncs the stream).
-    unsigned long long *host_stats = nullptr;  // [0] exact, [1] candidates, [4..6] fit, [8] clusters
+    unsigned long long *host_stats = nullptr;  // [0] exact, [1] candidates, [4..6] fit, [8] clusters, [10..13] pairs
     // pinned bounce buffer for the small read-backs the host waits on
     static constexpr size_t kHostSmall = 64 << 10;
     void *host_small = nullptr;
@@ -130,6 +130,9 @@ struct cnn_context {
     bool fit_stats_pending = false;
     int64_t pending_candidates = -1;  // >= 0: known on the host
     const int64_t *counted_labels = nullptr;  // labels whose counts the last fit left in flag
+    bool graph_slots = false;  // the list search's rows left in their slots (grid_qslot, grid_qend, deg, grid_slot_cols)
+    bool nnz_pending = false;  // nnz of such a graph not read back yet (host_stats[10..13])
+    int64_t slot_total = 0;    // their slots' total size, a bound of nnz
 
     // points (original order, row-major float64)
     int64_t n = 0;
@@ -166,7 +169,7 @@ struct cnn_context {
     cnn::DevBuf cell_start;  // int32[ncells+2]
     // one-pass grid search: per-cell slot offsets, the rows in their slots,
     // each row's slot start
-    cnn::DevBuf grid_slot_base, grid_slot_cols, grid_qslot;
+    cnn::DevBuf grid_slot_base, grid_slot_cols, grid_qslot, grid_qend;
 
     // extents (max - min of finite points) per dimension of the last grid search
     double grid_extent[3] = {0.0, 0.0, 0.0};
@@ -309,6 +312,8 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
                                  int form = kFormLists);
 // row_off/cols of the current graph (materialised from the masks if needed)
 cnn_status ensure_lists(cnn_context *ctx);
+cnn_status ensure_csr(cnn_context *ctx);   // the CSR of a graph left in its slots
+cnn_status resolve_nnz(cnn_context *ctx);  // its pair count (a stream sync)
 cnn_status export_neighbours_impl(cnn_context *ctx, int64_t *offsets_dev, int32_t *indices_dev);
 cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev,
                                const int32_t *indices_dev, int64_t n);
@@ -387,6 +392,7 @@ cnn_status sweep_impl(cnn_context *ctx, const double *radius_cutoffs, int32_t n_
 // timing helpers (cnngpu.cu): events only, no synchronisation
 void stage_begin(cnn_context *ctx, int slot);
 void stage_end(cnn_context *ctx, int slot);
+void stages_reset(cnn_context *ctx, int first, int last);  // slots first..last: not run yet
 
 inline unsigned grid_for(int64_t n, int block) {
     int64_t g = (n + block - 1) / block;

@@ -31,6 +31,7 @@
 #include <climits>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "common.cuh"
 #include "fit_kernels.cuh"
@@ -57,7 +58,9 @@ constexpr int kListUnroll = CNN_LIST_UNROLL;
 // (a, b > a, both nodes) whose roots differ; everything else is already
 // joined.  The worklist is then checked edge by edge with the same lazy
 // rule.  If it overflows its capacity, the full lazy pass runs instead.
-__global__ void __launch_bounds__(256) cross_filter_kernel(int64_t n, const int64_t *__restrict__ row_off,
+template <bool kSlotRows>
+__global__ void __launch_bounds__(256) cross_filter_kernel(int64_t n, const int64_t *__restrict__ row_start,
+                                                           const int64_t *__restrict__ row_end,
                                                            const int32_t *__restrict__ cols,
                                                            const int32_t *__restrict__ parent,
                                                            int2 *__restrict__ wl,
@@ -72,7 +75,7 @@ __global__ void __launch_bounds__(256) cross_filter_kernel(int64_t n, const int6
         // parent[a], the row bounds and split[a] in one round trip
         int64_t v = 0;
         if (lane == 0) v = parent[a];
-        else if (lane < 3) v = row_off[a + lane - 1];
+        else if (lane < 3) v = (kSlotRows && lane == 2) ? row_end[a] : row_start[a + (kSlotRows ? 0 : lane - 1)];
         else if (lane == 3 && split) v = split[a];
         const int32_t pa = (int32_t)__shfl_sync(0xffffffffu, v, 0);
         if (pa < 0) continue;
@@ -256,9 +259,11 @@ __global__ void __launch_bounds__(256) open_pairs_list_kernel(const int2 *__rest
     }
 }
 
+template <bool kSlotRows>
 __global__ void __launch_bounds__(kCheckWarps * 32, CNN_CHECK_MIN_BLOCKS) edge_check_kernel(const int2 *__restrict__ wl,
                                                          const unsigned long long *__restrict__ wl_count,
-                                                         int64_t cap, const int64_t *__restrict__ row_off,
+                                                         int64_t cap, const int64_t *__restrict__ row_start,
+                                                         const int64_t *__restrict__ row_end,
                                                          const int32_t *__restrict__ cols,
                                                          int32_t *__restrict__ parent, int32_t needed,
                                                          unsigned long long *__restrict__ counters) {
@@ -303,9 +308,10 @@ __global__ void __launch_bounds__(kCheckWarps * 32, CNN_CHECK_MIN_BLOCKS) edge_c
             if (needed <= 0) {
                 ok = needed == 0;
             } else {
-                const int64_t as = row_off[aa], bs = row_off[bb];
-                ok = warp_shares(cols + as, (int32_t)(row_off[aa + 1] - as), cols + bs, (int32_t)(row_off[bb + 1] - bs),
-                                 needed, lane, sA);
+                const int64_t as = row_start[aa], bs = row_start[bb];
+                const int64_t ae = kSlotRows ? row_end[aa] : row_start[aa + 1];
+                const int64_t be = kSlotRows ? row_end[bb] : row_start[bb + 1];
+                ok = warp_shares(cols + as, (int32_t)(ae - as), cols + bs, (int32_t)(be - bs), needed, lane, sA);
                 ++n_checks;
             }
             if (ok) {
@@ -321,13 +327,15 @@ __global__ void __launch_bounds__(kCheckWarps * 32, CNN_CHECK_MIN_BLOCKS) edge_c
 }
 
 // The full lazy pass, run only when the worklist overflowed.
+template <bool kSlotRows>
 __global__ void __launch_bounds__(kCheckWarps * 32) check_union_if_overflow_kernel(
-    int64_t n, const int64_t *__restrict__ row_off, const int32_t *__restrict__ cols, int32_t *__restrict__ parent,
+    int64_t n, const int64_t *__restrict__ row_start, const int64_t *__restrict__ row_end,
+    const int32_t *__restrict__ cols, int32_t *__restrict__ parent,
     int32_t needed, const unsigned long long *__restrict__ wl_count, int64_t cap,
     unsigned long long *__restrict__ counters) {
     if (*wl_count <= (unsigned long long)cap) return;
     // same body as the full pass of check_union_kernel
-    check_union_body(n, row_off, cols, parent, needed, INT32_MAX, counters);
+    check_union_body<kSlotRows>(n, row_start, row_end, cols, parent, needed, INT32_MAX, counters);
 }
 
 // ---- sort_by_size ---------------------------------------------------------
@@ -677,6 +685,7 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
                     const int2 *edge_list, const unsigned long long *edge_count, int2 *wl_buf,
                     int64_t wl_buf_cap) {
     ctx->counted_labels = nullptr;  // set by the label stage
+    stages_reset(ctx, 5, 8);           // nodes, check, labels, sort: this fit's own
     if (!ctx->have_graph) return ctx->fail(CNN_ERR_STATE, "no neighbour graph: call cnn_build_neighbours first");
     CNN_TRY(ensure_lists(ctx));
     const int64_t n = ctx->n;
@@ -722,23 +731,20 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
         }
         return std::min<unsigned>(grid_for(n, kCheckWarps), (unsigned)std::max(1, per_sm * sms));
     };
-    const unsigned check_blocks = resident((const void *)check_union_kernel, kCheckWarps * 32, 0);
-    // hook: every node checks its first kHookEdges candidate edges; compress; then
-    // the cross-root pairs only, where pairs inside joined sets cost one load
     // rows ascending: the entries > a start at split[a] when the search recorded it
     const int32_t *split = ctx->split_valid ? ctx->split.as<int32_t>() : nullptr;
-    check_union_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(
-        n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff, kHookEdges,
-        counters, seed_a, seed_b, split);
-    CNN_LAUNCH_CHECK(ctx);
-    root_store_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(n, node, parent);
-    CNN_LAUNCH_CHECK(ctx);
-    // cross edges between the hooked sets -> worklist -> checks
+    // the rows: the CSR, or the slots the search left them in (no CSR asked for yet)
+    const bool slots = ctx->graph_slots && !ctx->csr_valid;
+    const RowView g = slots ? RowView{ctx->grid_qslot.as<int64_t>(), ctx->grid_qend.as<int64_t>(),
+                                      ctx->grid_slot_cols.as<int32_t>()}
+                            : csr_view(ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>());
     // worklist capacity: a list-fed filter (pairs a finished fit left open)
     // holds more cross pairs than the graph-fed one after its hook pass;
     // overflow falls back to the full lazy pass (measured on the 1M-point
-    // sweep: nnz/4 for lists, nnz/16 for the graph)
-    int64_t wl_cap = std::max<int64_t>(int64_t(1) << 20, ctx->nnz / (edge_list ? 4 : 16));
+    // sweep: nnz/4 for lists, nnz/16 for the graph).  Rows in their slots:
+    // the pair count is not read back yet; the slot total bounds it.
+    const int64_t pairs = slots ? ctx->slot_total : ctx->nnz;
+    int64_t wl_cap = std::max<int64_t>(int64_t(1) << 20, pairs / (edge_list ? 4 : 16));
     int2 *wl = nullptr;
     if (wl_buf && wl_buf_cap > 0) {  // the caller's room: every pair the filter can emit
         wl = wl_buf;
@@ -748,26 +754,39 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
         wl = ctx->io_c.as<int2>();
     }
     unsigned long long *wl_count = counters + 8;
-    CNN_CUDA(ctx, cudaMemsetAsync(wl_count, 0, sizeof(unsigned long long), st));
-    if (edge_list) {
-        // only pairs a finished fit that refines this one left open can cross
-        cross_filter_list_kernel<<<ctx->sm_count * 16u, 256, 0, st>>>(edge_list, edge_count, parent, wl,
-                                                             wl_count, wl_cap);
-    } else {
-        cross_filter_kernel<<<resident((const void *)cross_filter_kernel, 256, 0), 256, 0, st>>>(
-            n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, wl, wl_count, wl_cap,
+    // hook: every node checks its first kHookEdges candidate edges; compress;
+    // then the cross-root pairs only, where pairs inside joined sets cost one
+    // load -- with the kernels of the rows' form
+    auto check_stage = [&](auto slot_rows) -> cnn_status {
+        constexpr bool kS = decltype(slot_rows)::value;
+        const unsigned check_blocks = resident((const void *)check_union_kernel<kS>, kCheckWarps * 32, 0);
+        check_union_kernel<kS><<<check_blocks, kCheckWarps * 32, 0, st>>>(
+            n, g.start, g.end, g.cols, parent, (int32_t)similarity_cutoff, kHookEdges, counters, seed_a, seed_b,
             split);
-    }
-    CNN_LAUNCH_CHECK(ctx);
-    edge_check_kernel<<<resident((const void *)edge_check_kernel, kCheckWarps * 32, 0), kCheckWarps * 32,
-                        0, st>>>(
-        wl, wl_count, wl_cap, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent,
-        (int32_t)similarity_cutoff, counters);
-    CNN_LAUNCH_CHECK(ctx);
-    check_union_if_overflow_kernel<<<check_blocks, kCheckWarps * 32, 0, st>>>(
-        n, ctx->row_off.as<int64_t>(), ctx->cols.as<int32_t>(), parent, (int32_t)similarity_cutoff, wl_count, wl_cap,
-        counters);
-    CNN_LAUNCH_CHECK(ctx);
+        CNN_LAUNCH_CHECK(ctx);
+        root_store_kernel<<<blocks_for(ctx, n), 256, 0, st>>>(n, node, parent);
+        CNN_LAUNCH_CHECK(ctx);
+        // cross edges between the hooked sets -> worklist -> checks
+        CNN_CUDA(ctx, cudaMemsetAsync(wl_count, 0, sizeof(unsigned long long), st));
+        if (edge_list) {
+            // only pairs a finished fit that refines this one left open can cross
+            cross_filter_list_kernel<<<ctx->sm_count * 16u, 256, 0, st>>>(edge_list, edge_count, parent, wl,
+                                                                 wl_count, wl_cap);
+        } else {
+            cross_filter_kernel<kS><<<resident((const void *)cross_filter_kernel<kS>, 256, 0), 256, 0, st>>>(
+                n, g.start, g.end, g.cols, parent, wl, wl_count, wl_cap, split);
+        }
+        CNN_LAUNCH_CHECK(ctx);
+        edge_check_kernel<kS><<<resident((const void *)edge_check_kernel<kS>, kCheckWarps * 32, 0),
+                                kCheckWarps * 32, 0, st>>>(wl, wl_count, wl_cap, g.start, g.end, g.cols, parent,
+                                                           (int32_t)similarity_cutoff, counters);
+        CNN_LAUNCH_CHECK(ctx);
+        check_union_if_overflow_kernel<kS><<<check_blocks, kCheckWarps * 32, 0, st>>>(
+            n, g.start, g.end, g.cols, parent, (int32_t)similarity_cutoff, wl_count, wl_cap, counters);
+        CNN_LAUNCH_CHECK(ctx);
+        return CNN_OK;
+    };
+    CNN_TRY(slots ? check_stage(std::true_type{}) : check_stage(std::false_type{}));
     stage_end(ctx, 6);
 
     stage_begin(ctx, 7);

@@ -12,6 +12,20 @@ namespace {
 
 constexpr int kCheckWarps = 8;
 
+// The neighbour rows a fit walks: row a is cols[start[a] .. end[a]).  CSR:
+// start = offsets, end = offsets + 1; rows left in the slots the cell-grid
+// search wrote them to: their starts and ends.  The kernels take the three
+// pointers as separate __restrict__ parameters (a struct parameter costs
+// the hook pass registers) and a kSlotRows flag: false reads a row's end as
+// the next row's start.
+struct RowView {
+    const int64_t *start;
+    const int64_t *end;
+    const int32_t *cols;
+};
+
+inline RowView csr_view(const int64_t *off, const int32_t *cols) { return RowView{off, off + 1, cols}; }
+
 // candidate edges each node checks in the hook pass
 #ifndef CNN_HOOK_EDGES
 #define CNN_HOOK_EDGES 3
@@ -192,9 +206,10 @@ __device__ __forceinline__ int64_t warp_upper_bound(const int32_t *__restrict__ 
 // search recorded it) or a warp-wide binary search.  Nodes with
 // skip_a[a] >= 0 or skip_b[a] >= 0 (already joined by seeds) are left to
 // the cross-edge pass.
+template <bool kSlotRows>
 __device__ __forceinline__ void check_union_body(
-    int64_t n, const int64_t *__restrict__ row_off, const int32_t *__restrict__ cols,
-    int32_t *__restrict__ parent, int32_t needed, int32_t max_edges,
+    int64_t n, const int64_t *__restrict__ row_start, const int64_t *__restrict__ row_end,
+    const int32_t *__restrict__ cols, int32_t *__restrict__ parent, int32_t needed, int32_t max_edges,
     unsigned long long *__restrict__ counters, const int32_t *__restrict__ skip_a = nullptr,
     const int32_t *__restrict__ skip_b = nullptr, const int32_t *__restrict__ split = nullptr) {
     __shared__ int32_t s_wide[kCheckWarps][kWideChunk];
@@ -215,7 +230,7 @@ __device__ __forceinline__ void check_union_body(
         // parent[a], the row bounds and split[a] in one round trip (lanes 0..3)
         int64_t v = 0;
         if (lane == 0) v = *(volatile int32_t *)&parent[a];
-        else if (lane < 3) v = row_off[a + lane - 1];
+        else if (lane < 3) v = (kSlotRows && lane == 2) ? row_end[a] : row_start[a + (kSlotRows ? 0 : lane - 1)];
         else if (lane == 3 && split) v = split[a];
         const int32_t pa = (int32_t)__shfl_sync(0xffffffffu, v, 0);
         if (pa < 0) continue;  // not a node
@@ -272,8 +287,8 @@ __device__ __forceinline__ void check_union_body(
                 if (needed <= 0) {
                     ok = needed == 0;
                 } else {
-                    const int64_t bs = row_off[bb];
-                    const int32_t lb = (int32_t)(row_off[bb + 1] - bs);
+                    const int64_t bs = row_start[bb];
+                    const int32_t lb = (int32_t)((kSlotRows ? row_end[bb] : row_start[bb + 1]) - bs);
                     ok = warp_shares(A, la, cols + bs, lb, needed, lane, sA);
                     ++n_checks;
                 }
@@ -305,12 +320,14 @@ __device__ __forceinline__ void check_union_body(
     if (lane == 0 && n_acc) atomicAdd(&counters[6], n_acc);
 }
 
+template <bool kSlotRows>
 __global__ void __launch_bounds__(kCheckWarps * 32, CNN_CHECK_MIN_BLOCKS) check_union_kernel(
-    int64_t n, const int64_t *__restrict__ row_off, const int32_t *__restrict__ cols,
-    int32_t *__restrict__ parent, int32_t needed, int32_t max_edges,
+    int64_t n, const int64_t *__restrict__ row_start, const int64_t *__restrict__ row_end,
+    const int32_t *__restrict__ cols, int32_t *__restrict__ parent, int32_t needed, int32_t max_edges,
     unsigned long long *__restrict__ counters, const int32_t *__restrict__ skip_a,
     const int32_t *__restrict__ skip_b, const int32_t *__restrict__ split = nullptr) {
-    check_union_body(n, row_off, cols, parent, needed, max_edges, counters, skip_a, skip_b, split);
+    check_union_body<kSlotRows>(n, row_start, row_end, cols, parent, needed, max_edges, counters, skip_a, skip_b,
+                                split);
 }
 
 // Full path compression and per-component minimum point index.

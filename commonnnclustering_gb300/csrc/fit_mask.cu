@@ -633,6 +633,7 @@ cnn_status masks_to_lists(cnn_context *ctx) {
 cnn_status fit_mask_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_member_cutoff, int64_t current_start,
                          uint8_t *consider_dev, int64_t *labels_dev) {
     ctx->counted_labels = nullptr;  // this fit leaves no label counts
+    stages_reset(ctx, 5, 8);
     if (!ctx->have_graph || !ctx->graph_mask) return ctx->fail(CNN_ERR_STATE, "no neighbour graph in mask form");
     const int64_t n = ctx->n;
     cudaStream_t st = ctx->stream;

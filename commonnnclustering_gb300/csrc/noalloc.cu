@@ -78,7 +78,7 @@ cnn_status setup_for_current_device(DeviceSetup *out) {
         int sms = 0, per_sm = 0;
         if (cudaGetSymbolAddress(&ptr, g_fit_scratch) != cudaSuccess || !ptr ||
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1 ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, check_union_kernel, kCheckWarps * 32, 0) !=
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, check_union_kernel<false>, kCheckWarps * 32, 0) !=
                 cudaSuccess) {
             (void)cudaGetLastError();
             return CNN_ERR_CUDA;
@@ -239,13 +239,15 @@ extern "C" CNN_API cnn_status cnn_fit_csr_noalloc(const int64_t *offsets, const 
     NOALLOC_LAUNCHED();
     noalloc_gate_kernel<<<pb, 256, 0, st>>>(n, sc);
     NOALLOC_LAUNCHED();
-    check_union_kernel<<<cb, kCheckWarps * 32, 0, st>>>(n, offsets, indices, sc->parent, (int32_t)similarity_cutoff,
-                                                        kHookEdges, counters, nullptr, nullptr);
+    check_union_kernel<false><<<cb, kCheckWarps * 32, 0, st>>>(n, offsets, offsets + 1, indices, sc->parent,
+                                                        (int32_t)similarity_cutoff, kHookEdges, counters, nullptr,
+                                                        nullptr);
     NOALLOC_LAUNCHED();
     root_store_kernel<<<pb, 256, 0, st>>>(n, sc->node, sc->parent);
     NOALLOC_LAUNCHED();
-    check_union_kernel<<<cb, kCheckWarps * 32, 0, st>>>(n, offsets, indices, sc->parent, (int32_t)similarity_cutoff,
-                                                        INT32_MAX, counters, nullptr, nullptr);
+    check_union_kernel<false><<<cb, kCheckWarps * 32, 0, st>>>(n, offsets, offsets + 1, indices, sc->parent,
+                                                        (int32_t)similarity_cutoff, INT32_MAX, counters, nullptr,
+                                                        nullptr);
     NOALLOC_LAUNCHED();
     root_min_kernel<<<pb, 256, 0, st>>>(n, sc->node, sc->parent, sc->perm, sc->comp_min);
     NOALLOC_LAUNCHED();

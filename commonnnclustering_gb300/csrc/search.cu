@@ -103,6 +103,17 @@ __device__ __forceinline__ bool exact_in_radius(const double *__restrict__ xa, c
 
 constexpr int kMaxGridDim = 3;
 
+// ctx->counters (unsigned long long): [0] pairs decided in float64,
+// [1] candidates (mask form, all-pairs search), [2..3] cnn_set_neighbours
+// validation, [4..8] the fit, [10..14] the tensor-core search, [15] sweep
+// buckets, [16..19] neighbour pairs of the rows the list search left in
+// their slots (four addresses against atomic contention)
+constexpr int kCounterSlots = 24, kSlotPairsAt = 16;
+// public cell-grid builds leave the list search's rows in their slots (0: CSR at once)
+#ifndef CNN_SLOT_ROWS
+#define CNN_SLOT_ROWS 1
+#endif
+
 // General-d extents: per dimension min/max of finite rows (for the float32
 // error bound of the all-pairs path).  part: [blocks][2*d + 1].
 __global__ void extent_partial_kernel(const double *__restrict__ x, int64_t n, int d,
@@ -315,6 +326,28 @@ __global__ void cell_slots_kernel(const int64_t *__restrict__ cell_start, GridGe
         const int64_t q = cell_start[c + 1] - cell_start[c];
         const int64_t t = q > 0 ? cell_candidates(c, geo, cell_start) : 0;
         slots[c] = q * (kWords ? (t + 31) / 32 : t);
+    }
+}
+
+// For rows left in their slots: end[a] = start[a] + len[a], and split[a] =
+// the entries <= a of row a (rows ascending) by bisection, one thread per
+// row -- the fit's walks over b > a start there (the compaction records the
+// same when it makes the CSR).
+__global__ void row_split_kernel(int64_t n, const int64_t *__restrict__ start, const int32_t *__restrict__ len,
+                                 const int32_t *__restrict__ cols, int64_t *__restrict__ end,
+                                 int32_t *__restrict__ split) {
+    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = start[a];
+        const int32_t l = len[a];
+        const int32_t *row = cols + s;
+        int32_t lo = 0, hi = l;
+        while (lo < hi) {
+            const int32_t mid = (lo + hi) >> 1;
+            if (row[mid] <= (int32_t)a) lo = mid + 1;
+            else hi = mid;
+        }
+        end[a] = s + l;
+        split[a] = lo;
     }
 }
 
@@ -604,9 +637,14 @@ __global__ void __launch_bounds__(kUnitWarps * 32, CNN_UNIT_MIN_BLOCKS) grid_uni
                 for (int o = 16; o > 0; o >>= 1) cnt[k] += __shfl_down_sync(0xffffffffu, cnt[k], o);
         }
         if (lane == 0) {
+            unsigned long long pairs = 0;
 #pragma unroll
             for (int k = 0; k < kUnitQueries; ++k)
-                if (qi[k] >= 0) deg[qi[k]] = cnt[k];
+                if (qi[k] >= 0) {
+                    deg[qi[k]] = cnt[k];
+                    pairs += (unsigned long long)cnt[k];
+                }
+            if (kMode == kSlots) atomicAdd(&counters[kSlotPairsAt + (u & 3)], pairs);  // the pair count, unread
         }
         for (int o = 16; o > 0; o >>= 1) n_exact += __shfl_down_sync(0xffffffffu, n_exact, o);
         if (lane == 0 && n_exact) atomicAdd(&counters[0], n_exact);
@@ -1024,13 +1062,16 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     ctx->csr_valid = true;
     ctx->tune_pending = false;
     ctx->split_valid = false;
+    ctx->graph_slots = false;
+    ctx->nnz_pending = false;
     ++ctx->graph_generation;
     ctx->stats = cnn_stats{};
+    stages_reset(ctx, 0, cnn_context::kSlots - 1);
     ctx->search_stats_pending = false;
     ctx->fit_stats_pending = false;
     ctx->stats.n_points = n;
-    CNN_TRY(ctx->ensure(ctx->counters, 16 * sizeof(unsigned long long)));
-    CNN_CUDA(ctx, cudaMemsetAsync(ctx->counters.ptr, 0, 16 * sizeof(unsigned long long), st));
+    CNN_TRY(ctx->ensure(ctx->counters, kCounterSlots * sizeof(unsigned long long)));
+    CNN_CUDA(ctx, cudaMemsetAsync(ctx->counters.ptr, 0, kCounterSlots * sizeof(unsigned long long), st));
     CNN_TRY(ctx->ensure(ctx->deg, sizeof(int32_t) * (size_t)(n + 1)));
     CNN_TRY(ctx->ensure(ctx->row_off, sizeof(int64_t) * (size_t)(n + 1)));
     CNN_TRY(ctx->ensure(ctx->perm, sizeof(int32_t) * (size_t)(n > 0 ? n : 1)));
@@ -1126,8 +1167,9 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
             ctx->have_graph = true;
             return CNN_OK;
         }
-        CNN_CUDA(ctx, cudaMemsetAsync(ctx->counters.ptr, 0, 16 * sizeof(unsigned long long), st));
+        CNN_CUDA(ctx, cudaMemsetAsync(ctx->counters.ptr, 0, kCounterSlots * sizeof(unsigned long long), st));
         ctx->stats = cnn_stats{};
+    stages_reset(ctx, 0, cnn_context::kSlots - 1);
         ctx->stats.n_points = n;
     }
 
@@ -1399,6 +1441,38 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
         ctx->identity_perm = true;
     }
 
+    // Rows left in their slots (a public build on the list search): the
+    // offsets, the read-back of the pair count and the compaction wait until
+    // something asks for the CSR (ensure_csr); the fit walks the slots.
+    const bool slot_form = CNN_SLOT_ROWS && form == kFormPref && use_grid && use_slots && !use_mask && !calibrate &&
+                           grid_items > 0 && ctx->host_stats != nullptr;
+    if (slot_form) {
+        ctx->graph_slots = true;
+        ctx->csr_valid = false;
+        ctx->slot_total = n_candidates;
+        stage_begin(ctx, 4);
+        CNN_TRY(ctx->ensure(ctx->split, sizeof(int32_t) * (size_t)n));
+        CNN_TRY(ctx->ensure(ctx->grid_qend, sizeof(int64_t) * (size_t)n));
+        row_split_kernel<<<std::min<unsigned>(grid_for(n, 256), ctx->sm_count * 16u), 256, 0, st>>>(
+            n, ctx->grid_qslot.as<int64_t>(), deg, ctx->grid_slot_cols.as<int32_t>(), ctx->grid_qend.as<int64_t>(),
+            ctx->split.as<int32_t>());
+        CNN_LAUNCH_CHECK(ctx);
+        stage_end(ctx, 4);
+        ctx->split_valid = true;
+        // the pair count, summed by the search, comes back with the statistics
+        CNN_CUDA(ctx, cudaMemcpyAsync(ctx->host_stats, counters, 2 * sizeof(unsigned long long),
+                                      cudaMemcpyDeviceToHost, st));
+        CNN_CUDA(ctx, cudaMemcpyAsync(ctx->host_stats + 10, counters + kSlotPairsAt, 4 * sizeof(unsigned long long),
+                                      cudaMemcpyDeviceToHost, st));
+        ctx->pending_candidates = n_candidates;
+        ctx->search_stats_pending = true;
+        ctx->nnz_pending = true;
+        ctx->nnz = -1;  // unknown until resolve_nnz
+        ctx->identity_perm = false;
+        ctx->have_graph = true;
+        return CNN_OK;
+    }
+
     // ---- offsets
     stage_begin(ctx, 3);
     if (!use_grid) {  // the grid path cleared deg[n] with deg
@@ -1473,6 +1547,37 @@ cnn_status build_neighbours_impl(cnn_context *ctx, double radius_cutoff, int met
     return CNN_OK;
 }
 
+// The pair count of a graph left in its slots, read back (a stream sync).
+cnn_status resolve_nnz(cnn_context *ctx) {
+    if (!ctx->nnz_pending) return CNN_OK;
+    CNN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const unsigned long long *h = ctx->host_stats + 10;
+    ctx->nnz = (int64_t)(h[0] + h[1] + h[2] + h[3]);
+    ctx->stats.n_nonzero = ctx->nnz;
+    ctx->nnz_pending = false;
+    return CNN_OK;
+}
+
+// The CSR of a graph left in its slots: the offsets from the row lengths
+// (deg[n] is 0 since the search), then the compaction with split points.
+cnn_status ensure_csr(cnn_context *ctx) {
+    if (!ctx->have_graph || !ctx->graph_slots || ctx->csr_valid) return CNN_OK;
+    CNN_TRY(resolve_nnz(ctx));
+    const int64_t n = ctx->n;
+    cudaStream_t st = ctx->stream;
+    int64_t *row_off = ctx->row_off.as<int64_t>();
+    CNN_TRY(scan_exclusive_i32_to_i64(ctx, ctx->deg.as<int32_t>(), row_off, n + 1));
+    CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(ctx->nnz > 0 ? ctx->nnz : 1)));
+    CNN_TRY(ctx->ensure(ctx->split, sizeof(int32_t) * (size_t)(n > 0 ? n : 1)));
+    compact_rows_kernel<<<std::min<unsigned>(grid_for(n * 32, 256), ctx->sm_count * 16u), 256, 0, st>>>(
+        n, ctx->grid_qslot.as<int64_t>(), ctx->grid_slot_cols.as<int32_t>(), row_off, ctx->cols.as<int32_t>(),
+        ctx->split.as<int32_t>());
+    CNN_LAUNCH_CHECK(ctx);
+    ctx->csr_valid = true;
+    ctx->split_valid = true;
+    return CNN_OK;
+}
+
 cnn_status ensure_lists(cnn_context *ctx) {
     if (!ctx->have_graph || !ctx->graph_mask || ctx->csr_valid) return CNN_OK;
     CNN_TRY(ctx->ensure(ctx->cols, sizeof(int32_t) * (size_t)(ctx->nnz > 0 ? ctx->nnz : 1)));
@@ -1484,6 +1589,7 @@ cnn_status ensure_lists(cnn_context *ctx) {
 // Graph as CSR in point-index order (device output buffers).
 cnn_status export_neighbours_impl(cnn_context *ctx, int64_t *offsets_dev, int32_t *indices_dev) {
     CNN_TRY(ensure_lists(ctx));
+    CNN_TRY(ensure_csr(ctx));
     const int64_t n = ctx->n, nnz = ctx->nnz;
     cudaStream_t st = ctx->stream;
     if (ctx->identity_perm) {
@@ -1713,10 +1819,13 @@ cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev, con
     ctx->have_graph = false;
     ctx->graph_mask = false;
     ctx->csr_valid = true;
+    ctx->graph_slots = false;
+    ctx->nnz_pending = false;
     ctx->tune_pending = false;
     ctx->split_valid = false;
     ++ctx->graph_generation;
     ctx->stats = cnn_stats{};
+    stages_reset(ctx, 0, cnn_context::kSlots - 1);
     ctx->search_stats_pending = false;
     ctx->fit_stats_pending = false;
     ctx->stats.n_points = n;
@@ -1725,8 +1834,8 @@ cnn_status set_neighbours_impl(cnn_context *ctx, const int64_t *offsets_dev, con
     ctx->x = nullptr;
     ctx->dist = nullptr;
     ctx->dist_set = false;
-    CNN_TRY(ctx->ensure(ctx->counters, 16 * sizeof(unsigned long long)));
-    CNN_CUDA(ctx, cudaMemsetAsync(ctx->counters.ptr, 0, 16 * sizeof(unsigned long long), st));
+    CNN_TRY(ctx->ensure(ctx->counters, kCounterSlots * sizeof(unsigned long long)));
+    CNN_CUDA(ctx, cudaMemsetAsync(ctx->counters.ptr, 0, kCounterSlots * sizeof(unsigned long long), st));
     CNN_TRY(ctx->ensure(ctx->deg, sizeof(int32_t) * (size_t)(n + 1)));
     CNN_TRY(ctx->ensure(ctx->row_off, sizeof(int64_t) * (size_t)(n + 1)));
     CNN_TRY(ctx->ensure(ctx->perm, sizeof(int32_t) * (size_t)(n > 0 ? n : 1)));

@@ -437,6 +437,41 @@ def test_fit_fresh_many_clusters(cnn, n_blobs):
         ctx.close()
 
 
+def test_rows_left_in_their_slots(cnn, oracle):
+    """A public cell-grid build leaves the rows where the search wrote them;
+    the pair count (cnn_neighbour_count, the statistics), a fit on the slots,
+    the exported CSR (made on request) and a fit after it all agree with the
+    oracle, and with each other."""
+    from commonnnclustering_gb300 import _abi, workloads
+    x = workloads.md3d(n=40000, seed=17, centre_spread=2.0)
+    r2 = 0.1 ** 2
+    want_off, want_idx = oracle.neighbourhoods(x, r2, grid=True)
+    ref = np.zeros(x.shape[0], dtype=np.int64)
+    oracle.fit_bfs_csr(want_off, want_idx, 12, 11, 1, np.ones(x.shape[0], dtype=np.uint8), ref)
+    ctx = cnn.Context(0)
+    try:
+        ctx.set_intersection(_abi.INTERSECT_MERGE)
+        ctx.set_points(x)
+        ctx.build_neighbours(r2)
+        assert ctx.neighbour_count() == want_idx.shape[0]
+        assert ctx.stats()["n_nonzero"] == want_idx.shape[0]
+        first = np.zeros(x.shape[0], dtype=np.int64)
+        ctx.fit(12, 11, 1, np.ones(x.shape[0], dtype=np.uint8), first)  # on the slots
+        assert np.array_equal(first, ref)
+        off, idx = ctx.get_neighbours(x.shape[0])  # the CSR, made now
+        assert np.array_equal(off, want_off) and np.array_equal(idx, want_idx)
+        again = np.zeros(x.shape[0], dtype=np.int64)
+        ctx.fit(12, 11, 1, np.ones(x.shape[0], dtype=np.uint8), again)  # on the CSR
+        assert np.array_equal(again, ref)
+        ctx.build_neighbours(r2)
+        got = ctx.fit_fresh(12, 11, True, 2, None)
+        sorted_ref = ref.copy()
+        ctx.sort_by_size(sorted_ref, 2, None)
+        assert np.array_equal(got, sorted_ref)
+    finally:
+        ctx.close()
+
+
 def test_fit_fresh_on_other_graphs(cnn):
     """cnn_fit_fresh after the tensor-core search (n_dim 16, the graph in the
     search's pivot-grouped order), after precomputed neighbourhoods
