@@ -742,8 +742,9 @@ cnn_status fit_impl(cnn_context *ctx, int64_t similarity_cutoff, int64_t n_membe
     // holds more cross pairs than the graph-fed one after its hook pass;
     // overflow falls back to the full lazy pass (measured on the 1M-point
     // sweep: nnz/4 for lists, nnz/16 for the graph).  Rows in their slots:
-    // the pair count is not read back yet; the slot total bounds it.
-    const int64_t pairs = slots ? ctx->slot_total : ctx->nnz;
+    // the pair count is not read back yet; a quarter of the slot total (the
+    // stencil candidates, about five per pair) stands in for it.
+    const int64_t pairs = slots ? ctx->slot_total / 4 : ctx->nnz;
     int64_t wl_cap = std::max<int64_t>(int64_t(1) << 20, pairs / (edge_list ? 4 : 16));
     int2 *wl = nullptr;
     if (wl_buf && wl_buf_cap > 0) {  // the caller's room: every pair the filter can emit
