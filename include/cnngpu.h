@@ -215,11 +215,15 @@ CNN_API cnn_status cnn_set_neighbours(cnn_context *ctx, const int64_t *offsets,
                                       const int32_t *indices, int64_t n_points,
                                       cnn_memspace mem);
 
-/* Number of stored neighbour pairs of the current graph. */
+/* Number of stored neighbour pairs of the current graph.  After a cell-grid
+ * cnn_build_neighbours the count is read back here (a stream sync) or by
+ * cnn_get_stats: the build itself does not wait for it. */
 CNN_API cnn_status cnn_neighbour_count(cnn_context *ctx, int64_t *nnz);
 
 /* The current graph as CSR in point-index order with ascending rows:
- * offsets int64[n+1], indices int32[nnz]. */
+ * offsets int64[n+1], indices int32[nnz].  A cell-grid cnn_build_neighbours
+ * leaves each row in the slot the search wrote it to (cnn_fit walks them
+ * there); the first call here makes the CSR (a scan and a compaction). */
 CNN_API cnn_status cnn_get_neighbours(cnn_context *ctx, int64_t *offsets, int32_t *indices,
                                       cnn_memspace mem);
 
