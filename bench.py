@@ -217,8 +217,10 @@ def hbm_roofline(stats_list, nnz, n, peaks, workload=None):
         # stage -> (kernel name, algorithmic bytes per launch)
         # one pass into per-row slots: float4 coordinates read, rows, lengths and slot starts written
         "ms_count": ("grid_unit_kernel<slots>", 16 * n + 4 * nnz + 4 * n + 8 * n),
-        # slots -> compact CSR: rows read and written, offsets read
-        "ms_fill": ("compact_rows_kernel", 8 * nnz + 16 * (n + 1)),
+        # rows left in their slots (a public build): each row's end and split
+        # point -- start and length read, end and split written, ~8 entries
+        # bisected per row; the compaction to CSR runs only when asked for
+        "ms_fill": ("row_split_kernel", 8 * n + 4 * n + 8 * n + 4 * n + 32 * n),
         "ms_check": ("check_union_kernel", 4 * nnz + 8 * (n + 1) + n + 8 * n),
         "ms_cells": ("cell binning (assign, scan, place)", 4 * 8 * n),
         "ms_label": ("labelling", 24 * n),
