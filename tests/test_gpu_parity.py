@@ -472,6 +472,33 @@ def test_rows_left_in_their_slots(cnn, oracle):
         ctx.close()
 
 
+def test_stage_times_belong_to_the_last_call(cnn):
+    """With timing on, a stage the last build or fit did not run reports 0,
+    not an earlier call's time: a fit without its sort after one with it, a
+    build that leaves the rows in their slots (no row-offset scan, no fit yet)
+    after one whose CSR was made."""
+    from commonnnclustering_gb300 import _abi, workloads
+    x = workloads.md3d(n=20000, seed=23, centre_spread=2.0)
+    ctx = cnn.Context(0)
+    try:
+        ctx.set_timing(True)
+        ctx.set_intersection(_abi.INTERSECT_MERGE)
+        ctx.set_points(x)
+        ctx.build_neighbours(0.1 ** 2)
+        ctx.get_neighbours(x.shape[0])  # the CSR, made on request
+        ctx.fit_fresh(12, 11, True, 2, None)
+        st = ctx.stats()
+        assert st["ms_sort"] > 0 and st["ms_check"] > 0
+        ctx.fit_fresh(12, 11, False, 2, None)
+        st = ctx.stats()
+        assert st["ms_sort"] == 0 and st["ms_check"] > 0
+        ctx.build_neighbours(0.1 ** 2)
+        st = ctx.stats()
+        assert st["ms_count"] > 0 and st["ms_scan"] == 0 and st["ms_check"] == 0
+    finally:
+        ctx.close()
+
+
 def test_fit_fresh_on_other_graphs(cnn):
     """cnn_fit_fresh after the tensor-core search (n_dim 16, the graph in the
     search's pivot-grouped order), after precomputed neighbourhoods
