@@ -51,3 +51,12 @@ def test_python_binding_covers_header():
 def test_build_targets_sm_103a_only():
     from commonnnclustering_gb300 import _build
     assert _build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_binding_abi_version_is_the_headers():
+    """The ctypes structs mirror one version of include/cnngpu.h; the binding
+    refuses a library of another version at load time."""
+    from commonnnclustering_gb300 import _abi
+    hdr = open(HEADER).read()
+    m = re.search(r"#define CNN_ABI_VERSION (\d+)", hdr)
+    assert m and int(m.group(1)) == _abi.ABI_VERSION
