@@ -253,6 +253,31 @@ def hbm_roofline(stats_list, nnz, n, peaks, workload=None):
     }
 
 
+def issue_roofline(roof, workload, sm_count, clocks):
+    """The dominant kernel against the SM issue rate, for a kernel that is
+    issue-bound rather than HBM-bound (the cell-grid search): warp
+    instructions of one launch from the committed ncu capture of this
+    workload, over the live launch time, against 4 warp instructions per SM
+    per cycle at the median SM clock sampled during the run."""
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(tpath) as f:
+            tj = json.load(f)
+    except Exception:
+        return None
+    if tj.get("_workload") != workload:
+        return None
+    inst = (tj.get("_issue") or {}).get(roof.get("kernel"))
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
+    ms = roof.get("ms_per_launch")
+    if not inst or not mhz or not ms or not sm_count:
+        return None
+    achieved = inst / (ms * 1e-3)
+    peak = 4.0 * sm_count * mhz * 1e6
+    return {"warp_instructions": inst, "achieved": achieved, "peak": peak, "unit": "warp instructions/s",
+            "frac": achieved / peak, "source": tj.get("_issue_source")}
+
+
 # ---------------------------------------------------------------------------
 # CPU baselines (the oracle port of the reference path; bounded samples)
 # ---------------------------------------------------------------------------
@@ -433,6 +458,11 @@ def fit_record(W, args, peaks, dist=None, world=1, local=0, rank=0, cpu=True):
         "intersection": {"requested": args.intersection,
                          "used": {1: "merge", 2: "bitset"}.get(stats_list[-1]["intersection"], "none")},
     }
+    if W["d"] < 16:
+        sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+        issue = issue_roofline(rec["roofline"], W["name"], sm_count, rec["clocks"])
+        if issue:
+            rec["roofline"]["issue"] = issue
     if W["d"] >= 16:
         rec["fit_stats"]["recheck_fraction"] = (stats_list[-1]["n_exact"] / stats_list[-1]["n_candidates"]
                                                 if stats_list[-1]["n_candidates"] else None)
